@@ -1,0 +1,143 @@
+"""Regenerate the golden fixtures in tests/golden/ (run in a tree where the
+reference is available; the GPU host never runs this).
+
+Writes:
+  web_reference.json   the reference's own golden vectors
+                       (web/verify/reference.json): equities only, at all
+                       indices for n <= 300 and at 120 sampled indices above;
+                       inputs are rebuilt by webgen.py, which is checked here
+                       against the JSON bit for bit.
+  ref_workloads.json   equities from the reference's src/cpu/icm.c (compiled
+                       unmodified into oracle/_ref) on seeded workloads of the
+                       shapes the benchmarks use, at sizes the CPU finishes in
+                       minutes, plus the full-size drop-in workload's subset.
+  closed_form.json     exact closed-form equities (no quadrature) for the
+                       full-size drop-in workload's 64 subset targets:
+                       payout (k-j+1)^2 with k = n gives E = 2 V2 + 3 V1 - 2
+                       (unnormalised), from oracle V1/V2.
+
+Usage:  python tests/golden/make_golden.py [--skip-large]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from icm_gb300 import workloads as W  # noqa: E402
+from oracle.oracle import Oracle, ReferenceLib, build  # noqa: E402
+from tests.golden.webgen import all_cases  # noqa: E402
+
+REF_JSON = os.path.join(os.environ.get("ICM_REFERENCE_DIR", "/root/reference"),
+                        "web", "verify", "reference.json")
+
+
+def sample_idx(n: int, count: int, S: np.ndarray | None = None) -> np.ndarray:
+    if n <= count:
+        return np.arange(n)
+    idx = set(np.linspace(0, n - 1, count - 2).astype(int).tolist())
+    if S is not None:
+        idx.add(int(np.argmin(S)))
+        idx.add(int(np.argmax(S)))
+    return np.array(sorted(idx))
+
+
+def fl(a):
+    return [float(x) for x in a]
+
+
+def web_fixture():
+    ref = json.load(open(REF_JSON))
+    out = []
+    for (name, n, k, Q, S, P), c in zip(all_cases(), ref):
+        assert c["name"] == name and c["n"] == n and c["k"] == k and c["Q"] == Q
+        assert np.array_equal(S, np.array(c["stacks"])), name
+        assert np.array_equal(P, np.array(c["payouts"])), name
+        E = np.array(c["equity"])
+        idx = np.arange(n) if n <= 300 else sample_idx(n, 120, S)
+        out.append({"name": name, "n": n, "k": k, "Q": Q,
+                    "idx": idx.tolist(), "equity": fl(E[idx])})
+    return {"source": "web/verify/reference.json (reference native build)", "cases": out}
+
+
+def workload_fixture(ref: ReferenceLib, skip_large: bool):
+    cases = []
+
+    def add(name, S, P, Q=256, targets=None, count=256, meta=None):
+        t0 = time.time()
+        E = ref.equity(S, P, Q=Q)
+        rec = {"name": name, "n": len(S), "k": len(P), "Q": Q,
+               "sum_S": float(S.sum()), "sum_P": float(P.sum()), **(meta or {})}
+        idx = sample_idx(len(S), count, S)
+        rec["idx"] = idx.tolist()
+        rec["equity"] = fl(E[idx])
+        if targets is not None:
+            Es = ref.equity(S, P, Q=Q, targets=targets)
+            rec["targets"] = [int(t) for t in targets]
+            rec["subset_equity"] = fl(Es[targets])
+            rec["full_at_targets"] = fl(E[targets])
+        print(f"  {name}: n={len(S)} k={len(P)} {time.time() - t0:.1f}s", flush=True)
+        cases.append(rec)
+
+    S, P = W.plain_small()
+    add("plain_small", S, P, count=1024, meta={"gen": "plain_small()"})
+    S, P, T = W.dropin(n=4096)
+    add("dropin_4096", S, P, targets=T, meta={"gen": "dropin(n=4096)"})
+    S, P, T = W.dropin(n=3000, k=3000, n_targets=17)
+    add("dropin_3000_ragged", S, P, targets=T, meta={"gen": "dropin(n=3000, k=3000, n_targets=17)"})
+    S, P = W.gpu_scale(n=8192, shape="linear")
+    add("gpu_scale_8192_linear", S, P, meta={"gen": "gpu_scale(n=8192, shape='linear')"})
+    S, P = W.gpu_scale(n=8192, shape="geometric")
+    add("gpu_scale_8192_geometric", S, P, meta={"gen": "gpu_scale(n=8192, shape='geometric')"})
+    for i, (S, P) in enumerate(W.batched(count=24, n_hi=3000)):
+        add(f"batched_small_{i}", S, P, count=32, meta={"gen": "batched(count=24, n_hi=3000)", "member": i})
+    for shape in ("linear", "quadratic"):
+        S, P, _ = W.vjp(n=2048, k=256, payout=shape)
+        add(f"vjp_2048_{shape}", S, P, count=128, meta={"gen": f"vjp(n=2048, k=256, payout='{shape}')"})
+    if not skip_large:
+        S, P, T = W.dropin()
+        add("dropin_65536", S, P, targets=T, count=128, meta={"gen": "dropin()"})
+    return {"source": "reference src/cpu/icm.c via oracle/_ref (FFTW shim, devices/generic, OpenMP)",
+            "cases": cases}
+
+
+def closed_form_fixture(orc: Oracle):
+    S, P, T = W.dropin()
+    n = len(S)
+    t0 = time.time()
+    v1 = orc.v1(S, idx=T)
+    v2 = orc.v2(S, idx=T)
+    r = np.arange(n, dtype=np.float64)[::-1]            # r = n-1-m
+    norm = float(np.sum((r + 1.0) ** 2))
+    exact = (2.0 * v2 + 3.0 * v1 - 2.0) / norm
+    print(f"  closed form n={n}: {time.time() - t0:.1f}s", flush=True)
+    return {"source": "oracle V1/V2 closed forms, E = (2 V2 + 3 V1 - 2) / sum (n-m)^2",
+            "gen": "dropin()", "n": n, "targets": [int(t) for t in T], "equity": fl(exact)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--skip-large", action="store_true")
+    args = ap.parse_args()
+    build()
+    ref = ReferenceLib(openmp=True)
+    orc = Oracle()
+    print("web_reference.json")
+    json.dump(web_fixture(), open(os.path.join(HERE, "web_reference.json"), "w"))
+    print("ref_workloads.json")
+    json.dump(workload_fixture(ref, args.skip_large), open(os.path.join(HERE, "ref_workloads.json"), "w"))
+    if not args.skip_large:
+        print("closed_form.json")
+        json.dump(closed_form_fixture(orc), open(os.path.join(HERE, "closed_form.json"), "w"))
+
+
+if __name__ == "__main__":
+    main()
