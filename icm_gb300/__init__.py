@@ -1,0 +1,243 @@
+"""GB300-native ICM equity engine (sm_103a), Python binding.
+
+Drop-in for the reference's ``icm`` package (python/icm/__init__.py): the same
+``init``, ``equity``, ``equity_subset`` and ``ICMError`` with the same argument
+checks and messages, reaching ``libicm_gb300.so`` through ctypes.  The
+computation runs on the GPU; if the library or a GPU is missing the calls
+raise ``ICMError`` (there is no CPU fallback).
+
+Additions: ``gpu_equity`` (with run statistics), ``GpuPlan`` (reusable
+tournament plan), ``equity_batched`` (many tournaments), ``configure``
+(block size / FFT crossover / chunking) and the FP64 peak probe.
+
+Example::
+
+    import icm_gb300 as icm
+    icm.init()
+    eq = icm.equity([1000, 2000, 3000], [0.5, 0.3, 0.2])
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from ._lib import (IcmGb300Config, IcmGpuOptions, IcmGpuPlanSummary, IcmGpuRunStats, ICMError, lib,
+                   library_path)
+
+__all__ = ["init", "equity", "equity_subset", "ICMError", "gpu_equity", "gpu_equity_subset", "GpuPlan",
+           "equity_batched", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
+           "last_launch_count"]
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def _to_double_array(data, name):
+    arr = np.ascontiguousarray(data, dtype=np.float64)
+    if arr.ndim != 1:
+        raise ValueError(f"{name} must be a 1-D array, got shape {arr.shape}")
+    if arr.size == 0:
+        raise ValueError(f"{name} must not be empty")
+    return arr
+
+
+def _to_int_array(data, name):
+    arr = np.ascontiguousarray(data, dtype=np.int32)
+    if arr.ndim != 1:
+        raise ValueError(f"{name} must be a 1-D array, got shape {arr.shape}")
+    if arr.size == 0:
+        raise ValueError(f"{name} must not be empty")
+    return arr
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _check(n, k, Q):
+    if k < 1 or k > n:
+        raise ValueError(f"payouts length k={k} must satisfy 1 <= k <= n={n}")
+    if Q < 1:
+        raise ValueError(f"Q must be positive, got {Q}")
+
+
+_initialized = False
+
+
+def init(wisdom_path=None):
+    """Initialise the library (selects GPU 0 unless ``icm_gpu_init`` chose one).
+
+    ``wisdom_path`` names an optional tuner table (text lines ``block_size 8``,
+    ``fft_min_degree 64``, ``q_chunk 64``), the analogue of the reference's
+    FFTW wisdom file.
+    """
+    global _initialized
+    L = lib()
+    L.icm_init(wisdom_path.encode() if isinstance(wisdom_path, str) else wisdom_path)
+    _initialized = True
+
+
+def _auto_init():
+    if not _initialized:
+        init()
+
+
+def _raise_if_failed(what):
+    if lib().icm_last_status() != 0:
+        raise ICMError(f"{what} failed: {lib().icm_gpu_last_error().decode(errors='replace')}")
+
+
+def equity(stacks, payouts, Q=256):
+    """ICM equities for all players (reference ``icm.equity``)."""
+    stacks_arr = _to_double_array(stacks, "stacks")
+    payouts_arr = _to_double_array(payouts, "payouts")
+    n, k = len(stacks_arr), len(payouts_arr)
+    _check(n, k, Q)
+    _auto_init()
+    out = np.zeros(n, dtype=np.float64)
+    lib().icm_equity(n, _d(stacks_arr), int(Q), _d(payouts_arr), k, _d(out))
+    _raise_if_failed("icm_equity")
+    return out
+
+
+def equity_subset(stacks, payouts, targets, Q=256):
+    """Equities for the target players only; other entries are 0
+    (reference ``icm.equity_subset``)."""
+    stacks_arr = _to_double_array(stacks, "stacks")
+    payouts_arr = _to_double_array(payouts, "payouts")
+    targets_arr = _to_int_array(targets, "targets")
+    n, k, nt = len(stacks_arr), len(payouts_arr), len(targets_arr)
+    _check(n, k, Q)
+    if nt < 1:
+        raise ValueError("targets must not be empty")
+    if np.any(targets_arr < 0) or np.any(targets_arr >= n):
+        raise ValueError(f"target indices must be in [0, {n-1}]")
+    _auto_init()
+    out = np.zeros(n, dtype=np.float64)
+    lib().icm_equity_subset(n, _d(stacks_arr), int(Q), _d(payouts_arr), k, _d(out),
+                            targets_arr.ctypes.data_as(_ip), nt)
+    _raise_if_failed("icm_equity_subset")
+    return out
+
+
+def _stats_dict(st):
+    return {name: getattr(st, name) for name, _ in IcmGpuRunStats._fields_}
+
+
+def gpu_equity(stacks, payouts, Q=256, return_stats=False):
+    """``icm_gpu_equity``: like ``equity`` but returns run statistics too."""
+    S = _to_double_array(stacks, "stacks")
+    P = _to_double_array(payouts, "payouts")
+    _check(len(S), len(P), Q)
+    _auto_init()
+    out = np.zeros(len(S))
+    st = IcmGpuRunStats()
+    if lib().icm_gpu_equity(len(S), _d(S), int(Q), _d(P), len(P), _d(out), None, ctypes.byref(st)) != 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return (out, _stats_dict(st)) if return_stats else out
+
+
+def gpu_equity_subset(stacks, payouts, targets, Q=256):
+    S = _to_double_array(stacks, "stacks")
+    P = _to_double_array(payouts, "payouts")
+    T = _to_int_array(targets, "targets")
+    _check(len(S), len(P), Q)
+    if np.any(T < 0) or np.any(T >= len(S)):
+        raise ValueError(f"target indices must be in [0, {len(S)-1}]")
+    _auto_init()
+    out = np.zeros(len(S))
+    if lib().icm_gpu_equity_subset(len(S), _d(S), int(Q), _d(P), len(P), _d(out), T.ctypes.data_as(_ip),
+                                   len(T), None, None) != 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return out
+
+
+class GpuPlan:
+    """Reusable plan for one tournament (``IcmGpuPlan``): sorted stacks, tree
+    geometry and device buffers are set up once; ``equity`` runs the
+    quadrature for any payout vector of length k."""
+
+    def __init__(self, stacks, k, options: IcmGpuOptions | None = None):
+        _auto_init()
+        self.S = _to_double_array(stacks, "stacks")
+        self.n, self.k = len(self.S), int(k)
+        _check(self.n, self.k, 1)
+        self._p = lib().icm_gpu_plan_create(self.n, _d(self.S), self.k,
+                                            ctypes.byref(options) if options else None)
+        if not self._p:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+
+    def equity(self, payouts, Q=256, return_stats=False):
+        P = _to_double_array(payouts, "payouts")
+        if len(P) != self.k:
+            raise ValueError(f"payouts length {len(P)} != plan k={self.k}")
+        out = np.zeros(self.n)
+        st = IcmGpuRunStats()
+        if lib().icm_gpu_equity_with_plan(self._p, int(Q), _d(P), _d(out), ctypes.byref(st)) != 0:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+        return (out, _stats_dict(st)) if return_stats else out
+
+    def summary(self):
+        s = IcmGpuPlanSummary()
+        lib().icm_gpu_plan_summary(self._p, ctypes.byref(s))
+        return {name: getattr(s, name) for name, _ in IcmGpuPlanSummary._fields_}
+
+    def close(self):
+        if getattr(self, "_p", None):
+            lib().icm_gpu_plan_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def equity_batched(tournaments, Q=256, return_stats=False):
+    """Equities of many independent tournaments: ``tournaments`` is a list of
+    (stacks, payouts).  Returns a list of arrays."""
+    Ss = [_to_double_array(s, "stacks") for s, _ in tournaments]
+    Ps = [_to_double_array(p, "payouts") for _, p in tournaments]
+    ns = np.array([len(s) for s in Ss], dtype=np.int32)
+    ks = np.array([len(p) for p in Ps], dtype=np.int32)
+    for n, k in zip(ns, ks):
+        _check(int(n), int(k), Q)
+    _auto_init()
+    S = np.ascontiguousarray(np.concatenate(Ss))
+    P = np.ascontiguousarray(np.concatenate(Ps))
+    out = np.zeros(len(S))
+    st = IcmGpuRunStats()
+    if lib().icm_gpu_equity_batched(len(Ss), ns.ctypes.data_as(_ip), ks.ctypes.data_as(_ip), _d(S), _d(P),
+                                    int(Q), _d(out), ctypes.byref(st)) != 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    res = np.split(out, np.cumsum(ns)[:-1])
+    return (res, _stats_dict(st)) if return_stats else res
+
+
+def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0):
+    """Process-wide engine settings for plans created afterwards (0 = default)."""
+    cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 0, max_device_bytes)
+    lib().icm_gb300_set_config(ctypes.byref(cfg))
+
+
+def measure_fp64_gflops():
+    _auto_init()
+    v = ctypes.c_double()
+    if lib().icm_gpu_measure_fp64_gflops(ctypes.byref(v)) != 1:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return v.value
+
+
+def measure_hbm_gbps():
+    _auto_init()
+    v = ctypes.c_double()
+    if lib().icm_gpu_measure_hbm_bandwidth_gbps(ctypes.byref(v)) != 1:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return v.value
+
+
+def last_launch_count():
+    return int(lib().icm_gpu_last_launch_count())

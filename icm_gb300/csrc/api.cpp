@@ -1,0 +1,319 @@
+// api.cpp -- the C ABI of libicm_gb300.so: the reference's icm.h / icm_gpu.h
+// entry points (same names, arguments and return conventions) plus the
+// additions in icm_gb300.h.  Plain pointers and sizes only.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "kernels.h"
+
+using namespace icmg;
+
+namespace {
+thread_local std::string t_last_error;
+thread_local int t_last_status = 0;
+thread_local long t_launches = 0;
+
+void set_error(const std::string &e) { t_last_error = e; }
+
+bool ensure_device() {
+    if (g_device >= 0) {
+        cudaError_t e = cudaSetDevice(g_device);
+        if (e != cudaSuccess) { set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e)); return false; }
+        return true;
+    }
+    return icm_gpu_init(0) == 1;
+}
+
+double now_ns() {
+    return (double)std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+// void entry points report failure through NaN output, stderr and
+// icm_last_status() (the reference's icm_equity has no status to return)
+void fail_void(int n, double *equity, const std::string &what) {
+    t_last_status = -1;
+    set_error(what);
+    fprintf(stderr, "icm_gb300: %s\n", what.c_str());
+    if (equity)
+        for (int i = 0; i < n; ++i) equity[i] = std::nan("");
+}
+
+int run_full(int n, const double *S, int Q, const double *payout, int k, double *equity, const int *targets,
+             int n_targets, const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
+    if (!ensure_device()) return -1;
+    std::string err;
+    Plan *p = plan_create(n, S, k, opts, err);
+    if (!p) { set_error(err); return -1; }
+    int rc = 0;
+    if (targets) rc = plan_set_targets(p, targets, n_targets, err);
+    if (rc == 0) rc = plan_run(p, Q, payout, equity, stats, err);
+    t_launches = p->launches;
+    plan_destroy(p);
+    if (rc != 0) { set_error(err); return -1; }
+    return 0;
+}
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------ icm.h
+void icm_init(const char *wisdom_path) {
+    // The tuner table (the analogue of the reference's FFTW wisdom) is a
+    // text file of "key value" lines: block_size, fft_min_degree, q_chunk.
+    if (wisdom_path) {
+        FILE *f = fopen(wisdom_path, "r");
+        if (f) {
+            char key[64];
+            long val;
+            while (fscanf(f, "%63s %ld", key, &val) == 2) {
+                if (!strcmp(key, "block_size")) g_config.block_size = (int)val;
+                else if (!strcmp(key, "fft_min_degree")) g_config.fft_min_degree = (int)val;
+                else if (!strcmp(key, "q_chunk")) g_config.q_chunk = (int)val;
+            }
+            fclose(f);
+        }
+    }
+    if (g_device < 0) icm_gpu_init(0);
+}
+
+void icm_equity(int n, const double *S, int Q, const double *payout, int k, double *equity) {
+    t_last_status = 0;
+    if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !equity) {
+        fail_void(n, equity, "icm_equity: invalid arguments (need 1 <= k <= n, Q >= 1)");
+        return;
+    }
+    if (run_full(n, S, Q, payout, k, equity, nullptr, 0, nullptr, nullptr) != 0)
+        fail_void(n, equity, "icm_equity failed: " + t_last_error);
+}
+
+void icm_equity_subset(int n, const double *S, int Q, const double *payout, int k, double *equity,
+                       const int *targets, int n_targets) {
+    t_last_status = 0;
+    if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !equity || !targets || n_targets < 1) {
+        fail_void(n, equity, "icm_equity_subset: invalid arguments");
+        return;
+    }
+    if (run_full(n, S, Q, payout, k, equity, targets, n_targets, nullptr, nullptr) != 0)
+        fail_void(n, equity, "icm_equity_subset failed: " + t_last_error);
+}
+
+void *icm_tree_ctx_create(int, int) { return nullptr; }
+void *icm_hybrid_ctx_create(int, const double *, int, int) { return nullptr; }
+void *icm_linear_ctx_create(int, int) { return nullptr; }
+void icm_ctx_destroy(void *, int) {}
+IcmEngine icm_engine_tree(void) { return nullptr; }
+IcmEngine icm_engine_hybrid(void) { return nullptr; }
+IcmEngine icm_engine_linear(void) { return nullptr; }
+double icm_run_engine(int, const double *, int, const double *, int, double *, IcmEngine, void *) {
+    set_error("icm_run_engine: the GB300 library has a single GPU engine; use icm_equity");
+    return -1.0;
+}
+double icm_run_linear_batched(int, const double *, int, const double *, int, double *, void *) {
+    set_error("icm_run_linear_batched: the GB300 library has a single GPU engine; use icm_equity");
+    return -1.0;
+}
+int icm_select_engine(int n, int k) { return select_block_size(n, k); }
+int icm_select_best_B(int n, int k) { return select_block_size(n, k); }
+
+// closed forms (reference src/cpu/icm.c:145-170), host-side
+void icm_v1_exact(int n, const double *S, double *V1) {
+    for (int i = 0; i < n; ++i) {
+        double v = 1.0;
+        for (int j = 0; j < n; ++j)
+            if (j != i) v += S[i] / (S[i] + S[j]);
+        V1[i] = v;
+    }
+}
+
+void icm_v2_exact(int n, const double *S, double *V2) {
+    for (int i = 0; i < n; ++i) {
+        double v = 0.0;
+        for (int j = 0; j < n; ++j) {
+            if (j == i) continue;
+            for (int l = j + 1; l < n; ++l) {
+                if (l == i) continue;
+                v += S[i] / (S[i] + S[j] + S[l]);
+            }
+        }
+        V2[i] = v;
+    }
+}
+
+// ------------------------------------------------------------ icm_gpu.h
+int icm_gpu_init(int device_id) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) { set_error(std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e)); return 0; }
+    if (count <= 0) { set_error("No CUDA devices found"); return 0; }
+    if (device_id < 0) device_id = 0;
+    if (device_id >= count) {
+        set_error("Invalid CUDA device id " + std::to_string(device_id) + " (count=" + std::to_string(count) + ")");
+        return 0;
+    }
+    e = cudaSetDevice(device_id);
+    if (e != cudaSuccess) { set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e)); return 0; }
+    fft_set_smem_limits();
+    g_device = device_id;
+    return 1;
+}
+
+void icm_gpu_shutdown(void) {
+    if (g_device >= 0) {
+        cudaSetDevice(g_device);
+        cudaDeviceSynchronize();
+    }
+}
+
+const char *icm_gpu_last_error(void) { return t_last_error.c_str(); }
+
+int icm_gpu_release_pooled_memory(void) {
+    if (g_device < 0) return -1;
+    cudaMemPool_t pool = nullptr;
+    if (cudaDeviceGetDefaultMemPool(&pool, g_device) != cudaSuccess) return -1;
+    if (cudaMemPoolTrimTo(pool, 0) != cudaSuccess) return -1;
+    return 0;
+}
+
+IcmGpuPlan *icm_gpu_plan_create(int n, const double *S, int k, const IcmGpuOptions *opts) {
+    if (g_device < 0) {
+        set_error("icm_gpu_init must be called before icm_gpu_plan_create");
+        return nullptr;
+    }
+    if (!ensure_device()) return nullptr;
+    std::string err;
+    Plan *p = plan_create(n, S, k, opts, err);
+    if (!p) set_error(err);
+    return reinterpret_cast<IcmGpuPlan *>(p);
+}
+
+void icm_gpu_plan_destroy(IcmGpuPlan *plan) { plan_destroy(reinterpret_cast<Plan *>(plan)); }
+
+int icm_gpu_plan_summary(const IcmGpuPlan *plan, IcmGpuPlanSummary *summary) {
+    const Plan *p = reinterpret_cast<const Plan *>(plan);
+    if (!p || !summary) return 0;
+    memset(summary, 0, sizeof(*summary));
+    summary->n = p->n;
+    summary->k = p->k;
+    summary->B = p->B;
+    summary->engine = 1;
+    summary->n_levels = p->L;
+    for (int l = 1; l < p->L; ++l) {
+        if (!p->lv[l].fft) summary->n_tier1++;
+        else if (p->lv[l].fftn <= kSmemFftMax) summary->n_tier2++;
+        else summary->n_tier3++;
+    }
+    summary->q_batch = p->qc;
+    summary->planned_peak_vram_bytes = p->arena_bytes;
+    return 1;
+}
+
+int icm_gpu_equity_with_plan(IcmGpuPlan *plan, int Q, const double *payout, double *equity,
+                             IcmGpuRunStats *stats) {
+    Plan *p = reinterpret_cast<Plan *>(plan);
+    if (!p || !payout || !equity || Q <= 0) {
+        set_error("icm_gpu_equity_with_plan invalid arguments");
+        return -1;
+    }
+    if (!ensure_device()) return -1;
+    std::string err;
+    const int rc = plan_run(p, Q, payout, equity, stats, err);
+    t_launches = p->launches;
+    if (rc != 0) { set_error(err); return -1; }
+    return 0;
+}
+
+int icm_gpu_equity(int n, const double *S, int Q, const double *payout, int k, double *equity,
+                   const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
+    if (n <= 0 || k <= 0 || k > n || Q <= 0 || !S || !payout || !equity) {
+        set_error("icm_gpu_equity invalid arguments");
+        return -1;
+    }
+    const double t0 = now_ns();
+    const int rc = run_full(n, S, Q, payout, k, equity, nullptr, 0, opts, stats);
+    if (rc == 0 && stats) stats->total_ns = now_ns() - t0;   // includes plan creation
+    return rc;
+}
+
+int icm_gpu_equity_subset(int n, const double *S, int Q, const double *payout, int k, double *equity,
+                          const int *targets, int n_targets, const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
+    if (n <= 0 || k <= 0 || k > n || Q <= 0 || n_targets <= 0 || !targets || !S || !payout || !equity) {
+        set_error("icm_gpu_equity_subset invalid arguments");
+        return -1;
+    }
+    const double t0 = now_ns();
+    const int rc = run_full(n, S, Q, payout, k, equity, targets, n_targets, opts, stats);
+    if (rc == 0 && stats) stats->total_ns = now_ns() - t0;
+    return rc;
+}
+
+int icm_gpu_measure_hbm_bandwidth_gbps(double *gbps_out) {
+    if (!gbps_out || !ensure_device()) return 0;
+    std::string err;
+    if (measure_hbm_gbps(gbps_out, err) != 0) { set_error(err); return 0; }
+    return 1;
+}
+
+int icm_gpu_measure_fused_pair_ns(int fft_n, int batch, int quick, double *build_ns_out, double *corr_ns_out);
+int icm_gpu_measure_fused_r2c_pair_ns(int fft_n, int batch, int quick, double *build_ns_out,
+                                      double *corr_ns_out) {
+    return icm_gpu_measure_fused_pair_ns(fft_n, batch, quick, build_ns_out, corr_ns_out);
+}
+
+// ------------------------------------------------------------ icm_gb300.h
+int icm_last_status(void) { return t_last_status; }
+
+int icm_gb300_set_config(const IcmGb300Config *cfg) {
+    if (cfg) g_config = *cfg;
+    else memset(&g_config, 0, sizeof(g_config));
+    return 0;
+}
+
+int icm_gpu_equity_batched(int T, const int *n, const int *k, const double *S, const double *payout, int Q,
+                           double *equity, IcmGpuRunStats *stats) {
+    if (T < 1 || !n || !k || !S || !payout || !equity || Q < 1) {
+        set_error("icm_gpu_equity_batched invalid arguments");
+        return -1;
+    }
+    for (int t = 0; t < T; ++t)
+        if (n[t] < 1 || k[t] < 1 || k[t] > n[t]) {
+            set_error("icm_gpu_equity_batched: tournament " + std::to_string(t) + " needs 1 <= k <= n");
+            return -1;
+        }
+    const double t0 = now_ns();
+    long so = 0, po = 0, launches = 0;
+    for (int t = 0; t < T; ++t) {
+        if (run_full(n[t], S + so, Q, payout + po, k[t], equity + so, nullptr, 0, nullptr, nullptr) != 0)
+            return -1;
+        launches += t_launches;
+        so += n[t];
+        po += k[t];
+    }
+    t_launches = launches;
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->total_ns = now_ns() - t0;
+        stats->engine = 1;
+    }
+    return 0;
+}
+
+int icm_gpu_measure_fp64_gflops(double *gflops_out) {
+    if (!gflops_out || !ensure_device()) return 0;
+    std::string err;
+    if (measure_fp64_gflops(gflops_out, err) != 0) { set_error(err); return 0; }
+    return 1;
+}
+
+long icm_gpu_last_launch_count(void) { return t_launches; }
+
+}  // extern "C"

@@ -1,0 +1,435 @@
+// engine.cu -- plans (geometry, buffers) and the per-call launch sequence.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "engine.h"
+#include "kernels.h"
+
+namespace icmg {
+
+IcmGb300Config g_config = {};
+int g_device = -1;
+
+static double now_ns() {
+    return (double)std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+// ------------------------------------------------------------ nodes
+// erfc-trapezoid rule in probit space (reference src/cpu/icm.c:117-132):
+// y_q = y_lo + q h on [-7.7, max(6.5, sqrt(2) sqrt(ln Smax + 25))],
+// logv_q = log Phi(y_q), w_q = h phi(y_q).
+static double log_Phi(double y) {
+    if (y >= 0) return std::log1p(-std::erfc(y / std::sqrt(2.0)) / 2.0);
+    return std::log(std::erfc(-y / std::sqrt(2.0)) / 2.0);
+}
+
+void make_nodes(int Q, double Smax, std::vector<double> &logv, std::vector<double> &w) {
+    const double y_lo = -7.7;
+    double y_hi = std::sqrt(2.0) * std::sqrt(std::log(Smax) + 25.0);
+    if (y_hi < 6.5) y_hi = 6.5;
+    const double h = (y_hi - y_lo) / (Q - 1);
+    logv.resize(Q);
+    w.resize(Q);
+    for (int q = 0; q < Q; ++q) {
+        const double y = y_lo + q * h;
+        logv[q] = log_Phi(y);
+        w[q] = h * std::exp(-0.5 * y * y) / std::sqrt(2 * M_PI);
+    }
+}
+
+// ------------------------------------------------------------ twiddles
+// tw[t] = exp(-2 pi i t / 2^L).  Each entry is computed in long double from
+// an angle folded into [0, pi/4] with exact integer reflections.
+static void unit_root(long t, long N, double *re, double *im) {
+    static const long double two_pi = 6.283185307179586476925286766559005768L;
+    t %= N;
+    int conj = 0, neg_c = 0;
+    if (2 * t > N) { t = N - t; conj = 1; }
+    long num = t, den = N;
+    if (4 * t > N) { num = N - 2 * t; den = 2 * N; neg_c = 1; }
+    long double c, s;
+    if (8 * num > den) {
+        const long double b = two_pi * (long double)(den - 4 * num) / (4.0L * (long double)den);
+        c = sinl(b);
+        s = cosl(b);
+    } else {
+        const long double a = two_pi * (long double)num / (long double)den;
+        c = cosl(a);
+        s = sinl(a);
+    }
+    if (neg_c) c = -c;
+    *re = (double)c;
+    *im = conj ? (double)s : (double)(-s);
+}
+
+static std::mutex g_tw_mu;
+static double2 *g_tw[64] = {};   // per device
+static int g_tw_log[64] = {};
+
+const double2 *twiddles(int logN, cudaStream_t s, std::string &err, int *logTW) {
+    std::lock_guard<std::mutex> lk(g_tw_mu);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) { err = "device index out of range"; return nullptr; }
+    if (g_tw[dev] && g_tw_log[dev] >= logN) { *logTW = g_tw_log[dev]; return g_tw[dev]; }
+    const int L = std::max(logN, 12);
+    const long N = 1L << L;
+    std::vector<double2> h((size_t)N);
+    // first octant directly, the rest by symmetry of the table
+    for (long t = 0; t < N; ++t) unit_root(t, N, &h[(size_t)t].x, &h[(size_t)t].y);
+    double2 *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(double2) * (size_t)N);
+    if (e != cudaSuccess) { err = std::string("twiddle table: ") + cudaGetErrorString(e); return nullptr; }
+    e = cudaMemcpyAsync(d, h.data(), sizeof(double2) * (size_t)N, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { err = std::string("twiddle upload: ") + cudaGetErrorString(e); cudaFree(d); return nullptr; }
+    // older tables stay allocated: plans in flight may still read them
+    g_tw[dev] = d;
+    g_tw_log[dev] = L;
+    *logTW = L;
+    return d;
+}
+
+// ------------------------------------------------------------ plans
+static int pow2_ge(long v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+static int ilog2(long v) {
+    int l = 0;
+    while ((1L << l) < v) ++l;
+    return l;
+}
+static int round2(int v) { return (v + 1) & ~1; }
+
+int select_block_size(int n, int k) {
+    (void)k;
+    int B = g_config.block_size > 0 ? g_config.block_size : 8;
+    if (B <= 4) B = 4;
+    else if (B <= 8) B = 8;
+    else if (B <= 16) B = 16;
+    else B = 32;
+    (void)n;
+    return B;
+}
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err) {
+    if (n < 1 || k < 1 || k > n || !S) {
+        err = "invalid plan arguments n=" + std::to_string(n) + " k=" + std::to_string(k);
+        return nullptr;
+    }
+    for (int i = 0; i < n; ++i)
+        if (!(S[i] > 0.0) || !std::isfinite(S[i])) {
+            err = "stacks must be finite and positive (S[" + std::to_string(i) + "])";
+            return nullptr;
+        }
+    Plan *p = new Plan();
+    p->n = n;
+    p->k = k;
+    if (opts) p->opts = *opts;
+    p->opts.device_id = g_device;
+    p->B = select_block_size(n, k);
+    p->fft_min_deg = g_config.fft_min_degree > 0 ? g_config.fft_min_degree : 64;
+    const int B = p->B;
+
+    // descending stacks, ties by original index (reference gpu_plan.cu:405-409)
+    p->perm.resize(n);
+    for (int i = 0; i < n; ++i) p->perm[i] = i;
+    std::sort(p->perm.begin(), p->perm.end(), [S](int a, int b) {
+        return S[a] > S[b] || (S[a] == S[b] && a < b);
+    });
+    p->S_sorted.resize(n);
+    p->inv_perm.resize(n);
+    for (int i = 0; i < n; ++i) {
+        p->S_sorted[i] = S[p->perm[i]];
+        p->inv_perm[p->perm[i]] = i;
+    }
+    p->Smax = p->S_sorted[0];
+
+    // geometry: node at level l covers B << l players
+    p->nblocks = (n + B - 1) / B;
+    const int Nt = pow2_ge(p->nblocks);
+    p->L = ilog2(Nt) + 1;
+    if (p->L > kMaxLevels) { err = "tournament too large"; delete p; return nullptr; }
+    for (int l = 0; l < p->L; ++l) {
+        Level &v = p->lv[l];
+        v.nreal = (l == 0) ? p->nblocks : (p->lv[l - 1].nreal + 1) / 2;
+        v.deg = (long)B << l;
+        v.plen = (int)std::min<long>(v.deg + 1, k);
+        v.glen = (int)std::min<long>(v.deg, k);
+        v.pst = round2(v.plen);
+        v.gst = round2(v.glen);
+        if (l >= 1) {
+            const Level &c = p->lv[l - 1];
+            v.npairs = c.nreal / 2;
+            v.fft = (c.deg >= p->fft_min_deg) ? 1 : 0;
+            if (v.fft) {
+                long need = std::max<long>(2L * c.plen - 2, (long)c.glen + c.plen - 1);
+                v.fftn = std::max(4, pow2_ge(need));
+            }
+        }
+    }
+    // per-node element counts
+    size_t per_q = 0;
+    size_t fa = 0, fb = 0;
+    for (int l = 0; l < p->L; ++l) {
+        Level &v = p->lv[l];
+        if (l <= p->L - 2 || l == 0) {   // level 0 always exists (leaf blocks)
+            v.P_q = (size_t)v.nreal * v.pst;
+            v.g_q = (size_t)v.nreal * v.gst;
+        }
+        if (l >= 1 && v.fft) {
+            v.spec_q = (size_t)2 * v.npairs * (v.fftn / 2 + 1);
+            fa = std::max(fa, (size_t)v.npairs * v.fftn);
+            fb = std::max(fb, (size_t)v.npairs * (v.fftn / 2));
+        }
+        per_q += (v.P_q + v.g_q) * 8 + v.spec_q * 16 + 512;
+    }
+    per_q += ((size_t)2 * n + (size_t)p->nblocks * (B + 1)) * 8 + 1024;
+    per_q += (fa * 2 + fb) * 16;
+
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    size_t budget = g_config.max_device_bytes ? g_config.max_device_bytes
+                                              : std::min<size_t>((size_t)(free_b * 0.6), (size_t)48 << 30);
+    int qc = (int)std::min<size_t>(256, std::max<size_t>(1, budget / std::max<size_t>(per_q, 1)));
+    if (g_config.q_chunk > 0) qc = std::min(qc, g_config.q_chunk);
+    p->qc = qc;
+
+    // arena
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
+    const size_t o_S = take(sizeof(double) * n), o_perm = take(sizeof(int) * n);
+    const size_t o_pay = take(sizeof(double) * k), o_acc = take(sizeof(double) * n);
+    const size_t o_out = take(sizeof(double) * n), o_act = take(n);
+    size_t hot_total = 0;
+    for (int l = 0; l < p->L; ++l) { p->hot_off[l] = hot_total; hot_total += (size_t)(Nt >> l); }
+    const size_t o_hot = take(hot_total);
+    const size_t o_a = take(sizeof(double) * (size_t)qc * n);
+    const size_t o_bp = take(sizeof(double) * (size_t)qc * p->nblocks * (B + 1));
+    const size_t o_con = take(sizeof(double) * (size_t)qc * n);
+    size_t o_P[kMaxLevels], o_g[kMaxLevels], o_spec[kMaxLevels];
+    for (int l = 0; l < p->L; ++l) {
+        const Level &v = p->lv[l];
+        o_P[l] = v.P_q ? take(sizeof(double) * (size_t)qc * v.P_q) : 0;
+        o_g[l] = v.g_q ? take(sizeof(double) * (size_t)qc * v.g_q) : 0;
+        o_spec[l] = v.spec_q ? take(sizeof(double2) * (size_t)qc * v.spec_q) : 0;
+    }
+    p->fft_work = std::max(fa, fb) * qc;
+    const size_t o_fa = fa ? take(sizeof(double2) * (size_t)qc * fa) : 0;
+    const size_t o_fb = fa ? take(sizeof(double2) * (size_t)qc * std::max(fa, fb)) : 0;
+    const size_t o_fc = fa ? take(sizeof(double2) * (size_t)qc * fa) : 0;
+
+    cudaError_t e = cudaMalloc(&p->arena, off);
+    if (e != cudaSuccess) {
+        err = "device allocation of " + std::to_string(off) + " bytes failed: " + cudaGetErrorString(e);
+        delete p;
+        return nullptr;
+    }
+    p->arena_bytes = off;
+    p->peak_bytes = (double)off;
+    char *A = p->arena;
+    p->d_S = (double *)(A + o_S);
+    p->d_perm = (int *)(A + o_perm);
+    p->d_payout = (double *)(A + o_pay);
+    p->d_acc = (double *)(A + o_acc);
+    p->d_out = (double *)(A + o_out);
+    p->d_active = (uint8_t *)(A + o_act);
+    p->d_hot = (uint8_t *)(A + o_hot);
+    p->d_a = (double *)(A + o_a);
+    p->d_blockP = (double *)(A + o_bp);
+    p->d_contrib = (double *)(A + o_con);
+    for (int l = 0; l < p->L; ++l) {
+        Level &v = p->lv[l];
+        v.P = v.P_q ? (double *)(A + o_P[l]) : nullptr;
+        v.g = v.g_q ? (double *)(A + o_g[l]) : nullptr;
+        v.spec = v.spec_q ? (double2 *)(A + o_spec[l]) : nullptr;
+    }
+    if (fa) {
+        p->d_fa = (double2 *)(A + o_fa);
+        p->d_fb = (double2 *)(A + o_fb);
+        p->d_fc = (double2 *)(A + o_fc);
+    }
+    e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_perm, p->perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) {
+        err = std::string("plan upload: ") + cudaGetErrorString(e);
+        plan_destroy(p);
+        return nullptr;
+    }
+    if (p->opts.verbose) {
+        fprintf(stderr, "icm_gb300 plan: n=%d k=%d B=%d L=%d qc=%d arena=%.1f MB\n", n, k, B, p->L, qc,
+                off / 1e6);
+        for (int l = 0; l < p->L; ++l) {
+            const Level &v = p->lv[l];
+            fprintf(stderr, "  level %2d nreal=%7d deg=%8ld plen=%7d glen=%7d %s N=%d\n", l, v.nreal, v.deg,
+                    v.plen, v.glen, v.fft ? "fft" : "school", v.fftn);
+        }
+    }
+    return p;
+}
+
+void plan_destroy(Plan *p) {
+    if (!p) return;
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    if (p->graph) cudaGraphExecDestroy(p->graph);
+    if (p->d_node) cudaFree(p->d_node);
+    if (p->arena) cudaFree(p->arena);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+// subset: active players (sorted order) and per-level hot bitmaps
+// (reference src/cpu/icm.c:2430-2473)
+int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &err) {
+    const int n = p->n, B = p->B;
+    std::vector<uint8_t> act(n, 0);
+    for (int t = 0; t < n_targets; ++t) {
+        const int o = targets[t];
+        if (o >= 0 && o < n) act[p->inv_perm[o]] = 1;
+    }
+    const int Nt = 1 << (p->L - 1);
+    size_t total = 0;
+    for (int l = 0; l < p->L; ++l) total += (size_t)(Nt >> l);
+    std::vector<uint8_t> hot(total, 0);
+    for (int b = 0; b < p->nblocks; ++b) {
+        const int s = b * B, e = std::min(n, s + B);
+        for (int j = s; j < e; ++j)
+            if (act[j]) { hot[p->hot_off[0] + b] = 1; break; }
+    }
+    for (int l = 1; l < p->L; ++l) {
+        const int nc = Nt >> (l - 1), np = Nt >> l;
+        for (int j = 0; j < np; ++j) {
+            const int lft = (2 * j < nc) ? hot[p->hot_off[l - 1] + 2 * j] : 0;
+            const int rgt = (2 * j + 1 < nc) ? hot[p->hot_off[l - 1] + 2 * j + 1] : 0;
+            hot[p->hot_off[l] + j] = (uint8_t)(lft | rgt);
+        }
+    }
+    cudaError_t e = cudaMemcpyAsync(p->d_active, act.data(), n, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_hot, hot.data(), total, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) { err = std::string("subset upload: ") + cudaGetErrorString(e); return -1; }
+    p->subset = true;
+    return 0;
+}
+
+// one chunk of nq nodes starting at active-node index q0
+static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first) {
+    cudaStream_t st = p->stream;
+    const int L = p->L;
+    Level *lv = p->lv;
+    launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, lv[0].P, lv[0].pst,
+                lv[0].plen, st);
+    ++p->launches;
+    for (int l = 1; l <= L - 2; ++l) {
+        if (lv[l].fft) {
+            launch_fft_build(lv[l - 1], lv[l], nq, p->d_fa, p->d_fb, p->d_fc, false, tw, logTW, st, &p->launches);
+            if (lv[l - 1].nreal & 1) { launch_school_build(lv[l - 1], lv[l], nq, lv[l].npairs, st); ++p->launches; }
+        } else {
+            launch_school_build(lv[l - 1], lv[l], nq, 0, st);
+            ++p->launches;
+        }
+    }
+    if (L >= 2 && lv[L - 1].fft)
+        launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches);
+    for (int l = L - 1; l >= 1; --l) {
+        const bool root = (l == L - 1);
+        const double *gp = root ? p->d_payout : lv[l].g;
+        const size_t gp_q = root ? 0 : lv[l].g_q;
+        const int gst_p = root ? 0 : lv[l].gst;
+        const int gpl = root ? p->k : lv[l].glen;
+        const uint8_t *hot_c = p->subset ? p->d_hot + p->hot_off[l - 1] : nullptr;
+        if (lv[l].fft) {
+            launch_fft_prop(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nq, hot_c, p->d_fa, p->d_fb, p->d_fc, tw, logTW,
+                            st, &p->launches);
+            if (lv[l - 1].nreal & 1) {
+                launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 2 * lv[l].npairs, st);
+                ++p->launches;
+            }
+        } else {
+            launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 0, st);
+            ++p->launches;
+        }
+    }
+    const double *g0 = (L == 1) ? p->d_payout : lv[0].g;
+    const size_t g0_q = (L == 1) ? 0 : lv[0].g_q;
+    const int gst0 = (L == 1) ? 0 : lv[0].gst;
+    launch_divide(p->B, p->n, p->k, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, g0, g0_q, gst0,
+                  p->subset ? p->d_active : nullptr, p->d_contrib, st);
+    launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, first ? 1 : 0, st);
+    p->launches += 2;
+}
+
+int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats, std::string &err) {
+    if (!p || Q < 1 || !payout || !equity) { err = "invalid arguments"; return -1; }
+    const double t0 = now_ns();
+    p->launches = 0;
+    std::vector<double> logv, w;
+    make_nodes(Q, p->Smax, logv, w);
+    std::vector<double> node;
+    node.reserve(3 * (size_t)Q);
+    for (int q = 0; q < Q; ++q) {
+        if (w[q] == 0.0) continue;   // the reference skips zero-weight nodes
+        node.push_back(logv[q]);
+        node.push_back(w[q]);
+        node.push_back(std::exp(-logv[q]));
+    }
+    const int nact = (int)(node.size() / 3);
+    cudaError_t e = cudaSuccess;
+    if (nact > p->qmax) {
+        if (p->d_node) cudaFree(p->d_node);
+        p->d_node = nullptr;
+        e = cudaMalloc(&p->d_node, sizeof(double) * 3 * (size_t)std::max(nact, 1));
+        if (e != cudaSuccess) { err = std::string("node buffer: ") + cudaGetErrorString(e); return -1; }
+        p->qmax = nact;
+    }
+    if (nact)
+        e = cudaMemcpyAsync(p->d_node, node.data(), sizeof(double) * node.size(), cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * p->k, cudaMemcpyHostToDevice, p->stream);
+    if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return -1; }
+    int logNeed = 12, logTW = 0;
+    for (int l = 1; l < p->L; ++l)
+        if (p->lv[l].fft) logNeed = std::max(logNeed, ilog2(p->lv[l].fftn));
+    const double2 *tw = twiddles(logNeed, p->stream, err, &logTW);
+    if (!tw) return -1;
+    if (nact == 0) {
+        e = cudaMemsetAsync(p->d_acc, 0, sizeof(double) * p->n, p->stream);
+        if (e != cudaSuccess) { err = cudaGetErrorString(e); return -1; }
+    }
+    for (int q0 = 0; q0 < nact; q0 += p->qc) {
+        const int nq = std::min(p->qc, nact - q0);
+        run_chunk(p, q0, nq, tw, logTW, q0 == 0);
+    }
+    launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
+    ++p->launches;
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(equity, p->d_out, sizeof(double) * p->n, cudaMemcpyDeviceToHost, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) { err = std::string("execution: ") + cudaGetErrorString(e); return -1; }
+    const double t1 = now_ns();
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->total_ns = t1 - t0;
+        stats->peak_vram_bytes = (size_t)p->peak_bytes;
+        stats->engine = 1;
+        stats->B = p->B;
+    }
+    return 0;
+}
+
+}  // namespace icmg

@@ -1,0 +1,106 @@
+// engine.h -- internal interface of the GB300 ICM engine (not installed).
+//
+// One plan = one tournament (or one batch of tournaments) with its tree
+// geometry and device buffers.  The quadrature nodes are processed in chunks
+// of `qc` nodes; every kernel of a chunk covers all nodes of the chunk
+// (grid.y = node), so one launch per tree level does the work of qc trees.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/icm.h"
+#include "../../include/icm_gb300.h"
+#include "../../include/icm_gpu.h"
+
+namespace icmg {
+
+constexpr int kMaxLevels = 40;
+constexpr int kMaxB = 32;            // largest leaf block
+constexpr int kSmemFftMax = 8192;    // complex points one CTA transforms in shared memory
+
+// Per tree level.  Level 0 = leaf blocks; level l >= 1 nodes are parents of
+// level l-1 nodes.  Quantities for the *products computed at level l* (the
+// FFT size etc.) are stored on level l.
+struct Level {
+    int nreal = 0;        // real nodes
+    long deg = 0;         // players under a full node (B << l)
+    int plen = 0;         // polynomial coefficients kept: min(deg+1, k)
+    int glen = 0;         // g entries kept: min(deg, k)
+    int pst = 0, gst = 0; // strides in doubles
+    int fft = 0;          // 1: products/correlations of this parent level use FFTs
+    int fftn = 0;         // real FFT size N (power of two)
+    int npairs = 0;       // parents with two children (FFT levels)
+    size_t P_q = 0, g_q = 0, spec_q = 0;   // per-node element counts (doubles / double2)
+    double *P = nullptr, *g = nullptr;
+    double2 *spec = nullptr;               // child spectra cached build -> propagate
+};
+
+struct TourDesc {          // batched mode: one tournament inside a batch plan
+    int n, k, off;         // players, paid places, offset into concatenated arrays
+};
+
+struct Plan {
+    int n = 0, k = 0, B = 0, nblocks = 0, L = 0;
+    int fft_min_deg = 64;
+    std::vector<double> S_sorted;
+    std::vector<int> perm;          // perm[i] = original index of sorted player i
+    std::vector<int> inv_perm;
+    double Smax = 0.0;
+    Level lv[kMaxLevels];
+    int qc = 1;                     // quadrature nodes per chunk
+    int qmax = 0;                   // capacity of the node arrays
+    IcmGpuOptions opts{};
+    // device
+    cudaStream_t stream = nullptr;
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    double *d_S = nullptr;          // sorted stacks
+    int *d_perm = nullptr;
+    double *d_payout = nullptr;     // g at the root: payout zero-padded to glen(root)
+    double *d_a = nullptr;          // [qc][n]
+    double *d_blockP = nullptr;     // [qc][nblocks][B+1]
+    double *d_contrib = nullptr;    // [qc][n]
+    double *d_acc = nullptr;        // [n] sorted order
+    double *d_out = nullptr;        // [n] original order
+    double *d_node = nullptr;       // [qmax][3]: logv, w, 1/v for the active nodes
+    uint8_t *d_active = nullptr;    // [n] sorted order (subset), or null
+    uint8_t *d_hot = nullptr;       // hot bitmap, all levels
+    size_t hot_off[kMaxLevels] = {};
+    double2 *d_fa = nullptr, *d_fb = nullptr, *d_fc = nullptr;  // FFT work buffers
+    size_t fft_work = 0;            // double2 per buffer
+    bool subset = false;
+    long launches = 0;
+    // graph replay (enable_graphs)
+    cudaGraphExec_t graph = nullptr;
+    int graph_nq = -1;
+    double peak_bytes = 0;
+};
+
+// lifecycle (engine.cu)
+Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err);
+void plan_destroy(Plan *p);
+int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &err);
+int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats,
+             std::string &err);
+int select_block_size(int n, int k);
+
+// quadrature nodes (host), restating the reference's erfc-trapezoid rule
+void make_nodes(int Q, double Smax, std::vector<double> &logv, std::vector<double> &w);
+
+// device-wide twiddle table exp(-2 pi i t / 2^logTW); *logTW receives the
+// table's size, which may exceed the request
+const double2 *twiddles(int logN, cudaStream_t s, std::string &err, int *logTW);
+
+// probes (probes.cu)
+int measure_fp64_gflops(double *out, std::string &err);
+int measure_hbm_gbps(double *out, std::string &err);
+
+// process-wide configuration
+extern IcmGb300Config g_config;
+extern int g_device;
+
+}  // namespace icmg

@@ -1,0 +1,519 @@
+// kernels.cu -- device kernels of the GB300 ICM engine and their launchers.
+//
+// Per quadrature node q the engine evaluates (reference src/cpu/icm.c:2523-2695)
+//   a_i = exp(S_i logv_q)                    (0 when S_i logv_q < -700)
+//   inner_i = sum_{m<k} payout[m] [x^m] prod_{j != i} (a_j + (1-a_j) x)
+//   equity_i += w_q S_i a_i / v_q * inner_i  (non-finite weight -> 0)
+// through a subproduct tree over blocks of B players (sorted by stack,
+// descending): leaf block products, truncated products up the tree, middle
+// products of the payout down the tree, then a per-player synthetic
+// division of its block product fused with the dot against the block's g.
+//
+// Every kernel covers a whole chunk of nodes: blockIdx.y (or the batch
+// index) selects the node, so one launch per tree level serves qc trees.
+#include <algorithm>
+
+#include "engine.h"
+#include "fft.cuh"
+#include "kernels.h"
+
+namespace icmg {
+
+// ------------------------------------------------------------------ leaves
+// Leaf factors and block products (reference src/cpu/icm.c:2199-2224,
+// src/gpu/gpu_kernels.cu:909-936,1030-1091).  One thread per (node, block);
+// the block product lives in registers.  Updating all B+1 coefficients for
+// every player adds exact zeros above the running degree, so the result is
+// the reference's recurrence P[m] = a P[m] + (1-a) P[m-1] bit for bit.
+template <int B>
+__global__ void k_leaf(int n, int nblocks, const double *__restrict__ S, const double *__restrict__ node,
+                       int q0, double *__restrict__ a_out, double *__restrict__ blockP,
+                       double *__restrict__ P0, int pst0, int plen0) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    if (b >= nblocks) return;
+    const double logv = node[3 * (q0 + q)];
+    const int start = b * B;
+    const int bs = min(B, n - start);
+    double P[B + 1];
+    P[0] = 1.0;
+#pragma unroll
+    for (int m = 1; m <= B; ++m) P[m] = 0.0;
+    double *arow = a_out + (size_t)q * n + start;
+    for (int j = 0; j < bs; ++j) {
+        const double arg = S[start + j] * logv;
+        const double a = (arg < -700.0) ? 0.0 : exp(arg);
+        arow[j] = a;
+        const double bb = 1.0 - a;
+#pragma unroll
+        for (int m = B; m >= 1; --m) P[m] = a * P[m] + bb * P[m - 1];
+        P[0] *= a;
+    }
+    double *bp = blockP + ((size_t)q * nblocks + b) * (B + 1);
+#pragma unroll
+    for (int m = 0; m <= B; ++m) bp[m] = P[m];
+    double *leaf = P0 + ((size_t)q * nblocks + b) * pst0;
+#pragma unroll
+    for (int m = 0; m <= B; ++m)
+        if (m < pst0) leaf[m] = (m < plen0) ? P[m] : 0.0;
+    for (int m = B + 1; m < pst0; ++m) leaf[m] = 0.0;
+}
+
+// ------------------------------------------------------- schoolbook build
+// parent j = L*R mod x^lp, children of length lc (reference icm.c:465-480).
+// One thread per output coefficient; parents >= j0 only (the FFT path uses
+// j0 = npairs to let this kernel copy a lone left child).
+__global__ void k_school_build(const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc, int nreal_c,
+                               double *__restrict__ Pp, size_t Pp_q, int pst_p, int lp, int nreal_p, int j0) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int j = j0 + (int)(idx / pst_p);
+    const int t = (int)(idx % pst_p);
+    if (j >= nreal_p) return;
+    const double *L = Pc + q * Pc_q + (size_t)(2 * j) * pst_c;
+    double *out = Pp + q * Pp_q + (size_t)j * pst_p;
+    if (t >= lp) { out[t] = 0.0; return; }
+    if (2 * j + 1 >= nreal_c) { out[t] = (t < lc) ? L[t] : 0.0; return; }
+    const double *R = L + pst_c;
+    const int ilo = max(0, t - (lc - 1));
+    const int ihi = min(t, lc - 1);
+    double s = 0.0;
+    for (int i = ilo; i <= ihi; ++i) s = fma(L[i], R[t - i], s);
+    out[t] = s;
+}
+
+// --------------------------------------------------- schoolbook propagate
+// g_c[m] = sum_i P_sib[i] g_parent[m+i] (reference icm.c:489-507, 1667-1819).
+// One thread per child coefficient, children >= c0 only.  gp_q == 0 lets the
+// root's g be the payout vector shared by all nodes.
+__global__ void k_school_prop(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl,
+                              const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc,
+                              double *__restrict__ gc, size_t gc_q, int gst_c, int gcl, int nreal_c,
+                              const uint8_t *__restrict__ hot_c, int c0) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int c = c0 + (int)(idx / gst_c);
+    const int m = (int)(idx % gst_c);
+    if (c >= nreal_c) return;
+    double *out = gc + q * gc_q + (size_t)c * gst_c;
+    if (m >= gcl || (hot_c && !hot_c[c])) { out[m] = 0.0; return; }
+    const double *g = gp + q * gp_q + (size_t)(c >> 1) * gst_p;
+    const int sib = c ^ 1;
+    if (sib >= nreal_c) { out[m] = (m < gpl) ? g[m] : 0.0; return; }
+    const double *P = Pc + q * Pc_q + (size_t)sib * pst_c;
+    const int imax = min(lc, gpl - m);
+    double s = 0.0;
+    for (int i = 0; i < imax; ++i) s = fma(P[i], g[m + i], s);
+    out[m] = s;
+}
+
+// --------------------------------------------------------- divide + dot
+// Per player: Q_i = P_block / (a_i + (1-a_i) x) by the forward recurrence
+// when a_i > 0.5, the backward one when a_i > 1e-15, else a shift; then
+// inner_i = sum_{m < min(bs,k)} g_block[m] Q_i[m] and the node's weight
+// (reference icm.c:2230-2302 and 2584-2589).
+template <int B>
+__global__ void k_divide(int n, int k, int nblocks, const double *__restrict__ S, const double *__restrict__ node,
+                         int q0, const double *__restrict__ a_in, const double *__restrict__ blockP,
+                         const double *__restrict__ g0, size_t g0_q, int gst0,
+                         const uint8_t *__restrict__ active, double *__restrict__ contrib) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    if (i >= n) return;
+    double *out = contrib + (size_t)q * n + i;
+    if (active && !active[i]) { *out = 0.0; return; }
+    const int b = i / B;
+    const int start = b * B;
+    const int bs = min(B, n - start);
+    const int pk = min(bs, k);
+    const double a = a_in[(size_t)q * n + i];
+    const double bb = 1.0 - a;
+    const double *P = blockP + ((size_t)q * nblocks + b) * (B + 1);
+    const double *g = g0 + q * g0_q + (size_t)b * gst0;
+    double eq = 0.0;
+    if (a > 0.5) {
+        const double ia = 1.0 / a, c = -bb * ia;
+        double Qv = P[0] * ia;
+        eq = g[0] * Qv;
+        for (int m = 1; m < pk; ++m) {
+            Qv = c * Qv + P[m] * ia;
+            eq += g[m] * Qv;
+        }
+    } else if (a > 1e-15) {
+        const double ib = 1.0 / bb, c = -a * ib;
+        double Qa[B];
+        double Qp = P[bs] * ib;
+        Qa[bs - 1] = Qp;
+        for (int m = bs - 2; m >= 0; --m) {
+            Qp = c * Qp + P[m + 1] * ib;
+            Qa[m] = Qp;
+        }
+        for (int m = 0; m < pk; ++m) eq += g[m] * Qa[m];
+    } else {
+        for (int m = 0; m < pk; ++m) eq += g[m] * P[m + 1];
+    }
+    const double *nd = node + 3 * (q0 + q);
+    double pw = nd[1] * S[i] * a * nd[2];
+    if (!isfinite(pw)) pw = 0.0;
+    *out = pw * eq;
+}
+
+// ordered sum over the chunk's nodes: deterministic for a fixed chunking
+__global__ void k_accumulate(int n, int nq, const double *__restrict__ contrib, double *__restrict__ acc,
+                             int first) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = first ? 0.0 : acc[i];
+    for (int q = 0; q < nq; ++q) s += contrib[(size_t)q * n + i];
+    acc[i] = s;
+}
+
+__global__ void k_scatter(int n, const double *__restrict__ acc, const int *__restrict__ perm,
+                          const uint8_t *__restrict__ active, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[perm[i]] = (active && !active[i]) ? 0.0 : acc[i];
+}
+
+// --------------------------------------------------------------- FFT core
+// Batched complex transforms of size 2^logM, in place in `data` (natural
+// order).  Sizes up to kSmemFftMax run in one kernel; larger sizes use the
+// four-step split M = M1 * M2 through `scratch`.
+__global__ void k_fft_smem_fwd(double2 *data, long batch, int logM, int cb, const double2 *tw, int logTW);
+__global__ void k_fft_smem_inv(double2 *data, long batch, int logM, int cb, const double2 *tw, int logTW);
+
+template <int SIGN>
+__global__ void k_fft_smem(double2 *__restrict__ data, long batch, int logM, int cb,
+                           const double2 *__restrict__ tw, int logTW) {
+    extern __shared__ double2 sx[];
+    const int M = 1 << logM;
+    const long item0 = (long)blockIdx.x * cb;
+    const int cnt = (int)min((long)cb, batch - item0);
+    for (int e = threadIdx.x; e < cnt * M; e += blockDim.x) {
+        const int it = e >> logM, s = e & (M - 1);
+        sx[e] = data[(item0 + it) * M + bitrev(s, logM)];
+    }
+    __syncthreads();
+    smem_fft_dit<SIGN>(sx, logM, cnt, tw, logTW);
+    for (int e = threadIdx.x; e < cnt * M; e += blockDim.x) data[item0 * M + e] = sx[e];
+}
+
+// four-step, pass A: columns n2 of the M1 x M2 view x[M2 n1 + n2]
+template <int SIGN>
+__global__ void k_fft4_cols(const double2 *__restrict__ in, double2 *__restrict__ out, int logM1, int logM2,
+                            int cb, const double2 *__restrict__ tw, int logTW) {
+    extern __shared__ double2 sx[];
+    const int M1 = 1 << logM1, M2 = 1 << logM2;
+    const long item = blockIdx.y;
+    const int n20 = blockIdx.x * cb;
+    const double2 *src = in + (item << (logM1 + logM2));
+    for (int e = threadIdx.x; e < cb * M1; e += blockDim.x) {
+        const int c = e % cb, s = e / cb;
+        sx[c * M1 + s] = src[(long)bitrev(s, logM1) * M2 + n20 + c];
+    }
+    __syncthreads();
+    smem_fft_dit<SIGN>(sx, logM1, cb, tw, logTW);
+    const int logM = logM1 + logM2;
+    double2 *dst = out + (item << logM);
+    for (int e = threadIdx.x; e < cb * M1; e += blockDim.x) {
+        const int c = e >> logM1, k1 = e & (M1 - 1);
+        const int n2 = n20 + c;
+        const int t = (n2 * k1) & ((1 << logM) - 1);
+        double2 v = sx[e];
+        if (t) v = twmul<SIGN>(v, __ldg(&tw[(long)t << (logTW - logM)]));
+        dst[(long)n2 * M1 + k1] = v;
+    }
+}
+
+// four-step, pass B: rows k1, FFT over n2, output X[k1 + M1 k2]
+template <int SIGN>
+__global__ void k_fft4_rows(const double2 *__restrict__ in, double2 *__restrict__ out, int logM1, int logM2,
+                            int cb, const double2 *__restrict__ tw, int logTW) {
+    extern __shared__ double2 sx[];
+    const int M1 = 1 << logM1, M2 = 1 << logM2;
+    const long item = blockIdx.y;
+    const int k10 = blockIdx.x * cb;
+    const double2 *src = in + (item << (logM1 + logM2));
+    for (int e = threadIdx.x; e < cb * M2; e += blockDim.x) {
+        const int c = e % cb, s = e / cb;
+        sx[c * M2 + s] = src[(long)bitrev(s, logM2) * M1 + k10 + c];
+    }
+    __syncthreads();
+    smem_fft_dit<SIGN>(sx, logM2, cb, tw, logTW);
+    double2 *dst = out + (item << (logM1 + logM2));
+    for (int e = threadIdx.x; e < cb * M2; e += blockDim.x) {
+        const int c = e % cb, k2 = e / cb;
+        dst[(long)k2 * M1 + k10 + c] = sx[c * M2 + k2];
+    }
+}
+
+int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
+                cudaStream_t st, long *launches) {
+    if (batch <= 0) return 0;
+    const int M = 1 << logM;
+    const int threads = 256;
+    if (M <= kSmemFftMax) {
+        const int cb = (M >= 4096) ? 1 : 4096 / M;
+        const long blocks = (batch + cb - 1) / cb;
+        const size_t smem = (size_t)cb * M * sizeof(double2);
+        if (sign < 0)
+            k_fft_smem<-1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW);
+        else
+            k_fft_smem<+1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW);
+        ++*launches;
+        return 0;
+    }
+    if (batch > 65535) {   // grid.y limit of the four-step kernels
+        for (long b0 = 0; b0 < batch; b0 += 65535)
+            fft_batched(data + (b0 << logM), scratch + (b0 << logM), std::min(65535L, batch - b0), logM, sign, tw,
+                        logTW, st, launches);
+        return 0;
+    }
+    const int logM1 = (logM + 1) / 2, logM2 = logM - logM1;
+    const int M1 = 1 << logM1, M2 = 1 << logM2;
+    const int cbA = max(1, min(M2, 4096 / M1));
+    const int cbB = max(1, min(M1, 4096 / M2));
+    dim3 gA(M2 / cbA, (unsigned)batch), gB(M1 / cbB, (unsigned)batch);
+    const size_t smA = (size_t)cbA * M1 * sizeof(double2), smB = (size_t)cbB * M2 * sizeof(double2);
+    if (sign < 0) {
+        k_fft4_cols<-1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW);
+        k_fft4_rows<-1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW);
+    } else {
+        k_fft4_cols<+1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW);
+        k_fft4_rows<+1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW);
+    }
+    *launches += 2;
+    return 0;
+}
+
+void fft_set_smem_limits() {
+    const int mx = kSmemFftMax * (int)sizeof(double2);
+    cudaFuncSetAttribute(k_fft_smem<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft_smem<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_cols<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_cols<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_rows<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_rows<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+// ------------------------------------------------------ FFT tree levels
+// Build at an FFT level: children L, R of length lc packed as z = L + iR,
+// one complex transform of size N gives both spectra; the product spectrum
+// goes back through a half-size complex transform (real-output packing).
+// N >= 2 lc - 2, so only coefficient 0 can alias (with coefficient N); it is
+// taken directly as L[0] R[0], and coefficient N (needed when lp > N) as
+// L[lc-1] R[lc-1].
+__global__ void k_pack_pair(const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc, int npairs, int N,
+                            double2 *__restrict__ z) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int j = (int)(idx / N), t = (int)(idx % N);
+    if (j >= npairs) return;
+    const double *L = Pc + q * Pc_q + (size_t)(2 * j) * pst_c;
+    const double *R = L + pst_c;
+    z[((size_t)q * npairs + j) * N + t] = (t < lc) ? make_double2(L[t], R[t]) : make_double2(0.0, 0.0);
+}
+
+// spectra of both children from Z = FFT(L + iR); optionally the product's
+// half-size inverse input U[f] = E[f] + i O[f].
+__global__ void k_build_mid(const double2 *__restrict__ Z, int npairs, int N, double2 *__restrict__ spec,
+                            double2 *__restrict__ U, const double2 *__restrict__ tw, int logTW, int logN) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int h = N >> 1;
+    const int j = (int)(idx / h), f = (int)(idx % h);
+    if (j >= npairs) return;
+    const size_t item = (size_t)q * npairs + j;
+    const double2 *z = Z + item * N;
+    const int fc = h - f;                       // partner frequency for the real inverse
+    const double2 zf = z[f], zn = z[(N - f) & (N - 1)];
+    const double2 zc = z[fc], zcn = z[(N - fc) & (N - 1)];
+    // S_L = (Z[f] + conj Z[-f]) / 2, S_R = (Z[f] - conj Z[-f]) / (2i)
+    const double2 SLf = cscale(cadd(zf, cconj(zn)), 0.5);
+    const double2 SRf = cscale(cmul_mi(csub(zf, cconj(zn))), 0.5);
+    double2 *sL = spec + (2 * item) * (size_t)(h + 1);
+    double2 *sR = sL + (h + 1);
+    sL[f] = SLf;
+    sR[f] = SRf;
+    const double2 SLc = cscale(cadd(zc, cconj(zcn)), 0.5);
+    const double2 SRc = cscale(cmul_mi(csub(zc, cconj(zcn))), 0.5);
+    if (f == 0) { sL[h] = SLc; sR[h] = SRc; }
+    if (!U) return;
+    const double2 Cf = cmul(SLf, SRf);
+    const double2 Cc = cmul(SLc, SRc);
+    // E = C[f] + conj C[h-f];  O = (C[f] - conj C[h-f]) e^{+2 pi i f/N}
+    double2 E = cadd(Cf, cconj(Cc));
+    double2 D = csub(Cf, cconj(Cc));
+    if (f == 0) { E.y = 0.0; D.y = 0.0; }
+    const double2 w = __ldg(&tw[(long)f << (logTW - logN)]);
+    const double2 O = cmulc(D, w);
+    U[item * h + f] = cadd(E, cmul_pi(O));
+}
+
+__global__ void k_build_post(const double2 *__restrict__ u, int npairs, int N,
+                             const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc,
+                             double *__restrict__ Pp, size_t Pp_q, int pst_p, int lp) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int j = (int)(idx / pst_p), t = (int)(idx % pst_p);
+    if (j >= npairs) return;
+    double *out = Pp + q * Pp_q + (size_t)j * pst_p;
+    if (t >= lp) { out[t] = 0.0; return; }
+    const double *L = Pc + q * Pc_q + (size_t)(2 * j) * pst_c;
+    const double *R = L + pst_c;
+    double v;
+    if (t == 0) v = L[0] * R[0];
+    else if (t == N) v = L[lc - 1] * R[lc - 1];
+    else if (t > N) v = 0.0;
+    else {
+        const double2 uv = u[((size_t)q * npairs + j) * (N >> 1) + (t >> 1)];
+        v = ((t & 1) ? uv.y : uv.x) * (1.0 / N);
+    }
+    out[t] = v;
+}
+
+// Propagate at an FFT level: W = FFT_{N/2}(g[2t] + i g[2t+1]) gives the
+// parent's real spectrum G; Y_L = G conj(S_R), Y_R = G conj(S_L); one size-N
+// inverse of Z = Y_L + i Y_R yields both children's g (cyclic correlation,
+// exact because N >= glen_child + lc - 1).
+__global__ void k_prop_pack(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl, int npairs, int N,
+                            const uint8_t *__restrict__ hot_c, double2 *__restrict__ w) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int h = N >> 1;
+    const int j = (int)(idx / h), t = (int)(idx % h);
+    if (j >= npairs) return;
+    const double *g = gp + q * gp_q + (size_t)j * gst_p;
+    const int t0 = 2 * t, t1 = 2 * t + 1;
+    double2 v = make_double2(t0 < gpl ? g[t0] : 0.0, t1 < gpl ? g[t1] : 0.0);
+    if (hot_c && !hot_c[2 * j] && !hot_c[2 * j + 1]) v = make_double2(0.0, 0.0);
+    w[((size_t)q * npairs + j) * h + t] = v;
+}
+
+__global__ void k_prop_mid(const double2 *__restrict__ W, const double2 *__restrict__ spec, int npairs, int N,
+                           double2 *__restrict__ Z, const double2 *__restrict__ tw, int logTW, int logN) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int h = N >> 1;
+    const int j = (int)(idx / (h + 1)), f = (int)(idx % (h + 1));
+    if (j >= npairs) return;
+    const size_t item = (size_t)q * npairs + j;
+    const double2 *w = W + item * h;
+    const double2 wf = w[f & (h - 1)], wc = w[(h - f) & (h - 1)];
+    // G[f] = (W[f] + conj W[h-f])/2 + e^{-2 pi i f/N} (W[f] - conj W[h-f]) / (2i)
+    const double2 Ev = cscale(cadd(wf, cconj(wc)), 0.5);
+    const double2 Od = cscale(cmul_mi(csub(wf, cconj(wc))), 0.5);
+    const double2 tf = __ldg(&tw[(long)f << (logTW - logN)]);
+    const double2 G = cadd(Ev, cmul(Od, tf));
+    const double2 *sL = spec + (2 * item) * (size_t)(h + 1);
+    const double2 *sR = sL + (h + 1);
+    const double2 YL = cmulc(G, sR[f]);
+    const double2 YR = cmulc(G, sL[f]);
+    double2 *z = Z + item * N;
+    z[f] = cadd(YL, cmul_pi(YR));
+    if (f != 0 && f != h) z[N - f] = cadd(cconj(YL), cmul_pi(cconj(YR)));
+}
+
+__global__ void k_prop_post(const double2 *__restrict__ Z, int npairs, int N, double *__restrict__ gc,
+                            size_t gc_q, int gst_c, int gcl, const uint8_t *__restrict__ hot_c) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int c = (int)(idx / gst_c), m = (int)(idx % gst_c);
+    if (c >= 2 * npairs) return;
+    double *out = gc + q * gc_q + (size_t)c * gst_c;
+    if (m >= gcl || (hot_c && !hot_c[c])) { out[m] = 0.0; return; }
+    const double2 zv = Z[((size_t)q * npairs + (c >> 1)) * N + m];
+    out[m] = ((c & 1) ? zv.y : zv.x) * (1.0 / N);
+}
+
+// ------------------------------------------------------------ launchers
+static inline unsigned nblk(long work, int threads) { return (unsigned)((work + threads - 1) / threads); }
+
+void launch_leaf(int B, int n, int nblocks, const double *S, const double *node, int q0, int nq, double *a,
+                 double *blockP, double *P0, int pst0, int plen0, cudaStream_t st) {
+    dim3 g(nblk(nblocks, 128), nq);
+    switch (B) {
+        case 4: k_leaf<4><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
+        case 8: k_leaf<8><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
+        case 16: k_leaf<16><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
+        default: k_leaf<32><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
+    }
+}
+
+void launch_divide(int B, int n, int k, int nblocks, const double *S, const double *node, int q0, int nq,
+                   const double *a, const double *blockP, const double *g0, size_t g0_q, int gst0,
+                   const uint8_t *active, double *contrib, cudaStream_t st) {
+    dim3 g(nblk(n, 128), nq);
+    switch (B) {
+        case 4: k_divide<4><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
+        case 8: k_divide<8><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
+        case 16: k_divide<16><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
+        default: k_divide<32><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
+    }
+}
+
+void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStream_t st) {
+    const long work = (long)(p.nreal - j0) * p.pst;
+    if (work <= 0) return;
+    dim3 g(nblk(work, 256), nq);
+    k_school_build<<<g, 256, 0, st>>>(c.P, c.P_q, c.pst, c.plen, c.nreal, p.P, p.P_q, p.pst, p.plen, p.nreal, j0);
+}
+
+void launch_school_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, int nq,
+                        const uint8_t *hot_c, int c0, cudaStream_t st) {
+    const long work = (long)(c.nreal - c0) * c.gst;
+    if (work <= 0) return;
+    dim3 g(nblk(work, 256), nq);
+    k_school_prop<<<g, 256, 0, st>>>(gp, gp_q, gst_p, gpl, c.P, c.P_q, c.pst, c.plen, c.g, c.g_q, c.gst, c.glen,
+                                     c.nreal, hot_c, c0);
+}
+
+void launch_accumulate(int n, int nq, const double *contrib, double *acc, int first, cudaStream_t st) {
+    k_accumulate<<<nblk(n, 256), 256, 0, st>>>(n, nq, contrib, acc, first);
+}
+
+void launch_scatter(int n, const double *acc, const int *perm, const uint8_t *active, double *out,
+                    cudaStream_t st) {
+    k_scatter<<<nblk(n, 256), 256, 0, st>>>(n, acc, perm, active, out);
+}
+
+// FFT build for parents [0, npairs) of level p (children c); spectra only when
+// U == nullptr (the root level, whose product is never used).
+void launch_fft_build(const Level &c, const Level &p, int nq, double2 *fa, double2 *fb, double2 *fc,
+                      bool spectra_only, const double2 *tw, int logTW, cudaStream_t st, long *launches) {
+    const int N = p.fftn, npairs = p.npairs;
+    if (npairs <= 0) return;
+    int logN = 0;
+    while ((1 << logN) < N) ++logN;
+    dim3 g1(nblk((long)npairs * N, 256), nq);
+    k_pack_pair<<<g1, 256, 0, st>>>(c.P, c.P_q, c.pst, c.plen, npairs, N, fa);
+    fft_batched(fa, fc, (long)nq * npairs, logN, -1, tw, logTW, st, launches);
+    dim3 g2(nblk((long)npairs * (N / 2), 256), nq);
+    k_build_mid<<<g2, 256, 0, st>>>(fa, npairs, N, p.spec, spectra_only ? nullptr : fb, tw, logTW, logN);
+    *launches += 2;
+    if (spectra_only) return;
+    fft_batched(fb, fc, (long)nq * npairs, logN - 1, +1, tw, logTW, st, launches);
+    dim3 g3(nblk((long)npairs * p.pst, 256), nq);
+    k_build_post<<<g3, 256, 0, st>>>(fb, npairs, N, c.P, c.P_q, c.pst, c.plen, p.P, p.P_q, p.pst, p.plen);
+    *launches += 1;
+}
+
+void launch_fft_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
+                     const uint8_t *hot_c, double2 *fa, double2 *fb, double2 *fc, const double2 *tw, int logTW,
+                     cudaStream_t st, long *launches) {
+    const int N = p.fftn, npairs = p.npairs;
+    if (npairs <= 0) return;
+    int logN = 0;
+    while ((1 << logN) < N) ++logN;
+    dim3 g1(nblk((long)npairs * (N / 2), 256), nq);
+    k_prop_pack<<<g1, 256, 0, st>>>(gp, gp_q, gst_p, gpl, npairs, N, hot_c, fb);
+    fft_batched(fb, fc, (long)nq * npairs, logN - 1, -1, tw, logTW, st, launches);
+    dim3 g2(nblk((long)npairs * (N / 2 + 1), 256), nq);
+    k_prop_mid<<<g2, 256, 0, st>>>(fb, p.spec, npairs, N, fa, tw, logTW, logN);
+    fft_batched(fa, fc, (long)nq * npairs, logN, +1, tw, logTW, st, launches);
+    dim3 g3(nblk((long)2 * npairs * c.gst, 256), nq);
+    k_prop_post<<<g3, 256, 0, st>>>(fa, npairs, N, c.g, c.g_q, c.gst, c.glen, hot_c);
+    *launches += 3;
+}
+
+}  // namespace icmg

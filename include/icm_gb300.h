@@ -1,0 +1,63 @@
+/*
+ * icm_gb300.h -- additions of the GB300 engine beyond the reference's API.
+ *
+ * None of these has a counterpart in the reference's headers; they extend
+ * the drop-in surface of icm.h / icm_gpu.h without changing it.
+ */
+#ifndef ICM_GB300_H
+#define ICM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "icm_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status of the last icm_equity / icm_equity_subset call on this thread:
+ * 0 = success, -1 = failure (message in icm_gpu_last_error()).  The
+ * reference's void entry points have no status; this is how callers of the
+ * drop-in learn that the GPU path failed. */
+int icm_last_status(void);
+
+/* Engine configuration (all optional).  Zero fields keep the default.
+ *   block_size        players per leaf block B (default chosen per (n, k))
+ *   fft_min_degree    child degree at which tree levels switch from
+ *                     schoolbook to FFT products (default from the tuner)
+ *   q_chunk           quadrature nodes processed per launch sequence
+ *   max_device_bytes  cap on the plan's device memory                     */
+typedef struct {
+    int block_size;
+    int fft_min_degree;
+    int q_chunk;
+    int reserved0;
+    size_t max_device_bytes;
+} IcmGb300Config;
+
+/* Set the process-wide engine configuration used by plans created
+ * afterwards (NULL restores the defaults).  Returns 0. */
+int icm_gb300_set_config(const IcmGb300Config *cfg);
+
+/* Batched tournaments: T independent tournaments of uneven size.
+ *   n[t], k[t]        players and paid places of tournament t
+ *   S, payout         concatenated stacks (sum n) and payouts (sum k)
+ *   equity            concatenated output (sum n)
+ * All tournaments share Q.  Returns 0 / -1. */
+int icm_gpu_equity_batched(int T, const int *n, const int *k,
+                           const double *S, const double *payout, int Q,
+                           double *equity, IcmGpuRunStats *stats);
+
+/* Measured peak of this GPU's FP64 pipe: a register-resident DFMA loop over
+ * all SMs, in GFLOP/s (2 flops per DFMA).  Returns 1 / 0. */
+int icm_gpu_measure_fp64_gflops(double *gflops_out);
+
+/* Number of kernels the last equity call launched (for benchmarks). */
+long icm_gpu_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ICM_GB300_H */

@@ -1,0 +1,137 @@
+"""The drop-in boundary, checked without a GPU: the C-ABI library builds for
+sm_103a, loads, and exports every function include/*.h declares; the Python
+binding rejects bad arguments exactly as the reference's package does
+(python/tests/test_icm.py:183-208)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("icm.h", "icm_gpu.h", "icm_gb300.h")]
+
+
+def declared_functions():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"typedef[^;]*;", "", text, flags=re.S)
+        for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text):
+            name = m.group(1)
+            if name.startswith("icm_"):
+                names.add(name)
+    return names
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from icm_gb300 import build
+    path = build.build()
+    return ctypes.CDLL(path)
+
+
+def test_headers_declare_the_reference_api():
+    names = declared_functions()
+    # every entry point of the reference's src/cpu/icm.h and src/gpu/icm_gpu.h
+    ref = {"icm_equity", "icm_equity_subset", "icm_init", "icm_tree_ctx_create", "icm_hybrid_ctx_create",
+           "icm_linear_ctx_create", "icm_ctx_destroy", "icm_engine_tree", "icm_engine_hybrid",
+           "icm_engine_linear", "icm_run_engine", "icm_run_linear_batched", "icm_select_engine",
+           "icm_select_best_B", "icm_v1_exact", "icm_v2_exact", "icm_gpu_init", "icm_gpu_shutdown",
+           "icm_gpu_last_error", "icm_gpu_release_pooled_memory", "icm_gpu_plan_create",
+           "icm_gpu_plan_destroy", "icm_gpu_plan_summary", "icm_gpu_equity_with_plan", "icm_gpu_equity",
+           "icm_gpu_equity_subset", "icm_gpu_measure_hbm_bandwidth_gbps", "icm_gpu_measure_fused_pair_ns",
+           "icm_gpu_measure_fused_r2c_pair_ns"}
+    assert ref <= names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    missing = [n for n in sorted(declared_functions()) if not hasattr(built_lib, n)]
+    assert not missing, missing
+
+
+def test_python_signatures_cover_the_headers():
+    from icm_gb300._lib import SIGNATURES
+    engine_api = {"icm_tree_ctx_create", "icm_hybrid_ctx_create", "icm_linear_ctx_create", "icm_ctx_destroy",
+                  "icm_engine_tree", "icm_engine_hybrid", "icm_engine_linear", "icm_run_engine",
+                  "icm_run_linear_batched"}
+    assert declared_functions() - engine_api <= set(SIGNATURES)
+
+
+def test_struct_layouts_match_reference_sizes():
+    from icm_gb300._lib import IcmGpuOptions, IcmGpuPlanSummary, IcmGpuRunStats
+    assert ctypes.sizeof(IcmGpuOptions) == 9 * 4
+    assert ctypes.sizeof(IcmGpuRunStats) == 8 * 8 + 8 + 4 * 4
+    assert ctypes.sizeof(IcmGpuPlanSummary) == 9 * 4 + 4 + 8
+
+
+def test_closed_forms_on_host(built_lib):
+    """icm_v1_exact / icm_v2_exact run on the host and need no GPU."""
+    import icm_gb300._lib as L
+    lib = L.lib()
+    rng = np.random.default_rng(0)
+    S = 1 + 99 * rng.random(30)
+    v1 = np.zeros(30)
+    v2 = np.zeros(30)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.icm_v1_exact(30, S.ctypes.data_as(dp), v1.ctypes.data_as(dp))
+    lib.icm_v2_exact(30, S.ctypes.data_as(dp), v2.ctypes.data_as(dp))
+    ref1 = np.array([1 + sum(S[i] / (S[i] + S[j]) for j in range(30) if j != i) for i in range(30)])
+    assert np.allclose(v1, ref1, rtol=1e-14)
+    # sum over players of V2 equals the total quadratic payout sum_m C(n-1-m, 2)
+    assert abs(v2.sum() - sum((30 - 1 - m) * (30 - 2 - m) / 2 for m in range(30))) < 1e-9
+
+
+class TestInputValidation:
+    """Same checks and messages as the reference binding."""
+
+    def test_empty_stacks(self):
+        import icm_gb300 as icm
+        with pytest.raises(ValueError, match="must not be empty"):
+            icm.equity([], [0.5, 0.3, 0.2])
+
+    def test_empty_payouts(self):
+        import icm_gb300 as icm
+        with pytest.raises(ValueError, match="must not be empty"):
+            icm.equity([1000, 2000], [])
+
+    def test_k_greater_than_n(self):
+        import icm_gb300 as icm
+        with pytest.raises(ValueError, match="k=3 must satisfy 1 <= k <= n=2"):
+            icm.equity([1000, 2000], [0.5, 0.3, 0.2])
+
+    def test_invalid_target_index(self):
+        import icm_gb300 as icm
+        with pytest.raises(ValueError, match="target indices"):
+            icm.equity_subset([1000, 2000, 3000], [0.5, 0.3], targets=[5])
+
+    def test_negative_target_index(self):
+        import icm_gb300 as icm
+        with pytest.raises(ValueError, match="target indices"):
+            icm.equity_subset([1000, 2000, 3000], [0.5, 0.3], targets=[-1])
+
+    def test_invalid_Q(self):
+        import icm_gb300 as icm
+        with pytest.raises(ValueError, match="Q must be positive"):
+            icm.equity([1000, 2000, 3000], [0.5, 0.3, 0.2], Q=0)
+
+    def test_two_dimensional_stacks(self):
+        import icm_gb300 as icm
+        with pytest.raises(ValueError, match="1-D"):
+            icm.equity([[1.0, 2.0]], [1.0])
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    """No silent CPU fallback: a missing library raises ICMError."""
+    import importlib
+    import icm_gb300._lib as L
+    monkeypatch.setenv("ICM_GB300_LIB", str(tmp_path / "absent.so"))
+    monkeypatch.setattr(L, "_lib", None)
+    with pytest.raises(L.ICMError):
+        L.lib()
+    monkeypatch.delenv("ICM_GB300_LIB")
+    monkeypatch.setattr(L, "_lib", None)
+    importlib.reload(L)

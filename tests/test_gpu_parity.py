@@ -1,0 +1,184 @@
+"""Parity of the GB300 engine (through the C ABI) with the oracle, the
+reference's golden vectors, the reference library's outputs and the exact
+closed forms.  Tolerances: 1e-8 relative against the reference (its own
+GPU-vs-CPU gate, bench/bench_gpu.cu:157) and 1e-9 against the closed forms,
+as the engine's accuracy target states; tighter where the case allows."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN, max_rel
+from tests.golden.webgen import all_cases
+from tests.test_oracle import _regen
+from icm_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+WEB = json.load(open(os.path.join(GOLDEN, "web_reference.json")))
+REFW = json.load(open(os.path.join(GOLDEN, "ref_workloads.json")))
+CLOSED = json.load(open(os.path.join(GOLDEN, "closed_form.json")))
+WEB_INPUTS = {name: (n, k, Q, S, P) for name, n, k, Q, S, P in all_cases()}
+
+TOL_REF = 1e-8
+TOL_EXACT = 1e-9
+
+
+@pytest.fixture(autouse=True)
+def default_config(gpu_icm):
+    gpu_icm.configure()
+    yield
+    gpu_icm.configure()
+
+
+@pytest.mark.parametrize("case", WEB["cases"], ids=lambda c: c["name"])
+def test_reference_golden_vectors(gpu_icm, case):
+    n, k, Q, S, P = WEB_INPUTS[case["name"]]
+    E = gpu_icm.equity(S, P, Q=Q)
+    idx = np.array(case["idx"])
+    assert max_rel(E[idx], case["equity"]) < TOL_REF
+
+
+@pytest.mark.parametrize("case", REFW["cases"], ids=lambda c: c["name"])
+def test_reference_library_workloads(gpu_icm, case):
+    S, P = _regen(case)
+    E = gpu_icm.equity(S, P, Q=case["Q"])
+    idx = np.array(case["idx"])
+    assert max_rel(E[idx], case["equity"]) < TOL_REF
+    if "targets" in case:
+        T = case["targets"]
+        Es = gpu_icm.equity_subset(S, P, T, Q=case["Q"])
+        assert max_rel(Es[T], case["subset_equity"]) < TOL_REF
+        assert np.count_nonzero(np.delete(Es, T)) == 0
+
+
+def test_dropin_full_size_against_closed_form(gpu_icm):
+    """n = k = 65536, stacks log-uniform over [1, 1e9], payout (k-j+1)^2:
+    the 64 subset targets against E = 2 V2 + 3 V1 - 2 (exact)."""
+    S, P, T = W.dropin()
+    assert list(T) == CLOSED["targets"]
+    Es = gpu_icm.equity_subset(S, P, T)
+    assert max_rel(Es[T], CLOSED["equity"]) < TOL_EXACT
+    E = gpu_icm.equity(S, P)
+    assert max_rel(E[T], CLOSED["equity"]) < TOL_EXACT
+    assert max_rel(E[T], Es[T]) < 1e-12
+    assert abs(E.sum() - 1.0) < 1e-9
+
+
+def _stacks(rng, n, dist):
+    if dist == "uniform":
+        return 1 + 99 * rng.random(n)
+    if dist == "loguniform":
+        return 10.0 ** (9 * rng.random(n))
+    if dist == "equal":
+        return np.full(n, 100.0)
+    if dist == "adversarial":
+        S = np.ones(n)
+        S[0] = 1e4
+        return S
+    S = np.ones(n)        # adv_1e9 (bench/bench.c:83-86)
+    S[0] = 1e9
+    return S
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 7, 8, 9, 16, 17, 33, 100, 257, 1000, 3001])
+@pytest.mark.parametrize("dist", ["uniform", "loguniform", "equal", "adversarial"])
+def test_against_oracle_shapes(gpu_icm, oracle, n, dist):
+    rng = np.random.default_rng(n * 7 + len(dist))
+    S = _stacks(rng, n, dist)
+    for k in sorted({1, min(3, n), max(1, n // 2), n}):
+        P = np.sort(rng.random(k))[::-1] + 0.01
+        E = gpu_icm.equity(S, P, Q=128)
+        R = oracle.equity(S, P, Q=128, B=8, fft_min_deg=64)
+        assert max_rel(E, R, floor=1e-300) < 1e-9, (n, k, dist)
+
+
+@pytest.mark.parametrize("B", [4, 8, 16, 32])
+@pytest.mark.parametrize("fft_min", [4, 16, 64, 1 << 20])
+def test_block_size_and_fft_crossover(gpu_icm, oracle, B, fft_min):
+    """Every tree level forced through the FFT path, or through schoolbook."""
+    gpu_icm.configure(block_size=B, fft_min_degree=fft_min)
+    rng = np.random.default_rng(B + fft_min)
+    S = 1 + 999 * rng.random(1500)
+    for k in (1500, 200, 5):
+        P = (k - np.arange(k)).astype(float)
+        E = gpu_icm.equity(S, P, Q=64)
+        R = oracle.equity(S, P, Q=64, B=B)
+        assert max_rel(E, R) < 1e-10, (B, fft_min, k)
+
+
+@pytest.mark.parametrize("n,dist", [(64, "uniform"), (256, "adversarial"), (1024, "uniform"),
+                                    (4096, "adversarial"), (16384, "uniform"), (256, "adv_1e9")])
+def test_closed_form_v1(gpu_icm, oracle, n, dist):
+    """payout[m] = n - m, k = n: equity = V1 (reference bench/bench.c:699-723)."""
+    S = _stacks(np.random.default_rng(42), n, dist)
+    P = (n - np.arange(n)).astype(float)
+    E = gpu_icm.equity(S, P)
+    tol = 1e-9 if dist == "adv_1e9" else 5e-12
+    assert max_rel(E, oracle.v1(S)) < tol
+
+
+def test_closed_form_v2(gpu_icm, oracle):
+    """payout C(n-1-m, 2): equity = V2 (reference bench/bench.c:769-798)."""
+    n = 200
+    S = 1 + 99 * np.random.default_rng(5).random(n)
+    r = n - 1 - np.arange(n)
+    P = np.where(r >= 2, r * (r - 1) / 2.0, 0.0)
+    assert max_rel(gpu_icm.equity(S, P), oracle.v2(S)) < 5e-12
+
+
+def test_properties(gpu_icm):
+    """Reference python/tests/test_icm.py: sums, symmetry, k = 1 closed form."""
+    eq = gpu_icm.equity([1000, 1000, 1000], [0.5, 0.3, 0.2])
+    assert max_rel(eq, np.full(3, 1 / 3)) < 1e-12
+    S = np.array([100.0 * (i + 1) for i in range(10)])
+    assert max_rel(gpu_icm.equity(S, [1.0]), S / S.sum()) < 1e-10
+    S = 10.0 ** (6 * np.random.default_rng(1).random(5000))
+    P = W.geometric_payout(700, 0.9)
+    assert abs(gpu_icm.equity(S, P).sum() - 1.0) < 1e-9
+    eq = gpu_icm.equity([500, 1000, 1500, 2000, 5000], [0.40, 0.25, 0.18, 0.10, 0.07])
+    assert np.all(np.diff(eq) > 0)
+
+
+def test_subset(gpu_icm, oracle):
+    S, P = W.plain_small()
+    T = [0, 7, 42, 100, 255, 500, 777, 900, 999, 1023]
+    full = gpu_icm.equity(S, P)
+    sub = gpu_icm.equity_subset(S, P, T)
+    assert max_rel(sub[T], full[T]) < 1e-13
+    assert np.count_nonzero(np.delete(sub, T)) == 0
+    sub2 = gpu_icm.gpu_equity_subset(S, P, [3])
+    assert max_rel(sub2[[3]], full[[3]]) < 1e-13
+
+
+def test_plan_reuse_and_stats(gpu_icm):
+    S, P, _ = W.dropin(n=5000)
+    plan = gpu_icm.GpuPlan(S, len(P))
+    a, st = plan.equity(P, return_stats=True)
+    b = plan.equity(P * 2.0)
+    assert max_rel(b, 2.0 * a) < 1e-14
+    assert st["total_ns"] > 0 and st["engine"] == 1
+    s = plan.summary()
+    assert s["n"] == 5000 and s["n_levels"] >= 2
+    plan.close()
+    assert max_rel(gpu_icm.equity(S, P), a) < 1e-14
+
+
+def test_batched_matches_single(gpu_icm):
+    ts = W.batched(count=12, n_hi=2000)
+    res = gpu_icm.equity_batched(ts)
+    for (S, P), E in zip(ts, res):
+        assert max_rel(E, gpu_icm.equity(S, P)) < 1e-13
+
+
+def test_deterministic_repeat(gpu_icm):
+    S, P, _ = W.dropin(n=20000)
+    a = gpu_icm.equity(S, P)
+    b = gpu_icm.equity(S, P)
+    assert np.array_equal(a, b)
+
+
+def test_probes(gpu_icm):
+    assert gpu_icm.measure_fp64_gflops() > 100.0
+    assert gpu_icm.measure_hbm_gbps() > 1000.0
