@@ -1,0 +1,319 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 ICM quadrature engine.
+
+One step = one full quadrature solve (Q = 256 nodes) of the drop-in workload:
+n = k = 65536 players, stacks log-uniform over [1, 1e9], quadratic payouts
+(k-j+1)^2 normalised, FP64.  Prints one JSON line:
+
+  value     ms per solve, CUDA-event time of the kernel sequence with the
+            plan (sorted stacks, buffers) resident on the device
+  e2e       ms per solve through icm_equity (the reference's C entry point):
+            host stacks and payouts in, host equities out, plan set-up,
+            copies and synchronisation inside the timed region
+  roofline  dominant kernel: algorithmic FP64 flops per launch / its mean
+            CUDA-event duration over the timed region, against the FP64
+            peak measured on this GPU by a DFMA microbenchmark
+  cpu_baseline  the CPU oracle (this project's C port of the reference
+            engine) on the host cores, a bounded sample of the same
+            workload, scaled to one full solve
+
+--impl reference times the reference's own CPU implementation instead
+(oracle/_ref when it was compiled on this host, else the C port), with all
+host threads, on the same workload and metric.
+
+Multi-GPU (torchrun, N ranks): each rank solves its own copy (replicas; the
+solve does not shard across GPUs), times are maxed over ranks and the whole
+job's ms per solve is the max time / (K * N).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms @n=k=65536 Q=256"
+UNIT = "ms/solve"
+WORKLOAD = "drop-in: one tournament n=k=65536, Q=256, stacks log-uniform [1,1e9], payout (k-j+1)^2 normalised"
+B200_PUBLISHED_MS = 20.26   # reference RESULTS.md:551, B200, n=k=65536, Q=256 (uniform [1,100] stacks)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=65536)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for nm, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def cpu_port_time(S, P, threads, q_sample):
+    """Seconds per full Q=256 solve of the C port, from a q_sample-node run."""
+    from oracle.oracle import Oracle, build
+    build()
+    orc = Oracle()
+    orc.equity(S[:4096], P[:512], Q=4, B=8, fft_min_deg=64, threads=threads)   # warm caches
+    t0 = time.perf_counter()
+    orc.equity(S, P, Q=q_sample, B=8, fft_min_deg=64, threads=threads)
+    dt = time.perf_counter() - t0
+    return dt * 256.0 / q_sample
+
+
+def run_reference(args):
+    """The reference's own CPU implementation, all host threads."""
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from icm_gb300 import workloads as W
+    S, P, _ = W.dropin(n=args.n)
+    threads = os.cpu_count() or 1
+    # a full 256-node solve per step when it fits the time box (it does at
+    # n = 65536: seconds on the host cores); a node sample above that
+    q_sample = 256 if args.n <= 65536 else 2 * threads
+    kind, fn = "port", None
+    try:
+        from oracle.oracle import ReferenceLib
+        if ReferenceLib.available(openmp=True):
+            os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+            ref = ReferenceLib(openmp=True)
+            kind = "reference"
+
+            def fn():
+                t0 = time.perf_counter()
+                ref.equity(S, P, Q=q_sample)
+                return (time.perf_counter() - t0) * 256.0 / q_sample
+    except OSError:
+        fn = None
+    if fn is None:
+        def fn():
+            return cpu_port_time(S, P, threads, q_sample)
+    for _ in range(max(args.warmup, 0)):
+        fn()
+    times = [fn() for _ in range(args.steps)]
+    ms = 1e3 * float(np.mean(times))
+    sample = (f"one full solve per step (all 256 nodes, n=k={args.n})" if q_sample == 256 else
+              f"{q_sample} of the 256 quadrature nodes per step (full n=k={args.n} tree each), "
+              f"time scaled by 256/{q_sample}")
+    line = {"metric": METRIC, "value": ms, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded splitmix64)",
+            "config": {"workload": WORKLOAD, "n": args.n, "k": args.n, "Q": 256},
+            "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_info()
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    from icm_gb300 import build as b
+    b.build()
+    import ctypes
+    import icm_gb300 as icm
+    from icm_gb300 import workloads as W
+    from icm_gb300._lib import lib
+
+    L = lib()
+    if L.icm_gpu_init(local) != 1:
+        raise SystemExit(f"icm_gpu_init({local}) failed: {L.icm_gpu_last_error().decode()}")
+    icm.init()
+    S, P, T = W.dropin(n=args.n)
+    n, k = len(S), len(P)
+    fp64_peak_gflops = icm.measure_fp64_gflops()
+
+    plan = icm.GpuPlan(S, k)
+    summ = plan.summary()
+    for _ in range(max(args.warmup, 3)):
+        plan.equity(P)
+    L.icm_gb300_plan_set_profiling(plan._p, 1)
+
+    barrier()
+    dev_ms = []
+    launches = 0
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            plan.equity(P)
+            dev_ms.append(L.icm_gb300_plan_device_ms(plan._p))
+            launches += icm.last_launch_count()
+        wall = time.perf_counter() - t0
+    barrier()
+    clocks = clk.summary()
+
+    # per-kernel table from the profiled timed region
+    kst = []
+    cnt = L.icm_gb300_plan_kernel_stats(plan._p, -1, None, 0, None, None, None)
+    for i in range(cnt):
+        nm = ctypes.create_string_buffer(64)
+        ms, nl, fl = ctypes.c_double(), ctypes.c_long(), ctypes.c_double()
+        L.icm_gb300_plan_kernel_stats(plan._p, i, nm, 64, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(fl))
+        kst.append({"kernel": nm.value.decode(), "ms": ms.value, "launches": nl.value, "flops": fl.value})
+    kst.sort(key=lambda r: -r["ms"])
+    plan.close()
+
+    # end to end through icm_equity (host buffers, plan set-up inside)
+    e2e = []
+    for _ in range(2):
+        icm.equity(S, P)
+    barrier()
+    for _ in range(max(1, args.steps // 2)):
+        t1 = time.perf_counter()
+        icm.equity(S, P)
+        e2e.append(time.perf_counter() - t1)
+    barrier()
+
+    total_dev = float(np.sum(dev_ms))
+    if pg:
+        import torch
+        t = torch.tensor([total_dev, float(np.mean(e2e))], device=f"cuda:{local}", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_dev, e2e_mean = float(t[0]), float(t[1])
+    else:
+        e2e_mean = float(np.mean(e2e))
+    if rank != 0:
+        return
+    ms_per_solve = total_dev / (args.steps * world)
+    top = kst[0] if kst else None
+    roofline = None
+    if top:
+        per_launch_s = top["ms"] / top["launches"] * 1e-3
+        ach = top["flops"] / top["launches"] / per_launch_s / 1e12
+        peak = fp64_peak_gflops / 1e3
+        roofline = {"bound": "fp64", "kernel": top["kernel"], "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                    "frac": ach / peak,
+                    "peak_source": "measured on this GPU (register-resident DFMA loop); MEASURED_PEAKS.json has no FP64 figure",
+                    "traffic": traffic_for(top["kernel"]),
+                    "share_of_device_time": top["ms"] / total_dev}
+    total_flops = sum(r["flops"] for r in kst) / args.steps
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        q_sample = 256 if n <= 65536 else 2 * threads
+        secs = cpu_port_time(S, P, threads, q_sample)
+        cpu = {"value": secs * 1e3, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": (f"one full solve (256 nodes, n=k={n}) on {threads} threads" if q_sample == 256 else
+                          f"{q_sample} of 256 quadrature nodes (full n=k={n} tree each) on {threads} threads, "
+                          f"scaled by 256/{q_sample}")}
+    line = {
+        "metric": METRIC, "value": ms_per_solve, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": total_dev / args.steps, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": ms_per_solve / B200_PUBLISHED_MS, "dtype": "f64",
+        "data": "synthetic (seeded splitmix64; the reference publishes no dataset)",
+        "config": {"workload": WORKLOAD, "n": n, "k": k, "Q": 256, "B": summ["B"], "levels": summ["n_levels"],
+                   "q_chunk": summ["q_batch"], "device_bytes": summ["planned_peak_vram_bytes"],
+                   "l2": "inputs larger than L2: the plan's working set exceeds 129 MB",
+                   "parallelism": f"replicas x{world}",
+                   "vs_baseline_note": "B200 reference, uniform [1,100] stacks (RESULTS.md:551); run time does not depend on stack values"},
+        "e2e": {"value": e2e_mean * 1e3, "unit": UNIT, "h2d_bytes_per_step": 8 * (n + k), "d2h_bytes_per_step": 8 * n,
+                "path": "icm_equity (C ABI, host buffers)"},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "algorithmic_tflops_per_s": total_flops / (ms_per_solve * 1e-3) / 1e12,
+        "fp64_peak_tflops_measured": fp64_peak_gflops / 1e3,
+        "kernels": [{**r, "ms_per_solve": r["ms"] / args.steps} for r in kst[:8]],
+        "cpu_baseline": cpu, "clocks": clocks, "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def traffic_for(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/traffic.txt: '<kernel> <bytes_per_launch> <workload note>'),
+    or None when no capture covers it."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.isfile(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+if __name__ == "__main__":
+    main()

@@ -75,6 +75,10 @@ SIGNATURES = {
                                               ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gpu_measure_fp64_gflops": (ctypes.c_int, [_dp]),
     "icm_gpu_last_launch_count": (ctypes.c_long, []),
+    "icm_gb300_plan_set_profiling": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "icm_gb300_plan_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _dp,
+                                                   ctypes.POINTER(ctypes.c_long), _dp]),
+    "icm_gb300_plan_device_ms": (ctypes.c_double, [_vp]),
 }
 
 _lib = None

@@ -316,4 +316,31 @@ int icm_gpu_measure_fp64_gflops(double *gflops_out) {
 
 long icm_gpu_last_launch_count(void) { return t_launches; }
 
+int icm_gb300_plan_set_profiling(IcmGpuPlan *plan, int enable) {
+    Plan *p = reinterpret_cast<Plan *>(plan);
+    if (!p) return -1;
+    p->prof.on = enable != 0;
+    p->kstats.clear();
+    return 0;
+}
+
+int icm_gb300_plan_kernel_stats(const IcmGpuPlan *plan, int i, char *name, int name_len, double *ms,
+                                long *launches, double *flops) {
+    const Plan *p = reinterpret_cast<const Plan *>(plan);
+    if (!p) return -1;
+    const int cnt = (int)p->kstats.size();
+    if (i < 0 || i >= cnt) return cnt;
+    const Plan::KStat &k = p->kstats[i];
+    if (name && name_len > 0) snprintf(name, (size_t)name_len, "%s", k.name.c_str());
+    if (ms) *ms = k.ms;
+    if (launches) *launches = k.launches;
+    if (flops) *flops = k.flops;
+    return cnt;
+}
+
+double icm_gb300_plan_device_ms(const IcmGpuPlan *plan) {
+    const Plan *p = reinterpret_cast<const Plan *>(plan);
+    return p ? p->last_device_ms : -1.0;
+}
+
 }  // extern "C"

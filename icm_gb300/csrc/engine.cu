@@ -288,6 +288,9 @@ void plan_destroy(Plan *p) {
     if (p->graph) cudaGraphExecDestroy(p->graph);
     if (p->d_node) cudaFree(p->d_node);
     if (p->arena) cudaFree(p->arena);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    for (cudaEvent_t ev : p->prof.pool) cudaEventDestroy(ev);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -331,20 +334,21 @@ static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, boo
     cudaStream_t st = p->stream;
     const int L = p->L;
     Level *lv = p->lv;
+    Prof *pr = &p->prof;
     launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, lv[0].P, lv[0].pst,
-                lv[0].plen, st);
+                lv[0].plen, st, pr);
     ++p->launches;
     for (int l = 1; l <= L - 2; ++l) {
         if (lv[l].fft) {
-            launch_fft_build(lv[l - 1], lv[l], nq, p->d_fa, p->d_fb, p->d_fc, false, tw, logTW, st, &p->launches);
-            if (lv[l - 1].nreal & 1) { launch_school_build(lv[l - 1], lv[l], nq, lv[l].npairs, st); ++p->launches; }
+            launch_fft_build(lv[l - 1], lv[l], nq, p->d_fa, p->d_fb, p->d_fc, false, tw, logTW, st, &p->launches, pr);
+            if (lv[l - 1].nreal & 1) { launch_school_build(lv[l - 1], lv[l], nq, lv[l].npairs, st, pr); ++p->launches; }
         } else {
-            launch_school_build(lv[l - 1], lv[l], nq, 0, st);
+            launch_school_build(lv[l - 1], lv[l], nq, 0, st, pr);
             ++p->launches;
         }
     }
     if (L >= 2 && lv[L - 1].fft)
-        launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches);
+        launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches, pr);
     for (int l = L - 1; l >= 1; --l) {
         const bool root = (l == L - 1);
         const double *gp = root ? p->d_payout : lv[l].g;
@@ -354,13 +358,13 @@ static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, boo
         const uint8_t *hot_c = p->subset ? p->d_hot + p->hot_off[l - 1] : nullptr;
         if (lv[l].fft) {
             launch_fft_prop(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nq, hot_c, p->d_fa, p->d_fb, p->d_fc, tw, logTW,
-                            st, &p->launches);
+                            st, &p->launches, pr);
             if (lv[l - 1].nreal & 1) {
-                launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 2 * lv[l].npairs, st);
+                launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 2 * lv[l].npairs, st, pr);
                 ++p->launches;
             }
         } else {
-            launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 0, st);
+            launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 0, st, pr);
             ++p->launches;
         }
     }
@@ -368,8 +372,8 @@ static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, boo
     const size_t g0_q = (L == 1) ? 0 : lv[0].g_q;
     const int gst0 = (L == 1) ? 0 : lv[0].gst;
     launch_divide(p->B, p->n, p->k, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, g0, g0_q, gst0,
-                  p->subset ? p->d_active : nullptr, p->d_contrib, st);
-    launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, first ? 1 : 0, st);
+                  p->subset ? p->d_active : nullptr, p->d_contrib, st, pr);
+    launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, first ? 1 : 0, st, pr);
     p->launches += 2;
 }
 
@@ -410,17 +414,40 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         e = cudaMemsetAsync(p->d_acc, 0, sizeof(double) * p->n, p->stream);
         if (e != cudaSuccess) { err = cudaGetErrorString(e); return -1; }
     }
+    if (!p->ev0) { cudaEventCreate(&p->ev0); cudaEventCreate(&p->ev1); }
+    p->prof.used = 0;
+    p->prof.recs.clear();
+    cudaEventRecord(p->ev0, p->stream);
     for (int q0 = 0; q0 < nact; q0 += p->qc) {
         const int nq = std::min(p->qc, nact - q0);
         run_chunk(p, q0, nq, tw, logTW, q0 == 0);
     }
     launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
     ++p->launches;
+    cudaEventRecord(p->ev1, p->stream);
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(equity, p->d_out, sizeof(double) * p->n, cudaMemcpyDeviceToHost, p->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) { err = std::string("execution: ") + cudaGetErrorString(e); return -1; }
+    {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        p->last_device_ms = ms;
+    }
+    if (p->prof.on) {
+        for (const ProfRec &r : p->prof.recs) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, r.a, r.b);
+            Plan::KStat *ks = nullptr;
+            for (auto &x : p->kstats)
+                if (x.name == r.name) ks = &x;
+            if (!ks) { p->kstats.push_back({r.name, 0.0, 0, 0.0}); ks = &p->kstats.back(); }
+            ks->ms += ms;
+            ks->launches += 1;
+            ks->flops += r.flops;
+        }
+    }
     const double t1 = now_ns();
     if (stats) {
         memset(stats, 0, sizeof(*stats));

@@ -15,6 +15,7 @@
 #include "../../include/icm.h"
 #include "../../include/icm_gb300.h"
 #include "../../include/icm_gpu.h"
+#include "kernels.h"
 
 namespace icmg {
 
@@ -78,6 +79,18 @@ struct Plan {
     cudaGraphExec_t graph = nullptr;
     int graph_nq = -1;
     double peak_bytes = 0;
+    // timing: events around the kernel sequence of each run, optional
+    // per-kernel events (prof.on) aggregated by kernel name
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_device_ms = 0.0;
+    Prof prof;
+    struct KStat {
+        std::string name;
+        double ms;
+        long launches;
+        double flops;
+    };
+    std::vector<KStat> kstats;
 };
 
 // lifecycle (engine.cu)

@@ -248,7 +248,7 @@ __global__ void k_fft4_rows(const double2 *__restrict__ in, double2 *__restrict_
 }
 
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
-                cudaStream_t st, long *launches) {
+                cudaStream_t st, long *launches, Prof *pr) {
     if (batch <= 0) return 0;
     const int M = 1 << logM;
     const int threads = 256;
@@ -256,17 +256,19 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
         const int cb = (M >= 4096) ? 1 : 4096 / M;
         const long blocks = (batch + cb - 1) / cb;
         const size_t smem = (size_t)cb * M * sizeof(double2);
+        pr->begin("fft_smem", 5.0 * M * logM * (double)batch, st);
         if (sign < 0)
             k_fft_smem<-1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW);
         else
             k_fft_smem<+1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW);
+        pr->end(st);
         ++*launches;
         return 0;
     }
     if (batch > 65535) {   // grid.y limit of the four-step kernels
         for (long b0 = 0; b0 < batch; b0 += 65535)
             fft_batched(data + (b0 << logM), scratch + (b0 << logM), std::min(65535L, batch - b0), logM, sign, tw,
-                        logTW, st, launches);
+                        logTW, st, launches, pr);
         return 0;
     }
     const int logM1 = (logM + 1) / 2, logM2 = logM - logM1;
@@ -275,13 +277,14 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
     const int cbB = max(1, min(M1, 4096 / M2));
     dim3 gA(M2 / cbA, (unsigned)batch), gB(M1 / cbB, (unsigned)batch);
     const size_t smA = (size_t)cbA * M1 * sizeof(double2), smB = (size_t)cbB * M2 * sizeof(double2);
-    if (sign < 0) {
-        k_fft4_cols<-1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW);
-        k_fft4_rows<-1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW);
-    } else {
-        k_fft4_cols<+1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW);
-        k_fft4_rows<+1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW);
-    }
+    pr->begin("fft4_cols", (5.0 * logM1 + 6.0) * M * (double)batch, st);
+    if (sign < 0) k_fft4_cols<-1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW);
+    else k_fft4_cols<+1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW);
+    pr->end(st);
+    pr->begin("fft4_rows", 5.0 * logM2 * M * (double)batch, st);
+    if (sign < 0) k_fft4_rows<-1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW);
+    else k_fft4_rows<+1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW);
+    pr->end(st);
     *launches += 2;
     return 0;
 }
@@ -430,46 +433,69 @@ __global__ void k_prop_post(const double2 *__restrict__ Z, int npairs, int N, do
 static inline unsigned nblk(long work, int threads) { return (unsigned)((work + threads - 1) / threads); }
 
 void launch_leaf(int B, int n, int nblocks, const double *S, const double *node, int q0, int nq, double *a,
-                 double *blockP, double *P0, int pst0, int plen0, cudaStream_t st) {
+                 double *blockP, double *P0, int pst0, int plen0, cudaStream_t st, Prof *pr) {
     dim3 g(nblk(nblocks, 128), nq);
+    {   // reference recurrence: per player bs coefficient updates (2 mul + 1 add) and P[0] *= a
+        const double full = (double)(n / B) * B * (3.0 * B + 1.0);
+        const int r = n % B;
+        pr->begin("leaf", (double)nq * (full + (double)r * (3.0 * r + 1.0)), st);
+    }
     switch (B) {
         case 4: k_leaf<4><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
         case 8: k_leaf<8><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
         case 16: k_leaf<16><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
         default: k_leaf<32><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
     }
+    pr->end(st);
 }
 
 void launch_divide(int B, int n, int k, int nblocks, const double *S, const double *node, int q0, int nq,
                    const double *a, const double *blockP, const double *g0, size_t g0_q, int gst0,
-                   const uint8_t *active, double *contrib, cudaStream_t st) {
+                   const uint8_t *active, double *contrib, cudaStream_t st, Prof *pr) {
     dim3 g(nblk(n, 128), nq);
+    {   // divide (3 flops per term) + dot (2 per term) + weight (4)
+        const int pk = std::min(B, k);
+        pr->begin("divide", (double)nq * n * (5.0 * pk + 4.0), st);
+    }
     switch (B) {
         case 4: k_divide<4><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
         case 8: k_divide<8><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
         case 16: k_divide<16><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
         default: k_divide<32><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
     }
+    pr->end(st);
 }
 
-void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStream_t st) {
+void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStream_t st, Prof *pr) {
     const long work = (long)(p.nreal - j0) * p.pst;
     if (work <= 0) return;
     dim3 g(nblk(work, 256), nq);
+    double terms = 0.0;   // multiply-adds of one full pair: sum_t (ihi - ilo + 1)
+    for (int t = 0; t < p.plen; ++t) terms += std::min(t, c.plen - 1) - std::max(0, t - (c.plen - 1)) + 1;
+    const long pairs = std::max(0, std::min(p.nreal, c.nreal / 2) - j0);
+    pr->begin("school_build", 2.0 * terms * pairs * nq, st);
     k_school_build<<<g, 256, 0, st>>>(c.P, c.P_q, c.pst, c.plen, c.nreal, p.P, p.P_q, p.pst, p.plen, p.nreal, j0);
+    pr->end(st);
 }
 
 void launch_school_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, int nq,
-                        const uint8_t *hot_c, int c0, cudaStream_t st) {
+                        const uint8_t *hot_c, int c0, cudaStream_t st, Prof *pr) {
     const long work = (long)(c.nreal - c0) * c.gst;
     if (work <= 0) return;
     dim3 g(nblk(work, 256), nq);
+    double terms = 0.0;   // per child with a sibling: sum_m min(lc, gpl - m)
+    for (int m = 0; m < c.glen; ++m) terms += std::max(0, std::min(c.plen, gpl - m));
+    const long kids = std::max(0, 2 * (c.nreal / 2) - c0);
+    pr->begin("school_prop", 2.0 * terms * kids * nq, st);
     k_school_prop<<<g, 256, 0, st>>>(gp, gp_q, gst_p, gpl, c.P, c.P_q, c.pst, c.plen, c.g, c.g_q, c.gst, c.glen,
                                      c.nreal, hot_c, c0);
+    pr->end(st);
 }
 
-void launch_accumulate(int n, int nq, const double *contrib, double *acc, int first, cudaStream_t st) {
+void launch_accumulate(int n, int nq, const double *contrib, double *acc, int first, cudaStream_t st, Prof *pr) {
+    pr->begin("accumulate", (double)n * nq, st);
     k_accumulate<<<nblk(n, 256), 256, 0, st>>>(n, nq, contrib, acc, first);
+    pr->end(st);
 }
 
 void launch_scatter(int n, const double *acc, const int *perm, const uint8_t *active, double *out,
@@ -480,39 +506,53 @@ void launch_scatter(int n, const double *acc, const int *perm, const uint8_t *ac
 // FFT build for parents [0, npairs) of level p (children c); spectra only when
 // U == nullptr (the root level, whose product is never used).
 void launch_fft_build(const Level &c, const Level &p, int nq, double2 *fa, double2 *fb, double2 *fc,
-                      bool spectra_only, const double2 *tw, int logTW, cudaStream_t st, long *launches) {
+                      bool spectra_only, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr) {
     const int N = p.fftn, npairs = p.npairs;
     if (npairs <= 0) return;
     int logN = 0;
     while ((1 << logN) < N) ++logN;
+    const double items = (double)nq * npairs;
     dim3 g1(nblk((long)npairs * N, 256), nq);
+    pr->begin("fft_pack", 0.0, st);
     k_pack_pair<<<g1, 256, 0, st>>>(c.P, c.P_q, c.pst, c.plen, npairs, N, fa);
-    fft_batched(fa, fc, (long)nq * npairs, logN, -1, tw, logTW, st, launches);
+    pr->end(st);
+    fft_batched(fa, fc, (long)nq * npairs, logN, -1, tw, logTW, st, launches, pr);
     dim3 g2(nblk((long)npairs * (N / 2), 256), nq);
+    pr->begin("build_mid", items * (N / 2) * (spectra_only ? 8.0 : 40.0), st);
     k_build_mid<<<g2, 256, 0, st>>>(fa, npairs, N, p.spec, spectra_only ? nullptr : fb, tw, logTW, logN);
+    pr->end(st);
     *launches += 2;
     if (spectra_only) return;
-    fft_batched(fb, fc, (long)nq * npairs, logN - 1, +1, tw, logTW, st, launches);
+    fft_batched(fb, fc, (long)nq * npairs, logN - 1, +1, tw, logTW, st, launches, pr);
     dim3 g3(nblk((long)npairs * p.pst, 256), nq);
+    pr->begin("build_post", items * p.plen, st);
     k_build_post<<<g3, 256, 0, st>>>(fb, npairs, N, c.P, c.P_q, c.pst, c.plen, p.P, p.P_q, p.pst, p.plen);
+    pr->end(st);
     *launches += 1;
 }
 
 void launch_fft_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
                      const uint8_t *hot_c, double2 *fa, double2 *fb, double2 *fc, const double2 *tw, int logTW,
-                     cudaStream_t st, long *launches) {
+                     cudaStream_t st, long *launches, Prof *pr) {
     const int N = p.fftn, npairs = p.npairs;
     if (npairs <= 0) return;
     int logN = 0;
     while ((1 << logN) < N) ++logN;
+    const double items = (double)nq * npairs;
     dim3 g1(nblk((long)npairs * (N / 2), 256), nq);
+    pr->begin("prop_pack", 0.0, st);
     k_prop_pack<<<g1, 256, 0, st>>>(gp, gp_q, gst_p, gpl, npairs, N, hot_c, fb);
-    fft_batched(fb, fc, (long)nq * npairs, logN - 1, -1, tw, logTW, st, launches);
+    pr->end(st);
+    fft_batched(fb, fc, (long)nq * npairs, logN - 1, -1, tw, logTW, st, launches, pr);
     dim3 g2(nblk((long)npairs * (N / 2 + 1), 256), nq);
+    pr->begin("prop_mid", items * (N / 2 + 1) * 40.0, st);
     k_prop_mid<<<g2, 256, 0, st>>>(fb, p.spec, npairs, N, fa, tw, logTW, logN);
-    fft_batched(fa, fc, (long)nq * npairs, logN, +1, tw, logTW, st, launches);
+    pr->end(st);
+    fft_batched(fa, fc, (long)nq * npairs, logN, +1, tw, logTW, st, launches, pr);
     dim3 g3(nblk((long)2 * npairs * c.gst, 256), nq);
+    pr->begin("prop_post", items * 2 * c.glen, st);
     k_prop_post<<<g3, 256, 0, st>>>(fa, npairs, N, c.g, c.g_q, c.gst, c.glen, hot_c);
+    pr->end(st);
     *launches += 3;
 }
 

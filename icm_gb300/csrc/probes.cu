@@ -145,6 +145,7 @@ extern "C" int icm_gpu_measure_fused_pair_ns(int fft_n, int batch, int quick, do
     const double2 *tw = ok ? twiddles(logN, 0, err, &logTW) : nullptr;
     if (ok && tw) {
         long launches = 0;
+        Prof prof;
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
@@ -152,14 +153,14 @@ extern "C" int icm_gpu_measure_fused_pair_ns(int fft_n, int batch, int quick, do
         std::vector<double> tb, tp;
         for (int r = 0; r < reps + 1; ++r) {
             cudaEventRecord(e0);
-            launch_fft_build(c, p, 1, fa, fb, fc, false, tw, logTW, 0, &launches);
+            launch_fft_build(c, p, 1, fa, fb, fc, false, tw, logTW, 0, &launches, &prof);
             cudaEventRecord(e1);
             cudaEventSynchronize(e1);
             float ms;
             cudaEventElapsedTime(&ms, e0, e1);
             if (r) tb.push_back(ms * 1e6 / batch);
             cudaEventRecord(e0);
-            launch_fft_prop(p.g, 0, p.gst, p.glen, c, p, 1, nullptr, fa, fb, fc, tw, logTW, 0, &launches);
+            launch_fft_prop(p.g, 0, p.gst, p.glen, c, p, 1, nullptr, fa, fb, fc, tw, logTW, 0, &launches, &prof);
             cudaEventRecord(e1);
             cudaEventSynchronize(e1);
             cudaEventElapsedTime(&ms, e0, e1);

@@ -56,6 +56,20 @@ int icm_gpu_measure_fp64_gflops(double *gflops_out);
 /* Number of kernels the last equity call launched (for benchmarks). */
 long icm_gpu_last_launch_count(void);
 
+/* Diagnostics for a plan (the analogue of the reference's instrumented
+ * IcmGpuRunStats path, without synchronising between kernels):
+ *   set_profiling   1 = bracket every kernel launch of later runs with CUDA
+ *                   events on the plan's stream (timings accumulate until
+ *                   profiling is set again)
+ *   kernel_stats    entry i of the per-kernel table: name, total ms,
+ *                   launches and algorithmic FP64 flops; returns the number
+ *                   of entries (call with i = -1 to get the count)
+ *   device_ms       CUDA-event time of the last run's kernel sequence       */
+int icm_gb300_plan_set_profiling(IcmGpuPlan *plan, int enable);
+int icm_gb300_plan_kernel_stats(const IcmGpuPlan *plan, int i, char *name, int name_len, double *ms,
+                                long *launches, double *flops);
+double icm_gb300_plan_device_ms(const IcmGpuPlan *plan);
+
 #ifdef __cplusplus
 }
 #endif
