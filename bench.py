@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--q-chunk", type=int, default=0, help="quadrature nodes per launch sequence (0 = auto)")
     return ap.parse_args()
 
 
@@ -199,6 +200,8 @@ def main():
     if L.icm_gpu_init(local) != 1:
         raise SystemExit(f"icm_gpu_init({local}) failed: {L.icm_gpu_last_error().decode()}")
     icm.init()
+    if args.q_chunk:
+        icm.configure(q_chunk=args.q_chunk)
     S, P, T = W.dropin(n=args.n)
     n, k = len(S), len(P)
     fp64_peak_gflops = icm.measure_fp64_gflops()
