@@ -79,6 +79,7 @@ SIGNATURES = {
     "icm_gb300_plan_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _dp,
                                                    ctypes.POINTER(ctypes.c_long), _dp]),
     "icm_gb300_plan_device_ms": (ctypes.c_double, [_vp]),
+    "icm_gpu_equity_noalloc": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, _dp]),
 }
 
 _lib = None

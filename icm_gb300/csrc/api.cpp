@@ -64,6 +64,10 @@ int run_full(int n, const double *S, int Q, const double *payout, int k, double 
 }
 }  // namespace
 
+namespace icmg {
+void api_set_error(const std::string &e) { set_error(e); }
+}
+
 extern "C" {
 
 // ------------------------------------------------------------ icm.h
