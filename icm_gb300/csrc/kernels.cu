@@ -290,6 +290,7 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
 }
 
 void fft_set_smem_limits() {
+    fused_set_smem_limits();
     const int mx = kSmemFftMax * (int)sizeof(double2);
     cudaFuncSetAttribute(k_fft_smem<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft_smem<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -509,6 +510,11 @@ void launch_fft_build(const Level &c, const Level &p, int nq, double2 *fa, doubl
                       bool spectra_only, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr) {
     const int N = p.fftn, npairs = p.npairs;
     if (npairs <= 0) return;
+    if (fused_ok(N)) {
+        launch_fused_build(c, p, nq, spectra_only, tw, logTW, st, pr);
+        ++*launches;
+        return;
+    }
     int logN = 0;
     while ((1 << logN) < N) ++logN;
     const double items = (double)nq * npairs;
@@ -536,6 +542,11 @@ void launch_fft_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Le
                      cudaStream_t st, long *launches, Prof *pr) {
     const int N = p.fftn, npairs = p.npairs;
     if (npairs <= 0) return;
+    if (fused_ok(N)) {
+        launch_fused_prop(gp, gp_q, gst_p, gpl, c, p, nq, hot_c, tw, logTW, st, pr);
+        ++*launches;
+        return;
+    }
     int logN = 0;
     while ((1 << logN) < N) ++logN;
     const double items = (double)nq * npairs;

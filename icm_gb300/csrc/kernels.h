@@ -43,6 +43,14 @@ struct Prof {
 };
 
 void fft_set_smem_limits();
+
+// one-kernel FFT levels (fused.cu), used when the level's real FFT size fits
+bool fused_ok(int N);
+void fused_set_smem_limits();
+void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_only, const double2 *tw, int logTW,
+                        cudaStream_t st, Prof *pr);
+void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
+                       const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
                 cudaStream_t st, long *launches, Prof *pr);
 
