@@ -217,9 +217,12 @@ def equity_batched(tournaments, Q=256, return_stats=False):
     return (res, _stats_dict(st)) if return_stats else res
 
 
-def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0):
-    """Process-wide engine settings for plans created afterwards (0 = default)."""
-    cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 0, max_device_bytes)
+def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False):
+    """Process-wide engine settings for plans created afterwards (0 = default).
+
+    coefficient_fft_only=True keeps every FFT tree level on coefficients
+    (no spectral levels), for comparison and testing."""
+    cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes)
     lib().icm_gb300_set_config(ctypes.byref(cfg))
 
 

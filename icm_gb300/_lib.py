@@ -37,7 +37,7 @@ class IcmGpuPlanSummary(ctypes.Structure):
 
 class IcmGb300Config(ctypes.Structure):
     _fields_ = [("block_size", ctypes.c_int), ("fft_min_degree", ctypes.c_int), ("q_chunk", ctypes.c_int),
-                ("reserved0", ctypes.c_int), ("max_device_bytes", ctypes.c_size_t)]
+                ("coefficient_fft_only", ctypes.c_int), ("max_device_bytes", ctypes.c_size_t)]
 
 
 _dp = ctypes.POINTER(ctypes.c_double)

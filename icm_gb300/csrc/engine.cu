@@ -139,6 +139,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     p->opts.device_id = g_device;
     p->B = select_block_size(n, k);
     p->fft_min_deg = g_config.fft_min_degree > 0 ? g_config.fft_min_degree : 64;
+    p->spectral = g_config.coefficient_fft_only != 1;
     const int B = p->B;
 
     // descending stacks, ties by original index (reference gpu_plan.cu:405-409)
@@ -171,7 +172,14 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
         if (l >= 1) {
             const Level &c = p->lv[l - 1];
             v.npairs = c.nreal / 2;
-            v.fft = (c.deg >= p->fft_min_deg) ? 1 : 0;
+            const bool can_fft = c.deg >= p->fft_min_deg;
+            // spectral when the children's and this level's products are exact
+            // (not truncated at k) and the transforms fit one CTA
+            bool spec = p->spectral && can_fft && c.deg + 1 <= k && c.deg <= kSpecMaxD;
+            if (l <= p->L - 2) spec = spec && v.deg + 1 <= k;
+            else spec = spec && v.deg <= 2L * kSpecMaxD;   // root: G of the payout
+            v.kind = spec ? 2 : (can_fft ? 1 : 0);
+            v.fft = (v.kind == 1) ? 1 : 0;
             if (v.fft) {
                 long need = std::max<long>(2L * c.plen - 2, (long)c.glen + c.plen - 1);
                 v.fftn = std::max(4, pow2_ge(need));
@@ -192,7 +200,12 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
             fa = std::max(fa, (size_t)v.npairs * v.fftn);
             fb = std::max(fb, (size_t)v.npairs * (v.fftn / 2));
         }
-        per_q += (v.P_q + v.g_q) * 8 + v.spec_q * 16 + 512;
+        if (l + 1 < p->L && p->lv[l + 1].kind == 2) {   // parent level is spectral
+            v.spec2_q = (size_t)v.nreal * (v.deg + 1);
+            v.ends_q = (size_t)v.nreal * 2;
+        }
+        if (v.kind == 2) v.G_q = (size_t)v.nreal * (v.deg / 2 + 1);
+        per_q += (v.P_q + v.g_q + v.ends_q) * 8 + (v.spec_q + v.spec2_q + v.G_q) * 16 + 1024;
     }
     per_q += ((size_t)2 * n + (size_t)p->nblocks * (B + 1)) * 8 + 1024;
     per_q += (fa * 2 + fb) * 16;
@@ -217,12 +230,18 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     const size_t o_a = take(sizeof(double) * (size_t)qc * n);
     const size_t o_bp = take(sizeof(double) * (size_t)qc * p->nblocks * (B + 1));
     const size_t o_con = take(sizeof(double) * (size_t)qc * n);
-    size_t o_P[kMaxLevels], o_g[kMaxLevels], o_spec[kMaxLevels];
+    size_t o_P[kMaxLevels], o_g[kMaxLevels], o_spec[kMaxLevels], o_s2[kMaxLevels], o_en[kMaxLevels],
+        o_G[kMaxLevels];
     for (int l = 0; l < p->L; ++l) {
         const Level &v = p->lv[l];
         o_P[l] = v.P_q ? take(sizeof(double) * (size_t)qc * v.P_q) : 0;
         o_g[l] = v.g_q ? take(sizeof(double) * (size_t)qc * v.g_q) : 0;
         o_spec[l] = v.spec_q ? take(sizeof(double2) * (size_t)qc * v.spec_q) : 0;
+        o_s2[l] = v.spec2_q ? take(sizeof(double2) * (size_t)qc * v.spec2_q) : 0;
+        o_en[l] = v.ends_q ? take(sizeof(double) * (size_t)qc * v.ends_q) : 0;
+        // the root's G (the payout's spectrum) is shared by all nodes of a chunk
+        const size_t gq = (l == p->L - 1) ? 1 : (size_t)qc;
+        o_G[l] = v.G_q ? take(sizeof(double2) * gq * v.G_q) : 0;
     }
     p->fft_work = std::max(fa, fb) * qc;
     const size_t o_fa = fa ? take(sizeof(double2) * (size_t)qc * fa) : 0;
@@ -253,6 +272,9 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
         v.P = v.P_q ? (double *)(A + o_P[l]) : nullptr;
         v.g = v.g_q ? (double *)(A + o_g[l]) : nullptr;
         v.spec = v.spec_q ? (double2 *)(A + o_spec[l]) : nullptr;
+        v.spec2 = v.spec2_q ? (double2 *)(A + o_s2[l]) : nullptr;
+        v.ends = v.ends_q ? (double *)(A + o_en[l]) : nullptr;
+        v.G = v.G_q ? (double2 *)(A + o_G[l]) : nullptr;
     }
     if (fa) {
         p->d_fa = (double2 *)(A + o_fa);
@@ -276,7 +298,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
         for (int l = 0; l < p->L; ++l) {
             const Level &v = p->lv[l];
             fprintf(stderr, "  level %2d nreal=%7d deg=%8ld plen=%7d glen=%7d %s N=%d\n", l, v.nreal, v.deg,
-                    v.plen, v.glen, v.fft ? "fft" : "school", v.fftn);
+                    v.plen, v.glen, v.kind == 2 ? "spectral" : (v.fft ? "fft" : "school"), v.fftn);
         }
     }
     return p;
@@ -338,14 +360,19 @@ static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, boo
     launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, lv[0].P, lv[0].pst,
                 lv[0].plen, st, pr);
     ++p->launches;
+    if (L >= 2 && lv[1].kind == 2) { launch_spec_init(lv[0], nq, tw, logTW, st, pr); ++p->launches; }
     for (int l = 1; l <= L - 2; ++l) {
-        if (lv[l].fft) {
+        if (lv[l].kind == 2) {
+            launch_spec_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, tw, logTW, st, pr);
+            ++p->launches;
+        } else if (lv[l].fft) {
             launch_fft_build(lv[l - 1], lv[l], nq, p->d_fa, p->d_fb, p->d_fc, false, tw, logTW, st, &p->launches, pr);
             if (lv[l - 1].nreal & 1) { launch_school_build(lv[l - 1], lv[l], nq, lv[l].npairs, st, pr); ++p->launches; }
         } else {
             launch_school_build(lv[l - 1], lv[l], nq, 0, st, pr);
             ++p->launches;
         }
+        if (lv[l].kind != 2 && lv[l + 1].kind == 2) { launch_spec_init(lv[l], nq, tw, logTW, st, pr); ++p->launches; }
     }
     if (L >= 2 && lv[L - 1].fft)
         launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches, pr);
@@ -356,7 +383,19 @@ static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, boo
         const int gst_p = root ? 0 : lv[l].gst;
         const int gpl = root ? p->k : lv[l].glen;
         const uint8_t *hot_c = p->subset ? p->d_hot + p->hot_off[l - 1] : nullptr;
-        if (lv[l].fft) {
+        if (lv[l].kind == 2) {
+            // the parent's g spectrum: the payout's at the root, converted from
+            // coefficients below a coefficient level, else left by the level above
+            if (root || lv[l + 1].kind != 2) {
+                const uint8_t *hot_p = p->subset ? p->d_hot + p->hot_off[l] : nullptr;
+                launch_gspec_init(gp, gp_q, gst_p, gpl, lv[l].nreal, lv[l], lv[l].G, root ? 0 : lv[l].G_q,
+                                  root ? 1 : nq, hot_p, tw, logTW, st, pr);
+                ++p->launches;
+            }
+            launch_spec_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l], l - 1 >= 1 && lv[l - 1].kind == 2, nq,
+                             hot_c, tw, logTW, st, pr);
+            ++p->launches;
+        } else if (lv[l].fft) {
             launch_fft_prop(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nq, hot_c, p->d_fa, p->d_fb, p->d_fc, tw, logTW,
                             st, &p->launches, pr);
             if (lv[l - 1].nreal & 1) {
@@ -406,8 +445,10 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * p->k, cudaMemcpyHostToDevice, p->stream);
     if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return -1; }
     int logNeed = 12, logTW = 0;
-    for (int l = 1; l < p->L; ++l)
+    for (int l = 1; l < p->L; ++l) {
         if (p->lv[l].fft) logNeed = std::max(logNeed, ilog2(p->lv[l].fftn));
+        if (p->lv[l].kind == 2) logNeed = std::max(logNeed, ilog2(2 * p->lv[l].deg));
+    }
     const double2 *tw = twiddles(logNeed, p->stream, err, &logTW);
     if (!tw) return -1;
     if (nact == 0) {

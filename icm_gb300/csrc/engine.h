@@ -38,6 +38,15 @@ struct Level {
     size_t P_q = 0, g_q = 0, spec_q = 0;   // per-node element counts (doubles / double2)
     double *P = nullptr, *g = nullptr;
     double2 *spec = nullptr;               // child spectra cached build -> propagate
+    // Level kind (as a parent level): 0 schoolbook, 1 FFT on coefficients,
+    // 2 spectral (nodes carried as spectra; spectral.cu).
+    int kind = 0;
+    // spectral representation of this level's nodes: spec2 = DFT_{2 deg} (deg+1
+    // bins) and end coefficients, present when the parent level is spectral;
+    // G = DFT_{deg}(g) (deg/2+1 bins), present when this level is spectral
+    size_t spec2_q = 0, ends_q = 0, G_q = 0;
+    double2 *spec2 = nullptr, *G = nullptr;
+    double *ends = nullptr;
 };
 
 struct TourDesc {          // batched mode: one tournament inside a batch plan
@@ -47,6 +56,7 @@ struct TourDesc {          // batched mode: one tournament inside a batch plan
 struct Plan {
     int n = 0, k = 0, B = 0, nblocks = 0, L = 0;
     int fft_min_deg = 64;
+    bool spectral = true;           // use spectral levels where they apply
     std::vector<double> S_sorted;
     std::vector<int> perm;          // perm[i] = original index of sorted player i
     std::vector<int> inv_perm;

@@ -95,4 +95,62 @@ __device__ void smem_fft_dit(double2 *x, int logM, int cnt, const double2 *__res
     }
 }
 
+// Decimation in frequency: natural-order input, bit-reversed output.  Two
+// radix-2 stages (half sizes 2h and h) per pass, largest first; with
+// t = w_{4h}^j the fused pass is
+//   x0 = (a + c) + (b + d)            x1 = ((a + c) - (b + d)) t^2
+//   x2 = ((a - c) -+ i (b - d)) t     x3 = ((a - c) +- i (b - d)) t^3
+// (upper signs forward).  A leading radix-2 stage handles odd log2(M).
+// Pairing a DIF inverse with a DIT forward transform lets a pointwise step
+// between them run in bit-reversed order with no permutation.
+template <int SIGN>
+__device__ void smem_fft_dif(double2 *x, int logM, int cnt, const double2 *__restrict__ tw, int logTW) {
+    const int M = 1 << logM;
+    int s = logM;   // stages left
+    if (logM & 1) {  // radix-2 stage with half size M/2
+        const int h = M >> 1;
+        const int nb = cnt << (logM - 1);
+        const int sh = logTW - logM;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            const int item = b >> (logM - 1);
+            const int j = b & (h - 1);
+            const int i = item * M + j;
+            const double2 a = x[i], bq = x[i + h];
+            x[i] = cadd(a, bq);
+            const double2 d = csub(a, bq);
+            x[i + h] = (j != 0) ? twmul<SIGN>(d, __ldg(&tw[j << sh])) : d;
+        }
+        __syncthreads();
+        s -= 1;
+    }
+    for (; s >= 2; s -= 2) {
+        const int hs = s - 2;         // log2 of h
+        const int h = 1 << hs;        // pass covers half sizes 2h and h; groups of 4h
+        const int nb = cnt << (logM - 2);
+        const int sh = logTW - hs - 2;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            const int item = b >> (logM - 2);
+            const int r = b & ((M >> 2) - 1);
+            const int j = r & (h - 1);
+            const int i = item * M + ((r >> hs) << (hs + 2)) + j;
+            const double2 a = x[i], bq = x[i + h], c = x[i + 2 * h], d = x[i + 3 * h];
+            const double2 s0 = cadd(a, c), d0 = csub(a, c);
+            const double2 s1 = cadd(bq, d), d1 = csub(bq, d);
+            double2 y1 = csub(s0, s1), y2, y3;
+            if (SIGN < 0) { y2 = cadd(d0, cmul_mi(d1)); y3 = csub(d0, cmul_mi(d1)); }
+            else { y2 = cadd(d0, cmul_pi(d1)); y3 = csub(d0, cmul_pi(d1)); }
+            x[i] = cadd(s0, s1);
+            if (j != 0) {
+                y1 = twmul<SIGN>(y1, __ldg(&tw[(2 * j) << sh]));
+                y2 = twmul<SIGN>(y2, __ldg(&tw[j << sh]));
+                y3 = twmul<SIGN>(y3, __ldg(&tw[(3 * j) << sh]));
+            }
+            x[i + h] = y1;
+            x[i + 2 * h] = y2;
+            x[i + 3 * h] = y3;
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace icmg

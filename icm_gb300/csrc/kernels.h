@@ -49,6 +49,18 @@ bool fused_ok(int N);
 void fused_set_smem_limits();
 void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_only, const double2 *tw, int logTW,
                         cudaStream_t st, Prof *pr);
+// spectral levels (spectral.cu)
+constexpr int kSpecMaxD = 8192;   // largest child degree of a spectral level
+void spec_set_smem_limits();
+void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
+void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq, const double2 *tw, int logTW,
+                       cudaStream_t st, Prof *pr);
+void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G,
+                       size_t G_q, int nq, const uint8_t *hot, const double2 *tw, int logTW, cudaStream_t st,
+                       Prof *pr);
+void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral, int nq,
+                      const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
+
 void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
                        const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,

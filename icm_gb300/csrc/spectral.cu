@@ -1,0 +1,391 @@
+// spectral.cu -- tree levels carried in the frequency domain.
+//
+// A node X of degree d (d+1 coefficients) keeps spec2(X) = DFT_{2d}(x), the
+// d+1 Hermitian bins of its spectrum at twice its degree, plus its end
+// coefficients x_0 and x_d.  For a parent X of two children of degree D
+// (d = 2D), with children spectra S_L, S_R at size 2D:
+//
+// build:  C = S_L S_R is X's spectrum at size 2D (x_{2D} folded onto x_0),
+//         i.e. the even bins of spec2(X).  One inverse transform of size D
+//         gives x (endpoints replaced by L_0 R_0 and L_D R_D); the odd bins
+//         are the half-bin transform H[f] = sum_t y_t e^{-2 pi i (2f+1) t/4D}
+//         of y = x with y_0 = x_0 - x_{2D}, one forward transform of size D
+//         of the twisted packing (y_{2s} + i y_{2s+1}) e^{-2 pi i s/2D}.
+//         Two size-D transforms per node instead of one size-2D and one
+//         size-D on the coefficient path.
+// propagate (the transpose): with G = DFT_{2D}(g_X), a child's correlation
+//         y = IDFT_{2D}(G conj S_sib) has g_child = y[0:D).  Its even bins
+//         are DFT_D(a + b), its odd bins the half-bin transform of a - b
+//         (a = y[0:D), b = y[D:2D)).  One inverse half-bin transform gives
+//         a - b; the child's g spectrum DFT_D(a) is (even bins + DFT_D(a-b))/2,
+//         or, where the level below works on coefficients, a = (IDFT_D(even
+//         bins) + (a - b))/2.  Two size-D/2 transforms per child.
+//
+// Inverses run as decimation-in-frequency (natural in, bit-reversed out) and
+// forwards as decimation-in-time (bit-reversed in, natural out), so the
+// pointwise twist between them needs no permutation.  A missing sibling
+// (ragged tree edge) is the polynomial 1: spectrum 1, ends (1, 0).
+#include "engine.h"
+#include "fft.cuh"
+#include "kernels.h"
+
+namespace icmg {
+
+constexpr int kSpecThreads = 256;
+constexpr int kSpecMaxM = kSpecMaxD;   // largest transform one CTA holds in shared memory
+
+static inline int ilog2s(long v) {
+    int l = 0;
+    while ((1L << l) < v) ++l;
+    return l;
+}
+static inline int spec_cb(int M) { return M >= 4096 ? 1 : 4096 / M; }
+static inline size_t spec_smem(int M) { return (size_t)spec_cb(M) * M * sizeof(double2); }
+
+__device__ __forceinline__ double2 twl(const double2 *__restrict__ tw, long idx) { return __ldg(&tw[idx]); }
+
+// ---------------------------------------------------------------------------
+// spec2 and ends of nodes given by coefficients: real FFT of size 2d through
+// a complex transform of size d.  cb nodes per CTA.
+__global__ void __launch_bounds__(kSpecThreads)
+k_spec_init(const double *__restrict__ P, size_t P_q, int pst, int plen, int nreal, int logd,
+            double2 *__restrict__ spec2, size_t s2_q, double *__restrict__ ends, size_t e_q,
+            const double2 *__restrict__ tw, int logTW) {
+    extern __shared__ double2 sm[];
+    const int d = 1 << logd;
+    const int cb = d >= 4096 ? 1 : 4096 / d;
+    const int q = blockIdx.y;
+    const int j0 = blockIdx.x * cb;
+    const int cnt = min(cb, nreal - j0);
+    if (cnt <= 0) return;
+    for (int e = threadIdx.x; e < cnt * d; e += blockDim.x) {
+        const int it = e >> logd, r = e & (d - 1);
+        const int s = (int)bitrev(r, logd);
+        const double *x = P + q * P_q + (size_t)(j0 + it) * pst;
+        const int t0 = 2 * s, t1 = 2 * s + 1;
+        sm[e] = make_double2(t0 < plen ? x[t0] : 0.0, t1 < plen ? x[t1] : 0.0);
+    }
+    __syncthreads();
+    smem_fft_dit<-1>(sm, logd, cnt, tw, logTW);
+    // X[f] = (Z[f] + conj Z[d-f])/2 + e^{-2 pi i f/2d} (Z[f] - conj Z[d-f])/(2i), f = 0..d
+    for (int e = threadIdx.x; e < cnt * d; e += blockDim.x) {
+        const int it = e >> logd, f = e & (d - 1);
+        const double2 *z = sm + (size_t)it * d;
+        const double2 zf = z[f], zc = z[(d - f) & (d - 1)];
+        const double2 Ev = cscale(cadd(zf, cconj(zc)), 0.5);
+        const double2 Od = cscale(cmul_mi(csub(zf, cconj(zc))), 0.5);
+        double2 *out = spec2 + q * s2_q + (size_t)(j0 + it) * (d + 1);
+        out[f] = cadd(Ev, cmul(Od, twl(tw, (long)f << (logTW - logd - 1))));
+        if (f == 0) {
+            out[d] = csub(Ev, Od);
+            const double *x = P + q * P_q + (size_t)(j0 + it) * pst;
+            double *en = ends + q * e_q + (size_t)(j0 + it) * 2;
+            en[0] = x[0];
+            en[1] = (d < plen) ? x[d] : 0.0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Build of one spectral level: nodes j of level l from children 2j, 2j+1 of
+// level l-1 (degree D = 2^logD, spec2 of D+1 bins).  Writes spec2 (2D+1 bins)
+// and ends of each node, and its coefficients when Pout != null.
+__global__ void __launch_bounds__(kSpecThreads)
+k_spec_build(const double2 *__restrict__ cspec, size_t cs_q, const double *__restrict__ cends, size_t ce_q,
+             int nreal_c, int nreal_p, int logD, double2 *__restrict__ pspec, size_t ps_q,
+             double *__restrict__ pends, size_t pe_q, double *__restrict__ Pout, size_t Po_q, int pst_p, int plen_p,
+             const double2 *__restrict__ tw, int logTW) {
+    extern __shared__ double2 sm[];
+    const int D = 1 << logD;
+    const int cb = D >= 4096 ? 1 : 4096 / D;
+    const int q = blockIdx.y;
+    const int j0 = blockIdx.x * cb;
+    const int cnt = min(cb, nreal_p - j0);
+    if (cnt <= 0) return;
+    const double one_over_2D = 1.0 / (2.0 * D);
+    // 1. product spectrum (even bins of spec2(X)) and the inverse input U
+    for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) {
+        const int it = e >> logD, f = e & (D - 1);
+        const int j = j0 + it;
+        const double2 *sL = cspec + q * cs_q + (size_t)(2 * j) * (D + 1);
+        const bool has_r = (2 * j + 1) < nreal_c;
+        const double2 *sR = sL + (D + 1);
+        const double2 one = make_double2(1.0, 0.0);
+        const double2 Cf = cmul(sL[f], has_r ? sR[f] : one);
+        const double2 Cc = cmul(sL[D - f], has_r ? sR[D - f] : one);
+        if (pspec) {
+            double2 *ps = pspec + q * ps_q + (size_t)j * (2 * D + 1);
+            ps[2 * f] = Cf;
+            if (f == 0) ps[2 * D] = Cc;
+        }
+        double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
+        if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
+        const double2 O = cmulc(Dd, twl(tw, (long)f << (logTW - logD - 1)));   // * e^{+2 pi i f/2D}
+        sm[e] = cadd(E, cmul_pi(O));
+    }
+    __syncthreads();
+    smem_fft_dif<+1>(sm, logD, cnt, tw, logTW);
+    // 2. coefficients (bit-reversed slots), endpoint fix, twist for the half-bin transform
+    for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) {
+        const int it = e >> logD, r = e & (D - 1);
+        const int s = (int)bitrev(r, logD);
+        const int j = j0 + it;
+        const double *eL = cends + q * ce_q + (size_t)(2 * j) * 2;
+        const bool has_r = (2 * j + 1) < nreal_c;
+        const double R0 = has_r ? eL[2] : 1.0, Rt = has_r ? eL[3] : 0.0;
+        const double2 u = sm[e];
+        double x0 = u.x * one_over_2D, x1 = u.y * one_over_2D;
+        const double xtop = eL[1] * Rt;
+        if (s == 0) {
+            x0 = eL[0] * R0;
+            if (pends) {
+                double *en = pends + q * pe_q + (size_t)j * 2;
+                en[0] = x0;
+                en[1] = xtop;
+            }
+        }
+        if (Pout) {
+            double *out = Pout + q * Po_q + (size_t)j * pst_p;
+            if (2 * s < plen_p) out[2 * s] = x0;
+            if (2 * s + 1 < plen_p) out[2 * s + 1] = x1;
+            if (s == 0) {
+                if (2 * D < plen_p) out[2 * D] = xtop;
+                for (int t = 2 * D + 1; t < pst_p; ++t) out[t] = 0.0;
+            }
+        }
+        const double y0 = (s == 0) ? x0 - xtop : x0;
+        sm[e] = cmul(make_double2(y0, x1), twl(tw, (long)s << (logTW - logD - 1)));   // e^{-2 pi i s/2D}
+    }
+    if (!pspec) return;   // the level above works on coefficients: no spectrum needed
+    __syncthreads();
+    smem_fft_dit<-1>(sm, logD, cnt, tw, logTW);
+    // 3. odd bins: H[f] = E'[f] + e^{-2 pi i (2f+1)/4D} O'[f]
+    for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) {
+        const int it = e >> logD, f = e & (D - 1);
+        const double2 *c = sm + (size_t)it * D;
+        const double2 a = c[f], b = cconj(c[D - 1 - f]);
+        const double2 Ep = cscale(cadd(a, b), 0.5);
+        const double2 Op = cscale(cmul_mi(csub(a, b)), 0.5);
+        double2 *ps = pspec + q * ps_q + (size_t)(j0 + it) * (2 * D + 1);
+        ps[2 * f + 1] = cadd(Ep, cmul(Op, twl(tw, (long)(2 * f + 1) << (logTW - logD - 2))));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// g spectra from g coefficients: G = DFT_d(g) (bins 0..d/2), real FFT of size
+// d through a complex transform of size d/2.  g_q == 0 and one node: the root.
+__global__ void __launch_bounds__(kSpecThreads)
+k_gspec_init(const double *__restrict__ g, size_t g_q, int gst, int glen, int nreal, int logd,
+             double2 *__restrict__ G, size_t G_q, const uint8_t *__restrict__ hot, const double2 *__restrict__ tw,
+             int logTW) {
+    extern __shared__ double2 sm[];
+    const int h = 1 << (logd - 1);
+    const int lh = logd - 1;
+    const int cb = h >= 4096 ? 1 : 4096 / h;
+    const int q = blockIdx.y;
+    const int j0 = blockIdx.x * cb;
+    const int cnt = min(cb, nreal - j0);
+    if (cnt <= 0) return;
+    for (int e = threadIdx.x; e < cnt * h; e += blockDim.x) {
+        const int it = e >> lh, r = e & (h - 1);
+        const int s = (int)bitrev(r, lh);
+        const double *x = g + q * g_q + (size_t)(j0 + it) * gst;
+        const int t0 = 2 * s, t1 = 2 * s + 1;
+        sm[e] = make_double2(t0 < glen ? x[t0] : 0.0, t1 < glen ? x[t1] : 0.0);
+    }
+    __syncthreads();
+    smem_fft_dit<-1>(sm, lh, cnt, tw, logTW);
+    for (int e = threadIdx.x; e < cnt * h; e += blockDim.x) {
+        const int it = e >> lh, f = e & (h - 1);
+        const int j = j0 + it;
+        double2 *out = G + q * G_q + (size_t)j * (h + 1);
+        if (hot && !hot[j]) {
+            out[f] = make_double2(0.0, 0.0);
+            if (f == 0) out[h] = make_double2(0.0, 0.0);
+            continue;
+        }
+        const double2 *z = sm + (size_t)it * h;
+        const double2 zf = z[f], zc = z[(h - f) & (h - 1)];
+        const double2 Ev = cscale(cadd(zf, cconj(zc)), 0.5);
+        const double2 Od = cscale(cmul_mi(csub(zf, cconj(zc))), 0.5);
+        out[f] = cadd(Ev, cmul(Od, twl(tw, (long)f << (logTW - logd))));
+        if (f == 0) out[h] = csub(Ev, Od);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Propagate of one spectral level: parent j (degree 2D, G of D+1 bins),
+// children 2j, 2j+1 (degree D = 2^logD, spec2 of D+1 bins).  Each child gets
+// its g spectrum (D/2+1 bins) when Gout != null, else its g coefficients.
+// Work per child: a transform of size D/2 (inverse half-bin), then a second
+// one (forward for the spectrum, inverse of the even bins for coefficients).
+__global__ void __launch_bounds__(kSpecThreads)
+k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restrict__ cspec, size_t cs_q, int nreal_c,
+            int npar, int logD, double2 *__restrict__ Gout, size_t Go_q, double *__restrict__ gout, size_t go_q,
+            int gst_c, int glen_c, const uint8_t *__restrict__ hot_c, const double2 *__restrict__ tw, int logTW) {
+    extern __shared__ double2 sm[];
+    const int D = 1 << logD;
+    const int h = D >> 1, lh = logD - 1;
+    const int cbp = D >= 4096 ? 1 : 4096 / D;            // parents per CTA; 2 children each
+    const int q = blockIdx.y;
+    const int j0 = blockIdx.x * cbp;
+    const int cnt = min(cbp, npar - j0);
+    if (cnt <= 0) return;
+    const int nk = 2 * cnt;                               // children handled, h slots each
+    const double2 one = make_double2(1.0, 0.0);
+    // 1. odd bins of Y = G conj(S_sib) -> inverse half-bin input C'[f]
+    for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
+        const int kk = e >> lh, f = e & (h - 1);
+        const int j = j0 + (kk >> 1), side = kk & 1;
+        const int c = 2 * j + side, sib = c ^ 1;
+        const double2 *G = Gp + q * Gp_q + (size_t)j * (D + 1);
+        const bool has_sib = sib < nreal_c;
+        const double2 *S = cspec + q * cs_q + (size_t)sib * (D + 1);
+        const int f1 = 2 * f + 1, f2 = 2 * (h - 1 - f) + 1;
+        const double2 Y1 = cmulc(G[f1], has_sib ? S[f1] : one);
+        const double2 Y2 = cconj(cmulc(G[f2], has_sib ? S[f2] : one));
+        const double2 w = twl(tw, (long)f1 << (logTW - logD - 1));     // e^{-2 pi i (2f+1)/2D}
+        const double2 Ep = cscale(cadd(Y1, Y2), 0.5);
+        const double2 Op = cscale(cmulc(csub(Y1, Y2), w), 0.5);
+        sm[e] = cadd(Ep, cmul_pi(Op));
+    }
+    __syncthreads();
+    smem_fft_dif<+1>(sm, lh, nk, tw, logTW);
+    // 2. untwist: w_s = c'_s e^{+2 pi i s/D} / (D/2) = (a-b)_{2s} + i (a-b)_{2s+1}
+    const double inv_h = 1.0 / h;
+    for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
+        const int r = e & (h - 1);
+        const int s = (int)bitrev(r, lh);
+        sm[e] = cscale(cmulc(sm[e], twl(tw, (long)s << (logTW - logD))), inv_h);
+    }
+    if (Gout) {
+        __syncthreads();
+        smem_fft_dit<-1>(sm, lh, nk, tw, logTW);
+        // 3a. G_child[f] = (Y[2f] + DFT_D(a-b)[f]) / 2, f = 0..h
+        for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
+            const int kk = e >> lh, f = e & (h - 1);
+            const int j = j0 + (kk >> 1), side = kk & 1;
+            const int c = 2 * j + side, sib = c ^ 1;
+            if (c >= nreal_c) continue;   // lone child: no right sibling node
+            double2 *out = Gout + q * Go_q + (size_t)c * (h + 1);
+            if (hot_c && !hot_c[c]) {
+                out[f] = make_double2(0.0, 0.0);
+                if (f == 0) out[h] = make_double2(0.0, 0.0);
+                continue;
+            }
+            const double2 *G = Gp + q * Gp_q + (size_t)j * (D + 1);
+            const bool has_sib = sib < nreal_c;
+            const double2 *S = cspec + q * cs_q + (size_t)sib * (D + 1);
+            const double2 *z = sm + (size_t)kk * h;
+            const double2 zf = z[f], zc = z[(h - f) & (h - 1)];
+            const double2 Ev = cscale(cadd(zf, cconj(zc)), 0.5);
+            const double2 Od = cscale(cmul_mi(csub(zf, cconj(zc))), 0.5);
+            const double2 Xf = cadd(Ev, cmul(Od, twl(tw, (long)f << (logTW - logD))));
+            const double2 Ye = cmulc(G[2 * f], has_sib ? S[2 * f] : one);
+            out[f] = cscale(cadd(Ye, Xf), 0.5);
+            if (f == 0) {
+                const double2 Xh = csub(Ev, Od);
+                const double2 Yh = cmulc(G[D], has_sib ? S[D] : one);
+                out[h] = cscale(cadd(Yh, Xh), 0.5);
+            }
+        }
+        return;
+    }
+    // 3b. coefficients: store (a-b)/2, then add IDFT_D(even bins)/2 = (a+b)/2
+    for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
+        const int kk = e >> lh, r = e & (h - 1);
+        const int s = (int)bitrev(r, lh);
+        const int c = 2 * (j0 + (kk >> 1)) + (kk & 1);
+        if (c >= nreal_c) continue;
+        double *out = gout + q * go_q + (size_t)c * gst_c;
+        const double2 v = sm[e];
+        if (2 * s < glen_c) out[2 * s] = 0.5 * v.x;
+        if (2 * s + 1 < glen_c) out[2 * s + 1] = 0.5 * v.y;
+    }
+    __syncthreads();
+    // U[f] = E + i O of the even-bin spectrum Ye (bins 0..h of a real size-D spectrum)
+    for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
+        const int kk = e >> lh, f = e & (h - 1);
+        const int j = j0 + (kk >> 1), side = kk & 1;
+        const int sib = (2 * j + side) ^ 1;
+        const double2 *G = Gp + q * Gp_q + (size_t)j * (D + 1);
+        const bool has_sib = sib < nreal_c;
+        const double2 *S = cspec + q * cs_q + (size_t)sib * (D + 1);
+        const double2 Cf = cmulc(G[2 * f], has_sib ? S[2 * f] : one);
+        const double2 Cc = cmulc(G[2 * (h - f)], has_sib ? S[2 * (h - f)] : one);
+        double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
+        if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
+        const double2 O = cmulc(Dd, twl(tw, (long)f << (logTW - logD)));      // e^{+2 pi i f/D}
+        sm[e] = cadd(E, cmul_pi(O));
+    }
+    __syncthreads();
+    smem_fft_dif<+1>(sm, lh, nk, tw, logTW);
+    const double inv_D = 1.0 / D;
+    for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
+        const int kk = e >> lh, r = e & (h - 1);
+        const int s = (int)bitrev(r, lh);
+        const int c = 2 * (j0 + (kk >> 1)) + (kk & 1);
+        if (c >= nreal_c) continue;
+        double *out = gout + q * go_q + (size_t)c * gst_c;
+        const bool cold = hot_c && !hot_c[c];
+        const double2 v = sm[e];
+        if (2 * s < gst_c) out[2 * s] = (cold || 2 * s >= glen_c) ? 0.0 : out[2 * s] + 0.5 * v.x * inv_D;
+        if (2 * s + 1 < gst_c) out[2 * s + 1] = (cold || 2 * s + 1 >= glen_c) ? 0.0 : out[2 * s + 1] + 0.5 * v.y * inv_D;
+    }
+}
+
+// ---------------------------------------------------------------------------
+void spec_set_smem_limits() {
+    const int mx = (int)spec_smem(kSpecMaxM);
+    cudaFuncSetAttribute(k_spec_init, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_spec_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_gspec_init, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cudaStream_t st, Prof *pr) {
+    const int logd = ilog2s(v.deg), d = 1 << logd;
+    const int cb = spec_cb(d);
+    dim3 g((v.nreal + cb - 1) / cb, nq);
+    pr->begin("spec_init", (5.0 * d * logd + 20.0 * d) * v.nreal * (double)nq, st);
+    k_spec_init<<<g, kSpecThreads, spec_smem(d), st>>>(v.P, v.P_q, v.pst, v.plen, v.nreal, logd, v.spec2, v.spec2_q,
+                                                       v.ends, v.ends_q, tw, logTW);
+    pr->end(st);
+}
+
+void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq, const double2 *tw, int logTW,
+                       cudaStream_t st, Prof *pr) {
+    const int logD = ilog2s(c.deg), D = 1 << logD;
+    const int cb = spec_cb(D);
+    dim3 g((p.nreal + cb - 1) / cb, nq);
+    pr->begin("spec_build", (10.0 * D * logD + 60.0 * D) * p.nreal * (double)nq, st);
+    k_spec_build<<<g, kSpecThreads, spec_smem(D), st>>>(c.spec2, c.spec2_q, c.ends, c.ends_q, c.nreal, p.nreal, logD,
+                                                        p.spec2, p.spec2_q, p.spec2 ? p.ends : nullptr, p.ends_q,
+                                                        write_coeffs ? p.P : nullptr, p.P_q, p.pst, p.plen, tw, logTW);
+    pr->end(st);
+}
+
+void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G,
+                       size_t G_q, int nq, const uint8_t *hot, const double2 *tw, int logTW, cudaStream_t st,
+                       Prof *pr) {
+    const int logd = ilog2s(v.deg), h = 1 << (logd - 1);
+    const int cb = spec_cb(h);
+    dim3 gr((nreal + cb - 1) / cb, nq);
+    pr->begin("gspec_init", (5.0 * h * (logd - 1) + 20.0 * h) * nreal * (double)nq, st);
+    k_gspec_init<<<gr, kSpecThreads, spec_smem(h), st>>>(g, g_q, gst, glen, nreal, logd, G, G_q, hot, tw, logTW);
+    pr->end(st);
+}
+
+void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral, int nq,
+                      const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr) {
+    const int logD = ilog2s(c.deg), D = 1 << logD;
+    const int cbp = spec_cb(D);
+    dim3 g((p.nreal + cbp - 1) / cbp, nq);
+    pr->begin("spec_prop", (2.0 * 2 * 5.0 * (D / 2) * (logD - 1) + 60.0 * D) * p.nreal * (double)nq, st);
+    k_spec_prop<<<g, kSpecThreads, spec_smem(D), st>>>(Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, p.nreal, logD,
+                                                       children_spectral ? c.G : nullptr, c.G_q, c.g, c.g_q, c.gst,
+                                                       c.glen, hot_c, tw, logTW);
+    pr->end(st);
+}
+
+}  // namespace icmg

@@ -27,12 +27,14 @@ int icm_last_status(void);
  *   fft_min_degree    child degree at which tree levels switch from
  *                     schoolbook to FFT products (default from the tuner)
  *   q_chunk           quadrature nodes processed per launch sequence
+ *   coefficient_fft_only  1 = keep every FFT level on coefficients (no
+ *                     spectral levels; for comparison and testing)
  *   max_device_bytes  cap on the plan's device memory                     */
 typedef struct {
     int block_size;
     int fft_min_degree;
     int q_chunk;
-    int reserved0;
+    int coefficient_fft_only;
     size_t max_device_bytes;
 } IcmGb300Config;
 

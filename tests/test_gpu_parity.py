@@ -182,3 +182,22 @@ def test_deterministic_repeat(gpu_icm):
 def test_probes(gpu_icm):
     assert gpu_icm.measure_fp64_gflops() > 100.0
     assert gpu_icm.measure_hbm_gbps() > 1000.0
+
+
+@pytest.mark.parametrize("n", [300, 1025, 4096, 20000])
+@pytest.mark.parametrize("kfrac", [1.0, 0.3, 0.01])
+def test_spectral_levels_match_coefficient_levels(gpu_icm, n, kfrac):
+    """Spectral tree levels (nodes carried as spectra) against the
+    coefficient FFT path and the oracle, ragged trees and truncated k included."""
+    rng = np.random.default_rng(n)
+    S = 10.0 ** (4 * rng.random(n))
+    k = max(1, int(kfrac * n))
+    P = np.sort(rng.random(k))[::-1] + 0.01
+    T = sorted(rng.choice(n, size=min(5, n), replace=False).tolist())
+    outs = {}
+    for coeff in (False, True):
+        gpu_icm.configure(fft_min_degree=16, coefficient_fft_only=coeff)
+        outs[coeff] = (gpu_icm.equity(S, P, Q=64), gpu_icm.equity_subset(S, P, T, Q=64))
+    assert max_rel(outs[False][0], outs[True][0]) < 1e-11
+    assert max_rel(outs[False][1][T], outs[True][0][T]) < 1e-11
+    assert np.count_nonzero(np.delete(outs[False][1], T)) == 0
