@@ -167,6 +167,12 @@ int icm_gpu_init(int device_id) {
     e = cudaSetDevice(device_id);
     if (e != cudaSuccess) { set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e)); return 0; }
     fft_set_smem_limits();
+    // keep freed plan arenas in this process's default pool for the next plan
+    cudaMemPool_t pool = nullptr;
+    if (cudaDeviceGetDefaultMemPool(&pool, device_id) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     g_device = device_id;
     return 1;
 }

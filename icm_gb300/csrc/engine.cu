@@ -44,30 +44,7 @@ void make_nodes(int Q, double Smax, std::vector<double> &logv, std::vector<doubl
 }
 
 // ------------------------------------------------------------ twiddles
-// tw[t] = exp(-2 pi i t / 2^L).  Each entry is computed in long double from
-// an angle folded into [0, pi/4] with exact integer reflections.
-static void unit_root(long t, long N, double *re, double *im) {
-    static const long double two_pi = 6.283185307179586476925286766559005768L;
-    t %= N;
-    int conj = 0, neg_c = 0;
-    if (2 * t > N) { t = N - t; conj = 1; }
-    long num = t, den = N;
-    if (4 * t > N) { num = N - 2 * t; den = 2 * N; neg_c = 1; }
-    long double c, s;
-    if (8 * num > den) {
-        const long double b = two_pi * (long double)(den - 4 * num) / (4.0L * (long double)den);
-        c = sinl(b);
-        s = cosl(b);
-    } else {
-        const long double a = two_pi * (long double)num / (long double)den;
-        c = cosl(a);
-        s = sinl(a);
-    }
-    if (neg_c) c = -c;
-    *re = (double)c;
-    *im = conj ? (double)s : (double)(-s);
-}
-
+// tables built by twiddle.cpp; one allocation per device, grown on demand
 static std::mutex g_tw_mu;
 static double2 *g_tw[64] = {};   // per device
 static int g_tw_log[64] = {};
@@ -78,15 +55,13 @@ const double2 *twiddles(int logN, cudaStream_t s, std::string &err, int *logTW) 
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) { err = "device index out of range"; return nullptr; }
     if (g_tw[dev] && g_tw_log[dev] >= logN) { *logTW = g_tw_log[dev]; return g_tw[dev]; }
-    const int L = std::max(logN, 12);
-    const long N = 1L << L;
-    std::vector<double2> h((size_t)N);
-    // first octant directly, the rest by symmetry of the table
-    for (long t = 0; t < N; ++t) unit_root(t, N, &h[(size_t)t].x, &h[(size_t)t].y);
+    const int L = std::max(logN, 14);
+    std::vector<unsigned char> h;
+    fill_twiddles(L, h);
     double2 *d = nullptr;
-    cudaError_t e = cudaMalloc(&d, sizeof(double2) * (size_t)N);
+    cudaError_t e = cudaMalloc(&d, h.size());
     if (e != cudaSuccess) { err = std::string("twiddle table: ") + cudaGetErrorString(e); return nullptr; }
-    e = cudaMemcpyAsync(d, h.data(), sizeof(double2) * (size_t)N, cudaMemcpyHostToDevice, s);
+    e = cudaMemcpyAsync(d, h.data(), h.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { err = std::string("twiddle upload: ") + cudaGetErrorString(e); cudaFree(d); return nullptr; }
     // older tables stay allocated: plans in flight may still read them
@@ -143,16 +118,20 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     const int B = p->B;
 
     // descending stacks, ties by original index (reference gpu_plan.cu:405-409)
-    p->perm.resize(n);
-    for (int i = 0; i < n; ++i) p->perm[i] = i;
-    std::sort(p->perm.begin(), p->perm.end(), [S](int a, int b) {
-        return S[a] > S[b] || (S[a] == S[b] && a < b);
-    });
-    p->S_sorted.resize(n);
-    p->inv_perm.resize(n);
-    for (int i = 0; i < n; ++i) {
-        p->S_sorted[i] = S[p->perm[i]];
-        p->inv_perm[p->perm[i]] = i;
+    {   // sort (stack, index) pairs: contiguous keys, no indirection in the compare
+        std::vector<std::pair<double, int>> kv(n);
+        for (int i = 0; i < n; ++i) kv[i] = {S[i], i};
+        std::sort(kv.begin(), kv.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+            return a.first > b.first || (a.first == b.first && a.second < b.second);
+        });
+        p->perm.resize(n);
+        p->S_sorted.resize(n);
+        p->inv_perm.resize(n);
+        for (int i = 0; i < n; ++i) {
+            p->perm[i] = kv[i].second;
+            p->S_sorted[i] = kv[i].first;
+            p->inv_perm[kv[i].second] = i;
+        }
     }
     p->Smax = p->S_sorted[0];
 
@@ -248,9 +227,18 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     const size_t o_fb = fa ? take(sizeof(double2) * (size_t)qc * std::max(fa, fb)) : 0;
     const size_t o_fc = fa ? take(sizeof(double2) * (size_t)qc * fa) : 0;
 
-    cudaError_t e = cudaMalloc(&p->arena, off);
+    // stream-ordered allocation from the device's default pool, whose release
+    // threshold icm_gpu_init raises so that freed arenas are kept for the next
+    // plan (icm_gpu_release_pooled_memory returns them to the driver);
+    // memory_strategy 1 asks for plain cudaMalloc instead
+    cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        p->pooled = p->opts.memory_strategy != 1;
+        e = p->pooled ? cudaMallocAsync((void **)&p->arena, off, p->stream) : cudaMalloc(&p->arena, off);
+    }
     if (e != cudaSuccess) {
         err = "device allocation of " + std::to_string(off) + " bytes failed: " + cudaGetErrorString(e);
+        if (p->stream) cudaStreamDestroy(p->stream);
         delete p;
         return nullptr;
     }
@@ -281,9 +269,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
         p->d_fb = (double2 *)(A + o_fb);
         p->d_fc = (double2 *)(A + o_fc);
     }
-    e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
+    e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_perm, p->perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
@@ -309,7 +295,14 @@ void plan_destroy(Plan *p) {
     if (p->stream) cudaStreamSynchronize(p->stream);
     if (p->graph) cudaGraphExecDestroy(p->graph);
     if (p->d_node) cudaFree(p->d_node);
-    if (p->arena) cudaFree(p->arena);
+    if (p->arena) {
+        if (p->pooled) {
+            cudaFreeAsync(p->arena, p->stream);
+            cudaStreamSynchronize(p->stream);
+        } else {
+            cudaFree(p->arena);
+        }
+    }
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     for (cudaEvent_t ev : p->prof.pool) cudaEventDestroy(ev);

@@ -69,6 +69,7 @@ struct Plan {
     cudaStream_t stream = nullptr;
     char *arena = nullptr;
     size_t arena_bytes = 0;
+    bool pooled = false;            // arena from the stream-ordered pool
     double *d_S = nullptr;          // sorted stacks
     int *d_perm = nullptr;
     double *d_payout = nullptr;     // g at the root: payout zero-padded to glen(root)
@@ -117,6 +118,9 @@ void make_nodes(int Q, double Smax, std::vector<double> &logv, std::vector<doubl
 // device-wide twiddle table exp(-2 pi i t / 2^logTW); *logTW receives the
 // table's size, which may exceed the request
 const double2 *twiddles(int logN, cudaStream_t s, std::string &err, int *logTW);
+// host image of those tables (twiddle.cpp)
+size_t twiddle_bytes(int logTW);
+void fill_twiddles(int logTW, std::vector<unsigned char> &out);
 
 // probes (probes.cu)
 int measure_fp64_gflops(double *out, std::string &err);

@@ -3,9 +3,9 @@
 // Transforms run in shared memory as in-place radix-4 decimation-in-time
 // passes over bit-reversed input (two radix-2 stages fused per pass, so the
 // output is in natural order), with one radix-2 pass when log2(M) is odd.
-// Per fused pass a butterfly costs 3 complex twiddle products and 8 complex
-// additions: 28 FP64 instructions for 4 points and 2 stages.  Twiddles come
-// from one device table tw[t] = exp(-2 pi i t / 2^logTW).
+// Twiddles for pointwise steps come from one device table
+// tw[t] = exp(-2 pi i t / 2^logTW); the butterflies use the tangent-form
+// tables stored right after it (below).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -37,120 +37,160 @@ __device__ __forceinline__ double2 twmul(double2 a, double2 w) {
     return SIGN < 0 ? cmul(a, w) : cmulc(a, w);
 }
 
+// Tangent-form twiddles.  Every twiddle w is stored as w = R r (1 + i tau)
+// with R in {1, -i, -1, i} (2-bit code), r >= 1/sqrt(2) and |tau| <= 1, so
+// z w = r ((R z) + i tau (R z)): the rotation is a swap/sign change on the
+// integer pipe, (1 + i tau) costs 2 FMAs and r folds into the following
+// additions.  A radix-4 DIT butterfly then costs 22 FP64 instructions
+// (6 for the three (1 + i tau) products, 16 FMAs for the sums with r1, r2 and
+// rho = r3 / r1 folded in) instead of 28.
+//
+// The tables follow the plain table tw[0 .. 2^logTW) in the same allocation:
+//   R4[h + j]  j < h, h = 4^m:  {tau1, r1}, {tau2, r2}, {tau3, rho} for the
+//              twiddles w^j, w^2j, w^3j of a pass with groups of 4h (w = e^{-2 pi i/4h})
+//   R4C[h + j] rotation codes of those three twiddles (bits 0-1, 2-3, 4-5)
+//   R2[h + j]  {tau, r} of e^{-2 pi i j/2h} for the final radix-2 pass
+//   R2C[h + j] its rotation code
+constexpr int kTwMaxH4 = 2048;   // radix-4 passes of transforms up to 8192 points
+constexpr int kTwMaxH2 = 4096;   // radix-2 pass of an 8192-point transform
+
+struct GTw {
+    double2 a, b, c;
+};
+
+struct TwTables {
+    const GTw *r4;
+    const int *r4c;
+    const double2 *r2;
+    const int *r2c;
+};
+
+__device__ __forceinline__ TwTables tw_tables(const double2 *tw, int logTW) {
+    const char *base = (const char *)(tw + (1L << logTW));
+    TwTables t;
+    t.r4 = (const GTw *)base;
+    base += sizeof(GTw) * 2 * kTwMaxH4;
+    t.r4c = (const int *)base;
+    base += sizeof(int) * 2 * kTwMaxH4;
+    t.r2 = (const double2 *)base;
+    base += sizeof(double2) * 2 * kTwMaxH2;
+    t.r2c = (const int *)base;
+    return t;
+}
+
+// bytes of the tangent tables that follow the plain table
+constexpr size_t kTwExtraBytes = sizeof(double2) * 3 * 2 * kTwMaxH4 + sizeof(int) * 2 * kTwMaxH4 +
+                                 sizeof(double2) * 2 * kTwMaxH2 + sizeof(int) * 2 * kTwMaxH2;
+
+__device__ __forceinline__ double dneg_if(double v, int neg) {
+    return __longlong_as_double(__double_as_longlong(v) ^ ((long long)neg << 63));
+}
+
+// R z for code 0: 1, 1: -i, 2: -1, 3: i (SIGN = +1 uses conj(R): codes 1 <-> 3)
+template <int SIGN>
+__device__ __forceinline__ double2 rot(double2 z, int code) {
+    if (SIGN > 0) code = (4 - code) & 3;
+    const int sw = code & 1;
+    const double x = sw ? z.y : z.x, y = sw ? z.x : z.y;
+    return make_double2(dneg_if(x, code >> 1), dneg_if(y, (code == 1) | (code == 2)));
+}
+
+// (R z)(1 + i tau); the inverse transform uses conj: R -> conj R, tau -> -tau
+template <int SIGN>
+__device__ __forceinline__ double2 tanmul(double2 z, int code, double tau) {
+    const double2 v = rot<SIGN>(z, code);
+    if (SIGN < 0) return make_double2(fma(-tau, v.y, v.x), fma(tau, v.x, v.y));
+    return make_double2(fma(tau, v.y, v.x), fma(-tau, v.x, v.y));
+}
+
 // `cnt` transforms of size 2^logM stored back to back in x (shared memory),
 // each already in bit-reversed order.  All threads of the block take part;
 // the caller synchronises before (after filling x) and this function ends
 // with a barrier.
 template <int SIGN>
 __device__ void smem_fft_dit(double2 *x, int logM, int cnt, const double2 *__restrict__ tw, int logTW) {
+    const TwTables T = tw_tables(tw, logTW);
     const int M = 1 << logM;
     int s = 0;
     for (; s + 1 < logM; s += 2) {
         const int h = 1 << s;
         const int nb = cnt << (logM - 2);
-        const int sh = logTW - s - 2;
         for (int b = threadIdx.x; b < nb; b += blockDim.x) {
             const int item = b >> (logM - 2);
             const int r = b & ((M >> 2) - 1);
             const int j = r & (h - 1);
             const int i = item * M + ((r >> s) << (s + 2)) + j;
-            double2 a = x[i], bq = x[i + h], c = x[i + 2 * h], d = x[i + 3 * h];
-            if (j != 0) {
-                const double2 t1 = __ldg(&tw[j << sh]);
-                const double2 t2 = __ldg(&tw[(2 * j) << sh]);
-                const double2 t3 = __ldg(&tw[(3 * j) << sh]);
-                c = twmul<SIGN>(c, t1);
-                bq = twmul<SIGN>(bq, t2);
-                d = twmul<SIGN>(d, t3);
-            }
-            const double2 s0 = cadd(a, bq), d0 = csub(a, bq);
-            const double2 s1 = cadd(c, d), d1 = csub(c, d);
-            x[i] = cadd(s0, s1);
-            x[i + 2 * h] = csub(s0, s1);
-            if (SIGN < 0) {
-                x[i + h] = cadd(d0, cmul_mi(d1));
-                x[i + 3 * h] = csub(d0, cmul_mi(d1));
+            const double2 a = x[i], bq = x[i + h], c = x[i + 2 * h], d = x[i + 3 * h];
+            double2 x0, x1, x2, x3;
+            if (h == 1) {   // first pass: all twiddles are 1
+                const double2 s0 = cadd(a, bq), d0 = csub(a, bq);
+                const double2 s1 = cadd(c, d), d1 = csub(c, d);
+                x0 = cadd(s0, s1);
+                x2 = csub(s0, s1);
+                if (SIGN < 0) { x1 = cadd(d0, cmul_mi(d1)); x3 = csub(d0, cmul_mi(d1)); }
+                else { x1 = cadd(d0, cmul_pi(d1)); x3 = csub(d0, cmul_pi(d1)); }
             } else {
-                x[i + h] = cadd(d0, cmul_pi(d1));
-                x[i + 3 * h] = csub(d0, cmul_pi(d1));
+                const GTw g = T.r4[h + j];
+                const int code = __ldg(&T.r4c[h + j]);
+                const double2 uc = tanmul<SIGN>(c, code & 3, g.a.x);          // t1 = R1 r1 (1 + i tau1)
+                const double2 ub = tanmul<SIGN>(bq, (code >> 2) & 3, g.b.x);  // t2
+                const double2 ud = tanmul<SIGN>(d, (code >> 4) & 3, g.c.x);   // t3, r3 = rho r1
+                const double r1 = g.a.y, r2 = g.b.y, rho = g.c.y;
+                const double2 s0 = make_double2(fma(r2, ub.x, a.x), fma(r2, ub.y, a.y));
+                const double2 d0 = make_double2(fma(-r2, ub.x, a.x), fma(-r2, ub.y, a.y));
+                const double2 e = make_double2(fma(rho, ud.x, uc.x), fma(rho, ud.y, uc.y));
+                const double2 f = make_double2(fma(-rho, ud.x, uc.x), fma(-rho, ud.y, uc.y));
+                x0 = make_double2(fma(r1, e.x, s0.x), fma(r1, e.y, s0.y));
+                x2 = make_double2(fma(-r1, e.x, s0.x), fma(-r1, e.y, s0.y));
+                if (SIGN < 0) {   // x1 = d0 - i r1 f, x3 = d0 + i r1 f
+                    x1 = make_double2(fma(r1, f.y, d0.x), fma(-r1, f.x, d0.y));
+                    x3 = make_double2(fma(-r1, f.y, d0.x), fma(r1, f.x, d0.y));
+                } else {
+                    x1 = make_double2(fma(-r1, f.y, d0.x), fma(r1, f.x, d0.y));
+                    x3 = make_double2(fma(r1, f.y, d0.x), fma(-r1, f.x, d0.y));
+                }
             }
+            x[i] = x0;
+            x[i + h] = x1;
+            x[i + 2 * h] = x2;
+            x[i + 3 * h] = x3;
         }
         __syncthreads();
     }
     if (s < logM) {  // one radix-2 stage left, half size h = M/2
         const int h = 1 << s;
         const int nb = cnt << (logM - 1);
-        const int sh = logTW - s - 1;
         for (int b = threadIdx.x; b < nb; b += blockDim.x) {
             const int item = b >> (logM - 1);
             const int r = b & ((M >> 1) - 1);
             const int j = r & (h - 1);
             const int i = item * M + ((r >> s) << (s + 1)) + j;
-            double2 a = x[i], bq = x[i + h];
-            if (j != 0) bq = twmul<SIGN>(bq, __ldg(&tw[j << sh]));
-            x[i] = cadd(a, bq);
-            x[i + h] = csub(a, bq);
+            const double2 a = x[i], bq = x[i + h];
+            const double2 g = T.r2[h + j];
+            const double2 u = tanmul<SIGN>(bq, __ldg(&T.r2c[h + j]), g.x);
+            x[i] = make_double2(fma(g.y, u.x, a.x), fma(g.y, u.y, a.y));
+            x[i + h] = make_double2(fma(-g.y, u.x, a.x), fma(-g.y, u.y, a.y));
         }
         __syncthreads();
     }
 }
 
-// Decimation in frequency: natural-order input, bit-reversed output.  Two
-// radix-2 stages (half sizes 2h and h) per pass, largest first; with
-// t = w_{4h}^j the fused pass is
-//   x0 = (a + c) + (b + d)            x1 = ((a + c) - (b + d)) t^2
-//   x2 = ((a - c) -+ i (b - d)) t     x3 = ((a - c) +- i (b - d)) t^3
-// (upper signs forward).  A leading radix-2 stage handles odd log2(M).
-// Pairing a DIF inverse with a DIT forward transform lets a pointwise step
-// between them run in bit-reversed order with no permutation.
-template <int SIGN>
-__device__ void smem_fft_dif(double2 *x, int logM, int cnt, const double2 *__restrict__ tw, int logTW) {
+// In-place bit-reversal permutation of `cnt` arrays of 2^logM points with a
+// pointwise map applied on the way: slot bitrev(s) <- op(it, s, x[s]).  Each
+// thread owns whole pairs (s, bitrev(s)), so there is no read/write race.
+template <typename Op>
+__device__ void smem_bitrev_map(double2 *x, int logM, int cnt, Op op) {
     const int M = 1 << logM;
-    int s = logM;   // stages left
-    if (logM & 1) {  // radix-2 stage with half size M/2
-        const int h = M >> 1;
-        const int nb = cnt << (logM - 1);
-        const int sh = logTW - logM;
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-            const int item = b >> (logM - 1);
-            const int j = b & (h - 1);
-            const int i = item * M + j;
-            const double2 a = x[i], bq = x[i + h];
-            x[i] = cadd(a, bq);
-            const double2 d = csub(a, bq);
-            x[i + h] = (j != 0) ? twmul<SIGN>(d, __ldg(&tw[j << sh])) : d;
-        }
-        __syncthreads();
-        s -= 1;
+    for (int e = threadIdx.x; e < cnt * M; e += blockDim.x) {
+        const int it = e >> logM, s = e & (M - 1);
+        const int r = (int)bitrev(s, logM);
+        if (r < s) continue;
+        double2 *xi = x + (size_t)it * M;
+        const double2 vs = xi[s], vr = xi[r];
+        xi[r] = op(it, s, vs);
+        if (r != s) xi[s] = op(it, r, vr);
     }
-    for (; s >= 2; s -= 2) {
-        const int hs = s - 2;         // log2 of h
-        const int h = 1 << hs;        // pass covers half sizes 2h and h; groups of 4h
-        const int nb = cnt << (logM - 2);
-        const int sh = logTW - hs - 2;
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-            const int item = b >> (logM - 2);
-            const int r = b & ((M >> 2) - 1);
-            const int j = r & (h - 1);
-            const int i = item * M + ((r >> hs) << (hs + 2)) + j;
-            const double2 a = x[i], bq = x[i + h], c = x[i + 2 * h], d = x[i + 3 * h];
-            const double2 s0 = cadd(a, c), d0 = csub(a, c);
-            const double2 s1 = cadd(bq, d), d1 = csub(bq, d);
-            double2 y1 = csub(s0, s1), y2, y3;
-            if (SIGN < 0) { y2 = cadd(d0, cmul_mi(d1)); y3 = csub(d0, cmul_mi(d1)); }
-            else { y2 = cadd(d0, cmul_pi(d1)); y3 = csub(d0, cmul_pi(d1)); }
-            x[i] = cadd(s0, s1);
-            if (j != 0) {
-                y1 = twmul<SIGN>(y1, __ldg(&tw[(2 * j) << sh]));
-                y2 = twmul<SIGN>(y2, __ldg(&tw[j << sh]));
-                y3 = twmul<SIGN>(y3, __ldg(&tw[(3 * j) << sh]));
-            }
-            x[i + h] = y1;
-            x[i + 2 * h] = y2;
-            x[i + 3 * h] = y3;
-        }
-        __syncthreads();
-    }
+    __syncthreads();
 }
 
 }  // namespace icmg

@@ -61,28 +61,6 @@ static int noalloc_setup(std::string &err) {
     return dev;
 }
 
-// e^{-2 pi i t / N}, folded into [0, pi/4] before the long-double sine/cosine
-static void noalloc_root(long t, long N, double *re, double *im) {
-    const long double two_pi = 6.283185307179586476925286766559005768L;
-    int conj = 0, neg_c = 0;
-    if (2 * t > N) { t = N - t; conj = 1; }
-    long num = t, den = N;
-    if (4 * t > N) { num = N - 2 * t; den = 2 * N; neg_c = 1; }
-    long double c, s;
-    if (8 * num > den) {
-        const long double b = two_pi * (long double)(den - 4 * num) / (4.0L * (long double)den);
-        c = sinl(b);
-        s = cosl(b);
-    } else {
-        const long double a = two_pi * (long double)num / (long double)den;
-        c = cosl(a);
-        s = sinl(a);
-    }
-    if (neg_c) c = -c;
-    *re = (double)c;
-    *im = conj ? (double)s : (double)(-s);
-}
-
 static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Geometry of the same tree the allocating path builds (engine.cu), with
@@ -146,7 +124,7 @@ static int noalloc_plan(NoallocPlan &p, int n, int k, int nact, char *base, std:
     per_q += al256(fa * 16) * 2 + al256(std::max(fa, fb) * 16);
     p.logTW = logN;
     const size_t fixed = al256((size_t)n * 8) * 3 + al256((size_t)n * 4) + al256((size_t)k * 8) +
-                         al256((size_t)3 * std::max(nact, 1) * 8) + al256(((size_t)1 << logN) * 16) +
+                         al256((size_t)3 * std::max(nact, 1) * 8) + al256(twiddle_bytes(logN)) +
                          (size_t)kMaxLevels * 3 * 256 + 4096;
     if (fixed + per_q > kNoallocBytes) {
         err = "tournament needs " + std::to_string(fixed + per_q) + " bytes of scratch for one node; the "
@@ -162,7 +140,7 @@ static int noalloc_plan(NoallocPlan &p, int n, int k, int nact, char *base, std:
     p.d_perm = (int *)take((size_t)n * 4);
     p.d_payout = (double *)take((size_t)k * 8);
     p.d_node = (double *)take((size_t)3 * std::max(nact, 1) * 8);
-    p.tw = (double2 *)take(((size_t)1 << logN) * 16);
+    p.tw = (double2 *)take(twiddle_bytes(logN));
     p.d_a = (double *)take((size_t)p.qc * n * 8);
     p.d_contrib = (double *)take((size_t)p.qc * n * 8);
     p.d_blockP = (double *)take((size_t)p.qc * p.nblocks * (B + 1) * 8);
@@ -226,8 +204,8 @@ extern "C" int icm_gpu_equity_noalloc(int n, const double *S, int Q, const doubl
     const int nact = (int)(node.size() / 3);
     NoallocPlan p;
     if (noalloc_plan(p, n, k, nact, g_noalloc_ptr[dev], err) != 0) return fail(err);
-    std::vector<double2> tw((size_t)1 << p.logTW);
-    for (long t = 0; t < (1L << p.logTW); ++t) noalloc_root(t, 1L << p.logTW, &tw[(size_t)t].x, &tw[(size_t)t].y);
+    std::vector<unsigned char> tw;
+    fill_twiddles(p.logTW, tw);
 
     cudaStream_t st = 0;   // legacy default stream: no stream creation
     cudaError_t e = cudaMemcpyAsync(p.d_S, Ss.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
@@ -236,7 +214,7 @@ extern "C" int icm_gpu_equity_noalloc(int n, const double *S, int Q, const doubl
     if (e == cudaSuccess && nact)
         e = cudaMemcpyAsync(p.d_node, node.data(), sizeof(double) * node.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(p.tw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice, st);
+        e = cudaMemcpyAsync(p.tw, tw.data(), tw.size(), cudaMemcpyHostToDevice, st);
     // the accumulator must start at zero when no node has weight
     if (e == cudaSuccess) e = cudaMemsetAsync(p.d_acc, 0, sizeof(double) * n, st);
     if (e != cudaSuccess) return fail(std::string("upload: ") + cudaGetErrorString(e));

@@ -21,9 +21,9 @@
 //         or, where the level below works on coefficients, a = (IDFT_D(even
 //         bins) + (a - b))/2.  Two size-D/2 transforms per child.
 //
-// Inverses run as decimation-in-frequency (natural in, bit-reversed out) and
-// forwards as decimation-in-time (bit-reversed in, natural out), so the
-// pointwise twist between them needs no permutation.  A missing sibling
+// All transforms are decimation-in-time (bit-reversed in, natural out); the
+// pointwise twist between two transforms is applied while permuting the data
+// into bit-reversed order in place (smem_bitrev_map).  A missing sibling
 // (ragged tree edge) is the polynomial 1: spectrum 1, ends (1, 0).
 #include "engine.h"
 #include "fft.cuh"
@@ -121,23 +121,20 @@ k_spec_build(const double2 *__restrict__ cspec, size_t cs_q, const double *__res
         double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
         const double2 O = cmulc(Dd, twl(tw, (long)f << (logTW - logD - 1)));   // * e^{+2 pi i f/2D}
-        sm[e] = cadd(E, cmul_pi(O));
+        sm[(size_t)it * D + bitrev(f, logD)] = cadd(E, cmul_pi(O));
     }
     __syncthreads();
-    smem_fft_dif<+1>(sm, logD, cnt, tw, logTW);
-    // 2. coefficients (bit-reversed slots), endpoint fix, twist for the half-bin transform
-    for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) {
-        const int it = e >> logD, r = e & (D - 1);
-        const int s = (int)bitrev(r, logD);
+    smem_fft_dit<+1>(sm, logD, cnt, tw, logTW);
+    // 2. coefficients x_{2s}, x_{2s+1} = u_s / 2D (natural order), endpoint fix,
+    //    then the twist for the half-bin transform into bit-reversed slots
+    auto coeffs = [&](int it, int s, double2 u) -> double2 {
         const int j = j0 + it;
         const double *eL = cends + q * ce_q + (size_t)(2 * j) * 2;
         const bool has_r = (2 * j + 1) < nreal_c;
-        const double R0 = has_r ? eL[2] : 1.0, Rt = has_r ? eL[3] : 0.0;
-        const double2 u = sm[e];
         double x0 = u.x * one_over_2D, x1 = u.y * one_over_2D;
-        const double xtop = eL[1] * Rt;
+        const double xtop = eL[1] * (has_r ? eL[3] : 0.0);
         if (s == 0) {
-            x0 = eL[0] * R0;
+            x0 = eL[0] * (has_r ? eL[2] : 1.0);
             if (pends) {
                 double *en = pends + q * pe_q + (size_t)j * 2;
                 en[0] = x0;
@@ -154,10 +151,13 @@ k_spec_build(const double2 *__restrict__ cspec, size_t cs_q, const double *__res
             }
         }
         const double y0 = (s == 0) ? x0 - xtop : x0;
-        sm[e] = cmul(make_double2(y0, x1), twl(tw, (long)s << (logTW - logD - 1)));   // e^{-2 pi i s/2D}
+        return cmul(make_double2(y0, x1), twl(tw, (long)s << (logTW - logD - 1)));   // e^{-2 pi i s/2D}
+    };
+    if (!pspec) {   // the level above works on coefficients: no spectrum needed
+        for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) coeffs(e >> logD, e & (D - 1), sm[e]);
+        return;
     }
-    if (!pspec) return;   // the level above works on coefficients: no spectrum needed
-    __syncthreads();
+    smem_bitrev_map(sm, logD, cnt, coeffs);
     smem_fft_dit<-1>(sm, logD, cnt, tw, logTW);
     // 3. odd bins: H[f] = E'[f] + e^{-2 pi i (2f+1)/4D} O'[f]
     for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) {
@@ -247,19 +247,17 @@ k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restri
         const double2 w = twl(tw, (long)f1 << (logTW - logD - 1));     // e^{-2 pi i (2f+1)/2D}
         const double2 Ep = cscale(cadd(Y1, Y2), 0.5);
         const double2 Op = cscale(cmulc(csub(Y1, Y2), w), 0.5);
-        sm[e] = cadd(Ep, cmul_pi(Op));
+        sm[(size_t)kk * h + bitrev(f, lh)] = cadd(Ep, cmul_pi(Op));
     }
     __syncthreads();
-    smem_fft_dif<+1>(sm, lh, nk, tw, logTW);
+    smem_fft_dit<+1>(sm, lh, nk, tw, logTW);
     // 2. untwist: w_s = c'_s e^{+2 pi i s/D} / (D/2) = (a-b)_{2s} + i (a-b)_{2s+1}
     const double inv_h = 1.0 / h;
-    for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
-        const int r = e & (h - 1);
-        const int s = (int)bitrev(r, lh);
-        sm[e] = cscale(cmulc(sm[e], twl(tw, (long)s << (logTW - logD))), inv_h);
-    }
+    auto untwist = [&](int, int s, double2 v) -> double2 {
+        return cscale(cmulc(v, twl(tw, (long)s << (logTW - logD))), inv_h);
+    };
     if (Gout) {
-        __syncthreads();
+        smem_bitrev_map(sm, lh, nk, untwist);
         smem_fft_dit<-1>(sm, lh, nk, tw, logTW);
         // 3a. G_child[f] = (Y[2f] + DFT_D(a-b)[f]) / 2, f = 0..h
         for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
@@ -293,12 +291,11 @@ k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restri
     }
     // 3b. coefficients: store (a-b)/2, then add IDFT_D(even bins)/2 = (a+b)/2
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
-        const int kk = e >> lh, r = e & (h - 1);
-        const int s = (int)bitrev(r, lh);
+        const int kk = e >> lh, s = e & (h - 1);
         const int c = 2 * (j0 + (kk >> 1)) + (kk & 1);
         if (c >= nreal_c) continue;
         double *out = gout + q * go_q + (size_t)c * gst_c;
-        const double2 v = sm[e];
+        const double2 v = untwist(kk, s, sm[e]);
         if (2 * s < glen_c) out[2 * s] = 0.5 * v.x;
         if (2 * s + 1 < glen_c) out[2 * s + 1] = 0.5 * v.y;
     }
@@ -316,14 +313,13 @@ k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restri
         double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
         const double2 O = cmulc(Dd, twl(tw, (long)f << (logTW - logD)));      // e^{+2 pi i f/D}
-        sm[e] = cadd(E, cmul_pi(O));
+        sm[(size_t)kk * h + bitrev(f, lh)] = cadd(E, cmul_pi(O));
     }
     __syncthreads();
-    smem_fft_dif<+1>(sm, lh, nk, tw, logTW);
+    smem_fft_dit<+1>(sm, lh, nk, tw, logTW);
     const double inv_D = 1.0 / D;
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
-        const int kk = e >> lh, r = e & (h - 1);
-        const int s = (int)bitrev(r, lh);
+        const int kk = e >> lh, s = e & (h - 1);
         const int c = 2 * (j0 + (kk >> 1)) + (kk & 1);
         if (c >= nreal_c) continue;
         double *out = gout + q * go_q + (size_t)c * gst_c;
