@@ -90,6 +90,15 @@ k_spec_init(const double *__restrict__ P, size_t P_q, int pst, int plen, int nre
 // Build of one spectral level: nodes j of level l from children 2j, 2j+1 of
 // level l-1 (degree D = 2^logD, spec2 of D+1 bins).  Writes spec2 (2D+1 bins)
 // and ends of each node, and its coefficients when Pout != null.
+//
+// Pointwise phases work on mirror pairs of bins so shared products are
+// computed once and the halves and 1/2D scalings are applied once, at the
+// end: with C = S_L S_R, the inverse input for bins f and D-f is
+//   U(f) = E + i O,  U(D-f) = conj(E) + i conj(O),
+//   E = C[f] + conj C[D-f],  O = (C[f] - conj C[D-f]) e^{+2 pi i f/2D},
+// and the odd output bins of a mirror pair (f, D-1-f) are
+//   H(f) = (Ep + T) / 4D,  H(D-1-f) = conj(Ep - T) / 4D,
+//   Ep = c[f] + conj c[D-1-f],  T = -i (c[f] - conj c[D-1-f]) e^{-2 pi i (2f+1)/4D}.
 __global__ void __launch_bounds__(kSpecThreads)
 k_spec_build(const double2 *__restrict__ cspec, size_t cs_q, const double *__restrict__ cends, size_t ce_q,
              int nreal_c, int nreal_p, int logD, double2 *__restrict__ pspec, size_t ps_q,
@@ -97,61 +106,65 @@ k_spec_build(const double2 *__restrict__ cspec, size_t cs_q, const double *__res
              const double2 *__restrict__ tw, int logTW) {
     extern __shared__ double2 sm[];
     const int D = 1 << logD;
+    const int hD = D >> 1;
     const int cb = D >= 4096 ? 1 : 4096 / D;
     const int q = blockIdx.y;
     const int j0 = blockIdx.x * cb;
     const int cnt = min(cb, nreal_p - j0);
     if (cnt <= 0) return;
-    const double one_over_2D = 1.0 / (2.0 * D);
-    // 1. product spectrum (even bins of spec2(X)) and the inverse input U
-    for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) {
-        const int it = e >> logD, f = e & (D - 1);
+    const double2 one = make_double2(1.0, 0.0);
+    // 1. product spectrum (even bins of spec2(X)) and the inverse input, by mirror pairs
+    const int np1 = hD + 1;
+    for (int e = threadIdx.x; e < cnt * np1; e += blockDim.x) {
+        const int it = e / np1, f = e - it * np1;
         const int j = j0 + it;
         const double2 *sL = cspec + q * cs_q + (size_t)(2 * j) * (D + 1);
         const bool has_r = (2 * j + 1) < nreal_c;
         const double2 *sR = sL + (D + 1);
-        const double2 one = make_double2(1.0, 0.0);
         const double2 Cf = cmul(sL[f], has_r ? sR[f] : one);
         const double2 Cc = cmul(sL[D - f], has_r ? sR[D - f] : one);
         if (pspec) {
             double2 *ps = pspec + q * ps_q + (size_t)j * (2 * D + 1);
             ps[2 * f] = Cf;
-            if (f == 0) ps[2 * D] = Cc;
+            ps[2 * (D - f)] = Cc;
         }
         double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
-        const double2 O = cmulc(Dd, twl(tw, (long)f << (logTW - logD - 1)));   // * e^{+2 pi i f/2D}
-        sm[(size_t)it * D + bitrev(f, logD)] = cadd(E, cmul_pi(O));
+        const double2 O = (f == 0) ? Dd : cmulc(Dd, twl(tw, (long)f << (logTW - logD - 1)));   // e^{+2 pi i f/2D}
+        double2 *u = sm + (size_t)it * D;
+        u[bitrev(f, logD)] = cadd(E, cmul_pi(O));
+        if (f != 0 && f != hD) u[bitrev(D - f, logD)] = cadd(cconj(E), cmul_pi(cconj(O)));
     }
     __syncthreads();
     smem_fft_dit<+1>(sm, logD, cnt, tw, logTW);
-    // 2. coefficients x_{2s}, x_{2s+1} = u_s / 2D (natural order), endpoint fix,
-    //    then the twist for the half-bin transform into bit-reversed slots
+    // 2. u_s = 2D (x_{2s} + i x_{2s+1}); coefficients where a coefficient level
+    //    sits above, the endpoint fix, and the (unscaled) twist
+    const double one_over_2D = 1.0 / (2.0 * D);
     auto coeffs = [&](int it, int s, double2 u) -> double2 {
         const int j = j0 + it;
         const double *eL = cends + q * ce_q + (size_t)(2 * j) * 2;
         const bool has_r = (2 * j + 1) < nreal_c;
-        double x0 = u.x * one_over_2D, x1 = u.y * one_over_2D;
         const double xtop = eL[1] * (has_r ? eL[3] : 0.0);
         if (s == 0) {
-            x0 = eL[0] * (has_r ? eL[2] : 1.0);
+            const double x0 = eL[0] * (has_r ? eL[2] : 1.0);
             if (pends) {
                 double *en = pends + q * pe_q + (size_t)j * 2;
                 en[0] = x0;
                 en[1] = xtop;
             }
+            u.x = (x0 - xtop) * (2.0 * D);   // y_0 = x_0 - x_{2D}, in the unscaled units of u
         }
         if (Pout) {
             double *out = Pout + q * Po_q + (size_t)j * pst_p;
+            const double x0 = (s == 0) ? eL[0] * (has_r ? eL[2] : 1.0) : u.x * one_over_2D;
             if (2 * s < plen_p) out[2 * s] = x0;
-            if (2 * s + 1 < plen_p) out[2 * s + 1] = x1;
+            if (2 * s + 1 < plen_p) out[2 * s + 1] = u.y * one_over_2D;
             if (s == 0) {
                 if (2 * D < plen_p) out[2 * D] = xtop;
                 for (int t = 2 * D + 1; t < pst_p; ++t) out[t] = 0.0;
             }
         }
-        const double y0 = (s == 0) ? x0 - xtop : x0;
-        return cmul(make_double2(y0, x1), twl(tw, (long)s << (logTW - logD - 1)));   // e^{-2 pi i s/2D}
+        return (s == 0) ? u : cmul(u, twl(tw, (long)s << (logTW - logD - 1)));   // e^{-2 pi i s/2D}
     };
     if (!pspec) {   // the level above works on coefficients: no spectrum needed
         for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) coeffs(e >> logD, e & (D - 1), sm[e]);
@@ -159,15 +172,17 @@ k_spec_build(const double2 *__restrict__ cspec, size_t cs_q, const double *__res
     }
     smem_bitrev_map(sm, logD, cnt, coeffs);
     smem_fft_dit<-1>(sm, logD, cnt, tw, logTW);
-    // 3. odd bins: H[f] = E'[f] + e^{-2 pi i (2f+1)/4D} O'[f]
-    for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) {
-        const int it = e >> logD, f = e & (D - 1);
+    // 3. odd bins by mirror pairs (f, D-1-f), f < D/2
+    const double kb = 1.0 / (4.0 * D);
+    for (int e = threadIdx.x; e < cnt * hD; e += blockDim.x) {
+        const int it = e / hD, f = e - it * hD;
         const double2 *c = sm + (size_t)it * D;
         const double2 a = c[f], b = cconj(c[D - 1 - f]);
-        const double2 Ep = cscale(cadd(a, b), 0.5);
-        const double2 Op = cscale(cmul_mi(csub(a, b)), 0.5);
+        const double2 Ep = cadd(a, b);
+        const double2 T = cmul(cmul_mi(csub(a, b)), twl(tw, (long)(2 * f + 1) << (logTW - logD - 2)));
         double2 *ps = pspec + q * ps_q + (size_t)(j0 + it) * (2 * D + 1);
-        ps[2 * f + 1] = cadd(Ep, cmul(Op, twl(tw, (long)(2 * f + 1) << (logTW - logD - 2))));
+        ps[2 * f + 1] = cscale(cadd(Ep, T), kb);
+        ps[2 * (D - 1 - f) + 1] = cscale(cconj(csub(Ep, T)), kb);
     }
 }
 
@@ -219,6 +234,15 @@ k_gspec_init(const double *__restrict__ g, size_t g_q, int gst, int glen, int nr
 // its g spectrum (D/2+1 bins) when Gout != null, else its g coefficients.
 // Work per child: a transform of size D/2 (inverse half-bin), then a second
 // one (forward for the spectrum, inverse of the even bins for coefficients).
+//
+// With Y = G conj(S_sib) and w_f = e^{-2 pi i (2f+1)/2D}, the inverse
+// half-bin input of a mirror pair (f, h-1-f), h = D/2, is (doubled)
+//   C'(f) = A + i B,  C'(h-1-f) = conj A + i conj B,
+//   A = Y[2f+1] + conj Y[2f'+1],  B = (Y[2f+1] - conj Y[2f'+1]) conj w_f;
+// the child's spectrum bins f and h-f come from the forward transform z as
+//   X(f) = E + T,  X(h-f) = conj(E - T),  E = z_f + conj z_{h-f},
+//   T = -i (z_f - conj z_{h-f}) e^{-2 pi i f/D},
+//   G_child[f] = Y[2f]/2 + X(f)/8h   (all scalings folded into the last step).
 __global__ void __launch_bounds__(kSpecThreads)
 k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restrict__ cspec, size_t cs_q, int nreal_c,
             int npar, int logD, double2 *__restrict__ Gout, size_t Go_q, double *__restrict__ gout, size_t go_q,
@@ -233,71 +257,78 @@ k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restri
     if (cnt <= 0) return;
     const int nk = 2 * cnt;                               // children handled, h slots each
     const double2 one = make_double2(1.0, 0.0);
-    // 1. odd bins of Y = G conj(S_sib) -> inverse half-bin input C'[f]
-    for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
-        const int kk = e >> lh, f = e & (h - 1);
+    // 1. odd bins of Y -> inverse half-bin input, by mirror pairs
+    const int hp = (h + 1) >> 1;                          // pairs per child (h = 1: one self pair)
+    for (int e = threadIdx.x; e < nk * hp; e += blockDim.x) {
+        const int kk = e / hp, f = e - kk * hp;
+        const int fp = h - 1 - f;
         const int j = j0 + (kk >> 1), side = kk & 1;
-        const int c = 2 * j + side, sib = c ^ 1;
+        const int sib = (2 * j + side) ^ 1;
         const double2 *G = Gp + q * Gp_q + (size_t)j * (D + 1);
         const bool has_sib = sib < nreal_c;
         const double2 *S = cspec + q * cs_q + (size_t)sib * (D + 1);
-        const int f1 = 2 * f + 1, f2 = 2 * (h - 1 - f) + 1;
-        const double2 Y1 = cmulc(G[f1], has_sib ? S[f1] : one);
-        const double2 Y2 = cconj(cmulc(G[f2], has_sib ? S[f2] : one));
-        const double2 w = twl(tw, (long)f1 << (logTW - logD - 1));     // e^{-2 pi i (2f+1)/2D}
-        const double2 Ep = cscale(cadd(Y1, Y2), 0.5);
-        const double2 Op = cscale(cmulc(csub(Y1, Y2), w), 0.5);
-        sm[(size_t)kk * h + bitrev(f, lh)] = cadd(Ep, cmul_pi(Op));
+        const double2 Y1 = cmulc(G[2 * f + 1], has_sib ? S[2 * f + 1] : one);
+        const double2 Y2 = cconj(cmulc(G[2 * fp + 1], has_sib ? S[2 * fp + 1] : one));
+        const double2 A = cadd(Y1, Y2);
+        const double2 B = cmulc(csub(Y1, Y2), twl(tw, (long)(2 * f + 1) << (logTW - logD - 1)));
+        double2 *x = sm + (size_t)kk * h;
+        x[bitrev(f, lh)] = cadd(A, cmul_pi(B));
+        if (fp != f) x[bitrev(fp, lh)] = cadd(cconj(A), cmul_pi(cconj(B)));
     }
     __syncthreads();
     smem_fft_dit<+1>(sm, lh, nk, tw, logTW);
-    // 2. untwist: w_s = c'_s e^{+2 pi i s/D} / (D/2) = (a-b)_{2s} + i (a-b)_{2s+1}
-    const double inv_h = 1.0 / h;
+    // 2. untwist (unscaled): w_s = c'_s e^{+2 pi i s/D}
     auto untwist = [&](int, int s, double2 v) -> double2 {
-        return cscale(cmulc(v, twl(tw, (long)s << (logTW - logD))), inv_h);
+        return (s == 0) ? v : cmulc(v, twl(tw, (long)s << (logTW - logD)));
     };
     if (Gout) {
         smem_bitrev_map(sm, lh, nk, untwist);
         smem_fft_dit<-1>(sm, lh, nk, tw, logTW);
-        // 3a. G_child[f] = (Y[2f] + DFT_D(a-b)[f]) / 2, f = 0..h
-        for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
-            const int kk = e >> lh, f = e & (h - 1);
+        // 3a. child spectra by mirror pairs (f, h-f), f <= h/2
+        const double kx = 1.0 / (8.0 * h);
+        const int hq = (h >> 1) + 1;
+        for (int e = threadIdx.x; e < nk * hq; e += blockDim.x) {
+            const int kk = e / hq, f = e - kk * hq;
+            const int fp = h - f;
             const int j = j0 + (kk >> 1), side = kk & 1;
             const int c = 2 * j + side, sib = c ^ 1;
             if (c >= nreal_c) continue;   // lone child: no right sibling node
             double2 *out = Gout + q * Go_q + (size_t)c * (h + 1);
             if (hot_c && !hot_c[c]) {
                 out[f] = make_double2(0.0, 0.0);
-                if (f == 0) out[h] = make_double2(0.0, 0.0);
+                out[fp] = make_double2(0.0, 0.0);
                 continue;
             }
             const double2 *G = Gp + q * Gp_q + (size_t)j * (D + 1);
             const bool has_sib = sib < nreal_c;
             const double2 *S = cspec + q * cs_q + (size_t)sib * (D + 1);
             const double2 *z = sm + (size_t)kk * h;
-            const double2 zf = z[f], zc = z[(h - f) & (h - 1)];
-            const double2 Ev = cscale(cadd(zf, cconj(zc)), 0.5);
-            const double2 Od = cscale(cmul_mi(csub(zf, cconj(zc))), 0.5);
-            const double2 Xf = cadd(Ev, cmul(Od, twl(tw, (long)f << (logTW - logD))));
-            const double2 Ye = cmulc(G[2 * f], has_sib ? S[2 * f] : one);
-            out[f] = cscale(cadd(Ye, Xf), 0.5);
-            if (f == 0) {
-                const double2 Xh = csub(Ev, Od);
-                const double2 Yh = cmulc(G[D], has_sib ? S[D] : one);
-                out[h] = cscale(cadd(Yh, Xh), 0.5);
+            const double2 zf = z[f & (h - 1)], zc = cconj(z[fp & (h - 1)]);
+            const double2 E = cadd(zf, zc);
+            const double2 T = (f == 0) ? cmul_mi(csub(zf, zc))
+                                       : cmul(cmul_mi(csub(zf, zc)), twl(tw, (long)f << (logTW - logD)));
+            const double2 Yf = cmulc(G[2 * f], has_sib ? S[2 * f] : one);
+            const double2 Xf = cadd(E, T);
+            out[f] = make_double2(fma(kx, Xf.x, 0.5 * Yf.x), fma(kx, Xf.y, 0.5 * Yf.y));
+            if (fp != f) {
+                const double2 Yc = cmulc(G[2 * fp], has_sib ? S[2 * fp] : one);
+                const double2 Xc = cconj(csub(E, T));
+                out[fp] = make_double2(fma(kx, Xc.x, 0.5 * Yc.x), fma(kx, Xc.y, 0.5 * Yc.y));
             }
         }
         return;
     }
-    // 3b. coefficients: store (a-b)/2, then add IDFT_D(even bins)/2 = (a+b)/2
+    // 3b. coefficients: (a-b) = w / 2h (C' doubled, inverse unscaled); store
+    //     (a-b)/2, then add (a+b)/2 from the inverse of the even bins
+    const double ka = 1.0 / (4.0 * h);
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
         const int kk = e >> lh, s = e & (h - 1);
         const int c = 2 * (j0 + (kk >> 1)) + (kk & 1);
         if (c >= nreal_c) continue;
         double *out = gout + q * go_q + (size_t)c * gst_c;
         const double2 v = untwist(kk, s, sm[e]);
-        if (2 * s < glen_c) out[2 * s] = 0.5 * v.x;
-        if (2 * s + 1 < glen_c) out[2 * s + 1] = 0.5 * v.y;
+        if (2 * s < glen_c) out[2 * s] = ka * v.x;
+        if (2 * s + 1 < glen_c) out[2 * s + 1] = ka * v.y;
     }
     __syncthreads();
     // U[f] = E + i O of the even-bin spectrum Ye (bins 0..h of a real size-D spectrum)
