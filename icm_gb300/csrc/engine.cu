@@ -154,9 +154,11 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
             const bool can_fft = c.deg >= p->fft_min_deg;
             // spectral when the children's and this level's products are exact
             // (not truncated at k) and the transforms fit one CTA
-            bool spec = p->spectral && can_fft && c.deg + 1 <= k && c.deg <= kSpecMaxD;
+            // children beyond one CTA's transform use the multi-pass kernels,
+            // which hand g spectra (not coefficients) to a spectral level below
+            bool spec = p->spectral && can_fft && c.deg + 1 <= k;
+            if (c.deg > kSpecMaxD) spec = spec && l - 1 >= 1 && p->lv[l - 1].kind == 2;
             if (l <= p->L - 2) spec = spec && v.deg + 1 <= k;
-            else spec = spec && v.deg <= 2L * kSpecMaxD;   // root: G of the payout
             v.kind = spec ? 2 : (can_fft ? 1 : 0);
             v.fft = (v.kind == 1) ? 1 : 0;
             if (v.fft) {
@@ -183,7 +185,15 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
             v.spec2_q = (size_t)v.nreal * (v.deg + 1);
             v.ends_q = (size_t)v.nreal * 2;
         }
-        if (v.kind == 2) v.G_q = (size_t)v.nreal * (v.deg / 2 + 1);
+        if (v.kind == 2) {
+            v.G_q = (size_t)v.nreal * (v.deg / 2 + 1);
+            const Level &c = p->lv[l - 1];
+            if (c.deg > kSpecMaxD) {   // multi-pass build and propagate buffers
+                fa = std::max(fa, (size_t)v.nreal * (size_t)c.deg);
+                fa = std::max(fa, (size_t)c.nreal * (size_t)(c.deg / 2));
+            }
+            if (v.deg / 2 > kSpecMaxD) fa = std::max(fa, (size_t)v.nreal * (size_t)(v.deg / 2));
+        }
         per_q += (v.P_q + v.g_q + v.ends_q) * 8 + (v.spec_q + v.spec2_q + v.G_q) * 16 + 1024;
     }
     per_q += ((size_t)2 * n + (size_t)p->nblocks * (B + 1)) * 8 + 1024;
@@ -356,8 +366,13 @@ static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, boo
     if (L >= 2 && lv[1].kind == 2) { launch_spec_init(lv[0], nq, tw, logTW, st, pr); ++p->launches; }
     for (int l = 1; l <= L - 2; ++l) {
         if (lv[l].kind == 2) {
-            launch_spec_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, tw, logTW, st, pr);
-            ++p->launches;
+            if (lv[l - 1].deg > kSpecMaxD) {
+                launch_specbig_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, p->d_fa, p->d_fc, tw, logTW, st,
+                                     &p->launches, pr);
+            } else {
+                launch_spec_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, tw, logTW, st, pr);
+                ++p->launches;
+            }
         } else if (lv[l].fft) {
             launch_fft_build(lv[l - 1], lv[l], nq, p->d_fa, p->d_fb, p->d_fc, false, tw, logTW, st, &p->launches, pr);
             if (lv[l - 1].nreal & 1) { launch_school_build(lv[l - 1], lv[l], nq, lv[l].npairs, st, pr); ++p->launches; }
@@ -381,13 +396,25 @@ static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, boo
             // coefficients below a coefficient level, else left by the level above
             if (root || lv[l + 1].kind != 2) {
                 const uint8_t *hot_p = p->subset ? p->d_hot + p->hot_off[l] : nullptr;
-                launch_gspec_init(gp, gp_q, gst_p, gpl, lv[l].nreal, lv[l], lv[l].G, root ? 0 : lv[l].G_q,
-                                  root ? 1 : nq, hot_p, tw, logTW, st, pr);
+                if (lv[l].deg / 2 > kSpecMaxD) {
+                    int logd = 0;
+                    while ((1L << logd) < lv[l].deg) ++logd;
+                    launch_gspecbig_init(gp, gp_q, gst_p, gpl, lv[l].nreal, logd, lv[l].G, root ? 0 : lv[l].G_q,
+                                         root ? 1 : nq, hot_p, p->d_fa, p->d_fc, tw, logTW, st, &p->launches, pr);
+                } else {
+                    launch_gspec_init(gp, gp_q, gst_p, gpl, lv[l].nreal, lv[l], lv[l].G, root ? 0 : lv[l].G_q,
+                                      root ? 1 : nq, hot_p, tw, logTW, st, pr);
+                    ++p->launches;
+                }
+            }
+            if (lv[l - 1].deg > kSpecMaxD) {
+                launch_specbig_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], nq, hot_c, p->d_fa, p->d_fc, tw, logTW,
+                                    st, &p->launches, pr);
+            } else {
+                launch_spec_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l], l - 1 >= 1 && lv[l - 1].kind == 2,
+                                 nq, hot_c, tw, logTW, st, pr);
                 ++p->launches;
             }
-            launch_spec_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l], l - 1 >= 1 && lv[l - 1].kind == 2, nq,
-                             hot_c, tw, logTW, st, pr);
-            ++p->launches;
         } else if (lv[l].fft) {
             launch_fft_prop(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nq, hot_c, p->d_fa, p->d_fb, p->d_fc, tw, logTW,
                             st, &p->launches, pr);

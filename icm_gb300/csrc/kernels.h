@@ -61,6 +61,15 @@ void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal
 void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral, int nq,
                       const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
 
+// spectral levels with transforms beyond one CTA (spectral_big.cu)
+void launch_specbig_build(const Level &c, const Level &p, bool write_coeffs, int nq, double2 *buf, double2 *scratch,
+                          const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr);
+void launch_specbig_prop(const double2 *Gp, size_t Gp_q, const Level &c, int nq, const uint8_t *hot_c, double2 *buf,
+                         double2 *scratch, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr);
+void launch_gspecbig_init(const double *g, size_t g_q, int gst, int glen, int nreal, int logd, double2 *G, size_t G_q,
+                          int nq, const uint8_t *hot, double2 *buf, double2 *scratch, const double2 *tw, int logTW,
+                          cudaStream_t st, long *launches, Prof *pr);
+
 void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
                        const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
