@@ -112,6 +112,11 @@ k_fused_prop(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl, int
     const int cnt = min(cb, npairs - j0);
     double2 *Z = sm;                  // cb x N
     double2 *W = sm + (size_t)cb * N; // cb x h
+    if (hot_c) {   // subset pruning: nothing below a cold child is ever read
+        bool any = false;
+        for (int c = 2 * j0; c < 2 * (j0 + cnt); ++c) any = any || hot_c[c];
+        if (!any) return;
+    }
     // 1. parent g as w[t] = g[2t] + i g[2t+1], bit-reversed
     for (int e = threadIdx.x; e < cnt * h; e += blockDim.x) {
         const int it = e / h, s = e - it * h;

@@ -257,6 +257,11 @@ k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restri
     if (cnt <= 0) return;
     const int nk = 2 * cnt;                               // children handled, h slots each
     const double2 one = make_double2(1.0, 0.0);
+    if (hot_c) {   // subset pruning: nothing below a cold child is ever read
+        bool any = false;
+        for (int c = 2 * j0; c < 2 * (j0 + cnt) && c < nreal_c; ++c) any = any || hot_c[c];
+        if (!any) return;
+    }
     // 1. odd bins of Y -> inverse half-bin input, by mirror pairs
     const int hp = (h + 1) >> 1;                          // pairs per child (h = 1: one self pair)
     for (int e = threadIdx.x; e < nk * hp; e += blockDim.x) {

@@ -108,12 +108,12 @@ __global__ void k_sb_build3(int nreal_p, int logD, double2 *__restrict__ pspec, 
 // ---- propagate (children get g spectra): 1. inverse half-bin input per child
 __global__ void k_sb_prop1(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restrict__ cspec,
                            size_t cs_q, int nreal_c, int logD, double2 *__restrict__ buf,
-                           const double2 *__restrict__ tw, int logTW) {
+                           const uint8_t *__restrict__ hot_c, const double2 *__restrict__ tw, int logTW) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int D = 1 << logD, h = D >> 1, hp = (h + 1) >> 1;
     const int c = (int)(idx / hp), f = (int)(idx % hp);
-    if (c >= nreal_c) return;
+    if (c >= nreal_c || (hot_c && !hot_c[c])) return;   // cold: output zeroed in pass 3
     const int fp = h - 1 - f;
     const int j = c >> 1, sib = c ^ 1;
     const double2 one = make_double2(1.0, 0.0);
@@ -245,7 +245,7 @@ void launch_specbig_prop(const double2 *Gp, size_t Gp_q, const Level &c, int nq,
     const double pts = (double)items * h;
     pr->begin("specbig_prop", pts * 10.0, st);
     k_sb_prop1<<<dim3(nb((long)c.nreal * ((h + 1) / 2), 256), nq), 256, 0, st>>>(Gp, Gp_q, c.spec2, c.spec2_q,
-                                                                                c.nreal, logD, buf, tw, logTW);
+                                                                                c.nreal, logD, buf, hot_c, tw, logTW);
     pr->end(st);
     fft_batched(buf, scratch, items, logD - 1, +1, tw, logTW, st, launches, pr);
     pr->begin("specbig_prop", pts * 4.0, st);
