@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--q-chunk", type=int, default=0, help="quadrature nodes per launch sequence (0 = auto)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-tournaments leg")
+    ap.add_argument("--batch-count", type=int, default=4096, help="tournaments in the batched leg")
     return ap.parse_args()
 
 
@@ -249,6 +251,8 @@ def main():
             sub_ms.append((t2 - t1) * 1e3)
             full_ms.append((t3 - t2) * 1e3)
 
+    batched = None if args.no_batched else batched_leg(icm, W, max(2, args.steps // 3), args.batch_count)
+
     # end to end through icm_equity (host buffers, plan set-up inside)
     e2e = []
     for _ in range(2):
@@ -307,6 +311,7 @@ def main():
         "gpu_launches": launches,
         "subset": {"targets": int(len(T)), "ms": float(np.median(sub_ms)), "full_ms": float(np.median(full_ms)),
                    "path": "icm_gpu_equity_subset vs icm_gpu_equity, plan set-up included"},
+        "batched": batched,
         "roofline": roofline,
         "algorithmic_tflops_per_s": total_flops / (ms_per_solve * 1e-3) / 1e12,
         "fp64_peak_tflops_measured": fp64_peak_gflops / 1e3,
@@ -314,6 +319,72 @@ def main():
         "cpu_baseline": cpu, "clocks": clocks, "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
+
+
+def batched_leg(icm, W, steps, count):
+    """Batched form: `count` tournaments, n log-uniform in [9, 20000],
+    k = ceil(0.15 n), lognormal(sigma=1) stacks x 1e4, geometric payouts 0.8,
+    Q = 256.  Device time of the work-list engine (graph replay, stacks and
+    buffers resident), end to end through icm_gpu_equity_batched (host arrays,
+    set-up inside), and the plain loop of icm_gpu_equity calls on the same
+    GPU, with the largest relative difference between the two."""
+    ts = W.batched(count=count)
+    Ss = [S for S, _ in ts]
+    Ps = [P for _, P in ts]
+    ks = [len(P) for P in Ps]
+    players = int(sum(len(S) for S in Ss))
+    b = icm.GpuBatch(Ss, ks)
+    info = b.info()
+    for _ in range(2):
+        b.equity(Ps, split=False)
+    dev, wall = [], []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        out = b.equity(Ps, split=False)
+        wall.append(time.perf_counter() - t0)
+        dev.append(b.info()["device_ms"])
+    launches = icm.last_launch_count()
+    b.set_options(graphs=False, profiling=True)
+    b.equity(Ps, split=False)
+    kst = sorted(b.kernel_stats(), key=lambda r: -r["ms"])
+    b.close()
+    # end to end through the C entry point: create + run + destroy per call
+    icm.equity_batched(ts[:64])
+    e2e = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        res = icm.equity_batched(ts)
+        e2e.append(time.perf_counter() - t0)
+    # the plain loop: one icm_gpu_equity call per tournament
+    for S, P in ts[:16]:
+        icm.gpu_equity(S, P)
+    t0 = time.perf_counter()
+    loop = [icm.gpu_equity(S, P) for S, P in ts]
+    loop_s = time.perf_counter() - t0
+    err = 0.0
+    for a, r in zip(res, loop):
+        err = max(err, float(np.max(np.abs(a - r) / np.maximum(np.abs(r), 1e-300))))
+    split = np.split(out, np.cumsum([len(S) for S in Ss])[:-1])
+    err_replay = max(float(np.max(np.abs(a - r) / np.maximum(np.abs(r), 1e-300))) for a, r in zip(split, loop))
+    dev_ms = float(np.mean(dev))
+    tot = sum(r["ms"] for r in kst)
+    return {
+        "metric": "batched tourn/s", "value": count / (dev_ms * 1e-3), "unit": "tournaments/s",
+        "ms_per_batch": dev_ms, "tournaments": count, "players": players, "Q": 256,
+        "q_chunk": info["q_chunk"], "device_bytes": info["device_bytes"], "fallback_tournaments": info["fallbacks"],
+        "gpu_launches_per_batch": launches,
+        "replay_wall_ms": 1e3 * float(np.mean(wall)),
+        "e2e": {"value": count / float(np.mean(e2e)), "unit": "tournaments/s", "ms_per_batch": 1e3 * float(np.mean(e2e)),
+                "h2d_bytes_per_step": 8 * (players + sum(ks)) + 8 * count, "d2h_bytes_per_step": 8 * players,
+                "path": "icm_gpu_equity_batched (C ABI, host arrays, batch set-up inside)"},
+        "plain_loop": {"value": count / loop_s, "unit": "tournaments/s", "ms_per_batch": 1e3 * loop_s,
+                       "path": "one icm_gpu_equity call per tournament (host arrays)"},
+        "speedup_vs_loop": {"device": (loop_s * 1e3) / dev_ms, "e2e": loop_s / float(np.mean(e2e))},
+        "max_rel_err_vs_loop": max(err, err_replay),
+        "kernels": [{"kernel": r["name"], "ms": r["ms"], "launches": r["launches"], "flops": r["flops"],
+                     "share": r["ms"] / tot if tot else None} for r in kst],
+        "config": "n log-uniform [9,20000], k=ceil(0.15n), stacks 1e4*lognormal(0,1), payout 0.8^j normalised",
+    }
 
 
 def traffic_for(kernel: str):

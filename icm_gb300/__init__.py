@@ -27,7 +27,7 @@ from ._lib import (IcmGb300Config, IcmGpuOptions, IcmGpuPlanSummary, IcmGpuRunSt
                    library_path)
 
 __all__ = ["init", "equity", "equity_subset", "ICMError", "gpu_equity", "gpu_equity_subset", "GpuPlan",
-           "equity_batched", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
+           "equity_batched", "GpuBatch", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
            "last_launch_count"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -196,25 +196,107 @@ class GpuPlan:
             pass
 
 
-def equity_batched(tournaments, Q=256, return_stats=False):
-    """Equities of many independent tournaments: ``tournaments`` is a list of
-    (stacks, payouts).  Returns a list of arrays."""
+def _batch_arrays(tournaments, Q):
     Ss = [_to_double_array(s, "stacks") for s, _ in tournaments]
     Ps = [_to_double_array(p, "payouts") for _, p in tournaments]
+    if not Ss:
+        raise ValueError("tournaments must not be empty")
     ns = np.array([len(s) for s in Ss], dtype=np.int32)
     ks = np.array([len(p) for p in Ps], dtype=np.int32)
     for n, k in zip(ns, ks):
         _check(int(n), int(k), Q)
+    return ns, ks, np.ascontiguousarray(np.concatenate(Ss)), np.ascontiguousarray(np.concatenate(Ps))
+
+
+def equity_batched(tournaments, Q=256, return_stats=False):
+    """Equities of many independent tournaments: ``tournaments`` is a list of
+    (stacks, payouts).  Every tree-level step of all tournaments runs as one
+    work-list launch; results equal single-tournament solves bit for bit.
+    Returns a list of arrays."""
+    ns, ks, S, P = _batch_arrays(tournaments, Q)
     _auto_init()
-    S = np.ascontiguousarray(np.concatenate(Ss))
-    P = np.ascontiguousarray(np.concatenate(Ps))
     out = np.zeros(len(S))
     st = IcmGpuRunStats()
-    if lib().icm_gpu_equity_batched(len(Ss), ns.ctypes.data_as(_ip), ks.ctypes.data_as(_ip), _d(S), _d(P),
+    if lib().icm_gpu_equity_batched(len(ns), ns.ctypes.data_as(_ip), ks.ctypes.data_as(_ip), _d(S), _d(P),
                                     int(Q), _d(out), ctypes.byref(st)) != 0:
         raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
     res = np.split(out, np.cumsum(ns)[:-1])
     return (res, _stats_dict(st)) if return_stats else res
+
+
+class GpuBatch:
+    """Reusable batch of tournaments: sorts, geometry, device buffers and the
+    work lists are built once from the stacks; ``equity(payouts)`` uploads the
+    payouts and replays the captured CUDA graph of the launch sequence."""
+
+    def __init__(self, stacks_list, ks):
+        Ss = [_to_double_array(s, "stacks") for s in stacks_list]
+        self.ns = np.array([len(s) for s in Ss], dtype=np.int32)
+        self.ks = np.array([int(k) for k in ks], dtype=np.int32)
+        if len(self.ks) != len(self.ns):
+            raise ValueError("one k per tournament")
+        for n, k in zip(self.ns, self.ks):
+            _check(int(n), int(k), 1)
+        _auto_init()
+        S = np.ascontiguousarray(np.concatenate(Ss))
+        self._h = lib().icm_gb300_batch_create(len(Ss), self.ns.ctypes.data_as(_ip), self.ks.ctypes.data_as(_ip),
+                                               _d(S))
+        if not self._h:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+        self._splits = np.cumsum(self.ns)[:-1]
+
+    def equity(self, payouts, Q=256, return_stats=False, split=True):
+        """``payouts``: list of arrays (one per tournament) or their
+        concatenation.  Returns the list of equity arrays (or the
+        concatenation with ``split=False``)."""
+        if isinstance(payouts, (list, tuple)):
+            P = np.ascontiguousarray(np.concatenate([_to_double_array(p, "payouts") for p in payouts]))
+        else:
+            P = _to_double_array(payouts, "payouts")
+        if P.size != int(self.ks.sum()):
+            raise ValueError(f"payouts: expected {int(self.ks.sum())} values, got {P.size}")
+        if Q < 1:
+            raise ValueError(f"Q must be >= 1, got Q={Q}")
+        out = np.zeros(int(self.ns.sum()))
+        st = IcmGpuRunStats()
+        if lib().icm_gb300_batch_run(self._h, int(Q), _d(P), _d(out), ctypes.byref(st)) != 0:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+        res = np.split(out, self._splits) if split else out
+        return (res, _stats_dict(st)) if return_stats else res
+
+    def set_options(self, graphs=True, profiling=None):
+        prof = -1 if profiling is None else int(bool(profiling))
+        lib().icm_gb300_batch_set_options(self._h, int(bool(graphs)), prof)
+
+    def info(self):
+        m, fb, pl = ctypes.c_long(), ctypes.c_long(), ctypes.c_long()
+        qc, ms, nb = ctypes.c_int(), ctypes.c_double(), ctypes.c_size_t()
+        lib().icm_gb300_batch_info(self._h, ctypes.byref(m), ctypes.byref(fb), ctypes.byref(pl), ctypes.byref(qc),
+                                   ctypes.byref(ms), ctypes.byref(nb))
+        return {"members": m.value, "fallbacks": fb.value, "players": pl.value, "q_chunk": qc.value,
+                "device_ms": ms.value, "device_bytes": nb.value}
+
+    def kernel_stats(self):
+        L = lib()
+        cnt = L.icm_gb300_batch_kernel_stats(self._h, -1, None, 0, None, None, None)
+        out = []
+        for i in range(max(cnt, 0)):
+            name = ctypes.create_string_buffer(64)
+            ms, fl, ln = ctypes.c_double(), ctypes.c_double(), ctypes.c_long()
+            L.icm_gb300_batch_kernel_stats(self._h, i, name, 64, ctypes.byref(ms), ctypes.byref(ln), ctypes.byref(fl))
+            out.append({"name": name.value.decode(), "ms": ms.value, "launches": ln.value, "flops": fl.value})
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().icm_gb300_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False):

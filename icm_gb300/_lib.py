@@ -80,6 +80,15 @@ SIGNATURES = {
                                                    ctypes.POINTER(ctypes.c_long), _dp]),
     "icm_gb300_plan_device_ms": (ctypes.c_double, [_vp]),
     "icm_gpu_equity_noalloc": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, _dp]),
+    "icm_gb300_batch_create": (_vp, [ctypes.c_int, _ip, _ip, _dp]),
+    "icm_gb300_batch_run": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, ctypes.POINTER(IcmGpuRunStats)]),
+    "icm_gb300_batch_destroy": (None, [_vp]),
+    "icm_gb300_batch_set_options": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "icm_gb300_batch_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
+                                            ctypes.POINTER(ctypes.c_long), _ip, _dp,
+                                            ctypes.POINTER(ctypes.c_size_t)]),
+    "icm_gb300_batch_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _dp,
+                                                    ctypes.POINTER(ctypes.c_long), _dp]),
 }
 
 _lib = None

@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.h"
 #include "engine.h"
 #include "kernels.h"
 
@@ -294,27 +295,80 @@ int icm_gpu_equity_batched(int T, const int *n, const int *k, const double *S, c
         set_error("icm_gpu_equity_batched invalid arguments");
         return -1;
     }
-    for (int t = 0; t < T; ++t)
-        if (n[t] < 1 || k[t] < 1 || k[t] > n[t]) {
-            set_error("icm_gpu_equity_batched: tournament " + std::to_string(t) + " needs 1 <= k <= n");
-            return -1;
-        }
+    if (!ensure_device()) return -1;
     const double t0 = now_ns();
-    long so = 0, po = 0, launches = 0;
-    for (int t = 0; t < T; ++t) {
-        if (run_full(n[t], S + so, Q, payout + po, k[t], equity + so, nullptr, 0, nullptr, nullptr) != 0)
-            return -1;
-        launches += t_launches;
-        so += n[t];
-        po += k[t];
-    }
-    t_launches = launches;
-    if (stats) {
-        memset(stats, 0, sizeof(*stats));
-        stats->total_ns = now_ns() - t0;
-        stats->engine = 1;
+    std::string err;
+    Forest *f = forest_create(T, n, k, S, err);
+    if (!f) { set_error("icm_gpu_equity_batched: " + err); return -1; }
+    f->graphs = false;   // one run: capturing would not pay
+    const int rc = forest_run(f, Q, payout, equity, stats, err);
+    t_launches = f->launches;
+    forest_destroy(f);
+    if (rc != 0) { set_error("icm_gpu_equity_batched: " + err); return -1; }
+    if (stats) stats->total_ns = now_ns() - t0;
+    return 0;
+}
+
+IcmGb300Batch *icm_gb300_batch_create(int T, const int *n, const int *k, const double *S) {
+    if (!ensure_device()) return nullptr;
+    std::string err;
+    Forest *f = forest_create(T, n, k, S, err);
+    if (!f) { set_error("icm_gb300_batch_create: " + err); return nullptr; }
+    return reinterpret_cast<IcmGb300Batch *>(f);
+}
+
+int icm_gb300_batch_run(IcmGb300Batch *b, int Q, const double *payout, double *equity, IcmGpuRunStats *stats) {
+    if (!b) { set_error("icm_gb300_batch_run: null batch"); return -1; }
+    if (!ensure_device()) return -1;
+    Forest *f = reinterpret_cast<Forest *>(b);
+    std::string err;
+    const int rc = forest_run(f, Q, payout, equity, stats, err);
+    t_launches = f->launches;
+    if (rc != 0) { set_error("icm_gb300_batch_run: " + err); return -1; }
+    return 0;
+}
+
+void icm_gb300_batch_destroy(IcmGb300Batch *b) { forest_destroy(reinterpret_cast<Forest *>(b)); }
+
+int icm_gb300_batch_set_options(IcmGb300Batch *b, int use_graphs, int profiling) {
+    if (!b) return -1;
+    Forest *f = reinterpret_cast<Forest *>(b);
+    f->graphs = use_graphs != 0;
+    if (profiling >= 0) {
+        f->prof.on = profiling != 0;
+        f->kstats.clear();
     }
     return 0;
+}
+
+int icm_gb300_batch_info(const IcmGb300Batch *b, long *members, long *fallbacks, long *players, int *q_chunk,
+                         double *device_ms, size_t *device_bytes) {
+    if (!b) return -1;
+    const Forest *f = reinterpret_cast<const Forest *>(b);
+    if (members) *members = (long)f->tr.size();
+    if (fallbacks) *fallbacks = (long)f->fallback.size();
+    if (players) *players = f->Ntot;
+    if (q_chunk) *q_chunk = f->qc;
+    if (device_ms) *device_ms = f->last_device_ms;
+    if (device_bytes) *device_bytes = f->arena_bytes;
+    return 0;
+}
+
+int icm_gb300_batch_kernel_stats(const IcmGb300Batch *b, int i, char *name, int name_len, double *ms,
+                                 long *launches, double *flops) {
+    if (!b) return -1;
+    const Forest *f = reinterpret_cast<const Forest *>(b);
+    if (i < 0) return (int)f->kstats.size();
+    if (i >= (int)f->kstats.size()) return -1;
+    const auto &k = f->kstats[i];
+    if (name && name_len > 0) {
+        strncpy(name, k.name.c_str(), name_len - 1);
+        name[name_len - 1] = 0;
+    }
+    if (ms) *ms = k.ms;
+    if (launches) *launches = k.launches;
+    if (flops) *flops = k.flops;
+    return (int)f->kstats.size();
 }
 
 int icm_gpu_measure_fp64_gflops(double *gflops_out) {

@@ -1,0 +1,593 @@
+// batch.cu -- many tournaments per launch: one work list per tree-level step.
+//
+// A forest holds T independent tournaments of uneven size, each with its own
+// tree geometry (plan_geometry) and tree buffers, all in one arena.  For a
+// chunk of quadrature nodes every step of the single-plan sequence -- leaf
+// blocks, the products of tree level l, the spectral transitions, the
+// propagate of level l, the per-player divide -- becomes ONE launch that
+// covers every tournament having that step: a work list of descriptors (the
+// kernel's argument block for one tournament level) plus a table that maps
+// each CTA of the launch to (descriptor, block).  Kernels whose shared memory
+// depends on a transform size are split into one list per size.  Players of
+// all tournaments share the node-major arrays a[q][N] and contrib[q][N], so
+// one accumulate and one scatter serve the whole forest.  The launch
+// sequence of a run is captured once as a CUDA graph and replayed while the
+// node count stays the same.
+//
+// Every tournament's arithmetic is the single-plan path's, kernel for kernel,
+// so batched equities equal single-plan equities bit for bit.  Tournaments
+// whose levels need the multi-pass transforms (products beyond one CTA's
+// shared memory) are solved by single plans after the forest.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <thread>
+
+#include "batch.h"
+#include "kernels.h"
+
+namespace icmg {
+
+static double now_ns() {
+    return (double)std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+static int ilog2l(long v) {
+    int l = 0;
+    while ((1L << l) < v) ++l;
+    return l;
+}
+
+// run fn(i) for i in [0, count) on up to hardware_concurrency threads
+template <class F>
+static void parallel_for(int count, F fn) {
+    int nt = (int)std::max(1u, std::thread::hardware_concurrency());
+    nt = std::min(nt, std::max(1, count / 8));
+    if (nt <= 1) {
+        for (int i = 0; i < count; ++i) fn(i);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int w = 0; w < nt; ++w)
+        th.emplace_back([&, w] {
+            for (int i = w; i < count; i += nt) fn(i);
+        });
+    for (auto &t : th) t.join();
+}
+
+// every level of the tree runs on one-CTA kernels
+static bool fits_worklist(const Plan *p) {
+    for (int l = 1; l < p->L; ++l) {
+        const Level &v = p->lv[l], &c = p->lv[l - 1];
+        if (v.kind == 1 && v.npairs > 0 && !fused_ok(v.fftn)) return false;
+        if (v.kind == 2 && (c.deg > kSpecMaxD || v.deg / 2 > kSpecMaxD)) return false;
+    }
+    return true;
+}
+
+// ------------------------------------------------------------ step lists
+namespace {
+struct PhaseBuilder {
+    std::vector<WStep> steps;
+    template <class A>
+    void add(WOp op, int key, const char *name, const A &a, size_t smem, double fq, int one = 0) {
+        if (a.nbx <= 0) return;
+        WStep *s = nullptr;
+        for (auto &x : steps)
+            if (x.op == op && x.key == key && x.one == one) s = &x;
+        if (!s) {
+            steps.emplace_back();
+            s = &steps.back();
+            s->op = op;
+            s->key = key;
+            s->one = one;
+            s->name = name;
+            s->esz = sizeof(A);
+        }
+        const unsigned char *b = (const unsigned char *)&a;
+        s->desc.insert(s->desc.end(), b, b + sizeof(A));
+        for (int bx = 0; bx < a.nbx; ++bx) s->tab.push_back(make_int2(s->nd, bx));
+        ++s->nd;
+        s->smem = std::max(s->smem, smem);
+        s->fq += fq;
+    }
+};
+}  // namespace
+
+// descriptors of every step for Q nodes (pointers into the forest arena)
+static void build_steps(Forest *f) {
+    const int T = (int)f->tr.size();
+    int Lmax = 0;
+    for (Plan *p : f->tr) Lmax = std::max(Lmax, p->L);
+    const double2 *tw = f->tw;
+    const int logTW = f->logTW;
+    const size_t aq = (size_t)f->Ntot;
+    std::vector<PhaseBuilder> pre(1);
+    std::deque<PhaseBuilder> ph;   // stable references while phases are added
+    auto phase = [&]() -> PhaseBuilder & { ph.emplace_back(); return ph.back(); };
+
+    {   // leaf blocks
+        PhaseBuilder &b = phase();
+        for (int t = 0; t < T; ++t) {
+            Plan *p = f->tr[t];
+            double fq = 0;
+            LeafArgs A = leaf_args(p->B, p->n, p->nblocks, p->d_S, p->d_node, f->d_a + f->off[t], aq, p->d_blockP,
+                                   p->lv[0].P, p->lv[0].pst, p->lv[0].plen, &fq);
+            b.add(WOp::Leaf, 0, "wl_leaf", A, 0, fq);
+        }
+        PhaseBuilder &c = phase();
+        for (int t = 0; t < T; ++t) {
+            Plan *p = f->tr[t];
+            if (p->L >= 2 && p->lv[1].kind == 2) {
+                double fq = 0;
+                size_t sm = 0;
+                SpecInitArgs A = spec_init_args(p->lv[0], tw, logTW, &fq, &sm);
+                c.add(WOp::SpecInit, A.logd, "wl_spec_init", A, sm, fq);
+            }
+        }
+    }
+    // products, level by level
+    for (int l = 1; l < Lmax; ++l) {
+        PhaseBuilder &b = phase();
+        for (int t = 0; t < T; ++t) {
+            Plan *p = f->tr[t];
+            Level *lv = p->lv;
+            double fq = 0;
+            size_t sm = 0;
+            if (l <= p->L - 2) {
+                if (lv[l].kind == 2) {
+                    SpecBuildArgs A = spec_build_args(lv[l - 1], lv[l], lv[l + 1].kind != 2, tw, logTW, &fq, &sm);
+                    b.add(WOp::SpecBuild, A.logD, "wl_spec_build", A, sm, fq);
+                } else if (lv[l].fft) {
+                    if (lv[l].npairs > 0) {
+                        FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], false, tw, logTW, &fq, &sm);
+                        b.add(WOp::FusedBuild, A.logN, "wl_fused_build", A, sm, fq);
+                    }
+                    if (lv[l - 1].nreal & 1) {
+                        SchoolBuildArgs A = school_build_args(lv[l - 1], lv[l], lv[l].npairs, &fq);
+                        b.add(WOp::SchoolBuild, 0, "wl_school_build", A, 0, fq);
+                    }
+                } else {
+                    SchoolBuildArgs A = school_build_args(lv[l - 1], lv[l], 0, &fq);
+                    b.add(WOp::SchoolBuild, 0, "wl_school_build", A, 0, fq);
+                }
+            } else if (l == p->L - 1 && lv[l].fft && lv[l].npairs > 0) {
+                // the root: child spectra for its propagate only
+                FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], true, tw, logTW, &fq, &sm);
+                b.add(WOp::FusedBuild, A.logN, "wl_fused_spectra", A, sm, fq);
+            }
+        }
+        PhaseBuilder &c = phase();
+        for (int t = 0; t < T; ++t) {
+            Plan *p = f->tr[t];
+            Level *lv = p->lv;
+            if (l <= p->L - 2 && lv[l].kind != 2 && lv[l + 1].kind == 2) {
+                double fq = 0;
+                size_t sm = 0;
+                SpecInitArgs A = spec_init_args(lv[l], tw, logTW, &fq, &sm);
+                c.add(WOp::SpecInit, A.logd, "wl_spec_init", A, sm, fq);
+            }
+        }
+    }
+    // propagate, root to leaves
+    for (int l = Lmax - 1; l >= 1; --l) {
+        PhaseBuilder &a = phase();
+        for (int t = 0; t < T; ++t) {
+            Plan *p = f->tr[t];
+            Level *lv = p->lv;
+            if (l > p->L - 1 || lv[l].kind != 2) continue;
+            const bool root = (l == p->L - 1);
+            double fq = 0;
+            size_t sm = 0;
+            if (root) {   // the payout's spectrum, shared by the nodes: once per run
+                GspecArgs A = gspec_args(p->d_payout, 0, 0, p->k, lv[l].nreal, lv[l], lv[l].G, 0, nullptr, tw, logTW,
+                                         &fq, &sm);
+                pre[0].add(WOp::Gspec, A.logd, "wl_gspec_root", A, sm, fq, 1);
+            } else if (lv[l + 1].kind != 2) {
+                GspecArgs A = gspec_args(lv[l].g, lv[l].g_q, lv[l].gst, lv[l].glen, lv[l].nreal, lv[l], lv[l].G,
+                                         lv[l].G_q, nullptr, tw, logTW, &fq, &sm);
+                a.add(WOp::Gspec, A.logd, "wl_gspec_init", A, sm, fq);
+            }
+        }
+        PhaseBuilder &b = phase();
+        for (int t = 0; t < T; ++t) {
+            Plan *p = f->tr[t];
+            Level *lv = p->lv;
+            if (l > p->L - 1) continue;
+            const bool root = (l == p->L - 1);
+            const double *gp = root ? p->d_payout : lv[l].g;
+            const size_t gp_q = root ? 0 : lv[l].g_q;
+            const int gst_p = root ? 0 : lv[l].gst;
+            const int gpl = root ? p->k : lv[l].glen;
+            double fq = 0;
+            size_t sm = 0;
+            if (lv[l].kind == 2) {
+                SpecPropArgs A = spec_prop_args(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l],
+                                                l - 1 >= 1 && lv[l - 1].kind == 2, nullptr, tw, logTW, &fq, &sm);
+                b.add(WOp::SpecProp, A.logD, "wl_spec_prop", A, sm, fq);
+            } else if (lv[l].fft) {
+                if (lv[l].npairs > 0) {
+                    FusedPropArgs A = fused_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nullptr, tw, logTW, &fq,
+                                                      &sm);
+                    b.add(WOp::FusedProp, A.logN, "wl_fused_prop", A, sm, fq);
+                }
+                if (lv[l - 1].nreal & 1) {
+                    SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], nullptr, 2 * lv[l].npairs, &fq);
+                    b.add(WOp::SchoolProp, 0, "wl_school_prop", A, 0, fq);
+                }
+            } else {
+                SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], nullptr, 0, &fq);
+                b.add(WOp::SchoolProp, 0, "wl_school_prop", A, 0, fq);
+            }
+        }
+    }
+    {   // per-player divide
+        PhaseBuilder &b = phase();
+        for (int t = 0; t < T; ++t) {
+            Plan *p = f->tr[t];
+            const int L = p->L;
+            const double *g0 = (L == 1) ? p->d_payout : p->lv[0].g;
+            const size_t g0_q = (L == 1) ? 0 : p->lv[0].g_q;
+            const int gst0 = (L == 1) ? 0 : p->lv[0].gst;
+            double fq = 0;
+            DivideArgs A = divide_args(p->B, p->n, p->k, p->nblocks, p->d_S, p->d_node, f->d_a + f->off[t], aq,
+                                       p->d_blockP, g0, g0_q, gst0, nullptr, f->d_contrib + f->off[t], &fq);
+            b.add(WOp::Divide, 0, "wl_divide", A, 0, fq);
+        }
+    }
+    f->pre = std::move(pre[0].steps);
+    f->steps.clear();
+    for (auto &b : ph)
+        for (auto &s : b.steps) f->steps.push_back(std::move(s));
+}
+
+// descriptors and tables into one device buffer
+static int upload_steps(Forest *f, std::string &err) {
+    size_t bytes = 0;
+    auto size_of = [&](std::vector<WStep> &v) {
+        for (auto &s : v) bytes += align256(s.desc.size()) + align256(s.tab.size() * sizeof(int2));
+    };
+    size_of(f->pre);
+    size_of(f->steps);
+    if (bytes > f->desc_cap) {
+        if (f->d_desc) cudaFree(f->d_desc);
+        f->d_desc = nullptr;
+        f->desc_cap = 0;
+        cudaError_t e = cudaMalloc(&f->d_desc, bytes);
+        if (e != cudaSuccess) { err = std::string("work lists: ") + cudaGetErrorString(e); return -1; }
+        f->desc_cap = bytes;
+    }
+    std::vector<unsigned char> h(bytes, 0);
+    size_t off = 0;
+    auto place = [&](std::vector<WStep> &v) {
+        for (auto &s : v) {
+            memcpy(h.data() + off, s.desc.data(), s.desc.size());
+            s.d_desc = f->d_desc + off;
+            off += align256(s.desc.size());
+            memcpy(h.data() + off, s.tab.data(), s.tab.size() * sizeof(int2));
+            s.d_tab = (const int2 *)(f->d_desc + off);
+            off += align256(s.tab.size() * sizeof(int2));
+        }
+    };
+    place(f->pre);
+    place(f->steps);
+    cudaError_t e = cudaMemcpyAsync(f->d_desc, h.data(), bytes, cudaMemcpyHostToDevice, f->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
+    if (e != cudaSuccess) { err = std::string("work list upload: ") + cudaGetErrorString(e); return -1; }
+    return 0;
+}
+
+static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
+    const int nctas = (int)s.tab.size();
+    const int qn = s.one ? 1 : nq;
+    f->prof.begin(s.name, s.fq * qn, f->stream);
+    switch (s.op) {
+        case WOp::Leaf:
+        case WOp::Divide:
+        case WOp::SchoolBuild:
+        case WOp::SchoolProp: launch_worklist_basic(s.op, s.d_desc, s.d_tab, nctas, qn, q0, f->stream); break;
+        case WOp::FusedBuild:
+        case WOp::FusedProp: launch_worklist_fused(s.op, s.d_desc, s.d_tab, nctas, qn, s.smem, f->stream); break;
+        default: launch_worklist_spec(s.op, s.d_desc, s.d_tab, nctas, qn, s.smem, f->stream); break;
+    }
+    f->prof.end(f->stream);
+    ++f->launches;
+}
+
+// the kernel sequence of one run (Q nodes in chunks of qc)
+static void enqueue_run(Forest *f) {
+    for (const WStep &s : f->pre) launch_step(f, s, 1, 0);
+    for (int q0 = 0; q0 < f->Q; q0 += f->qc) {
+        const int nq = std::min(f->qc, f->Q - q0);
+        for (const WStep &s : f->steps) launch_step(f, s, nq, q0);
+        launch_accumulate((int)f->Ntot, nq, f->d_contrib, f->d_acc, q0 == 0 ? 1 : 0, f->stream, &f->prof);
+        ++f->launches;
+    }
+    launch_scatter((int)f->Ntot, f->d_acc, f->d_perm, nullptr, f->d_out, f->stream);
+    ++f->launches;
+}
+
+// ------------------------------------------------------------ lifecycle
+Forest *forest_create(int T, const int *n, const int *k, const double *S, std::string &err) {
+    if (T < 1 || !n || !k || !S) { err = "invalid batch arguments"; return nullptr; }
+    long tot = 0;
+    std::vector<long> ioff(T + 1, 0), ipoff(T + 1, 0);
+    for (int t = 0; t < T; ++t) {
+        if (n[t] < 1 || k[t] < 1 || k[t] > n[t]) {
+            err = "tournament " + std::to_string(t) + " needs 1 <= k <= n";
+            return nullptr;
+        }
+        ioff[t + 1] = ioff[t] + n[t];
+        ipoff[t + 1] = ipoff[t] + k[t];
+        tot += n[t];
+    }
+    if (tot > (long)INT32_MAX / 2) { err = "batch too large (total players)"; return nullptr; }
+    Forest *f = new Forest();
+    f->T = T;
+    f->ioff = ioff;
+    f->ipoff = ipoff;
+    f->n.assign(n, n + T);
+    f->k.assign(k, k + T);
+    // geometry of every tournament (sorts in parallel)
+    std::vector<Plan *> all(T, nullptr);
+    std::vector<std::string> errs(T);
+    parallel_for(T, [&](int t) {
+        Plan *p = new Plan();
+        if (plan_geometry(p, n[t], S + ioff[t], k[t], errs[t]) != 0) {
+            delete p;
+            p = nullptr;
+        }
+        all[t] = p;
+    });
+    for (int t = 0; t < T; ++t)
+        if (!all[t]) {
+            err = "tournament " + std::to_string(t) + ": " + errs[t];
+            for (Plan *p : all) delete p;
+            delete f;
+            return nullptr;
+        }
+    for (int t = 0; t < T; ++t) {
+        if (fits_worklist(all[t])) {
+            f->tr.push_back(all[t]);
+            f->tid.push_back(t);
+        } else {
+            delete all[t];
+            f->fallback.push_back(t);
+        }
+    }
+    for (int t : f->fallback) {   // own plans (own arenas and streams)
+        Plan *p = plan_create(n[t], S + ioff[t], k[t], nullptr, err);
+        if (!p) {
+            err = "tournament " + std::to_string(t) + ": " + err;
+            forest_destroy(f);
+            return nullptr;
+        }
+        f->fb_plans.push_back(p);
+    }
+    const int F = (int)f->tr.size();
+    f->off.assign(F + 1, 0);
+    f->poff.assign(F + 1, 0);
+    for (int i = 0; i < F; ++i) {
+        f->off[i + 1] = f->off[i] + f->tr[i]->n;
+        f->poff[i + 1] = f->poff[i] + f->tr[i]->k;
+    }
+    f->Ntot = f->off[F];
+    f->Ktot = f->poff[F];
+    f->compact = f->fallback.empty();
+
+    cudaError_t e = cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { err = std::string("stream: ") + cudaGetErrorString(e); forest_destroy(f); return nullptr; }
+    if (F == 0) return f;
+
+    // node chunk from the memory budget
+    size_t per_q = (size_t)2 * f->Ntot * 8 + 1024;
+    for (Plan *p : f->tr) per_q += p->tree_q_bytes;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t budget = g_config.max_device_bytes ? g_config.max_device_bytes
+                                                    : std::min<size_t>((size_t)(free_b * 0.6), (size_t)64 << 30);
+    int qc = (int)std::min<size_t>(256, std::max<size_t>(1, budget / std::max<size_t>(per_q, 1)));
+    if (g_config.q_chunk > 0) qc = std::min(qc, g_config.q_chunk);
+    f->qc = qc;
+
+    // arena: shared arrays, then every tournament's tree buffers
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
+    const size_t Nt = (size_t)f->Ntot;
+    const size_t o_S = take(8 * Nt), o_perm = take(4 * Nt), o_pay = take(8 * (size_t)f->Ktot);
+    const size_t o_acc = take(8 * Nt), o_out = take(8 * Nt);
+    const size_t o_a = take(8 * Nt * qc), o_con = take(8 * Nt * qc);
+    std::vector<size_t> o_tree(F);
+    for (int i = 0; i < F; ++i) o_tree[i] = take(plan_tree_layout(f->tr[i], qc, nullptr));
+    e = cudaMallocAsync((void **)&f->arena, off, f->stream);
+    if (e != cudaSuccess) {
+        err = "device allocation of " + std::to_string(off) + " bytes failed: " + cudaGetErrorString(e);
+        forest_destroy(f);
+        return nullptr;
+    }
+    f->arena_bytes = off;
+    char *A = f->arena;
+    f->d_S = (double *)(A + o_S);
+    f->d_perm = (int *)(A + o_perm);
+    f->d_payout = (double *)(A + o_pay);
+    f->d_acc = (double *)(A + o_acc);
+    f->d_out = (double *)(A + o_out);
+    f->d_a = (double *)(A + o_a);
+    f->d_contrib = (double *)(A + o_con);
+    std::vector<double> hS(Nt);
+    std::vector<int> hperm(Nt);
+    int logNeed = 12;
+    for (int i = 0; i < F; ++i) {
+        Plan *p = f->tr[i];
+        plan_tree_layout(p, qc, A + o_tree[i]);
+        p->qc = qc;
+        p->d_S = f->d_S + f->off[i];
+        p->d_payout = f->d_payout + f->poff[i];
+        const long fo = f->off[i];
+        for (int j = 0; j < p->n; ++j) {
+            hS[fo + j] = p->S_sorted[j];
+            hperm[fo + j] = (int)(fo + p->perm[j]);
+        }
+        for (int l = 1; l < p->L; ++l) {
+            if (p->lv[l].fft) logNeed = std::max(logNeed, ilog2l(p->lv[l].fftn));
+            if (p->lv[l].kind == 2) logNeed = std::max(logNeed, ilog2l(2 * p->lv[l].deg));
+        }
+    }
+    f->tw = twiddles(logNeed, f->stream, err, &f->logTW);
+    if (!f->tw) { forest_destroy(f); return nullptr; }
+    e = cudaMemcpyAsync(f->d_S, hS.data(), 8 * Nt, cudaMemcpyHostToDevice, f->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(f->d_perm, hperm.data(), 4 * Nt, cudaMemcpyHostToDevice, f->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
+    if (e != cudaSuccess) { err = std::string("batch upload: ") + cudaGetErrorString(e); forest_destroy(f); return nullptr; }
+    return f;
+}
+
+void forest_destroy(Forest *f) {
+    if (!f) return;
+    if (f->stream) cudaStreamSynchronize(f->stream);
+    if (f->graph) cudaGraphExecDestroy(f->graph);
+    if (f->d_desc) cudaFree(f->d_desc);
+    if (f->d_node) cudaFree(f->d_node);
+    if (f->arena) {
+        cudaFreeAsync(f->arena, f->stream);
+        cudaStreamSynchronize(f->stream);
+    }
+    if (f->ev0) cudaEventDestroy(f->ev0);
+    if (f->ev1) cudaEventDestroy(f->ev1);
+    for (cudaEvent_t ev : f->prof.pool) cudaEventDestroy(ev);
+    if (f->stream) cudaStreamDestroy(f->stream);
+    for (Plan *p : f->tr) delete p;   // geometry only: their buffers live in the forest arena
+    for (Plan *p : f->fb_plans) plan_destroy(p);
+    delete f;
+}
+
+// nodes per tournament (its own Smax), node-major per tournament: [t][Q][3]
+static int prepare_nodes(Forest *f, int Q, std::string &err) {
+    const int F = (int)f->tr.size();
+    std::vector<double> h((size_t)F * Q * 3);
+    parallel_for(F, [&](int i) {
+        std::vector<double> logv, w;
+        make_nodes(Q, f->tr[i]->Smax, logv, w);
+        double *o = h.data() + (size_t)i * Q * 3;
+        for (int q = 0; q < Q; ++q) {
+            o[3 * q] = logv[q];
+            o[3 * q + 1] = w[q];
+            o[3 * q + 2] = std::exp(-logv[q]);
+        }
+    });
+    if (f->d_node) cudaFree(f->d_node);
+    f->d_node = nullptr;
+    cudaError_t e = cudaMalloc(&f->d_node, sizeof(double) * h.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(f->d_node, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, f->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
+    if (e != cudaSuccess) { err = std::string("node table: ") + cudaGetErrorString(e); return -1; }
+    for (int i = 0; i < F; ++i) f->tr[i]->d_node = f->d_node + (size_t)i * Q * 3;
+    return 0;
+}
+
+int forest_run(Forest *f, int Q, const double *payout, double *equity, IcmGpuRunStats *stats, std::string &err) {
+    if (!f || Q < 1 || !payout || !equity) { err = "invalid arguments"; return -1; }
+    const double t0 = now_ns();
+    f->launches = 0;
+    const int F = (int)f->tr.size();
+    cudaError_t e = cudaSuccess;
+    if (F > 0) {
+        if (Q != f->Q) {
+            if (f->graph) cudaGraphExecDestroy(f->graph);
+            f->graph = nullptr;
+            f->Q = Q;
+            if (prepare_nodes(f, Q, err) != 0) { f->Q = 0; return -1; }
+            build_steps(f);
+            if (upload_steps(f, err) != 0) { f->Q = 0; return -1; }
+        }
+        // payouts in forest order
+        if (f->compact) {
+            e = cudaMemcpyAsync(f->d_payout, payout, sizeof(double) * f->Ktot, cudaMemcpyHostToDevice, f->stream);
+        } else {
+            f->h_pay.resize(f->Ktot);
+            for (int i = 0; i < F; ++i)
+                memcpy(f->h_pay.data() + f->poff[i], payout + f->ipoff[f->tid[i]], sizeof(double) * f->tr[i]->k);
+            e = cudaMemcpyAsync(f->d_payout, f->h_pay.data(), sizeof(double) * f->Ktot, cudaMemcpyHostToDevice,
+                                f->stream);
+        }
+        if (e != cudaSuccess) { err = std::string("payout upload: ") + cudaGetErrorString(e); return -1; }
+        if (!f->ev0) { cudaEventCreate(&f->ev0); cudaEventCreate(&f->ev1); }
+        f->prof.used = 0;
+        f->prof.recs.clear();
+        const bool use_graph = f->graphs && !f->prof.on;
+        if (use_graph && !f->graph) {   // capture the kernel sequence once per node count
+            cudaGraph_t g = nullptr;
+            e = cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                enqueue_run(f);
+                e = cudaStreamEndCapture(f->stream, &g);
+            }
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&f->graph, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return -1; }
+            f->graph_launches = f->launches;
+        }
+        cudaEventRecord(f->ev0, f->stream);
+        if (use_graph) {
+            e = cudaGraphLaunch(f->graph, f->stream);
+            f->launches = f->graph_launches;
+        } else {
+            f->launches = 0;
+            enqueue_run(f);
+            e = cudaGetLastError();
+        }
+        cudaEventRecord(f->ev1, f->stream);
+        if (e != cudaSuccess) { err = std::string("batch launch: ") + cudaGetErrorString(e); return -1; }
+        if (f->compact) {
+            e = cudaMemcpyAsync(equity, f->d_out, sizeof(double) * f->Ntot, cudaMemcpyDeviceToHost, f->stream);
+        } else {
+            f->h_out.resize(f->Ntot);
+            e = cudaMemcpyAsync(f->h_out.data(), f->d_out, sizeof(double) * f->Ntot, cudaMemcpyDeviceToHost,
+                                f->stream);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
+        if (e != cudaSuccess) { err = std::string("batch execution: ") + cudaGetErrorString(e); return -1; }
+        if (!f->compact)
+            for (int i = 0; i < F; ++i)
+                memcpy(equity + f->ioff[f->tid[i]], f->h_out.data() + f->off[i], sizeof(double) * f->tr[i]->n);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, f->ev0, f->ev1);
+        f->last_device_ms = ms;
+        if (f->prof.on) {
+            for (const ProfRec &r : f->prof.recs) {
+                float ems = 0.f;
+                cudaEventElapsedTime(&ems, r.a, r.b);
+                Plan::KStat *ks = nullptr;
+                for (auto &x : f->kstats)
+                    if (x.name == r.name) ks = &x;
+                if (!ks) { f->kstats.push_back({r.name, 0.0, 0, 0.0}); ks = &f->kstats.back(); }
+                ks->ms += ems;
+                ks->launches += 1;
+                ks->flops += r.flops;
+            }
+        }
+    } else {
+        f->last_device_ms = 0.0;
+    }
+    // tournaments beyond the one-CTA kernels: single plans
+    for (size_t i = 0; i < f->fallback.size(); ++i) {
+        const int t = f->fallback[i];
+        Plan *p = f->fb_plans[i];
+        if (plan_run(p, Q, payout + f->ipoff[t], equity + f->ioff[t], nullptr, err) != 0) return -1;
+        f->launches += p->launches;
+    }
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->total_ns = now_ns() - t0;
+        stats->peak_vram_bytes = f->arena_bytes;
+        stats->engine = 1;
+    }
+    return 0;
+}
+
+}  // namespace icmg

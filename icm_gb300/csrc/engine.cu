@@ -97,21 +97,18 @@ int select_block_size(int n, int k) {
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err) {
+int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     if (n < 1 || k < 1 || k > n || !S) {
         err = "invalid plan arguments n=" + std::to_string(n) + " k=" + std::to_string(k);
-        return nullptr;
+        return -1;
     }
     for (int i = 0; i < n; ++i)
         if (!(S[i] > 0.0) || !std::isfinite(S[i])) {
             err = "stacks must be finite and positive (S[" + std::to_string(i) + "])";
-            return nullptr;
+            return -1;
         }
-    Plan *p = new Plan();
     p->n = n;
     p->k = k;
-    if (opts) p->opts = *opts;
-    p->opts.device_id = g_device;
     p->B = select_block_size(n, k);
     p->fft_min_deg = g_config.fft_min_degree > 0 ? g_config.fft_min_degree : 64;
     p->spectral = g_config.coefficient_fft_only != 1;
@@ -139,7 +136,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     p->nblocks = (n + B - 1) / B;
     const int Nt = pow2_ge(p->nblocks);
     p->L = ilog2(Nt) + 1;
-    if (p->L > kMaxLevels) { err = "tournament too large"; delete p; return nullptr; }
+    if (p->L > kMaxLevels) { err = "tournament too large"; return -1; }
     for (int l = 0; l < p->L; ++l) {
         Level &v = p->lv[l];
         v.nreal = (l == 0) ? p->nblocks : (p->lv[l - 1].nreal + 1) / 2;
@@ -196,29 +193,20 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
         }
         per_q += (v.P_q + v.g_q + v.ends_q) * 8 + (v.spec_q + v.spec2_q + v.G_q) * 16 + 1024;
     }
-    per_q += ((size_t)2 * n + (size_t)p->nblocks * (B + 1)) * 8 + 1024;
+    per_q += (size_t)p->nblocks * (B + 1) * 8 + 1024;
     per_q += (fa * 2 + fb) * 16;
+    p->tree_q_bytes = per_q;
+    p->fa_elems = fa;
+    p->fb_elems = fb;
+    return 0;
+}
 
-    size_t free_b = 0, total_b = 0;
-    cudaMemGetInfo(&free_b, &total_b);
-    size_t budget = g_config.max_device_bytes ? g_config.max_device_bytes
-                                              : std::min<size_t>((size_t)(free_b * 0.6), (size_t)48 << 30);
-    int qc = (int)std::min<size_t>(256, std::max<size_t>(1, budget / std::max<size_t>(per_q, 1)));
-    if (g_config.q_chunk > 0) qc = std::min(qc, g_config.q_chunk);
-    p->qc = qc;
-
-    // arena
+// tree buffers for chunks of qc nodes: leaf block products, per-level
+// polynomials, spectra and end coefficients, FFT work buffers
+size_t plan_tree_layout(Plan *p, int qc, char *base) {
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
-    const size_t o_S = take(sizeof(double) * n), o_perm = take(sizeof(int) * n);
-    const size_t o_pay = take(sizeof(double) * k), o_acc = take(sizeof(double) * n);
-    const size_t o_out = take(sizeof(double) * n), o_act = take(n);
-    size_t hot_total = 0;
-    for (int l = 0; l < p->L; ++l) { p->hot_off[l] = hot_total; hot_total += (size_t)(Nt >> l); }
-    const size_t o_hot = take(hot_total);
-    const size_t o_a = take(sizeof(double) * (size_t)qc * n);
-    const size_t o_bp = take(sizeof(double) * (size_t)qc * p->nblocks * (B + 1));
-    const size_t o_con = take(sizeof(double) * (size_t)qc * n);
+    const size_t o_bp = take(sizeof(double) * (size_t)qc * p->nblocks * (p->B + 1));
     size_t o_P[kMaxLevels], o_g[kMaxLevels], o_spec[kMaxLevels], o_s2[kMaxLevels], o_en[kMaxLevels],
         o_G[kMaxLevels];
     for (int l = 0; l < p->L; ++l) {
@@ -232,10 +220,60 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
         const size_t gq = (l == p->L - 1) ? 1 : (size_t)qc;
         o_G[l] = v.G_q ? take(sizeof(double2) * gq * v.G_q) : 0;
     }
-    p->fft_work = std::max(fa, fb) * qc;
+    const size_t fa = p->fa_elems, fb = p->fb_elems;
     const size_t o_fa = fa ? take(sizeof(double2) * (size_t)qc * fa) : 0;
     const size_t o_fb = fa ? take(sizeof(double2) * (size_t)qc * std::max(fa, fb)) : 0;
     const size_t o_fc = fa ? take(sizeof(double2) * (size_t)qc * fa) : 0;
+    if (!base) return off;
+    p->d_blockP = (double *)(base + o_bp);
+    for (int l = 0; l < p->L; ++l) {
+        Level &v = p->lv[l];
+        v.P = v.P_q ? (double *)(base + o_P[l]) : nullptr;
+        v.g = v.g_q ? (double *)(base + o_g[l]) : nullptr;
+        v.spec = v.spec_q ? (double2 *)(base + o_spec[l]) : nullptr;
+        v.spec2 = v.spec2_q ? (double2 *)(base + o_s2[l]) : nullptr;
+        v.ends = v.ends_q ? (double *)(base + o_en[l]) : nullptr;
+        v.G = v.G_q ? (double2 *)(base + o_G[l]) : nullptr;
+    }
+    p->fft_work = std::max(fa, fb) * qc;
+    if (fa) {
+        p->d_fa = (double2 *)(base + o_fa);
+        p->d_fb = (double2 *)(base + o_fb);
+        p->d_fc = (double2 *)(base + o_fc);
+    }
+    return off;
+}
+
+Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err) {
+    Plan *p = new Plan();
+    if (opts) p->opts = *opts;
+    p->opts.device_id = g_device;
+    if (plan_geometry(p, n, S, k, err) != 0) { delete p; return nullptr; }
+    const int B = p->B;
+    const int Nt = 1 << (p->L - 1);
+    const size_t per_q = p->tree_q_bytes + (size_t)2 * n * 8 + 1024;
+
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    size_t budget = g_config.max_device_bytes ? g_config.max_device_bytes
+                                              : std::min<size_t>((size_t)(free_b * 0.6), (size_t)48 << 30);
+    int qc = (int)std::min<size_t>(256, std::max<size_t>(1, budget / std::max<size_t>(per_q, 1)));
+    if (g_config.q_chunk > 0) qc = std::min(qc, g_config.q_chunk);
+    p->qc = qc;
+
+    // arena: per-plan arrays, then the tree buffers
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
+    const size_t o_S = take(sizeof(double) * n), o_perm = take(sizeof(int) * n);
+    const size_t o_pay = take(sizeof(double) * k), o_acc = take(sizeof(double) * n);
+    const size_t o_out = take(sizeof(double) * n), o_act = take(n);
+    size_t hot_total = 0;
+    for (int l = 0; l < p->L; ++l) { p->hot_off[l] = hot_total; hot_total += (size_t)(Nt >> l); }
+    const size_t o_hot = take(hot_total);
+    const size_t o_a = take(sizeof(double) * (size_t)qc * n);
+    const size_t o_con = take(sizeof(double) * (size_t)qc * n);
+    const size_t o_tree = take(plan_tree_layout(p, qc, nullptr));
+    (void)B;
 
     // stream-ordered allocation from the device's default pool, whose release
     // threshold icm_gpu_init raises so that freed arenas are kept for the next
@@ -263,22 +301,8 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     p->d_active = (uint8_t *)(A + o_act);
     p->d_hot = (uint8_t *)(A + o_hot);
     p->d_a = (double *)(A + o_a);
-    p->d_blockP = (double *)(A + o_bp);
     p->d_contrib = (double *)(A + o_con);
-    for (int l = 0; l < p->L; ++l) {
-        Level &v = p->lv[l];
-        v.P = v.P_q ? (double *)(A + o_P[l]) : nullptr;
-        v.g = v.g_q ? (double *)(A + o_g[l]) : nullptr;
-        v.spec = v.spec_q ? (double2 *)(A + o_spec[l]) : nullptr;
-        v.spec2 = v.spec2_q ? (double2 *)(A + o_s2[l]) : nullptr;
-        v.ends = v.ends_q ? (double *)(A + o_en[l]) : nullptr;
-        v.G = v.G_q ? (double2 *)(A + o_G[l]) : nullptr;
-    }
-    if (fa) {
-        p->d_fa = (double2 *)(A + o_fa);
-        p->d_fb = (double2 *)(A + o_fb);
-        p->d_fc = (double2 *)(A + o_fc);
-    }
+    plan_tree_layout(p, qc, A + o_tree);
     e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_perm, p->perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, p->stream);
@@ -289,7 +313,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
         return nullptr;
     }
     if (p->opts.verbose) {
-        fprintf(stderr, "icm_gb300 plan: n=%d k=%d B=%d L=%d qc=%d arena=%.1f MB\n", n, k, B, p->L, qc,
+        fprintf(stderr, "icm_gb300 plan: n=%d k=%d B=%d L=%d qc=%d arena=%.1f MB\n", n, k, p->B, p->L, qc,
                 off / 1e6);
         for (int l = 0; l < p->L; ++l) {
             const Level &v = p->lv[l];

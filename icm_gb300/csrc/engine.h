@@ -84,6 +84,8 @@ struct Plan {
     size_t hot_off[kMaxLevels] = {};
     double2 *d_fa = nullptr, *d_fb = nullptr, *d_fc = nullptr;  // FFT work buffers
     size_t fft_work = 0;            // double2 per buffer
+    size_t fa_elems = 0, fb_elems = 0;   // FFT work buffers per node (double2)
+    size_t tree_q_bytes = 0;        // tree buffers per node: block products, levels, work buffers
     bool subset = false;
     long launches = 0;
     // graph replay (enable_graphs)
@@ -105,6 +107,10 @@ struct Plan {
 };
 
 // lifecycle (engine.cu)
+// geometry only: validation, sort, levels, per-node element counts
+int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err);
+// tree buffers for chunks of qc nodes from `base` (nullptr: size only)
+size_t plan_tree_layout(Plan *p, int qc, char *base);
 Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err);
 void plan_destroy(Plan *p);
 int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &err);

@@ -33,15 +33,26 @@ static inline size_t fused_smem(int N) {
     return (size_t)cb * (N + N / 2) * sizeof(double2);
 }
 
-__global__ void __launch_bounds__(kFusedThreads)
-k_fused_build(const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc, int npairs, int logN,
-              double *__restrict__ Pp, size_t Pp_q, int pst_p, int lp, double2 *__restrict__ spec,
-              const double2 *__restrict__ tw, int logTW, int spectra_only) {
+__device__ void fused_build_body(const FusedBuildArgs &A, int bx, int q) {
+    const auto Pc = A.Pc;
+    const auto Pc_q = A.Pc_q;
+    const auto pst_c = A.pst_c;
+    const auto lc = A.lc;
+    const auto npairs = A.npairs;
+    const auto logN = A.logN;
+    const auto Pp = A.Pp;
+    const auto Pp_q = A.Pp_q;
+    const auto pst_p = A.pst_p;
+    const auto lp = A.lp;
+    const auto spec = A.spec;
+    const auto tw = A.tw;
+    const auto logTW = A.logTW;
+    const auto spectra_only = A.spectra_only;
+
     extern __shared__ double2 sm[];
     const int N = 1 << logN, h = N >> 1;
     const int cb = fused_cb(N);
-    const int q = blockIdx.y;
-    const int j0 = blockIdx.x * cb;
+        const int j0 = bx * cb;
     const int cnt = min(cb, npairs - j0);
     double2 *Z = sm;                 // cb x N
     double2 *U = sm + (size_t)cb * N; // cb x h
@@ -100,15 +111,26 @@ k_fused_build(const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc, int
     }
 }
 
-__global__ void __launch_bounds__(kFusedThreads)
-k_fused_prop(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl, int npairs, int logN,
-             const double2 *__restrict__ spec, double *__restrict__ gc, size_t gc_q, int gst_c, int gcl,
-             const uint8_t *__restrict__ hot_c, const double2 *__restrict__ tw, int logTW) {
+__device__ void fused_prop_body(const FusedPropArgs &A, int bx, int q) {
+    const auto gp = A.gp;
+    const auto gp_q = A.gp_q;
+    const auto gst_p = A.gst_p;
+    const auto gpl = A.gpl;
+    const auto npairs = A.npairs;
+    const auto logN = A.logN;
+    const auto spec = A.spec;
+    const auto gc = A.gc;
+    const auto gc_q = A.gc_q;
+    const auto gst_c = A.gst_c;
+    const auto gcl = A.gcl;
+    const auto hot_c = A.hot_c;
+    const auto tw = A.tw;
+    const auto logTW = A.logTW;
+
     extern __shared__ double2 sm[];
     const int N = 1 << logN, h = N >> 1;
     const int cb = fused_cb(N);
-    const int q = blockIdx.y;
-    const int j0 = blockIdx.x * cb;
+        const int j0 = bx * cb;
     const int cnt = min(cb, npairs - j0);
     double2 *Z = sm;                  // cb x N
     double2 *W = sm + (size_t)cb * N; // cb x h
@@ -167,12 +189,21 @@ k_fused_prop(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl, int
     }
 }
 
+__global__ void __launch_bounds__(kFusedThreads) k_fused_build(FusedBuildArgs A) { fused_build_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kFusedThreads) k_fused_prop(FusedPropArgs A) { fused_prop_body(A, blockIdx.x, blockIdx.y); }
+
+size_t fused_smem_bytes(int N) { return fused_smem(N); }
+__global__ void kw_fused_build(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ tab);
+__global__ void kw_fused_prop(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ tab);
+
 bool fused_ok(int N) { return N >= 8 && N <= kFusedMaxN; }
 
 void fused_set_smem_limits() {
     const int mx = (int)fused_smem(kFusedMaxN);
     cudaFuncSetAttribute(k_fused_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fused_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_fused_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_fused_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
 static int ilog2i(int v) {
@@ -181,29 +212,68 @@ static int ilog2i(int v) {
     return l;
 }
 
-void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_only, const double2 *tw, int logTW,
-                        cudaStream_t st, Prof *pr) {
+FusedBuildArgs fused_build_args(const Level &c, const Level &p, bool spectra_only, const double2 *tw, int logTW,
+                                double *fq, size_t *smem) {
     const int N = p.fftn, logN = ilog2i(N);
     const int cb = N >= 8192 ? 1 : 4096 / N;
-    dim3 g((p.npairs + cb - 1) / cb, nq);
     // transforms: forward N (5 N log N) and inverse N/2; spectra/product ~40 flops per bin
-    const double per = 5.0 * N * logN + (spectra_only ? 8.0 : 40.0 + 2.5 * logN) * (N / 2);
-    pr->begin(spectra_only ? "fused_spectra" : "fused_build", per * p.npairs * (double)nq, st);
-    k_fused_build<<<g, kFusedThreads, fused_smem(N), st>>>(c.P, c.P_q, c.pst, c.plen, p.npairs, logN, p.P, p.P_q,
-                                                          p.pst, p.plen, p.spec, tw, logTW, spectra_only ? 1 : 0);
+    if (fq) *fq = (5.0 * N * logN + (spectra_only ? 8.0 : 40.0 + 2.5 * logN) * (N / 2)) * p.npairs;
+    if (smem) *smem = fused_smem(N);
+    return FusedBuildArgs{c.P, c.P_q, c.pst, c.plen, p.npairs, logN, p.P, p.P_q, p.pst, p.plen, p.spec, tw, logTW,
+                          spectra_only ? 1 : 0, (p.npairs + cb - 1) / cb};
+}
+
+FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p,
+                              const uint8_t *hot_c, const double2 *tw, int logTW, double *fq, size_t *smem) {
+    const int N = p.fftn, logN = ilog2i(N);
+    const int cb = N >= 8192 ? 1 : 4096 / N;
+    if (fq) *fq = (5.0 * N * logN + 2.5 * N * (logN - 1) + 40.0 * (N / 2)) * p.npairs;
+    if (smem) *smem = fused_smem(N);
+    return FusedPropArgs{gp, gp_q, gst_p, gpl, p.npairs, logN, p.spec, c.g, c.g_q, c.gst, c.glen, hot_c, tw, logTW,
+                         (p.npairs + cb - 1) / cb};
+}
+
+void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_only, const double2 *tw, int logTW,
+                        cudaStream_t st, Prof *pr) {
+    double fq = 0.0;
+    size_t sm = 0;
+    FusedBuildArgs A = fused_build_args(c, p, spectra_only, tw, logTW, &fq, &sm);
+    pr->begin(spectra_only ? "fused_spectra" : "fused_build", fq * nq, st);
+    k_fused_build<<<dim3(A.nbx, nq), kFusedThreads, sm, st>>>(A);
     pr->end(st);
 }
 
 void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
                        const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr) {
-    const int N = p.fftn, logN = ilog2i(N);
-    const int cb = N >= 8192 ? 1 : 4096 / N;
-    dim3 g((p.npairs + cb - 1) / cb, nq);
-    const double per = 5.0 * N * logN + 2.5 * N * (logN - 1) + 40.0 * (N / 2);
-    pr->begin("fused_prop", per * p.npairs * (double)nq, st);
-    k_fused_prop<<<g, kFusedThreads, fused_smem(N), st>>>(gp, gp_q, gst_p, gpl, p.npairs, logN, p.spec, c.g, c.g_q,
-                                                         c.gst, c.glen, hot_c, tw, logTW);
+    double fq = 0.0;
+    size_t sm = 0;
+    FusedPropArgs A = fused_prop_args(gp, gp_q, gst_p, gpl, c, p, hot_c, tw, logTW, &fq, &sm);
+    pr->begin("fused_prop", fq * nq, st);
+    k_fused_prop<<<dim3(A.nbx, nq), kFusedThreads, sm, st>>>(A);
     pr->end(st);
+}
+
+// ---------------------------------------------------------------- work lists
+__global__ void __launch_bounds__(kFusedThreads)
+kw_fused_build(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ tab) {
+    const int2 t = tab[blockIdx.x];
+    fused_build_body(D[t.x], t.y, blockIdx.y);
+}
+__global__ void __launch_bounds__(kFusedThreads)
+kw_fused_prop(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ tab) {
+    const int2 t = tab[blockIdx.x];
+    fused_prop_body(D[t.x], t.y, blockIdx.y);
+}
+
+void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, size_t smem,
+                           cudaStream_t st) {
+    if (nctas <= 0 || nq <= 0) return;
+    const dim3 g(nctas, nq);
+    switch (op) {
+        case WOp::FusedBuild: kw_fused_build<<<g, kFusedThreads, smem, st>>>((const FusedBuildArgs *)desc, tab); break;
+        case WOp::FusedProp: kw_fused_prop<<<g, kFusedThreads, smem, st>>>((const FusedPropArgs *)desc, tab); break;
+        default: break;
+    }
 }
 
 }  // namespace icmg

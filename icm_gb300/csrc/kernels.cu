@@ -26,22 +26,20 @@ namespace icmg {
 // every player adds exact zeros above the running degree, so the result is
 // the reference's recurrence P[m] = a P[m] + (1-a) P[m-1] bit for bit.
 template <int B>
-__global__ void k_leaf(int n, int nblocks, const double *__restrict__ S, const double *__restrict__ node,
-                       int q0, double *__restrict__ a_out, double *__restrict__ blockP,
-                       double *__restrict__ P0, int pst0, int plen0) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
-    if (b >= nblocks) return;
-    const double logv = node[3 * (q0 + q)];
+__device__ __forceinline__ void leaf_body_t(const LeafArgs &A, int bx, int q) {
+    const int b = bx * blockDim.x + threadIdx.x;
+    if (b >= A.nblocks) return;
+    const int n = A.n, nblocks = A.nblocks;
+    const double logv = A.node[3 * (A.q0 + q)];
     const int start = b * B;
     const int bs = min(B, n - start);
     double P[B + 1];
     P[0] = 1.0;
 #pragma unroll
     for (int m = 1; m <= B; ++m) P[m] = 0.0;
-    double *arow = a_out + (size_t)q * n + start;
+    double *arow = A.a + (size_t)q * A.aq + start;
     for (int j = 0; j < bs; ++j) {
-        const double arg = S[start + j] * logv;
+        const double arg = A.S[start + j] * logv;
         const double a = (arg < -700.0) ? 0.0 : exp(arg);
         arow[j] = a;
         const double bb = 1.0 - a;
@@ -49,31 +47,42 @@ __global__ void k_leaf(int n, int nblocks, const double *__restrict__ S, const d
         for (int m = B; m >= 1; --m) P[m] = a * P[m] + bb * P[m - 1];
         P[0] *= a;
     }
-    double *bp = blockP + ((size_t)q * nblocks + b) * (B + 1);
+    double *bp = A.blockP + ((size_t)q * nblocks + b) * (B + 1);
 #pragma unroll
     for (int m = 0; m <= B; ++m) bp[m] = P[m];
-    double *leaf = P0 + ((size_t)q * nblocks + b) * pst0;
+    const int pst0 = A.pst0, plen0 = A.plen0;
+    double *leaf = A.P0 + ((size_t)q * nblocks + b) * pst0;
 #pragma unroll
     for (int m = 0; m <= B; ++m)
         if (m < pst0) leaf[m] = (m < plen0) ? P[m] : 0.0;
     for (int m = B + 1; m < pst0; ++m) leaf[m] = 0.0;
 }
 
+__device__ void leaf_body(const LeafArgs &A, int bx, int q) {
+    switch (A.B) {
+        case 4: leaf_body_t<4>(A, bx, q); break;
+        case 8: leaf_body_t<8>(A, bx, q); break;
+        case 16: leaf_body_t<16>(A, bx, q); break;
+        default: leaf_body_t<32>(A, bx, q); break;
+    }
+}
+
+__global__ void k_leaf(LeafArgs A) { leaf_body(A, blockIdx.x, blockIdx.y); }
+
 // ------------------------------------------------------- schoolbook build
 // parent j = L*R mod x^lp, children of length lc (reference icm.c:465-480).
 // One thread per output coefficient; parents >= j0 only (the FFT path uses
 // j0 = npairs to let this kernel copy a lone left child).
-__global__ void k_school_build(const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc, int nreal_c,
-                               double *__restrict__ Pp, size_t Pp_q, int pst_p, int lp, int nreal_p, int j0) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
-    const int j = j0 + (int)(idx / pst_p);
+__device__ void school_build_body(const SchoolBuildArgs &A, int bx, int q) {
+    const long idx = (long)bx * blockDim.x + threadIdx.x;
+    const int pst_p = A.pst_p, pst_c = A.pst_c, lc = A.lc;
+    const int j = A.j0 + (int)(idx / pst_p);
     const int t = (int)(idx % pst_p);
-    if (j >= nreal_p) return;
-    const double *L = Pc + q * Pc_q + (size_t)(2 * j) * pst_c;
-    double *out = Pp + q * Pp_q + (size_t)j * pst_p;
-    if (t >= lp) { out[t] = 0.0; return; }
-    if (2 * j + 1 >= nreal_c) { out[t] = (t < lc) ? L[t] : 0.0; return; }
+    if (j >= A.nreal_p) return;
+    const double *L = A.Pc + q * A.Pc_q + (size_t)(2 * j) * pst_c;
+    double *out = A.Pp + q * A.Pp_q + (size_t)j * pst_p;
+    if (t >= A.lp) { out[t] = 0.0; return; }
+    if (2 * j + 1 >= A.nreal_c) { out[t] = (t < lc) ? L[t] : 0.0; return; }
     const double *R = L + pst_c;
     const int ilo = max(0, t - (lc - 1));
     const int ihi = min(t, lc - 1);
@@ -82,30 +91,32 @@ __global__ void k_school_build(const double *__restrict__ Pc, size_t Pc_q, int p
     out[t] = s;
 }
 
+__global__ void k_school_build(SchoolBuildArgs A) { school_build_body(A, blockIdx.x, blockIdx.y); }
+
 // --------------------------------------------------- schoolbook propagate
 // g_c[m] = sum_i P_sib[i] g_parent[m+i] (reference icm.c:489-507, 1667-1819).
 // One thread per child coefficient, children >= c0 only.  gp_q == 0 lets the
 // root's g be the payout vector shared by all nodes.
-__global__ void k_school_prop(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl,
-                              const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc,
-                              double *__restrict__ gc, size_t gc_q, int gst_c, int gcl, int nreal_c,
-                              const uint8_t *__restrict__ hot_c, int c0) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
-    const int c = c0 + (int)(idx / gst_c);
+__device__ void school_prop_body(const SchoolPropArgs &A, int bx, int q) {
+    const long idx = (long)bx * blockDim.x + threadIdx.x;
+    const int gst_c = A.gst_c;
+    const int c = A.c0 + (int)(idx / gst_c);
     const int m = (int)(idx % gst_c);
-    if (c >= nreal_c) return;
-    double *out = gc + q * gc_q + (size_t)c * gst_c;
-    if (m >= gcl || (hot_c && !hot_c[c])) { out[m] = 0.0; return; }
-    const double *g = gp + q * gp_q + (size_t)(c >> 1) * gst_p;
+    if (c >= A.nreal_c) return;
+    double *out = A.gc + q * A.gc_q + (size_t)c * gst_c;
+    if (m >= A.gcl || (A.hot_c && !A.hot_c[c])) { out[m] = 0.0; return; }
+    const double *g = A.gp + q * A.gp_q + (size_t)(c >> 1) * A.gst_p;
     const int sib = c ^ 1;
-    if (sib >= nreal_c) { out[m] = (m < gpl) ? g[m] : 0.0; return; }
-    const double *P = Pc + q * Pc_q + (size_t)sib * pst_c;
-    const int imax = min(lc, gpl - m);
+    const int gpl = A.gpl;
+    if (sib >= A.nreal_c) { out[m] = (m < gpl) ? g[m] : 0.0; return; }
+    const double *P = A.Pc + q * A.Pc_q + (size_t)sib * A.pst_c;
+    const int imax = min(A.lc, gpl - m);
     double s = 0.0;
     for (int i = 0; i < imax; ++i) s = fma(P[i], g[m + i], s);
     out[m] = s;
 }
+
+__global__ void k_school_prop(SchoolPropArgs A) { school_prop_body(A, blockIdx.x, blockIdx.y); }
 
 // --------------------------------------------------------- divide + dot
 // Per player: Q_i = P_block / (a_i + (1-a_i) x) by the forward recurrence
@@ -113,23 +124,22 @@ __global__ void k_school_prop(const double *__restrict__ gp, size_t gp_q, int gs
 // inner_i = sum_{m < min(bs,k)} g_block[m] Q_i[m] and the node's weight
 // (reference icm.c:2230-2302 and 2584-2589).
 template <int B>
-__global__ void k_divide(int n, int k, int nblocks, const double *__restrict__ S, const double *__restrict__ node,
-                         int q0, const double *__restrict__ a_in, const double *__restrict__ blockP,
-                         const double *__restrict__ g0, size_t g0_q, int gst0,
-                         const uint8_t *__restrict__ active, double *__restrict__ contrib) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
+__device__ __forceinline__ void divide_body_t(const DivideArgs &A, int bx, int q) {
+    const int i = bx * blockDim.x + threadIdx.x;
+    const int n = A.n;
     if (i >= n) return;
-    double *out = contrib + (size_t)q * n + i;
-    if (active && !active[i]) { *out = 0.0; return; }
+    double *out = A.contrib + (size_t)q * A.aq + i;
+    if (A.active && !A.active[i]) { *out = 0.0; return; }
+    const double *nd = A.node + 3 * (A.q0 + q);
+    if (nd[1] == 0.0) { *out = 0.0; return; }   // zero-weight node (the reference skips it)
     const int b = i / B;
     const int start = b * B;
     const int bs = min(B, n - start);
-    const int pk = min(bs, k);
-    const double a = a_in[(size_t)q * n + i];
+    const int pk = min(bs, A.k);
+    const double a = A.a[(size_t)q * A.aq + i];
     const double bb = 1.0 - a;
-    const double *P = blockP + ((size_t)q * nblocks + b) * (B + 1);
-    const double *g = g0 + q * g0_q + (size_t)b * gst0;
+    const double *P = A.blockP + ((size_t)q * A.nblocks + b) * (B + 1);
+    const double *g = A.g0 + q * A.g0_q + (size_t)b * A.gst0;
     double eq = 0.0;
     if (a > 0.5) {
         const double ia = 1.0 / a, c = -bb * ia;
@@ -152,11 +162,21 @@ __global__ void k_divide(int n, int k, int nblocks, const double *__restrict__ S
     } else {
         for (int m = 0; m < pk; ++m) eq += g[m] * P[m + 1];
     }
-    const double *nd = node + 3 * (q0 + q);
-    double pw = nd[1] * S[i] * a * nd[2];
+    double pw = nd[1] * A.S[i] * a * nd[2];
     if (!isfinite(pw)) pw = 0.0;
     *out = pw * eq;
 }
+
+__device__ void divide_body(const DivideArgs &A, int bx, int q) {
+    switch (A.B) {
+        case 4: divide_body_t<4>(A, bx, q); break;
+        case 8: divide_body_t<8>(A, bx, q); break;
+        case 16: divide_body_t<16>(A, bx, q); break;
+        default: divide_body_t<32>(A, bx, q); break;
+    }
+}
+
+__global__ void k_divide(DivideArgs A) { divide_body(A, blockIdx.x, blockIdx.y); }
 
 // ordered sum over the chunk's nodes: deterministic for a fixed chunking
 __global__ void k_accumulate(int n, int nq, const double *__restrict__ contrib, double *__restrict__ acc,
@@ -434,64 +454,131 @@ __global__ void k_prop_post(const double2 *__restrict__ Z, int npairs, int N, do
 // ------------------------------------------------------------ launchers
 static inline unsigned nblk(long work, int threads) { return (unsigned)((work + threads - 1) / threads); }
 
+LeafArgs leaf_args(int B, int n, int nblocks, const double *S, const double *node, double *a, size_t aq,
+                   double *blockP, double *P0, int pst0, int plen0, double *fq) {
+    LeafArgs A{};
+    A.B = B; A.n = n; A.nblocks = nblocks; A.S = S; A.node = node; A.q0 = 0;
+    A.a = a; A.blockP = blockP; A.P0 = P0; A.pst0 = pst0; A.plen0 = plen0;
+    A.nbx = (int)nblk(nblocks, 128);
+    A.aq = aq;
+    if (fq) {   // reference recurrence: per player bs coefficient updates (2 mul + 1 add) and P[0] *= a
+        const int r = n % B;
+        *fq = (double)(n / B) * B * (3.0 * B + 1.0) + (double)r * (3.0 * r + 1.0);
+    }
+    return A;
+}
+
+DivideArgs divide_args(int B, int n, int k, int nblocks, const double *S, const double *node, const double *a,
+                       size_t aq, const double *blockP, const double *g0, size_t g0_q, int gst0, const uint8_t *active,
+                       double *contrib, double *fq) {
+    DivideArgs A{};
+    A.B = B; A.n = n; A.k = k; A.nblocks = nblocks; A.S = S; A.node = node; A.q0 = 0;
+    A.a = a; A.blockP = blockP; A.g0 = g0; A.g0_q = g0_q; A.gst0 = gst0; A.active = active; A.contrib = contrib;
+    A.nbx = (int)nblk(n, 128);
+    A.aq = aq;
+    if (fq) *fq = (double)n * (5.0 * std::min(B, k) + 4.0);   // divide 3 + dot 2 per term, weight 4
+    return A;
+}
+
+SchoolBuildArgs school_build_args(const Level &c, const Level &p, int j0, double *fq) {
+    const long work = (long)(p.nreal - j0) * p.pst;
+    SchoolBuildArgs A{c.P, c.P_q, c.pst, c.plen, c.nreal, p.P, p.P_q, p.pst, p.plen, p.nreal, j0,
+                      work > 0 ? (int)nblk(work, 256) : 0};
+    if (fq) {
+        double terms = 0.0;   // multiply-adds of one full pair: sum_t (ihi - ilo + 1)
+        for (int t = 0; t < p.plen; ++t) terms += std::min(t, c.plen - 1) - std::max(0, t - (c.plen - 1)) + 1;
+        const long pairs = std::max(0, std::min(p.nreal, c.nreal / 2) - j0);
+        *fq = 2.0 * terms * pairs;
+    }
+    return A;
+}
+
+SchoolPropArgs school_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const uint8_t *hot_c,
+                                int c0, double *fq) {
+    const long work = (long)(c.nreal - c0) * c.gst;
+    SchoolPropArgs A{gp, gp_q, gst_p, gpl, c.P, c.P_q, c.pst, c.plen, c.g, c.g_q, c.gst, c.glen, c.nreal, hot_c, c0,
+                     work > 0 ? (int)nblk(work, 256) : 0};
+    if (fq) {
+        double terms = 0.0;   // per child with a sibling: sum_m min(lc, gpl - m)
+        for (int m = 0; m < c.glen; ++m) terms += std::max(0, std::min(c.plen, gpl - m));
+        const long kids = std::max(0, 2 * (c.nreal / 2) - c0);
+        *fq = 2.0 * terms * kids;
+    }
+    return A;
+}
+
 void launch_leaf(int B, int n, int nblocks, const double *S, const double *node, int q0, int nq, double *a,
                  double *blockP, double *P0, int pst0, int plen0, cudaStream_t st, Prof *pr) {
-    dim3 g(nblk(nblocks, 128), nq);
-    {   // reference recurrence: per player bs coefficient updates (2 mul + 1 add) and P[0] *= a
-        const double full = (double)(n / B) * B * (3.0 * B + 1.0);
-        const int r = n % B;
-        pr->begin("leaf", (double)nq * (full + (double)r * (3.0 * r + 1.0)), st);
-    }
-    switch (B) {
-        case 4: k_leaf<4><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
-        case 8: k_leaf<8><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
-        case 16: k_leaf<16><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
-        default: k_leaf<32><<<g, 128, 0, st>>>(n, nblocks, S, node, q0, a, blockP, P0, pst0, plen0); break;
-    }
+    double fq = 0.0;
+    LeafArgs A = leaf_args(B, n, nblocks, S, node, a, (size_t)n, blockP, P0, pst0, plen0, &fq);
+    A.q0 = q0;
+    pr->begin("leaf", fq * nq, st);
+    k_leaf<<<dim3(A.nbx, nq), 128, 0, st>>>(A);
     pr->end(st);
 }
 
 void launch_divide(int B, int n, int k, int nblocks, const double *S, const double *node, int q0, int nq,
                    const double *a, const double *blockP, const double *g0, size_t g0_q, int gst0,
                    const uint8_t *active, double *contrib, cudaStream_t st, Prof *pr) {
-    dim3 g(nblk(n, 128), nq);
-    {   // divide (3 flops per term) + dot (2 per term) + weight (4)
-        const int pk = std::min(B, k);
-        pr->begin("divide", (double)nq * n * (5.0 * pk + 4.0), st);
-    }
-    switch (B) {
-        case 4: k_divide<4><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
-        case 8: k_divide<8><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
-        case 16: k_divide<16><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
-        default: k_divide<32><<<g, 128, 0, st>>>(n, k, nblocks, S, node, q0, a, blockP, g0, g0_q, gst0, active, contrib); break;
-    }
+    double fq = 0.0;
+    DivideArgs A = divide_args(B, n, k, nblocks, S, node, a, (size_t)n, blockP, g0, g0_q, gst0, active, contrib, &fq);
+    A.q0 = q0;
+    pr->begin("divide", fq * nq, st);
+    k_divide<<<dim3(A.nbx, nq), 128, 0, st>>>(A);
     pr->end(st);
 }
 
 void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStream_t st, Prof *pr) {
-    const long work = (long)(p.nreal - j0) * p.pst;
-    if (work <= 0) return;
-    dim3 g(nblk(work, 256), nq);
-    double terms = 0.0;   // multiply-adds of one full pair: sum_t (ihi - ilo + 1)
-    for (int t = 0; t < p.plen; ++t) terms += std::min(t, c.plen - 1) - std::max(0, t - (c.plen - 1)) + 1;
-    const long pairs = std::max(0, std::min(p.nreal, c.nreal / 2) - j0);
-    pr->begin("school_build", 2.0 * terms * pairs * nq, st);
-    k_school_build<<<g, 256, 0, st>>>(c.P, c.P_q, c.pst, c.plen, c.nreal, p.P, p.P_q, p.pst, p.plen, p.nreal, j0);
+    double fq = 0.0;
+    SchoolBuildArgs A = school_build_args(c, p, j0, &fq);
+    if (A.nbx <= 0) return;
+    pr->begin("school_build", fq * nq, st);
+    k_school_build<<<dim3(A.nbx, nq), 256, 0, st>>>(A);
     pr->end(st);
 }
 
 void launch_school_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, int nq,
                         const uint8_t *hot_c, int c0, cudaStream_t st, Prof *pr) {
-    const long work = (long)(c.nreal - c0) * c.gst;
-    if (work <= 0) return;
-    dim3 g(nblk(work, 256), nq);
-    double terms = 0.0;   // per child with a sibling: sum_m min(lc, gpl - m)
-    for (int m = 0; m < c.glen; ++m) terms += std::max(0, std::min(c.plen, gpl - m));
-    const long kids = std::max(0, 2 * (c.nreal / 2) - c0);
-    pr->begin("school_prop", 2.0 * terms * kids * nq, st);
-    k_school_prop<<<g, 256, 0, st>>>(gp, gp_q, gst_p, gpl, c.P, c.P_q, c.pst, c.plen, c.g, c.g_q, c.gst, c.glen,
-                                     c.nreal, hot_c, c0);
+    double fq = 0.0;
+    SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, c, hot_c, c0, &fq);
+    if (A.nbx <= 0) return;
+    pr->begin("school_prop", fq * nq, st);
+    k_school_prop<<<dim3(A.nbx, nq), 256, 0, st>>>(A);
     pr->end(st);
+}
+
+// ---------------------------------------------------------------- work lists
+__global__ void kw_leaf(const LeafArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    LeafArgs A = D[t.x];
+    A.q0 = q0;
+    leaf_body(A, t.y, blockIdx.y);
+}
+__global__ void kw_divide(const DivideArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    DivideArgs A = D[t.x];
+    A.q0 = q0;
+    divide_body(A, t.y, blockIdx.y);
+}
+__global__ void kw_school_build(const SchoolBuildArgs *__restrict__ D, const int2 *__restrict__ tab) {
+    const int2 t = tab[blockIdx.x];
+    school_build_body(D[t.x], t.y, blockIdx.y);
+}
+__global__ void kw_school_prop(const SchoolPropArgs *__restrict__ D, const int2 *__restrict__ tab) {
+    const int2 t = tab[blockIdx.x];
+    school_prop_body(D[t.x], t.y, blockIdx.y);
+}
+
+void launch_worklist_basic(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, cudaStream_t st) {
+    if (nctas <= 0 || nq <= 0) return;
+    const dim3 g(nctas, nq);
+    switch (op) {
+        case WOp::Leaf: kw_leaf<<<g, 128, 0, st>>>((const LeafArgs *)desc, tab, q0); break;
+        case WOp::Divide: kw_divide<<<g, 128, 0, st>>>((const DivideArgs *)desc, tab, q0); break;
+        case WOp::SchoolBuild: kw_school_build<<<g, 256, 0, st>>>((const SchoolBuildArgs *)desc, tab); break;
+        case WOp::SchoolProp: kw_school_prop<<<g, 256, 0, st>>>((const SchoolPropArgs *)desc, tab); break;
+        default: break;
+    }
 }
 
 void launch_accumulate(int n, int nq, const double *contrib, double *acc, int first, cudaStream_t st, Prof *pr) {

@@ -42,6 +42,172 @@ struct Prof {
     }
 };
 
+// ---- kernel argument blocks.  Each kernel body is a __device__ function of
+// (args, bx, q): bx the block index within one tree level of one tournament,
+// q the quadrature node within the chunk.  Single plans launch it with
+// grid (nbx, nq); batches of tournaments launch one work list per level
+// (batch.cu) whose blocks map to (tournament level, bx, q).
+struct LeafArgs {
+    int B, n, nblocks;
+    const double *S, *node;
+    int q0;
+    double *a, *blockP, *P0;
+    int pst0, plen0;
+    int nbx;
+    size_t aq;          // per-node stride of a (n for one tournament)
+};
+struct SchoolBuildArgs {
+    const double *Pc;
+    size_t Pc_q;
+    int pst_c, lc, nreal_c;
+    double *Pp;
+    size_t Pp_q;
+    int pst_p, lp, nreal_p, j0;
+    int nbx;
+};
+struct SchoolPropArgs {
+    const double *gp;
+    size_t gp_q;
+    int gst_p, gpl;
+    const double *Pc;
+    size_t Pc_q;
+    int pst_c, lc;
+    double *gc;
+    size_t gc_q;
+    int gst_c, gcl, nreal_c;
+    const uint8_t *hot_c;
+    int c0;
+    int nbx;
+};
+struct DivideArgs {
+    int B, n, k, nblocks;
+    const double *S, *node;
+    int q0;
+    const double *a, *blockP, *g0;
+    size_t g0_q;
+    int gst0;
+    const uint8_t *active;
+    double *contrib;
+    int nbx;
+    size_t aq;          // per-node stride of a and contrib
+};
+
+struct SpecInitArgs {
+    const double *P;
+    size_t P_q;
+    int pst, plen, nreal, logd;
+    double2 *spec2;
+    size_t s2_q;
+    double *ends;
+    size_t e_q;
+    const double2 *tw;
+    int logTW;
+    int nbx;
+};
+struct SpecBuildArgs {
+    const double2 *cspec;
+    size_t cs_q;
+    const double *cends;
+    size_t ce_q;
+    int nreal_c, nreal_p, logD;
+    double2 *pspec;
+    size_t ps_q;
+    double *pends;
+    size_t pe_q;
+    double *Pout;
+    size_t Po_q;
+    int pst_p, plen_p;
+    const double2 *tw;
+    int logTW;
+    int nbx;
+};
+struct GspecArgs {
+    const double *g;
+    size_t g_q;
+    int gst, glen, nreal, logd;
+    double2 *G;
+    size_t G_q;
+    const uint8_t *hot;
+    const double2 *tw;
+    int logTW;
+    int nbx;
+};
+struct SpecPropArgs {
+    const double2 *Gp;
+    size_t Gp_q;
+    const double2 *cspec;
+    size_t cs_q;
+    int nreal_c, npar, logD;
+    double2 *Gout;
+    size_t Go_q;
+    double *gout;
+    size_t go_q;
+    int gst_c, glen_c;
+    const uint8_t *hot_c;
+    const double2 *tw;
+    int logTW;
+    int nbx;
+};
+struct FusedBuildArgs {
+    const double *Pc;
+    size_t Pc_q;
+    int pst_c, lc, npairs, logN;
+    double *Pp;
+    size_t Pp_q;
+    int pst_p, lp;
+    double2 *spec;
+    const double2 *tw;
+    int logTW, spectra_only;
+    int nbx;
+};
+struct FusedPropArgs {
+    const double *gp;
+    size_t gp_q;
+    int gst_p, gpl, npairs, logN;
+    const double2 *spec;
+    double *gc;
+    size_t gc_q;
+    int gst_c, gcl;
+    const uint8_t *hot_c;
+    const double2 *tw;
+    int logTW;
+    int nbx;
+};
+
+// ---- argument builders shared by the single-plan launchers and the work
+// lists.  Each fills its block count per node (nbx; 0 = no work), the
+// dynamic shared memory where the kernel uses some, and the algorithmic FP64
+// flops per node (*fq).  Leaf and divide take the node offset at launch.
+LeafArgs leaf_args(int B, int n, int nblocks, const double *S, const double *node, double *a, size_t aq,
+                   double *blockP, double *P0, int pst0, int plen0, double *fq);
+DivideArgs divide_args(int B, int n, int k, int nblocks, const double *S, const double *node, const double *a,
+                       size_t aq, const double *blockP, const double *g0, size_t g0_q, int gst0, const uint8_t *active,
+                       double *contrib, double *fq);
+SchoolBuildArgs school_build_args(const Level &c, const Level &p, int j0, double *fq);
+SchoolPropArgs school_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const uint8_t *hot_c,
+                                int c0, double *fq);
+SpecInitArgs spec_init_args(const Level &v, const double2 *tw, int logTW, double *fq, size_t *smem);
+SpecBuildArgs spec_build_args(const Level &c, const Level &p, bool write_coeffs, const double2 *tw, int logTW,
+                              double *fq, size_t *smem);
+GspecArgs gspec_args(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G, size_t G_q,
+                     const uint8_t *hot, const double2 *tw, int logTW, double *fq, size_t *smem);
+SpecPropArgs spec_prop_args(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral,
+                            const uint8_t *hot_c, const double2 *tw, int logTW, double *fq, size_t *smem);
+FusedBuildArgs fused_build_args(const Level &c, const Level &p, bool spectra_only, const double2 *tw, int logTW,
+                                double *fq, size_t *smem);
+FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p,
+                              const uint8_t *hot_c, const double2 *tw, int logTW, double *fq, size_t *smem);
+
+// ---- work lists (batch.cu drives them).  One launch runs one kind of step
+// for many tournaments: grid (nctas, nq), tab[blockIdx.x] = (descriptor,
+// block within the descriptor), blockIdx.y = node within the chunk.
+enum class WOp : int { Leaf, SchoolBuild, SchoolProp, Divide, SpecInit, SpecBuild, Gspec, SpecProp, FusedBuild, FusedProp };
+void launch_worklist_basic(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, cudaStream_t st);
+void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, size_t smem, cudaStream_t st);
+void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, size_t smem, cudaStream_t st);
+size_t spec_smem_bytes(int M);     // dynamic shared memory of the spectral kernels
+size_t fused_smem_bytes(int N);    // dynamic shared memory of the fused kernels
+
 void fft_set_smem_limits();
 
 // one-kernel FFT levels (fused.cu), used when the level's real FFT size fits

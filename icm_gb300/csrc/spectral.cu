@@ -47,15 +47,24 @@ __device__ __forceinline__ double2 twl(const double2 *__restrict__ tw, long idx)
 // ---------------------------------------------------------------------------
 // spec2 and ends of nodes given by coefficients: real FFT of size 2d through
 // a complex transform of size d.  cb nodes per CTA.
-__global__ void __launch_bounds__(kSpecThreads)
-k_spec_init(const double *__restrict__ P, size_t P_q, int pst, int plen, int nreal, int logd,
-            double2 *__restrict__ spec2, size_t s2_q, double *__restrict__ ends, size_t e_q,
-            const double2 *__restrict__ tw, int logTW) {
+__device__ void spec_init_body(const SpecInitArgs &A, int bx, int q) {
+    const auto P = A.P;
+    const auto P_q = A.P_q;
+    const auto pst = A.pst;
+    const auto plen = A.plen;
+    const auto nreal = A.nreal;
+    const auto logd = A.logd;
+    const auto spec2 = A.spec2;
+    const auto s2_q = A.s2_q;
+    const auto ends = A.ends;
+    const auto e_q = A.e_q;
+    const auto tw = A.tw;
+    const auto logTW = A.logTW;
+
     extern __shared__ double2 sm[];
     const int d = 1 << logd;
     const int cb = d >= 4096 ? 1 : 4096 / d;
-    const int q = blockIdx.y;
-    const int j0 = blockIdx.x * cb;
+        const int j0 = bx * cb;
     const int cnt = min(cb, nreal - j0);
     if (cnt <= 0) return;
     for (int e = threadIdx.x; e < cnt * d; e += blockDim.x) {
@@ -99,17 +108,30 @@ k_spec_init(const double *__restrict__ P, size_t P_q, int pst, int plen, int nre
 // and the odd output bins of a mirror pair (f, D-1-f) are
 //   H(f) = (Ep + T) / 4D,  H(D-1-f) = conj(Ep - T) / 4D,
 //   Ep = c[f] + conj c[D-1-f],  T = -i (c[f] - conj c[D-1-f]) e^{-2 pi i (2f+1)/4D}.
-__global__ void __launch_bounds__(kSpecThreads)
-k_spec_build(const double2 *__restrict__ cspec, size_t cs_q, const double *__restrict__ cends, size_t ce_q,
-             int nreal_c, int nreal_p, int logD, double2 *__restrict__ pspec, size_t ps_q,
-             double *__restrict__ pends, size_t pe_q, double *__restrict__ Pout, size_t Po_q, int pst_p, int plen_p,
-             const double2 *__restrict__ tw, int logTW) {
+__device__ void spec_build_body(const SpecBuildArgs &A, int bx, int q) {
+    const auto cspec = A.cspec;
+    const auto cs_q = A.cs_q;
+    const auto cends = A.cends;
+    const auto ce_q = A.ce_q;
+    const auto nreal_c = A.nreal_c;
+    const auto nreal_p = A.nreal_p;
+    const auto logD = A.logD;
+    const auto pspec = A.pspec;
+    const auto ps_q = A.ps_q;
+    const auto pends = A.pends;
+    const auto pe_q = A.pe_q;
+    const auto Pout = A.Pout;
+    const auto Po_q = A.Po_q;
+    const auto pst_p = A.pst_p;
+    const auto plen_p = A.plen_p;
+    const auto tw = A.tw;
+    const auto logTW = A.logTW;
+
     extern __shared__ double2 sm[];
     const int D = 1 << logD;
     const int hD = D >> 1;
     const int cb = D >= 4096 ? 1 : 4096 / D;
-    const int q = blockIdx.y;
-    const int j0 = blockIdx.x * cb;
+        const int j0 = bx * cb;
     const int cnt = min(cb, nreal_p - j0);
     if (cnt <= 0) return;
     const double2 one = make_double2(1.0, 0.0);
@@ -189,16 +211,24 @@ k_spec_build(const double2 *__restrict__ cspec, size_t cs_q, const double *__res
 // ---------------------------------------------------------------------------
 // g spectra from g coefficients: G = DFT_d(g) (bins 0..d/2), real FFT of size
 // d through a complex transform of size d/2.  g_q == 0 and one node: the root.
-__global__ void __launch_bounds__(kSpecThreads)
-k_gspec_init(const double *__restrict__ g, size_t g_q, int gst, int glen, int nreal, int logd,
-             double2 *__restrict__ G, size_t G_q, const uint8_t *__restrict__ hot, const double2 *__restrict__ tw,
-             int logTW) {
+__device__ void gspec_body(const GspecArgs &A, int bx, int q) {
+    const auto g = A.g;
+    const auto g_q = A.g_q;
+    const auto gst = A.gst;
+    const auto glen = A.glen;
+    const auto nreal = A.nreal;
+    const auto logd = A.logd;
+    const auto G = A.G;
+    const auto G_q = A.G_q;
+    const auto hot = A.hot;
+    const auto tw = A.tw;
+    const auto logTW = A.logTW;
+
     extern __shared__ double2 sm[];
     const int h = 1 << (logd - 1);
     const int lh = logd - 1;
     const int cb = h >= 4096 ? 1 : 4096 / h;
-    const int q = blockIdx.y;
-    const int j0 = blockIdx.x * cb;
+        const int j0 = bx * cb;
     const int cnt = min(cb, nreal - j0);
     if (cnt <= 0) return;
     for (int e = threadIdx.x; e < cnt * h; e += blockDim.x) {
@@ -243,16 +273,29 @@ k_gspec_init(const double *__restrict__ g, size_t g_q, int gst, int glen, int nr
 //   X(f) = E + T,  X(h-f) = conj(E - T),  E = z_f + conj z_{h-f},
 //   T = -i (z_f - conj z_{h-f}) e^{-2 pi i f/D},
 //   G_child[f] = Y[2f]/2 + X(f)/8h   (all scalings folded into the last step).
-__global__ void __launch_bounds__(kSpecThreads)
-k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restrict__ cspec, size_t cs_q, int nreal_c,
-            int npar, int logD, double2 *__restrict__ Gout, size_t Go_q, double *__restrict__ gout, size_t go_q,
-            int gst_c, int glen_c, const uint8_t *__restrict__ hot_c, const double2 *__restrict__ tw, int logTW) {
+__device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
+    const auto Gp = A.Gp;
+    const auto Gp_q = A.Gp_q;
+    const auto cspec = A.cspec;
+    const auto cs_q = A.cs_q;
+    const auto nreal_c = A.nreal_c;
+    const auto npar = A.npar;
+    const auto logD = A.logD;
+    const auto Gout = A.Gout;
+    const auto Go_q = A.Go_q;
+    const auto gout = A.gout;
+    const auto go_q = A.go_q;
+    const auto gst_c = A.gst_c;
+    const auto glen_c = A.glen_c;
+    const auto hot_c = A.hot_c;
+    const auto tw = A.tw;
+    const auto logTW = A.logTW;
+
     extern __shared__ double2 sm[];
     const int D = 1 << logD;
     const int h = D >> 1, lh = logD - 1;
     const int cbp = D >= 4096 ? 1 : 4096 / D;            // parents per CTA; 2 children each
-    const int q = blockIdx.y;
-    const int j0 = blockIdx.x * cbp;
+        const int j0 = bx * cbp;
     const int cnt = min(cbp, npar - j0);
     if (cnt <= 0) return;
     const int nk = 2 * cnt;                               // children handled, h slots each
@@ -366,6 +409,14 @@ k_spec_prop(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restri
     }
 }
 
+__global__ void __launch_bounds__(kSpecThreads) k_spec_init(SpecInitArgs A) { spec_init_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kSpecThreads) k_spec_build(SpecBuildArgs A) { spec_build_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kSpecThreads) k_gspec_init(GspecArgs A) { gspec_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kSpecThreads) k_spec_prop(SpecPropArgs A) { spec_prop_body(A, blockIdx.x, blockIdx.y); }
+
+size_t spec_smem_bytes(int M) { return spec_smem(M); }
+void spec_wl_set_smem_limits();
+
 // ---------------------------------------------------------------------------
 void spec_set_smem_limits() {
     const int mx = (int)spec_smem(kSpecMaxM);
@@ -373,51 +424,128 @@ void spec_set_smem_limits() {
     cudaFuncSetAttribute(k_spec_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_gspec_init, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    spec_wl_set_smem_limits();
+}
+
+SpecInitArgs spec_init_args(const Level &v, const double2 *tw, int logTW, double *fq, size_t *smem) {
+    const int logd = ilog2s(v.deg), d = 1 << logd;
+    const int cb = spec_cb(d);
+    if (fq) *fq = (5.0 * d * logd + 20.0 * d) * v.nreal;
+    if (smem) *smem = spec_smem(d);
+    return SpecInitArgs{v.P, v.P_q, v.pst, v.plen, v.nreal, logd, v.spec2, v.spec2_q, v.ends, v.ends_q, tw, logTW,
+                        (v.nreal + cb - 1) / cb};
+}
+
+SpecBuildArgs spec_build_args(const Level &c, const Level &p, bool write_coeffs, const double2 *tw, int logTW,
+                              double *fq, size_t *smem) {
+    const int logD = ilog2s(c.deg), D = 1 << logD;
+    const int cb = spec_cb(D);
+    if (fq) *fq = (10.0 * D * logD + 60.0 * D) * p.nreal;
+    if (smem) *smem = spec_smem(D);
+    return SpecBuildArgs{c.spec2, c.spec2_q, c.ends, c.ends_q, c.nreal, p.nreal, logD, p.spec2, p.spec2_q,
+                         p.spec2 ? p.ends : nullptr, p.ends_q, write_coeffs ? p.P : nullptr, p.P_q, p.pst, p.plen, tw,
+                         logTW, (p.nreal + cb - 1) / cb};
+}
+
+GspecArgs gspec_args(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G, size_t G_q,
+                     const uint8_t *hot, const double2 *tw, int logTW, double *fq, size_t *smem) {
+    const int logd = ilog2s(v.deg), h = 1 << (logd - 1);
+    const int cb = spec_cb(h);
+    if (fq) *fq = (5.0 * h * (logd - 1) + 20.0 * h) * nreal;
+    if (smem) *smem = spec_smem(h);
+    return GspecArgs{g, g_q, gst, glen, nreal, logd, G, G_q, hot, tw, logTW, (nreal + cb - 1) / cb};
+}
+
+SpecPropArgs spec_prop_args(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral,
+                            const uint8_t *hot_c, const double2 *tw, int logTW, double *fq, size_t *smem) {
+    const int logD = ilog2s(c.deg), D = 1 << logD;
+    const int cbp = spec_cb(D);
+    if (fq) *fq = (2.0 * 2 * 5.0 * (D / 2) * (logD - 1) + 60.0 * D) * p.nreal;
+    if (smem) *smem = spec_smem(D);
+    return SpecPropArgs{Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, p.nreal, logD, children_spectral ? c.G : nullptr,
+                        c.G_q, c.g, c.g_q, c.gst, c.glen, hot_c, tw, logTW, (p.nreal + cbp - 1) / cbp};
 }
 
 void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cudaStream_t st, Prof *pr) {
-    const int logd = ilog2s(v.deg), d = 1 << logd;
-    const int cb = spec_cb(d);
-    dim3 g((v.nreal + cb - 1) / cb, nq);
-    pr->begin("spec_init", (5.0 * d * logd + 20.0 * d) * v.nreal * (double)nq, st);
-    k_spec_init<<<g, kSpecThreads, spec_smem(d), st>>>(v.P, v.P_q, v.pst, v.plen, v.nreal, logd, v.spec2, v.spec2_q,
-                                                       v.ends, v.ends_q, tw, logTW);
+    double fq = 0.0;
+    size_t sm = 0;
+    SpecInitArgs A = spec_init_args(v, tw, logTW, &fq, &sm);
+    pr->begin("spec_init", fq * nq, st);
+    k_spec_init<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
     pr->end(st);
 }
 
 void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq, const double2 *tw, int logTW,
                        cudaStream_t st, Prof *pr) {
-    const int logD = ilog2s(c.deg), D = 1 << logD;
-    const int cb = spec_cb(D);
-    dim3 g((p.nreal + cb - 1) / cb, nq);
-    pr->begin("spec_build", (10.0 * D * logD + 60.0 * D) * p.nreal * (double)nq, st);
-    k_spec_build<<<g, kSpecThreads, spec_smem(D), st>>>(c.spec2, c.spec2_q, c.ends, c.ends_q, c.nreal, p.nreal, logD,
-                                                        p.spec2, p.spec2_q, p.spec2 ? p.ends : nullptr, p.ends_q,
-                                                        write_coeffs ? p.P : nullptr, p.P_q, p.pst, p.plen, tw, logTW);
+    double fq = 0.0;
+    size_t sm = 0;
+    SpecBuildArgs A = spec_build_args(c, p, write_coeffs, tw, logTW, &fq, &sm);
+    pr->begin("spec_build", fq * nq, st);
+    k_spec_build<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
     pr->end(st);
 }
 
 void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G,
                        size_t G_q, int nq, const uint8_t *hot, const double2 *tw, int logTW, cudaStream_t st,
                        Prof *pr) {
-    const int logd = ilog2s(v.deg), h = 1 << (logd - 1);
-    const int cb = spec_cb(h);
-    dim3 gr((nreal + cb - 1) / cb, nq);
-    pr->begin("gspec_init", (5.0 * h * (logd - 1) + 20.0 * h) * nreal * (double)nq, st);
-    k_gspec_init<<<gr, kSpecThreads, spec_smem(h), st>>>(g, g_q, gst, glen, nreal, logd, G, G_q, hot, tw, logTW);
+    double fq = 0.0;
+    size_t sm = 0;
+    GspecArgs A = gspec_args(g, g_q, gst, glen, nreal, v, G, G_q, hot, tw, logTW, &fq, &sm);
+    pr->begin("gspec_init", fq * nq, st);
+    k_gspec_init<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
     pr->end(st);
 }
 
 void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral, int nq,
                       const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr) {
-    const int logD = ilog2s(c.deg), D = 1 << logD;
-    const int cbp = spec_cb(D);
-    dim3 g((p.nreal + cbp - 1) / cbp, nq);
-    pr->begin("spec_prop", (2.0 * 2 * 5.0 * (D / 2) * (logD - 1) + 60.0 * D) * p.nreal * (double)nq, st);
-    k_spec_prop<<<g, kSpecThreads, spec_smem(D), st>>>(Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, p.nreal, logD,
-                                                       children_spectral ? c.G : nullptr, c.G_q, c.g, c.g_q, c.gst,
-                                                       c.glen, hot_c, tw, logTW);
+    double fq = 0.0;
+    size_t sm = 0;
+    SpecPropArgs A = spec_prop_args(Gp, Gp_q, c, p, children_spectral, hot_c, tw, logTW, &fq, &sm);
+    pr->begin("spec_prop", fq * nq, st);
+    k_spec_prop<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
     pr->end(st);
+}
+
+// ---------------------------------------------------------------- work lists
+__global__ void __launch_bounds__(kSpecThreads)
+kw_spec_init(const SpecInitArgs *__restrict__ D, const int2 *__restrict__ tab) {
+    const int2 t = tab[blockIdx.x];
+    spec_init_body(D[t.x], t.y, blockIdx.y);
+}
+__global__ void __launch_bounds__(kSpecThreads)
+kw_spec_build(const SpecBuildArgs *__restrict__ D, const int2 *__restrict__ tab) {
+    const int2 t = tab[blockIdx.x];
+    spec_build_body(D[t.x], t.y, blockIdx.y);
+}
+__global__ void __launch_bounds__(kSpecThreads)
+kw_gspec(const GspecArgs *__restrict__ D, const int2 *__restrict__ tab) {
+    const int2 t = tab[blockIdx.x];
+    gspec_body(D[t.x], t.y, blockIdx.y);
+}
+__global__ void __launch_bounds__(kSpecThreads)
+kw_spec_prop(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ tab) {
+    const int2 t = tab[blockIdx.x];
+    spec_prop_body(D[t.x], t.y, blockIdx.y);
+}
+
+void spec_wl_set_smem_limits() {
+    const int mx = (int)spec_smem(kSpecMaxM);
+    cudaFuncSetAttribute(kw_spec_init, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_spec_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_gspec, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, size_t smem, cudaStream_t st) {
+    if (nctas <= 0 || nq <= 0) return;
+    const dim3 g(nctas, nq);
+    switch (op) {
+        case WOp::SpecInit: kw_spec_init<<<g, kSpecThreads, smem, st>>>((const SpecInitArgs *)desc, tab); break;
+        case WOp::SpecBuild: kw_spec_build<<<g, kSpecThreads, smem, st>>>((const SpecBuildArgs *)desc, tab); break;
+        case WOp::Gspec: kw_gspec<<<g, kSpecThreads, smem, st>>>((const GspecArgs *)desc, tab); break;
+        case WOp::SpecProp: kw_spec_prop<<<g, kSpecThreads, smem, st>>>((const SpecPropArgs *)desc, tab); break;
+        default: break;
+    }
 }
 
 }  // namespace icmg

@@ -46,10 +46,36 @@ int icm_gb300_set_config(const IcmGb300Config *cfg);
  *   n[t], k[t]        players and paid places of tournament t
  *   S, payout         concatenated stacks (sum n) and payouts (sum k)
  *   equity            concatenated output (sum n)
- * All tournaments share Q.  Returns 0 / -1. */
+ * All tournaments share Q.  Every tree-level step of all tournaments runs as
+ * one work-list launch; each tournament's equities equal those of a single
+ * icm_gpu_equity call bit for bit.  Returns 0 / -1. */
 int icm_gpu_equity_batched(int T, const int *n, const int *k,
                            const double *S, const double *payout, int Q,
                            double *equity, IcmGpuRunStats *stats);
+
+/* Reusable batch (the batched analogue of IcmGpuPlan): sorts, tree geometry,
+ * device buffers and work lists are built once; every run uploads the
+ * payouts, replays the captured CUDA graph of the whole launch sequence
+ * (recaptured when Q changes) and downloads the equities.
+ *   batch_create      stacks concatenated as for icm_gpu_equity_batched;
+ *                     NULL on failure (icm_gpu_last_error())
+ *   batch_run         payouts concatenated (sum k), equities (sum n)
+ *   batch_set_options use_graphs 0/1; profiling 1 = per-launch CUDA events
+ *                     (graphs off while profiling), 0 = off, -1 = unchanged
+ *   batch_info        members solved by work lists, tournaments solved by
+ *                     their own plans (transforms beyond one CTA), players,
+ *                     nodes per chunk, device ms of the last run, arena bytes
+ *   batch_kernel_stats  as icm_gb300_plan_kernel_stats                      */
+typedef struct IcmGb300Batch IcmGb300Batch;
+IcmGb300Batch *icm_gb300_batch_create(int T, const int *n, const int *k, const double *S);
+int icm_gb300_batch_run(IcmGb300Batch *batch, int Q, const double *payout, double *equity,
+                        IcmGpuRunStats *stats);
+void icm_gb300_batch_destroy(IcmGb300Batch *batch);
+int icm_gb300_batch_set_options(IcmGb300Batch *batch, int use_graphs, int profiling);
+int icm_gb300_batch_info(const IcmGb300Batch *batch, long *members, long *fallbacks, long *players,
+                         int *q_chunk, double *device_ms, size_t *device_bytes);
+int icm_gb300_batch_kernel_stats(const IcmGb300Batch *batch, int i, char *name, int name_len,
+                                 double *ms, long *launches, double *flops);
 
 /* Measured peak of this GPU's FP64 pipe: a register-resident DFMA loop over
  * all SMs, in GFLOP/s (2 flops per DFMA).  Returns 1 / 0. */
