@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--q-chunk", type=int, default=0, help="quadrature nodes per launch sequence (0 = auto)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-tournaments leg")
     ap.add_argument("--batch-count", type=int, default=4096, help="tournaments in the batched leg")
+    ap.add_argument("--no-vjp", action="store_true", help="skip the VJP leg")
     return ap.parse_args()
 
 
@@ -252,6 +253,7 @@ def main():
             full_ms.append((t3 - t2) * 1e3)
 
     batched = None if args.no_batched else batched_leg(icm, W, max(2, args.steps // 3), args.batch_count)
+    vjp = None if args.no_vjp else vjp_leg(icm, W, 3)
 
     # end to end through icm_equity (host buffers, plan set-up inside)
     e2e = []
@@ -312,6 +314,7 @@ def main():
         "subset": {"targets": int(len(T)), "ms": float(np.median(sub_ms)), "full_ms": float(np.median(full_ms)),
                    "path": "icm_gpu_equity_subset vs icm_gpu_equity, plan set-up included"},
         "batched": batched,
+        "vjp": vjp,
         "roofline": roofline,
         "algorithmic_tflops_per_s": total_flops / (ms_per_solve * 1e-3) / 1e12,
         "fp64_peak_tflops_measured": fp64_peak_gflops / 1e3,
@@ -385,6 +388,54 @@ def batched_leg(icm, W, steps, count):
                      "share": r["ms"] / tot if tot else None} for r in kst],
         "config": "n log-uniform [9,20000], k=ceil(0.15n), stacks 1e4*lognormal(0,1), payout 0.8^j normalised",
     }
+
+
+def vjp_leg(icm, W, steps):
+    """Differentiated form: n = 16384, k = 2000, Q = 256, gamma(2, 5000)
+    stacks, N(0, 1) cotangent, linear and quadratic payouts.  Device time of
+    the VJP (forward tree recomputed inside) against the forward solve on the
+    same stacks, both with plans resident; e2e through icm_gb300_equity_vjp;
+    and the batched VJP over 256 tournaments with n in [100, 4000]."""
+    out = {"metric": "VJP/fwd time", "config": "n=16384, k=2000, Q=256, stacks gamma(2,5000), cotangent N(0,1)"}
+    for shape in ("linear", "quadratic"):
+        S, P, cot = W.vjp(payout=shape)
+        k = len(P)
+        fplan = icm.GpuPlan(S, k)
+        vplan = icm.VjpPlan(S, k)
+        for _ in range(2):
+            fplan.equity(P)
+            vplan.run(P, cot)
+        fwd, vjp = [], []
+        from icm_gb300._lib import lib
+        for _ in range(max(2, steps)):
+            fplan.equity(P)
+            fwd.append(lib().icm_gb300_plan_device_ms(fplan._p))
+            vplan.run(P, cot)
+            vjp.append(vplan.device_ms())
+        fplan.close()
+        vplan.close()
+        t0 = time.perf_counter()
+        icm.equity_vjp(S, P, cot)
+        e2e = time.perf_counter() - t0
+        out[shape] = {"fwd_ms": float(np.median(fwd)), "vjp_ms": float(np.median(vjp)),
+                      "ratio": float(np.median(vjp) / np.median(fwd)), "vjp_e2e_ms": e2e * 1e3}
+    rng = np.random.default_rng(77)
+    ts, cots = [], []
+    for _ in range(256):
+        n = int(rng.integers(100, 4001))
+        k = max(1, int(np.ceil(0.15 * n)))
+        ts.append((1e4 * np.exp(rng.standard_normal(n)), 0.8 ** np.arange(k)))
+        cots.append(rng.standard_normal(n))
+    icm.equity_vjp_batched(ts[:4], cots[:4])
+    t0 = time.perf_counter()
+    icm.equity_vjp_batched(ts, cots)
+    tv = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    icm.equity_batched(ts)
+    tf = time.perf_counter() - t0
+    out["batched_256"] = {"vjp_ms": tv * 1e3, "fwd_ms": tf * 1e3, "ratio": tv / tf,
+                          "config": "256 tournaments, n uniform [100,4000], k=ceil(0.15n), payout 0.8^j, wall time"}
+    return out
 
 
 def traffic_for(kernel: str):

@@ -27,7 +27,7 @@ from ._lib import (IcmGb300Config, IcmGpuOptions, IcmGpuPlanSummary, IcmGpuRunSt
                    library_path)
 
 __all__ = ["init", "equity", "equity_subset", "ICMError", "gpu_equity", "gpu_equity_subset", "GpuPlan",
-           "equity_batched", "GpuBatch", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
+           "equity_batched", "GpuBatch", "equity_vjp", "equity_vjp_batched", "VjpPlan", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
            "last_launch_count"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -290,6 +290,80 @@ class GpuBatch:
     def close(self):
         if getattr(self, "_h", None):
             lib().icm_gb300_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def equity_vjp(stacks, payouts, cotangent, Q=256, node_terms=False):
+    """dL/dS and dL/dpayout of L = sum_i cot_i equity_i(S, payout), through
+    the GPU adjoint passes.  Returns (grad_stacks, grad_payouts).
+    ``node_terms`` also differentiates the quadrature nodes' dependence on
+    max S (the exact derivative of the Q-node formula)."""
+    S = _to_double_array(stacks, "stacks")
+    P = _to_double_array(payouts, "payouts")
+    C = _to_double_array(cotangent, "cotangent")
+    n, k = len(S), len(P)
+    _check(n, k, Q)
+    if len(C) != n:
+        raise ValueError(f"cotangent: expected {n} values, got {len(C)}")
+    _auto_init()
+    gS, gP = np.zeros(n), np.zeros(k)
+    if lib().icm_gb300_equity_vjp(n, _d(S), int(Q), _d(P), k, _d(C), _d(gS), _d(gP), int(bool(node_terms))) != 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return gS, gP
+
+
+def equity_vjp_batched(tournaments, cotangents, Q=256, node_terms=False):
+    """VJPs of many tournaments: lists of (stacks, payouts) and cotangents.
+    Returns a list of (grad_stacks, grad_payouts)."""
+    ns, ks, S, P = _batch_arrays(tournaments, Q)
+    C = np.ascontiguousarray(np.concatenate([_to_double_array(c, "cotangent") for c in cotangents]))
+    if C.size != S.size:
+        raise ValueError("one cotangent value per player")
+    _auto_init()
+    gS, gP = np.zeros(S.size), np.zeros(P.size)
+    if lib().icm_gb300_equity_vjp_batched(len(ns), ns.ctypes.data_as(_ip), ks.ctypes.data_as(_ip), _d(S), _d(P),
+                                          int(Q), _d(C), _d(gS), _d(gP), int(bool(node_terms))) != 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return list(zip(np.split(gS, np.cumsum(ns)[:-1]), np.split(gP, np.cumsum(ks)[:-1])))
+
+
+class VjpPlan:
+    """Reusable VJP plan for one set of stacks (sort, geometry and buffers
+    once); ``run(payouts, cotangent)`` returns (grad_stacks, grad_payouts)."""
+
+    def __init__(self, stacks, k):
+        S = _to_double_array(stacks, "stacks")
+        self.n, self.k = len(S), int(k)
+        _check(self.n, self.k, 1)
+        _auto_init()
+        self._h = lib().icm_gb300_vjp_create(self.n, _d(S), self.k)
+        if not self._h:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+
+    def run(self, payouts, cotangent, Q=256, return_stats=False, node_terms=False):
+        P = _to_double_array(payouts, "payouts")
+        C = _to_double_array(cotangent, "cotangent")
+        if len(P) != self.k or len(C) != self.n:
+            raise ValueError("payouts must have k values and cotangent n values")
+        gS, gP = np.zeros(self.n), np.zeros(self.k)
+        st = IcmGpuRunStats()
+        if lib().icm_gb300_vjp_run(self._h, int(Q), _d(P), _d(C), _d(gS), _d(gP), int(bool(node_terms)),
+                                   ctypes.byref(st)) != 0:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+        return ((gS, gP), _stats_dict(st)) if return_stats else (gS, gP)
+
+    def device_ms(self):
+        return lib().icm_gb300_vjp_device_ms(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().icm_gb300_vjp_destroy(self._h)
             self._h = None
 
     def __del__(self):

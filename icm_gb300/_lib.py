@@ -80,6 +80,15 @@ SIGNATURES = {
                                                    ctypes.POINTER(ctypes.c_long), _dp]),
     "icm_gb300_plan_device_ms": (ctypes.c_double, [_vp]),
     "icm_gpu_equity_noalloc": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, _dp]),
+    "icm_gb300_equity_vjp": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp,
+                                            ctypes.c_int]),
+    "icm_gb300_vjp_create": (_vp, [ctypes.c_int, _dp, ctypes.c_int]),
+    "icm_gb300_vjp_run": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                         ctypes.POINTER(IcmGpuRunStats)]),
+    "icm_gb300_vjp_destroy": (None, [_vp]),
+    "icm_gb300_vjp_device_ms": (ctypes.c_double, [_vp]),
+    "icm_gb300_equity_vjp_batched": (ctypes.c_int, [ctypes.c_int, _ip, _ip, _dp, _dp, ctypes.c_int, _dp, _dp, _dp,
+                                                    ctypes.c_int]),
     "icm_gb300_batch_create": (_vp, [ctypes.c_int, _ip, _ip, _dp]),
     "icm_gb300_batch_run": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gb300_batch_destroy": (None, [_vp]),

@@ -14,6 +14,7 @@
 #include "batch.h"
 #include "engine.h"
 #include "kernels.h"
+#include "vjp.h"
 
 using namespace icmg;
 
@@ -369,6 +370,69 @@ int icm_gb300_batch_kernel_stats(const IcmGb300Batch *b, int i, char *name, int 
     if (launches) *launches = k.launches;
     if (flops) *flops = k.flops;
     return (int)f->kstats.size();
+}
+
+// ------------------------------------------------------------ VJP
+IcmGb300Vjp *icm_gb300_vjp_create(int n, const double *S, int k) {
+    if (!ensure_device()) return nullptr;
+    std::string err;
+    VjpPlan *v = vjp_plan_create(n, S, k, err);
+    if (!v) { set_error("icm_gb300_vjp_create: " + err); return nullptr; }
+    return reinterpret_cast<IcmGb300Vjp *>(v);
+}
+
+int icm_gb300_vjp_run(IcmGb300Vjp *plan, int Q, const double *payout, const double *cot, double *grad_S,
+                      double *grad_payout, int flags, IcmGpuRunStats *stats) {
+    if (!plan) { set_error("icm_gb300_vjp_run: null plan"); return -1; }
+    if (!ensure_device()) return -1;
+    VjpPlan *v = reinterpret_cast<VjpPlan *>(plan);
+    std::string err;
+    const int rc = vjp_plan_run(v, Q, payout, cot, grad_S, grad_payout, flags, stats, err);
+    t_launches = v->p->launches;
+    if (rc != 0) { set_error("icm_gb300_vjp_run: " + err); return -1; }
+    return 0;
+}
+
+void icm_gb300_vjp_destroy(IcmGb300Vjp *plan) { vjp_plan_destroy(reinterpret_cast<VjpPlan *>(plan)); }
+
+double icm_gb300_vjp_device_ms(const IcmGb300Vjp *plan) {
+    return plan ? reinterpret_cast<const VjpPlan *>(plan)->p->last_device_ms : 0.0;
+}
+
+int icm_gb300_equity_vjp(int n, const double *S, int Q, const double *payout, int k, const double *cot,
+                         double *grad_S, double *grad_payout, int flags) {
+    if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !cot || !grad_S || !grad_payout) {
+        set_error("icm_gb300_equity_vjp: invalid arguments (need 1 <= k <= n, Q >= 1)");
+        return -1;
+    }
+    IcmGb300Vjp *v = icm_gb300_vjp_create(n, S, k);
+    if (!v) return -1;
+    const int rc = icm_gb300_vjp_run(v, Q, payout, cot, grad_S, grad_payout, flags, nullptr);
+    icm_gb300_vjp_destroy(v);
+    return rc;
+}
+
+int icm_gb300_equity_vjp_batched(int T, const int *n, const int *k, const double *S, const double *payout, int Q,
+                                 const double *cot, double *grad_S, double *grad_payout, int flags) {
+    if (T < 1 || !n || !k || !S || !payout || !cot || !grad_S || !grad_payout || Q < 1) {
+        set_error("icm_gb300_equity_vjp_batched: invalid arguments");
+        return -1;
+    }
+    long so = 0, po = 0, launches = 0;
+    for (int t = 0; t < T; ++t) {
+        if (n[t] < 1 || k[t] < 1 || k[t] > n[t]) {
+            set_error("icm_gb300_equity_vjp_batched: tournament " + std::to_string(t) + " needs 1 <= k <= n");
+            return -1;
+        }
+        if (icm_gb300_equity_vjp(n[t], S + so, Q, payout + po, k[t], cot + so, grad_S + so, grad_payout + po,
+                                 flags) != 0)
+            return -1;
+        launches += t_launches;
+        so += n[t];
+        po += k[t];
+    }
+    t_launches = launches;
+    return 0;
 }
 
 int icm_gpu_measure_fp64_gflops(double *gflops_out) {

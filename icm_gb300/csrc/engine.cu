@@ -111,7 +111,7 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     p->k = k;
     p->B = select_block_size(n, k);
     p->fft_min_deg = g_config.fft_min_degree > 0 ? g_config.fft_min_degree : 64;
-    p->spectral = g_config.coefficient_fft_only != 1;
+    p->spectral = g_config.coefficient_fft_only != 1 && !p->coeff_only;
     const int B = p->B;
 
     // descending stacks, ties by original index (reference gpu_plan.cu:405-409)
@@ -244,14 +244,16 @@ size_t plan_tree_layout(Plan *p, int qc, char *base) {
     return off;
 }
 
-Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err) {
+Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err, bool coeff_only,
+                  double q_bytes_scale) {
     Plan *p = new Plan();
     if (opts) p->opts = *opts;
     p->opts.device_id = g_device;
+    p->coeff_only = coeff_only;
     if (plan_geometry(p, n, S, k, err) != 0) { delete p; return nullptr; }
     const int B = p->B;
     const int Nt = 1 << (p->L - 1);
-    const size_t per_q = p->tree_q_bytes + (size_t)2 * n * 8 + 1024;
+    const size_t per_q = (size_t)((double)(p->tree_q_bytes + (size_t)2 * n * 8 + 1024) * q_bytes_scale);
 
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
@@ -379,7 +381,7 @@ int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &er
 }
 
 // one chunk of nq nodes starting at active-node index q0
-static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first) {
+void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide) {
     cudaStream_t st = p->stream;
     const int L = p->L;
     Level *lv = p->lv;
@@ -451,6 +453,7 @@ static void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, boo
             ++p->launches;
         }
     }
+    if (!divide) return;
     const double *g0 = (L == 1) ? p->d_payout : lv[0].g;
     const size_t g0_q = (L == 1) ? 0 : lv[0].g_q;
     const int gst0 = (L == 1) ? 0 : lv[0].gst;
@@ -505,7 +508,7 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     cudaEventRecord(p->ev0, p->stream);
     for (int q0 = 0; q0 < nact; q0 += p->qc) {
         const int nq = std::min(p->qc, nact - q0);
-        run_chunk(p, q0, nq, tw, logTW, q0 == 0);
+        run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);
     }
     launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
     ++p->launches;

@@ -57,6 +57,7 @@ struct Plan {
     int n = 0, k = 0, B = 0, nblocks = 0, L = 0;
     int fft_min_deg = 64;
     bool spectral = true;           // use spectral levels where they apply
+    bool coeff_only = false;        // never use spectral levels
     std::vector<double> S_sorted;
     std::vector<int> perm;          // perm[i] = original index of sorted player i
     std::vector<int> inv_perm;
@@ -111,7 +112,19 @@ struct Plan {
 int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err);
 // tree buffers for chunks of qc nodes from `base` (nullptr: size only)
 size_t plan_tree_layout(Plan *p, int qc, char *base);
-Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err);
+// coeff_only: every FFT level on coefficients (the adjoint passes need the
+// coefficients of every level); q_bytes_scale sizes the node chunk for
+// callers that add per-node buffers of their own
+Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err,
+                  bool coeff_only = false, double q_bytes_scale = 1.0);
+// launch sequence of one chunk of nq nodes (engine.cu); divide = false stops
+// after the propagate pass (the tree of the chunk stays in the plan's buffers)
+void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide);
+static inline int plan_ilog2(long v) {
+    int l = 0;
+    while ((1L << l) < v) ++l;
+    return l;
+}
 void plan_destroy(Plan *p);
 int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &err);
 int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats,

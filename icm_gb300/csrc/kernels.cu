@@ -309,9 +309,12 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
     return 0;
 }
 
+void vjp_set_smem_limits();   // vjp.cu
+
 void fft_set_smem_limits() {
     fused_set_smem_limits();
     spec_set_smem_limits();
+    vjp_set_smem_limits();
     const int mx = kSmemFftMax * (int)sizeof(double2);
     cudaFuncSetAttribute(k_fft_smem<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft_smem<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);

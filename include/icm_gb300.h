@@ -77,6 +77,42 @@ int icm_gb300_batch_info(const IcmGb300Batch *batch, long *members, long *fallba
 int icm_gb300_batch_kernel_stats(const IcmGb300Batch *batch, int i, char *name, int name_len,
                                  double *ms, long *launches, double *flops);
 
+/* Vector-Jacobian products of the equities.  No counterpart in the reference.
+ *
+ * For the loss L = sum_i cot[i] * equity_i(S, payout) (equity as from
+ * icm_equity with the same n, S, Q, payout, k) these return
+ *   grad_S[n]        dL/dS_i        (caller's player order)
+ *   grad_payout[k]   dL/dpayout_m   (equity is linear in the payout, so
+ *                    sum_m grad_payout[m] payout[m] = L)
+ * by reverse mode through the quadrature, the per-player division, the
+ * propagate and build passes of the tree and the leaf factors.  The forward
+ * tree of each chunk of nodes is recomputed inside the call.
+ *   flags = 0                the quadrature nodes are held fixed (they move
+ *                            with max S only through the quadrature rule)
+ *   flags = ICM_VJP_NODE_TERMS  also differentiate the nodes' dependence on
+ *                            max S: the exact derivative of the Q-node
+ *                            formula, equal to finite differences of it; it
+ *                            adds the derivative of the quadrature error to
+ *                            the largest stack's entry
+ * Returns 0 / -1 (message in icm_gpu_last_error()).
+ *   vjp_create/run/destroy   reusable plan for repeated calls on one S
+ *   vjp_device_ms            CUDA-event time of the last run's kernels
+ *   equity_vjp_batched       T tournaments, arrays concatenated as for
+ *                            icm_gpu_equity_batched (cot and grad_S: sum n;
+ *                            payout and grad_payout: sum k)                */
+#define ICM_VJP_NODE_TERMS 1
+typedef struct IcmGb300Vjp IcmGb300Vjp;
+int icm_gb300_equity_vjp(int n, const double *S, int Q, const double *payout, int k,
+                         const double *cot, double *grad_S, double *grad_payout, int flags);
+IcmGb300Vjp *icm_gb300_vjp_create(int n, const double *S, int k);
+int icm_gb300_vjp_run(IcmGb300Vjp *plan, int Q, const double *payout, const double *cot,
+                      double *grad_S, double *grad_payout, int flags, IcmGpuRunStats *stats);
+void icm_gb300_vjp_destroy(IcmGb300Vjp *plan);
+double icm_gb300_vjp_device_ms(const IcmGb300Vjp *plan);
+int icm_gb300_equity_vjp_batched(int T, const int *n, const int *k, const double *S,
+                                 const double *payout, int Q, const double *cot,
+                                 double *grad_S, double *grad_payout, int flags);
+
 /* Measured peak of this GPU's FP64 pipe: a register-resident DFMA loop over
  * all SMs, in GFLOP/s (2 flops per DFMA).  Returns 1 / 0. */
 int icm_gpu_measure_fp64_gflops(double *gflops_out);
