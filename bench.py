@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-tournaments leg")
     ap.add_argument("--batch-count", type=int, default=4096, help="tournaments in the batched leg")
     ap.add_argument("--no-vjp", action="store_true", help="skip the VJP leg")
+    ap.add_argument("--no-gpu-scale", action="store_true", help="skip the n = 2^20 leg")
     return ap.parse_args()
 
 
@@ -254,6 +255,7 @@ def main():
 
     batched = None if args.no_batched else batched_leg(icm, W, max(2, args.steps // 3), args.batch_count)
     vjp = None if args.no_vjp else vjp_leg(icm, W, 3)
+    gscale = None if args.no_gpu_scale else gpu_scale_leg(icm, W, 2)
 
     # end to end through icm_equity (host buffers, plan set-up inside)
     e2e = []
@@ -315,6 +317,7 @@ def main():
                    "path": "icm_gpu_equity_subset vs icm_gpu_equity, plan set-up included"},
         "batched": batched,
         "vjp": vjp,
+        "gpu_scale": gscale,
         "roofline": roofline,
         "algorithmic_tflops_per_s": total_flops / (ms_per_solve * 1e-3) / 1e12,
         "fp64_peak_tflops_measured": fp64_peak_gflops / 1e3,
@@ -388,6 +391,37 @@ def batched_leg(icm, W, steps, count):
                      "share": r["ms"] / tot if tot else None} for r in kst],
         "config": "n log-uniform [9,20000], k=ceil(0.15n), stacks 1e4*lognormal(0,1), payout 0.8^j normalised",
     }
+
+
+def gpu_scale_leg(icm, W, steps):
+    """GPU-only scale: n = 2^20 players, stacks 1e4 exp(1.5 N(0,1)), Q = 256;
+    (a) k = n linear payout, (b) k = 1000 geometric 0.97.  Device ms per solve
+    with the plan resident, end-to-end ms through icm_equity, and the
+    closed-form error of (a) on 64 sampled players (E = V1 / sum(n - m))."""
+    out = {"config": "n=1048576, stacks 1e4*exp(1.5 N(0,1)), Q=256"}
+    from icm_gb300._lib import lib
+    for shape in ("linear", "geometric"):
+        S, P = W.gpu_scale(shape=shape)
+        plan = icm.GpuPlan(S, len(P))
+        E = plan.equity(P)
+        dev = []
+        for _ in range(max(2, steps)):
+            plan.equity(P)
+            dev.append(lib().icm_gb300_plan_device_ms(plan._p))
+        summ = plan.summary()
+        plan.close()
+        t0 = time.perf_counter()
+        icm.equity(S, P)
+        e2e = time.perf_counter() - t0
+        rec = {"k": len(P), "device_ms": float(np.median(dev)), "e2e_ms": e2e * 1e3,
+               "q_chunk": summ["q_batch"], "device_bytes": summ["planned_peak_vram_bytes"]}
+        if shape == "linear":   # V1_i = 1 + sum_{j != i} S_i / (S_i + S_j); payout (n - m) / sum
+            idx = np.random.default_rng(3).choice(len(S), 64, replace=False)
+            n = len(S)
+            ref = np.array([0.5 + np.sum(S[i] / (S[i] + S)) for i in idx]) * (P[0] / n)
+            rec["max_rel_err_vs_closed_form_64_players"] = float(np.max(np.abs(E[idx] - ref) / np.abs(ref)))
+        out[shape] = rec
+    return out
 
 
 def vjp_leg(icm, W, steps):
