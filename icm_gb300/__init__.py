@@ -373,12 +373,16 @@ class VjpPlan:
             pass
 
 
-def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False):
+def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False,
+              zero_prefix=True):
     """Process-wide engine settings for plans created afterwards (0 = default).
 
     coefficient_fft_only=True keeps every FFT tree level on coefficients
-    (no spectral levels), for comparison and testing."""
-    cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes)
+    (no spectral levels), for comparison and testing; zero_prefix=False
+    computes tree nodes whose players all have a leaf factor of exactly 0 at
+    a quadrature node instead of writing them as monomials / skipping them."""
+    cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes,
+                         0 if zero_prefix else 1)
     lib().icm_gb300_set_config(ctypes.byref(cfg))
 
 

@@ -98,6 +98,8 @@ struct PhaseBuilder {
 };
 }  // namespace
 
+static const int *zpre(const Plan *p) { return p->zskip ? p->d_z : nullptr; }
+
 // descriptors of every step for Q nodes (pointers into the forest arena)
 static void build_steps(Forest *f) {
     const int T = (int)f->tr.size();
@@ -126,6 +128,7 @@ static void build_steps(Forest *f) {
                 double fq = 0;
                 size_t sm = 0;
                 SpecInitArgs A = spec_init_args(p->lv[0], tw, logTW, &fq, &sm);
+                A.z.zp = zpre(p);
                 c.add(WOp::SpecInit, A.logd, "wl_spec_init", A, sm, fq);
             }
         }
@@ -141,18 +144,22 @@ static void build_steps(Forest *f) {
             if (l <= p->L - 2) {
                 if (lv[l].kind == 2) {
                     SpecBuildArgs A = spec_build_args(lv[l - 1], lv[l], lv[l + 1].kind != 2, tw, logTW, &fq, &sm);
+                    A.z.zp = zpre(p);
                     b.add(WOp::SpecBuild, A.logD, "wl_spec_build", A, sm, fq);
                 } else if (lv[l].fft) {
                     if (lv[l].npairs > 0) {
                         FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], false, tw, logTW, &fq, &sm);
+                        A.z.zp = zpre(p);
                         b.add(WOp::FusedBuild, A.logN, "wl_fused_build", A, sm, fq);
                     }
                     if (lv[l - 1].nreal & 1) {
                         SchoolBuildArgs A = school_build_args(lv[l - 1], lv[l], lv[l].npairs, &fq);
+                        A.z.zp = zpre(p);
                         b.add(WOp::SchoolBuild, 0, "wl_school_build", A, 0, fq);
                     }
                 } else {
                     SchoolBuildArgs A = school_build_args(lv[l - 1], lv[l], 0, &fq);
+                    A.z.zp = zpre(p);
                     b.add(WOp::SchoolBuild, 0, "wl_school_build", A, 0, fq);
                 }
             } else if (l == p->L - 1 && lv[l].fft && lv[l].npairs > 0) {
@@ -169,6 +176,7 @@ static void build_steps(Forest *f) {
                 double fq = 0;
                 size_t sm = 0;
                 SpecInitArgs A = spec_init_args(lv[l], tw, logTW, &fq, &sm);
+                A.z.zp = zpre(p);
                 c.add(WOp::SpecInit, A.logd, "wl_spec_init", A, sm, fq);
             }
         }
@@ -190,6 +198,7 @@ static void build_steps(Forest *f) {
             } else if (lv[l + 1].kind != 2) {
                 GspecArgs A = gspec_args(lv[l].g, lv[l].g_q, lv[l].gst, lv[l].glen, lv[l].nreal, lv[l], lv[l].G,
                                          lv[l].G_q, nullptr, tw, logTW, &fq, &sm);
+                A.z.zp = zpre(p);
                 a.add(WOp::Gspec, A.logd, "wl_gspec_init", A, sm, fq);
             }
         }
@@ -208,19 +217,23 @@ static void build_steps(Forest *f) {
             if (lv[l].kind == 2) {
                 SpecPropArgs A = spec_prop_args(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l],
                                                 l - 1 >= 1 && lv[l - 1].kind == 2, nullptr, tw, logTW, &fq, &sm);
+                A.z.zp = zpre(p);
                 b.add(WOp::SpecProp, A.logD, "wl_spec_prop", A, sm, fq);
             } else if (lv[l].fft) {
                 if (lv[l].npairs > 0) {
                     FusedPropArgs A = fused_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nullptr, tw, logTW, &fq,
                                                       &sm);
+                    A.z.zp = zpre(p);
                     b.add(WOp::FusedProp, A.logN, "wl_fused_prop", A, sm, fq);
                 }
                 if (lv[l - 1].nreal & 1) {
                     SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], nullptr, 2 * lv[l].npairs, &fq);
+                    A.z.zp = zpre(p);
                     b.add(WOp::SchoolProp, 0, "wl_school_prop", A, 0, fq);
                 }
             } else {
                 SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], nullptr, 0, &fq);
+                A.z.zp = zpre(p);
                 b.add(WOp::SchoolProp, 0, "wl_school_prop", A, 0, fq);
             }
         }
@@ -291,8 +304,8 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
         case WOp::SchoolBuild:
         case WOp::SchoolProp: launch_worklist_basic(s.op, s.d_desc, s.d_tab, nctas, qn, q0, f->stream); break;
         case WOp::FusedBuild:
-        case WOp::FusedProp: launch_worklist_fused(s.op, s.d_desc, s.d_tab, nctas, qn, s.smem, f->stream); break;
-        default: launch_worklist_spec(s.op, s.d_desc, s.d_tab, nctas, qn, s.smem, f->stream); break;
+        case WOp::FusedProp: launch_worklist_fused(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
+        default: launch_worklist_spec(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
     }
     f->prof.end(f->stream);
     ++f->launches;
@@ -469,24 +482,35 @@ void forest_destroy(Forest *f) {
 static int prepare_nodes(Forest *f, int Q, std::string &err) {
     const int F = (int)f->tr.size();
     std::vector<double> h((size_t)F * Q * 3);
+    std::vector<int> hz((size_t)F * Q);
     parallel_for(F, [&](int i) {
         std::vector<double> logv, w;
-        make_nodes(Q, f->tr[i]->Smax, logv, w);
+        const Plan *p = f->tr[i];
+        make_nodes(Q, p->Smax, logv, w);
         double *o = h.data() + (size_t)i * Q * 3;
+        int *z = hz.data() + (size_t)i * Q;
         for (int q = 0; q < Q; ++q) {
             o[3 * q] = logv[q];
             o[3 * q + 1] = w[q];
             o[3 * q + 2] = std::exp(-logv[q]);
+            z[q] = zero_prefix(p->S_sorted.data(), p->n, logv[q]);
         }
     });
     if (f->d_node) cudaFree(f->d_node);
     f->d_node = nullptr;
-    cudaError_t e = cudaMalloc(&f->d_node, sizeof(double) * h.size());
+    const size_t nb = sizeof(double) * h.size();
+    cudaError_t e = cudaMalloc(&f->d_node, nb + sizeof(int) * hz.size());
+    int *dz = e == cudaSuccess ? (int *)((char *)f->d_node + nb) : nullptr;
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(f->d_node, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, f->stream);
+        e = cudaMemcpyAsync(f->d_node, h.data(), nb, cudaMemcpyHostToDevice, f->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dz, hz.data(), sizeof(int) * hz.size(), cudaMemcpyHostToDevice, f->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
     if (e != cudaSuccess) { err = std::string("node table: ") + cudaGetErrorString(e); return -1; }
-    for (int i = 0; i < F; ++i) f->tr[i]->d_node = f->d_node + (size_t)i * Q * 3;
+    for (int i = 0; i < F; ++i) {
+        f->tr[i]->d_node = f->d_node + (size_t)i * Q * 3;
+        f->tr[i]->d_z = dz + (size_t)i * Q;
+    }
     return 0;
 }
 

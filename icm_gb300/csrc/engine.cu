@@ -43,6 +43,19 @@ void make_nodes(int Q, double Smax, std::vector<double> &logv, std::vector<doubl
     }
 }
 
+// players (sorted by stack, descending) whose leaf factor is exactly 0: the
+// leaf kernel sets a = 0 when S logv < -700, a prefix since S logv grows
+// along the sorted order (logv < 0; rounding of the product is monotone)
+int zero_prefix(const double *S_sorted, int n, double logv) {
+    int lo = 0, hi = n;   // first index with S logv >= -700
+    while (lo < hi) {
+        const int mid = lo + (hi - lo) / 2;
+        if (S_sorted[mid] * logv < -700.0) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // ------------------------------------------------------------ twiddles
 // tables built by twiddle.cpp; one allocation per device, grown on demand
 static std::mutex g_tw_mu;
@@ -112,6 +125,7 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     p->B = select_block_size(n, k);
     p->fft_min_deg = g_config.fft_min_degree > 0 ? g_config.fft_min_degree : 64;
     p->spectral = g_config.coefficient_fft_only != 1 && !p->coeff_only;
+    p->zskip = g_config.disable_zero_prefix != 1 && !p->coeff_only;
     const int B = p->B;
 
     // descending stacks, ties by original index (reference gpu_plan.cu:405-409)
@@ -386,27 +400,35 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     const int L = p->L;
     Level *lv = p->lv;
     Prof *pr = &p->prof;
+    const int *zp = p->zskip ? p->d_z : nullptr;   // zero-prefix pruning (one-CTA levels)
     launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, lv[0].P, lv[0].pst,
                 lv[0].plen, st, pr);
     ++p->launches;
-    if (L >= 2 && lv[1].kind == 2) { launch_spec_init(lv[0], nq, tw, logTW, st, pr); ++p->launches; }
+    if (L >= 2 && lv[1].kind == 2) { launch_spec_init(lv[0], nq, tw, logTW, st, pr, zp, q0); ++p->launches; }
     for (int l = 1; l <= L - 2; ++l) {
         if (lv[l].kind == 2) {
             if (lv[l - 1].deg > kSpecMaxD) {
                 launch_specbig_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, p->d_fa, p->d_fc, tw, logTW, st,
-                                     &p->launches, pr);
+                                     &p->launches, pr, zp, q0);
             } else {
-                launch_spec_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, tw, logTW, st, pr);
+                launch_spec_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, tw, logTW, st, pr, zp, q0);
                 ++p->launches;
             }
         } else if (lv[l].fft) {
-            launch_fft_build(lv[l - 1], lv[l], nq, p->d_fa, p->d_fb, p->d_fc, false, tw, logTW, st, &p->launches, pr);
-            if (lv[l - 1].nreal & 1) { launch_school_build(lv[l - 1], lv[l], nq, lv[l].npairs, st, pr); ++p->launches; }
+            launch_fft_build(lv[l - 1], lv[l], nq, p->d_fa, p->d_fb, p->d_fc, false, tw, logTW, st, &p->launches, pr,
+                             zp, q0);
+            if (lv[l - 1].nreal & 1) {
+                launch_school_build(lv[l - 1], lv[l], nq, lv[l].npairs, st, pr, zp, q0);
+                ++p->launches;
+            }
         } else {
-            launch_school_build(lv[l - 1], lv[l], nq, 0, st, pr);
+            launch_school_build(lv[l - 1], lv[l], nq, 0, st, pr, zp, q0);
             ++p->launches;
         }
-        if (lv[l].kind != 2 && lv[l + 1].kind == 2) { launch_spec_init(lv[l], nq, tw, logTW, st, pr); ++p->launches; }
+        if (lv[l].kind != 2 && lv[l + 1].kind == 2) {
+            launch_spec_init(lv[l], nq, tw, logTW, st, pr, zp, q0);
+            ++p->launches;
+        }
     }
     if (L >= 2 && lv[L - 1].fft)
         launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches, pr);
@@ -426,30 +448,32 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
                     int logd = 0;
                     while ((1L << logd) < lv[l].deg) ++logd;
                     launch_gspecbig_init(gp, gp_q, gst_p, gpl, lv[l].nreal, logd, lv[l].G, root ? 0 : lv[l].G_q,
-                                         root ? 1 : nq, hot_p, p->d_fa, p->d_fc, tw, logTW, st, &p->launches, pr);
+                                         root ? 1 : nq, hot_p, p->d_fa, p->d_fc, tw, logTW, st, &p->launches, pr,
+                                         root ? nullptr : zp, q0);
                 } else {
+                    // the root's spectrum is shared by the chunk's nodes: never pruned
                     launch_gspec_init(gp, gp_q, gst_p, gpl, lv[l].nreal, lv[l], lv[l].G, root ? 0 : lv[l].G_q,
-                                      root ? 1 : nq, hot_p, tw, logTW, st, pr);
+                                      root ? 1 : nq, hot_p, tw, logTW, st, pr, root ? nullptr : zp, q0);
                     ++p->launches;
                 }
             }
             if (lv[l - 1].deg > kSpecMaxD) {
                 launch_specbig_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], nq, hot_c, p->d_fa, p->d_fc, tw, logTW,
-                                    st, &p->launches, pr);
+                                    st, &p->launches, pr, zp, q0);
             } else {
                 launch_spec_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l], l - 1 >= 1 && lv[l - 1].kind == 2,
-                                 nq, hot_c, tw, logTW, st, pr);
+                                 nq, hot_c, tw, logTW, st, pr, zp, q0);
                 ++p->launches;
             }
         } else if (lv[l].fft) {
             launch_fft_prop(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nq, hot_c, p->d_fa, p->d_fb, p->d_fc, tw, logTW,
-                            st, &p->launches, pr);
+                            st, &p->launches, pr, zp, q0);
             if (lv[l - 1].nreal & 1) {
-                launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 2 * lv[l].npairs, st, pr);
+                launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 2 * lv[l].npairs, st, pr, zp, q0);
                 ++p->launches;
             }
         } else {
-            launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 0, st, pr);
+            launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 0, st, pr, zp, q0);
             ++p->launches;
         }
     }
@@ -482,12 +506,19 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     if (nact > p->qmax) {
         if (p->d_node) cudaFree(p->d_node);
         p->d_node = nullptr;
-        e = cudaMalloc(&p->d_node, sizeof(double) * 3 * (size_t)std::max(nact, 1));
+        p->d_z = nullptr;
+        const size_t nb = sizeof(double) * 3 * (size_t)std::max(nact, 1);
+        e = cudaMalloc(&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1));
         if (e != cudaSuccess) { err = std::string("node buffer: ") + cudaGetErrorString(e); return -1; }
+        p->d_z = (int *)((char *)p->d_node + nb);
         p->qmax = nact;
     }
+    p->h_z.resize(nact);
+    for (int j = 0; j < nact; ++j) p->h_z[j] = zero_prefix(p->S_sorted.data(), p->n, node[3 * j]);
     if (nact)
         e = cudaMemcpyAsync(p->d_node, node.data(), sizeof(double) * node.size(), cudaMemcpyHostToDevice, p->stream);
+    if (nact && e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_z, p->h_z.data(), sizeof(int) * nact, cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * p->k, cudaMemcpyHostToDevice, p->stream);
     if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return -1; }

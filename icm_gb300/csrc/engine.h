@@ -58,6 +58,7 @@ struct Plan {
     int fft_min_deg = 64;
     bool spectral = true;           // use spectral levels where they apply
     bool coeff_only = false;        // never use spectral levels
+    bool zskip = true;              // prune wholly-zero tree nodes per quadrature node
     std::vector<double> S_sorted;
     std::vector<int> perm;          // perm[i] = original index of sorted player i
     std::vector<int> inv_perm;
@@ -80,6 +81,8 @@ struct Plan {
     double *d_acc = nullptr;        // [n] sorted order
     double *d_out = nullptr;        // [n] original order
     double *d_node = nullptr;       // [qmax][3]: logv, w, 1/v for the active nodes
+    int *d_z = nullptr;             // [qmax] zero prefix of each active node (same allocation)
+    std::vector<int> h_z;
     uint8_t *d_active = nullptr;    // [n] sorted order (subset), or null
     uint8_t *d_hot = nullptr;       // hot bitmap, all levels
     size_t hot_off[kMaxLevels] = {};
@@ -133,6 +136,8 @@ int select_block_size(int n, int k);
 
 // quadrature nodes (host), restating the reference's erfc-trapezoid rule
 void make_nodes(int Q, double Smax, std::vector<double> &logv, std::vector<double> &w);
+// number of sorted players with a leaf factor of exactly 0 at a node
+int zero_prefix(const double *S_sorted, int n, double logv);
 
 // device-wide twiddle table exp(-2 pi i t / 2^logTW); *logTW receives the
 // table's size, which may exceed the request

@@ -57,6 +57,13 @@ __device__ void fused_build_body(const FusedBuildArgs &A, int bx, int q) {
     double2 *Z = sm;                 // cb x N
     double2 *U = sm + (size_t)cb * N; // cb x h
     const double *base = Pc + q * Pc_q;
+    if (!spectra_only && zp_cold(A.z, q, j0 + cnt - 1)) {   // every parent x^deg (its spectra are never read)
+        for (int e = threadIdx.x; e < cnt * pst_p; e += blockDim.x) {
+            const int it = e / pst_p, t = e - it * pst_p;
+            Pp[q * Pp_q + (size_t)(j0 + it) * pst_p + t] = (t == A.z.span && t < lp) ? 1.0 : 0.0;
+        }
+        return;
+    }
     // 1. children into bit-reversed slots
     for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
         const int it = e >> logN, s = e & (N - 1);
@@ -134,6 +141,7 @@ __device__ void fused_prop_body(const FusedPropArgs &A, int bx, int q) {
     const int cnt = min(cb, npairs - j0);
     double2 *Z = sm;                  // cb x N
     double2 *W = sm + (size_t)cb * N; // cb x h
+    if (zp_cold(A.z, q, j0 + cnt - 1)) return;   // wholly-zero parents: no child g is read
     if (hot_c) {   // subset pruning: nothing below a cold child is ever read
         bool any = false;
         for (int c = 2 * j0; c < 2 * (j0 + cnt); ++c) any = any || hot_c[c];
@@ -193,8 +201,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_fused_build(FusedBuildArgs A)
 __global__ void __launch_bounds__(kFusedThreads) k_fused_prop(FusedPropArgs A) { fused_prop_body(A, blockIdx.x, blockIdx.y); }
 
 size_t fused_smem_bytes(int N) { return fused_smem(N); }
-__global__ void kw_fused_build(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ tab);
-__global__ void kw_fused_prop(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ tab);
+__global__ void kw_fused_build(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ tab, int q0);
+__global__ void kw_fused_prop(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ tab, int q0);
 
 bool fused_ok(int N) { return N >= 8 && N <= kFusedMaxN; }
 
@@ -220,7 +228,7 @@ FusedBuildArgs fused_build_args(const Level &c, const Level &p, bool spectra_onl
     if (fq) *fq = (5.0 * N * logN + (spectra_only ? 8.0 : 40.0 + 2.5 * logN) * (N / 2)) * p.npairs;
     if (smem) *smem = fused_smem(N);
     return FusedBuildArgs{c.P, c.P_q, c.pst, c.plen, p.npairs, logN, p.P, p.P_q, p.pst, p.plen, p.spec, tw, logTW,
-                          spectra_only ? 1 : 0, (p.npairs + cb - 1) / cb};
+                          spectra_only ? 1 : 0, (p.npairs + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}};
 }
 
 FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p,
@@ -230,24 +238,29 @@ FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl,
     if (fq) *fq = (5.0 * N * logN + 2.5 * N * (logN - 1) + 40.0 * (N / 2)) * p.npairs;
     if (smem) *smem = fused_smem(N);
     return FusedPropArgs{gp, gp_q, gst_p, gpl, p.npairs, logN, p.spec, c.g, c.g_q, c.gst, c.glen, hot_c, tw, logTW,
-                         (p.npairs + cb - 1) / cb};
+                         (p.npairs + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}};
 }
 
 void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_only, const double2 *tw, int logTW,
-                        cudaStream_t st, Prof *pr) {
+                        cudaStream_t st, Prof *pr, const int *zp, int zq0) {
     double fq = 0.0;
     size_t sm = 0;
     FusedBuildArgs A = fused_build_args(c, p, spectra_only, tw, logTW, &fq, &sm);
+    A.z.zp = zp;
+    A.z.q0 = zq0;
     pr->begin(spectra_only ? "fused_spectra" : "fused_build", fq * nq, st);
     k_fused_build<<<dim3(A.nbx, nq), kFusedThreads, sm, st>>>(A);
     pr->end(st);
 }
 
 void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
-                       const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr) {
+                       const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr, const int *zp,
+                       int zq0) {
     double fq = 0.0;
     size_t sm = 0;
     FusedPropArgs A = fused_prop_args(gp, gp_q, gst_p, gpl, c, p, hot_c, tw, logTW, &fq, &sm);
+    A.z.zp = zp;
+    A.z.q0 = zq0;
     pr->begin("fused_prop", fq * nq, st);
     k_fused_prop<<<dim3(A.nbx, nq), kFusedThreads, sm, st>>>(A);
     pr->end(st);
@@ -255,23 +268,27 @@ void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const 
 
 // ---------------------------------------------------------------- work lists
 __global__ void __launch_bounds__(kFusedThreads)
-kw_fused_build(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ tab) {
+kw_fused_build(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
-    fused_build_body(D[t.x], t.y, blockIdx.y);
+    FusedBuildArgs A = D[t.x];
+    A.z.q0 = q0;
+    fused_build_body(A, t.y, blockIdx.y);
 }
 __global__ void __launch_bounds__(kFusedThreads)
-kw_fused_prop(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ tab) {
+kw_fused_prop(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
-    fused_prop_body(D[t.x], t.y, blockIdx.y);
+    FusedPropArgs A = D[t.x];
+    A.z.q0 = q0;
+    fused_prop_body(A, t.y, blockIdx.y);
 }
 
-void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, size_t smem,
+void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
                            cudaStream_t st) {
     if (nctas <= 0 || nq <= 0) return;
     const dim3 g(nctas, nq);
     switch (op) {
-        case WOp::FusedBuild: kw_fused_build<<<g, kFusedThreads, smem, st>>>((const FusedBuildArgs *)desc, tab); break;
-        case WOp::FusedProp: kw_fused_prop<<<g, kFusedThreads, smem, st>>>((const FusedPropArgs *)desc, tab); break;
+        case WOp::FusedBuild: kw_fused_build<<<g, kFusedThreads, smem, st>>>((const FusedBuildArgs *)desc, tab, q0); break;
+        case WOp::FusedProp: kw_fused_prop<<<g, kFusedThreads, smem, st>>>((const FusedPropArgs *)desc, tab, q0); break;
         default: break;
     }
 }

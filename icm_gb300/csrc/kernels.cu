@@ -81,6 +81,7 @@ __device__ void school_build_body(const SchoolBuildArgs &A, int bx, int q) {
     if (j >= A.nreal_p) return;
     const double *L = A.Pc + q * A.Pc_q + (size_t)(2 * j) * pst_c;
     double *out = A.Pp + q * A.Pp_q + (size_t)j * pst_p;
+    if (zp_cold(A.z, q, j)) { out[t] = (t == A.z.span && t < A.lp) ? 1.0 : 0.0; return; }   // x^deg
     if (t >= A.lp) { out[t] = 0.0; return; }
     if (2 * j + 1 >= A.nreal_c) { out[t] = (t < lc) ? L[t] : 0.0; return; }
     const double *R = L + pst_c;
@@ -102,7 +103,7 @@ __device__ void school_prop_body(const SchoolPropArgs &A, int bx, int q) {
     const int gst_c = A.gst_c;
     const int c = A.c0 + (int)(idx / gst_c);
     const int m = (int)(idx % gst_c);
-    if (c >= A.nreal_c) return;
+    if (c >= A.nreal_c || zp_cold(A.z, q, c)) return;
     double *out = A.gc + q * A.gc_q + (size_t)c * gst_c;
     if (m >= A.gcl || (A.hot_c && !A.hot_c[c])) { out[m] = 0.0; return; }
     const double *g = A.gp + q * A.gp_q + (size_t)(c >> 1) * A.gst_p;
@@ -137,6 +138,7 @@ __device__ __forceinline__ void divide_body_t(const DivideArgs &A, int bx, int q
     const int bs = min(B, n - start);
     const int pk = min(bs, A.k);
     const double a = A.a[(size_t)q * A.aq + i];
+    if (a == 0.0) { *out = 0.0; return; }   // S logv < -700: zero weight (g of its block may be pruned)
     const double bb = 1.0 - a;
     const double *P = A.blockP + ((size_t)q * A.nblocks + b) * (B + 1);
     const double *g = A.g0 + q * A.g0_q + (size_t)b * A.gst0;
@@ -199,16 +201,25 @@ __global__ void k_scatter(int n, const double *__restrict__ acc, const int *__re
 // Batched complex transforms of size 2^logM, in place in `data` (natural
 // order).  Sizes up to kSmemFftMax run in one kernel; larger sizes use the
 // four-step split M = M1 * M2 through `scratch`.
-__global__ void k_fft_smem_fwd(double2 *data, long batch, int logM, int cb, const double2 *tw, int logTW);
-__global__ void k_fft_smem_inv(double2 *data, long batch, int logM, int cb, const double2 *tw, int logTW);
+__device__ __forceinline__ bool fft_skip(const FftSkip &k, long item) {
+    if (!k.zp) return false;
+    const long it = k.item0 + item;
+    const long q = it / k.per_q, j = it - q * k.per_q;
+    return (j + 1) * k.span <= (long)k.zp[k.q0 + q];
+}
 
 template <int SIGN>
 __global__ void k_fft_smem(double2 *__restrict__ data, long batch, int logM, int cb,
-                           const double2 *__restrict__ tw, int logTW) {
+                           const double2 *__restrict__ tw, int logTW, FftSkip skip) {
     extern __shared__ double2 sx[];
     const int M = 1 << logM;
     const long item0 = (long)blockIdx.x * cb;
     const int cnt = (int)min((long)cb, batch - item0);
+    if (skip.zp) {   // every item of the block wholly zero: nothing reads them
+        bool all = true;
+        for (int it = 0; it < cnt; ++it) all = all && fft_skip(skip, item0 + it);
+        if (all) return;
+    }
     for (int e = threadIdx.x; e < cnt * M; e += blockDim.x) {
         const int it = e >> logM, s = e & (M - 1);
         sx[e] = data[(item0 + it) * M + bitrev(s, logM)];
@@ -221,10 +232,11 @@ __global__ void k_fft_smem(double2 *__restrict__ data, long batch, int logM, int
 // four-step, pass A: columns n2 of the M1 x M2 view x[M2 n1 + n2]
 template <int SIGN>
 __global__ void k_fft4_cols(const double2 *__restrict__ in, double2 *__restrict__ out, int logM1, int logM2,
-                            int cb, const double2 *__restrict__ tw, int logTW) {
+                            int cb, const double2 *__restrict__ tw, int logTW, FftSkip skip) {
     extern __shared__ double2 sx[];
     const int M1 = 1 << logM1, M2 = 1 << logM2;
     const long item = blockIdx.y;
+    if (fft_skip(skip, item)) return;
     const int n20 = blockIdx.x * cb;
     const double2 *src = in + (item << (logM1 + logM2));
     for (int e = threadIdx.x; e < cb * M1; e += blockDim.x) {
@@ -248,10 +260,11 @@ __global__ void k_fft4_cols(const double2 *__restrict__ in, double2 *__restrict_
 // four-step, pass B: rows k1, FFT over n2, output X[k1 + M1 k2]
 template <int SIGN>
 __global__ void k_fft4_rows(const double2 *__restrict__ in, double2 *__restrict__ out, int logM1, int logM2,
-                            int cb, const double2 *__restrict__ tw, int logTW) {
+                            int cb, const double2 *__restrict__ tw, int logTW, FftSkip skip) {
     extern __shared__ double2 sx[];
     const int M1 = 1 << logM1, M2 = 1 << logM2;
     const long item = blockIdx.y;
+    if (fft_skip(skip, item)) return;
     const int k10 = blockIdx.x * cb;
     const double2 *src = in + (item << (logM1 + logM2));
     for (int e = threadIdx.x; e < cb * M2; e += blockDim.x) {
@@ -268,7 +281,7 @@ __global__ void k_fft4_rows(const double2 *__restrict__ in, double2 *__restrict_
 }
 
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
-                cudaStream_t st, long *launches, Prof *pr) {
+                cudaStream_t st, long *launches, Prof *pr, FftSkip skip) {
     if (batch <= 0) return 0;
     const int M = 1 << logM;
     const int threads = 256;
@@ -278,17 +291,20 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
         const size_t smem = (size_t)cb * M * sizeof(double2);
         pr->begin("fft_smem", 5.0 * M * logM * (double)batch, st);
         if (sign < 0)
-            k_fft_smem<-1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW);
+            k_fft_smem<-1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
         else
-            k_fft_smem<+1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW);
+            k_fft_smem<+1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
         pr->end(st);
         ++*launches;
         return 0;
     }
     if (batch > 65535) {   // grid.y limit of the four-step kernels
-        for (long b0 = 0; b0 < batch; b0 += 65535)
+        for (long b0 = 0; b0 < batch; b0 += 65535) {
+            FftSkip sk = skip;
+            sk.item0 += b0;
             fft_batched(data + (b0 << logM), scratch + (b0 << logM), std::min(65535L, batch - b0), logM, sign, tw,
-                        logTW, st, launches, pr);
+                        logTW, st, launches, pr, sk);
+        }
         return 0;
     }
     const int logM1 = (logM + 1) / 2, logM2 = logM - logM1;
@@ -298,12 +314,12 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
     dim3 gA(M2 / cbA, (unsigned)batch), gB(M1 / cbB, (unsigned)batch);
     const size_t smA = (size_t)cbA * M1 * sizeof(double2), smB = (size_t)cbB * M2 * sizeof(double2);
     pr->begin("fft4_cols", (5.0 * logM1 + 6.0) * M * (double)batch, st);
-    if (sign < 0) k_fft4_cols<-1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW);
-    else k_fft4_cols<+1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW);
+    if (sign < 0) k_fft4_cols<-1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    else k_fft4_cols<+1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
     pr->end(st);
     pr->begin("fft4_rows", 5.0 * logM2 * M * (double)batch, st);
-    if (sign < 0) k_fft4_rows<-1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW);
-    else k_fft4_rows<+1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW);
+    if (sign < 0) k_fft4_rows<-1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW, skip);
+    else k_fft4_rows<+1><<<gB, threads, smB, st>>>(scratch, data, logM1, logM2, cbB, tw, logTW, skip);
     pr->end(st);
     *launches += 2;
     return 0;
@@ -486,7 +502,7 @@ DivideArgs divide_args(int B, int n, int k, int nblocks, const double *S, const 
 SchoolBuildArgs school_build_args(const Level &c, const Level &p, int j0, double *fq) {
     const long work = (long)(p.nreal - j0) * p.pst;
     SchoolBuildArgs A{c.P, c.P_q, c.pst, c.plen, c.nreal, p.P, p.P_q, p.pst, p.plen, p.nreal, j0,
-                      work > 0 ? (int)nblk(work, 256) : 0};
+                      work > 0 ? (int)nblk(work, 256) : 0, ZeroPrefix{nullptr, 0, p.deg}};
     if (fq) {
         double terms = 0.0;   // multiply-adds of one full pair: sum_t (ihi - ilo + 1)
         for (int t = 0; t < p.plen; ++t) terms += std::min(t, c.plen - 1) - std::max(0, t - (c.plen - 1)) + 1;
@@ -500,7 +516,7 @@ SchoolPropArgs school_prop_args(const double *gp, size_t gp_q, int gst_p, int gp
                                 int c0, double *fq) {
     const long work = (long)(c.nreal - c0) * c.gst;
     SchoolPropArgs A{gp, gp_q, gst_p, gpl, c.P, c.P_q, c.pst, c.plen, c.g, c.g_q, c.gst, c.glen, c.nreal, hot_c, c0,
-                     work > 0 ? (int)nblk(work, 256) : 0};
+                     work > 0 ? (int)nblk(work, 256) : 0, ZeroPrefix{nullptr, 0, c.deg}};
     if (fq) {
         double terms = 0.0;   // per child with a sibling: sum_m min(lc, gpl - m)
         for (int m = 0; m < c.glen; ++m) terms += std::max(0, std::min(c.plen, gpl - m));
@@ -531,9 +547,12 @@ void launch_divide(int B, int n, int k, int nblocks, const double *S, const doub
     pr->end(st);
 }
 
-void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStream_t st, Prof *pr) {
+void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStream_t st, Prof *pr, const int *zp,
+                         int zq0) {
     double fq = 0.0;
     SchoolBuildArgs A = school_build_args(c, p, j0, &fq);
+    A.z.zp = zp;
+    A.z.q0 = zq0;
     if (A.nbx <= 0) return;
     pr->begin("school_build", fq * nq, st);
     k_school_build<<<dim3(A.nbx, nq), 256, 0, st>>>(A);
@@ -541,9 +560,11 @@ void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStr
 }
 
 void launch_school_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, int nq,
-                        const uint8_t *hot_c, int c0, cudaStream_t st, Prof *pr) {
+                        const uint8_t *hot_c, int c0, cudaStream_t st, Prof *pr, const int *zp, int zq0) {
     double fq = 0.0;
     SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, c, hot_c, c0, &fq);
+    A.z.zp = zp;
+    A.z.q0 = zq0;
     if (A.nbx <= 0) return;
     pr->begin("school_prop", fq * nq, st);
     k_school_prop<<<dim3(A.nbx, nq), 256, 0, st>>>(A);
@@ -563,13 +584,17 @@ __global__ void kw_divide(const DivideArgs *__restrict__ D, const int2 *__restri
     A.q0 = q0;
     divide_body(A, t.y, blockIdx.y);
 }
-__global__ void kw_school_build(const SchoolBuildArgs *__restrict__ D, const int2 *__restrict__ tab) {
+__global__ void kw_school_build(const SchoolBuildArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
-    school_build_body(D[t.x], t.y, blockIdx.y);
+    SchoolBuildArgs A = D[t.x];
+    A.z.q0 = q0;
+    school_build_body(A, t.y, blockIdx.y);
 }
-__global__ void kw_school_prop(const SchoolPropArgs *__restrict__ D, const int2 *__restrict__ tab) {
+__global__ void kw_school_prop(const SchoolPropArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
-    school_prop_body(D[t.x], t.y, blockIdx.y);
+    SchoolPropArgs A = D[t.x];
+    A.z.q0 = q0;
+    school_prop_body(A, t.y, blockIdx.y);
 }
 
 void launch_worklist_basic(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, cudaStream_t st) {
@@ -578,8 +603,8 @@ void launch_worklist_basic(WOp op, const void *desc, const int2 *tab, int nctas,
     switch (op) {
         case WOp::Leaf: kw_leaf<<<g, 128, 0, st>>>((const LeafArgs *)desc, tab, q0); break;
         case WOp::Divide: kw_divide<<<g, 128, 0, st>>>((const DivideArgs *)desc, tab, q0); break;
-        case WOp::SchoolBuild: kw_school_build<<<g, 256, 0, st>>>((const SchoolBuildArgs *)desc, tab); break;
-        case WOp::SchoolProp: kw_school_prop<<<g, 256, 0, st>>>((const SchoolPropArgs *)desc, tab); break;
+        case WOp::SchoolBuild: kw_school_build<<<g, 256, 0, st>>>((const SchoolBuildArgs *)desc, tab, q0); break;
+        case WOp::SchoolProp: kw_school_prop<<<g, 256, 0, st>>>((const SchoolPropArgs *)desc, tab, q0); break;
         default: break;
     }
 }
@@ -598,11 +623,12 @@ void launch_scatter(int n, const double *acc, const int *perm, const uint8_t *ac
 // FFT build for parents [0, npairs) of level p (children c); spectra only when
 // U == nullptr (the root level, whose product is never used).
 void launch_fft_build(const Level &c, const Level &p, int nq, double2 *fa, double2 *fb, double2 *fc,
-                      bool spectra_only, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr) {
+                      bool spectra_only, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr,
+                      const int *zp, int zq0) {
     const int N = p.fftn, npairs = p.npairs;
     if (npairs <= 0) return;
     if (fused_ok(N)) {
-        launch_fused_build(c, p, nq, spectra_only, tw, logTW, st, pr);
+        launch_fused_build(c, p, nq, spectra_only, tw, logTW, st, pr, zp, zq0);
         ++*launches;
         return;
     }
@@ -630,11 +656,11 @@ void launch_fft_build(const Level &c, const Level &p, int nq, double2 *fa, doubl
 
 void launch_fft_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
                      const uint8_t *hot_c, double2 *fa, double2 *fb, double2 *fc, const double2 *tw, int logTW,
-                     cudaStream_t st, long *launches, Prof *pr) {
+                     cudaStream_t st, long *launches, Prof *pr, const int *zp, int zq0) {
     const int N = p.fftn, npairs = p.npairs;
     if (npairs <= 0) return;
     if (fused_ok(N)) {
-        launch_fused_prop(gp, gp_q, gst_p, gpl, c, p, nq, hot_c, tw, logTW, st, pr);
+        launch_fused_prop(gp, gp_q, gst_p, gpl, c, p, nq, hot_c, tw, logTW, st, pr, zp, zq0);
         ++*launches;
         return;
     }

@@ -42,6 +42,22 @@ struct Prof {
     }
 };
 
+// Zero prefix of a quadrature node: players are sorted by stack, descending,
+// so the players whose leaf factor a = exp(S logv) is exactly 0 (S logv < -700)
+// are the first zp[q0 + q] of them.  A tree node lying wholly inside that
+// prefix is the monomial x^deg and nothing of it reaches an equity (those
+// players' weights are 0): builds write the monomial without transforms,
+// propagates skip it.  span = players under one node of the level the kernel
+// decides on.  zp == nullptr: no pruning.
+struct ZeroPrefix {
+    const int *zp;
+    int q0;
+    long span;
+};
+__host__ __device__ __forceinline__ bool zp_cold(const ZeroPrefix &z, int q, long node) {
+    return z.zp && (node + 1) * z.span <= (long)z.zp[z.q0 + q];
+}
+
 // ---- kernel argument blocks.  Each kernel body is a __device__ function of
 // (args, bx, q): bx the block index within one tree level of one tournament,
 // q the quadrature node within the chunk.  Single plans launch it with
@@ -64,6 +80,7 @@ struct SchoolBuildArgs {
     size_t Pp_q;
     int pst_p, lp, nreal_p, j0;
     int nbx;
+    ZeroPrefix z;
 };
 struct SchoolPropArgs {
     const double *gp;
@@ -78,6 +95,7 @@ struct SchoolPropArgs {
     const uint8_t *hot_c;
     int c0;
     int nbx;
+    ZeroPrefix z;
 };
 struct DivideArgs {
     int B, n, k, nblocks;
@@ -103,6 +121,7 @@ struct SpecInitArgs {
     const double2 *tw;
     int logTW;
     int nbx;
+    ZeroPrefix z;
 };
 struct SpecBuildArgs {
     const double2 *cspec;
@@ -120,6 +139,7 @@ struct SpecBuildArgs {
     const double2 *tw;
     int logTW;
     int nbx;
+    ZeroPrefix z;
 };
 struct GspecArgs {
     const double *g;
@@ -131,6 +151,7 @@ struct GspecArgs {
     const double2 *tw;
     int logTW;
     int nbx;
+    ZeroPrefix z;
 };
 struct SpecPropArgs {
     const double2 *Gp;
@@ -147,6 +168,7 @@ struct SpecPropArgs {
     const double2 *tw;
     int logTW;
     int nbx;
+    ZeroPrefix z;
 };
 struct FusedBuildArgs {
     const double *Pc;
@@ -159,6 +181,7 @@ struct FusedBuildArgs {
     const double2 *tw;
     int logTW, spectra_only;
     int nbx;
+    ZeroPrefix z;
 };
 struct FusedPropArgs {
     const double *gp;
@@ -172,6 +195,7 @@ struct FusedPropArgs {
     const double2 *tw;
     int logTW;
     int nbx;
+    ZeroPrefix z;
 };
 
 // ---- argument builders shared by the single-plan launchers and the work
@@ -203,8 +227,10 @@ FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl,
 // block within the descriptor), blockIdx.y = node within the chunk.
 enum class WOp : int { Leaf, SchoolBuild, SchoolProp, Divide, SpecInit, SpecBuild, Gspec, SpecProp, FusedBuild, FusedProp };
 void launch_worklist_basic(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, cudaStream_t st);
-void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, size_t smem, cudaStream_t st);
-void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, size_t smem, cudaStream_t st);
+void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                          cudaStream_t st);
+void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                           cudaStream_t st);
 size_t spec_smem_bytes(int M);     // dynamic shared memory of the spectral kernels
 size_t fused_smem_bytes(int N);    // dynamic shared memory of the fused kernels
 
@@ -214,48 +240,65 @@ void fft_set_smem_limits();
 bool fused_ok(int N);
 void fused_set_smem_limits();
 void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_only, const double2 *tw, int logTW,
-                        cudaStream_t st, Prof *pr);
+                        cudaStream_t st, Prof *pr, const int *zp = nullptr, int zq0 = 0);
 // spectral levels (spectral.cu)
 constexpr int kSpecMaxD = 8192;   // largest child degree of a spectral level
 void spec_set_smem_limits();
-void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
+void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cudaStream_t st, Prof *pr,
+                      const int *zp = nullptr, int zq0 = 0);
 void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq, const double2 *tw, int logTW,
-                       cudaStream_t st, Prof *pr);
+                       cudaStream_t st, Prof *pr, const int *zp = nullptr, int zq0 = 0);
 void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G,
                        size_t G_q, int nq, const uint8_t *hot, const double2 *tw, int logTW, cudaStream_t st,
-                       Prof *pr);
+                       Prof *pr, const int *zp = nullptr, int zq0 = 0);
 void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral, int nq,
-                      const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
+                      const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr,
+                      const int *zp = nullptr, int zq0 = 0);
 
 // spectral levels with transforms beyond one CTA (spectral_big.cu)
 void launch_specbig_build(const Level &c, const Level &p, bool write_coeffs, int nq, double2 *buf, double2 *scratch,
-                          const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr);
+                          const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr,
+                          const int *zp = nullptr, int zq0 = 0);
 void launch_specbig_prop(const double2 *Gp, size_t Gp_q, const Level &c, int nq, const uint8_t *hot_c, double2 *buf,
-                         double2 *scratch, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr);
+                         double2 *scratch, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr,
+                         const int *zp = nullptr, int zq0 = 0);
 void launch_gspecbig_init(const double *g, size_t g_q, int gst, int glen, int nreal, int logd, double2 *G, size_t G_q,
                           int nq, const uint8_t *hot, double2 *buf, double2 *scratch, const double2 *tw, int logTW,
-                          cudaStream_t st, long *launches, Prof *pr);
+                          cudaStream_t st, long *launches, Prof *pr, const int *zp = nullptr, int zq0 = 0);
 
 void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
-                       const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr);
+                       const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr,
+                       const int *zp = nullptr, int zq0 = 0);
+// items of a batched transform that lie wholly inside a node's zero prefix
+// are skipped: item i is tree node (i % per_q) of chunk node (i / per_q)
+struct FftSkip {
+    const int *zp = nullptr;
+    int q0 = 0;
+    long span = 0;
+    int per_q = 1;
+    long item0 = 0;
+};
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
-                cudaStream_t st, long *launches, Prof *pr);
+                cudaStream_t st, long *launches, Prof *pr, FftSkip skip = FftSkip());
 
 void launch_leaf(int B, int n, int nblocks, const double *S, const double *node, int q0, int nq, double *a,
                  double *blockP, double *P0, int pst0, int plen0, cudaStream_t st, Prof *pr);
 void launch_divide(int B, int n, int k, int nblocks, const double *S, const double *node, int q0, int nq,
                    const double *a, const double *blockP, const double *g0, size_t g0_q, int gst0,
                    const uint8_t *active, double *contrib, cudaStream_t st, Prof *pr);
-void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStream_t st, Prof *pr);
+void launch_school_build(const Level &c, const Level &p, int nq, int j0, cudaStream_t st, Prof *pr,
+                         const int *zp = nullptr, int zq0 = 0);
 void launch_school_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, int nq,
-                        const uint8_t *hot_c, int c0, cudaStream_t st, Prof *pr);
+                        const uint8_t *hot_c, int c0, cudaStream_t st, Prof *pr, const int *zp = nullptr,
+                        int zq0 = 0);
 void launch_accumulate(int n, int nq, const double *contrib, double *acc, int first, cudaStream_t st, Prof *pr);
 void launch_scatter(int n, const double *acc, const int *perm, const uint8_t *active, double *out,
                     cudaStream_t st);
 void launch_fft_build(const Level &c, const Level &p, int nq, double2 *fa, double2 *fb, double2 *fc,
-                      bool spectra_only, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr);
+                      bool spectra_only, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr,
+                      const int *zp = nullptr, int zq0 = 0);
 void launch_fft_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
                      const uint8_t *hot_c, double2 *fa, double2 *fb, double2 *fc, const double2 *tw, int logTW,
-                     cudaStream_t st, long *launches, Prof *pr);
+                     cudaStream_t st, long *launches, Prof *pr, const int *zp = nullptr, int zq0 = 0);
 
 }  // namespace icmg

@@ -67,6 +67,18 @@ __device__ void spec_init_body(const SpecInitArgs &A, int bx, int q) {
         const int j0 = bx * cb;
     const int cnt = min(cb, nreal - j0);
     if (cnt <= 0) return;
+    if (zp_cold(A.z, q, j0 + cnt - 1)) {   // every node x^d: spec2 = (-1)^f, ends (0, 1)
+        for (int e = threadIdx.x; e < cnt * (d + 1); e += blockDim.x) {
+            const int it = e / (d + 1), f = e - it * (d + 1);
+            spec2[q * s2_q + (size_t)(j0 + it) * (d + 1) + f] = make_double2((f & 1) ? -1.0 : 1.0, 0.0);
+            if (f == 0) {
+                double *en = ends + q * e_q + (size_t)(j0 + it) * 2;
+                en[0] = 0.0;
+                en[1] = (d < plen) ? 1.0 : 0.0;
+            }
+        }
+        return;
+    }
     for (int e = threadIdx.x; e < cnt * d; e += blockDim.x) {
         const int it = e >> logd, r = e & (d - 1);
         const int s = (int)bitrev(r, logd);
@@ -134,6 +146,22 @@ __device__ void spec_build_body(const SpecBuildArgs &A, int bx, int q) {
         const int j0 = bx * cb;
     const int cnt = min(cb, nreal_p - j0);
     if (cnt <= 0) return;
+    if (zp_cold(A.z, q, j0 + cnt - 1)) {   // every parent x^{2D}
+        const int nb2 = 2 * D + 1;
+        const int per = max(nb2, Pout ? pst_p : 0);
+        for (int e = threadIdx.x; e < cnt * per; e += blockDim.x) {
+            const int it = e / per, f = e - it * per;
+            const int j = j0 + it;
+            if (pspec && f < nb2) pspec[q * ps_q + (size_t)j * nb2 + f] = make_double2((f & 1) ? -1.0 : 1.0, 0.0);
+            if (pends && f == 0) {
+                double *en = pends + q * pe_q + (size_t)j * 2;
+                en[0] = 0.0;
+                en[1] = 1.0;
+            }
+            if (Pout && f < pst_p) Pout[q * Po_q + (size_t)j * pst_p + f] = (f == 2 * D && f < plen_p) ? 1.0 : 0.0;
+        }
+        return;
+    }
     const double2 one = make_double2(1.0, 0.0);
     // 1. product spectrum (even bins of spec2(X)) and the inverse input, by mirror pairs
     const int np1 = hD + 1;
@@ -230,7 +258,7 @@ __device__ void gspec_body(const GspecArgs &A, int bx, int q) {
     const int cb = h >= 4096 ? 1 : 4096 / h;
         const int j0 = bx * cb;
     const int cnt = min(cb, nreal - j0);
-    if (cnt <= 0) return;
+    if (cnt <= 0 || zp_cold(A.z, q, j0 + cnt - 1)) return;   // nothing below reads a wholly-zero node's g
     for (int e = threadIdx.x; e < cnt * h; e += blockDim.x) {
         const int it = e >> lh, r = e & (h - 1);
         const int s = (int)bitrev(r, lh);
@@ -297,7 +325,7 @@ __device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
     const int cbp = D >= 4096 ? 1 : 4096 / D;            // parents per CTA; 2 children each
         const int j0 = bx * cbp;
     const int cnt = min(cbp, npar - j0);
-    if (cnt <= 0) return;
+    if (cnt <= 0 || zp_cold(A.z, q, j0 + cnt - 1)) return;   // wholly-zero parents: no child g is read
     const int nk = 2 * cnt;                               // children handled, h slots each
     const double2 one = make_double2(1.0, 0.0);
     if (hot_c) {   // subset pruning: nothing below a cold child is ever read
@@ -433,7 +461,7 @@ SpecInitArgs spec_init_args(const Level &v, const double2 *tw, int logTW, double
     if (fq) *fq = (5.0 * d * logd + 20.0 * d) * v.nreal;
     if (smem) *smem = spec_smem(d);
     return SpecInitArgs{v.P, v.P_q, v.pst, v.plen, v.nreal, logd, v.spec2, v.spec2_q, v.ends, v.ends_q, tw, logTW,
-                        (v.nreal + cb - 1) / cb};
+                        (v.nreal + cb - 1) / cb, ZeroPrefix{nullptr, 0, v.deg}};
 }
 
 SpecBuildArgs spec_build_args(const Level &c, const Level &p, bool write_coeffs, const double2 *tw, int logTW,
@@ -444,7 +472,7 @@ SpecBuildArgs spec_build_args(const Level &c, const Level &p, bool write_coeffs,
     if (smem) *smem = spec_smem(D);
     return SpecBuildArgs{c.spec2, c.spec2_q, c.ends, c.ends_q, c.nreal, p.nreal, logD, p.spec2, p.spec2_q,
                          p.spec2 ? p.ends : nullptr, p.ends_q, write_coeffs ? p.P : nullptr, p.P_q, p.pst, p.plen, tw,
-                         logTW, (p.nreal + cb - 1) / cb};
+                         logTW, (p.nreal + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}};
 }
 
 GspecArgs gspec_args(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G, size_t G_q,
@@ -453,7 +481,8 @@ GspecArgs gspec_args(const double *g, size_t g_q, int gst, int glen, int nreal, 
     const int cb = spec_cb(h);
     if (fq) *fq = (5.0 * h * (logd - 1) + 20.0 * h) * nreal;
     if (smem) *smem = spec_smem(h);
-    return GspecArgs{g, g_q, gst, glen, nreal, logd, G, G_q, hot, tw, logTW, (nreal + cb - 1) / cb};
+    return GspecArgs{g, g_q, gst, glen, nreal, logd, G, G_q, hot, tw, logTW, (nreal + cb - 1) / cb,
+                     ZeroPrefix{nullptr, 0, v.deg}};
 }
 
 SpecPropArgs spec_prop_args(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral,
@@ -463,23 +492,29 @@ SpecPropArgs spec_prop_args(const double2 *Gp, size_t Gp_q, const Level &c, cons
     if (fq) *fq = (2.0 * 2 * 5.0 * (D / 2) * (logD - 1) + 60.0 * D) * p.nreal;
     if (smem) *smem = spec_smem(D);
     return SpecPropArgs{Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, p.nreal, logD, children_spectral ? c.G : nullptr,
-                        c.G_q, c.g, c.g_q, c.gst, c.glen, hot_c, tw, logTW, (p.nreal + cbp - 1) / cbp};
+                        c.G_q, c.g, c.g_q, c.gst, c.glen, hot_c, tw, logTW, (p.nreal + cbp - 1) / cbp,
+                        ZeroPrefix{nullptr, 0, p.deg}};
 }
 
-void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cudaStream_t st, Prof *pr) {
+void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cudaStream_t st, Prof *pr, const int *zp,
+                      int zq0) {
     double fq = 0.0;
     size_t sm = 0;
     SpecInitArgs A = spec_init_args(v, tw, logTW, &fq, &sm);
+    A.z.zp = zp;
+    A.z.q0 = zq0;
     pr->begin("spec_init", fq * nq, st);
     k_spec_init<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
     pr->end(st);
 }
 
 void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq, const double2 *tw, int logTW,
-                       cudaStream_t st, Prof *pr) {
+                       cudaStream_t st, Prof *pr, const int *zp, int zq0) {
     double fq = 0.0;
     size_t sm = 0;
     SpecBuildArgs A = spec_build_args(c, p, write_coeffs, tw, logTW, &fq, &sm);
+    A.z.zp = zp;
+    A.z.q0 = zq0;
     pr->begin("spec_build", fq * nq, st);
     k_spec_build<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
     pr->end(st);
@@ -487,20 +522,25 @@ void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq
 
 void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G,
                        size_t G_q, int nq, const uint8_t *hot, const double2 *tw, int logTW, cudaStream_t st,
-                       Prof *pr) {
+                       Prof *pr, const int *zp, int zq0) {
     double fq = 0.0;
     size_t sm = 0;
     GspecArgs A = gspec_args(g, g_q, gst, glen, nreal, v, G, G_q, hot, tw, logTW, &fq, &sm);
+    A.z.zp = zp;
+    A.z.q0 = zq0;
     pr->begin("gspec_init", fq * nq, st);
     k_gspec_init<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
     pr->end(st);
 }
 
 void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral, int nq,
-                      const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr) {
+                      const uint8_t *hot_c, const double2 *tw, int logTW, cudaStream_t st, Prof *pr, const int *zp,
+                      int zq0) {
     double fq = 0.0;
     size_t sm = 0;
     SpecPropArgs A = spec_prop_args(Gp, Gp_q, c, p, children_spectral, hot_c, tw, logTW, &fq, &sm);
+    A.z.zp = zp;
+    A.z.q0 = zq0;
     pr->begin("spec_prop", fq * nq, st);
     k_spec_prop<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
     pr->end(st);
@@ -508,24 +548,32 @@ void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Leve
 
 // ---------------------------------------------------------------- work lists
 __global__ void __launch_bounds__(kSpecThreads)
-kw_spec_init(const SpecInitArgs *__restrict__ D, const int2 *__restrict__ tab) {
+kw_spec_init(const SpecInitArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
-    spec_init_body(D[t.x], t.y, blockIdx.y);
+    SpecInitArgs A = D[t.x];
+    A.z.q0 = q0;
+    spec_init_body(A, t.y, blockIdx.y);
 }
 __global__ void __launch_bounds__(kSpecThreads)
-kw_spec_build(const SpecBuildArgs *__restrict__ D, const int2 *__restrict__ tab) {
+kw_spec_build(const SpecBuildArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
-    spec_build_body(D[t.x], t.y, blockIdx.y);
+    SpecBuildArgs A = D[t.x];
+    A.z.q0 = q0;
+    spec_build_body(A, t.y, blockIdx.y);
 }
 __global__ void __launch_bounds__(kSpecThreads)
-kw_gspec(const GspecArgs *__restrict__ D, const int2 *__restrict__ tab) {
+kw_gspec(const GspecArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
-    gspec_body(D[t.x], t.y, blockIdx.y);
+    GspecArgs A = D[t.x];
+    A.z.q0 = q0;
+    gspec_body(A, t.y, blockIdx.y);
 }
 __global__ void __launch_bounds__(kSpecThreads)
-kw_spec_prop(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ tab) {
+kw_spec_prop(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
-    spec_prop_body(D[t.x], t.y, blockIdx.y);
+    SpecPropArgs A = D[t.x];
+    A.z.q0 = q0;
+    spec_prop_body(A, t.y, blockIdx.y);
 }
 
 void spec_wl_set_smem_limits() {
@@ -536,14 +584,15 @@ void spec_wl_set_smem_limits() {
     cudaFuncSetAttribute(kw_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
-void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, size_t smem, cudaStream_t st) {
+void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                          cudaStream_t st) {
     if (nctas <= 0 || nq <= 0) return;
     const dim3 g(nctas, nq);
     switch (op) {
-        case WOp::SpecInit: kw_spec_init<<<g, kSpecThreads, smem, st>>>((const SpecInitArgs *)desc, tab); break;
-        case WOp::SpecBuild: kw_spec_build<<<g, kSpecThreads, smem, st>>>((const SpecBuildArgs *)desc, tab); break;
-        case WOp::Gspec: kw_gspec<<<g, kSpecThreads, smem, st>>>((const GspecArgs *)desc, tab); break;
-        case WOp::SpecProp: kw_spec_prop<<<g, kSpecThreads, smem, st>>>((const SpecPropArgs *)desc, tab); break;
+        case WOp::SpecInit: kw_spec_init<<<g, kSpecThreads, smem, st>>>((const SpecInitArgs *)desc, tab, q0); break;
+        case WOp::SpecBuild: kw_spec_build<<<g, kSpecThreads, smem, st>>>((const SpecBuildArgs *)desc, tab, q0); break;
+        case WOp::Gspec: kw_gspec<<<g, kSpecThreads, smem, st>>>((const GspecArgs *)desc, tab, q0); break;
+        case WOp::SpecProp: kw_spec_prop<<<g, kSpecThreads, smem, st>>>((const SpecPropArgs *)desc, tab, q0); break;
         default: break;
     }
 }

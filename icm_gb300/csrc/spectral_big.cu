@@ -18,16 +18,28 @@ static inline int ilog2b(long v) {
 }
 static inline unsigned nb(long work, int threads) { return (unsigned)((work + threads - 1) / threads); }
 __device__ __forceinline__ double2 twb(const double2 *__restrict__ tw, long idx) { return __ldg(&tw[idx]); }
+// tree node `node` of chunk node q lies wholly inside the zero prefix
+__device__ __forceinline__ bool zcold(const int *__restrict__ zp, int zq0, long span, int q, long node) {
+    return zp && (node + 1) * span <= (long)zp[zq0 + q];
+}
 
 // ---- build: 1. even bins of spec2(X) and the inverse input U (mirror pairs)
 __global__ void k_sb_build1(const double2 *__restrict__ cspec, size_t cs_q, int nreal_c, int nreal_p, int logD,
                             double2 *__restrict__ pspec, size_t ps_q, double2 *__restrict__ buf,
-                            const double2 *__restrict__ tw, int logTW) {
+                            const double2 *__restrict__ tw, int logTW, const int *__restrict__ zp, int zq0) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int D = 1 << logD, hD = D >> 1, np1 = hD + 1;
     const int j = (int)(idx / np1), f = (int)(idx % np1);
     if (j >= nreal_p) return;
+    if (zcold(zp, zq0, 2L * D, q, j)) {   // x^{2D}: even bins of spec2 are 1
+        if (pspec) {
+            double2 *ps = pspec + q * ps_q + (size_t)j * (2 * D + 1);
+            ps[2 * f] = make_double2(1.0, 0.0);
+            ps[2 * (D - f)] = make_double2(1.0, 0.0);
+        }
+        return;
+    }
     const double2 one = make_double2(1.0, 0.0);
     const double2 *sL = cspec + q * cs_q + (size_t)(2 * j) * (D + 1);
     const bool has_r = (2 * j + 1) < nreal_c;
@@ -51,12 +63,29 @@ __global__ void k_sb_build1(const double2 *__restrict__ cspec, size_t cs_q, int 
 __global__ void k_sb_build2(const double *__restrict__ cends, size_t ce_q, int nreal_c, int nreal_p, int logD,
                             double *__restrict__ pends, size_t pe_q, double *__restrict__ Pout, size_t Po_q,
                             int pst_p, int plen_p, double2 *__restrict__ buf, const double2 *__restrict__ tw,
-                            int logTW) {
+                            int logTW, const int *__restrict__ zp, int zq0) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int D = 1 << logD;
     const int j = (int)(idx >> logD), s = (int)(idx & (D - 1));
     if (j >= nreal_p) return;
+    if (zcold(zp, zq0, 2L * D, q, j)) {   // x^{2D}: coefficients and ends
+        if (Pout) {
+            double *out = Pout + q * Po_q + (size_t)j * pst_p;
+            if (2 * s < plen_p) out[2 * s] = 0.0;
+            if (2 * s + 1 < plen_p) out[2 * s + 1] = 0.0;
+            if (s == 0) {
+                if (2 * D < plen_p) out[2 * D] = 1.0;
+                for (int t = 2 * D + 1; t < pst_p; ++t) out[t] = 0.0;
+            }
+        }
+        if (s == 0 && pends) {
+            double *en = pends + q * pe_q + (size_t)j * 2;
+            en[0] = 0.0;
+            en[1] = 1.0;
+        }
+        return;
+    }
     double2 *up = buf + ((size_t)q * nreal_p + j) * D + s;
     double2 u = *up;
     const double *eL = cends + q * ce_q + (size_t)(2 * j) * 2;
@@ -89,12 +118,19 @@ __global__ void k_sb_build2(const double *__restrict__ cends, size_t ce_q, int n
 
 // ---- build: 3. odd bins from the forward transform (mirror pairs f, D-1-f)
 __global__ void k_sb_build3(int nreal_p, int logD, double2 *__restrict__ pspec, size_t ps_q,
-                            const double2 *__restrict__ buf, const double2 *__restrict__ tw, int logTW) {
+                            const double2 *__restrict__ buf, const double2 *__restrict__ tw, int logTW,
+                            const int *__restrict__ zp, int zq0) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int D = 1 << logD, hD = D >> 1;
     const int j = (int)(idx / hD), f = (int)(idx % hD);
     if (j >= nreal_p) return;
+    if (zcold(zp, zq0, 2L * D, q, j)) {   // x^{2D}: odd bins of spec2 are -1
+        double2 *ps = pspec + q * ps_q + (size_t)j * (2 * D + 1);
+        ps[2 * f + 1] = make_double2(-1.0, 0.0);
+        ps[2 * (D - 1 - f) + 1] = make_double2(-1.0, 0.0);
+        return;
+    }
     const double2 *c = buf + ((size_t)q * nreal_p + j) * D;
     const double2 a = c[f], b = cconj(c[D - 1 - f]);
     const double2 Ep = cadd(a, b);
@@ -108,12 +144,14 @@ __global__ void k_sb_build3(int nreal_p, int logD, double2 *__restrict__ pspec, 
 // ---- propagate (children get g spectra): 1. inverse half-bin input per child
 __global__ void k_sb_prop1(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restrict__ cspec,
                            size_t cs_q, int nreal_c, int logD, double2 *__restrict__ buf,
-                           const uint8_t *__restrict__ hot_c, const double2 *__restrict__ tw, int logTW) {
+                           const uint8_t *__restrict__ hot_c, const double2 *__restrict__ tw, int logTW,
+                           const int *__restrict__ zp, int zq0) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int D = 1 << logD, h = D >> 1, hp = (h + 1) >> 1;
     const int c = (int)(idx / hp), f = (int)(idx % hp);
     if (c >= nreal_c || (hot_c && !hot_c[c])) return;   // cold: output zeroed in pass 3
+    if (zcold(zp, zq0, D, q, c)) return;                 // wholly zero: never read
     const int fp = h - 1 - f;
     const int j = c >> 1, sib = c ^ 1;
     const double2 one = make_double2(1.0, 0.0);
@@ -131,12 +169,12 @@ __global__ void k_sb_prop1(const double2 *__restrict__ Gp, size_t Gp_q, const do
 
 // ---- propagate: 2. untwist in place (unscaled)
 __global__ void k_sb_prop2(int nreal_c, int logD, double2 *__restrict__ buf, const double2 *__restrict__ tw,
-                           int logTW) {
+                           int logTW, const int *__restrict__ zp, int zq0) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int h = 1 << (logD - 1);
     const int c = (int)(idx >> (logD - 1)), s = (int)(idx & (h - 1));
-    if (c >= nreal_c || s == 0) return;
+    if (c >= nreal_c || s == 0 || zcold(zp, zq0, 1L << logD, q, c)) return;
     double2 *x = buf + ((size_t)q * nreal_c + c) * h + s;
     *x = cmulc(*x, twb(tw, (long)s << (logTW - logD)));
 }
@@ -145,12 +183,12 @@ __global__ void k_sb_prop2(int nreal_c, int logD, double2 *__restrict__ buf, con
 __global__ void k_sb_prop3(const double2 *__restrict__ Gp, size_t Gp_q, const double2 *__restrict__ cspec,
                            size_t cs_q, int nreal_c, int logD, const double2 *__restrict__ buf,
                            double2 *__restrict__ Gout, size_t Go_q, const uint8_t *__restrict__ hot_c,
-                           const double2 *__restrict__ tw, int logTW) {
+                           const double2 *__restrict__ tw, int logTW, const int *__restrict__ zp, int zq0) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int D = 1 << logD, h = D >> 1, hq = (h >> 1) + 1;
     const int c = (int)(idx / hq), f = (int)(idx % hq);
-    if (c >= nreal_c) return;
+    if (c >= nreal_c || zcold(zp, zq0, D, q, c)) return;
     const int fp = h - f;
     double2 *out = Gout + q * Go_q + (size_t)c * (h + 1);
     if (hot_c && !hot_c[c]) {
@@ -180,24 +218,25 @@ __global__ void k_sb_prop3(const double2 *__restrict__ Gp, size_t Gp_q, const do
 
 // ---- g spectra from coefficients: pack, transform, post
 __global__ void k_sb_gpack(const double *__restrict__ g, size_t g_q, int gst, int glen, int nreal, int logd,
-                           double2 *__restrict__ buf) {
+                           double2 *__restrict__ buf, const int *__restrict__ zp, int zq0) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int h = 1 << (logd - 1);
     const int j = (int)(idx >> (logd - 1)), s = (int)(idx & (h - 1));
-    if (j >= nreal) return;
+    if (j >= nreal || zcold(zp, zq0, 1L << logd, q, j)) return;
     const double *x = g + q * g_q + (size_t)j * gst;
     const int t0 = 2 * s, t1 = 2 * s + 1;
     buf[((size_t)q * nreal + j) * h + s] = make_double2(t0 < glen ? x[t0] : 0.0, t1 < glen ? x[t1] : 0.0);
 }
 
 __global__ void k_sb_gpost(int nreal, int logd, const double2 *__restrict__ buf, double2 *__restrict__ G, size_t G_q,
-                           const uint8_t *__restrict__ hot, const double2 *__restrict__ tw, int logTW) {
+                           const uint8_t *__restrict__ hot, const double2 *__restrict__ tw, int logTW,
+                           const int *__restrict__ zp, int zq0) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int h = 1 << (logd - 1);
     const int j = (int)(idx >> (logd - 1)), f = (int)(idx & (h - 1));
-    if (j >= nreal) return;
+    if (j >= nreal || zcold(zp, zq0, 1L << logd, q, j)) return;
     double2 *out = G + q * G_q + (size_t)j * (h + 1);
     if (hot && !hot[j]) {
         out[f] = make_double2(0.0, 0.0);
@@ -214,62 +253,79 @@ __global__ void k_sb_gpost(int nreal, int logd, const double2 *__restrict__ buf,
 
 // ------------------------------------------------------------ launchers
 void launch_specbig_build(const Level &c, const Level &p, bool write_coeffs, int nq, double2 *buf, double2 *scratch,
-                          const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr) {
+                          const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr, const int *zp,
+                          int zq0) {
     const int logD = ilog2b(c.deg), D = 1 << logD;
     const long items = (long)nq * p.nreal;
     const double pts = (double)items * D;
+    FftSkip sk;
+    sk.zp = zp;
+    sk.q0 = zq0;
+    sk.span = p.deg;
+    sk.per_q = p.nreal;
     pr->begin("specbig_build", pts * 10.0, st);
     k_sb_build1<<<dim3(nb((long)p.nreal * (D / 2 + 1), 256), nq), 256, 0, st>>>(
-        c.spec2, c.spec2_q, c.nreal, p.nreal, logD, p.spec2, p.spec2_q, buf, tw, logTW);
+        c.spec2, c.spec2_q, c.nreal, p.nreal, logD, p.spec2, p.spec2_q, buf, tw, logTW, zp, zq0);
     pr->end(st);
-    fft_batched(buf, scratch, items, logD, +1, tw, logTW, st, launches, pr);
+    fft_batched(buf, scratch, items, logD, +1, tw, logTW, st, launches, pr, sk);
     pr->begin("specbig_build", pts * 4.0, st);
     k_sb_build2<<<dim3(nb((long)p.nreal * D, 256), nq), 256, 0, st>>>(
         c.ends, c.ends_q, c.nreal, p.nreal, logD, p.spec2 ? p.ends : nullptr, p.ends_q, write_coeffs ? p.P : nullptr,
-        p.P_q, p.pst, p.plen, buf, tw, logTW);
+        p.P_q, p.pst, p.plen, buf, tw, logTW, zp, zq0);
     pr->end(st);
     *launches += 2;
     if (!p.spec2) return;
-    fft_batched(buf, scratch, items, logD, -1, tw, logTW, st, launches, pr);
+    fft_batched(buf, scratch, items, logD, -1, tw, logTW, st, launches, pr, sk);
     pr->begin("specbig_build", pts * 8.0, st);
     k_sb_build3<<<dim3(nb((long)p.nreal * (D / 2), 256), nq), 256, 0, st>>>(p.nreal, logD, p.spec2, p.spec2_q, buf,
-                                                                          tw, logTW);
+                                                                          tw, logTW, zp, zq0);
     pr->end(st);
     *launches += 1;
 }
 
 void launch_specbig_prop(const double2 *Gp, size_t Gp_q, const Level &c, int nq, const uint8_t *hot_c, double2 *buf,
-                         double2 *scratch, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr) {
+                         double2 *scratch, const double2 *tw, int logTW, cudaStream_t st, long *launches, Prof *pr,
+                         const int *zp, int zq0) {
     const int logD = ilog2b(c.deg), D = 1 << logD, h = D / 2;
     const long items = (long)nq * c.nreal;
     const double pts = (double)items * h;
+    FftSkip sk;
+    sk.zp = zp;
+    sk.q0 = zq0;
+    sk.span = c.deg;
+    sk.per_q = c.nreal;
     pr->begin("specbig_prop", pts * 10.0, st);
-    k_sb_prop1<<<dim3(nb((long)c.nreal * ((h + 1) / 2), 256), nq), 256, 0, st>>>(Gp, Gp_q, c.spec2, c.spec2_q,
-                                                                                c.nreal, logD, buf, hot_c, tw, logTW);
+    k_sb_prop1<<<dim3(nb((long)c.nreal * ((h + 1) / 2), 256), nq), 256, 0, st>>>(
+        Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, logD, buf, hot_c, tw, logTW, zp, zq0);
     pr->end(st);
-    fft_batched(buf, scratch, items, logD - 1, +1, tw, logTW, st, launches, pr);
+    fft_batched(buf, scratch, items, logD - 1, +1, tw, logTW, st, launches, pr, sk);
     pr->begin("specbig_prop", pts * 4.0, st);
-    k_sb_prop2<<<dim3(nb((long)c.nreal * h, 256), nq), 256, 0, st>>>(c.nreal, logD, buf, tw, logTW);
+    k_sb_prop2<<<dim3(nb((long)c.nreal * h, 256), nq), 256, 0, st>>>(c.nreal, logD, buf, tw, logTW, zp, zq0);
     pr->end(st);
-    fft_batched(buf, scratch, items, logD - 1, -1, tw, logTW, st, launches, pr);
+    fft_batched(buf, scratch, items, logD - 1, -1, tw, logTW, st, launches, pr, sk);
     pr->begin("specbig_prop", pts * 14.0, st);
     k_sb_prop3<<<dim3(nb((long)c.nreal * (h / 2 + 1), 256), nq), 256, 0, st>>>(
-        Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, logD, buf, c.G, c.G_q, hot_c, tw, logTW);
+        Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, logD, buf, c.G, c.G_q, hot_c, tw, logTW, zp, zq0);
     pr->end(st);
     *launches += 3;
 }
 
 void launch_gspecbig_init(const double *g, size_t g_q, int gst, int glen, int nreal, int logd, double2 *G, size_t G_q,
                           int nq, const uint8_t *hot, double2 *buf, double2 *scratch, const double2 *tw, int logTW,
-                          cudaStream_t st, long *launches, Prof *pr) {
+                          cudaStream_t st, long *launches, Prof *pr, const int *zp, int zq0) {
     const int h = 1 << (logd - 1);
     const long items = (long)nq * nreal;
+    FftSkip sk;
+    sk.zp = zp;
+    sk.q0 = zq0;
+    sk.span = 1L << logd;
+    sk.per_q = nreal;
     pr->begin("gspec_init", 0.0, st);
-    k_sb_gpack<<<dim3(nb((long)nreal * h, 256), nq), 256, 0, st>>>(g, g_q, gst, glen, nreal, logd, buf);
+    k_sb_gpack<<<dim3(nb((long)nreal * h, 256), nq), 256, 0, st>>>(g, g_q, gst, glen, nreal, logd, buf, zp, zq0);
     pr->end(st);
-    fft_batched(buf, scratch, items, logd - 1, -1, tw, logTW, st, launches, pr);
+    fft_batched(buf, scratch, items, logd - 1, -1, tw, logTW, st, launches, pr, sk);
     pr->begin("gspec_init", (double)items * h * 20.0, st);
-    k_sb_gpost<<<dim3(nb((long)nreal * h, 256), nq), 256, 0, st>>>(nreal, logd, buf, G, G_q, hot, tw, logTW);
+    k_sb_gpost<<<dim3(nb((long)nreal * h, 256), nq), 256, 0, st>>>(nreal, logd, buf, G, G_q, hot, tw, logTW, zp, zq0);
     pr->end(st);
     *launches += 2;
 }

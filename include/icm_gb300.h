@@ -29,13 +29,17 @@ int icm_last_status(void);
  *   q_chunk           quadrature nodes processed per launch sequence
  *   coefficient_fft_only  1 = keep every FFT level on coefficients (no
  *                     spectral levels; for comparison and testing)
- *   max_device_bytes  cap on the plan's device memory                     */
+ *   max_device_bytes  cap on the plan's device memory
+ *   disable_zero_prefix  1 = compute tree nodes whose players all have a
+ *                     leaf factor of exactly 0 at a quadrature node (by
+ *                     default they are written as monomials or skipped)  */
 typedef struct {
     int block_size;
     int fft_min_degree;
     int q_chunk;
     int coefficient_fft_only;
     size_t max_device_bytes;
+    int disable_zero_prefix;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created

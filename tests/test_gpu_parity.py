@@ -201,3 +201,39 @@ def test_spectral_levels_match_coefficient_levels(gpu_icm, n, kfrac):
     assert max_rel(outs[False][0], outs[True][0]) < 1e-11
     assert max_rel(outs[False][1][T], outs[True][0][T]) < 1e-11
     assert np.count_nonzero(np.delete(outs[False][1], T)) == 0
+
+
+@pytest.mark.parametrize("wl", ["lognormal", "loguniform", "adv_1e9", "batched"])
+def test_zero_prefix_pruning_matches_full_tree(gpu_icm, oracle, wl):
+    """Tree nodes whose players all have a leaf factor of exactly 0 at a node
+    are written as monomials / skipped; equities equal the full tree's to
+    rounding, spectral and coefficient levels, single and batched."""
+    rng = np.random.default_rng(17)
+    if wl == "batched":
+        ts = W.batched(count=24)
+        outs = []
+        for zp in (True, False):
+            gpu_icm.configure(zero_prefix=zp)
+            outs.append(gpu_icm.equity_batched(ts))
+        for a, b in zip(*outs):
+            assert max_rel(a, b, floor=1e-300) < 1e-11
+        return
+    n = 30000
+    if wl == "lognormal":
+        S, P = W.gpu_scale(n=n, shape="linear")
+    elif wl == "loguniform":
+        S, P, _ = W.dropin(n=n)
+    else:
+        S = np.ones(n)
+        S[:50] = 1e9
+        P = (n - np.arange(n)).astype(float)
+    for coeff in (False, True):
+        res = []
+        for zp in (True, False):
+            gpu_icm.configure(zero_prefix=zp, coefficient_fft_only=coeff)
+            res.append(gpu_icm.equity(S, P))
+        assert max_rel(res[0], res[1], floor=1e-300) < 1e-11, coeff
+    if wl == "lognormal":   # k = n linear: closed form
+        idx = rng.choice(n, 32, replace=False)
+        ref = oracle.v1(S, idx=idx) * (P[0] / n)
+        assert max_rel(res[0][idx], ref) < 1e-9
