@@ -74,7 +74,8 @@ namespace {
 struct PhaseBuilder {
     std::vector<WStep> steps;
     template <class A>
-    void add(WOp op, int key, const char *name, const A &a, size_t smem, double fq, int one = 0) {
+    void add(WOp op, int key, const char *name, const A &a, size_t smem, double fq, int one = 0, int mem = -1,
+             long span = 0, int nreal = 0) {
         if (a.nbx <= 0) return;
         WStep *s = nullptr;
         for (auto &x : steps)
@@ -94,6 +95,10 @@ struct PhaseBuilder {
         ++s->nd;
         s->smem = std::max(s->smem, smem);
         s->fq += fq;
+        s->dmem.push_back(mem);
+        s->dspan.push_back(span);
+        s->dnreal.push_back(nreal);
+        s->dfq.push_back(fq);
     }
 };
 }  // namespace
@@ -129,7 +134,7 @@ static void build_steps(Forest *f) {
                 size_t sm = 0;
                 SpecInitArgs A = spec_init_args(p->lv[0], tw, logTW, &fq, &sm);
                 A.z.zp = zpre(p);
-                c.add(WOp::SpecInit, A.logd, "wl_spec_init", A, sm, fq);
+                c.add(WOp::SpecInit, A.logd, "wl_spec_init", A, sm, fq, 0, t, p->lv[0].deg, p->lv[0].nreal);
             }
         }
     }
@@ -145,22 +150,22 @@ static void build_steps(Forest *f) {
                 if (lv[l].kind == 2) {
                     SpecBuildArgs A = spec_build_args(lv[l - 1], lv[l], lv[l + 1].kind != 2, tw, logTW, &fq, &sm);
                     A.z.zp = zpre(p);
-                    b.add(WOp::SpecBuild, A.logD, "wl_spec_build", A, sm, fq);
+                    b.add(WOp::SpecBuild, A.logD, "wl_spec_build", A, sm, fq, 0, t, lv[l].deg, lv[l].nreal);
                 } else if (lv[l].fft) {
                     if (lv[l].npairs > 0) {
                         FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], false, tw, logTW, &fq, &sm);
                         A.z.zp = zpre(p);
-                        b.add(WOp::FusedBuild, A.logN, "wl_fused_build", A, sm, fq);
+                        b.add(WOp::FusedBuild, A.logN, "wl_fused_build", A, sm, fq, 0, t, lv[l].deg, lv[l].nreal);
                     }
                     if (lv[l - 1].nreal & 1) {
                         SchoolBuildArgs A = school_build_args(lv[l - 1], lv[l], lv[l].npairs, &fq);
                         A.z.zp = zpre(p);
-                        b.add(WOp::SchoolBuild, 0, "wl_school_build", A, 0, fq);
+                        b.add(WOp::SchoolBuild, 0, "wl_school_build", A, 0, fq, 0, t, lv[l].deg, lv[l].nreal);
                     }
                 } else {
                     SchoolBuildArgs A = school_build_args(lv[l - 1], lv[l], 0, &fq);
                     A.z.zp = zpre(p);
-                    b.add(WOp::SchoolBuild, 0, "wl_school_build", A, 0, fq);
+                    b.add(WOp::SchoolBuild, 0, "wl_school_build", A, 0, fq, 0, t, lv[l].deg, lv[l].nreal);
                 }
             } else if (l == p->L - 1 && lv[l].fft && lv[l].npairs > 0) {
                 // the root: child spectra for its propagate only
@@ -177,7 +182,7 @@ static void build_steps(Forest *f) {
                 size_t sm = 0;
                 SpecInitArgs A = spec_init_args(lv[l], tw, logTW, &fq, &sm);
                 A.z.zp = zpre(p);
-                c.add(WOp::SpecInit, A.logd, "wl_spec_init", A, sm, fq);
+                c.add(WOp::SpecInit, A.logd, "wl_spec_init", A, sm, fq, 0, t, lv[l].deg, lv[l].nreal);
             }
         }
     }
@@ -199,7 +204,7 @@ static void build_steps(Forest *f) {
                 GspecArgs A = gspec_args(lv[l].g, lv[l].g_q, lv[l].gst, lv[l].glen, lv[l].nreal, lv[l], lv[l].G,
                                          lv[l].G_q, nullptr, tw, logTW, &fq, &sm);
                 A.z.zp = zpre(p);
-                a.add(WOp::Gspec, A.logd, "wl_gspec_init", A, sm, fq);
+                a.add(WOp::Gspec, A.logd, "wl_gspec_init", A, sm, fq, 0, t, lv[l].deg, lv[l].nreal);
             }
         }
         PhaseBuilder &b = phase();
@@ -218,23 +223,23 @@ static void build_steps(Forest *f) {
                 SpecPropArgs A = spec_prop_args(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l],
                                                 l - 1 >= 1 && lv[l - 1].kind == 2, nullptr, tw, logTW, &fq, &sm);
                 A.z.zp = zpre(p);
-                b.add(WOp::SpecProp, A.logD, "wl_spec_prop", A, sm, fq);
+                b.add(WOp::SpecProp, A.logD, "wl_spec_prop", A, sm, fq, 0, t, root ? 0 : lv[l].deg, lv[l].nreal);
             } else if (lv[l].fft) {
                 if (lv[l].npairs > 0) {
                     FusedPropArgs A = fused_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nullptr, tw, logTW, &fq,
                                                       &sm);
                     A.z.zp = zpre(p);
-                    b.add(WOp::FusedProp, A.logN, "wl_fused_prop", A, sm, fq);
+                    b.add(WOp::FusedProp, A.logN, "wl_fused_prop", A, sm, fq, 0, t, root ? 0 : lv[l].deg, lv[l].nreal);
                 }
                 if (lv[l - 1].nreal & 1) {
                     SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], nullptr, 2 * lv[l].npairs, &fq);
                     A.z.zp = zpre(p);
-                    b.add(WOp::SchoolProp, 0, "wl_school_prop", A, 0, fq);
+                    b.add(WOp::SchoolProp, 0, "wl_school_prop", A, 0, fq, 0, t, lv[l - 1].deg, lv[l - 1].nreal);
                 }
             } else {
                 SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], nullptr, 0, &fq);
                 A.z.zp = zpre(p);
-                b.add(WOp::SchoolProp, 0, "wl_school_prop", A, 0, fq);
+                b.add(WOp::SchoolProp, 0, "wl_school_prop", A, 0, fq, 0, t, lv[l - 1].deg, lv[l - 1].nreal);
             }
         }
     }
@@ -249,7 +254,7 @@ static void build_steps(Forest *f) {
             double fq = 0;
             DivideArgs A = divide_args(p->B, p->n, p->k, p->nblocks, p->d_S, p->d_node, f->d_a + f->off[t], aq,
                                        p->d_blockP, g0, g0_q, gst0, nullptr, f->d_contrib + f->off[t], &fq);
-            b.add(WOp::Divide, 0, "wl_divide", A, 0, fq);
+            b.add(WOp::Divide, 0, "wl_divide", A, 0, fq, 0, t, 1, p->n);
         }
     }
     f->pre = std::move(pre[0].steps);
@@ -294,10 +299,30 @@ static int upload_steps(Forest *f, std::string &err) {
     return 0;
 }
 
+// flops of one launch over nq nodes, without the pruned (node, q) pairs
+static double step_flops(const Forest *f, const WStep &s, int nq, int q0) {
+    if (s.one) return s.fq;
+    double fl = 0.0;
+    for (int d = 0; d < s.nd; ++d) {
+        const int m = s.dmem[d];
+        const long span = s.dspan[d];
+        const int nr = s.dnreal[d];
+        if (m < 0 || span <= 0 || nr <= 0 || f->h_z.empty() || !f->tr[m]->zskip) {
+            fl += s.dfq[d] * nq;
+            continue;
+        }
+        const int *z = f->h_z.data() + (size_t)m * f->Q;
+        double hot = 0.0;
+        for (int q = 0; q < nq; ++q) hot += nr - std::min<long>(nr, z[q0 + q] / span);
+        fl += s.dfq[d] * hot / nr;
+    }
+    return fl;
+}
+
 static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
     const int nctas = (int)s.tab.size();
     const int qn = s.one ? 1 : nq;
-    f->prof.begin(s.name, s.fq * qn, f->stream);
+    if (f->prof.on) f->prof.begin(s.name, step_flops(f, s, qn, q0), f->stream);
     switch (s.op) {
         case WOp::Leaf:
         case WOp::Divide:
@@ -496,6 +521,7 @@ static int prepare_nodes(Forest *f, int Q, std::string &err) {
             z[q] = zero_prefix(p->S_sorted.data(), p->n, logv[q]);
         }
     });
+    f->h_z = hz;
     if (f->d_node) cudaFree(f->d_node);
     f->d_node = nullptr;
     const size_t nb = sizeof(double) * h.size();

@@ -22,6 +22,11 @@ struct WStep {
     std::vector<int2> tab;            // per CTA: (descriptor, block)
     size_t smem = 0;                  // dynamic shared memory of the launch
     double fq = 0.0;                  // algorithmic FP64 flops per node
+    // per descriptor, for the profiler: member, units the kernel prunes on
+    // (span players each, nreal of them; span 0 = no pruning), flops per node
+    std::vector<int> dmem, dnreal;
+    std::vector<long> dspan;
+    std::vector<double> dfq;
     const void *d_desc = nullptr;
     const int2 *d_tab = nullptr;
 };
@@ -53,6 +58,7 @@ struct Forest {
     cudaGraphExec_t graph = nullptr;
     long launches = 0, graph_launches = 0;
     std::vector<double> h_pay, h_out;
+    std::vector<int> h_z;             // [member][Q] zero prefixes (host copy)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_device_ms = 0.0;
     Prof prof;

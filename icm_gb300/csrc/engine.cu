@@ -125,7 +125,7 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     p->B = select_block_size(n, k);
     p->fft_min_deg = g_config.fft_min_degree > 0 ? g_config.fft_min_degree : 64;
     p->spectral = g_config.coefficient_fft_only != 1 && !p->coeff_only;
-    p->zskip = g_config.disable_zero_prefix != 1 && !p->coeff_only;
+    p->zskip = g_config.disable_zero_prefix != 1;
     const int B = p->B;
 
     // descending stacks, ties by original index (reference gpu_plan.cu:405-409)
@@ -395,6 +395,15 @@ int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &er
 }
 
 // one chunk of nq nodes starting at active-node index q0
+// share of a level's (tree node, chunk node) pairs outside the zero prefix:
+// the work the pruned kernels actually do, for the profiler's flop counts
+static double hot_frac(const Plan *p, int q0, int nq, long span, int nreal) {
+    if (!p->zskip || nreal <= 0 || span <= 0 || p->h_z.empty()) return 1.0;
+    double hot = 0.0;
+    for (int q = 0; q < nq; ++q) hot += nreal - std::min<long>(nreal, p->h_z[q0 + q] / span);
+    return hot / ((double)nq * nreal);
+}
+
 void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide) {
     cudaStream_t st = p->stream;
     const int L = p->L;
@@ -404,8 +413,14 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, lv[0].P, lv[0].pst,
                 lv[0].plen, st, pr);
     ++p->launches;
-    if (L >= 2 && lv[1].kind == 2) { launch_spec_init(lv[0], nq, tw, logTW, st, pr, zp, q0); ++p->launches; }
+    auto frac = [&](long span, int nreal) { pr->scale = zp ? hot_frac(p, q0, nq, span, nreal) : 1.0; };
+    if (L >= 2 && lv[1].kind == 2) {
+        frac(lv[0].deg, lv[0].nreal);
+        launch_spec_init(lv[0], nq, tw, logTW, st, pr, zp, q0);
+        ++p->launches;
+    }
     for (int l = 1; l <= L - 2; ++l) {
+        frac(lv[l].deg, lv[l].nreal);   // builds decide per parent
         if (lv[l].kind == 2) {
             if (lv[l - 1].deg > kSpecMaxD) {
                 launch_specbig_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, p->d_fa, p->d_fc, tw, logTW, st,
@@ -430,6 +445,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
             ++p->launches;
         }
     }
+    pr->scale = 1.0;
     if (L >= 2 && lv[L - 1].fft)
         launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches, pr);
     for (int l = L - 1; l >= 1; --l) {
@@ -439,6 +455,8 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
         const int gst_p = root ? 0 : lv[l].gst;
         const int gpl = root ? p->k : lv[l].glen;
         const uint8_t *hot_c = p->subset ? p->d_hot + p->hot_off[l - 1] : nullptr;
+        frac(lv[l].deg, lv[l].nreal);   // propagates decide per parent (multi-pass: per child, close)
+        if (root) pr->scale = 1.0;
         if (lv[l].kind == 2) {
             // the parent's g spectrum: the payout's at the root, converted from
             // coefficients below a coefficient level, else left by the level above
@@ -477,12 +495,19 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
             ++p->launches;
         }
     }
+    pr->scale = 1.0;
     if (!divide) return;
+    if (zp) {   // players with a leaf factor of 0 skip the division
+        double hot = 0.0;
+        for (int q = 0; q < nq; ++q) hot += p->n - p->h_z[q0 + q];
+        pr->scale = hot / ((double)nq * p->n);
+    }
     const double *g0 = (L == 1) ? p->d_payout : lv[0].g;
     const size_t g0_q = (L == 1) ? 0 : lv[0].g_q;
     const int gst0 = (L == 1) ? 0 : lv[0].gst;
     launch_divide(p->B, p->n, p->k, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, g0, g0_q, gst0,
                   p->subset ? p->d_active : nullptr, p->d_contrib, st, pr);
+    pr->scale = 1.0;
     launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, first ? 1 : 0, st, pr);
     p->launches += 2;
 }

@@ -635,6 +635,8 @@ void launch_fft_build(const Level &c, const Level &p, int nq, double2 *fa, doubl
     int logN = 0;
     while ((1 << logN) < N) ++logN;
     const double items = (double)nq * npairs;
+    const double sc = pr->scale;   // the multi-pass path computes every parent
+    pr->scale = 1.0;
     dim3 g1(nblk((long)npairs * N, 256), nq);
     pr->begin("fft_pack", 0.0, st);
     k_pack_pair<<<g1, 256, 0, st>>>(c.P, c.P_q, c.pst, c.plen, npairs, N, fa);
@@ -645,13 +647,14 @@ void launch_fft_build(const Level &c, const Level &p, int nq, double2 *fa, doubl
     k_build_mid<<<g2, 256, 0, st>>>(fa, npairs, N, p.spec, spectra_only ? nullptr : fb, tw, logTW, logN);
     pr->end(st);
     *launches += 2;
-    if (spectra_only) return;
+    if (spectra_only) { pr->scale = sc; return; }
     fft_batched(fb, fc, (long)nq * npairs, logN - 1, +1, tw, logTW, st, launches, pr);
     dim3 g3(nblk((long)npairs * p.pst, 256), nq);
     pr->begin("build_post", items * p.plen, st);
     k_build_post<<<g3, 256, 0, st>>>(fb, npairs, N, c.P, c.P_q, c.pst, c.plen, p.P, p.P_q, p.pst, p.plen);
     pr->end(st);
     *launches += 1;
+    pr->scale = sc;
 }
 
 void launch_fft_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p, int nq,
@@ -667,6 +670,8 @@ void launch_fft_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Le
     int logN = 0;
     while ((1 << logN) < N) ++logN;
     const double items = (double)nq * npairs;
+    const double sc = pr->scale;   // the multi-pass path computes every parent
+    pr->scale = 1.0;
     dim3 g1(nblk((long)npairs * (N / 2), 256), nq);
     pr->begin("prop_pack", 0.0, st);
     k_prop_pack<<<g1, 256, 0, st>>>(gp, gp_q, gst_p, gpl, npairs, N, hot_c, fb);
@@ -682,6 +687,7 @@ void launch_fft_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const Le
     k_prop_post<<<g3, 256, 0, st>>>(fa, npairs, N, c.g, c.g_q, c.gst, c.glen, hot_c);
     pr->end(st);
     *launches += 3;
+    pr->scale = sc;
 }
 
 }  // namespace icmg

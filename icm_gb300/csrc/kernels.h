@@ -23,6 +23,7 @@ struct Prof {
     std::vector<cudaEvent_t> pool;
     size_t used = 0;
     std::vector<ProfRec> recs;
+    double scale = 1.0;   // share of the launch's nominal work not pruned (set by the caller)
     cudaEvent_t get() {
         if (used == pool.size()) {
             cudaEvent_t e;
@@ -33,7 +34,7 @@ struct Prof {
     }
     void begin(const char *name, double flops, cudaStream_t st) {
         if (!on) return;
-        ProfRec r{name, get(), get(), flops};
+        ProfRec r{name, get(), get(), flops * scale};
         cudaEventRecord(r.a, st);
         recs.push_back(r);
     }

@@ -115,6 +115,14 @@ __global__ void k_adj_leaf_down(int n, int k, const double *__restrict__ S, cons
     const int b = i / B, start = b * B, bs = min(B, n - start), pk = min(bs, k);
     const int me = i - start;
     const double *arow = a + (size_t)q * n + start;
+    if (arow[me] == 0.0) {   // leaf factor 0 (S logv < -700): no share; g of its block may be pruned
+        contrib[(size_t)q * n + i] = 0.0;
+        if (partA) {
+            partA[(size_t)q * n + i] = 0.0;
+            partB[(size_t)q * n + i] = 0.0;
+        }
+        return;
+    }
     double P[B], H[B];
 #pragma unroll
     for (int m = 0; m < B; ++m) { P[m] = 0.0; H[m] = 0.0; }
@@ -167,14 +175,15 @@ __global__ void k_adj_leaf_down(int n, int k, const double *__restrict__ S, cons
 // child passes its gbar up unchanged (its g was the parent's).
 __global__ void k_adj_up_school(const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc, int nreal_c,
                                 const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen_c,
-                                double *__restrict__ gbp, size_t gbp_q, int gst_p, int gpl, int nreal_p, int j0) {
+                                double *__restrict__ gbp, size_t gbp_q, int gst_p, int gpl, int nreal_p, int j0,
+                                ZeroPrefix z) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int j = j0 + (int)(idx / gst_p);
     const int t = (int)(idx % gst_p);
     if (j >= nreal_p) return;
     double *out = gbp + q * gbp_q + (size_t)j * gst_p;
-    if (t >= gpl) { out[t] = 0.0; return; }
+    if (t >= gpl || zp_cold(z, q, j)) { out[t] = 0.0; return; }   // wholly-zero node: gbar = 0
     const double *gL = gbc + q * gbc_q + (size_t)(2 * j) * gst_c;
     if (2 * j + 1 >= nreal_c) { out[t] = (t < glen_c) ? gL[t] : 0.0; return; }
     const double *gR = gL + gst_c;
@@ -195,12 +204,12 @@ __global__ void k_adj_down_school(const double *__restrict__ gp, size_t gp_q, in
                                   const double *__restrict__ Pbp, size_t Pbp_q, int pst_p, int lp,
                                   const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc,
                                   const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen_c,
-                                  double *__restrict__ Pbc, int nreal_c, int c0) {
+                                  double *__restrict__ Pbc, int nreal_c, int c0, ZeroPrefix z) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int c = c0 + (int)(idx / pst_c);
     const int i = (int)(idx % pst_c);
-    if (c >= nreal_c) return;
+    if (c >= nreal_c || zp_cold(z, q, c)) return;   // wholly zero: its Pbar meets only zero factors
     double *out = Pbc + q * Pc_q + (size_t)c * pst_c;
     if (i >= lc) { out[i] = 0.0; return; }
     const int j = c >> 1, sib = c ^ 1;
@@ -230,13 +239,18 @@ __global__ void k_adj_down_school(const double *__restrict__ gp, size_t gp_q, in
 __global__ void __launch_bounds__(kVjpThreads)
 k_adj_up_fused(const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen_c, int npairs, int logN,
                const double2 *__restrict__ spec, double2 *__restrict__ gspec, double *__restrict__ gbp, size_t gbp_q,
-               int gst_p, int gpl, const double2 *__restrict__ tw, int logTW) {
+               int gst_p, int gpl, const double2 *__restrict__ tw, int logTW, ZeroPrefix z) {
     extern __shared__ double2 sm[];
     const int N = 1 << logN, h = N >> 1;
     const int cb = vjp_cb(N);
     const int q = blockIdx.y;
     const int j0 = blockIdx.x * cb;
     const int cnt = min(cb, npairs - j0);
+    if (zp_cold(z, q, j0 + cnt - 1)) {   // wholly-zero parents: gbar = 0
+        for (int e = threadIdx.x; e < cnt * gst_p; e += blockDim.x)
+            gbp[q * gbp_q + (size_t)(j0 + e / gst_p) * gst_p + e % gst_p] = 0.0;
+        return;
+    }
     double2 *Z = sm;
     double2 *U = sm + (size_t)cb * N;
     const double *base = gbc + q * gbc_q;
@@ -296,13 +310,14 @@ __global__ void __launch_bounds__(kVjpThreads)
 k_adj_down_fused(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl, const double *__restrict__ Pbp,
                  size_t Pbp_q, int pst_p, int lp, const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc,
                  int npairs, int logN, const double2 *__restrict__ spec, const double2 *__restrict__ gspec,
-                 double *__restrict__ Pbc, const double2 *__restrict__ tw, int logTW) {
+                 double *__restrict__ Pbc, const double2 *__restrict__ tw, int logTW, ZeroPrefix z) {
     extern __shared__ double2 sm[];
     const int N = 1 << logN, h = N >> 1;
     const int cb = vjp_cb(N);
     const int q = blockIdx.y;
     const int j0 = blockIdx.x * cb;
     const int cnt = min(cb, npairs - j0);
+    if (zp_cold(z, q, j0 + cnt - 1)) return;   // children of wholly-zero parents: not needed
     double2 *Z = sm;
     for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
         const int it = e >> logN, s = e & (N - 1);
@@ -498,6 +513,7 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
     const int L = p->L, B = p->B, n = p->n, k = p->k;
     Level *lv = p->lv;
     long &launches = p->launches;
+    const int *zp = p->zskip ? p->d_z : nullptr;   // zero-prefix pruning, as in the forward
     const dim3 gb0((unsigned)nblkv(p->nblocks, 128), nq);
     // gbar of the leaf blocks (for L = 1 the single block is the root)
     switch (B) {
@@ -515,13 +531,14 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         const size_t out_q = root ? (size_t)v->kst : pl.g_q;
         const int gst_p = root ? v->kst : pl.gst;
         const int gpl = root ? k : pl.glen;
+        const ZeroPrefix zpar{zp, q0, pl.deg};
         int j0 = 0;
         if (level_fused(pl)) {
             const int N = pl.fftn, logN = plan_ilog2(N);
             const int cb = vjp_cb_h(N);
             k_adj_up_fused<<<dim3((pl.npairs + cb - 1) / cb, nq), kVjpThreads, vjp_up_smem(N), st>>>(
                 v->gb[l - 1], c.g_q, c.gst, c.glen, pl.npairs, logN, pl.spec, v->gspec[l], out, out_q, gst_p, gpl, tw,
-                logTW);
+                logTW, zpar);
             ++launches;
             j0 = pl.npairs;
         }
@@ -529,7 +546,7 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         if (work > 0) {
             k_adj_up_school<<<dim3(nblkv(work, 256), nq), 256, 0, st>>>(c.P, c.P_q, c.pst, c.plen, c.nreal,
                                                                        v->gb[l - 1], c.g_q, c.gst, c.glen, out,
-                                                                       out_q, gst_p, gpl, pl.nreal, j0);
+                                                                       out_q, gst_p, gpl, pl.nreal, j0, zpar);
             ++launches;
         }
     }
@@ -542,13 +559,14 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         const int gst_p = root ? 0 : pl.gst;
         const int gpl = root ? k : pl.glen;
         const double *Pbp = root ? nullptr : v->Pb[l];
+        const ZeroPrefix zpar{zp, q0, pl.deg}, zch{zp, q0, c.deg};
         int c0 = 0;
         if (level_fused(pl)) {
             const int N = pl.fftn, logN = plan_ilog2(N);
             const int cb = vjp_cb_h(N);
             k_adj_down_fused<<<dim3((pl.npairs + cb - 1) / cb, nq), kVjpThreads, vjp_down_smem(N), st>>>(
                 gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen, pl.npairs, logN,
-                pl.spec, v->gspec[l], v->Pb[l - 1], tw, logTW);
+                pl.spec, v->gspec[l], v->Pb[l - 1], tw, logTW, zpar);
             ++launches;
             c0 = 2 * pl.npairs;
         }
@@ -556,7 +574,7 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         if (work > 0) {
             k_adj_down_school<<<dim3(nblkv(work, 256), nq), 256, 0, st>>>(
                 gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen, v->gb[l - 1], c.g_q,
-                c.gst, c.glen, v->Pb[l - 1], c.nreal, c0);
+                c.gst, c.glen, v->Pb[l - 1], c.nreal, c0, zch);
             ++launches;
         }
     }
@@ -620,13 +638,19 @@ int vjp_plan_run(VjpPlan *v, int Q, const double *payout, const double *cot, dou
     if (nact > p->qmax) {
         if (p->d_node) cudaFree(p->d_node);
         p->d_node = nullptr;
-        e = cudaMalloc(&p->d_node, sizeof(double) * 3 * (size_t)std::max(nact, 1));
+        p->d_z = nullptr;
+        const size_t nb = sizeof(double) * 3 * (size_t)std::max(nact, 1);
+        e = cudaMalloc(&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1));
         if (e != cudaSuccess) { err = std::string("node buffer: ") + cudaGetErrorString(e); return -1; }
+        p->d_z = (int *)((char *)p->d_node + nb);
         p->qmax = nact;
     }
+    p->h_z.resize(nact);
+    for (int j = 0; j < nact; ++j) p->h_z[j] = zero_prefix(p->S_sorted.data(), n, node[3 * j]);
+    if (nact) e = cudaMemcpyAsync(p->d_z, p->h_z.data(), sizeof(int) * nact, cudaMemcpyHostToDevice, p->stream);
     v->h_cot.resize(n);
     for (int i = 0; i < n; ++i) v->h_cot[i] = cot[p->perm[i]];   // sorted order
-    if (nact)
+    if (nact && e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_node, node.data(), sizeof(double) * node.size(), cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * k, cudaMemcpyHostToDevice, p->stream);

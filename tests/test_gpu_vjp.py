@@ -183,3 +183,21 @@ def test_autograd_function(gpu_icm):
     (equity(S2, P2) * cot).sum().backward()
     gS, gP = gpu_icm.equity_vjp(S2.detach().numpy(), P2.detach().numpy(), cot.numpy())
     assert np.array_equal(S2.grad.numpy(), gS) and np.array_equal(P2.grad.numpy(), gP)
+
+
+@pytest.mark.parametrize("wl", ["vjp", "lognormal_wide"])
+def test_vjp_zero_prefix_pruning(gpu_icm, wl):
+    """Pruning wholly-zero tree nodes leaves both gradients unchanged to rounding."""
+    if wl == "vjp":
+        S, P, cot = W.vjp(n=8192, k=900)
+    else:
+        rng = np.random.default_rng(4)
+        S = 1e4 * np.exp(1.5 * rng.standard_normal(20000))
+        P = np.linspace(1.0, 0.0, 20000, endpoint=False)
+        cot = rng.standard_normal(20000)
+    out = []
+    for zp in (True, False):
+        gpu_icm.configure(zero_prefix=zp)
+        out.append(gpu_icm.equity_vjp(S, P, cot, node_terms=True))
+    for a, b in zip(out[0], out[1]):
+        assert np.abs(a - b).max() <= 1e-11 * np.abs(b).max()
