@@ -27,7 +27,8 @@ from ._lib import (IcmGb300Config, IcmGpuOptions, IcmGpuPlanSummary, IcmGpuRunSt
                    library_path)
 
 __all__ = ["init", "equity", "equity_subset", "ICMError", "gpu_equity", "gpu_equity_subset", "GpuPlan",
-           "equity_batched", "GpuBatch", "equity_vjp", "equity_vjp_batched", "VjpPlan", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
+           "equity_batched", "GpuBatch", "equity_vjp", "equity_vjp_batched", "VjpPlan", "autotune", "tuner_load",
+           "tuner_save", "tuner_clear", "tuner_lookup", "equity_adaptive", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
            "last_launch_count"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -371,6 +372,64 @@ class VjpPlan:
             self.close()
         except Exception:
             pass
+
+
+def autotune(stacks, payouts, Q=256, runs=2):
+    """Time every (block size, FFT crossover) candidate on these stacks and
+    payouts, record the fastest in the tuner table for their size class and
+    return (block_size, fft_min_degree, best_ms)."""
+    S = _to_double_array(stacks, "stacks")
+    P = _to_double_array(payouts, "payouts")
+    _check(len(S), len(P), Q)
+    _auto_init()
+    b, f, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+    if lib().icm_gb300_autotune(len(S), _d(S), int(Q), _d(P), len(P), int(runs), ctypes.byref(b), ctypes.byref(f),
+                                ctypes.byref(ms)) != 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return b.value, f.value, ms.value
+
+
+def tuner_load(path):
+    """Load a tuner table file; returns the number of size-class entries read."""
+    r = lib().icm_gb300_tuner_load(os.fsencode(path))
+    if r < 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return r
+
+
+def tuner_save(path):
+    """Write the tuner table; returns the number of size-class entries."""
+    r = lib().icm_gb300_tuner_save(os.fsencode(path))
+    if r < 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return r
+
+
+def tuner_clear():
+    lib().icm_gb300_tuner_clear()
+
+
+def tuner_lookup(n, k):
+    """(block_size, fft_min_degree) the table holds for (n, k)'s class, or None."""
+    b, f = ctypes.c_int(), ctypes.c_int()
+    if lib().icm_gb300_tuner_lookup(int(n), int(k), ctypes.byref(b), ctypes.byref(f)) == 1:
+        return b.value, f.value
+    return None
+
+
+def equity_adaptive(stacks, payouts, tol=1e-9, Q0=256, Qmax=4096):
+    """Equities with Q doubled from Q0 until two successive node counts agree
+    to `tol` per player.  Returns (equity, Q_used, estimated_error)."""
+    S = _to_double_array(stacks, "stacks")
+    P = _to_double_array(payouts, "payouts")
+    _check(len(S), len(P), Q0)
+    _auto_init()
+    out = np.zeros(len(S))
+    qu, est = ctypes.c_int(), ctypes.c_double()
+    if lib().icm_gb300_equity_adaptive(len(S), _d(S), _d(P), len(P), int(Q0), float(tol), int(Qmax), _d(out),
+                                       ctypes.byref(qu), ctypes.byref(est)) != 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+    return out, qu.value, est.value
 
 
 def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False,

@@ -90,6 +90,14 @@ SIGNATURES = {
     "icm_gb300_vjp_device_ms": (ctypes.c_double, [_vp]),
     "icm_gb300_equity_vjp_batched": (ctypes.c_int, [ctypes.c_int, _ip, _ip, _dp, _dp, ctypes.c_int, _dp, _dp, _dp,
                                                     ctypes.c_int]),
+    "icm_gb300_tuner_load": (ctypes.c_int, [ctypes.c_char_p]),
+    "icm_gb300_tuner_save": (ctypes.c_int, [ctypes.c_char_p]),
+    "icm_gb300_tuner_clear": (None, []),
+    "icm_gb300_tuner_lookup": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _ip, _ip]),
+    "icm_gb300_autotune": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int, _ip, _ip,
+                                          _dp]),
+    "icm_gb300_equity_adaptive": (ctypes.c_int, [ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                 ctypes.c_int, _dp, _ip, _dp]),
     "icm_gb300_batch_create": (_vp, [ctypes.c_int, _ip, _ip, _dp]),
     "icm_gb300_batch_run": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gb300_batch_destroy": (None, [_vp]),

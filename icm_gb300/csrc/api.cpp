@@ -74,20 +74,12 @@ extern "C" {
 
 // ------------------------------------------------------------ icm.h
 void icm_init(const char *wisdom_path) {
-    // The tuner table (the analogue of the reference's FFTW wisdom) is a
-    // text file of "key value" lines: block_size, fft_min_degree, q_chunk.
+    // The tuner table (the analogue of the reference's FFTW wisdom, read from
+    // the given path; a missing file keeps the defaults, as the reference's
+    // missing wisdom file does)
     if (wisdom_path) {
-        FILE *f = fopen(wisdom_path, "r");
-        if (f) {
-            char key[64];
-            long val;
-            while (fscanf(f, "%63s %ld", key, &val) == 2) {
-                if (!strcmp(key, "block_size")) g_config.block_size = (int)val;
-                else if (!strcmp(key, "fft_min_degree")) g_config.fft_min_degree = (int)val;
-                else if (!strcmp(key, "q_chunk")) g_config.q_chunk = (int)val;
-            }
-            fclose(f);
-        }
+        std::string err;
+        tune_load(wisdom_path, err);
     }
     if (g_device < 0) icm_gpu_init(0);
 }
@@ -432,6 +424,86 @@ int icm_gb300_equity_vjp_batched(int T, const int *n, const int *k, const double
         po += k[t];
     }
     t_launches = launches;
+    return 0;
+}
+
+// ------------------------------------------------------------ tuner, Q ladder
+int icm_gb300_tuner_load(const char *path) {
+    if (!path) { set_error("icm_gb300_tuner_load: null path"); return -1; }
+    std::string err;
+    const int r = tune_load(path, err);
+    if (r < 0) set_error("icm_gb300_tuner_load: " + err);
+    return r;
+}
+
+int icm_gb300_tuner_save(const char *path) {
+    if (!path) { set_error("icm_gb300_tuner_save: null path"); return -1; }
+    std::string err;
+    const int r = tune_save(path, err);
+    if (r < 0) set_error("icm_gb300_tuner_save: " + err);
+    return r;
+}
+
+void icm_gb300_tuner_clear(void) { tune_clear(); }
+
+int icm_gb300_tuner_lookup(int n, int k, int *block_size, int *fft_min_degree) {
+    if (!block_size || !fft_min_degree || n < 1 || k < 1) return -1;
+    tune_lookup(n, k, block_size, fft_min_degree);
+    return (*block_size > 0) ? 1 : 0;
+}
+
+int icm_gb300_autotune(int n, const double *S, int Q, const double *payout, int k, int runs, int *block_size,
+                       int *fft_min_degree, double *best_ms) {
+    if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !block_size || !fft_min_degree || !best_ms) {
+        set_error("icm_gb300_autotune: invalid arguments");
+        return -1;
+    }
+    if (!ensure_device()) return -1;
+    std::string err;
+    if (tune_search(n, S, Q, payout, k, runs, block_size, fft_min_degree, best_ms, err) != 0) {
+        set_error("icm_gb300_autotune: " + err);
+        return -1;
+    }
+    return 0;
+}
+
+int icm_gb300_equity_adaptive(int n, const double *S, const double *payout, int k, int Q0, double tol, int Qmax,
+                              double *equity, int *Q_used, double *est_err) {
+    if (n < 1 || k < 1 || k > n || Q0 < 2 || Qmax < Q0 || !(tol > 0.0) || !S || !payout || !equity) {
+        set_error("icm_gb300_equity_adaptive: invalid arguments (need 1 <= k <= n, 2 <= Q0 <= Qmax, tol > 0)");
+        return -1;
+    }
+    if (!ensure_device()) return -1;
+    std::string err;
+    Plan *p = plan_create(n, S, k, nullptr, err);
+    if (!p) { set_error("icm_gb300_equity_adaptive: " + err); return -1; }
+    std::vector<double> prev(n), cur(n);
+    int Q = Q0;
+    double e = INFINITY;
+    int rc = plan_run(p, Q, payout, prev.data(), nullptr, err);
+    long launches = p->launches;
+    // double Q until two successive rules agree to tol (relative, per player,
+    // against a floor of 1e-12 of the largest equity)
+    while (rc == 0 && 2L * Q <= Qmax) {
+        rc = plan_run(p, 2 * Q, payout, cur.data(), nullptr, err);
+        launches += p->launches;
+        if (rc != 0) break;
+        Q *= 2;
+        double mx = 0.0;
+        for (int i = 0; i < n; ++i) mx = std::max(mx, std::fabs(cur[i]));
+        const double floor = 1e-12 * mx;
+        e = 0.0;
+        for (int i = 0; i < n; ++i)
+            e = std::max(e, std::fabs(cur[i] - prev[i]) / std::max(std::fabs(cur[i]), floor));
+        prev.swap(cur);
+        if (e <= tol) break;
+    }
+    plan_destroy(p);
+    t_launches = launches;
+    if (rc != 0) { set_error("icm_gb300_equity_adaptive: " + err); return -1; }
+    memcpy(equity, prev.data(), sizeof(double) * n);
+    if (Q_used) *Q_used = Q;
+    if (est_err) *est_err = e;
     return 0;
 }
 

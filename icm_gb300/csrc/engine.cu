@@ -98,14 +98,24 @@ static int ilog2(long v) {
 static int round2(int v) { return (v + 1) & ~1; }
 
 int select_block_size(int n, int k) {
-    (void)k;
-    int B = g_config.block_size > 0 ? g_config.block_size : 8;
+    int B = g_config.block_size;
+    if (B <= 0) {   // the tuner table's choice for this size class, else 8
+        int tF = 0;
+        tune_lookup(n, k, &B, &tF);
+        if (B <= 0) B = 8;
+    }
     if (B <= 4) B = 4;
     else if (B <= 8) B = 8;
     else if (B <= 16) B = 16;
     else B = 32;
-    (void)n;
     return B;
+}
+
+static int select_fft_min(int n, int k) {
+    if (g_config.fft_min_degree > 0) return g_config.fft_min_degree;
+    int tB = 0, tF = 0;
+    tune_lookup(n, k, &tB, &tF);
+    return tF > 0 ? tF : 64;
 }
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -123,7 +133,7 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     p->n = n;
     p->k = k;
     p->B = select_block_size(n, k);
-    p->fft_min_deg = g_config.fft_min_degree > 0 ? g_config.fft_min_degree : 64;
+    p->fft_min_deg = select_fft_min(n, k);
     p->spectral = g_config.coefficient_fft_only != 1 && !p->coeff_only;
     p->zskip = g_config.disable_zero_prefix != 1;
     const int B = p->B;

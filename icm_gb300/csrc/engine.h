@@ -150,6 +150,15 @@ void fill_twiddles(int logTW, std::vector<unsigned char> &out);
 int measure_fp64_gflops(double *out, std::string &err);
 int measure_hbm_gbps(double *out, std::string &err);
 
+// tuner table (tune.cpp)
+void tune_lookup(int n, int k, int *B, int *fft_min);
+void tune_record(int n, int k, int B, int fft_min, double ms);
+int tune_load(const char *path, std::string &err);
+int tune_save(const char *path, std::string &err);
+void tune_clear();
+int tune_search(int n, const double *S, int Q, const double *payout, int k, int runs, int *bestB, int *best_fft,
+                double *best_ms, std::string &err);
+
 // process-wide configuration
 extern IcmGb300Config g_config;
 extern int g_device;

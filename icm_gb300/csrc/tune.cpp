@@ -1,0 +1,161 @@
+// tune.cpp -- the tuner table (the analogue of the reference's FFTW wisdom,
+// src/cpu/icm.c:184-192) and the search that fills it.
+//
+// The table maps a size class of tournaments to the two choices that shape
+// the tree: the leaf block size B and the child degree at which tree levels
+// switch from schoolbook to FFT products (fft_min_degree).  A size class is
+// (ceil(log2 n), k/n bucket) with buckets k/n <= 1/64, <= 1/8, <= 1/2, > 1/2.
+// The search times every candidate pair on the caller's stacks and payouts
+// (CUDA events around the kernel sequence, best of several runs) and keeps
+// the fastest; results are bitwise different between candidates but all
+// within the engine's accuracy, so the choice is a pure speed decision.
+//
+// File format (text, one entry per line; '#' starts a comment):
+//   block_size <B>            global defaults (also set by icm_gb300_set_config)
+//   fft_min_degree <d>
+//   q_chunk <q>
+//   tune <log2n> <kbucket> <B> <fft_min_degree> <ms>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+namespace icmg {
+
+namespace {
+struct TuneEntry {
+    int log2n, kbucket, B, fft_min;
+    double ms;
+};
+std::mutex g_tune_mu;
+std::vector<TuneEntry> g_tune;
+
+int log2ceil(long v) {
+    int l = 0;
+    while ((1L << l) < v) ++l;
+    return l;
+}
+}  // namespace
+
+int tune_kbucket(int n, int k) {
+    const double r = (double)k / (double)n;
+    return r <= 1.0 / 64 ? 0 : r <= 1.0 / 8 ? 1 : r <= 0.5 ? 2 : 3;
+}
+
+// the table's choice for (n, k); 0 where the table has no entry
+void tune_lookup(int n, int k, int *B, int *fft_min) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    *B = 0;
+    *fft_min = 0;
+    const int ln = log2ceil(n), kb = tune_kbucket(n, k);
+    for (const TuneEntry &e : g_tune)
+        if (e.log2n == ln && e.kbucket == kb) {
+            *B = e.B;
+            *fft_min = e.fft_min;
+        }
+}
+
+void tune_record(int n, int k, int B, int fft_min, double ms) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    const int ln = log2ceil(n), kb = tune_kbucket(n, k);
+    for (TuneEntry &e : g_tune)
+        if (e.log2n == ln && e.kbucket == kb) {
+            e = {ln, kb, B, fft_min, ms};
+            return;
+        }
+    g_tune.push_back({ln, kb, B, fft_min, ms});
+}
+
+int tune_load(const char *path, std::string &err) {
+    FILE *f = fopen(path, "r");
+    if (!f) { err = std::string("cannot open ") + path; return -1; }
+    char line[512];
+    int nent = 0;
+    while (fgets(line, sizeof line, f)) {
+        char *hash = strchr(line, '#');
+        if (hash) *hash = 0;
+        char key[64];
+        if (sscanf(line, "%63s", key) != 1) continue;
+        long v = 0;
+        if (!strcmp(key, "tune")) {
+            int ln, kb, B, fm;
+            double ms = 0.0;
+            if (sscanf(line, "%*s %d %d %d %d %lf", &ln, &kb, &B, &fm, &ms) >= 4 && ln >= 0 && ln < 40 && kb >= 0 &&
+                kb <= 3 && (B == 4 || B == 8 || B == 16 || B == 32) && fm >= 1) {
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                bool found = false;
+                for (TuneEntry &e : g_tune)
+                    if (e.log2n == ln && e.kbucket == kb) { e = {ln, kb, B, fm, ms}; found = true; }
+                if (!found) g_tune.push_back({ln, kb, B, fm, ms});
+                ++nent;
+            }
+        } else if (sscanf(line, "%*s %ld", &v) == 1) {
+            if (!strcmp(key, "block_size")) g_config.block_size = (int)v;
+            else if (!strcmp(key, "fft_min_degree")) g_config.fft_min_degree = (int)v;
+            else if (!strcmp(key, "q_chunk")) g_config.q_chunk = (int)v;
+        }
+    }
+    fclose(f);
+    return nent;
+}
+
+int tune_save(const char *path, std::string &err) {
+    FILE *f = fopen(path, "w");
+    if (!f) { err = std::string("cannot write ") + path; return -1; }
+    fprintf(f, "# icm_gb300 tuner table: tune <ceil log2 n> <k/n bucket 0..3> <block size> <fft_min_degree> <ms>\n");
+    if (g_config.block_size > 0) fprintf(f, "block_size %d\n", g_config.block_size);
+    if (g_config.fft_min_degree > 0) fprintf(f, "fft_min_degree %d\n", g_config.fft_min_degree);
+    if (g_config.q_chunk > 0) fprintf(f, "q_chunk %d\n", g_config.q_chunk);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const TuneEntry &e : g_tune) fprintf(f, "tune %d %d %d %d %.6f\n", e.log2n, e.kbucket, e.B, e.fft_min, e.ms);
+    fclose(f);
+    return (int)g_tune.size();
+}
+
+void tune_clear() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+}
+
+// Time every (B, fft_min_degree) candidate on (S, payout); record the best.
+int tune_search(int n, const double *S, int Q, const double *payout, int k, int runs, int *bestB, int *best_fft,
+                double *best_ms, std::string &err) {
+    static const int kB[] = {4, 8, 16};
+    static const int kF[] = {16, 32, 64, 128};
+    const IcmGb300Config saved = g_config;
+    std::vector<double> out(n);
+    double best = 1e300;
+    int bB = 0, bF = 0;
+    for (int B : kB) {
+        for (int F : kF) {
+            g_config.block_size = B;
+            g_config.fft_min_degree = F;
+            Plan *p = plan_create(n, S, k, nullptr, err);
+            if (!p) { g_config = saved; return -1; }
+            double t = 1e300;
+            for (int r = 0; r <= std::max(1, runs); ++r) {   // first run warms caches and pools
+                if (plan_run(p, Q, payout, out.data(), nullptr, err) != 0) {
+                    plan_destroy(p);
+                    g_config = saved;
+                    return -1;
+                }
+                if (r) t = std::min(t, p->last_device_ms);
+            }
+            plan_destroy(p);
+            if (t < best) { best = t; bB = B; bF = F; }
+        }
+    }
+    g_config = saved;
+    tune_record(n, k, bB, bF, best);
+    *bestB = bB;
+    *best_fft = bF;
+    *best_ms = best;
+    return 0;
+}
+
+}  // namespace icmg

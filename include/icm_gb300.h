@@ -117,6 +117,36 @@ int icm_gb300_equity_vjp_batched(int T, const int *n, const int *k, const double
                                  const double *payout, int Q, const double *cot,
                                  double *grad_S, double *grad_payout, int flags);
 
+/* Tuner table (the analogue of the reference's FFTW wisdom; icm_init(path)
+ * loads it too).  Entries map a size class -- ceil(log2 n) and a k/n bucket
+ * (<= 1/64, <= 1/8, <= 1/2, > 1/2) -- to a leaf block size and the child
+ * degree where tree levels switch from schoolbook to FFT products; plans of
+ * that class use them unless icm_gb300_set_config fixes the values.
+ *   tuner_load/save   text file; return the number of entries or -1
+ *   tuner_lookup      1 and the class's entry, 0 when the class has none
+ *   autotune          times every candidate (block sizes 4, 8, 16; FFT
+ *                     crossover 16, 32, 64, 128) on the given stacks and
+ *                     payouts (best device time of `runs` solves after one
+ *                     warm-up each), records the fastest in the table and
+ *                     returns it; 0 / -1                                    */
+int icm_gb300_tuner_load(const char *path);
+int icm_gb300_tuner_save(const char *path);
+void icm_gb300_tuner_clear(void);
+int icm_gb300_tuner_lookup(int n, int k, int *block_size, int *fft_min_degree);
+int icm_gb300_autotune(int n, const double *S, int Q, const double *payout, int k, int runs,
+                       int *block_size, int *fft_min_degree, double *best_ms);
+
+/* Quadrature ladder: solves with Q0, 2 Q0, 4 Q0, ... nodes of the
+ * reference's rule (never more than Qmax) until two successive results
+ * agree per player to tol (relative, against a floor of 1e-12 of the
+ * largest equity).  equity receives the finest result, *Q_used its node
+ * count, *est_err the last difference (INFINITY if only Q0 ran).  The
+ * default entry points keep the caller's Q; this is for callers that want
+ * a stated accuracy where Q = 256 does not resolve the integrand.
+ * Returns 0 / -1. */
+int icm_gb300_equity_adaptive(int n, const double *S, const double *payout, int k, int Q0,
+                              double tol, int Qmax, double *equity, int *Q_used, double *est_err);
+
 /* Measured peak of this GPU's FP64 pipe: a register-resident DFMA loop over
  * all SMs, in GFLOP/s (2 flops per DFMA).  Returns 1 / 0. */
 int icm_gpu_measure_fp64_gflops(double *gflops_out);

@@ -237,3 +237,33 @@ def test_zero_prefix_pruning_matches_full_tree(gpu_icm, oracle, wl):
         idx = rng.choice(n, 32, replace=False)
         ref = oracle.v1(S, idx=idx) * (P[0] / n)
         assert max_rel(res[0][idx], ref) < 1e-9
+
+
+def test_autotune_and_table(gpu_icm, oracle, tmp_path):
+    """The search returns a candidate, records it for the size class, plans
+    of that class use it, and results stay on the oracle."""
+    gpu_icm.tuner_clear()
+    S, P = W.batched(count=1, n_lo=3000, n_hi=3000)[0]
+    b, f, ms = gpu_icm.autotune(S, P, Q=64, runs=1)
+    assert b in (4, 8, 16) and f in (16, 32, 64, 128) and ms > 0
+    assert gpu_icm.tuner_lookup(len(S), len(P)) == (b, f)
+    path = tmp_path / "tuner.txt"
+    assert gpu_icm.tuner_save(path) == 1
+    gpu_icm.tuner_clear()
+    assert gpu_icm.tuner_load(path) == 1
+    plan = gpu_icm.GpuPlan(S, len(P))
+    assert plan.summary()["B"] == b
+    E = plan.equity(P, Q=64)
+    plan.close()
+    assert max_rel(E, oracle.equity(S, P, Q=64, B=8, fft_min_deg=64), floor=1e-300) < 1e-9
+    gpu_icm.tuner_clear()
+
+
+def test_quadrature_ladder(gpu_icm, oracle):
+    """Q doubles until successive rules agree; the result is the oracle's at that Q."""
+    S, P, _ = W.vjp(n=4096, k=600)
+    E, Q, err = gpu_icm.equity_adaptive(S, P, tol=1e-9, Q0=128, Qmax=8192)
+    assert Q > 128 and err <= 1e-9
+    assert max_rel(E, oracle.equity(S, P, Q=Q), floor=1e-12 * np.abs(E).max()) < 1e-9
+    E2, Q2, err2 = gpu_icm.equity_adaptive(S, P, tol=1e-30, Q0=128, Qmax=512)   # capped
+    assert Q2 == 512 and err2 > 0
