@@ -410,18 +410,46 @@ int icm_gb300_equity_vjp_batched(int T, const int *n, const int *k, const double
         set_error("icm_gb300_equity_vjp_batched: invalid arguments");
         return -1;
     }
-    long so = 0, po = 0, launches = 0;
+    std::vector<long> so(T + 1, 0), po(T + 1, 0);
     for (int t = 0; t < T; ++t) {
         if (n[t] < 1 || k[t] < 1 || k[t] > n[t]) {
             set_error("icm_gb300_equity_vjp_batched: tournament " + std::to_string(t) + " needs 1 <= k <= n");
             return -1;
         }
-        if (icm_gb300_equity_vjp(n[t], S + so, Q, payout + po, k[t], cot + so, grad_S + so, grad_payout + po,
-                                 flags) != 0)
-            return -1;
-        launches += t_launches;
-        so += n[t];
-        po += k[t];
+        so[t + 1] = so[t] + n[t];
+        po[t + 1] = po[t] + k[t];
+    }
+    if (!ensure_device()) return -1;
+    // waves of members, each on its own plan and stream: every member of a
+    // wave is enqueued before any is awaited, so small members overlap
+    const int W = 64;
+    long launches = 0;
+    std::string err;
+    for (int w0 = 0; w0 < T; w0 += W) {
+        const int w1 = std::min(T, w0 + W);
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        const size_t budget = std::max<size_t>((size_t)64 << 20, (size_t)(free_b * 0.5) / (size_t)(w1 - w0));
+        std::vector<VjpPlan *> plans;
+        int rc = 0;
+        for (int t = w0; t < w1 && rc == 0; ++t) {
+            VjpPlan *v = vjp_plan_create(n[t], S + so[t], k[t], err, budget);
+            if (!v) { rc = -1; break; }
+            plans.push_back(v);
+            rc = vjp_plan_enqueue(v, Q, payout + po[t], cot + so[t], flags, err);
+        }
+        for (size_t i = 0; i < plans.size(); ++i) {
+            const int t = w0 + (int)i;
+            if (rc == 0 && plans[i]->pending) {
+                rc = vjp_plan_finish(plans[i], grad_S + so[t], grad_payout + po[t], nullptr, err);
+                launches += plans[i]->p->launches;
+            }
+        }
+        for (VjpPlan *v : plans) {
+            if (v->pending) cudaStreamSynchronize(v->p->stream);
+            vjp_plan_destroy(v);
+        }
+        if (rc != 0) { set_error("icm_gb300_equity_vjp_batched: " + err); return -1; }
     }
     t_launches = launches;
     return 0;

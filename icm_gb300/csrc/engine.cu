@@ -269,7 +269,7 @@ size_t plan_tree_layout(Plan *p, int qc, char *base) {
 }
 
 Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err, bool coeff_only,
-                  double q_bytes_scale) {
+                  double q_bytes_scale, size_t budget_bytes) {
     Plan *p = new Plan();
     if (opts) p->opts = *opts;
     p->opts.device_id = g_device;
@@ -281,8 +281,9 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
 
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    size_t budget = g_config.max_device_bytes ? g_config.max_device_bytes
-                                              : std::min<size_t>((size_t)(free_b * 0.6), (size_t)48 << 30);
+    size_t budget = budget_bytes           ? budget_bytes
+                    : g_config.max_device_bytes ? g_config.max_device_bytes
+                                                : std::min<size_t>((size_t)(free_b * 0.6), (size_t)48 << 30);
     int qc = (int)std::min<size_t>(256, std::max<size_t>(1, budget / std::max<size_t>(per_q, 1)));
     if (g_config.q_chunk > 0) qc = std::min(qc, g_config.q_chunk);
     p->qc = qc;

@@ -119,7 +119,7 @@ size_t plan_tree_layout(Plan *p, int qc, char *base);
 // coefficients of every level); q_bytes_scale sizes the node chunk for
 // callers that add per-node buffers of their own
 Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err,
-                  bool coeff_only = false, double q_bytes_scale = 1.0);
+                  bool coeff_only = false, double q_bytes_scale = 1.0, size_t budget = 0);
 // launch sequence of one chunk of nq nodes (engine.cu); divide = false stops
 // after the propagate pass (the tree of the chunk stays in the plan's buffers)
 void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide);

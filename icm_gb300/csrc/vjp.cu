@@ -454,9 +454,9 @@ void vjp_set_smem_limits() {
 // ------------------------------------------------------------ plans
 static bool level_fused(const Level &v) { return v.fft && v.npairs > 0 && v.fftn <= kVjpMaxN && fused_ok(v.fftn); }
 
-VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err) {
+VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t budget) {
     // the adjoint buffers roughly double the tree's per-node memory
-    Plan *p = plan_create(n, S, k, nullptr, err, /*coeff_only=*/true, /*q_bytes_scale=*/2.2);
+    Plan *p = plan_create(n, S, k, nullptr, err, /*coeff_only=*/true, /*q_bytes_scale=*/2.2, budget);
     if (!p) return nullptr;
     VjpPlan *v = new VjpPlan();
     v->p = p;
@@ -602,9 +602,8 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
     }
 }
 
-int vjp_plan_run(VjpPlan *v, int Q, const double *payout, const double *cot, double *grad_S, double *grad_payout,
-                 int flags, IcmGpuRunStats *stats, std::string &err) {
-    if (!v || Q < 1 || !payout || !cot || !grad_S || !grad_payout) { err = "invalid arguments"; return -1; }
+int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot, int flags, std::string &err) {
+    if (!v || Q < 1 || !payout || !cot) { err = "invalid arguments"; return -1; }
     Plan *p = v->p;
     const double t0 = now_ns();
     p->launches = 0;
@@ -677,6 +676,24 @@ int vjp_plan_run(VjpPlan *v, int Q, const double *payout, const double *cot, dou
     ++p->launches;
     cudaEventRecord(p->ev1, p->stream);
     e = cudaGetLastError();
+    if (e != cudaSuccess) { err = std::string("launch: ") + cudaGetErrorString(e); return -1; }
+    v->pending = true;
+    v->pQ = Q;
+    v->pnode = node_terms;
+    v->pqidx = std::move(qidx);
+    v->pw = std::move(w);
+    v->pnact = nact;
+    v->pt0 = t0;
+    return 0;
+}
+
+int vjp_plan_finish(VjpPlan *v, double *grad_S, double *grad_payout, IcmGpuRunStats *stats, std::string &err) {
+    if (!v || !v->pending || !grad_S || !grad_payout) { err = "invalid arguments (no VJP enqueued)"; return -1; }
+    v->pending = false;
+    Plan *p = v->p;
+    const int n = p->n, k = p->k, nact = v->pnact, Q = v->pQ;
+    const bool node_terms = v->pnode;
+    cudaError_t e = cudaSuccess;
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(grad_S, p->d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, p->stream);
     if (e == cudaSuccess)
@@ -688,18 +705,25 @@ int vjp_plan_run(VjpPlan *v, int Q, const double *payout, const double *cot, dou
         e = cudaMemcpyAsync(hB.data(), v->d_nodeB, sizeof(double) * nact, cudaMemcpyDeviceToHost, p->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) { err = std::string("execution: ") + cudaGetErrorString(e); return -1; }
-    if (node_terms && nact) grad_S[p->perm[0]] += node_shift_term(Q, p->Smax, qidx, w, hA, hB);
+    if (node_terms && nact) grad_S[p->perm[0]] += node_shift_term(Q, p->Smax, v->pqidx, v->pw, hA, hB);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, p->ev0, p->ev1);
     p->last_device_ms = ms;
     if (stats) {
         memset(stats, 0, sizeof(*stats));
-        stats->total_ns = now_ns() - t0;
+        stats->total_ns = now_ns() - v->pt0;
         stats->peak_vram_bytes = p->arena_bytes + v->arena_bytes;
         stats->engine = 1;
         stats->B = p->B;
     }
     return 0;
+}
+
+int vjp_plan_run(VjpPlan *v, int Q, const double *payout, const double *cot, double *grad_S, double *grad_payout,
+                 int flags, IcmGpuRunStats *stats, std::string &err) {
+    if (!grad_S || !grad_payout) { err = "invalid arguments"; return -1; }
+    if (vjp_plan_enqueue(v, Q, payout, cot, flags, err) != 0) return -1;
+    return vjp_plan_finish(v, grad_S, grad_payout, stats, err);
 }
 
 }  // namespace icmg
