@@ -433,15 +433,17 @@ def equity_adaptive(stacks, payouts, tol=1e-9, Q0=256, Qmax=4096):
 
 
 def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False,
-              zero_prefix=True):
+              zero_prefix=True, subtree=False):
     """Process-wide engine settings for plans created afterwards (0 = default).
 
     coefficient_fft_only=True keeps every FFT tree level on coefficients
     (no spectral levels), for comparison and testing; zero_prefix=False
     computes tree nodes whose players all have a leaf factor of exactly 0 at
-    a quadrature node instead of writing them as monomials / skipping them."""
+    a quadrature node instead of writing them as monomials / skipping them;
+    subtree=True runs the leaf blocks and bottom schoolbook levels in one
+    kernel per direction (same results; measured slightly slower)."""
     cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes,
-                         0 if zero_prefix else 1)
+                         0 if zero_prefix else 1, 1 if subtree else 0)
     lib().icm_gb300_set_config(ctypes.byref(cfg))
 
 

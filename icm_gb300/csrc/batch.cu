@@ -75,7 +75,7 @@ struct PhaseBuilder {
     std::vector<WStep> steps;
     template <class A>
     void add(WOp op, int key, const char *name, const A &a, size_t smem, double fq, int one = 0, int mem = -1,
-             long span = 0, int nreal = 0) {
+             long span = 0, int nreal = 0, double fq0 = 0.0) {
         if (a.nbx <= 0) return;
         WStep *s = nullptr;
         for (auto &x : steps)
@@ -99,6 +99,7 @@ struct PhaseBuilder {
         s->dspan.push_back(span);
         s->dnreal.push_back(nreal);
         s->dfq.push_back(fq);
+        s->dfq0.push_back(fq0);
     }
 };
 }  // namespace
@@ -117,14 +118,26 @@ static void build_steps(Forest *f) {
     std::deque<PhaseBuilder> ph;   // stable references while phases are added
     auto phase = [&]() -> PhaseBuilder & { ph.emplace_back(); return ph.back(); };
 
-    {   // leaf blocks
+    std::vector<SubArgs> subs(T);
+    std::vector<SubFlops> subfl(T);
+    {   // leaf blocks (with the bottom schoolbook levels where they are fused)
         PhaseBuilder &b = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
             double fq = 0;
+            if (p->Lf >= 1) {
+                subs[t] = sub_args(p, p->Lf, p->d_S, p->d_node, f->d_a + f->off[t], aq, nullptr,
+                                   f->d_contrib + f->off[t], false, true, &subfl[t]);
+                // the levels' share is pruned like level Lf (profiler only)
+                double lvl = 0.0;
+                for (int l = 1; l <= p->Lf; ++l) lvl += subfl[t].build[l];
+                b.add(WOp::SubBuild, p->B, "wl_sub_build", subs[t], sub_build_smem(p->B), lvl, 0, t, p->lv[p->Lf].deg,
+                      p->lv[p->Lf].nreal, subfl[t].leaf);
+                continue;
+            }
             LeafArgs A = leaf_args(p->B, p->n, p->nblocks, p->d_S, p->d_node, f->d_a + f->off[t], aq, p->d_blockP,
                                    p->lv[0].P, p->lv[0].pst, p->lv[0].plen, &fq);
-            b.add(WOp::Leaf, 0, "wl_leaf", A, 0, fq);
+            b.add(WOp::Leaf, p->B, "wl_leaf", A, 0, fq);
         }
         PhaseBuilder &c = phase();
         for (int t = 0; t < T; ++t) {
@@ -146,6 +159,7 @@ static void build_steps(Forest *f) {
             Level *lv = p->lv;
             double fq = 0;
             size_t sm = 0;
+            if (l <= p->Lf) continue;   // in the subtree kernel
             if (l <= p->L - 2) {
                 if (lv[l].kind == 2) {
                     SpecBuildArgs A = spec_build_args(lv[l - 1], lv[l], lv[l + 1].kind != 2, tw, logTW, &fq, &sm);
@@ -211,7 +225,7 @@ static void build_steps(Forest *f) {
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
             Level *lv = p->lv;
-            if (l > p->L - 1) continue;
+            if (l > p->L - 1 || l <= p->Lf) continue;
             const bool root = (l == p->L - 1);
             const double *gp = root ? p->d_payout : lv[l].g;
             const size_t gp_q = root ? 0 : lv[l].g_q;
@@ -248,13 +262,20 @@ static void build_steps(Forest *f) {
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
             const int L = p->L;
+            if (p->Lf >= 1) {   // the bottom levels' propagate and the division
+                double lvl = 0.0;
+                for (int l = 1; l <= p->Lf; ++l) lvl += subfl[t].prop[l];
+                b.add(WOp::SubProp, p->B, "wl_sub_prop", subs[t], sub_prop_smem(p->B), lvl, 0, t, p->lv[0].deg,
+                      p->lv[0].nreal, subfl[t].divide);
+                continue;
+            }
             const double *g0 = (L == 1) ? p->d_payout : p->lv[0].g;
             const size_t g0_q = (L == 1) ? 0 : p->lv[0].g_q;
             const int gst0 = (L == 1) ? 0 : p->lv[0].gst;
             double fq = 0;
             DivideArgs A = divide_args(p->B, p->n, p->k, p->nblocks, p->d_S, p->d_node, f->d_a + f->off[t], aq,
                                        p->d_blockP, g0, g0_q, gst0, nullptr, f->d_contrib + f->off[t], &fq);
-            b.add(WOp::Divide, 0, "wl_divide", A, 0, fq, 0, t, 1, p->n);
+            b.add(WOp::Divide, p->B, "wl_divide", A, 0, fq, 0, t, 1, p->n);
         }
     }
     f->pre = std::move(pre[0].steps);
@@ -308,13 +329,13 @@ static double step_flops(const Forest *f, const WStep &s, int nq, int q0) {
         const long span = s.dspan[d];
         const int nr = s.dnreal[d];
         if (m < 0 || span <= 0 || nr <= 0 || f->h_z.empty() || !f->tr[m]->zskip) {
-            fl += s.dfq[d] * nq;
+            fl += (s.dfq[d] + s.dfq0[d]) * nq;
             continue;
         }
         const int *z = f->h_z.data() + (size_t)m * f->Q;
         double hot = 0.0;
         for (int q = 0; q < nq; ++q) hot += nr - std::min<long>(nr, z[q0 + q] / span);
-        fl += s.dfq[d] * hot / nr;
+        fl += s.dfq[d] * hot / nr + s.dfq0[d] * nq;
     }
     return fl;
 }
@@ -327,9 +348,11 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
         case WOp::Leaf:
         case WOp::Divide:
         case WOp::SchoolBuild:
-        case WOp::SchoolProp: launch_worklist_basic(s.op, s.d_desc, s.d_tab, nctas, qn, q0, f->stream); break;
+        case WOp::SchoolProp: launch_worklist_basic(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, f->stream); break;
         case WOp::FusedBuild:
         case WOp::FusedProp: launch_worklist_fused(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
+        case WOp::SubBuild:
+        case WOp::SubProp: launch_worklist_sub(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
         default: launch_worklist_spec(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
     }
     f->prof.end(f->stream);

@@ -26,7 +26,7 @@ struct WStep {
     // (span players each, nreal of them; span 0 = no pruning), flops per node
     std::vector<int> dmem, dnreal;
     std::vector<long> dspan;
-    std::vector<double> dfq;
+    std::vector<double> dfq, dfq0;   // pruned part (per unit of span) and unpruned part
     const void *d_desc = nullptr;
     const int2 *d_tab = nullptr;
 };

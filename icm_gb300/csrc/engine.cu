@@ -188,6 +188,11 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
             }
         }
     }
+    // bottom schoolbook levels fused into the subtree kernels (never the root,
+    // whose product is not built; at most the levels one CTA of blocks spans)
+    p->Lf = 0;
+    if (g_config.enable_subtree == 1)
+        for (int l = 1; l <= std::min(p->L - 2, kSubMaxLevels) && p->lv[l].kind == 0; ++l) p->Lf = l;
     // per-node element counts
     size_t per_q = 0;
     size_t fa = 0, fb = 0;
@@ -421,10 +426,23 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     Level *lv = p->lv;
     Prof *pr = &p->prof;
     const int *zp = p->zskip ? p->d_z : nullptr;   // zero-prefix pruning (one-CTA levels)
-    launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, lv[0].P, lv[0].pst,
-                lv[0].plen, st, pr);
-    ++p->launches;
     auto frac = [&](long span, int nreal) { pr->scale = zp ? hot_frac(p, q0, nq, span, nreal) : 1.0; };
+    const int Lf = p->Lf;
+    SubArgs SA{};
+    SubFlops SF{};
+    if (Lf >= 1) {   // leaf blocks and the bottom schoolbook levels in one kernel
+        SA = sub_args(p, Lf, p->d_S, p->d_node, p->d_a, (size_t)p->n, p->subset ? p->d_active : nullptr,
+                      p->d_contrib, !divide, divide, &SF);
+        double fl = SF.leaf;
+        for (int l = 1; l <= Lf; ++l)
+            fl += SF.build[l] * (zp ? hot_frac(p, q0, nq, lv[l].deg, lv[l].nreal) : 1.0);
+        pr->scale = 1.0;
+        launch_sub_build(SA, nq, q0, st, pr, fl);
+    } else {
+        launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, lv[0].P, lv[0].pst,
+                    lv[0].plen, st, pr);
+    }
+    ++p->launches;
     if (L >= 2 && lv[1].kind == 2) {
         frac(lv[0].deg, lv[0].nreal);
         launch_spec_init(lv[0], nq, tw, logTW, st, pr, zp, q0);
@@ -432,6 +450,13 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     }
     for (int l = 1; l <= L - 2; ++l) {
         frac(lv[l].deg, lv[l].nreal);   // builds decide per parent
+        if (l <= Lf) {   // built by the subtree kernel
+            if (l == Lf && lv[l + 1].kind == 2) {
+                launch_spec_init(lv[l], nq, tw, logTW, st, pr, zp, q0);
+                ++p->launches;
+            }
+            continue;
+        }
         if (lv[l].kind == 2) {
             if (lv[l - 1].deg > kSpecMaxD) {
                 launch_specbig_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, p->d_fa, p->d_fc, tw, logTW, st,
@@ -459,7 +484,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     pr->scale = 1.0;
     if (L >= 2 && lv[L - 1].fft)
         launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches, pr);
-    for (int l = L - 1; l >= 1; --l) {
+    for (int l = L - 1; l >= 1 + Lf; --l) {
         const bool root = (l == L - 1);
         const double *gp = root ? p->d_payout : lv[l].g;
         const size_t gp_q = root ? 0 : lv[l].g_q;
@@ -507,6 +532,22 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
         }
     }
     pr->scale = 1.0;
+    if (Lf >= 1) {   // the bottom levels' propagate and (with divide) the division in one kernel
+        double fl = 0.0, hotp = 1.0;
+        for (int l = 1; l <= Lf; ++l)
+            fl += SF.prop[l] * (zp ? hot_frac(p, q0, nq, lv[l - 1].deg, lv[l - 1].nreal) : 1.0);
+        if (zp) {
+            double hot = 0.0;
+            for (int q = 0; q < nq; ++q) hot += p->n - p->h_z[q0 + q];
+            hotp = hot / ((double)nq * p->n);
+        }
+        launch_sub_prop(SA, nq, q0, st, pr, fl + SF.divide * hotp);
+        ++p->launches;
+        if (!divide) return;
+        launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, first ? 1 : 0, st, pr);
+        ++p->launches;
+        return;
+    }
     if (!divide) return;
     if (zp) {   // players with a leaf factor of 0 skip the division
         double hot = 0.0;

@@ -59,6 +59,7 @@ struct Plan {
     bool spectral = true;           // use spectral levels where they apply
     bool coeff_only = false;        // never use spectral levels
     bool zskip = true;              // prune wholly-zero tree nodes per quadrature node
+    int Lf = 0;                     // bottom schoolbook levels fused into the subtree kernels
     std::vector<double> S_sorted;
     std::vector<int> perm;          // perm[i] = original index of sorted player i
     std::vector<int> inv_perm;

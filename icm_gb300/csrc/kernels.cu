@@ -16,15 +16,13 @@
 #include "engine.h"
 #include "fft.cuh"
 #include "kernels.h"
+#include "leafdiv.cuh"
 
 namespace icmg {
 
 // ------------------------------------------------------------------ leaves
-// Leaf factors and block products (reference src/cpu/icm.c:2199-2224,
-// src/gpu/gpu_kernels.cu:909-936,1030-1091).  One thread per (node, block);
-// the block product lives in registers.  Updating all B+1 coefficients for
-// every player adds exact zeros above the running degree, so the result is
-// the reference's recurrence P[m] = a P[m] + (1-a) P[m-1] bit for bit.
+// Leaf factors and block products (leafdiv.cuh).  One thread per (node, block);
+// the block product lives in registers.
 template <int B>
 __device__ __forceinline__ void leaf_body_t(const LeafArgs &A, int bx, int q) {
     const int b = bx * blockDim.x + threadIdx.x;
@@ -34,19 +32,7 @@ __device__ __forceinline__ void leaf_body_t(const LeafArgs &A, int bx, int q) {
     const int start = b * B;
     const int bs = min(B, n - start);
     double P[B + 1];
-    P[0] = 1.0;
-#pragma unroll
-    for (int m = 1; m <= B; ++m) P[m] = 0.0;
-    double *arow = A.a + (size_t)q * A.aq + start;
-    for (int j = 0; j < bs; ++j) {
-        const double arg = A.S[start + j] * logv;
-        const double a = (arg < -700.0) ? 0.0 : exp(arg);
-        arow[j] = a;
-        const double bb = 1.0 - a;
-#pragma unroll
-        for (int m = B; m >= 1; --m) P[m] = a * P[m] + bb * P[m - 1];
-        P[0] *= a;
-    }
+    block_product<B>(A.S + start, bs, logv, A.a + (size_t)q * A.aq + start, P);
     double *bp = A.blockP + ((size_t)q * nblocks + b) * (B + 1);
 #pragma unroll
     for (int m = 0; m <= B; ++m) bp[m] = P[m];
@@ -58,16 +44,9 @@ __device__ __forceinline__ void leaf_body_t(const LeafArgs &A, int bx, int q) {
     for (int m = B + 1; m < pst0; ++m) leaf[m] = 0.0;
 }
 
-__device__ void leaf_body(const LeafArgs &A, int bx, int q) {
-    switch (A.B) {
-        case 4: leaf_body_t<4>(A, bx, q); break;
-        case 8: leaf_body_t<8>(A, bx, q); break;
-        case 16: leaf_body_t<16>(A, bx, q); break;
-        default: leaf_body_t<32>(A, bx, q); break;
-    }
-}
-
-__global__ void k_leaf(LeafArgs A) { leaf_body(A, blockIdx.x, blockIdx.y); }
+// one kernel per block size: registers sized for that B
+template <int B>
+__global__ void k_leaf_t(LeafArgs A) { leaf_body_t<B>(A, blockIdx.x, blockIdx.y); }
 
 // ------------------------------------------------------- schoolbook build
 // parent j = L*R mod x^lp, children of length lc (reference icm.c:465-480).
@@ -139,46 +118,16 @@ __device__ __forceinline__ void divide_body_t(const DivideArgs &A, int bx, int q
     const int pk = min(bs, A.k);
     const double a = A.a[(size_t)q * A.aq + i];
     if (a == 0.0) { *out = 0.0; return; }   // S logv < -700: zero weight (g of its block may be pruned)
-    const double bb = 1.0 - a;
     const double *P = A.blockP + ((size_t)q * A.nblocks + b) * (B + 1);
     const double *g = A.g0 + q * A.g0_q + (size_t)b * A.gst0;
-    double eq = 0.0;
-    if (a > 0.5) {
-        const double ia = 1.0 / a, c = -bb * ia;
-        double Qv = P[0] * ia;
-        eq = g[0] * Qv;
-        for (int m = 1; m < pk; ++m) {
-            Qv = c * Qv + P[m] * ia;
-            eq += g[m] * Qv;
-        }
-    } else if (a > 1e-15) {
-        const double ib = 1.0 / bb, c = -a * ib;
-        double Qa[B];
-        double Qp = P[bs] * ib;
-        Qa[bs - 1] = Qp;
-        for (int m = bs - 2; m >= 0; --m) {
-            Qp = c * Qp + P[m + 1] * ib;
-            Qa[m] = Qp;
-        }
-        for (int m = 0; m < pk; ++m) eq += g[m] * Qa[m];
-    } else {
-        for (int m = 0; m < pk; ++m) eq += g[m] * P[m + 1];
-    }
+    const double eq = divide_dot<B>(a, P, bs, pk, g);
     double pw = nd[1] * A.S[i] * a * nd[2];
     if (!isfinite(pw)) pw = 0.0;
     *out = pw * eq;
 }
 
-__device__ void divide_body(const DivideArgs &A, int bx, int q) {
-    switch (A.B) {
-        case 4: divide_body_t<4>(A, bx, q); break;
-        case 8: divide_body_t<8>(A, bx, q); break;
-        case 16: divide_body_t<16>(A, bx, q); break;
-        default: divide_body_t<32>(A, bx, q); break;
-    }
-}
-
-__global__ void k_divide(DivideArgs A) { divide_body(A, blockIdx.x, blockIdx.y); }
+template <int B>
+__global__ void k_divide_t(DivideArgs A) { divide_body_t<B>(A, blockIdx.x, blockIdx.y); }
 
 // ordered sum over the chunk's nodes: deterministic for a fixed chunking
 __global__ void k_accumulate(int n, int nq, const double *__restrict__ contrib, double *__restrict__ acc,
@@ -331,6 +280,7 @@ void fft_set_smem_limits() {
     fused_set_smem_limits();
     spec_set_smem_limits();
     vjp_set_smem_limits();
+    sub_set_smem_limits();
     const int mx = kSmemFftMax * (int)sizeof(double2);
     cudaFuncSetAttribute(k_fft_smem<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft_smem<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -532,7 +482,13 @@ void launch_leaf(int B, int n, int nblocks, const double *S, const double *node,
     LeafArgs A = leaf_args(B, n, nblocks, S, node, a, (size_t)n, blockP, P0, pst0, plen0, &fq);
     A.q0 = q0;
     pr->begin("leaf", fq * nq, st);
-    k_leaf<<<dim3(A.nbx, nq), 128, 0, st>>>(A);
+    const dim3 g(A.nbx, nq);
+    switch (B) {
+        case 4: k_leaf_t<4><<<g, 128, 0, st>>>(A); break;
+        case 8: k_leaf_t<8><<<g, 128, 0, st>>>(A); break;
+        case 16: k_leaf_t<16><<<g, 128, 0, st>>>(A); break;
+        default: k_leaf_t<32><<<g, 128, 0, st>>>(A); break;
+    }
     pr->end(st);
 }
 
@@ -543,7 +499,13 @@ void launch_divide(int B, int n, int k, int nblocks, const double *S, const doub
     DivideArgs A = divide_args(B, n, k, nblocks, S, node, a, (size_t)n, blockP, g0, g0_q, gst0, active, contrib, &fq);
     A.q0 = q0;
     pr->begin("divide", fq * nq, st);
-    k_divide<<<dim3(A.nbx, nq), 128, 0, st>>>(A);
+    const dim3 g(A.nbx, nq);
+    switch (B) {
+        case 4: k_divide_t<4><<<g, 128, 0, st>>>(A); break;
+        case 8: k_divide_t<8><<<g, 128, 0, st>>>(A); break;
+        case 16: k_divide_t<16><<<g, 128, 0, st>>>(A); break;
+        default: k_divide_t<32><<<g, 128, 0, st>>>(A); break;
+    }
     pr->end(st);
 }
 
@@ -572,17 +534,19 @@ void launch_school_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const
 }
 
 // ---------------------------------------------------------------- work lists
+template <int B>
 __global__ void kw_leaf(const LeafArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
     LeafArgs A = D[t.x];
     A.q0 = q0;
-    leaf_body(A, t.y, blockIdx.y);
+    leaf_body_t<B>(A, t.y, blockIdx.y);
 }
+template <int B>
 __global__ void kw_divide(const DivideArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
     DivideArgs A = D[t.x];
     A.q0 = q0;
-    divide_body(A, t.y, blockIdx.y);
+    divide_body_t<B>(A, t.y, blockIdx.y);
 }
 __global__ void kw_school_build(const SchoolBuildArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
@@ -597,12 +561,29 @@ __global__ void kw_school_prop(const SchoolPropArgs *__restrict__ D, const int2 
     school_prop_body(A, t.y, blockIdx.y);
 }
 
-void launch_worklist_basic(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, cudaStream_t st) {
+void launch_worklist_basic(WOp op, int B, const void *desc, const int2 *tab, int nctas, int nq, int q0,
+                           cudaStream_t st) {
     if (nctas <= 0 || nq <= 0) return;
     const dim3 g(nctas, nq);
+    const LeafArgs *DL = (const LeafArgs *)desc;
+    const DivideArgs *DD = (const DivideArgs *)desc;
     switch (op) {
-        case WOp::Leaf: kw_leaf<<<g, 128, 0, st>>>((const LeafArgs *)desc, tab, q0); break;
-        case WOp::Divide: kw_divide<<<g, 128, 0, st>>>((const DivideArgs *)desc, tab, q0); break;
+        case WOp::Leaf:
+            switch (B) {
+                case 4: kw_leaf<4><<<g, 128, 0, st>>>(DL, tab, q0); break;
+                case 8: kw_leaf<8><<<g, 128, 0, st>>>(DL, tab, q0); break;
+                case 16: kw_leaf<16><<<g, 128, 0, st>>>(DL, tab, q0); break;
+                default: kw_leaf<32><<<g, 128, 0, st>>>(DL, tab, q0); break;
+            }
+            break;
+        case WOp::Divide:
+            switch (B) {
+                case 4: kw_divide<4><<<g, 128, 0, st>>>(DD, tab, q0); break;
+                case 8: kw_divide<8><<<g, 128, 0, st>>>(DD, tab, q0); break;
+                case 16: kw_divide<16><<<g, 128, 0, st>>>(DD, tab, q0); break;
+                default: kw_divide<32><<<g, 128, 0, st>>>(DD, tab, q0); break;
+            }
+            break;
         case WOp::SchoolBuild: kw_school_build<<<g, 256, 0, st>>>((const SchoolBuildArgs *)desc, tab, q0); break;
         case WOp::SchoolProp: kw_school_prop<<<g, 256, 0, st>>>((const SchoolPropArgs *)desc, tab, q0); break;
         default: break;

@@ -9,6 +9,7 @@
 namespace icmg {
 
 struct Level;
+struct Plan;
 
 // Optional per-launch timing: when `on`, every launcher brackets its kernel
 // with CUDA events on the launch stream and records the kernel's algorithmic
@@ -226,14 +227,59 @@ FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl,
 // ---- work lists (batch.cu drives them).  One launch runs one kind of step
 // for many tournaments: grid (nctas, nq), tab[blockIdx.x] = (descriptor,
 // block within the descriptor), blockIdx.y = node within the chunk.
-enum class WOp : int { Leaf, SchoolBuild, SchoolProp, Divide, SpecInit, SpecBuild, Gspec, SpecProp, FusedBuild, FusedProp };
-void launch_worklist_basic(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, cudaStream_t st);
+enum class WOp : int {
+    Leaf, SchoolBuild, SchoolProp, Divide, SpecInit, SpecBuild, Gspec, SpecProp, FusedBuild, FusedProp, SubBuild, SubProp
+};
+// B: leaf block size of the launch (Leaf and Divide lists are keyed by it)
+void launch_worklist_basic(WOp op, int B, const void *desc, const int2 *tab, int nctas, int nq, int q0,
+                           cudaStream_t st);
 void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
                           cudaStream_t st);
 void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
                            cudaStream_t st);
 size_t spec_smem_bytes(int M);     // dynamic shared memory of the spectral kernels
 size_t fused_smem_bytes(int N);    // dynamic shared memory of the fused kernels
+
+// ---- bottom subtree (subtree.cu): leaf blocks plus the lowest Lf schoolbook
+// levels in one kernel per direction, kSubBlocks leaf blocks per CTA
+constexpr int kSubBlocks = 256;
+constexpr int kSubMaxLevels = 8;
+struct SubLevel {
+    double *P;
+    size_t P_q;
+    int pst, plen, nreal;
+    double *g;
+    size_t g_q;
+    int gst, glen;
+    const uint8_t *hot;   // subset mask of this level, or null
+    long deg;
+};
+struct SubArgs {
+    int B, n, k, nblocks, Lf;
+    const double *S, *node;
+    double *a;
+    size_t aq;
+    double *blockP;
+    SubLevel lv[kSubMaxLevels + 1];
+    const uint8_t *active;
+    double *contrib;
+    int write_g, do_divide;
+    ZeroPrefix z;   // z.q0: the chunk's first node (also the node table's offset)
+    int nbx;
+};
+struct SubFlops {   // algorithmic FP64 flops per quadrature node
+    double leaf, divide;
+    double build[kSubMaxLevels + 1], prop[kSubMaxLevels + 1];   // level l products / middle products
+};
+SubArgs sub_args(const Plan *p, int Lf, const double *S, const double *node, double *a, size_t aq,
+                 const uint8_t *active, double *contrib, bool write_g, bool do_divide, SubFlops *fl);
+void launch_sub_build(const SubArgs &A, int nq, int q0, cudaStream_t st, Prof *pr, double fq);
+void launch_sub_prop(const SubArgs &A, int nq, int q0, cudaStream_t st, Prof *pr, double fq);
+void launch_worklist_sub(WOp op, int B, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                         cudaStream_t st);
+size_t sub_build_smem(int B);
+size_t sub_prop_smem(int B);
+void sub_set_smem_limits();
 
 void fft_set_smem_limits();
 

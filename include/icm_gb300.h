@@ -32,7 +32,11 @@ int icm_last_status(void);
  *   max_device_bytes  cap on the plan's device memory
  *   disable_zero_prefix  1 = compute tree nodes whose players all have a
  *                     leaf factor of exactly 0 at a quadrature node (by
- *                     default they are written as monomials or skipped)  */
+ *                     default they are written as monomials or skipped)
+ *   enable_subtree    1 = run the leaf blocks and the bottom schoolbook
+ *                     levels in one kernel per direction instead of level
+ *                     by level (same arithmetic; measured slightly slower
+ *                     on GB300, kept for comparison)                       */
 typedef struct {
     int block_size;
     int fft_min_degree;
@@ -40,6 +44,7 @@ typedef struct {
     int coefficient_fft_only;
     size_t max_device_bytes;
     int disable_zero_prefix;
+    int enable_subtree;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created

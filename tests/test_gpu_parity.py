@@ -267,3 +267,24 @@ def test_quadrature_ladder(gpu_icm, oracle):
     assert max_rel(E, oracle.equity(S, P, Q=Q), floor=1e-12 * np.abs(E).max()) < 1e-9
     E2, Q2, err2 = gpu_icm.equity_adaptive(S, P, tol=1e-30, Q0=128, Qmax=512)   # capped
     assert Q2 == 512 and err2 > 0
+
+
+@pytest.mark.parametrize("B,fft_min", [(4, 128), (8, 64), (16, 1 << 20), (32, 64), (8, 8)])
+def test_subtree_kernels_equal_level_by_level(gpu_icm, B, fft_min):
+    """Leaf blocks and bottom schoolbook levels fused per direction: the same
+    arithmetic as the level-by-level kernels, so bitwise equal results (full
+    query, subset, batched)."""
+    rng = np.random.default_rng(B + fft_min)
+    S = 10.0 ** (5 * rng.random(7001))
+    P = np.sort(rng.random(900))[::-1]
+    T = sorted(rng.choice(len(S), size=9, replace=False).tolist())
+    ts = W.batched(count=10)
+    out = []
+    for sub in (True, False):
+        gpu_icm.configure(block_size=B, fft_min_degree=fft_min, subtree=sub)
+        out.append((gpu_icm.equity(S, P, Q=64), gpu_icm.equity_subset(S, P, T, Q=64),
+                    gpu_icm.equity_batched(ts, Q=32)))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    for a, b in zip(out[0][2], out[1][2]):
+        assert np.array_equal(a, b)
