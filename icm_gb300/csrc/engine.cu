@@ -177,9 +177,10 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
             // (not truncated at k) and the transforms fit one CTA
             // children beyond one CTA's transform use the multi-pass kernels,
             // which hand g spectra (not coefficients) to a spectral level below
+            // (a parent truncated at k is fine: its build writes coefficients,
+            // and a truncated parent never has a spectral level above it)
             bool spec = p->spectral && can_fft && c.deg + 1 <= k;
             if (c.deg > kSpecMaxD) spec = spec && l - 1 >= 1 && p->lv[l - 1].kind == 2;
-            if (l <= p->L - 2) spec = spec && v.deg + 1 <= k;
             v.kind = spec ? 2 : (can_fft ? 1 : 0);
             v.fft = (v.kind == 1) ? 1 : 0;
             if (v.fft) {

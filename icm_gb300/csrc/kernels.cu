@@ -49,26 +49,72 @@ template <int B>
 __global__ void k_leaf_t(LeafArgs A) { leaf_body_t<B>(A, blockIdx.x, blockIdx.y); }
 
 // ------------------------------------------------------- schoolbook build
-// parent j = L*R mod x^lp, children of length lc (reference icm.c:465-480).
-// One thread per output coefficient; parents >= j0 only (the FFT path uses
-// j0 = npairs to let this kernel copy a lone left child).
+// parent j = L*R mod x^lp, children of length lc (reference icm.c:465-480);
+// parents >= j0 only (the FFT path uses j0 = npairs to let this kernel copy a
+// lone left child).  Output t of the full product has min(t, 2lc-2-t) + 1
+// terms, a triangle: one thread per output idles half the lanes of a warp.
+// Instead each thread takes a work item of two outputs whose term counts add
+// up to lc -- t and lc-2-t below the middle, t and 3lc-2-t above it -- and
+// walks both in one loop of uniform length.  Per output the terms are summed
+// in the same order as one thread per output would.
+__device__ __forceinline__ void school_item(int lc, int w, int *t1, int *t2) {
+    const int h = lc >> 1;   // pairs per half: ceil((lc - 1) / 2)
+    *t2 = -1;
+    if (w < h) {
+        *t1 = w;
+        *t2 = lc - 2 - w;
+    } else if (w == h) {
+        *t1 = lc - 1;   // the middle output: lc terms
+    } else if (w < 2 * h + 1) {
+        const int u = w - h - 1;
+        *t1 = lc + u;
+        *t2 = 2 * lc - 2 - u;
+    } else {
+        *t1 = 2 * lc - 1;   // the padding slot past the full product
+    }
+    if (*t2 == *t1) *t2 = -1;
+}
+__host__ __device__ __forceinline__ int school_items(int lc) { return 2 * (lc >> 1) + 2; }
+
 __device__ void school_build_body(const SchoolBuildArgs &A, int bx, int q) {
     const long idx = (long)bx * blockDim.x + threadIdx.x;
-    const int pst_p = A.pst_p, pst_c = A.pst_c, lc = A.lc;
-    const int j = A.j0 + (int)(idx / pst_p);
-    const int t = (int)(idx % pst_p);
+    const int pst_p = A.pst_p, pst_c = A.pst_c, lc = A.lc, lp = A.lp;
+    const int W = school_items(lc);
+    const int j = A.j0 + (int)(idx / W);
+    const int w = (int)(idx % W);
     if (j >= A.nreal_p) return;
+    int t1, t2;
+    school_item(lc, w, &t1, &t2);
     const double *L = A.Pc + q * A.Pc_q + (size_t)(2 * j) * pst_c;
     double *out = A.Pp + q * A.Pp_q + (size_t)j * pst_p;
-    if (zp_cold(A.z, q, j)) { out[t] = (t == A.z.span && t < A.lp) ? 1.0 : 0.0; return; }   // x^deg
-    if (t >= A.lp) { out[t] = 0.0; return; }
-    if (2 * j + 1 >= A.nreal_c) { out[t] = (t < lc) ? L[t] : 0.0; return; }
-    const double *R = L + pst_c;
-    const int ilo = max(0, t - (lc - 1));
-    const int ihi = min(t, lc - 1);
-    double s = 0.0;
-    for (int i = ilo; i <= ihi; ++i) s = fma(L[i], R[t - i], s);
-    out[t] = s;
+    double v1 = 0.0, v2 = 0.0;
+    if (zp_cold(A.z, q, j)) {   // x^deg
+        v1 = (t1 == A.z.span && t1 < lp) ? 1.0 : 0.0;
+        v2 = (t2 == A.z.span && t2 < lp) ? 1.0 : 0.0;
+    } else if (2 * j + 1 >= A.nreal_c) {   // lone child copied up
+        v1 = (t1 < lc && t1 < lp) ? L[t1] : 0.0;
+        v2 = (t2 >= 0 && t2 < lc && t2 < lp) ? L[t2] : 0.0;
+    } else {
+        const double *R = L + pst_c;
+        const int F = 2 * lc - 1;
+        const int lo1 = max(0, t1 - (lc - 1));
+        const int c1 = (t1 < lp && t1 < F) ? min(t1, lc - 1) - lo1 + 1 : 0;
+        const int lo2 = max(0, t2 - (lc - 1));
+        const int c2 = (t2 >= 0 && t2 < lp) ? min(t2, lc - 1) - lo2 + 1 : 0;
+        double s1 = 0.0, s2 = 0.0;
+        for (int r = 0; r < c1 + c2; ++r) {
+            const bool first = r < c1;
+            const int t = first ? t1 : t2;
+            const int i = first ? lo1 + r : lo2 + (r - c1);
+            const double acc = fma(L[i], R[t - i], first ? s1 : s2);
+            s1 = first ? acc : s1;
+            s2 = first ? s2 : acc;
+        }
+        v1 = s1;
+        v2 = s2;
+    }
+    if (t1 < pst_p) out[t1] = v1;
+    if (t2 >= 0 && t2 < pst_p) out[t2] = v2;
 }
 
 __global__ void k_school_build(SchoolBuildArgs A) { school_build_body(A, blockIdx.x, blockIdx.y); }
@@ -450,7 +496,7 @@ DivideArgs divide_args(int B, int n, int k, int nblocks, const double *S, const 
 }
 
 SchoolBuildArgs school_build_args(const Level &c, const Level &p, int j0, double *fq) {
-    const long work = (long)(p.nreal - j0) * p.pst;
+    const long work = (long)(p.nreal - j0) * school_items(c.plen);
     SchoolBuildArgs A{c.P, c.P_q, c.pst, c.plen, c.nreal, p.P, p.P_q, p.pst, p.plen, p.nreal, j0,
                       work > 0 ? (int)nblk(work, 256) : 0, ZeroPrefix{nullptr, 0, p.deg}};
     if (fq) {

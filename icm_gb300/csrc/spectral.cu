@@ -204,13 +204,13 @@ __device__ void spec_build_body(const SpecBuildArgs &A, int bx, int q) {
             }
             u.x = (x0 - xtop) * (2.0 * D);   // y_0 = x_0 - x_{2D}, in the unscaled units of u
         }
-        if (Pout) {
+        if (Pout) {   // truncated at plen_p; the row's padding up to pst_p is zero
             double *out = Pout + q * Po_q + (size_t)j * pst_p;
             const double x0 = (s == 0) ? eL[0] * (has_r ? eL[2] : 1.0) : u.x * one_over_2D;
-            if (2 * s < plen_p) out[2 * s] = x0;
-            if (2 * s + 1 < plen_p) out[2 * s + 1] = u.y * one_over_2D;
+            if (2 * s < pst_p) out[2 * s] = (2 * s < plen_p) ? x0 : 0.0;
+            if (2 * s + 1 < pst_p) out[2 * s + 1] = (2 * s + 1 < plen_p) ? u.y * one_over_2D : 0.0;
             if (s == 0) {
-                if (2 * D < plen_p) out[2 * D] = xtop;
+                if (2 * D < pst_p) out[2 * D] = (2 * D < plen_p) ? xtop : 0.0;
                 for (int t = 2 * D + 1; t < pst_p; ++t) out[t] = 0.0;
             }
         }

@@ -72,10 +72,10 @@ __global__ void k_sb_build2(const double *__restrict__ cends, size_t ce_q, int n
     if (zcold(zp, zq0, 2L * D, q, j)) {   // x^{2D}: coefficients and ends
         if (Pout) {
             double *out = Pout + q * Po_q + (size_t)j * pst_p;
-            if (2 * s < plen_p) out[2 * s] = 0.0;
-            if (2 * s + 1 < plen_p) out[2 * s + 1] = 0.0;
+            if (2 * s < pst_p) out[2 * s] = 0.0;
+            if (2 * s + 1 < pst_p) out[2 * s + 1] = 0.0;
             if (s == 0) {
-                if (2 * D < plen_p) out[2 * D] = 1.0;
+                if (2 * D < pst_p) out[2 * D] = (2 * D < plen_p) ? 1.0 : 0.0;
                 for (int t = 2 * D + 1; t < pst_p; ++t) out[t] = 0.0;
             }
         }
@@ -92,13 +92,13 @@ __global__ void k_sb_build2(const double *__restrict__ cends, size_t ce_q, int n
     const bool has_r = (2 * j + 1) < nreal_c;
     const double xtop = eL[1] * (has_r ? eL[3] : 0.0);
     const double inv2D = 1.0 / (2.0 * D);
-    if (Pout) {
+    if (Pout) {   // truncated at plen_p; the row's padding up to pst_p is zero
         double *out = Pout + q * Po_q + (size_t)j * pst_p;
         const double x0 = (s == 0) ? eL[0] * (has_r ? eL[2] : 1.0) : u.x * inv2D;
-        if (2 * s < plen_p) out[2 * s] = x0;
-        if (2 * s + 1 < plen_p) out[2 * s + 1] = u.y * inv2D;
+        if (2 * s < pst_p) out[2 * s] = (2 * s < plen_p) ? x0 : 0.0;
+        if (2 * s + 1 < pst_p) out[2 * s + 1] = (2 * s + 1 < plen_p) ? u.y * inv2D : 0.0;
         if (s == 0) {
-            if (2 * D < plen_p) out[2 * D] = xtop;
+            if (2 * D < pst_p) out[2 * D] = (2 * D < plen_p) ? xtop : 0.0;
             for (int t = 2 * D + 1; t < pst_p; ++t) out[t] = 0.0;
         }
     }
