@@ -73,6 +73,8 @@ static bool fits_worklist(const Plan *p) {
 namespace {
 struct PhaseBuilder {
     std::vector<WStep> steps;
+    // set before add() for packed steps: items of the descriptor, items per CTA
+    int pack_items = 0, pack_cb = 1;
     template <class A>
     void add(WOp op, int key, const char *name, const A &a, size_t smem, double fq, int one = 0, int mem = -1,
              long span = 0, int nreal = 0, double fq0 = 0.0) {
@@ -88,10 +90,15 @@ struct PhaseBuilder {
             s->one = one;
             s->name = name;
             s->esz = sizeof(A);
+            s->packed = pack_items > 0 ? 1 : 0;
+            s->cb = pack_cb;
         }
         const unsigned char *b = (const unsigned char *)&a;
         s->desc.insert(s->desc.end(), b, b + sizeof(A));
-        for (int bx = 0; bx < a.nbx; ++bx) s->tab.push_back(make_int2(s->nd, bx));
+        if (s->packed)
+            for (int j = 0; j < pack_items; ++j) s->tab.push_back(make_int2(s->nd, j));
+        else
+            for (int bx = 0; bx < a.nbx; ++bx) s->tab.push_back(make_int2(s->nd, bx));
         ++s->nd;
         s->smem = std::max(s->smem, smem);
         s->fq += fq;
@@ -164,7 +171,11 @@ static void build_steps(Forest *f) {
                 if (lv[l].kind == 2) {
                     SpecBuildArgs A = spec_build_args(lv[l - 1], lv[l], lv[l + 1].kind != 2, tw, logTW, &fq, &sm);
                     A.z.zp = zpre(p);
-                    b.add(WOp::SpecBuild, A.logD, "wl_spec_build", A, sm, fq, 0, t, lv[l].deg, lv[l].nreal);
+                    b.pack_items = lv[l].nreal;   // items of different members share CTAs
+                    b.pack_cb = A.logD >= 12 ? 1 : 4096 >> A.logD;
+                    b.add(WOp::SpecBuild, 2 * A.logD + (A.pspec ? 1 : 0), "wl_spec_build", A, sm, fq, 0, t, lv[l].deg,
+                          lv[l].nreal);
+                    b.pack_items = 0;
                 } else if (lv[l].fft) {
                     if (lv[l].npairs > 0) {
                         FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], false, tw, logTW, &fq, &sm);
@@ -237,7 +248,11 @@ static void build_steps(Forest *f) {
                 SpecPropArgs A = spec_prop_args(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l],
                                                 l - 1 >= 1 && lv[l - 1].kind == 2, nullptr, tw, logTW, &fq, &sm);
                 A.z.zp = zpre(p);
-                b.add(WOp::SpecProp, A.logD, "wl_spec_prop", A, sm, fq, 0, t, root ? 0 : lv[l].deg, lv[l].nreal);
+                b.pack_items = lv[l].nreal;
+                b.pack_cb = A.logD >= 12 ? 1 : 4096 >> A.logD;
+                b.add(WOp::SpecProp, 2 * A.logD + (A.Gout ? 1 : 0), "wl_spec_prop", A, sm, fq, 0, t,
+                      root ? 0 : lv[l].deg, lv[l].nreal);
+                b.pack_items = 0;
             } else if (lv[l].fft) {
                 if (lv[l].npairs > 0) {
                     FusedPropArgs A = fused_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nullptr, tw, logTW, &fq,
@@ -344,6 +359,12 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
     const int nctas = (int)s.tab.size();
     const int qn = s.one ? 1 : nq;
     if (f->prof.on) f->prof.begin(s.name, step_flops(f, s, qn, q0), f->stream);
+    if (s.packed) {
+        launch_packed_spec(s.op, s.d_desc, s.d_tab, nctas, s.cb, qn, q0, s.smem, f->stream);
+        f->prof.end(f->stream);
+        ++f->launches;
+        return;
+    }
     switch (s.op) {
         case WOp::Leaf:
         case WOp::Divide:

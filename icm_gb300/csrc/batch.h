@@ -15,6 +15,8 @@ struct WStep {
     WOp op = WOp::Leaf;
     int key = 0;                      // log2 of the transform size (0: plain kernels)
     int one = 0;                      // 1: one node (the root's payout spectrum)
+    int packed = 0;                   // 1: tab holds item slots (descriptor, item), cb per CTA
+    int cb = 1;
     const char *name = "";
     size_t esz = 0;                   // bytes per descriptor
     int nd = 0;                       // descriptors

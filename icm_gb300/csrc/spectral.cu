@@ -25,6 +25,8 @@
 // pointwise twist between two transforms is applied while permuting the data
 // into bit-reversed order in place (smem_bitrev_map).  A missing sibling
 // (ragged tree edge) is the polynomial 1: spectrum 1, ends (1, 0).
+#include <algorithm>
+
 #include "engine.h"
 #include "fft.cuh"
 #include "kernels.h"
@@ -41,6 +43,15 @@ static inline int ilog2s(long v) {
 }
 static inline int spec_cb(int M) { return M >= 4096 ? 1 : 4096 / M; }
 static inline size_t spec_smem(int M) { return (size_t)spec_cb(M) * M * sizeof(double2); }
+// build and propagate: the items' data plus one view and one index per item
+constexpr size_t kViewBytes = 96;
+constexpr size_t kItemBytes = kViewBytes + sizeof(int);
+static inline size_t spec_smem_v(int M) { return (size_t)spec_cb(M) * (M * sizeof(double2) + kItemBytes); }
+static size_t spec_smem_v_max() {   // over the transform sizes a level can use (D >= 4)
+    size_t mx = 0;
+    for (int M = 4; M <= kSpecMaxM; M *= 2) mx = std::max(mx, spec_smem_v(M));
+    return mx;
+}
 
 __device__ __forceinline__ double2 twl(const double2 *__restrict__ tw, long idx) { return __ldg(&tw[idx]); }
 
@@ -120,63 +131,71 @@ __device__ void spec_init_body(const SpecInitArgs &A, int bx, int q) {
 // and the odd output bins of a mirror pair (f, D-1-f) are
 //   H(f) = (Ep + T) / 4D,  H(D-1-f) = conj(Ep - T) / 4D,
 //   Ep = c[f] + conj c[D-1-f],  T = -i (c[f] - conj c[D-1-f]) e^{-2 pi i (2f+1)/4D}.
-__device__ void spec_build_body(const SpecBuildArgs &A, int bx, int q) {
-    const auto cspec = A.cspec;
-    const auto cs_q = A.cs_q;
-    const auto cends = A.cends;
-    const auto ce_q = A.ce_q;
-    const auto nreal_c = A.nreal_c;
-    const auto nreal_p = A.nreal_p;
-    const auto logD = A.logD;
-    const auto pspec = A.pspec;
-    const auto ps_q = A.ps_q;
-    const auto pends = A.pends;
-    const auto pe_q = A.pe_q;
-    const auto Pout = A.Pout;
-    const auto Po_q = A.Po_q;
-    const auto pst_p = A.pst_p;
-    const auto plen_p = A.plen_p;
-    const auto tw = A.tw;
-    const auto logTW = A.logTW;
+//
+// Every item (parent) of a CTA is described by a view staged in shared memory
+// (pointers for its node and quadrature node), so a CTA may hold items of
+// different tournaments (packed work lists); a single plan fills the views
+// from its one argument block.
+struct SbView {
+    const double2 *sL, *sR;   // children's spec2 (sR null: missing right child, the polynomial 1)
+    const double *eL, *eR;    // children's ends (eR null: (1, 0))
+    double2 *ps;              // parent spec2 (2D+1 bins) or null
+    double *pe;               // parent ends or null
+    double *po;               // parent coefficients or null
+    int pst, plen, cold;
+};
+static_assert(sizeof(SbView) <= kViewBytes, "view size");
 
-    extern __shared__ double2 sm[];
+__device__ __forceinline__ void sb_fill(const SpecBuildArgs &A, int q, int q0, int j, int D, SbView &v) {
+    v.sL = A.cspec + q * A.cs_q + (size_t)(2 * j) * (D + 1);
+    const bool has_r = (2 * j + 1) < A.nreal_c;
+    v.sR = has_r ? v.sL + (D + 1) : nullptr;
+    v.eL = A.cends + q * A.ce_q + (size_t)(2 * j) * 2;
+    v.eR = has_r ? v.eL + 2 : nullptr;
+    v.ps = A.pspec ? A.pspec + q * A.ps_q + (size_t)j * (2 * D + 1) : nullptr;
+    v.pe = A.pends ? A.pends + q * A.pe_q + (size_t)j * 2 : nullptr;
+    v.po = A.Pout ? A.Pout + q * A.Po_q + (size_t)j * A.pst_p : nullptr;
+    v.pst = A.pst_p;
+    v.plen = A.plen_p;
+    const ZeroPrefix z{A.z.zp, q0, A.z.span};
+    v.cold = zp_cold(z, q, j) ? 1 : 0;
+}
+
+// the build of cnt items whose views are in V (shared memory, synchronised);
+// idx from partition_items: nh items to transform first, wholly-zero ones
+// after; want_spec: the items' parents keep spec2 (uniform over a launch)
+__device__ void spec_build_core(const SbView *V, const int *idx, int cnt, int nh, int logD,
+                                const double2 *__restrict__ tw, int logTW, double2 *sm, bool want_spec) {
     const int D = 1 << logD;
     const int hD = D >> 1;
-    const int cb = D >= 4096 ? 1 : 4096 / D;
-        const int j0 = bx * cb;
-    const int cnt = min(cb, nreal_p - j0);
-    if (cnt <= 0) return;
-    if (zp_cold(A.z, q, j0 + cnt - 1)) {   // every parent x^{2D}
+    if (nh < cnt) {   // wholly-zero parents x^{2D}: spec2 (-1)^f, ends (0, 1), coefficients a single 1
+        int maxpst = 0;
+        for (int r = nh; r < cnt; ++r) maxpst = max(maxpst, V[idx[r]].pst);
         const int nb2 = 2 * D + 1;
-        const int per = max(nb2, Pout ? pst_p : 0);
-        for (int e = threadIdx.x; e < cnt * per; e += blockDim.x) {
-            const int it = e / per, f = e - it * per;
-            const int j = j0 + it;
-            if (pspec && f < nb2) pspec[q * ps_q + (size_t)j * nb2 + f] = make_double2((f & 1) ? -1.0 : 1.0, 0.0);
-            if (pends && f == 0) {
-                double *en = pends + q * pe_q + (size_t)j * 2;
-                en[0] = 0.0;
-                en[1] = 1.0;
+        const int per = max(nb2, maxpst);
+        for (int e = threadIdx.x; e < (cnt - nh) * per; e += blockDim.x) {
+            const int r = nh + e / per, f = e % per;
+            const SbView &v = V[idx[r]];
+            if (v.ps && f < nb2) v.ps[f] = make_double2((f & 1) ? -1.0 : 1.0, 0.0);
+            if (v.pe && f == 0) {
+                v.pe[0] = 0.0;
+                v.pe[1] = 1.0;
             }
-            if (Pout && f < pst_p) Pout[q * Po_q + (size_t)j * pst_p + f] = (f == 2 * D && f < plen_p) ? 1.0 : 0.0;
+            if (v.po && f < v.pst) v.po[f] = (f == 2 * D && f < v.plen) ? 1.0 : 0.0;
         }
-        return;
     }
+    if (nh == 0) return;
     const double2 one = make_double2(1.0, 0.0);
     // 1. product spectrum (even bins of spec2(X)) and the inverse input, by mirror pairs
     const int np1 = hD + 1;
-    for (int e = threadIdx.x; e < cnt * np1; e += blockDim.x) {
+    for (int e = threadIdx.x; e < nh * np1; e += blockDim.x) {
         const int it = e / np1, f = e - it * np1;
-        const int j = j0 + it;
-        const double2 *sL = cspec + q * cs_q + (size_t)(2 * j) * (D + 1);
-        const bool has_r = (2 * j + 1) < nreal_c;
-        const double2 *sR = sL + (D + 1);
-        const double2 Cf = cmul(sL[f], has_r ? sR[f] : one);
-        const double2 Cc = cmul(sL[D - f], has_r ? sR[D - f] : one);
-        if (pspec) {
-            double2 *ps = pspec + q * ps_q + (size_t)j * (2 * D + 1);
-            ps[2 * f] = Cf;
-            ps[2 * (D - f)] = Cc;
+        const SbView &v = V[idx[it]];
+        const double2 Cf = cmul(v.sL[f], v.sR ? v.sR[f] : one);
+        const double2 Cc = cmul(v.sL[D - f], v.sR ? v.sR[D - f] : one);
+        if (v.ps) {
+            v.ps[2 * f] = Cf;
+            v.ps[2 * (D - f)] = Cc;
         }
         double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
@@ -186,54 +205,117 @@ __device__ void spec_build_body(const SpecBuildArgs &A, int bx, int q) {
         if (f != 0 && f != hD) u[bitrev(D - f, logD)] = cadd(cconj(E), cmul_pi(cconj(O)));
     }
     __syncthreads();
-    smem_fft_dit<+1>(sm, logD, cnt, tw, logTW);
+    smem_fft_dit<+1>(sm, logD, nh, tw, logTW);
     // 2. u_s = 2D (x_{2s} + i x_{2s+1}); coefficients where a coefficient level
-    //    sits above, the endpoint fix, and the (unscaled) twist
+    //    sits above (truncated at plen, zero padding to pst), the endpoint fix,
+    //    and the (unscaled) twist
     const double one_over_2D = 1.0 / (2.0 * D);
     auto coeffs = [&](int it, int s, double2 u) -> double2 {
-        const int j = j0 + it;
-        const double *eL = cends + q * ce_q + (size_t)(2 * j) * 2;
-        const bool has_r = (2 * j + 1) < nreal_c;
-        const double xtop = eL[1] * (has_r ? eL[3] : 0.0);
+        const SbView &v = V[idx[it]];
+        const double xtop = v.eL[1] * (v.eR ? v.eR[1] : 0.0);
         if (s == 0) {
-            const double x0 = eL[0] * (has_r ? eL[2] : 1.0);
-            if (pends) {
-                double *en = pends + q * pe_q + (size_t)j * 2;
-                en[0] = x0;
-                en[1] = xtop;
+            const double x0 = v.eL[0] * (v.eR ? v.eR[0] : 1.0);
+            if (v.pe) {
+                v.pe[0] = x0;
+                v.pe[1] = xtop;
             }
             u.x = (x0 - xtop) * (2.0 * D);   // y_0 = x_0 - x_{2D}, in the unscaled units of u
         }
-        if (Pout) {   // truncated at plen_p; the row's padding up to pst_p is zero
-            double *out = Pout + q * Po_q + (size_t)j * pst_p;
-            const double x0 = (s == 0) ? eL[0] * (has_r ? eL[2] : 1.0) : u.x * one_over_2D;
-            if (2 * s < pst_p) out[2 * s] = (2 * s < plen_p) ? x0 : 0.0;
-            if (2 * s + 1 < pst_p) out[2 * s + 1] = (2 * s + 1 < plen_p) ? u.y * one_over_2D : 0.0;
+        if (v.po) {
+            const int pst = v.pst, plen = v.plen;
+            const double x0 = (s == 0) ? v.eL[0] * (v.eR ? v.eR[0] : 1.0) : u.x * one_over_2D;
+            if (2 * s < pst) v.po[2 * s] = (2 * s < plen) ? x0 : 0.0;
+            if (2 * s + 1 < pst) v.po[2 * s + 1] = (2 * s + 1 < plen) ? u.y * one_over_2D : 0.0;
             if (s == 0) {
-                if (2 * D < pst_p) out[2 * D] = (2 * D < plen_p) ? xtop : 0.0;
-                for (int t = 2 * D + 1; t < pst_p; ++t) out[t] = 0.0;
+                if (2 * D < pst) v.po[2 * D] = (2 * D < plen) ? xtop : 0.0;
+                for (int t = 2 * D + 1; t < pst; ++t) v.po[t] = 0.0;
             }
         }
         return (s == 0) ? u : cmul(u, twl(tw, (long)s << (logTW - logD - 1)));   // e^{-2 pi i s/2D}
     };
-    if (!pspec) {   // the level above works on coefficients: no spectrum needed
-        for (int e = threadIdx.x; e < cnt * D; e += blockDim.x) coeffs(e >> logD, e & (D - 1), sm[e]);
+    if (!want_spec) {   // the level above works on coefficients: no spectrum needed
+        for (int e = threadIdx.x; e < nh * D; e += blockDim.x) coeffs(e >> logD, e & (D - 1), sm[e]);
         return;
     }
-    smem_bitrev_map(sm, logD, cnt, coeffs);
-    smem_fft_dit<-1>(sm, logD, cnt, tw, logTW);
+    smem_bitrev_map(sm, logD, nh, coeffs);
+    smem_fft_dit<-1>(sm, logD, nh, tw, logTW);
     // 3. odd bins by mirror pairs (f, D-1-f), f < D/2
     const double kb = 1.0 / (4.0 * D);
-    for (int e = threadIdx.x; e < cnt * hD; e += blockDim.x) {
+    for (int e = threadIdx.x; e < nh * hD; e += blockDim.x) {
         const int it = e / hD, f = e - it * hD;
         const double2 *c = sm + (size_t)it * D;
         const double2 a = c[f], b = cconj(c[D - 1 - f]);
         const double2 Ep = cadd(a, b);
         const double2 T = cmul(cmul_mi(csub(a, b)), twl(tw, (long)(2 * f + 1) << (logTW - logD - 2)));
-        double2 *ps = pspec + q * ps_q + (size_t)(j0 + it) * (2 * D + 1);
+        double2 *ps = V[idx[it]].ps;
         ps[2 * f + 1] = cscale(cadd(Ep, T), kb);
         ps[2 * (D - 1 - f) + 1] = cscale(cconj(csub(Ep, T)), kb);
     }
+}
+
+template <class View>
+__device__ __forceinline__ View *item_views(double2 *sm, int cb, int M) {
+    return reinterpret_cast<View *>(sm + (size_t)cb * M);
+}
+template <class View>
+__device__ __forceinline__ int *item_index(View *V, int cb) {
+    return reinterpret_cast<int *>(V + cb);
+}
+// idx[0, nhot) = items to transform, idx[nhot, cnt) = wholly-zero items, in
+// order; a CTA may hold items of different tournaments, so pruning is per
+// item (one thread partitions at most a few hundred flags)
+__device__ __forceinline__ bool item_skip(const SbView &v) { return v.cold; }
+template <class View>
+__device__ __forceinline__ int partition_items(const View *V, int *idx, int cnt) {
+    __shared__ int nhot_s;
+    if (threadIdx.x == 0) {
+        int h = 0;
+        for (int it = 0; it < cnt; ++it)
+            if (!item_skip(V[it])) idx[h++] = it;
+        int c = h;
+        for (int it = 0; it < cnt; ++it)
+            if (item_skip(V[it])) idx[c++] = it;
+        nhot_s = h;
+    }
+    __syncthreads();
+    return nhot_s;
+}
+
+__device__ void spec_build_body(const SpecBuildArgs &A, int bx, int q) {
+    extern __shared__ double2 sm[];
+    const int D = 1 << A.logD;
+    const int cb = D >= 4096 ? 1 : 4096 / D;
+    const int j0 = bx * cb;
+    const int cnt = min(cb, A.nreal_p - j0);
+    if (cnt <= 0) return;
+    SbView *V = item_views<SbView>(sm, cb, D);
+    int *idx = item_index(V, cb);
+    for (int it = threadIdx.x; it < cnt; it += blockDim.x) sb_fill(A, q, A.z.q0, j0 + it, D, V[it]);
+    __syncthreads();
+    const int nh = partition_items(V, idx, cnt);
+    spec_build_core(V, idx, cnt, nh, A.logD, A.tw, A.logTW, sm, A.pspec != nullptr);
+}
+
+// packed: slots[s] = (descriptor, parent); all descriptors of a launch share
+// the transform size and whether parents keep spec2
+__device__ void spec_build_packed(const SpecBuildArgs *__restrict__ Dsc, const int2 *__restrict__ slots, int nslots,
+                                  int bx, int q, int q0) {
+    extern __shared__ double2 sm[];
+    const SpecBuildArgs &A0 = Dsc[slots[0].x];
+    const int D = 1 << A0.logD;
+    const int cb = D >= 4096 ? 1 : 4096 / D;
+    const int s0 = bx * cb;
+    const int cnt = min(cb, nslots - s0);
+    if (cnt <= 0) return;
+    SbView *V = item_views<SbView>(sm, cb, D);
+    int *idx = item_index(V, cb);
+    for (int it = threadIdx.x; it < cnt; it += blockDim.x) {
+        const int2 sl = slots[s0 + it];
+        sb_fill(Dsc[sl.x], q, q0, sl.y, D, V[it]);
+    }
+    __syncthreads();
+    const int nh = partition_items(V, idx, cnt);
+    spec_build_core(V, idx, cnt, nh, A0.logD, A0.tw, A0.logTW, sm, A0.pspec != nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -301,50 +383,62 @@ __device__ void gspec_body(const GspecArgs &A, int bx, int q) {
 //   X(f) = E + T,  X(h-f) = conj(E - T),  E = z_f + conj z_{h-f},
 //   T = -i (z_f - conj z_{h-f}) e^{-2 pi i f/D},
 //   G_child[f] = Y[2f]/2 + X(f)/8h   (all scalings folded into the last step).
-__device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
-    const auto Gp = A.Gp;
-    const auto Gp_q = A.Gp_q;
-    const auto cspec = A.cspec;
-    const auto cs_q = A.cs_q;
-    const auto nreal_c = A.nreal_c;
-    const auto npar = A.npar;
-    const auto logD = A.logD;
-    const auto Gout = A.Gout;
-    const auto Go_q = A.Go_q;
-    const auto gout = A.gout;
-    const auto go_q = A.go_q;
-    const auto gst_c = A.gst_c;
-    const auto glen_c = A.glen_c;
-    const auto hot_c = A.hot_c;
-    const auto tw = A.tw;
-    const auto logTW = A.logTW;
+struct SpView;
+__device__ __forceinline__ bool item_skip(const SpView &v);
+struct SpView {
+    const double2 *G;      // parent's g spectrum (D+1 bins)
+    const double2 *S[2];   // children's spec2 (null: no such child, as a sibling the polynomial 1)
+    double2 *Gout[2];      // children's g spectra (h+1 bins), or null
+    double *gout[2];       // children's g coefficients, or null
+    int gst, glen;
+    int live[2];           // the child exists
+    int zero[2];           // subset-cold child: its outputs are zero
+    int cold;              // wholly-zero parent: the item is skipped
+};
+static_assert(sizeof(SpView) <= kViewBytes, "view size");
+__device__ __forceinline__ bool item_skip(const SpView &v) {
+    return v.cold || !((v.live[0] && !v.zero[0]) || (v.live[1] && !v.zero[1]));
+}
 
-    extern __shared__ double2 sm[];
+__device__ __forceinline__ void sp_fill(const SpecPropArgs &A, int q, int q0, int j, int D, SpView &v) {
+    const int h = D >> 1;
+    v.G = A.Gp + q * A.Gp_q + (size_t)j * (D + 1);
+    for (int side = 0; side < 2; ++side) {
+        const int c = 2 * j + side;
+        const bool live = c < A.nreal_c;
+        v.live[side] = live ? 1 : 0;
+        v.S[side] = live ? A.cspec + q * A.cs_q + (size_t)c * (D + 1) : nullptr;
+        v.Gout[side] = (A.Gout && live) ? A.Gout + q * A.Go_q + (size_t)c * (h + 1) : nullptr;
+        v.gout[side] = (A.gout && live) ? A.gout + q * A.go_q + (size_t)c * A.gst_c : nullptr;
+        v.zero[side] = (live && A.hot_c && !A.hot_c[c]) ? 1 : 0;
+    }
+    v.gst = A.gst_c;
+    v.glen = A.glen_c;
+    const ZeroPrefix z{A.z.zp, q0, A.z.span};
+    v.cold = zp_cold(z, q, j) ? 1 : 0;
+}
+
+// the propagate of the nh parents idx[0, nh) (2 nh children) whose views are
+// in V (the others skipped: nothing below a wholly-zero parent or a pair of
+// subset-cold children is read); want_G: children get g spectra (else
+// coefficients), uniform over a launch
+__device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int logD, const double2 *__restrict__ tw,
+                               int logTW, double2 *sm, bool want_G) {
     const int D = 1 << logD;
     const int h = D >> 1, lh = logD - 1;
-    const int cbp = D >= 4096 ? 1 : 4096 / D;            // parents per CTA; 2 children each
-        const int j0 = bx * cbp;
-    const int cnt = min(cbp, npar - j0);
-    if (cnt <= 0 || zp_cold(A.z, q, j0 + cnt - 1)) return;   // wholly-zero parents: no child g is read
-    const int nk = 2 * cnt;                               // children handled, h slots each
+    const int nk = 2 * nh;   // children handled, h slots each
+    if (nh == 0) return;
     const double2 one = make_double2(1.0, 0.0);
-    if (hot_c) {   // subset pruning: nothing below a cold child is ever read
-        bool any = false;
-        for (int c = 2 * j0; c < 2 * (j0 + cnt) && c < nreal_c; ++c) any = any || hot_c[c];
-        if (!any) return;
-    }
     // 1. odd bins of Y -> inverse half-bin input, by mirror pairs
-    const int hp = (h + 1) >> 1;                          // pairs per child (h = 1: one self pair)
+    const int hp = (h + 1) >> 1;   // pairs per child (h = 1: one self pair)
     for (int e = threadIdx.x; e < nk * hp; e += blockDim.x) {
         const int kk = e / hp, f = e - kk * hp;
         const int fp = h - 1 - f;
-        const int j = j0 + (kk >> 1), side = kk & 1;
-        const int sib = (2 * j + side) ^ 1;
-        const double2 *G = Gp + q * Gp_q + (size_t)j * (D + 1);
-        const bool has_sib = sib < nreal_c;
-        const double2 *S = cspec + q * cs_q + (size_t)sib * (D + 1);
-        const double2 Y1 = cmulc(G[2 * f + 1], has_sib ? S[2 * f + 1] : one);
-        const double2 Y2 = cconj(cmulc(G[2 * fp + 1], has_sib ? S[2 * fp + 1] : one));
+        const SpView &v = V[idx[kk >> 1]];
+        const double2 *S = v.S[(kk & 1) ^ 1];   // the sibling's spectrum
+        const double2 *G = v.G;
+        const double2 Y1 = cmulc(G[2 * f + 1], S ? S[2 * f + 1] : one);
+        const double2 Y2 = cconj(cmulc(G[2 * fp + 1], S ? S[2 * fp + 1] : one));
         const double2 A = cadd(Y1, Y2);
         const double2 B = cmulc(csub(Y1, Y2), twl(tw, (long)(2 * f + 1) << (logTW - logD - 1)));
         double2 *x = sm + (size_t)kk * h;
@@ -357,7 +451,7 @@ __device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
     auto untwist = [&](int, int s, double2 v) -> double2 {
         return (s == 0) ? v : cmulc(v, twl(tw, (long)s << (logTW - logD)));
     };
-    if (Gout) {
+    if (want_G) {
         smem_bitrev_map(sm, lh, nk, untwist);
         smem_fft_dit<-1>(sm, lh, nk, tw, logTW);
         // 3a. child spectra by mirror pairs (f, h-f), f <= h/2
@@ -366,28 +460,27 @@ __device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
         for (int e = threadIdx.x; e < nk * hq; e += blockDim.x) {
             const int kk = e / hq, f = e - kk * hq;
             const int fp = h - f;
-            const int j = j0 + (kk >> 1), side = kk & 1;
-            const int c = 2 * j + side, sib = c ^ 1;
-            if (c >= nreal_c) continue;   // lone child: no right sibling node
-            double2 *out = Gout + q * Go_q + (size_t)c * (h + 1);
-            if (hot_c && !hot_c[c]) {
+            const SpView &v = V[idx[kk >> 1]];
+            const int side = kk & 1;
+            if (!v.live[side]) continue;   // lone child: no right sibling node
+            double2 *out = v.Gout[side];
+            if (v.zero[side]) {
                 out[f] = make_double2(0.0, 0.0);
                 out[fp] = make_double2(0.0, 0.0);
                 continue;
             }
-            const double2 *G = Gp + q * Gp_q + (size_t)j * (D + 1);
-            const bool has_sib = sib < nreal_c;
-            const double2 *S = cspec + q * cs_q + (size_t)sib * (D + 1);
+            const double2 *G = v.G;
+            const double2 *S = v.S[side ^ 1];
             const double2 *z = sm + (size_t)kk * h;
             const double2 zf = z[f & (h - 1)], zc = cconj(z[fp & (h - 1)]);
             const double2 E = cadd(zf, zc);
             const double2 T = (f == 0) ? cmul_mi(csub(zf, zc))
                                        : cmul(cmul_mi(csub(zf, zc)), twl(tw, (long)f << (logTW - logD)));
-            const double2 Yf = cmulc(G[2 * f], has_sib ? S[2 * f] : one);
+            const double2 Yf = cmulc(G[2 * f], S ? S[2 * f] : one);
             const double2 Xf = cadd(E, T);
             out[f] = make_double2(fma(kx, Xf.x, 0.5 * Yf.x), fma(kx, Xf.y, 0.5 * Yf.y));
             if (fp != f) {
-                const double2 Yc = cmulc(G[2 * fp], has_sib ? S[2 * fp] : one);
+                const double2 Yc = cmulc(G[2 * fp], S ? S[2 * fp] : one);
                 const double2 Xc = cconj(csub(E, T));
                 out[fp] = make_double2(fma(kx, Xc.x, 0.5 * Yc.x), fma(kx, Xc.y, 0.5 * Yc.y));
             }
@@ -399,27 +492,26 @@ __device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
     const double ka = 1.0 / (4.0 * h);
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
         const int kk = e >> lh, s = e & (h - 1);
-        const int c = 2 * (j0 + (kk >> 1)) + (kk & 1);
-        if (c >= nreal_c) continue;
-        double *out = gout + q * go_q + (size_t)c * gst_c;
-        const double2 v = untwist(kk, s, sm[e]);
-        if (2 * s < glen_c) out[2 * s] = ka * v.x;
-        if (2 * s + 1 < glen_c) out[2 * s + 1] = ka * v.y;
+        const SpView &v = V[idx[kk >> 1]];
+        const int side = kk & 1;
+        if (!v.live[side]) continue;
+        double *out = v.gout[side];
+        const double2 w = untwist(kk, s, sm[e]);
+        if (2 * s < v.glen) out[2 * s] = ka * w.x;
+        if (2 * s + 1 < v.glen) out[2 * s + 1] = ka * w.y;
     }
     __syncthreads();
     // U[f] = E + i O of the even-bin spectrum Ye (bins 0..h of a real size-D spectrum)
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
         const int kk = e >> lh, f = e & (h - 1);
-        const int j = j0 + (kk >> 1), side = kk & 1;
-        const int sib = (2 * j + side) ^ 1;
-        const double2 *G = Gp + q * Gp_q + (size_t)j * (D + 1);
-        const bool has_sib = sib < nreal_c;
-        const double2 *S = cspec + q * cs_q + (size_t)sib * (D + 1);
-        const double2 Cf = cmulc(G[2 * f], has_sib ? S[2 * f] : one);
-        const double2 Cc = cmulc(G[2 * (h - f)], has_sib ? S[2 * (h - f)] : one);
+        const SpView &v = V[idx[kk >> 1]];
+        const double2 *S = v.S[(kk & 1) ^ 1];
+        const double2 *G = v.G;
+        const double2 Cf = cmulc(G[2 * f], S ? S[2 * f] : one);
+        const double2 Cc = cmulc(G[2 * (h - f)], S ? S[2 * (h - f)] : one);
         double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
-        const double2 O = cmulc(Dd, twl(tw, (long)f << (logTW - logD)));      // e^{+2 pi i f/D}
+        const double2 O = cmulc(Dd, twl(tw, (long)f << (logTW - logD)));   // e^{+2 pi i f/D}
         sm[(size_t)kk * h + bitrev(f, lh)] = cadd(E, cmul_pi(O));
     }
     __syncthreads();
@@ -427,14 +519,53 @@ __device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
     const double inv_D = 1.0 / D;
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
         const int kk = e >> lh, s = e & (h - 1);
-        const int c = 2 * (j0 + (kk >> 1)) + (kk & 1);
-        if (c >= nreal_c) continue;
-        double *out = gout + q * go_q + (size_t)c * gst_c;
-        const bool cold = hot_c && !hot_c[c];
-        const double2 v = sm[e];
-        if (2 * s < gst_c) out[2 * s] = (cold || 2 * s >= glen_c) ? 0.0 : out[2 * s] + 0.5 * v.x * inv_D;
-        if (2 * s + 1 < gst_c) out[2 * s + 1] = (cold || 2 * s + 1 >= glen_c) ? 0.0 : out[2 * s + 1] + 0.5 * v.y * inv_D;
+        const SpView &v = V[idx[kk >> 1]];
+        const int side = kk & 1;
+        if (!v.live[side]) continue;
+        double *out = v.gout[side];
+        const bool zr = v.zero[side];
+        const int gst = v.gst, glen = v.glen;
+        const double2 w = sm[e];
+        if (2 * s < gst) out[2 * s] = (zr || 2 * s >= glen) ? 0.0 : out[2 * s] + 0.5 * w.x * inv_D;
+        if (2 * s + 1 < gst) out[2 * s + 1] = (zr || 2 * s + 1 >= glen) ? 0.0 : out[2 * s + 1] + 0.5 * w.y * inv_D;
     }
+}
+
+__device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
+    extern __shared__ double2 sm[];
+    const int D = 1 << A.logD;
+    const int cbp = D >= 4096 ? 1 : 4096 / D;   // parents per CTA; 2 children each
+    const int j0 = bx * cbp;
+    const int cnt = min(cbp, A.npar - j0);
+    if (cnt <= 0) return;
+    SpView *V = item_views<SpView>(sm, cbp, D);
+    int *idx = item_index(V, cbp);
+    for (int it = threadIdx.x; it < cnt; it += blockDim.x) sp_fill(A, q, A.z.q0, j0 + it, D, V[it]);
+    __syncthreads();
+    const int nh = partition_items(V, idx, cnt);
+    spec_prop_core(V, idx, nh, A.logD, A.tw, A.logTW, sm, A.Gout != nullptr);
+}
+
+// packed: slots[s] = (descriptor, parent); all descriptors of a launch share
+// the transform size and whether children get g spectra
+__device__ void spec_prop_packed(const SpecPropArgs *__restrict__ Dsc, const int2 *__restrict__ slots, int nslots,
+                                 int bx, int q, int q0) {
+    extern __shared__ double2 sm[];
+    const SpecPropArgs &A0 = Dsc[slots[0].x];
+    const int D = 1 << A0.logD;
+    const int cbp = D >= 4096 ? 1 : 4096 / D;
+    const int s0 = bx * cbp;
+    const int cnt = min(cbp, nslots - s0);
+    if (cnt <= 0) return;
+    SpView *V = item_views<SpView>(sm, cbp, D);
+    int *idx = item_index(V, cbp);
+    for (int it = threadIdx.x; it < cnt; it += blockDim.x) {
+        const int2 sl = slots[s0 + it];
+        sp_fill(Dsc[sl.x], q, q0, sl.y, D, V[it]);
+    }
+    __syncthreads();
+    const int nh = partition_items(V, idx, cnt);
+    spec_prop_core(V, idx, nh, A0.logD, A0.tw, A0.logTW, sm, A0.Gout != nullptr);
 }
 
 __global__ void __launch_bounds__(kSpecThreads) k_spec_init(SpecInitArgs A) { spec_init_body(A, blockIdx.x, blockIdx.y); }
@@ -447,11 +578,11 @@ void spec_wl_set_smem_limits();
 
 // ---------------------------------------------------------------------------
 void spec_set_smem_limits() {
-    const int mx = (int)spec_smem(kSpecMaxM);
+    const int mx = (int)spec_smem(kSpecMaxM), mv = (int)spec_smem_v_max();
     cudaFuncSetAttribute(k_spec_init, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_spec_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_spec_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
     cudaFuncSetAttribute(k_gspec_init, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
     spec_wl_set_smem_limits();
 }
 
@@ -469,7 +600,7 @@ SpecBuildArgs spec_build_args(const Level &c, const Level &p, bool write_coeffs,
     const int logD = ilog2s(c.deg), D = 1 << logD;
     const int cb = spec_cb(D);
     if (fq) *fq = (10.0 * D * logD + 60.0 * D) * p.nreal;
-    if (smem) *smem = spec_smem(D);
+    if (smem) *smem = spec_smem_v(D);
     return SpecBuildArgs{c.spec2, c.spec2_q, c.ends, c.ends_q, c.nreal, p.nreal, logD, p.spec2, p.spec2_q,
                          p.spec2 ? p.ends : nullptr, p.ends_q, write_coeffs ? p.P : nullptr, p.P_q, p.pst, p.plen, tw,
                          logTW, (p.nreal + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}};
@@ -490,7 +621,7 @@ SpecPropArgs spec_prop_args(const double2 *Gp, size_t Gp_q, const Level &c, cons
     const int logD = ilog2s(c.deg), D = 1 << logD;
     const int cbp = spec_cb(D);
     if (fq) *fq = (2.0 * 2 * 5.0 * (D / 2) * (logD - 1) + 60.0 * D) * p.nreal;
-    if (smem) *smem = spec_smem(D);
+    if (smem) *smem = spec_smem_v(D);
     return SpecPropArgs{Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, p.nreal, logD, children_spectral ? c.G : nullptr,
                         c.G_q, c.g, c.g_q, c.gst, c.glen, hot_c, tw, logTW, (p.nreal + cbp - 1) / cbp,
                         ZeroPrefix{nullptr, 0, p.deg}};
@@ -569,6 +700,14 @@ kw_gspec(const GspecArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) 
     gspec_body(A, t.y, blockIdx.y);
 }
 __global__ void __launch_bounds__(kSpecThreads)
+kw_spec_build_packed(const SpecBuildArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
+    spec_build_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
+}
+__global__ void __launch_bounds__(kSpecThreads)
+kw_spec_prop_packed(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
+    spec_prop_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
+}
+__global__ void __launch_bounds__(kSpecThreads)
 kw_spec_prop(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
     SpecPropArgs A = D[t.x];
@@ -577,11 +716,24 @@ kw_spec_prop(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ tab, i
 }
 
 void spec_wl_set_smem_limits() {
-    const int mx = (int)spec_smem(kSpecMaxM);
+    const int mx = (int)spec_smem(kSpecMaxM), mv = (int)spec_smem_v_max();
     cudaFuncSetAttribute(kw_spec_init, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(kw_spec_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_spec_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
     cudaFuncSetAttribute(kw_gspec, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(kw_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
+    cudaFuncSetAttribute(kw_spec_build_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
+    cudaFuncSetAttribute(kw_spec_prop_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
+}
+
+// packed launch: nslots items, cb items per CTA
+void launch_packed_spec(WOp op, const void *desc, const int2 *slots, int nslots, int cb, int nq, int q0, size_t smem,
+                        cudaStream_t st) {
+    if (nslots <= 0 || nq <= 0) return;
+    const dim3 g((nslots + cb - 1) / cb, nq);
+    if (op == WOp::SpecBuild)
+        kw_spec_build_packed<<<g, kSpecThreads, smem, st>>>((const SpecBuildArgs *)desc, slots, nslots, q0);
+    else
+        kw_spec_prop_packed<<<g, kSpecThreads, smem, st>>>((const SpecPropArgs *)desc, slots, nslots, q0);
 }
 
 void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
