@@ -180,7 +180,10 @@ static void build_steps(Forest *f) {
                     if (lv[l].npairs > 0) {
                         FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], false, tw, logTW, &fq, &sm);
                         A.z.zp = zpre(p);
-                        b.add(WOp::FusedBuild, A.logN, "wl_fused_build", A, sm, fq, 0, t, lv[l].deg, lv[l].nreal);
+                        b.pack_items = lv[l].npairs;
+                        b.pack_cb = A.logN >= 13 ? 1 : 4096 >> A.logN;
+                        b.add(WOp::FusedBuild, 2 * A.logN, "wl_fused_build", A, sm, fq, 0, t, lv[l].deg, lv[l].nreal);
+                        b.pack_items = 0;
                     }
                     if (lv[l - 1].nreal & 1) {
                         SchoolBuildArgs A = school_build_args(lv[l - 1], lv[l], lv[l].npairs, &fq);
@@ -195,7 +198,10 @@ static void build_steps(Forest *f) {
             } else if (l == p->L - 1 && lv[l].fft && lv[l].npairs > 0) {
                 // the root: child spectra for its propagate only
                 FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], true, tw, logTW, &fq, &sm);
-                b.add(WOp::FusedBuild, A.logN, "wl_fused_spectra", A, sm, fq);
+                b.pack_items = lv[l].npairs;
+                b.pack_cb = A.logN >= 13 ? 1 : 4096 >> A.logN;
+                b.add(WOp::FusedBuild, 2 * A.logN + 1, "wl_fused_spectra", A, sm, fq);
+                b.pack_items = 0;
             }
         }
         PhaseBuilder &c = phase();
@@ -258,7 +264,10 @@ static void build_steps(Forest *f) {
                     FusedPropArgs A = fused_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nullptr, tw, logTW, &fq,
                                                       &sm);
                     A.z.zp = zpre(p);
+                    b.pack_items = lv[l].npairs;
+                    b.pack_cb = A.logN >= 13 ? 1 : 4096 >> A.logN;
                     b.add(WOp::FusedProp, A.logN, "wl_fused_prop", A, sm, fq, 0, t, root ? 0 : lv[l].deg, lv[l].nreal);
+                    b.pack_items = 0;
                 }
                 if (lv[l - 1].nreal & 1) {
                     SchoolPropArgs A = school_prop_args(gp, gp_q, gst_p, gpl, lv[l - 1], nullptr, 2 * lv[l].npairs, &fq);
@@ -360,7 +369,10 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
     const int qn = s.one ? 1 : nq;
     if (f->prof.on) f->prof.begin(s.name, step_flops(f, s, qn, q0), f->stream);
     if (s.packed) {
-        launch_packed_spec(s.op, s.d_desc, s.d_tab, nctas, s.cb, qn, q0, s.smem, f->stream);
+        if (s.op == WOp::FusedBuild || s.op == WOp::FusedProp)
+            launch_packed_fused(s.op, s.d_desc, s.d_tab, nctas, s.cb, qn, q0, s.smem, f->stream);
+        else
+            launch_packed_spec(s.op, s.d_desc, s.d_tab, nctas, s.cb, qn, q0, s.smem, f->stream);
         f->prof.end(f->stream);
         ++f->launches;
         return;

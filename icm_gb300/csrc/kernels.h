@@ -241,6 +241,8 @@ void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas,
 // slots, which may belong to different tournaments (SpecBuild, SpecProp)
 void launch_packed_spec(WOp op, const void *desc, const int2 *slots, int nslots, int cb, int nq, int q0, size_t smem,
                         cudaStream_t st);
+void launch_packed_fused(WOp op, const void *desc, const int2 *slots, int nslots, int cb, int nq, int q0, size_t smem,
+                         cudaStream_t st);
 size_t spec_smem_bytes(int M);     // dynamic shared memory of the spectral kernels
 size_t fused_smem_bytes(int N);    // dynamic shared memory of the fused kernels
 
