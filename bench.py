@@ -468,8 +468,23 @@ def vjp_leg(icm, W, steps):
     t0 = time.perf_counter()
     icm.equity_batched(ts)
     tf = time.perf_counter() - t0
+    # resident batches: device time of one graph replay each
+    stacks, ks, pays = [S for S, _ in ts], [len(P) for _, P in ts], [P for _, P in ts]
+    fb, vb = icm.GpuBatch(stacks, ks), icm.GpuVjpBatch(stacks, ks)
+    fdev, vdev = [], []
+    for i in range(max(2, steps) + 2):
+        fb.equity(pays)
+        vb.vjp(pays, cots)
+        if i >= 2:
+            fdev.append(fb.info()["device_ms"])
+            vdev.append(vb.info()["device_ms"])
+    fb.close()
+    vb.close()
     out["batched_256"] = {"vjp_ms": tv * 1e3, "fwd_ms": tf * 1e3, "ratio": tv / tf,
-                          "config": "256 tournaments, n uniform [100,4000], k=ceil(0.15n), payout 0.8^j, wall time"}
+                          "vjp_device_ms": float(np.median(vdev)), "fwd_device_ms": float(np.median(fdev)),
+                          "device_ratio": float(np.median(vdev) / np.median(fdev)),
+                          "config": "256 tournaments, n uniform [100,4000], k=ceil(0.15n), payout 0.8^j; one-shot "
+                                    "wall time, and device time of resident batches (graph replay)"}
     return out
 
 

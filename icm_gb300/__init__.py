@@ -27,7 +27,7 @@ from ._lib import (IcmGb300Config, IcmGpuOptions, IcmGpuPlanSummary, IcmGpuRunSt
                    library_path)
 
 __all__ = ["init", "equity", "equity_subset", "ICMError", "gpu_equity", "gpu_equity_subset", "GpuPlan",
-           "equity_batched", "GpuBatch", "equity_vjp", "equity_vjp_batched", "VjpPlan", "autotune", "tuner_load",
+           "equity_batched", "GpuBatch", "GpuVjpBatch", "equity_vjp", "equity_vjp_batched", "VjpPlan", "autotune", "tuner_load",
            "tuner_save", "tuner_clear", "tuner_lookup", "equity_adaptive", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
            "last_launch_count"]
 
@@ -230,6 +230,8 @@ class GpuBatch:
     work lists are built once from the stacks; ``equity(payouts)`` uploads the
     payouts and replays the captured CUDA graph of the launch sequence."""
 
+    _create = "icm_gb300_batch_create"
+
     def __init__(self, stacks_list, ks):
         Ss = [_to_double_array(s, "stacks") for s in stacks_list]
         self.ns = np.array([len(s) for s in Ss], dtype=np.int32)
@@ -240,22 +242,26 @@ class GpuBatch:
             _check(int(n), int(k), 1)
         _auto_init()
         S = np.ascontiguousarray(np.concatenate(Ss))
-        self._h = lib().icm_gb300_batch_create(len(Ss), self.ns.ctypes.data_as(_ip), self.ks.ctypes.data_as(_ip),
+        self._h = getattr(lib(), self._create)(len(Ss), self.ns.ctypes.data_as(_ip), self.ks.ctypes.data_as(_ip),
                                                _d(S))
         if not self._h:
             raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
         self._splits = np.cumsum(self.ns)[:-1]
 
+    def _concat(self, xs, what, size):
+        if isinstance(xs, (list, tuple)):
+            X = np.ascontiguousarray(np.concatenate([_to_double_array(x, what) for x in xs]))
+        else:
+            X = _to_double_array(xs, what)
+        if X.size != size:
+            raise ValueError(f"{what}: expected {size} values, got {X.size}")
+        return X
+
     def equity(self, payouts, Q=256, return_stats=False, split=True):
         """``payouts``: list of arrays (one per tournament) or their
         concatenation.  Returns the list of equity arrays (or the
         concatenation with ``split=False``)."""
-        if isinstance(payouts, (list, tuple)):
-            P = np.ascontiguousarray(np.concatenate([_to_double_array(p, "payouts") for p in payouts]))
-        else:
-            P = _to_double_array(payouts, "payouts")
-        if P.size != int(self.ks.sum()):
-            raise ValueError(f"payouts: expected {int(self.ks.sum())} values, got {P.size}")
+        P = self._concat(payouts, "payouts", int(self.ks.sum()))
         if Q < 1:
             raise ValueError(f"Q must be >= 1, got Q={Q}")
         out = np.zeros(int(self.ns.sum()))
@@ -298,6 +304,31 @@ class GpuBatch:
             self.close()
         except Exception:
             pass
+
+
+class GpuVjpBatch(GpuBatch):
+    """Reusable batched VJP: the forward and adjoint passes of every
+    tournament as work-list launches, replayed as one CUDA graph.
+    ``vjp(payouts, cotangents)`` returns (grad_stacks, grad_payouts) lists
+    (or the concatenations with ``split=False``)."""
+
+    _create = "icm_gb300_vjp_batch_create"
+
+    def equity(self, *a, **kw):
+        raise ICMError("a VJP batch computes gradients: use vjp()")
+
+    def vjp(self, payouts, cotangents, Q=256, node_terms=False, return_stats=False, split=True):
+        P = self._concat(payouts, "payouts", int(self.ks.sum()))
+        C = self._concat(cotangents, "cotangent", int(self.ns.sum()))
+        if Q < 1:
+            raise ValueError(f"Q must be >= 1, got Q={Q}")
+        gS, gP = np.zeros(C.size), np.zeros(P.size)
+        st = IcmGpuRunStats()
+        if lib().icm_gb300_vjp_batch_run(self._h, int(Q), _d(P), _d(C), _d(gS), _d(gP), int(bool(node_terms)),
+                                         ctypes.byref(st)) != 0:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+        res = (list(zip(np.split(gS, self._splits), np.split(gP, np.cumsum(self.ks)[:-1]))) if split else (gS, gP))
+        return (res, _stats_dict(st)) if return_stats else res
 
 
 def equity_vjp(stacks, payouts, cotangent, Q=256, node_terms=False):

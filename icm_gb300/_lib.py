@@ -99,6 +99,9 @@ SIGNATURES = {
     "icm_gb300_equity_adaptive": (ctypes.c_int, [ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                  ctypes.c_int, _dp, _ip, _dp]),
     "icm_gb300_batch_create": (_vp, [ctypes.c_int, _ip, _ip, _dp]),
+    "icm_gb300_vjp_batch_create": (_vp, [ctypes.c_int, _ip, _ip, _dp]),
+    "icm_gb300_vjp_batch_run": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                               ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gb300_batch_run": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gb300_batch_destroy": (None, [_vp]),
     "icm_gb300_batch_set_options": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),

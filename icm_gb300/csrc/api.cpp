@@ -420,38 +420,34 @@ int icm_gb300_equity_vjp_batched(int T, const int *n, const int *k, const double
         po[t + 1] = po[t] + k[t];
     }
     if (!ensure_device()) return -1;
-    // waves of members, each on its own plan and stream: every member of a
-    // wave is enqueued before any is awaited, so small members overlap
-    const int W = 64;
-    long launches = 0;
     std::string err;
-    for (int w0 = 0; w0 < T; w0 += W) {
-        const int w1 = std::min(T, w0 + W);
-        size_t free_b = 0, total_b = 0;
-        cudaMemGetInfo(&free_b, &total_b);
-        const size_t budget = std::max<size_t>((size_t)64 << 20, (size_t)(free_b * 0.5) / (size_t)(w1 - w0));
-        std::vector<VjpPlan *> plans;
-        int rc = 0;
-        for (int t = w0; t < w1 && rc == 0; ++t) {
-            VjpPlan *v = vjp_plan_create(n[t], S + so[t], k[t], err, budget);
-            if (!v) { rc = -1; break; }
-            plans.push_back(v);
-            rc = vjp_plan_enqueue(v, Q, payout + po[t], cot + so[t], flags, err);
-        }
-        for (size_t i = 0; i < plans.size(); ++i) {
-            const int t = w0 + (int)i;
-            if (rc == 0 && plans[i]->pending) {
-                rc = vjp_plan_finish(plans[i], grad_S + so[t], grad_payout + po[t], nullptr, err);
-                launches += plans[i]->p->launches;
-            }
-        }
-        for (VjpPlan *v : plans) {
-            if (v->pending) cudaStreamSynchronize(v->p->stream);
-            vjp_plan_destroy(v);
-        }
-        if (rc != 0) { set_error("icm_gb300_equity_vjp_batched: " + err); return -1; }
-    }
-    t_launches = launches;
+    Forest *f = forest_create(T, n, k, S, err, /*vjp=*/true);
+    if (!f) { set_error("icm_gb300_equity_vjp_batched: " + err); return -1; }
+    f->graphs = false;   // one run: capturing would not pay
+    const int rc = forest_vjp_run(f, Q, payout, cot, flags, grad_S, grad_payout, nullptr, err);
+    t_launches = f->launches;
+    forest_destroy(f);
+    if (rc != 0) { set_error("icm_gb300_equity_vjp_batched: " + err); return -1; }
+    return 0;
+}
+
+IcmGb300Batch *icm_gb300_vjp_batch_create(int T, const int *n, const int *k, const double *S) {
+    if (!ensure_device()) return nullptr;
+    std::string err;
+    Forest *f = forest_create(T, n, k, S, err, /*vjp=*/true);
+    if (!f) { set_error("icm_gb300_vjp_batch_create: " + err); return nullptr; }
+    return reinterpret_cast<IcmGb300Batch *>(f);
+}
+
+int icm_gb300_vjp_batch_run(IcmGb300Batch *b, int Q, const double *payout, const double *cot, double *grad_S,
+                            double *grad_payout, int flags, IcmGpuRunStats *stats) {
+    if (!b) { set_error("icm_gb300_vjp_batch_run: null batch"); return -1; }
+    if (!ensure_device()) return -1;
+    Forest *f = reinterpret_cast<Forest *>(b);
+    std::string err;
+    const int rc = forest_vjp_run(f, Q, payout, cot, flags, grad_S, grad_payout, stats, err);
+    t_launches = f->launches;
+    if (rc != 0) { set_error("icm_gb300_vjp_batch_run: " + err); return -1; }
     return 0;
 }
 

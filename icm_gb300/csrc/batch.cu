@@ -281,7 +281,50 @@ static void build_steps(Forest *f) {
             }
         }
     }
-    {   // per-player divide
+    if (f->vjp) {   // adjoint passes: leaf blocks, up the tree, down the tree, players
+        const size_t pq = (size_t)f->qc * f->Ntot;
+        double *pA = f->node_terms ? f->d_part : nullptr, *pB = f->node_terms ? f->d_part + pq : nullptr;
+        PhaseBuilder &u = phase();
+        for (int t = 0; t < T; ++t)
+            u.add(WOp::AdjLeafUp, f->tr[t]->B, "wl_adj_leaf_up", adj_leaf_up_args(f->tr[t], f->vb[t]), 0, 0.0);
+        for (int l = 1; l < Lmax; ++l) {
+            PhaseBuilder &b = phase();
+            for (int t = 0; t < T; ++t) {
+                Plan *p = f->tr[t];
+                if (l > p->L - 1) continue;
+                AdjUpFusedArgs F;
+                AdjUpSchoolArgs Sa;
+                adj_up_args(p, f->vb[t], l, tw, logTW, F, Sa);
+                b.pack_items = F.npairs;   // pairs of different members share CTAs
+                b.pack_cb = F.nbx > 0 ? adj_items_per_cta(F.logN) : 1;
+                b.add(WOp::AdjUpFused, F.logN, "wl_adj_up_fused", F, adj_up_smem(F.logN), 0.0);
+                b.pack_items = 0;
+                b.add(WOp::AdjUpSchool, 0, "wl_adj_up_school", Sa, 0, 0.0);
+            }
+        }
+        for (int l = Lmax - 1; l >= 1; --l) {
+            PhaseBuilder &b = phase();
+            for (int t = 0; t < T; ++t) {
+                Plan *p = f->tr[t];
+                if (l > p->L - 1) continue;
+                AdjDownFusedArgs F;
+                AdjDownSchoolArgs Sa;
+                adj_down_args(p, f->vb[t], l, tw, logTW, F, Sa);
+                b.pack_items = F.npairs;
+                b.pack_cb = F.nbx > 0 ? adj_items_per_cta(F.logN) : 1;
+                b.add(WOp::AdjDownFused, F.logN, "wl_adj_down_fused", F, adj_down_smem(F.logN), 0.0);
+                b.pack_items = 0;
+                b.add(WOp::AdjDownSchool, 0, "wl_adj_down_school", Sa, 0, 0.0);
+            }
+        }
+        PhaseBuilder &d = phase();
+        for (int t = 0; t < T; ++t) {
+            Plan *p = f->tr[t];
+            const AdjLeafDownArgs A =
+                adj_leaf_down_args(p, f->vb[t], pA ? pA + f->off[t] : nullptr, pB ? pB + f->off[t] : nullptr);
+            d.add(WOp::AdjLeafDown, p->B, "wl_adj_leaf_down", A, 0, 0.0);
+        }
+    } else {   // per-player divide
         PhaseBuilder &b = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
@@ -371,6 +414,8 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
     if (s.packed) {
         if (s.op == WOp::FusedBuild || s.op == WOp::FusedProp)
             launch_packed_fused(s.op, s.d_desc, s.d_tab, nctas, s.cb, qn, q0, s.smem, f->stream);
+        else if (s.op == WOp::AdjUpFused || s.op == WOp::AdjDownFused)
+            launch_packed_adj(s.op, s.d_desc, s.d_tab, nctas, s.cb, qn, q0, s.smem, f->stream);
         else
             launch_packed_spec(s.op, s.d_desc, s.d_tab, nctas, s.cb, qn, q0, s.smem, f->stream);
         f->prof.end(f->stream);
@@ -386,6 +431,14 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
         case WOp::FusedProp: launch_worklist_fused(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
         case WOp::SubBuild:
         case WOp::SubProp: launch_worklist_sub(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
+        case WOp::AdjLeafUp:
+        case WOp::AdjUpSchool:
+        case WOp::AdjUpFused:
+        case WOp::AdjDownSchool:
+        case WOp::AdjDownFused:
+        case WOp::AdjLeafDown:
+            launch_worklist_adj(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream);
+            break;
         default: launch_worklist_spec(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
     }
     f->prof.end(f->stream);
@@ -398,6 +451,19 @@ static void enqueue_run(Forest *f) {
     for (int q0 = 0; q0 < f->Q; q0 += f->qc) {
         const int nq = std::min(f->qc, f->Q - q0);
         for (const WStep &s : f->steps) launch_step(f, s, nq, q0);
+        if (f->vjp) {   // ordered sums over nodes: dL/dS shares and the roots' gbar
+            launch_accum_strided((int)f->Ntot, nq, f->d_contrib, (size_t)f->Ntot, f->d_acc, q0 == 0, f->stream);
+            launch_accum_strided((int)f->Rtot, nq, f->d_root, (size_t)f->Rtot, f->d_gradP, q0 == 0, f->stream);
+            f->launches += 2;
+            if (f->node_terms) {
+                const size_t pq = (size_t)f->qc * f->Ntot, nodes = (size_t)f->tr.size() * f->Q;
+                double *nA = f->d_part + 2 * pq;
+                launch_node_reduce_members((int)f->tr.size(), f->d_mem, nq, (size_t)f->Ntot, f->d_part,
+                                           f->d_part + pq, nA, nA + nodes, f->Q, q0, f->stream);
+                ++f->launches;
+            }
+            continue;
+        }
         launch_accumulate((int)f->Ntot, nq, f->d_contrib, f->d_acc, q0 == 0 ? 1 : 0, f->stream, &f->prof);
         ++f->launches;
     }
@@ -406,7 +472,7 @@ static void enqueue_run(Forest *f) {
 }
 
 // ------------------------------------------------------------ lifecycle
-Forest *forest_create(int T, const int *n, const int *k, const double *S, std::string &err) {
+Forest *forest_create(int T, const int *n, const int *k, const double *S, std::string &err, bool vjp) {
     if (T < 1 || !n || !k || !S) { err = "invalid batch arguments"; return nullptr; }
     long tot = 0;
     std::vector<long> ioff(T + 1, 0), ipoff(T + 1, 0);
@@ -421,6 +487,7 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
     }
     if (tot > (long)INT32_MAX / 2) { err = "batch too large (total players)"; return nullptr; }
     Forest *f = new Forest();
+    f->vjp = vjp;
     f->T = T;
     f->ioff = ioff;
     f->ipoff = ipoff;
@@ -431,9 +498,12 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
     std::vector<std::string> errs(T);
     parallel_for(T, [&](int t) {
         Plan *p = new Plan();
+        p->coeff_only = vjp;   // the adjoint passes work on coefficients
         if (plan_geometry(p, n[t], S + ioff[t], k[t], errs[t]) != 0) {
             delete p;
             p = nullptr;
+        } else if (vjp) {
+            p->Lf = 0;   // every level's g is kept for the adjoint
         }
         all[t] = p;
     });
@@ -454,6 +524,16 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
         }
     }
     for (int t : f->fallback) {   // own plans (own arenas and streams)
+        if (vjp) {
+            VjpPlan *v = vjp_plan_create(n[t], S + ioff[t], k[t], err);
+            if (!v) {
+                err = "tournament " + std::to_string(t) + ": " + err;
+                forest_destroy(f);
+                return nullptr;
+            }
+            f->fb_vjp.push_back(v);
+            continue;
+        }
         Plan *p = plan_create(n[t], S + ioff[t], k[t], nullptr, err);
         if (!p) {
             err = "tournament " + std::to_string(t) + ": " + err;
@@ -471,6 +551,10 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
     }
     f->Ntot = f->off[F];
     f->Ktot = f->poff[F];
+    f->roff.assign(F + 1, 0);
+    if (vjp)
+        for (int i = 0; i < F; ++i) f->roff[i + 1] = f->roff[i] + ((f->tr[i]->k + 1) & ~1);
+    f->Rtot = f->roff[F];
     f->compact = f->fallback.empty();
 
     cudaError_t e = cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking);
@@ -480,6 +564,10 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
     // node chunk from the memory budget
     size_t per_q = (size_t)2 * f->Ntot * 8 + 1024;
     for (Plan *p : f->tr) per_q += p->tree_q_bytes;
+    if (vjp) {   // adjoint buffers, the roots' gbar rows, node-term partials
+        per_q += (size_t)f->Rtot * 8 + (size_t)2 * f->Ntot * 8;
+        for (Plan *p : f->tr) per_q += vjp_level_layout(p, 1, nullptr, nullptr);
+    }
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const size_t budget = g_config.max_device_bytes ? g_config.max_device_bytes
@@ -495,8 +583,16 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
     const size_t o_S = take(8 * Nt), o_perm = take(4 * Nt), o_pay = take(8 * (size_t)f->Ktot);
     const size_t o_acc = take(8 * Nt), o_out = take(8 * Nt);
     const size_t o_a = take(8 * Nt * qc), o_con = take(8 * Nt * qc);
-    std::vector<size_t> o_tree(F);
+    std::vector<size_t> o_tree(F), o_adj(F);
     for (int i = 0; i < F; ++i) o_tree[i] = take(plan_tree_layout(f->tr[i], qc, nullptr));
+    size_t o_cot = 0, o_gp = 0, o_root = 0, o_mem = 0;
+    if (vjp) {
+        o_cot = take(8 * Nt);
+        o_gp = take(8 * (size_t)f->Rtot);
+        o_root = take(8 * (size_t)qc * f->Rtot);
+        o_mem = take(sizeof(longlong2) * (size_t)F);
+        for (int i = 0; i < F; ++i) o_adj[i] = take(vjp_level_layout(f->tr[i], qc, nullptr, nullptr));
+    }
     e = cudaMallocAsync((void **)&f->arena, off, f->stream);
     if (e != cudaSuccess) {
         err = "device allocation of " + std::to_string(off) + " bytes failed: " + cudaGetErrorString(e);
@@ -531,10 +627,40 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
             if (p->lv[l].kind == 2) logNeed = std::max(logNeed, ilog2l(2 * p->lv[l].deg));
         }
     }
+    std::vector<longlong2> hmem;
+    if (vjp) {
+        f->d_cot = (double *)(A + o_cot);
+        f->d_gradP = (double *)(A + o_gp);
+        f->d_root = (double *)(A + o_root);
+        f->d_mem = (longlong2 *)(A + o_mem);
+        f->vb.assign(F, VjpBufs{});
+        for (int i = 0; i < F; ++i) {
+            Plan *p = f->tr[i];
+            VjpBufs &b = f->vb[i];
+            vjp_level_layout(p, qc, A + o_adj[i], &b);
+            b.kst = (p->k + 1) & ~1;
+            b.root = f->d_root + f->roff[i];   // rows of Rtot: every member's root gbar side by side
+            b.root_q = (size_t)f->Rtot;
+            b.cot = f->d_cot + f->off[i];
+            b.a = f->d_a + f->off[i];
+            b.aq = Nt;
+            b.contrib = f->d_contrib + f->off[i];
+            if (p->L == 1) {   // the single leaf block is the root: its gbar goes to the root rows
+                b.gb[0] = b.root;
+                b.gb_q[0] = b.root_q;
+                b.gb_st[0] = b.kst;
+            }
+            hmem.push_back(make_longlong2(f->off[i], p->n));
+        }
+    }
     f->tw = twiddles(logNeed, f->stream, err, &f->logTW);
     if (!f->tw) { forest_destroy(f); return nullptr; }
     e = cudaMemcpyAsync(f->d_S, hS.data(), 8 * Nt, cudaMemcpyHostToDevice, f->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(f->d_perm, hperm.data(), 4 * Nt, cudaMemcpyHostToDevice, f->stream);
+    if (e == cudaSuccess && vjp) {
+        e = cudaMemcpyAsync(f->d_mem, hmem.data(), sizeof(longlong2) * F, cudaMemcpyHostToDevice, f->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(f->d_root, 0, 8 * (size_t)qc * f->Rtot, f->stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
     if (e != cudaSuccess) { err = std::string("batch upload: ") + cudaGetErrorString(e); forest_destroy(f); return nullptr; }
     return f;
@@ -546,6 +672,7 @@ void forest_destroy(Forest *f) {
     if (f->graph) cudaGraphExecDestroy(f->graph);
     if (f->d_desc) cudaFree(f->d_desc);
     if (f->d_node) cudaFree(f->d_node);
+    if (f->d_part) cudaFree(f->d_part);
     if (f->arena) {
         cudaFreeAsync(f->arena, f->stream);
         cudaStreamSynchronize(f->stream);
@@ -556,6 +683,7 @@ void forest_destroy(Forest *f) {
     if (f->stream) cudaStreamDestroy(f->stream);
     for (Plan *p : f->tr) delete p;   // geometry only: their buffers live in the forest arena
     for (Plan *p : f->fb_plans) plan_destroy(p);
+    for (VjpPlan *v : f->fb_vjp) vjp_plan_destroy(v);
     delete f;
 }
 
@@ -596,59 +724,115 @@ static int prepare_nodes(Forest *f, int Q, std::string &err) {
     return 0;
 }
 
+// node tables, work lists and (adjoint forests with node terms) partials for
+// Q nodes; the graph is recaptured when any of them changes
+static int forest_prepare(Forest *f, int Q, bool node_terms, std::string &err) {
+    if (Q == f->Q && node_terms == f->node_terms) return 0;
+    if (f->graph) cudaGraphExecDestroy(f->graph);
+    f->graph = nullptr;
+    if (Q != f->Q) {
+        f->Q = Q;
+        if (prepare_nodes(f, Q, err) != 0) { f->Q = 0; return -1; }
+    }
+    f->node_terms = node_terms;
+    if (f->vjp && node_terms) {
+        const size_t need = 2 * (size_t)f->qc * f->Ntot + 2 * f->tr.size() * (size_t)Q;
+        if (need > f->part_cap) {
+            cudaStreamSynchronize(f->stream);
+            if (f->d_part) cudaFree(f->d_part);
+            f->d_part = nullptr;
+            f->part_cap = 0;
+            cudaError_t e = cudaMalloc((void **)&f->d_part, sizeof(double) * need);
+            if (e != cudaSuccess) { err = std::string("node-term buffers: ") + cudaGetErrorString(e); f->Q = 0; return -1; }
+            f->part_cap = need;
+        }
+    }
+    build_steps(f);
+    if (upload_steps(f, err) != 0) { f->Q = 0; return -1; }
+    return 0;
+}
+
+// payouts in forest order
+static int forest_upload_payout(Forest *f, const double *payout, std::string &err) {
+    cudaError_t e;
+    if (f->compact) {
+        e = cudaMemcpyAsync(f->d_payout, payout, sizeof(double) * f->Ktot, cudaMemcpyHostToDevice, f->stream);
+    } else {
+        f->h_pay.resize(f->Ktot);
+        for (size_t i = 0; i < f->tr.size(); ++i)
+            memcpy(f->h_pay.data() + f->poff[i], payout + f->ipoff[f->tid[i]], sizeof(double) * f->tr[i]->k);
+        e = cudaMemcpyAsync(f->d_payout, f->h_pay.data(), sizeof(double) * f->Ktot, cudaMemcpyHostToDevice,
+                            f->stream);
+    }
+    if (e != cudaSuccess) { err = std::string("payout upload: ") + cudaGetErrorString(e); return -1; }
+    return 0;
+}
+
+// the run's kernel sequence between two events: a graph replay, or direct
+// launches when profiling
+static int forest_launch(Forest *f, std::string &err) {
+    cudaError_t e = cudaSuccess;
+    if (!f->ev0) { cudaEventCreate(&f->ev0); cudaEventCreate(&f->ev1); }
+    f->prof.used = 0;
+    f->prof.recs.clear();
+    const bool use_graph = f->graphs && !f->prof.on;
+    if (use_graph && !f->graph) {   // capture the kernel sequence once per node count
+        cudaGraph_t g = nullptr;
+        f->launches = 0;
+        e = cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_run(f);
+            e = cudaStreamEndCapture(f->stream, &g);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&f->graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return -1; }
+        f->graph_launches = f->launches;
+    }
+    cudaEventRecord(f->ev0, f->stream);
+    if (use_graph) {
+        e = cudaGraphLaunch(f->graph, f->stream);
+        f->launches = f->graph_launches;
+    } else {
+        f->launches = 0;
+        enqueue_run(f);
+        e = cudaGetLastError();
+    }
+    cudaEventRecord(f->ev1, f->stream);
+    if (e != cudaSuccess) { err = std::string("batch launch: ") + cudaGetErrorString(e); return -1; }
+    return 0;
+}
+
+// device time of the run and, when profiling, the per-launch records
+static void forest_collect(Forest *f) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, f->ev0, f->ev1);
+    f->last_device_ms = ms;
+    if (!f->prof.on) return;
+    for (const ProfRec &r : f->prof.recs) {
+        float ems = 0.f;
+        cudaEventElapsedTime(&ems, r.a, r.b);
+        Plan::KStat *ks = nullptr;
+        for (auto &x : f->kstats)
+            if (x.name == r.name) ks = &x;
+        if (!ks) { f->kstats.push_back({r.name, 0.0, 0, 0.0}); ks = &f->kstats.back(); }
+        ks->ms += ems;
+        ks->launches += 1;
+        ks->flops += r.flops;
+    }
+}
+
 int forest_run(Forest *f, int Q, const double *payout, double *equity, IcmGpuRunStats *stats, std::string &err) {
     if (!f || Q < 1 || !payout || !equity) { err = "invalid arguments"; return -1; }
+    if (f->vjp) { err = "this batch computes VJPs (use the VJP run)"; return -1; }
     const double t0 = now_ns();
     f->launches = 0;
     const int F = (int)f->tr.size();
     cudaError_t e = cudaSuccess;
     if (F > 0) {
-        if (Q != f->Q) {
-            if (f->graph) cudaGraphExecDestroy(f->graph);
-            f->graph = nullptr;
-            f->Q = Q;
-            if (prepare_nodes(f, Q, err) != 0) { f->Q = 0; return -1; }
-            build_steps(f);
-            if (upload_steps(f, err) != 0) { f->Q = 0; return -1; }
-        }
-        // payouts in forest order
-        if (f->compact) {
-            e = cudaMemcpyAsync(f->d_payout, payout, sizeof(double) * f->Ktot, cudaMemcpyHostToDevice, f->stream);
-        } else {
-            f->h_pay.resize(f->Ktot);
-            for (int i = 0; i < F; ++i)
-                memcpy(f->h_pay.data() + f->poff[i], payout + f->ipoff[f->tid[i]], sizeof(double) * f->tr[i]->k);
-            e = cudaMemcpyAsync(f->d_payout, f->h_pay.data(), sizeof(double) * f->Ktot, cudaMemcpyHostToDevice,
-                                f->stream);
-        }
-        if (e != cudaSuccess) { err = std::string("payout upload: ") + cudaGetErrorString(e); return -1; }
-        if (!f->ev0) { cudaEventCreate(&f->ev0); cudaEventCreate(&f->ev1); }
-        f->prof.used = 0;
-        f->prof.recs.clear();
-        const bool use_graph = f->graphs && !f->prof.on;
-        if (use_graph && !f->graph) {   // capture the kernel sequence once per node count
-            cudaGraph_t g = nullptr;
-            e = cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal);
-            if (e == cudaSuccess) {
-                enqueue_run(f);
-                e = cudaStreamEndCapture(f->stream, &g);
-            }
-            if (e == cudaSuccess) e = cudaGraphInstantiate(&f->graph, g, 0);
-            if (g) cudaGraphDestroy(g);
-            if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return -1; }
-            f->graph_launches = f->launches;
-        }
-        cudaEventRecord(f->ev0, f->stream);
-        if (use_graph) {
-            e = cudaGraphLaunch(f->graph, f->stream);
-            f->launches = f->graph_launches;
-        } else {
-            f->launches = 0;
-            enqueue_run(f);
-            e = cudaGetLastError();
-        }
-        cudaEventRecord(f->ev1, f->stream);
-        if (e != cudaSuccess) { err = std::string("batch launch: ") + cudaGetErrorString(e); return -1; }
+        if (forest_prepare(f, Q, false, err) != 0) return -1;
+        if (forest_upload_payout(f, payout, err) != 0) return -1;
+        if (forest_launch(f, err) != 0) return -1;
         if (f->compact) {
             e = cudaMemcpyAsync(equity, f->d_out, sizeof(double) * f->Ntot, cudaMemcpyDeviceToHost, f->stream);
         } else {
@@ -661,22 +845,7 @@ int forest_run(Forest *f, int Q, const double *payout, double *equity, IcmGpuRun
         if (!f->compact)
             for (int i = 0; i < F; ++i)
                 memcpy(equity + f->ioff[f->tid[i]], f->h_out.data() + f->off[i], sizeof(double) * f->tr[i]->n);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, f->ev0, f->ev1);
-        f->last_device_ms = ms;
-        if (f->prof.on) {
-            for (const ProfRec &r : f->prof.recs) {
-                float ems = 0.f;
-                cudaEventElapsedTime(&ems, r.a, r.b);
-                Plan::KStat *ks = nullptr;
-                for (auto &x : f->kstats)
-                    if (x.name == r.name) ks = &x;
-                if (!ks) { f->kstats.push_back({r.name, 0.0, 0, 0.0}); ks = &f->kstats.back(); }
-                ks->ms += ems;
-                ks->launches += 1;
-                ks->flops += r.flops;
-            }
-        }
+        forest_collect(f);
     } else {
         f->last_device_ms = 0.0;
     }
@@ -686,6 +855,91 @@ int forest_run(Forest *f, int Q, const double *payout, double *equity, IcmGpuRun
         Plan *p = f->fb_plans[i];
         if (plan_run(p, Q, payout + f->ipoff[t], equity + f->ioff[t], nullptr, err) != 0) return -1;
         f->launches += p->launches;
+    }
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->total_ns = now_ns() - t0;
+        stats->peak_vram_bytes = f->arena_bytes;
+        stats->engine = 1;
+    }
+    return 0;
+}
+
+// Adjoint forest: per chunk of nodes the forward tree of every member (no
+// divide), then the adjoint passes; dL/dS and the roots' gbar are summed over
+// nodes in order, so each member's gradients equal its single-plan VJP's bit
+// for bit.
+int forest_vjp_run(Forest *f, int Q, const double *payout, const double *cot, int flags, double *grad_S,
+                   double *grad_payout, IcmGpuRunStats *stats, std::string &err) {
+    if (!f || Q < 1 || !payout || !cot || !grad_S || !grad_payout) { err = "invalid arguments"; return -1; }
+    if (!f->vjp) { err = "this batch computes equities (use the batch run)"; return -1; }
+    const double t0 = now_ns();
+    const bool node_terms = (flags & 1) != 0;
+    f->launches = 0;
+    const int F = (int)f->tr.size();
+    cudaError_t e = cudaSuccess;
+    if (F > 0) {
+        if (forest_prepare(f, Q, node_terms, err) != 0) return -1;
+        if (forest_upload_payout(f, payout, err) != 0) return -1;
+        // cotangents in each member's sorted order
+        f->h_cot.resize(f->Ntot);
+        for (int i = 0; i < F; ++i) {
+            const Plan *p = f->tr[i];
+            const double *c = cot + f->ioff[f->tid[i]];
+            double *o = f->h_cot.data() + f->off[i];
+            for (int j = 0; j < p->n; ++j) o[j] = c[p->perm[j]];
+        }
+        e = cudaMemcpyAsync(f->d_cot, f->h_cot.data(), sizeof(double) * f->Ntot, cudaMemcpyHostToDevice, f->stream);
+        if (e != cudaSuccess) { err = std::string("cotangent upload: ") + cudaGetErrorString(e); return -1; }
+        if (forest_launch(f, err) != 0) return -1;
+        f->h_out.resize(f->Ntot);
+        f->h_gp.resize(f->Rtot);
+        double *gs = f->compact ? grad_S : f->h_out.data();
+        e = cudaMemcpyAsync(gs, f->d_out, sizeof(double) * f->Ntot, cudaMemcpyDeviceToHost, f->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(f->h_gp.data(), f->d_gradP, sizeof(double) * f->Rtot, cudaMemcpyDeviceToHost,
+                                f->stream);
+        const size_t nodes = (size_t)F * Q;
+        if (node_terms) {
+            f->h_nodeA.resize(nodes);
+            f->h_nodeB.resize(nodes);
+            const double *nA = f->d_part + 2 * (size_t)f->qc * f->Ntot;
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(f->h_nodeA.data(), nA, sizeof(double) * nodes, cudaMemcpyDeviceToHost, f->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(f->h_nodeB.data(), nA + nodes, sizeof(double) * nodes, cudaMemcpyDeviceToHost,
+                                    f->stream);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
+        if (e != cudaSuccess) { err = std::string("batch execution: ") + cudaGetErrorString(e); return -1; }
+        if (!f->compact)
+            for (int i = 0; i < F; ++i)
+                memcpy(grad_S + f->ioff[f->tid[i]], f->h_out.data() + f->off[i], sizeof(double) * f->tr[i]->n);
+        for (int i = 0; i < F; ++i)
+            memcpy(grad_payout + f->ipoff[f->tid[i]], f->h_gp.data() + f->roff[i], sizeof(double) * f->tr[i]->k);
+        if (node_terms) {   // every node has a positive weight: all Q are active
+            std::vector<int> qidx(Q);
+            for (int q = 0; q < Q; ++q) qidx[q] = q;
+            const std::vector<double> none;
+            for (int i = 0; i < F; ++i) {
+                const Plan *p = f->tr[i];
+                const std::vector<double> A(f->h_nodeA.begin() + (size_t)i * Q, f->h_nodeA.begin() + (size_t)(i + 1) * Q);
+                const std::vector<double> Bw(f->h_nodeB.begin() + (size_t)i * Q,
+                                             f->h_nodeB.begin() + (size_t)(i + 1) * Q);
+                grad_S[f->ioff[f->tid[i]] + p->perm[0]] += node_shift_term(Q, p->Smax, qidx, none, A, Bw);
+            }
+        }
+        forest_collect(f);
+    } else {
+        f->last_device_ms = 0.0;
+    }
+    for (size_t i = 0; i < f->fallback.size(); ++i) {   // beyond the one-CTA kernels: single plans
+        const int t = f->fallback[i];
+        VjpPlan *v = f->fb_vjp[i];
+        if (vjp_plan_run(v, Q, payout + f->ipoff[t], cot + f->ioff[t], grad_S + f->ioff[t],
+                         grad_payout + f->ipoff[t], flags, nullptr, err) != 0)
+            return -1;
+        f->launches += v->p->launches;
     }
     if (stats) {
         memset(stats, 0, sizeof(*stats));

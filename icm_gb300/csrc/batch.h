@@ -7,6 +7,7 @@
 
 #include "engine.h"
 #include "kernels.h"
+#include "vjp.h"
 
 namespace icmg {
 
@@ -65,10 +66,27 @@ struct Forest {
     double last_device_ms = 0.0;
     Prof prof;
     std::vector<Plan::KStat> kstats;
+    // adjoint forests: coefficient-level member trees, forward without the
+    // divide, then the adjoint passes as work lists; d_acc sums dL/dS
+    bool vjp = false;
+    bool node_terms = false;          // the mode the steps were built for
+    std::vector<VjpBufs> vb;          // per member adjoint buffers
+    std::vector<long> roff;           // member offsets in the root gbar rows (kst each)
+    long Rtot = 0;
+    double *d_cot = nullptr, *d_gradP = nullptr, *d_root = nullptr;
+    longlong2 *d_mem = nullptr;       // per member (offset, players)
+    double *d_part = nullptr;         // node terms: partials [2][qc][Ntot], per-node sums [2][F][Q]
+    size_t part_cap = 0;
+    std::vector<VjpPlan *> fb_vjp;
+    std::vector<double> h_cot, h_gp, h_nodeA, h_nodeB;
 };
 
-Forest *forest_create(int T, const int *n, const int *k, const double *S, std::string &err);
+// vjp: an adjoint forest (forest_vjp_run), else a forward one (forest_run)
+Forest *forest_create(int T, const int *n, const int *k, const double *S, std::string &err, bool vjp = false);
 void forest_destroy(Forest *f);
 int forest_run(Forest *f, int Q, const double *payout, double *equity, IcmGpuRunStats *stats, std::string &err);
+// flags as vjp_plan_run; gradients in the caller's order (sum n, sum k)
+int forest_vjp_run(Forest *f, int Q, const double *payout, const double *cot, int flags, double *grad_S,
+                   double *grad_payout, IcmGpuRunStats *stats, std::string &err);
 
 }  // namespace icmg

@@ -361,7 +361,7 @@ void plan_destroy(Plan *p) {
     if (!p) return;
     if (p->stream) cudaStreamSynchronize(p->stream);
     if (p->graph) cudaGraphExecDestroy(p->graph);
-    if (p->d_node) cudaFree(p->d_node);
+    if (p->d_node) cudaFreeAsync(p->d_node, p->stream);
     if (p->arena) {
         if (p->pooled) {
             cudaFreeAsync(p->arena, p->stream);
@@ -582,11 +582,12 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     const int nact = (int)(node.size() / 3);
     cudaError_t e = cudaSuccess;
     if (nact > p->qmax) {
-        if (p->d_node) cudaFree(p->d_node);
+        // stream-ordered from the pool: no device-wide synchronisation
+        if (p->d_node) cudaFreeAsync(p->d_node, p->stream);
         p->d_node = nullptr;
         p->d_z = nullptr;
         const size_t nb = sizeof(double) * 3 * (size_t)std::max(nact, 1);
-        e = cudaMalloc(&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1));
+        e = cudaMallocAsync((void **)&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1), p->stream);
         if (e != cudaSuccess) { err = std::string("node buffer: ") + cudaGetErrorString(e); return -1; }
         p->d_z = (int *)((char *)p->d_node + nb);
         p->qmax = nact;

@@ -59,18 +59,34 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 __device__ __forceinline__ int vjp_cb(int N) { return N >= 8192 ? 1 : 4096 / N; }
 static inline int vjp_cb_h(int N) { return N >= 8192 ? 1 : 4096 / N; }
-static inline size_t vjp_up_smem(int N) { return (size_t)vjp_cb_h(N) * (N + N / 2) * sizeof(double2); }
-static inline size_t vjp_down_smem(int N) { return (size_t)vjp_cb_h(N) * N * sizeof(double2); }
+// Every pair of a CTA is described by a view staged in shared memory after
+// the transforms, so a CTA may hold pairs of different tournaments (packed
+// work lists) and pairs under wholly-zero parents are pruned per pair.
+constexpr size_t kAdjViewBytes = 80;
+constexpr size_t kAdjItemBytes = kAdjViewBytes + sizeof(int);
+static inline size_t vjp_up_smem(int N) {
+    return (size_t)vjp_cb_h(N) * ((N + N / 2) * sizeof(double2) + kAdjItemBytes);
+}
+static inline size_t vjp_down_smem(int N) { return (size_t)vjp_cb_h(N) * (N * sizeof(double2) + kAdjItemBytes); }
 
 // ------------------------------------------------------------ leaf adjoints
 // gbar of every leaf block: sum_i c_i Q_i by the running pair
 // (prod, wsum) -> (prod f, wsum f + c prod).  One thread per (block, node).
 template <int B>
-__global__ void k_adj_leaf_up(int n, int k, int nblocks, const double *__restrict__ S,
-                              const double *__restrict__ node, int q0, const double *__restrict__ a,
-                              const double *__restrict__ cot, double *__restrict__ gb0, size_t gb0_q, int gst0) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
+__device__ __forceinline__ void adj_leaf_up_t(const AdjLeafUpArgs &A, int bx, int q, int q0) {
+    const auto n = A.n;
+    const auto k = A.k;
+    const auto nblocks = A.nblocks;
+    const auto S = A.S;
+    const auto node = A.node;
+    const auto a = A.a;
+    const auto aq = A.aq;
+    const auto cot = A.cot;
+    const auto gb0 = A.gb0;
+    const auto gb0_q = A.gb0_q;
+    const auto gst0 = A.gst0;
+
+    const int b = bx * blockDim.x + threadIdx.x;
     if (b >= nblocks) return;
     const double *nd = node + 3 * (q0 + q);
     const double w = nd[1], iv = nd[2];
@@ -79,7 +95,7 @@ __global__ void k_adj_leaf_up(int n, int k, int nblocks, const double *__restric
 #pragma unroll
     for (int m = 0; m <= B; ++m) { P[m] = 0.0; W[m] = 0.0; }
     P[0] = 1.0;
-    const double *arow = a + (size_t)q * n + start;
+    const double *arow = a + (size_t)q * aq + start;
     for (int j = 0; j < bs; ++j) {
         const double aj = arow[j], bj = 1.0 - aj;
         double pw = w * S[start + j] * aj * iv;
@@ -102,24 +118,37 @@ __global__ void k_adj_leaf_up(int n, int k, int nblocks, const double *__restric
 // per player: Q_i and H_i by the same recurrence over the block without i,
 // then the three terms of abar_i and the node's share of dL/dS_i
 template <int B>
-__global__ void k_adj_leaf_down(int n, int k, const double *__restrict__ S, const double *__restrict__ node, int q0,
-                                const double *__restrict__ a, const double *__restrict__ cot,
-                                const double *__restrict__ g0, size_t g0_q, int gst0, const double *__restrict__ Pb0,
-                                size_t Pb0_q, int pst0, int plen0, double *__restrict__ contrib,
-                                double *__restrict__ partA, double *__restrict__ partB) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
+__device__ __forceinline__ void adj_leaf_down_t(const AdjLeafDownArgs &A, int bx, int q, int q0) {
+    const auto n = A.n;
+    const auto k = A.k;
+    const auto S = A.S;
+    const auto node = A.node;
+    const auto a = A.a;
+    const auto aq = A.aq;
+    const auto cot = A.cot;
+    const auto g0 = A.g0;
+    const auto g0_q = A.g0_q;
+    const auto gst0 = A.gst0;
+    const auto Pb0 = A.Pb0;
+    const auto Pb0_q = A.Pb0_q;
+    const auto pst0 = A.pst0;
+    const auto plen0 = A.plen0;
+    const auto contrib = A.contrib;
+    const auto partA = A.partA;
+    const auto partB = A.partB;
+
+    const int i = bx * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *nd = node + 3 * (q0 + q);
     const double logv = nd[0], w = nd[1], iv = nd[2];
     const int b = i / B, start = b * B, bs = min(B, n - start), pk = min(bs, k);
     const int me = i - start;
-    const double *arow = a + (size_t)q * n + start;
+    const double *arow = a + (size_t)q * aq + start;
     if (arow[me] == 0.0) {   // leaf factor 0 (S logv < -700): no share; g of its block may be pruned
-        contrib[(size_t)q * n + i] = 0.0;
+        contrib[(size_t)q * aq + i] = 0.0;
         if (partA) {
-            partA[(size_t)q * n + i] = 0.0;
-            partB[(size_t)q * n + i] = 0.0;
+            partA[(size_t)q * aq + i] = 0.0;
+            partB[(size_t)q * aq + i] = 0.0;
         }
         return;
     }
@@ -162,23 +191,36 @@ __global__ void k_adj_leaf_down(int n, int k, const double *__restrict__ S, cons
     const double pw = w * Si * ai * iv;
     const bool fin = isfinite(pw);
     const double abar = (fin ? ci * w * Si * iv * inner : 0.0) + bterm + cterm;
-    contrib[(size_t)q * n + i] = (fin ? ci * w * ai * iv * inner : 0.0) + abar * logv * ai;
+    contrib[(size_t)q * aq + i] = (fin ? ci * w * ai * iv * inner : 0.0) + abar * logv * ai;
     if (partA) {   // dL/dlogv and w dL/dw shares of this player (a = v^S, 1/v)
         const double li = fin ? ci * pw * inner : 0.0;
-        partA[(size_t)q * n + i] = abar * Si * ai - li;
-        partB[(size_t)q * n + i] = li;
+        partA[(size_t)q * aq + i] = abar * Si * ai - li;
+        partB[(size_t)q * aq + i] = li;
     }
 }
 
 // ------------------------------------------------------- schoolbook passes
 // gbar of parents j >= j0: P_R gbar_L + P_L gbar_R, truncated to gpl; a lone
 // child passes its gbar up unchanged (its g was the parent's).
-__global__ void k_adj_up_school(const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc, int nreal_c,
-                                const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen_c,
-                                double *__restrict__ gbp, size_t gbp_q, int gst_p, int gpl, int nreal_p, int j0,
-                                ZeroPrefix z) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
+__device__ __forceinline__ void adj_up_school_body(const AdjUpSchoolArgs &A, int bx, int q, int q0) {
+    const auto Pc = A.Pc;
+    const auto Pc_q = A.Pc_q;
+    const auto pst_c = A.pst_c;
+    const auto lc = A.lc;
+    const auto nreal_c = A.nreal_c;
+    const auto gbc = A.gbc;
+    const auto gbc_q = A.gbc_q;
+    const auto gst_c = A.gst_c;
+    const auto glen_c = A.glen_c;
+    const auto gbp = A.gbp;
+    const auto gbp_q = A.gbp_q;
+    const auto gst_p = A.gst_p;
+    const auto gpl = A.gpl;
+    const auto nreal_p = A.nreal_p;
+    const auto j0 = A.j0;
+
+    const long idx = (long)bx * blockDim.x + threadIdx.x;
+    const ZeroPrefix z{A.zp, q0, A.span};
     const int j = j0 + (int)(idx / gst_p);
     const int t = (int)(idx % gst_p);
     if (j >= nreal_p) return;
@@ -200,13 +242,29 @@ __global__ void k_adj_up_school(const double *__restrict__ Pc, size_t Pc_q, int 
 
 // Pbar of children c >= c0: sum_m gbar_sib[m] g_par[m+i] + sum_j Pbar_par[i+j] P_sib[j];
 // a lone child takes the parent's Pbar (the build copied it up).
-__global__ void k_adj_down_school(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl,
-                                  const double *__restrict__ Pbp, size_t Pbp_q, int pst_p, int lp,
-                                  const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc,
-                                  const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen_c,
-                                  double *__restrict__ Pbc, int nreal_c, int c0, ZeroPrefix z) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
+__device__ __forceinline__ void adj_down_school_body(const AdjDownSchoolArgs &A, int bx, int q, int q0) {
+    const auto gp = A.gp;
+    const auto gp_q = A.gp_q;
+    const auto gst_p = A.gst_p;
+    const auto gpl = A.gpl;
+    const auto Pbp = A.Pbp;
+    const auto Pbp_q = A.Pbp_q;
+    const auto pst_p = A.pst_p;
+    const auto lp = A.lp;
+    const auto Pc = A.Pc;
+    const auto Pc_q = A.Pc_q;
+    const auto pst_c = A.pst_c;
+    const auto lc = A.lc;
+    const auto gbc = A.gbc;
+    const auto gbc_q = A.gbc_q;
+    const auto gst_c = A.gst_c;
+    const auto glen_c = A.glen_c;
+    const auto Pbc = A.Pbc;
+    const auto nreal_c = A.nreal_c;
+    const auto c0 = A.c0;
+
+    const long idx = (long)bx * blockDim.x + threadIdx.x;
+    const ZeroPrefix z{A.zp, q0, A.span};
     const int c = c0 + (int)(idx / pst_c);
     const int i = (int)(idx % pst_c);
     if (c >= nreal_c || zp_cold(z, q, c)) return;   // wholly zero: its Pbar meets only zero factors
@@ -232,38 +290,100 @@ __global__ void k_adj_down_school(const double *__restrict__ gp, size_t gp_q, in
 }
 
 // ----------------------------------------------------- one-kernel FFT passes
-// Upward, pairs [0, npairs): z = gbar_L + i gbar_R -> FFT N -> the children's
-// gbar spectra (cached for the downward pass) -> Y = S_R G_L + S_L G_R with
-// the children's P spectra S cached by the forward build -> half-size inverse
-// -> gbar_parent.  N >= glen_c + lc - 1, so the products do not wrap.
-__global__ void __launch_bounds__(kVjpThreads)
-k_adj_up_fused(const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen_c, int npairs, int logN,
-               const double2 *__restrict__ spec, double2 *__restrict__ gspec, double *__restrict__ gbp, size_t gbp_q,
-               int gst_p, int gpl, const double2 *__restrict__ tw, int logTW, ZeroPrefix z) {
-    extern __shared__ double2 sm[];
-    const int N = 1 << logN, h = N >> 1;
-    const int cb = vjp_cb(N);
-    const int q = blockIdx.y;
-    const int j0 = blockIdx.x * cb;
-    const int cnt = min(cb, npairs - j0);
-    if (zp_cold(z, q, j0 + cnt - 1)) {   // wholly-zero parents: gbar = 0
-        for (int e = threadIdx.x; e < cnt * gst_p; e += blockDim.x)
-            gbp[q * gbp_q + (size_t)(j0 + e / gst_p) * gst_p + e % gst_p] = 0.0;
-        return;
-    }
-    double2 *Z = sm;
-    double2 *U = sm + (size_t)cb * N;
-    const double *base = gbc + q * gbc_q;
-    for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
-        const int it = e >> logN, s = e & (N - 1);
-        const int t = (int)bitrev(s, logN);
-        const double *gL = base + (size_t)(2 * (j0 + it)) * gst_c;
-        Z[e] = (t < glen_c) ? make_double2(gL[t], gL[gst_c + t]) : make_double2(0.0, 0.0);
+struct AuView {          // one pair of the upward pass
+    const double *gL;    // left child's gbar row (the right child's at + gst_c)
+    const double2 *sL;   // children's P spectra from the build (the right child's at + h + 1)
+    double2 *gsL;        // children's gbar spectra, cached for the downward pass (same layout)
+    double *out;         // parent's gbar row
+    int gst_c, glen_c, gst_p, gpl, cold;
+};
+static_assert(sizeof(AuView) <= kAdjViewBytes, "view size");
+struct AdView {          // one pair of the downward pass
+    const double *g;     // parent's g row (the payout at the root)
+    const double *pb;    // parent's Pbar row (null at the root)
+    const double *PsL;   // left child's P row (the right child's at + pst_c)
+    const double2 *sL;   // children's P spectra (the right child's at + h + 1)
+    const double2 *gsL;  // children's gbar spectra from the upward pass
+    double *outL;        // left child's Pbar row (the right child's at + pst_c)
+    int gpl, lp, lc, pst_c, cold;
+};
+static_assert(sizeof(AdView) <= kAdjViewBytes, "view size");
+
+__device__ __forceinline__ void au_fill(const AdjUpFusedArgs &A, int q, int q0, int j, int h, AuView &v) {
+    const size_t so = (2 * ((size_t)q * A.npairs + j)) * (size_t)(h + 1);
+    v.gL = A.gbc + q * A.gbc_q + (size_t)(2 * j) * A.gst_c;
+    v.sL = A.spec + so;
+    v.gsL = A.gspec + so;
+    v.out = A.gbp + q * A.gbp_q + (size_t)j * A.gst_p;
+    v.gst_c = A.gst_c;
+    v.glen_c = A.glen_c;
+    v.gst_p = A.gst_p;
+    v.gpl = A.gpl;
+    const ZeroPrefix z{A.zp, q0, A.span};
+    v.cold = zp_cold(z, q, j) ? 1 : 0;
+}
+
+__device__ __forceinline__ void ad_fill(const AdjDownFusedArgs &A, int q, int q0, int j, int h, AdView &v) {
+    const size_t so = (2 * ((size_t)q * A.npairs + j)) * (size_t)(h + 1);
+    v.g = A.gp + q * A.gp_q + (size_t)j * A.gst_p;
+    v.pb = A.Pbp ? A.Pbp + q * A.Pbp_q + (size_t)j * A.pst_p : nullptr;
+    v.PsL = A.Pc + q * A.Pc_q + (size_t)(2 * j) * A.pst_c;
+    v.sL = A.spec + so;
+    v.gsL = A.gspec + so;
+    v.outL = A.Pbc + q * A.Pc_q + (size_t)(2 * j) * A.pst_c;
+    v.gpl = A.gpl;
+    v.lp = A.lp;
+    v.lc = A.lc;
+    v.pst_c = A.pst_c;
+    const ZeroPrefix z{A.zp, q0, A.span};
+    v.cold = zp_cold(z, q, j) ? 1 : 0;
+}
+
+__device__ __forceinline__ int adj_width(const AuView &v) { return v.gst_p; }
+__device__ __forceinline__ int adj_width(const AdView &v) { return v.pst_c; }
+
+// hot pairs first in idx; *w = the widest output row of the CTA's pairs
+template <class View>
+__device__ __forceinline__ int adj_partition(const View *V, int *idx, int cnt, int *w) {
+    __shared__ int nhot_s, w_s;
+    if (threadIdx.x == 0) {
+        int h = 0, mw = 0;
+        for (int it = 0; it < cnt; ++it)
+            if (!V[it].cold) idx[h++] = it;
+        int c = h;
+        for (int it = 0; it < cnt; ++it) {
+            if (V[it].cold) idx[c++] = it;
+            mw = max(mw, adj_width(V[it]));
+        }
+        nhot_s = h;
+        w_s = mw;
     }
     __syncthreads();
-    smem_fft_dit<-1>(Z, logN, cnt, tw, logTW);
-    for (int e = threadIdx.x; e < cnt * h; e += blockDim.x) {
+    *w = w_s;
+    return nhot_s;
+}
+
+// Upward, pairs idx[0, nh): z = gbar_L + i gbar_R -> FFT N -> the children's
+// gbar spectra (cached for the downward pass) -> Y = S_R G_L + S_L G_R with
+// the children's P spectra S cached by the forward build -> half-size inverse
+// -> gbar_parent.  N >= glen_c + lc - 1, so the products do not wrap.  Pairs
+// idx[nh, cnt) sit under wholly-zero parents: their gbar is 0.
+__device__ void adj_up_core(const AuView *V, const int *idx, int cnt, int nh, int wmax, int cb, int logN,
+                            const double2 *__restrict__ tw, int logTW, double2 *sm) {
+    const int N = 1 << logN, h = N >> 1;
+    double2 *Z = sm;
+    double2 *U = sm + (size_t)cb * N;
+    for (int e = threadIdx.x; e < nh * N; e += blockDim.x) {
+        const int it = e >> logN, s = e & (N - 1);
+        const int t = (int)bitrev(s, logN);
+        const AuView &v = V[idx[it]];
+        Z[e] = (t < v.glen_c) ? make_double2(v.gL[t], v.gL[v.gst_c + t]) : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    smem_fft_dit<-1>(Z, logN, nh, tw, logTW);
+    for (int e = threadIdx.x; e < nh * h; e += blockDim.x) {
         const int it = e / h, f = e - it * h;
+        const AuView &v = V[idx[it]];
         const double2 *z = Z + (size_t)it * N;
         const int fc = h - f;
         const double2 zf = z[f], zn = z[(N - f) & (N - 1)];
@@ -272,9 +392,8 @@ k_adj_up_fused(const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen
         const double2 GRf = cscale(cmul_mi(csub(zf, cconj(zn))), 0.5);
         const double2 GLc = cscale(cadd(zc, cconj(zcn)), 0.5);
         const double2 GRc = cscale(cmul_mi(csub(zc, cconj(zcn))), 0.5);
-        const size_t so = (2 * ((size_t)q * npairs + j0 + it)) * (size_t)(h + 1);
-        const double2 *sL = spec + so, *sR = sL + (h + 1);
-        double2 *gL = gspec + so, *gR = gL + (h + 1);
+        const double2 *sL = v.sL, *sR = sL + (h + 1);
+        double2 *gL = v.gsL, *gR = gL + (h + 1);
         gL[f] = GLf;
         gR[f] = GRf;
         if (f == 0) { gL[h] = GLc; gR[h] = GRc; }
@@ -286,55 +405,47 @@ k_adj_up_fused(const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen
         U[(size_t)it * h + bitrev(f, logN - 1)] = cadd(E, cmul_pi(O));
     }
     __syncthreads();
-    smem_fft_dit<+1>(U, logN - 1, cnt, tw, logTW);
+    smem_fft_dit<+1>(U, logN - 1, nh, tw, logTW);
     const double inv = 1.0 / N;
-    for (int e = threadIdx.x; e < cnt * gst_p; e += blockDim.x) {
-        const int it = e / gst_p, t = e - it * gst_p;
-        double *out = gbp + q * gbp_q + (size_t)(j0 + it) * gst_p;
-        double v = 0.0;
-        if (t < gpl) {
+    for (int e = threadIdx.x; e < cnt * wmax; e += blockDim.x) {
+        const int it = e / wmax, t = e - it * wmax;
+        const AuView &v = V[idx[it]];
+        if (t >= v.gst_p) continue;
+        double val = 0.0;
+        if (it < nh && t < v.gpl) {
             const double2 uv = U[(size_t)it * h + (t >> 1)];
-            v = ((t & 1) ? uv.y : uv.x) * inv;
+            val = ((t & 1) ? uv.y : uv.x) * inv;
         }
-        out[t] = v;
+        v.out[t] = val;
     }
 }
 
-// Downward, pairs [0, npairs): w = g_parent + i Pbar_parent -> FFT N -> their
+// Downward, pairs idx[0, nh): w = g_parent + i Pbar_parent -> FFT N -> their
 // spectra G, R; Z = Y_L + i Y_R with Y_L = G conj(Gbar_R) + R conj(S_R)
 // (children's gbar spectra from the upward pass, P spectra from the build),
 // in place in natural order, then bit-reversed and inverted.  The only wrap
 // is P_sib[lc-1] Pbar_parent[2(lc-1)] when N = 2(lc-1); it is corrected
-// from the coefficients.
-__global__ void __launch_bounds__(kVjpThreads)
-k_adj_down_fused(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl, const double *__restrict__ Pbp,
-                 size_t Pbp_q, int pst_p, int lp, const double *__restrict__ Pc, size_t Pc_q, int pst_c, int lc,
-                 int npairs, int logN, const double2 *__restrict__ spec, const double2 *__restrict__ gspec,
-                 double *__restrict__ Pbc, const double2 *__restrict__ tw, int logTW, ZeroPrefix z) {
-    extern __shared__ double2 sm[];
+// from the coefficients.  Children of wholly-zero parents are not needed.
+__device__ void adj_down_core(const AdView *V, const int *idx, int nh, int wmax, int logN,
+                              const double2 *__restrict__ tw, int logTW, double2 *sm) {
     const int N = 1 << logN, h = N >> 1;
-    const int cb = vjp_cb(N);
-    const int q = blockIdx.y;
-    const int j0 = blockIdx.x * cb;
-    const int cnt = min(cb, npairs - j0);
-    if (zp_cold(z, q, j0 + cnt - 1)) return;   // children of wholly-zero parents: not needed
     double2 *Z = sm;
-    for (int e = threadIdx.x; e < cnt * N; e += blockDim.x) {
+    for (int e = threadIdx.x; e < nh * N; e += blockDim.x) {
         const int it = e >> logN, s = e & (N - 1);
         const int t = (int)bitrev(s, logN);
-        const double *g = gp + q * gp_q + (size_t)(j0 + it) * gst_p;
-        double x = (t < gpl) ? g[t] : 0.0, y = 0.0;
-        if (Pbp && t < lp) y = Pbp[q * Pbp_q + (size_t)(j0 + it) * pst_p + t];
+        const AdView &v = V[idx[it]];
+        const double x = (t < v.gpl) ? v.g[t] : 0.0;
+        const double y = (v.pb && t < v.lp) ? v.pb[t] : 0.0;
         Z[e] = make_double2(x, y);
     }
     __syncthreads();
-    smem_fft_dit<-1>(Z, logN, cnt, tw, logTW);
-    for (int e = threadIdx.x; e < cnt * h; e += blockDim.x) {
+    smem_fft_dit<-1>(Z, logN, nh, tw, logTW);
+    for (int e = threadIdx.x; e < nh * h; e += blockDim.x) {
         const int it = e / h, f = e - it * h;
+        const AdView &v = V[idx[it]];
         double2 *z = Z + (size_t)it * N;
-        const size_t so = (2 * ((size_t)q * npairs + j0 + it)) * (size_t)(h + 1);
-        const double2 *sL = spec + so, *sR = sL + (h + 1);
-        const double2 *gL = gspec + so, *gR = gL + (h + 1);
+        const double2 *sL = v.sL, *sR = sL + (h + 1);
+        const double2 *gL = v.gsL, *gR = gL + (h + 1);
         if (f == 0) {   // bins 0 and h: real spectra, each its own mirror
             const double2 z0 = z[0], zh = z[h];
             const double2 G0 = make_double2(z0.x, 0.0), R0 = make_double2(z0.y, 0.0);
@@ -356,28 +467,144 @@ k_adj_down_fused(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl,
         }
     }
     __syncthreads();
-    smem_bitrev_map(Z, logN, cnt, [](int, int, double2 v) { return v; });
-    smem_fft_dit<+1>(Z, logN, cnt, tw, logTW);
+    smem_bitrev_map(Z, logN, nh, [](int, int, double2 v) { return v; });
+    smem_fft_dit<+1>(Z, logN, nh, tw, logTW);
     const double inv = 1.0 / N;
-    const bool wrap = Pbp && 2 * (lc - 1) == N;
-    for (int e = threadIdx.x; e < cnt * 2 * pst_c; e += blockDim.x) {
-        const int it = e / (2 * pst_c), r = e - it * 2 * pst_c;
-        const int side = r / pst_c, i = r - side * pst_c;
-        const int c = 2 * (j0 + it) + side;
-        double *out = Pbc + q * Pc_q + (size_t)c * pst_c;
-        double v = 0.0;
-        if (i < lc) {
+    for (int e = threadIdx.x; e < nh * 2 * wmax; e += blockDim.x) {
+        const int it = e / (2 * wmax), r = e - it * 2 * wmax;
+        const int side = r / wmax, i = r - side * wmax;
+        const AdView &v = V[idx[it]];
+        if (i >= v.pst_c) continue;
+        double val = 0.0;
+        if (i < v.lc) {
             const double2 zv = Z[(size_t)it * N + i];
-            v = (side ? zv.y : zv.x) * inv;
-            if (wrap && i == lc - 1) {
-                const double *pb = Pbp + q * Pbp_q + (size_t)(j0 + it) * pst_p;
-                const double *Ps = Pc + q * Pc_q + (size_t)(c ^ 1) * pst_c;
-                const double top = (N < lp) ? pb[N] : 0.0;
-                v = fma(Ps[lc - 1], top - pb[0], v);
+            val = (side ? zv.y : zv.x) * inv;
+            if (v.pb && 2 * (v.lc - 1) == N && i == v.lc - 1) {
+                const double *Ps = v.PsL + (size_t)(side ^ 1) * v.pst_c;
+                const double top = (N < v.lp) ? v.pb[N] : 0.0;
+                val = fma(Ps[v.lc - 1], top - v.pb[0], val);
             }
         }
-        out[i] = v;
+        v.outL[(size_t)side * v.pst_c + i] = val;
     }
+}
+
+// single plans: pairs [bx cb, bx cb + cb) of one level
+__device__ __forceinline__ void adj_up_fused_body(const AdjUpFusedArgs &A, int bx, int q, int q0) {
+    extern __shared__ double2 sm[];
+    const int N = 1 << A.logN, h = N >> 1;
+    const int cb = vjp_cb(N);
+    const int j0 = bx * cb;
+    const int cnt = min(cb, A.npairs - j0);
+    if (cnt <= 0) return;
+    AuView *V = reinterpret_cast<AuView *>(sm + (size_t)cb * (N + h));
+    int *idx = reinterpret_cast<int *>(reinterpret_cast<char *>(V) + (size_t)cb * kAdjViewBytes);
+    for (int it = threadIdx.x; it < cnt; it += blockDim.x) au_fill(A, q, q0, j0 + it, h, V[it]);
+    __syncthreads();
+    int wmax;
+    const int nh = adj_partition(V, idx, cnt, &wmax);
+    adj_up_core(V, idx, cnt, nh, wmax, cb, A.logN, A.tw, A.logTW, sm);
+}
+
+__device__ __forceinline__ void adj_down_fused_body(const AdjDownFusedArgs &A, int bx, int q, int q0) {
+    extern __shared__ double2 sm[];
+    const int N = 1 << A.logN;
+    const int cb = vjp_cb(N);
+    const int j0 = bx * cb;
+    const int cnt = min(cb, A.npairs - j0);
+    if (cnt <= 0) return;
+    AdView *V = reinterpret_cast<AdView *>(sm + (size_t)cb * N);
+    int *idx = reinterpret_cast<int *>(reinterpret_cast<char *>(V) + (size_t)cb * kAdjViewBytes);
+    for (int it = threadIdx.x; it < cnt; it += blockDim.x) ad_fill(A, q, q0, j0 + it, N >> 1, V[it]);
+    __syncthreads();
+    int wmax;
+    const int nh = adj_partition(V, idx, cnt, &wmax);
+    adj_down_core(V, idx, nh, wmax, A.logN, A.tw, A.logTW, sm);
+}
+
+// packed work lists: slots[s] = (descriptor, pair); one transform size per launch
+__device__ __forceinline__ void adj_up_packed(const AdjUpFusedArgs *__restrict__ D, const int2 *__restrict__ slots,
+                                              int nslots, int bx, int q, int q0) {
+    extern __shared__ double2 sm[];
+    const AdjUpFusedArgs &A0 = D[slots[0].x];
+    const int N = 1 << A0.logN, h = N >> 1;
+    const int cb = vjp_cb(N);
+    const int s0 = bx * cb;
+    const int cnt = min(cb, nslots - s0);
+    if (cnt <= 0) return;
+    AuView *V = reinterpret_cast<AuView *>(sm + (size_t)cb * (N + h));
+    int *idx = reinterpret_cast<int *>(reinterpret_cast<char *>(V) + (size_t)cb * kAdjViewBytes);
+    for (int it = threadIdx.x; it < cnt; it += blockDim.x) {
+        const int2 sl = slots[s0 + it];
+        au_fill(D[sl.x], q, q0, sl.y, h, V[it]);
+    }
+    __syncthreads();
+    int wmax;
+    const int nh = adj_partition(V, idx, cnt, &wmax);
+    adj_up_core(V, idx, cnt, nh, wmax, cb, A0.logN, A0.tw, A0.logTW, sm);
+}
+
+__device__ __forceinline__ void adj_down_packed(const AdjDownFusedArgs *__restrict__ D, const int2 *__restrict__ slots,
+                                                int nslots, int bx, int q, int q0) {
+    extern __shared__ double2 sm[];
+    const AdjDownFusedArgs &A0 = D[slots[0].x];
+    const int N = 1 << A0.logN;
+    const int cb = vjp_cb(N);
+    const int s0 = bx * cb;
+    const int cnt = min(cb, nslots - s0);
+    if (cnt <= 0) return;
+    AdView *V = reinterpret_cast<AdView *>(sm + (size_t)cb * N);
+    int *idx = reinterpret_cast<int *>(reinterpret_cast<char *>(V) + (size_t)cb * kAdjViewBytes);
+    for (int it = threadIdx.x; it < cnt; it += blockDim.x) {
+        const int2 sl = slots[s0 + it];
+        ad_fill(D[sl.x], q, q0, sl.y, N >> 1, V[it]);
+    }
+    __syncthreads();
+    int wmax;
+    const int nh = adj_partition(V, idx, cnt, &wmax);
+    adj_down_core(V, idx, nh, wmax, A0.logN, A0.tw, A0.logTW, sm);
+}
+
+// ---- kernels: single plans launch (nbx, nq) grids; work lists map blocks
+// to (descriptor, block) through tab
+template <int B>
+__global__ void k_adj_leaf_up(AdjLeafUpArgs A, int q0) { adj_leaf_up_t<B>(A, blockIdx.x, blockIdx.y, q0); }
+template <int B>
+__global__ void k_adj_leaf_down(AdjLeafDownArgs A, int q0) { adj_leaf_down_t<B>(A, blockIdx.x, blockIdx.y, q0); }
+__global__ void k_adj_up_school(AdjUpSchoolArgs A, int q0) { adj_up_school_body(A, blockIdx.x, blockIdx.y, q0); }
+__global__ void k_adj_down_school(AdjDownSchoolArgs A, int q0) { adj_down_school_body(A, blockIdx.x, blockIdx.y, q0); }
+__global__ void __launch_bounds__(kVjpThreads) k_adj_up_fused(AdjUpFusedArgs A, int q0) {
+    adj_up_fused_body(A, blockIdx.x, blockIdx.y, q0);
+}
+__global__ void __launch_bounds__(kVjpThreads) k_adj_down_fused(AdjDownFusedArgs A, int q0) {
+    adj_down_fused_body(A, blockIdx.x, blockIdx.y, q0);
+}
+template <int B>
+__global__ void kw_adj_leaf_up(const AdjLeafUpArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    adj_leaf_up_t<B>(D[t.x], t.y, blockIdx.y, q0);
+}
+template <int B>
+__global__ void kw_adj_leaf_down(const AdjLeafDownArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    adj_leaf_down_t<B>(D[t.x], t.y, blockIdx.y, q0);
+}
+__global__ void kw_adj_up_school(const AdjUpSchoolArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    adj_up_school_body(D[t.x], t.y, blockIdx.y, q0);
+}
+__global__ void kw_adj_down_school(const AdjDownSchoolArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    adj_down_school_body(D[t.x], t.y, blockIdx.y, q0);
+}
+
+__global__ void __launch_bounds__(kVjpThreads)
+kw_adj_up_packed(const AdjUpFusedArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
+    adj_up_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
+}
+__global__ void __launch_bounds__(kVjpThreads)
+kw_adj_down_packed(const AdjDownFusedArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
+    adj_down_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
 }
 
 // ordered sum over nodes with a per-node stride
@@ -449,10 +676,74 @@ void vjp_set_smem_limits() {
     cudaFuncSetAttribute(k_adj_up_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vjp_up_smem(kVjpMaxN));
     cudaFuncSetAttribute(k_adj_down_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)vjp_down_smem(kVjpMaxN));
+    cudaFuncSetAttribute(kw_adj_up_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vjp_up_smem(kVjpMaxN));
+    cudaFuncSetAttribute(kw_adj_down_packed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)vjp_down_smem(kVjpMaxN));
+}
+
+// per (member, node): k_node_reduce over one member's players of a forest
+// (mem[t] = (offset, players); rows of sq players), in the same order
+__global__ void k_node_reduce_members(const longlong2 *__restrict__ mem, size_t sq, const double *__restrict__ partA,
+                                      const double *__restrict__ partB, double *__restrict__ outA,
+                                      double *__restrict__ outB, int Qs, int q0) {
+    __shared__ double sa[256], sb[256];
+    const int t = blockIdx.x, q = blockIdx.y;
+    const long off = (long)mem[t].x, n = (long)mem[t].y;
+    const double *pa = partA + (size_t)q * sq + off, *pb = partB + (size_t)q * sq + off;
+    double a = 0.0, b = 0.0;
+    for (long i = threadIdx.x; i < n; i += 256) {
+        a += pa[i];
+        b += pb[i];
+    }
+    sa[threadIdx.x] = a;
+    sb[threadIdx.x] = b;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sa[threadIdx.x] += sa[threadIdx.x + s];
+            sb[threadIdx.x] += sb[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        outA[(size_t)t * Qs + q0 + q] = sa[0];
+        outB[(size_t)t * Qs + q0 + q] = sb[0];
+    }
+}
+
+void launch_node_reduce_members(int F, const longlong2 *mem, int nq, size_t sq, const double *pA, const double *pB,
+                                double *outA, double *outB, int Qs, int q0, cudaStream_t st) {
+    if (F <= 0 || nq <= 0) return;
+    k_node_reduce_members<<<dim3(F, nq), 256, 0, st>>>(mem, sq, pA, pB, outA, outB, Qs, q0);
 }
 
 // ------------------------------------------------------------ plans
 static bool level_fused(const Level &v) { return v.fft && v.npairs > 0 && v.fftn <= kVjpMaxN && fused_ok(v.fftn); }
+
+// per-level adjoint buffers of one tournament for chunks of qc nodes: gbar
+// (shaped as g), Pbar (shaped as P) and the children's gbar spectra of
+// one-kernel FFT levels.  Returns the bytes; with base, fills b's level views.
+size_t vjp_level_layout(const Plan *p, int qc, char *base, VjpBufs *b) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
+    size_t o_gb[kMaxLevels], o_Pb[kMaxLevels], o_gsp[kMaxLevels];
+    for (int l = 0; l < p->L; ++l) {
+        const Level &lv = p->lv[l];
+        o_gb[l] = lv.g_q ? take(8 * (size_t)qc * lv.g_q) : 0;
+        o_Pb[l] = lv.P_q ? take(8 * (size_t)qc * lv.P_q) : 0;
+        o_gsp[l] = (l >= 1 && level_fused(lv)) ? take(16 * (size_t)qc * lv.spec_q) : 0;
+    }
+    if (!base) return off;
+    for (int l = 0; l < p->L; ++l) {
+        const Level &lv = p->lv[l];
+        b->gb[l] = lv.g_q ? (double *)(base + o_gb[l]) : nullptr;
+        b->gb_q[l] = lv.g_q;
+        b->gb_st[l] = lv.gst;
+        b->Pb[l] = lv.P_q ? (double *)(base + o_Pb[l]) : nullptr;
+        b->gspec[l] = o_gsp[l] ? (double2 *)(base + o_gsp[l]) : nullptr;
+    }
+    return off;
+}
 
 VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t budget) {
     // the adjoint buffers roughly double the tree's per-node memory
@@ -466,13 +757,7 @@ VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t
     auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
     const size_t o_cot = take(8 * (size_t)n), o_gs = take(8 * (size_t)n), o_gp = take(8 * (size_t)k);
     const size_t o_root = take(8 * (size_t)qc * v->kst);
-    size_t o_gb[kMaxLevels], o_Pb[kMaxLevels], o_gsp[kMaxLevels];
-    for (int l = 0; l < L; ++l) {
-        const Level &lv = p->lv[l];
-        o_gb[l] = lv.g_q ? take(8 * (size_t)qc * lv.g_q) : 0;
-        o_Pb[l] = lv.P_q ? take(8 * (size_t)qc * lv.P_q) : 0;
-        o_gsp[l] = (l >= 1 && level_fused(lv)) ? take(16 * (size_t)qc * lv.spec_q) : 0;
-    }
+    const size_t o_lv = take(vjp_level_layout(p, qc, nullptr, nullptr));
     cudaError_t e = cudaMallocAsync((void **)&v->arena, off, p->stream);
     if (e != cudaSuccess) {
         err = "VJP buffers (" + std::to_string(off) + " bytes): " + cudaGetErrorString(e);
@@ -486,12 +771,19 @@ VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t
     v->d_gradS = (double *)(A + o_gs);
     v->d_gradP = (double *)(A + o_gp);
     v->d_root = (double *)(A + o_root);
-    for (int l = 0; l < L; ++l) {
-        const Level &lv = p->lv[l];
-        v->gb[l] = lv.g_q ? (double *)(A + o_gb[l]) : nullptr;
-        v->Pb[l] = lv.P_q ? (double *)(A + o_Pb[l]) : nullptr;
-        v->gspec[l] = o_gsp[l] ? (double2 *)(A + o_gsp[l]) : nullptr;
-    }
+    VjpBufs &b = v->bufs;
+    b = VjpBufs{};
+    vjp_level_layout(p, qc, A + o_lv, &b);
+    b.root = v->d_root;
+    b.root_q = (size_t)v->kst;
+    b.kst = v->kst;
+    b.cot = v->d_cot;
+    b.a = p->d_a;
+    b.aq = (size_t)n;
+    b.contrib = p->d_contrib;
+    // the root's gbar summed over nodes: the level-0 buffer when the tree is one block
+    b.root_acc = (L == 1) ? b.gb[0] : v->d_root;
+    b.root_acc_q = (L == 1) ? p->lv[0].g_q : (size_t)v->kst;
     return v;
 }
 
@@ -501,100 +793,224 @@ void vjp_plan_destroy(VjpPlan *v) {
         cudaFreeAsync(v->arena, v->p->stream);
         cudaStreamSynchronize(v->p->stream);
     }
-    if (v->d_partA) cudaFree(v->d_partA);
+    if (v->d_partA) cudaFreeAsync(v->d_partA, v->p->stream);
     plan_destroy(v->p);
     delete v;
+}
+
+// ---- argument builders (one member level each; nbx = 0: nothing to launch)
+AdjLeafUpArgs adj_leaf_up_args(const Plan *p, const VjpBufs &b) {
+    AdjLeafUpArgs A{};
+    A.B = p->B;
+    A.n = p->n;
+    A.k = p->k;
+    A.nblocks = p->nblocks;
+    A.S = p->d_S;
+    A.node = p->d_node;
+    A.a = b.a;
+    A.aq = b.aq;
+    A.cot = b.cot;
+    A.gb0 = b.gb[0];
+    A.gb0_q = b.gb_q[0];
+    A.gst0 = b.gb_st[0];
+    A.nbx = (int)nblkv(p->nblocks, 128);
+    return A;
+}
+
+AdjLeafDownArgs adj_leaf_down_args(const Plan *p, const VjpBufs &b, double *pA, double *pB) {
+    const int L = p->L;
+    const Level *lv = p->lv;
+    AdjLeafDownArgs A{};
+    A.B = p->B;
+    A.n = p->n;
+    A.k = p->k;
+    A.S = p->d_S;
+    A.node = p->d_node;
+    A.a = b.a;
+    A.aq = b.aq;
+    A.cot = b.cot;
+    A.g0 = (L == 1) ? p->d_payout : lv[0].g;
+    A.g0_q = (L == 1) ? 0 : lv[0].g_q;
+    A.gst0 = (L == 1) ? 0 : lv[0].gst;
+    A.Pb0 = (L == 1) ? nullptr : b.Pb[0];
+    A.Pb0_q = lv[0].P_q;
+    A.pst0 = lv[0].pst;
+    A.plen0 = lv[0].plen;
+    A.contrib = b.contrib;
+    A.partA = pA;
+    A.partB = pB;
+    A.nbx = (int)nblkv(p->n, 128);
+    return A;
+}
+
+// upward step of level l (1 <= l <= L-1): the one-kernel FFT pairs and the
+// schoolbook rest (all parents, or the lone one after the pairs)
+void adj_up_args(const Plan *p, const VjpBufs &b, int l, const double2 *tw, int logTW, AdjUpFusedArgs &F,
+                 AdjUpSchoolArgs &Sa) {
+    const Level &c = p->lv[l - 1], &pl = p->lv[l];
+    const bool root = (l == p->L - 1);
+    double *out = root ? b.root : b.gb[l];
+    const size_t out_q = root ? b.root_q : b.gb_q[l];
+    const int gst_p = root ? b.kst : b.gb_st[l];
+    const int gpl = root ? p->k : pl.glen;
+    const int *zp = p->zskip ? p->d_z : nullptr;
+    F = AdjUpFusedArgs{};
+    Sa = AdjUpSchoolArgs{};
+    int j0 = 0;
+    if (level_fused(pl)) {
+        const int N = pl.fftn, logN = plan_ilog2(N), cb = vjp_cb_h(N);
+        F = AdjUpFusedArgs{b.gb[l - 1], b.gb_q[l - 1], b.gb_st[l - 1], c.glen, pl.npairs, logN, pl.spec, b.gspec[l],
+                           out, out_q, gst_p, gpl, tw, logTW, zp, pl.deg, (pl.npairs + cb - 1) / cb};
+        j0 = pl.npairs;
+    }
+    const long work = (long)(pl.nreal - j0) * gst_p;
+    if (work > 0)
+        Sa = AdjUpSchoolArgs{c.P, c.P_q, c.pst, c.plen, c.nreal, b.gb[l - 1], b.gb_q[l - 1], b.gb_st[l - 1], c.glen,
+                             out, out_q, gst_p, gpl, pl.nreal, j0, zp, pl.deg, (int)nblkv(work, 256)};
+}
+
+// downward step of level l: Pbar of level l-1
+void adj_down_args(const Plan *p, const VjpBufs &b, int l, const double2 *tw, int logTW, AdjDownFusedArgs &F,
+                   AdjDownSchoolArgs &Sa) {
+    const Level &c = p->lv[l - 1], &pl = p->lv[l];
+    const bool root = (l == p->L - 1);
+    const double *gp = root ? p->d_payout : pl.g;
+    const size_t gp_q = root ? 0 : pl.g_q;
+    const int gst_p = root ? 0 : pl.gst;
+    const int gpl = root ? p->k : pl.glen;
+    const double *Pbp = root ? nullptr : b.Pb[l];
+    const int *zp = p->zskip ? p->d_z : nullptr;
+    F = AdjDownFusedArgs{};
+    Sa = AdjDownSchoolArgs{};
+    int c0 = 0;
+    if (level_fused(pl)) {
+        const int N = pl.fftn, logN = plan_ilog2(N), cb = vjp_cb_h(N);
+        F = AdjDownFusedArgs{gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen,
+                             pl.npairs, logN, pl.spec, b.gspec[l], b.Pb[l - 1], tw, logTW, zp, pl.deg,
+                             (pl.npairs + cb - 1) / cb};
+        c0 = 2 * pl.npairs;
+    }
+    const long work = (long)(c.nreal - c0) * c.pst;
+    if (work > 0)
+        Sa = AdjDownSchoolArgs{gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen,
+                               b.gb[l - 1], b.gb_q[l - 1], b.gb_st[l - 1], c.glen, b.Pb[l - 1], c.nreal, c0, zp,
+                               c.deg, (int)nblkv(work, 256)};
+}
+
+size_t adj_up_smem(int logN) { return vjp_up_smem(1 << logN); }
+size_t adj_down_smem(int logN) { return vjp_down_smem(1 << logN); }
+
+// ---- launches: single plans
+static void launch_leaf_up(const AdjLeafUpArgs &A, int nq, int q0, cudaStream_t st) {
+    const dim3 g(A.nbx, nq);
+    switch (A.B) {
+        case 4: k_adj_leaf_up<4><<<g, 128, 0, st>>>(A, q0); break;
+        case 8: k_adj_leaf_up<8><<<g, 128, 0, st>>>(A, q0); break;
+        case 16: k_adj_leaf_up<16><<<g, 128, 0, st>>>(A, q0); break;
+        default: k_adj_leaf_up<32><<<g, 128, 0, st>>>(A, q0); break;
+    }
+}
+static void launch_leaf_down(const AdjLeafDownArgs &A, int nq, int q0, cudaStream_t st) {
+    const dim3 g(A.nbx, nq);
+    switch (A.B) {
+        case 4: k_adj_leaf_down<4><<<g, 128, 0, st>>>(A, q0); break;
+        case 8: k_adj_leaf_down<8><<<g, 128, 0, st>>>(A, q0); break;
+        case 16: k_adj_leaf_down<16><<<g, 128, 0, st>>>(A, q0); break;
+        default: k_adj_leaf_down<32><<<g, 128, 0, st>>>(A, q0); break;
+    }
+}
+
+// ---- launches: work lists (batch.cu builds the descriptors and tables); the
+// one-kernel FFT steps are packed (launch_packed_adj)
+void launch_worklist_adj(WOp op, int key, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                         cudaStream_t st) {
+    if (nctas <= 0 || nq <= 0) return;
+    const dim3 g(nctas, nq);
+    switch (op) {
+        case WOp::AdjLeafUp: {
+            const AdjLeafUpArgs *D = (const AdjLeafUpArgs *)desc;
+            switch (key) {
+                case 4: kw_adj_leaf_up<4><<<g, 128, 0, st>>>(D, tab, q0); break;
+                case 8: kw_adj_leaf_up<8><<<g, 128, 0, st>>>(D, tab, q0); break;
+                case 16: kw_adj_leaf_up<16><<<g, 128, 0, st>>>(D, tab, q0); break;
+                default: kw_adj_leaf_up<32><<<g, 128, 0, st>>>(D, tab, q0); break;
+            }
+            break;
+        }
+        case WOp::AdjLeafDown: {
+            const AdjLeafDownArgs *D = (const AdjLeafDownArgs *)desc;
+            switch (key) {
+                case 4: kw_adj_leaf_down<4><<<g, 128, 0, st>>>(D, tab, q0); break;
+                case 8: kw_adj_leaf_down<8><<<g, 128, 0, st>>>(D, tab, q0); break;
+                case 16: kw_adj_leaf_down<16><<<g, 128, 0, st>>>(D, tab, q0); break;
+                default: kw_adj_leaf_down<32><<<g, 128, 0, st>>>(D, tab, q0); break;
+            }
+            break;
+        }
+        case WOp::AdjUpSchool: kw_adj_up_school<<<g, 256, 0, st>>>((const AdjUpSchoolArgs *)desc, tab, q0); break;
+        case WOp::AdjDownSchool:
+            kw_adj_down_school<<<g, 256, 0, st>>>((const AdjDownSchoolArgs *)desc, tab, q0);
+            break;
+        default: break;
+    }
+}
+
+void launch_packed_adj(WOp op, const void *desc, const int2 *slots, int nslots, int cb, int nq, int q0, size_t smem,
+                       cudaStream_t st) {
+    if (nslots <= 0 || nq <= 0) return;
+    const dim3 g((nslots + cb - 1) / cb, nq);
+    if (op == WOp::AdjUpFused)
+        kw_adj_up_packed<<<g, kVjpThreads, smem, st>>>((const AdjUpFusedArgs *)desc, slots, nslots, q0);
+    else
+        kw_adj_down_packed<<<g, kVjpThreads, smem, st>>>((const AdjDownFusedArgs *)desc, slots, nslots, q0);
+}
+
+int adj_items_per_cta(int logN) { return vjp_cb_h(1 << logN); }
+
+void launch_accum_strided(int n, int nq, const double *src, size_t sq, double *acc, bool first, cudaStream_t st) {
+    k_accum_strided<<<nblkv(n, 256), 256, 0, st>>>(n, nq, src, sq, acc, first ? 1 : 0);
 }
 
 // adjoint passes of one chunk (the forward tree of the chunk is in place)
 static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int logTW, bool first, bool node_terms) {
     Plan *p = v->p;
     cudaStream_t st = p->stream;
-    const int L = p->L, B = p->B, n = p->n, k = p->k;
-    Level *lv = p->lv;
+    const int L = p->L, n = p->n, k = p->k;
     long &launches = p->launches;
-    const int *zp = p->zskip ? p->d_z : nullptr;   // zero-prefix pruning, as in the forward
-    const dim3 gb0((unsigned)nblkv(p->nblocks, 128), nq);
-    // gbar of the leaf blocks (for L = 1 the single block is the root)
-    switch (B) {
-        case 4: k_adj_leaf_up<4><<<gb0, 128, 0, st>>>(n, k, p->nblocks, p->d_S, p->d_node, q0, p->d_a, v->d_cot, v->gb[0], lv[0].g_q, lv[0].gst); break;
-        case 8: k_adj_leaf_up<8><<<gb0, 128, 0, st>>>(n, k, p->nblocks, p->d_S, p->d_node, q0, p->d_a, v->d_cot, v->gb[0], lv[0].g_q, lv[0].gst); break;
-        case 16: k_adj_leaf_up<16><<<gb0, 128, 0, st>>>(n, k, p->nblocks, p->d_S, p->d_node, q0, p->d_a, v->d_cot, v->gb[0], lv[0].g_q, lv[0].gst); break;
-        default: k_adj_leaf_up<32><<<gb0, 128, 0, st>>>(n, k, p->nblocks, p->d_S, p->d_node, q0, p->d_a, v->d_cot, v->gb[0], lv[0].g_q, lv[0].gst); break;
-    }
+    VjpBufs b = v->bufs;
+    launch_leaf_up(adj_leaf_up_args(p, b), nq, q0, st);   // for L = 1 the single block is the root
     ++launches;
-    // upward: gbar of every level; the root's is this chunk's dL/dpayout
-    for (int l = 1; l <= L - 1; ++l) {
-        const Level &c = lv[l - 1], &pl = lv[l];
-        const bool root = (l == L - 1);
-        double *out = root ? v->d_root : v->gb[l];
-        const size_t out_q = root ? (size_t)v->kst : pl.g_q;
-        const int gst_p = root ? v->kst : pl.gst;
-        const int gpl = root ? k : pl.glen;
-        const ZeroPrefix zpar{zp, q0, pl.deg};
-        int j0 = 0;
-        if (level_fused(pl)) {
-            const int N = pl.fftn, logN = plan_ilog2(N);
-            const int cb = vjp_cb_h(N);
-            k_adj_up_fused<<<dim3((pl.npairs + cb - 1) / cb, nq), kVjpThreads, vjp_up_smem(N), st>>>(
-                v->gb[l - 1], c.g_q, c.gst, c.glen, pl.npairs, logN, pl.spec, v->gspec[l], out, out_q, gst_p, gpl, tw,
-                logTW, zpar);
+    for (int l = 1; l <= L - 1; ++l) {   // upward: the root's gbar is this chunk's dL/dpayout
+        AdjUpFusedArgs F;
+        AdjUpSchoolArgs Sa;
+        adj_up_args(p, b, l, tw, logTW, F, Sa);
+        if (F.nbx > 0) {
+            k_adj_up_fused<<<dim3(F.nbx, nq), kVjpThreads, adj_up_smem(F.logN), st>>>(F, q0);
             ++launches;
-            j0 = pl.npairs;
         }
-        const long work = (long)(pl.nreal - j0) * gst_p;
-        if (work > 0) {
-            k_adj_up_school<<<dim3(nblkv(work, 256), nq), 256, 0, st>>>(c.P, c.P_q, c.pst, c.plen, c.nreal,
-                                                                       v->gb[l - 1], c.g_q, c.gst, c.glen, out,
-                                                                       out_q, gst_p, gpl, pl.nreal, j0, zpar);
+        if (Sa.nbx > 0) {
+            k_adj_up_school<<<dim3(Sa.nbx, nq), 256, 0, st>>>(Sa, q0);
             ++launches;
         }
     }
-    // downward: Pbar of every level below the root
-    for (int l = L - 1; l >= 1; --l) {
-        const Level &c = lv[l - 1], &pl = lv[l];
-        const bool root = (l == L - 1);
-        const double *gp = root ? p->d_payout : pl.g;
-        const size_t gp_q = root ? 0 : pl.g_q;
-        const int gst_p = root ? 0 : pl.gst;
-        const int gpl = root ? k : pl.glen;
-        const double *Pbp = root ? nullptr : v->Pb[l];
-        const ZeroPrefix zpar{zp, q0, pl.deg}, zch{zp, q0, c.deg};
-        int c0 = 0;
-        if (level_fused(pl)) {
-            const int N = pl.fftn, logN = plan_ilog2(N);
-            const int cb = vjp_cb_h(N);
-            k_adj_down_fused<<<dim3((pl.npairs + cb - 1) / cb, nq), kVjpThreads, vjp_down_smem(N), st>>>(
-                gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen, pl.npairs, logN,
-                pl.spec, v->gspec[l], v->Pb[l - 1], tw, logTW, zpar);
+    for (int l = L - 1; l >= 1; --l) {   // downward: Pbar of every level below the root
+        AdjDownFusedArgs F;
+        AdjDownSchoolArgs Sa;
+        adj_down_args(p, b, l, tw, logTW, F, Sa);
+        if (F.nbx > 0) {
+            k_adj_down_fused<<<dim3(F.nbx, nq), kVjpThreads, adj_down_smem(F.logN), st>>>(F, q0);
             ++launches;
-            c0 = 2 * pl.npairs;
         }
-        const long work = (long)(c.nreal - c0) * c.pst;
-        if (work > 0) {
-            k_adj_down_school<<<dim3(nblkv(work, 256), nq), 256, 0, st>>>(
-                gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen, v->gb[l - 1], c.g_q,
-                c.gst, c.glen, v->Pb[l - 1], c.nreal, c0, zch);
+        if (Sa.nbx > 0) {
+            k_adj_down_school<<<dim3(Sa.nbx, nq), 256, 0, st>>>(Sa, q0);
             ++launches;
         }
     }
     // per player: the node's share of dL/dS, then ordered sums over nodes
-    const double *g0 = (L == 1) ? p->d_payout : lv[0].g;
-    const size_t g0_q = (L == 1) ? 0 : lv[0].g_q;
-    const int gst0 = (L == 1) ? 0 : lv[0].gst;
-    const double *Pb0 = (L == 1) ? nullptr : v->Pb[0];
-    const dim3 gd((unsigned)nblkv(n, 128), nq);
     double *pA = node_terms ? v->d_partA : nullptr, *pB = node_terms ? v->d_partB : nullptr;
-    switch (B) {
-        case 4: k_adj_leaf_down<4><<<gd, 128, 0, st>>>(n, k, p->d_S, p->d_node, q0, p->d_a, v->d_cot, g0, g0_q, gst0, Pb0, lv[0].P_q, lv[0].pst, lv[0].plen, p->d_contrib, pA, pB); break;
-        case 8: k_adj_leaf_down<8><<<gd, 128, 0, st>>>(n, k, p->d_S, p->d_node, q0, p->d_a, v->d_cot, g0, g0_q, gst0, Pb0, lv[0].P_q, lv[0].pst, lv[0].plen, p->d_contrib, pA, pB); break;
-        case 16: k_adj_leaf_down<16><<<gd, 128, 0, st>>>(n, k, p->d_S, p->d_node, q0, p->d_a, v->d_cot, g0, g0_q, gst0, Pb0, lv[0].P_q, lv[0].pst, lv[0].plen, p->d_contrib, pA, pB); break;
-        default: k_adj_leaf_down<32><<<gd, 128, 0, st>>>(n, k, p->d_S, p->d_node, q0, p->d_a, v->d_cot, g0, g0_q, gst0, Pb0, lv[0].P_q, lv[0].pst, lv[0].plen, p->d_contrib, pA, pB); break;
-    }
-    k_accum_strided<<<nblkv(n, 256), 256, 0, st>>>(n, nq, p->d_contrib, (size_t)n, v->d_gradS, first ? 1 : 0);
-    const double *root = (L == 1) ? v->gb[0] : v->d_root;
-    const size_t root_q = (L == 1) ? lv[0].g_q : (size_t)v->kst;
-    k_accum_strided<<<nblkv(k, 256), 256, 0, st>>>(k, nq, root, root_q, v->d_gradP, first ? 1 : 0);
+    launch_leaf_down(adj_leaf_down_args(p, b, pA, pB), nq, q0, st);
+    launch_accum_strided(n, nq, p->d_contrib, (size_t)n, v->d_gradS, first, st);
+    launch_accum_strided(k, nq, b.root_acc, b.root_acc_q, v->d_gradP, first, st);
     launches += 3;
     if (node_terms) {
         k_node_reduce<<<nq, 256, 0, st>>>(n, pA, pB, v->d_nodeA + q0, v->d_nodeB + q0);
@@ -624,10 +1040,10 @@ int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot,
     const int nact = (int)(node.size() / 3);
     cudaError_t e = cudaSuccess;
     if (node_terms && (!v->d_partA || v->node_cap < nact)) {   // per-player partials and per-node sums
-        if (v->d_partA) cudaFree(v->d_partA);
+        if (v->d_partA) cudaFreeAsync(v->d_partA, p->stream);
         v->d_partA = nullptr;
         const size_t cap = std::max(nact, 1);
-        e = cudaMalloc(&v->d_partA, sizeof(double) * (2 * (size_t)p->qc * n + 2 * cap));
+        e = cudaMallocAsync((void **)&v->d_partA, sizeof(double) * (2 * (size_t)p->qc * n + 2 * cap), p->stream);
         if (e != cudaSuccess) { err = std::string("node-term buffers: ") + cudaGetErrorString(e); return -1; }
         v->d_partB = v->d_partA + (size_t)p->qc * n;
         v->d_nodeA = v->d_partB + (size_t)p->qc * n;
@@ -635,11 +1051,12 @@ int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot,
         v->node_cap = (int)cap;
     }
     if (nact > p->qmax) {
-        if (p->d_node) cudaFree(p->d_node);
+        // stream-ordered from the pool: no device-wide synchronisation
+        if (p->d_node) cudaFreeAsync(p->d_node, p->stream);
         p->d_node = nullptr;
         p->d_z = nullptr;
         const size_t nb = sizeof(double) * 3 * (size_t)std::max(nact, 1);
-        e = cudaMalloc(&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1));
+        e = cudaMallocAsync((void **)&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1), p->stream);
         if (e != cudaSuccess) { err = std::string("node buffer: ") + cudaGetErrorString(e); return -1; }
         p->d_z = (int *)((char *)p->d_node + nb);
         p->qmax = nact;

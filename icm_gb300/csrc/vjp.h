@@ -6,8 +6,120 @@
 #include <vector>
 
 #include "engine.h"
+#include "kernels.h"
 
 namespace icmg {
+
+// ---- argument blocks of the adjoint kernels (vjp.cu); one tournament level
+// each, so single plans and batch work lists run the same bodies.  zp/span:
+// zero-prefix pruning of the level the kernel decides on (null: none).
+struct AdjLeafUpArgs {
+    int B, n, k, nblocks;
+    const double *S, *node, *a;
+    size_t aq;             // per-node stride of a
+    const double *cot;
+    double *gb0;
+    size_t gb0_q;
+    int gst0;
+    int nbx;
+};
+struct AdjLeafDownArgs {
+    int B, n, k;
+    const double *S, *node, *a;
+    size_t aq;             // per-node stride of a, contrib, partA, partB
+    const double *cot, *g0;
+    size_t g0_q;
+    int gst0;
+    const double *Pb0;
+    size_t Pb0_q;
+    int pst0, plen0;
+    double *contrib, *partA, *partB;
+    int nbx;
+};
+struct AdjUpSchoolArgs {
+    const double *Pc;
+    size_t Pc_q;
+    int pst_c, lc, nreal_c;
+    const double *gbc;
+    size_t gbc_q;
+    int gst_c, glen_c;
+    double *gbp;
+    size_t gbp_q;
+    int gst_p, gpl, nreal_p, j0;
+    const int *zp;
+    long span;
+    int nbx;
+};
+struct AdjDownSchoolArgs {
+    const double *gp;
+    size_t gp_q;
+    int gst_p, gpl;
+    const double *Pbp;
+    size_t Pbp_q;
+    int pst_p, lp;
+    const double *Pc;
+    size_t Pc_q;
+    int pst_c, lc;
+    const double *gbc;
+    size_t gbc_q;
+    int gst_c, glen_c;
+    double *Pbc;
+    int nreal_c, c0;
+    const int *zp;
+    long span;
+    int nbx;
+};
+struct AdjUpFusedArgs {
+    const double *gbc;
+    size_t gbc_q;
+    int gst_c, glen_c, npairs, logN;
+    const double2 *spec;
+    double2 *gspec;
+    double *gbp;
+    size_t gbp_q;
+    int gst_p, gpl;
+    const double2 *tw;
+    int logTW;
+    const int *zp;
+    long span;
+    int nbx;
+};
+struct AdjDownFusedArgs {
+    const double *gp;
+    size_t gp_q;
+    int gst_p, gpl;
+    const double *Pbp;
+    size_t Pbp_q;
+    int pst_p, lp;
+    const double *Pc;
+    size_t Pc_q;
+    int pst_c, lc, npairs, logN;
+    const double2 *spec, *gspec;
+    double *Pbc;
+    const double2 *tw;
+    int logTW;
+    const int *zp;
+    long span;
+    int nbx;
+};
+
+// one tournament's adjoint buffers and the views of shared arrays it uses
+struct VjpBufs {
+    double *gb[kMaxLevels];      // gbar per level, shaped as g (gb[0] is the root's when L = 1)
+    size_t gb_q[kMaxLevels];
+    int gb_st[kMaxLevels];
+    double *Pb[kMaxLevels];      // Pbar per level, shaped as P
+    double2 *gspec[kMaxLevels];  // children's gbar spectra (one-kernel FFT levels)
+    double *root;                // root gbar rows (L >= 2): root + q root_q, stride kst
+    size_t root_q;
+    int kst;
+    const double *cot;           // cotangent, sorted order
+    double *a;                   // leaf factors and dL/dS shares: + q aq
+    size_t aq;
+    double *contrib;
+    const double *root_acc;      // what the payout gradient sums over nodes
+    size_t root_acc_q;
+};
 
 struct VjpPlan {
     Plan *p = nullptr;                   // coefficient-level plan (forward tree buffers)
@@ -18,9 +130,7 @@ struct VjpPlan {
     double *d_gradS = nullptr;           // dL/dS, sorted order (ordered sum over nodes)
     double *d_gradP = nullptr;           // dL/dpayout
     double *d_root = nullptr;            // [qc][kst] gbar of the root
-    double *gb[kMaxLevels] = {};         // gbar per level, shaped as g
-    double *Pb[kMaxLevels] = {};         // Pbar per level, shaped as P
-    double2 *gspec[kMaxLevels] = {};     // children's gbar spectra (one-kernel FFT levels)
+    VjpBufs bufs{};
     std::vector<double> h_cot;
     // node terms (flag 1): per-player partials [qc][n] and per-node sums
     double *d_partA = nullptr, *d_partB = nullptr, *d_nodeA = nullptr, *d_nodeB = nullptr;
@@ -46,5 +156,25 @@ int vjp_plan_run(VjpPlan *v, int Q, const double *payout, const double *cot, dou
 double node_shift_term(int Q, double Smax, const std::vector<int> &qidx, const std::vector<double> &w,
                        const std::vector<double> &A, const std::vector<double> &Bw);
 void vjp_set_smem_limits();
+
+// adjoint steps of one tournament (vjp.cu), for single plans and work lists
+size_t vjp_level_layout(const Plan *p, int qc, char *base, VjpBufs *b);
+AdjLeafUpArgs adj_leaf_up_args(const Plan *p, const VjpBufs &b);
+AdjLeafDownArgs adj_leaf_down_args(const Plan *p, const VjpBufs &b, double *pA, double *pB);
+void adj_up_args(const Plan *p, const VjpBufs &b, int l, const double2 *tw, int logTW, AdjUpFusedArgs &F,
+                 AdjUpSchoolArgs &S);
+void adj_down_args(const Plan *p, const VjpBufs &b, int l, const double2 *tw, int logTW, AdjDownFusedArgs &F,
+                   AdjDownSchoolArgs &S);
+size_t adj_up_smem(int logN);
+size_t adj_down_smem(int logN);
+void launch_worklist_adj(WOp op, int key, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                         cudaStream_t st);
+// packed one-kernel FFT adjoint steps: slots = (descriptor, pair), cb pairs per CTA
+void launch_packed_adj(WOp op, const void *desc, const int2 *slots, int nslots, int cb, int nq, int q0, size_t smem,
+                       cudaStream_t st);
+int adj_items_per_cta(int logN);
+void launch_accum_strided(int n, int nq, const double *src, size_t sq, double *acc, bool first, cudaStream_t st);
+void launch_node_reduce_members(int F, const longlong2 *mem, int nq, size_t sq, const double *pA, const double *pB,
+                                double *outA, double *outB, int Qs, int q0, cudaStream_t st);
 
 }  // namespace icmg

@@ -108,7 +108,14 @@ int icm_gb300_batch_kernel_stats(const IcmGb300Batch *batch, int i, char *name, 
  *   vjp_device_ms            CUDA-event time of the last run's kernels
  *   equity_vjp_batched       T tournaments, arrays concatenated as for
  *                            icm_gpu_equity_batched (cot and grad_S: sum n;
- *                            payout and grad_payout: sum k)                */
+ *                            payout and grad_payout: sum k); every step of
+ *                            the forward and adjoint passes of all
+ *                            tournaments is one work-list launch, and each
+ *                            tournament's gradients equal its single VJP's
+ *                            bit for bit
+ *   vjp_batch_create/run     the reusable form (an IcmGb300Batch: destroy,
+ *                            set_options, info and kernel_stats as for
+ *                            batches); runs replay one CUDA graph            */
 #define ICM_VJP_NODE_TERMS 1
 typedef struct IcmGb300Vjp IcmGb300Vjp;
 int icm_gb300_equity_vjp(int n, const double *S, int Q, const double *payout, int k,
@@ -121,6 +128,9 @@ double icm_gb300_vjp_device_ms(const IcmGb300Vjp *plan);
 int icm_gb300_equity_vjp_batched(int T, const int *n, const int *k, const double *S,
                                  const double *payout, int Q, const double *cot,
                                  double *grad_S, double *grad_payout, int flags);
+IcmGb300Batch *icm_gb300_vjp_batch_create(int T, const int *n, const int *k, const double *S);
+int icm_gb300_vjp_batch_run(IcmGb300Batch *batch, int Q, const double *payout, const double *cot,
+                            double *grad_S, double *grad_payout, int flags, IcmGpuRunStats *stats);
 
 /* Tuner table (the analogue of the reference's FFTW wisdom; icm_init(path)
  * loads it too).  Entries map a size class -- ceil(log2 n) and a k/n bucket

@@ -201,3 +201,67 @@ def test_vjp_zero_prefix_pruning(gpu_icm, wl):
         out.append(gpu_icm.equity_vjp(S, P, cot, node_terms=True))
     for a, b in zip(out[0], out[1]):
         assert np.abs(a - b).max() <= 1e-11 * np.abs(b).max()
+
+
+def _mixed_batch(rng, count=40, big=False):
+    """Uneven sizes: single-block tournaments (n <= B), schoolbook-only and
+    FFT trees, truncated and full k, wide stacks (zero-prefix pruning), and
+    optionally one tournament whose levels need the multi-pass transforms."""
+    ts, cots = [], []
+    sizes = [1, 2, 3, 5, 8, 17, 64, 100, 333, 1024, 2500, 6000] + list(rng.integers(1, 5000, count - 12))
+    if big:
+        sizes.append(70000)
+    for i, n in enumerate(sizes):
+        n = int(n)
+        k = n if i % 3 == 0 or n == 70000 else max(1, int(np.ceil(n * rng.uniform(0.02, 0.6))))
+        sig = 2.0 if i % 4 == 0 else 1.0
+        ts.append((1e4 * np.exp(sig * rng.standard_normal(n)), 0.85 ** np.arange(k)))
+        cots.append(rng.standard_normal(n))
+    return ts, cots
+
+
+@pytest.mark.parametrize("node_terms", [False, True])
+def test_batched_vjp_forest_bitwise(gpu_icm, node_terms):
+    """Every tournament's gradients from the adjoint forest equal its single VJP bit for bit."""
+    rng = np.random.default_rng(21 + node_terms)
+    ts, cots = _mixed_batch(rng, big=node_terms)
+    res = gpu_icm.equity_vjp_batched(ts, cots, Q=128, node_terms=node_terms)
+    for (S, P), c, (gS, gP) in zip(ts, cots, res):
+        a, b = gpu_icm.equity_vjp(S, P, c, Q=128, node_terms=node_terms)
+        assert np.array_equal(a, gS) and np.array_equal(b, gP), (len(S), len(P))
+
+
+@pytest.mark.parametrize("B,fft_min", [(4, 16), (16, 32)])
+def test_batched_vjp_forest_block_sizes(gpu_icm, B, fft_min):
+    gpu_icm.configure(block_size=B, fft_min_degree=fft_min)
+    rng = np.random.default_rng(B)
+    ts, cots = _mixed_batch(rng, count=20)
+    res = gpu_icm.equity_vjp_batched(ts, cots, Q=64)
+    for (S, P), c, (gS, gP) in zip(ts, cots, res):
+        a, b = gpu_icm.equity_vjp(S, P, c, Q=64)
+        assert np.array_equal(a, gS) and np.array_equal(b, gP), (len(S), len(P))
+
+
+def test_vjp_batch_reuse_graphs(gpu_icm):
+    """Reusable batched VJP: graph replays, Q changes, node-term toggles and
+    fallback members give the one-shot results; profiling changes nothing."""
+    rng = np.random.default_rng(33)
+    ts, cots = _mixed_batch(rng, count=16, big=True)
+    vb = gpu_icm.GpuVjpBatch([S for S, _ in ts], [len(P) for _, P in ts])
+    assert vb.info()["fallbacks"] == 1
+    Ps = [P for _, P in ts]
+    for Q, nt in [(64, False), (64, False), (96, True), (96, False), (64, True)]:
+        got = vb.vjp(Ps, cots, Q=Q, node_terms=nt)
+        ref = gpu_icm.equity_vjp_batched(ts, cots, Q=Q, node_terms=nt)
+        for (a, b), (c, d) in zip(got, ref):
+            assert np.array_equal(a, c) and np.array_equal(b, d)
+    vb.set_options(graphs=False, profiling=True)
+    got = vb.vjp(Ps, cots, Q=64)
+    stats = vb.kernel_stats()
+    assert any(s["name"].startswith("wl_adj_") for s in stats)
+    ref = gpu_icm.equity_vjp_batched(ts, cots, Q=64)
+    for (a, b), (c, d) in zip(got, ref):
+        assert np.array_equal(a, c) and np.array_equal(b, d)
+    with pytest.raises(gpu_icm.ICMError):
+        vb.equity(Ps)
+    vb.close()
