@@ -113,89 +113,100 @@ __device__ __forceinline__ void adj_leaf_up_t(const AdjLeafUpArgs &A, int bx, in
 #pragma unroll
     for (int m = 0; m <= B; ++m)
         if (m < gst0) out[m] = (m < pk) ? W[m] : 0.0;
+    if (A.blockW) {   // k < B: the leaf-down divisions need W beyond the truncation
+        double *wf = A.blockW + ((size_t)q * nblocks + b) * B;
+#pragma unroll
+        for (int m = 0; m < B; ++m) wf[m] = W[m];
+    }
 }
 
-// per player: Q_i and H_i by the same recurrence over the block without i,
-// then the three terms of abar_i and the node's share of dL/dS_i
+// Y = X / (a + (1 - a) x) for X of degree len (X[0..len], Y[0..len-1]):
+// the forward recurrence when a > 0.5, the backward one when a > 1e-15,
+// else a shift -- the rule of the forward pass's per-player division.
+// Constant indices keep X and Y in registers.
+template <int B>
+__device__ __forceinline__ void divide_factor(double a, const double (&X)[B + 1], int len, double (&Y)[B]) {
+    const double bb = 1.0 - a;
+    if (a > 0.5) {
+        const double ia = 1.0 / a, c = -bb * ia;
+        double y = 0.0;
+#pragma unroll
+        for (int m = 0; m < B; ++m) {
+            y = (m == 0) ? X[0] * ia : c * y + X[m] * ia;
+            Y[m] = (m < len) ? y : 0.0;
+        }
+    } else if (a > 1e-15) {
+        const double ib = 1.0 / bb, c = -a * ib;
+        double y = 0.0;
+#pragma unroll
+        for (int m = B - 1; m >= 0; --m) {
+            if (m == len - 1) y = X[m + 1] * ib;
+            else if (m < len - 1) y = c * y + X[m + 1] * ib;
+            Y[m] = (m < len) ? y : 0.0;
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < B; ++m) Y[m] = (m < len) ? X[m + 1] : 0.0;
+    }
+}
+
+// per player: Q_i = P_b / f_i and H_i = (gbar_b - c_i Q_i) / f_i (gbar_b =
+// sum_j c_j Q_j from the upward leaf step; both quotients are exact
+// polynomials), then the three terms of abar_i and the node's share of dL/dS_i
 template <int B>
 __device__ __forceinline__ void adj_leaf_down_t(const AdjLeafDownArgs &A, int bx, int q, int q0) {
-    const auto n = A.n;
-    const auto k = A.k;
-    const auto S = A.S;
-    const auto node = A.node;
-    const auto a = A.a;
-    const auto aq = A.aq;
-    const auto cot = A.cot;
-    const auto g0 = A.g0;
-    const auto g0_q = A.g0_q;
-    const auto gst0 = A.gst0;
-    const auto Pb0 = A.Pb0;
-    const auto Pb0_q = A.Pb0_q;
-    const auto pst0 = A.pst0;
-    const auto plen0 = A.plen0;
-    const auto contrib = A.contrib;
-    const auto partA = A.partA;
-    const auto partB = A.partB;
-
     const int i = bx * blockDim.x + threadIdx.x;
+    const int n = A.n;
     if (i >= n) return;
-    const double *nd = node + 3 * (q0 + q);
+    const size_t aq = A.aq;
+    const double *nd = A.node + 3 * (q0 + q);
     const double logv = nd[0], w = nd[1], iv = nd[2];
-    const int b = i / B, start = b * B, bs = min(B, n - start), pk = min(bs, k);
-    const int me = i - start;
-    const double *arow = a + (size_t)q * aq + start;
-    if (arow[me] == 0.0) {   // leaf factor 0 (S logv < -700): no share; g of its block may be pruned
-        contrib[(size_t)q * aq + i] = 0.0;
-        if (partA) {
-            partA[(size_t)q * aq + i] = 0.0;
-            partB[(size_t)q * aq + i] = 0.0;
+    const int b = i / B, start = b * B, bs = min(B, n - start), pk = min(bs, A.k);
+    const double ai = A.a[(size_t)q * aq + i];
+    if (ai == 0.0) {   // leaf factor 0 (S logv < -700): no share; g of its block may be pruned
+        A.contrib[(size_t)q * aq + i] = 0.0;
+        if (A.partA) {
+            A.partA[(size_t)q * aq + i] = 0.0;
+            A.partB[(size_t)q * aq + i] = 0.0;
         }
         return;
     }
-    double P[B], H[B];
+    const double Si = A.S[i], ci = A.cot[i];
+    const double pw = w * Si * ai * iv;
+    const bool fin = isfinite(pw);
+    const double cc = fin ? ci * pw : 0.0;   // c_i as in the upward leaf step
+    double X[B + 1], Q[B], H[B];
+    const double *Pr = A.blockP + ((size_t)q * A.nblocks + b) * (B + 1);
 #pragma unroll
-    for (int m = 0; m < B; ++m) { P[m] = 0.0; H[m] = 0.0; }
-    P[0] = 1.0;
+    for (int m = 0; m <= B; ++m) X[m] = (m <= bs) ? Pr[m] : 0.0;
+    divide_factor<B>(ai, X, bs, Q);
+    const double *Wr = A.W + q * A.Wq + (size_t)b * A.Wst;
 #pragma unroll
-    for (int j = 0; j < B; ++j) {
-        if (j >= bs || j == me) continue;
-        const double aj = arow[j], bj = 1.0 - aj;
-        double pw = w * S[start + j] * aj * iv;
-        if (!isfinite(pw)) pw = 0.0;
-        const double c = cot[start + j] * pw;
-#pragma unroll
-        for (int m = B - 1; m >= 1; --m) H[m] = fma(aj, H[m], fma(bj, H[m - 1], c * P[m]));
-        H[0] = fma(aj, H[0], c * P[0]);
-#pragma unroll
-        for (int m = B - 1; m >= 1; --m) P[m] = fma(aj, P[m], bj * P[m - 1]);
-        P[0] *= aj;
-    }
-    const double *g = g0 + q * g0_q + (size_t)b * gst0;
+    for (int m = 0; m <= B; ++m) X[m] = (m < bs) ? fma(-cc, Q[m < B ? m : 0], Wr[m]) : 0.0;
+    divide_factor<B>(ai, X, bs - 1, H);
+    const double *g = A.g0 + q * A.g0_q + (size_t)b * A.gst0;
     double inner = 0.0, bterm = 0.0;
 #pragma unroll
     for (int m = 0; m < B; ++m) {
         if (m < pk) {
             const double gm = g[m];
-            inner = fma(gm, P[m], inner);
+            inner = fma(gm, Q[m], inner);
             bterm = fma(gm, H[m] - (m ? H[m - 1] : 0.0), bterm);
         }
     }
     double cterm = 0.0;
-    if (Pb0) {
-        const double *pb = Pb0 + q * Pb0_q + (size_t)b * pst0;
+    if (A.Pb0) {
+        const double *pb = A.Pb0 + q * A.Pb0_q + (size_t)b * A.pst0;
 #pragma unroll
         for (int m = 0; m <= B; ++m)
-            if (m < plen0) cterm = fma(pb[m], (m < B ? P[m] : 0.0) - (m ? P[m - 1] : 0.0), cterm);
+            if (m < A.plen0) cterm = fma(pb[m], (m < B ? Q[m < B ? m : 0] : 0.0) - (m ? Q[m - 1] : 0.0), cterm);
     }
-    const double ai = arow[me], Si = S[i], ci = cot[i];
-    const double pw = w * Si * ai * iv;
-    const bool fin = isfinite(pw);
     const double abar = (fin ? ci * w * Si * iv * inner : 0.0) + bterm + cterm;
-    contrib[(size_t)q * aq + i] = (fin ? ci * w * ai * iv * inner : 0.0) + abar * logv * ai;
-    if (partA) {   // dL/dlogv and w dL/dw shares of this player (a = v^S, 1/v)
+    A.contrib[(size_t)q * aq + i] = (fin ? ci * w * ai * iv * inner : 0.0) + abar * logv * ai;
+    if (A.partA) {   // dL/dlogv and w dL/dw shares of this player (a = v^S, 1/v)
         const double li = fin ? ci * pw * inner : 0.0;
-        partA[(size_t)q * aq + i] = abar * Si * ai - li;
-        partB[(size_t)q * aq + i] = li;
+        A.partA[(size_t)q * aq + i] = abar * Si * ai - li;
+        A.partB[(size_t)q * aq + i] = li;
     }
 }
 
@@ -733,7 +744,9 @@ size_t vjp_level_layout(const Plan *p, int qc, char *base, VjpBufs *b) {
         o_Pb[l] = lv.P_q ? take(8 * (size_t)qc * lv.P_q) : 0;
         o_gsp[l] = (l >= 1 && level_fused(lv)) ? take(16 * (size_t)qc * lv.spec_q) : 0;
     }
+    const size_t o_bw = (p->k < p->B) ? take(8 * (size_t)qc * p->nblocks * p->B) : 0;
     if (!base) return off;
+    b->blockW = (p->k < p->B) ? (double *)(base + o_bw) : nullptr;
     for (int l = 0; l < p->L; ++l) {
         const Level &lv = p->lv[l];
         b->gb[l] = lv.g_q ? (double *)(base + o_gb[l]) : nullptr;
@@ -813,6 +826,7 @@ AdjLeafUpArgs adj_leaf_up_args(const Plan *p, const VjpBufs &b) {
     A.gb0 = b.gb[0];
     A.gb0_q = b.gb_q[0];
     A.gst0 = b.gb_st[0];
+    A.blockW = b.blockW;
     A.nbx = (int)nblkv(p->nblocks, 128);
     return A;
 }
@@ -839,6 +853,17 @@ AdjLeafDownArgs adj_leaf_down_args(const Plan *p, const VjpBufs &b, double *pA, 
     A.contrib = b.contrib;
     A.partA = pA;
     A.partB = pB;
+    A.blockP = p->d_blockP;
+    A.nblocks = p->nblocks;
+    if (b.blockW) {   // gbar of the leaf blocks in full
+        A.W = b.blockW;
+        A.Wq = (size_t)p->nblocks * p->B;
+        A.Wst = p->B;
+    } else {          // k >= B: the level-0 gbar rows hold every coefficient
+        A.W = b.gb[0];
+        A.Wq = b.gb_q[0];
+        A.Wst = b.gb_st[0];
+    }
     A.nbx = (int)nblkv(p->n, 128);
     return A;
 }

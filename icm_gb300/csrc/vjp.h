@@ -21,6 +21,7 @@ struct AdjLeafUpArgs {
     double *gb0;
     size_t gb0_q;
     int gst0;
+    double *blockW;        // [q][nblocks][B] full gbar of the blocks (k < B), or null
     int nbx;
 };
 struct AdjLeafDownArgs {
@@ -34,6 +35,11 @@ struct AdjLeafDownArgs {
     size_t Pb0_q;
     int pst0, plen0;
     double *contrib, *partA, *partB;
+    const double *blockP;  // [q][nblocks][B+1] block products from the forward leaf step
+    int nblocks;
+    const double *W;       // gbar of the blocks, all bs coefficients: + q Wq + b Wst
+    size_t Wq;
+    int Wst;
     int nbx;
 };
 struct AdjUpSchoolArgs {
@@ -119,6 +125,7 @@ struct VjpBufs {
     double *contrib;
     const double *root_acc;      // what the payout gradient sums over nodes
     size_t root_acc_q;
+    double *blockW;              // [qc][nblocks][B] full gbar of the leaf blocks when k < B
 };
 
 struct VjpPlan {
