@@ -464,7 +464,7 @@ def equity_adaptive(stacks, payouts, tol=1e-9, Q0=256, Qmax=4096):
 
 
 def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False,
-              zero_prefix=True, subtree=False):
+              zero_prefix=True, subtree=False, small_max_n=0):
     """Process-wide engine settings for plans created afterwards (0 = default).
 
     coefficient_fft_only=True keeps every FFT tree level on coefficients
@@ -472,9 +472,11 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
     computes tree nodes whose players all have a leaf factor of exactly 0 at
     a quadrature node instead of writing them as monomials / skipping them;
     subtree=True runs the leaf blocks and bottom schoolbook levels in one
-    kernel per direction (same results; measured slightly slower)."""
+    kernel per direction (same results; measured slightly slower);
+    small_max_n sets the largest n of the one-CTA-per-node small path
+    (0 = default k-dependent limit, -1 = never)."""
     cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes,
-                         0 if zero_prefix else 1, 1 if subtree else 0)
+                         0 if zero_prefix else 1, 1 if subtree else 0, int(small_max_n))
     lib().icm_gb300_set_config(ctypes.byref(cfg))
 
 

@@ -61,6 +61,7 @@ static void parallel_for(int count, F fn) {
 
 // every level of the tree runs on one-CTA kernels
 static bool fits_worklist(const Plan *p) {
+    if (p->small) return true;
     for (int l = 1; l < p->L; ++l) {
         const Level &v = p->lv[l], &c = p->lv[l - 1];
         if (v.kind == 1 && v.npairs > 0 && !fused_ok(v.fftn)) return false;
@@ -132,6 +133,12 @@ static void build_steps(Forest *f) {
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
             double fq = 0;
+            if (p->small) {   // the whole pipeline in one CTA per node
+                const SmallArgs A = small_args(p, p->d_S, p->d_node, p->d_payout, f->d_contrib + f->off[t], aq,
+                                               nullptr);
+                b.add(WOp::Small, p->B, "wl_small", A, A.smem, small_flops(p));
+                continue;
+            }
             if (p->Lf >= 1) {
                 subs[t] = sub_args(p, p->Lf, p->d_S, p->d_node, f->d_a + f->off[t], aq, nullptr,
                                    f->d_contrib + f->off[t], false, true, &subfl[t]);
@@ -149,7 +156,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &c = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
-            if (p->L >= 2 && p->lv[1].kind == 2) {
+            if (!p->small && p->L >= 2 && p->lv[1].kind == 2) {
                 double fq = 0;
                 size_t sm = 0;
                 SpecInitArgs A = spec_init_args(p->lv[0], tw, logTW, &fq, &sm);
@@ -163,6 +170,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &b = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
+            if (p->small) continue;
             Level *lv = p->lv;
             double fq = 0;
             size_t sm = 0;
@@ -207,6 +215,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &c = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
+            if (p->small) continue;
             Level *lv = p->lv;
             if (l <= p->L - 2 && lv[l].kind != 2 && lv[l + 1].kind == 2) {
                 double fq = 0;
@@ -222,6 +231,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &a = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
+            if (p->small) continue;
             Level *lv = p->lv;
             if (l > p->L - 1 || lv[l].kind != 2) continue;
             const bool root = (l == p->L - 1);
@@ -241,6 +251,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &b = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
+            if (p->small) continue;
             Level *lv = p->lv;
             if (l > p->L - 1 || l <= p->Lf) continue;
             const bool root = (l == p->L - 1);
@@ -329,6 +340,7 @@ static void build_steps(Forest *f) {
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
             const int L = p->L;
+            if (p->small) continue;
             if (p->Lf >= 1) {   // the bottom levels' propagate and the division
                 double lvl = 0.0;
                 for (int l = 1; l <= p->Lf; ++l) lvl += subfl[t].prop[l];
@@ -431,6 +443,7 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
         case WOp::FusedProp: launch_worklist_fused(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
         case WOp::SubBuild:
         case WOp::SubProp: launch_worklist_sub(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
+        case WOp::Small: launch_worklist_small(s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
         case WOp::AdjLeafUp:
         case WOp::AdjUpSchool:
         case WOp::AdjUpFused:

@@ -228,6 +228,7 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     p->tree_q_bytes = per_q;
     p->fa_elems = fa;
     p->fb_elems = fb;
+    p->small = plan_small_ok(p);
     return 0;
 }
 
@@ -306,6 +307,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     const size_t o_a = take(sizeof(double) * (size_t)qc * n);
     const size_t o_con = take(sizeof(double) * (size_t)qc * n);
     const size_t o_tree = take(plan_tree_layout(p, qc, nullptr));
+    const size_t o_cnt = take(sizeof(unsigned));
     (void)B;
 
     // stream-ordered allocation from the device's default pool, whose release
@@ -336,7 +338,10 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     p->d_a = (double *)(A + o_a);
     p->d_contrib = (double *)(A + o_con);
     plan_tree_layout(p, qc, A + o_tree);
-    e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
+    p->d_counter = (unsigned *)(A + o_cnt);
+    e = cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned), p->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_perm, p->perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
@@ -616,12 +621,29 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     p->prof.used = 0;
     p->prof.recs.clear();
     cudaEventRecord(p->ev0, p->stream);
-    for (int q0 = 0; q0 < nact; q0 += p->qc) {
-        const int nq = std::min(p->qc, nact - q0);
-        run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);
+    if (p->small && nact > 0) {   // one launch per chunk; its last CTA sums and scatters
+        SmallArgs A = small_args(p, p->d_S, p->d_node, p->d_payout, p->d_contrib, (size_t)p->n,
+                                 p->subset ? p->d_active : nullptr);
+        A.counter = p->d_counter;
+        A.acc = p->d_acc;
+        A.out = p->d_out;
+        A.perm = p->d_perm;
+        const double fq = small_flops(p);
+        for (int q0 = 0; q0 < nact; q0 += p->qc) {
+            const int nq = std::min(p->qc, nact - q0);
+            A.first = q0 == 0;
+            A.last = q0 + nq >= nact;
+            launch_small(A, nq, q0, p->stream, &p->prof, fq);
+            ++p->launches;
+        }
+    } else {
+        for (int q0 = 0; q0 < nact; q0 += p->qc) {
+            const int nq = std::min(p->qc, nact - q0);
+            run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);
+        }
+        launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
+        ++p->launches;
     }
-    launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
-    ++p->launches;
     cudaEventRecord(p->ev1, p->stream);
     e = cudaGetLastError();
     if (e == cudaSuccess)

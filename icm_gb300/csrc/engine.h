@@ -60,6 +60,7 @@ struct Plan {
     bool coeff_only = false;        // never use spectral levels
     bool zskip = true;              // prune wholly-zero tree nodes per quadrature node
     int Lf = 0;                     // bottom schoolbook levels fused into the subtree kernels
+    bool small = false;             // whole pipeline in one CTA per node (small.cu)
     std::vector<double> S_sorted;
     std::vector<int> perm;          // perm[i] = original index of sorted player i
     std::vector<int> inv_perm;
@@ -84,6 +85,7 @@ struct Plan {
     double *d_node = nullptr;       // [qmax][3]: logv, w, 1/v for the active nodes
     int *d_z = nullptr;             // [qmax] zero prefix of each active node (same allocation)
     std::vector<int> h_z;
+    unsigned *d_counter = nullptr;  // finished CTAs of a small-path launch
     uint8_t *d_active = nullptr;    // [n] sorted order (subset), or null
     uint8_t *d_hot = nullptr;       // hot bitmap, all levels
     size_t hot_off[kMaxLevels] = {};

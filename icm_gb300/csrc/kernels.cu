@@ -327,6 +327,7 @@ void fft_set_smem_limits() {
     spec_set_smem_limits();
     vjp_set_smem_limits();
     sub_set_smem_limits();
+    small_set_smem_limits();
     const int mx = kSmemFftMax * (int)sizeof(double2);
     cudaFuncSetAttribute(k_fft_smem<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft_smem<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);

@@ -229,7 +229,7 @@ FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl,
 // block within the descriptor), blockIdx.y = node within the chunk.
 enum class WOp : int {
     Leaf, SchoolBuild, SchoolProp, Divide, SpecInit, SpecBuild, Gspec, SpecProp, FusedBuild, FusedProp, SubBuild, SubProp,
-    AdjLeafUp, AdjUpSchool, AdjUpFused, AdjDownSchool, AdjDownFused, AdjLeafDown
+    AdjLeafUp, AdjUpSchool, AdjUpFused, AdjDownSchool, AdjDownFused, AdjLeafDown, Small
 };
 // B: leaf block size of the launch (Leaf and Divide lists are keyed by it)
 void launch_worklist_basic(WOp op, int B, const void *desc, const int2 *tab, int nctas, int nq, int q0,
@@ -287,6 +287,42 @@ void launch_worklist_sub(WOp op, int B, const void *desc, const int2 *tab, int n
 size_t sub_build_smem(int B);
 size_t sub_prop_smem(int B);
 void sub_set_smem_limits();
+
+// ---- small tournaments (small.cu): the whole per-node pipeline in one CTA
+constexpr size_t kSmallMaxSmem = 200 * 1024;
+constexpr int kSmallMaxLevels = 24;
+struct SmallLevel {
+    int nreal, pst, plen, gst, glen;
+    int offP;        // shared-memory offset of the level's rows (doubles)
+    int pad;
+};
+struct SmallArgs {
+    int B, n, k, nblocks, L;
+    const double *S, *node, *payout;
+    const uint8_t *active;   // subset mask (sorted order), or null
+    double *contrib;         // [q][aq] per-player shares
+    size_t aq;
+    // single solves: the last CTA sums the shares over the nodes in order
+    // (null counter: the caller sums them, as forests do)
+    unsigned *counter;
+    double *acc, *out;
+    const int *perm;
+    int first, last;
+    int q0;                  // the chunk's first node
+    int offA, offG0, offG1;  // shared-memory offsets: leaf factors, two g buffers
+    size_t smem;
+    SmallLevel lv[kSmallMaxLevels];
+    int nbx;
+};
+bool plan_small_ok(const Plan *p);
+size_t small_smem_bytes(const Plan *p);
+double small_flops(const Plan *p);   // algorithmic FP64 flops per node
+SmallArgs small_args(const Plan *p, const double *S, const double *node, const double *payout, double *contrib,
+                     size_t aq, const uint8_t *active);
+void launch_small(const SmallArgs &A, int nq, int q0, cudaStream_t st, Prof *pr, double fq);
+void launch_worklist_small(int B, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                           cudaStream_t st);
+void small_set_smem_limits();
 
 void fft_set_smem_limits();
 

@@ -36,7 +36,10 @@ int icm_last_status(void);
  *   enable_subtree    1 = run the leaf blocks and the bottom schoolbook
  *                     levels in one kernel per direction instead of level
  *                     by level (same arithmetic; measured slightly slower
- *                     on GB300, kept for comparison)                       */
+ *                     on GB300, kept for comparison)
+ *   small_max_n       largest n solved by the one-CTA-per-node small path
+ *                     (whole pipeline in shared memory, one launch per
+ *                     solve); 0 = the default k-dependent limit, -1 = never */
 typedef struct {
     int block_size;
     int fft_min_degree;
@@ -45,6 +48,7 @@ typedef struct {
     size_t max_device_bytes;
     int disable_zero_prefix;
     int enable_subtree;
+    int small_max_n;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created
