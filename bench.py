@@ -59,6 +59,10 @@ def parse():
     ap.add_argument("--batch-count", type=int, default=4096, help="tournaments in the batched leg")
     ap.add_argument("--no-vjp", action="store_true", help="skip the VJP leg")
     ap.add_argument("--no-gpu-scale", action="store_true", help="skip the n = 2^20 leg")
+    ap.add_argument("--case", default="",
+                    help="run one small workload once, untimed, and exit (for profilers): "
+                         "vjp_batch:T (T tournaments of the VJP leg's batch), batch:T (T of the batched leg), "
+                         "small:n:k (20 single solves)")
     return ap.parse_args()
 
 
@@ -80,16 +84,21 @@ class Clocks:
         self.device = device
         self.samples = []
         self.proc = None
+        self.n0, self.n1 = 0, None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.perf_counter()   # the timed region starts once sampling runs
+            while not self.samples and self.proc.poll() is None and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
+        self.n0 = len(self.samples)
         return self
 
     def _read(self):
@@ -97,7 +106,13 @@ class Clocks:
             self.samples.append([x.strip() for x in line.split(",")])
 
     def __exit__(self, *a):
+        self.n1 = len(self.samples)
         if self.proc:
+            if self.n1 == self.n0:   # region shorter than the sampling period: take the next sample
+                t0 = time.perf_counter()
+                while len(self.samples) == self.n0 and self.proc.poll() is None and time.perf_counter() - t0 < 1.0:
+                    time.sleep(0.005)
+                self.n1 = len(self.samples)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -105,18 +120,19 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
-        if not self.samples:
+        ss = self.samples[self.n0:self.n1] if self.n1 is not None else self.samples
+        if not ss:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        sm = [float(s[1]) for s in ss if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in ss if len(s) > 2 and s[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = set()
-        for s in self.samples:
+        for s in ss:
             for nm, v in zip(names, s[5:9]):
                 if v.strip().lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.samples)}
+                "reasons": sorted(reasons), "samples": len(ss)}
 
 
 def cpu_port_time(S, P, threads, q_sample):
@@ -204,6 +220,9 @@ def main():
     if L.icm_gpu_init(local) != 1:
         raise SystemExit(f"icm_gpu_init({local}) failed: {L.icm_gpu_last_error().decode()}")
     icm.init()
+    if args.case:
+        run_case(icm, W, args.case)
+        return
     if args.q_chunk:
         icm.configure(q_chunk=args.q_chunk)
     S, P, T = W.dropin(n=args.n)
@@ -454,13 +473,7 @@ def vjp_leg(icm, W, steps):
         e2e = time.perf_counter() - t0
         out[shape] = {"fwd_ms": float(np.median(fwd)), "vjp_ms": float(np.median(vjp)),
                       "ratio": float(np.median(vjp) / np.median(fwd)), "vjp_e2e_ms": e2e * 1e3}
-    rng = np.random.default_rng(77)
-    ts, cots = [], []
-    for _ in range(256):
-        n = int(rng.integers(100, 4001))
-        k = max(1, int(np.ceil(0.15 * n)))
-        ts.append((1e4 * np.exp(rng.standard_normal(n)), 0.8 ** np.arange(k)))
-        cots.append(rng.standard_normal(n))
+    ts, cots = vjp_batch_tournaments(256)
     icm.equity_vjp_batched(ts[:4], cots[:4])
     t0 = time.perf_counter()
     icm.equity_vjp_batched(ts, cots)
@@ -486,6 +499,45 @@ def vjp_leg(icm, W, steps):
                           "config": "256 tournaments, n uniform [100,4000], k=ceil(0.15n), payout 0.8^j; one-shot "
                                     "wall time, and device time of resident batches (graph replay)"}
     return out
+
+
+def vjp_batch_tournaments(count, seed=77):
+    """The VJP leg's batch: n uniform in [100, 4000], k = ceil(0.15 n),
+    1e4 lognormal(0, 1) stacks, payouts 0.8^j, N(0, 1) cotangents."""
+    rng = np.random.default_rng(seed)
+    ts, cots = [], []
+    for _ in range(count):
+        n = int(rng.integers(100, 4001))
+        k = max(1, int(np.ceil(0.15 * n)))
+        ts.append((1e4 * np.exp(rng.standard_normal(n)), 0.8 ** np.arange(k)))
+        cots.append(rng.standard_normal(n))
+    return ts, cots
+
+
+def run_case(icm, W, case):
+    """One untimed run of a named small workload (the target of an ncu capture)."""
+    kind, *rest = case.split(":")
+    if kind == "vjp_batch":
+        ts, cots = vjp_batch_tournaments(int(rest[0]))
+        vb = icm.GpuVjpBatch([S for S, _ in ts], [len(P) for _, P in ts])
+        vb.set_options(graphs=False)
+        vb.vjp([P for _, P in ts], cots)
+        vb.close()
+    elif kind == "batch":
+        ts = W.batched(count=int(rest[0]))
+        b = icm.GpuBatch([S for S, _ in ts], [len(P) for _, P in ts])
+        b.set_options(graphs=False)
+        b.equity([P for _, P in ts])
+        b.close()
+    elif kind == "small":
+        n, k = int(rest[0]), int(rest[1])
+        rng = np.random.default_rng(n)
+        S, P = 1e4 * np.exp(rng.standard_normal(n)), 0.8 ** np.arange(k)
+        for _ in range(20):
+            icm.gpu_equity(S, P)
+    else:
+        raise SystemExit(f"unknown case {case!r}")
+    print(json.dumps({"case": case, "status": "ok"}))
 
 
 def traffic_for(kernel: str):
