@@ -61,7 +61,7 @@ static void parallel_for(int count, F fn) {
 
 // every level of the tree runs on one-CTA kernels
 static bool fits_worklist(const Plan *p) {
-    if (p->small) return true;
+    if (p->small || p->linear) return true;
     for (int l = 1; l < p->L; ++l) {
         const Level &v = p->lv[l], &c = p->lv[l - 1];
         if (v.kind == 1 && v.npairs > 0 && !fused_ok(v.fftn)) return false;
@@ -139,6 +139,12 @@ static void build_steps(Forest *f) {
                 b.add(WOp::Small, p->B, "wl_small", A, A.smem, small_flops(p));
                 continue;
             }
+            if (p->linear) {   // one warp per node
+                const LinearArgs A = linear_args(p, p->d_S, p->d_node, p->d_payout, f->d_a + f->off[t],
+                                                 f->d_contrib + f->off[t], aq, nullptr, p->d_ck, zpre(p));
+                b.add(WOp::Linear, A.R, "wl_linear", A, 0, linear_flops(p));
+                continue;
+            }
             if (p->Lf >= 1) {
                 subs[t] = sub_args(p, p->Lf, p->d_S, p->d_node, f->d_a + f->off[t], aq, nullptr,
                                    f->d_contrib + f->off[t], false, true, &subfl[t]);
@@ -156,7 +162,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &c = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
-            if (!p->small && p->L >= 2 && p->lv[1].kind == 2) {
+            if (!p->small && !p->linear && p->L >= 2 && p->lv[1].kind == 2) {
                 double fq = 0;
                 size_t sm = 0;
                 SpecInitArgs A = spec_init_args(p->lv[0], tw, logTW, &fq, &sm);
@@ -170,7 +176,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &b = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
-            if (p->small) continue;
+            if (p->small || p->linear) continue;
             Level *lv = p->lv;
             double fq = 0;
             size_t sm = 0;
@@ -215,7 +221,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &c = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
-            if (p->small) continue;
+            if (p->small || p->linear) continue;
             Level *lv = p->lv;
             if (l <= p->L - 2 && lv[l].kind != 2 && lv[l + 1].kind == 2) {
                 double fq = 0;
@@ -231,7 +237,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &a = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
-            if (p->small) continue;
+            if (p->small || p->linear) continue;
             Level *lv = p->lv;
             if (l > p->L - 1 || lv[l].kind != 2) continue;
             const bool root = (l == p->L - 1);
@@ -251,7 +257,7 @@ static void build_steps(Forest *f) {
         PhaseBuilder &b = phase();
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
-            if (p->small) continue;
+            if (p->small || p->linear) continue;
             Level *lv = p->lv;
             if (l > p->L - 1 || l <= p->Lf) continue;
             const bool root = (l == p->L - 1);
@@ -340,7 +346,7 @@ static void build_steps(Forest *f) {
         for (int t = 0; t < T; ++t) {
             Plan *p = f->tr[t];
             const int L = p->L;
-            if (p->small) continue;
+            if (p->small || p->linear) continue;
             if (p->Lf >= 1) {   // the bottom levels' propagate and the division
                 double lvl = 0.0;
                 for (int l = 1; l <= p->Lf; ++l) lvl += subfl[t].prop[l];
@@ -444,6 +450,7 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
         case WOp::SubBuild:
         case WOp::SubProp: launch_worklist_sub(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
         case WOp::Small: launch_worklist_small(s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
+        case WOp::Linear: launch_worklist_linear(s.key, s.d_desc, s.d_tab, nctas, qn, q0, f->stream); break;
         case WOp::AdjLeafUp:
         case WOp::AdjUpSchool:
         case WOp::AdjUpFused:
@@ -576,7 +583,8 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
 
     // node chunk from the memory budget
     size_t per_q = (size_t)2 * f->Ntot * 8 + 1024;
-    for (Plan *p : f->tr) per_q += p->tree_q_bytes;
+    for (Plan *p : f->tr)   // linear members keep checkpoints instead of a tree
+        per_q += p->linear ? linear_ck_per_node(p->n, p->k) * sizeof(double) : p->tree_q_bytes;
     if (vjp) {   // adjoint buffers, the roots' gbar rows, node-term partials
         per_q += (size_t)f->Rtot * 8 + (size_t)2 * f->Ntot * 8;
         for (Plan *p : f->tr) per_q += vjp_level_layout(p, 1, nullptr, nullptr);
@@ -597,7 +605,11 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
     const size_t o_acc = take(8 * Nt), o_out = take(8 * Nt);
     const size_t o_a = take(8 * Nt * qc), o_con = take(8 * Nt * qc);
     std::vector<size_t> o_tree(F), o_adj(F);
-    for (int i = 0; i < F; ++i) o_tree[i] = take(plan_tree_layout(f->tr[i], qc, nullptr));
+    for (int i = 0; i < F; ++i) {
+        Plan *p = f->tr[i];
+        o_tree[i] = p->linear ? take(sizeof(double) * (size_t)qc * linear_ck_per_node(p->n, p->k))
+                              : take(plan_tree_layout(p, qc, nullptr));
+    }
     size_t o_cot = 0, o_gp = 0, o_root = 0, o_mem = 0;
     if (vjp) {
         o_cot = take(8 * Nt);
@@ -626,7 +638,8 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
     int logNeed = 12;
     for (int i = 0; i < F; ++i) {
         Plan *p = f->tr[i];
-        plan_tree_layout(p, qc, A + o_tree[i]);
+        if (p->linear) p->d_ck = (double *)(A + o_tree[i]);
+        else plan_tree_layout(p, qc, A + o_tree[i]);
         p->qc = qc;
         p->d_S = f->d_S + f->off[i];
         p->d_payout = f->d_payout + f->poff[i];

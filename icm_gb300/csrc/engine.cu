@@ -228,7 +228,11 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     p->tree_q_bytes = per_q;
     p->fa_elems = fa;
     p->fb_elems = fb;
-    p->small = plan_small_ok(p);
+    // engine: the small path, the linear engine or the tree
+    const int eng = g_config.engine;
+    p->small = eng != 2 && plan_small_ok(p);
+    p->linear = !p->coeff_only && !p->small && k <= kLinearMaxK &&
+                (eng == 2 || (eng == 0 && plan_linear_auto(n, k)));
     return 0;
 }
 
@@ -284,7 +288,8 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     if (plan_geometry(p, n, S, k, err) != 0) { delete p; return nullptr; }
     const int B = p->B;
     const int Nt = 1 << (p->L - 1);
-    const size_t per_q = (size_t)((double)(p->tree_q_bytes + (size_t)2 * n * 8 + 1024) * q_bytes_scale);
+    const size_t tree_q = p->linear ? linear_ck_per_node(n, k) * sizeof(double) : p->tree_q_bytes;
+    const size_t per_q = (size_t)((double)(tree_q + (size_t)2 * n * 8 + 1024) * q_bytes_scale);
 
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
@@ -306,7 +311,9 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     const size_t o_hot = take(hot_total);
     const size_t o_a = take(sizeof(double) * (size_t)qc * n);
     const size_t o_con = take(sizeof(double) * (size_t)qc * n);
-    const size_t o_tree = take(plan_tree_layout(p, qc, nullptr));
+    // the linear engine keeps checkpoints instead of a tree
+    const size_t o_tree = p->linear ? 0 : take(plan_tree_layout(p, qc, nullptr));
+    const size_t o_ck = p->linear ? take(sizeof(double) * (size_t)qc * linear_ck_per_node(n, k)) : 0;
     const size_t o_cnt = take(sizeof(unsigned));
     (void)B;
 
@@ -337,7 +344,8 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     p->d_hot = (uint8_t *)(A + o_hot);
     p->d_a = (double *)(A + o_a);
     p->d_contrib = (double *)(A + o_con);
-    plan_tree_layout(p, qc, A + o_tree);
+    if (p->linear) p->d_ck = (double *)(A + o_ck);
+    else plan_tree_layout(p, qc, A + o_tree);
     p->d_counter = (unsigned *)(A + o_cnt);
     e = cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned), p->stream);
     if (e == cudaSuccess)
@@ -636,6 +644,18 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
             launch_small(A, nq, q0, p->stream, &p->prof, fq);
             ++p->launches;
         }
+    } else if (p->linear) {   // one warp per node, then the ordered sum
+        const LinearArgs A = linear_args(p, p->d_S, p->d_node, p->d_payout, p->d_a, p->d_contrib, (size_t)p->n,
+                                         p->subset ? p->d_active : nullptr, p->d_ck, p->zskip ? p->d_z : nullptr);
+        const double fq = linear_flops(p);
+        for (int q0 = 0; q0 < nact; q0 += p->qc) {
+            const int nq = std::min(p->qc, nact - q0);
+            launch_linear(A, nq, q0, p->stream, &p->prof, fq);
+            launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, q0 == 0 ? 1 : 0, p->stream, &p->prof);
+            p->launches += 2;
+        }
+        launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
+        ++p->launches;
     } else {
         for (int q0 = 0; q0 < nact; q0 += p->qc) {
             const int nq = std::min(p->qc, nact - q0);

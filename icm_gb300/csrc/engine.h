@@ -61,6 +61,8 @@ struct Plan {
     bool zskip = true;              // prune wholly-zero tree nodes per quadrature node
     int Lf = 0;                     // bottom schoolbook levels fused into the subtree kernels
     bool small = false;             // whole pipeline in one CTA per node (small.cu)
+    bool linear = false;            // the linear engine (linear.cu)
+    double *d_ck = nullptr;         // [qc][ck per node] linear-engine checkpoints
     std::vector<double> S_sorted;
     std::vector<int> perm;          // perm[i] = original index of sorted player i
     std::vector<int> inv_perm;

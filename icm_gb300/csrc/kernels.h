@@ -229,7 +229,7 @@ FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl,
 // block within the descriptor), blockIdx.y = node within the chunk.
 enum class WOp : int {
     Leaf, SchoolBuild, SchoolProp, Divide, SpecInit, SpecBuild, Gspec, SpecProp, FusedBuild, FusedProp, SubBuild, SubProp,
-    AdjLeafUp, AdjUpSchool, AdjUpFused, AdjDownSchool, AdjDownFused, AdjLeafDown, Small
+    AdjLeafUp, AdjUpSchool, AdjUpFused, AdjDownSchool, AdjDownFused, AdjLeafDown, Small, Linear
 };
 // B: leaf block size of the launch (Leaf and Divide lists are keyed by it)
 void launch_worklist_basic(WOp op, int B, const void *desc, const int2 *tab, int nctas, int nq, int q0,
@@ -323,6 +323,29 @@ void launch_small(const SmallArgs &A, int nq, int q0, cudaStream_t st, Prof *pr,
 void launch_worklist_small(int B, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
                            cudaStream_t st);
 void small_set_smem_limits();
+
+// ---- linear engine (linear.cu): one warp per (tournament, node), k <= 256
+constexpr int kLinearMaxK = 256;
+struct LinearArgs {
+    int R, n, k;
+    const double *S, *node, *payout;
+    double *a;               // [q][aq] leaf factors (kept for the backward replays)
+    double *contrib;         // [q][aq] per-player shares
+    size_t aq;
+    const uint8_t *active;   // subset mask (sorted order), or null
+    double *ck;              // [q][ck_q] checkpoints of the forward sweep
+    size_t ck_q;
+    const int *zp;           // zero prefix per node (q0-based table), or null
+    int nbx;
+};
+int linear_lanes(int k);   // R: coefficients per lane
+bool plan_linear_auto(int n, int k);
+size_t linear_ck_per_node(int n, int k);
+LinearArgs linear_args(const Plan *p, const double *S, const double *node, const double *payout, double *a,
+                       double *contrib, size_t aq, const uint8_t *active, double *ck, const int *zp);
+double linear_flops(const Plan *p);
+void launch_linear(const LinearArgs &A, int nq, int q0, cudaStream_t st, Prof *pr, double fq);
+void launch_worklist_linear(int R, const void *desc, const int2 *tab, int nctas, int nq, int q0, cudaStream_t st);
 
 void fft_set_smem_limits();
 

@@ -39,7 +39,10 @@ int icm_last_status(void);
  *                     on GB300, kept for comparison)
  *   small_max_n       largest n solved by the one-CTA-per-node small path
  *                     (whole pipeline in shared memory, one launch per
- *                     solve); 0 = the default k-dependent limit, -1 = never */
+ *                     solve); 0 = the default k-dependent limit, -1 = never
+ *   engine            0 = choose per (n, k); 1 = the tree engine (and the
+ *                     small path); 2 = the linear engine (one warp per node,
+ *                     O(n k); k <= 256, larger k uses the tree)          */
 typedef struct {
     int block_size;
     int fft_min_degree;
@@ -49,6 +52,7 @@ typedef struct {
     int disable_zero_prefix;
     int enable_subtree;
     int small_max_n;
+    int engine;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created
