@@ -27,7 +27,7 @@ from ._lib import (IcmGb300Config, IcmGpuOptions, IcmGpuPlanSummary, IcmGpuRunSt
                    library_path)
 
 __all__ = ["init", "equity", "equity_subset", "ICMError", "gpu_equity", "gpu_equity_subset", "GpuPlan",
-           "equity_batched", "GpuBatch", "GpuVjpBatch", "equity_vjp", "equity_vjp_batched", "VjpPlan", "autotune", "tuner_load",
+           "equity_batched", "GpuBatch", "GpuVjpBatch", "player_order", "equity_vjp", "equity_vjp_batched", "VjpPlan", "autotune", "tuner_load",
            "tuner_save", "tuner_clear", "tuner_lookup", "equity_adaptive", "configure", "measure_fp64_gflops", "measure_hbm_gbps", "library_path",
            "last_launch_count"]
 
@@ -502,3 +502,13 @@ def measure_hbm_gbps():
 
 def last_launch_count():
     return int(lib().icm_gpu_last_launch_count())
+
+
+def player_order(stacks):
+    """The engine's player order (host only): indices by stack, descending,
+    ties by index."""
+    S = _to_double_array(stacks, "stacks")
+    perm = np.zeros(len(S), dtype=np.int32)
+    if len(S) == 0 or lib().icm_gb300_player_order(len(S), _d(S), perm.ctypes.data_as(_ip)) != 0:
+        raise ICMError(lib().icm_gpu_last_error().decode(errors="replace") if len(S) else "empty stacks")
+    return perm

@@ -73,6 +73,7 @@ SIGNATURES = {
     "icm_gpu_measure_fused_r2c_pair_ns": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "icm_last_status": (ctypes.c_int, []),
     "icm_gb300_set_config": (ctypes.c_int, [ctypes.POINTER(IcmGb300Config)]),
+    "icm_gb300_player_order": (ctypes.c_int, [ctypes.c_int, _dp, _ip]),
     "icm_gpu_equity_batched": (ctypes.c_int, [ctypes.c_int, _ip, _ip, _dp, _dp, ctypes.c_int, _dp,
                                               ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gpu_measure_fp64_gflops": (ctypes.c_int, [_dp]),

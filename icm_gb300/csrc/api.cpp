@@ -3,6 +3,7 @@
 // additions in icm_gb300.h.  Plain pointers and sizes only.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -275,6 +276,19 @@ int icm_gpu_measure_fused_r2c_pair_ns(int fft_n, int batch, int quick, double *b
 
 // ------------------------------------------------------------ icm_gb300.h
 int icm_last_status(void) { return t_last_status; }
+
+int icm_gb300_player_order(int n, const double *S, int *perm) {
+    if (n < 1 || !S || !perm) { set_error("icm_gb300_player_order: invalid arguments"); return -1; }
+    for (int i = 0; i < n; ++i)
+        if (!(S[i] > 0.0) || !std::isfinite(S[i])) {
+            set_error("icm_gb300_player_order: stacks must be finite and positive");
+            return -1;
+        }
+    std::vector<int> p;
+    sort_players_desc(S, n, p);
+    std::copy(p.begin(), p.end(), perm);
+    return 0;
+}
 
 int icm_gb300_set_config(const IcmGb300Config *cfg) {
     if (cfg) g_config = *cfg;

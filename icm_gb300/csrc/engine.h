@@ -118,6 +118,8 @@ struct Plan {
 // lifecycle (engine.cu)
 // geometry only: validation, sort, levels, per-node element counts
 int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err);
+// player order: stacks descending, ties by index
+void sort_players_desc(const double *S, int n, std::vector<int> &perm);
 // tree buffers for chunks of qc nodes from `base` (nullptr: size only)
 size_t plan_tree_layout(Plan *p, int qc, char *base);
 // coeff_only: every FFT level on coefficients (the adjoint passes need the

@@ -59,6 +59,12 @@ typedef struct {
  * afterwards (NULL restores the defaults).  Returns 0. */
 int icm_gb300_set_config(const IcmGb300Config *cfg);
 
+/* The engine's player order (host only, no device needed): perm[r] is the
+ * index of the player of rank r by stack, descending, ties by index (the
+ * reference's GPU order, src/gpu/gpu_plan.cu:405-409).  Returns 0, or -1 for
+ * invalid arguments (n < 1, a stack not finite and positive). */
+int icm_gb300_player_order(int n, const double *S, int *perm);
+
 /* Batched tournaments: T independent tournaments of uneven size.
  *   n[t], k[t]        players and paid places of tournament t
  *   S, payout         concatenated stacks (sum n) and payouts (sum k)

@@ -135,3 +135,20 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.delenv("ICM_GB300_LIB")
     monkeypatch.setattr(L, "_lib", None)
     importlib.reload(L)
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 4096, 4097, 70000, 300000])
+def test_player_order_host(built_lib, n):
+    """The engine's player order (host only): stacks descending, ties by index,
+    for the comparison sort (n <= 4096), the radix sort on one thread and on
+    several (n >= 32768)."""
+    import icm_gb300 as icm
+    rng = np.random.default_rng(n)
+    S = rng.integers(1, 50, n).astype(float)                    # many ties
+    if n > 3:
+        S[: n // 3] = 10.0 ** rng.uniform(-300, 300, n // 3)   # extreme magnitudes
+        S[1] = np.nextafter(S[0], 0.0)                          # neighbours in the last bit
+    ref = np.lexsort((np.arange(n), -S))
+    assert np.array_equal(icm.player_order(S), ref)
+    with pytest.raises(icm.ICMError):
+        icm.player_order(np.array([1.0, -2.0]))
