@@ -464,7 +464,7 @@ def equity_adaptive(stacks, payouts, tol=1e-9, Q0=256, Qmax=4096):
 
 
 def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False,
-              zero_prefix=True, subtree=False, small_max_n=0, engine="auto"):
+              zero_prefix=True, subtree=False, small_max_n=0, engine="auto", quadrature="erfc"):
     """Process-wide engine settings for plans created afterwards (0 = default).
 
     coefficient_fft_only=True keeps every FFT tree level on coefficients
@@ -475,12 +475,17 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
     kernel per direction (same results; measured slightly slower);
     small_max_n sets the largest n of the one-CTA-per-node small path
     (0 = default k-dependent limit, -1 = never); engine is "auto", "tree"
-    or "linear" (the O(n k) linear engine, one warp per node, k <= 256)."""
+    or "linear" (the O(n k) linear engine, one warp per node, k <= 256);
+    quadrature is "erfc" (the reference's erfc-trapezoid rule) or "tanh_sinh"."""
     engines = {"auto": 0, "tree": 1, "linear": 2}
+    rules = {"erfc": 0, "tanh_sinh": 1}
     if engine not in engines:
         raise ValueError(f"engine must be one of {sorted(engines)}, got {engine!r}")
+    if quadrature not in rules:
+        raise ValueError(f"quadrature must be one of {sorted(rules)}, got {quadrature!r}")
     cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes,
-                         0 if zero_prefix else 1, 1 if subtree else 0, int(small_max_n), engines[engine])
+                         0 if zero_prefix else 1, 1 if subtree else 0, int(small_max_n), engines[engine],
+                         rules[quadrature])
     lib().icm_gb300_set_config(ctypes.byref(cfg))
 
 

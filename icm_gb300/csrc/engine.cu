@@ -31,7 +31,33 @@ static double log_Phi(double y) {
     return std::log(std::erfc(-y / std::sqrt(2.0)) / 2.0);
 }
 
+// tanh-sinh rule on v in (0, 1) (the reference's accuracy study,
+// tools/accuracy_bench.c:52-90, offered behind IcmGb300Config.quadrature):
+// v = (1 + tanh t) / 2 with t = pi/2 sinh x, x = -5.5 + q h on [-5.5, 5.5],
+// w = h (pi/2) cosh x / (2 cosh^2 t).  Here log v = -log1p(e^{-2t}) and
+// 1 / (2 cosh^2 t) = 2 e^{-2|t|} / (1 + e^{-2|t|})^2, so both ends keep full
+// precision; nodes whose weight underflows get w = 0 (skipped).  The nodes do
+// not depend on the stacks.
+static void make_nodes_tanh_sinh(int Q, std::vector<double> &logv, std::vector<double> &w) {
+    const double x_max = 5.5;
+    const double h = 2.0 * x_max / (Q - 1);
+    logv.resize(Q);
+    w.resize(Q);
+    for (int q = 0; q < Q; ++q) {
+        const double x = -x_max + q * h;
+        const double t = 0.5 * M_PI * std::sinh(x);
+        const double e = std::exp(-2.0 * std::fabs(t));
+        logv[q] = (t >= 0) ? -std::log1p(e) : 2.0 * t - std::log1p(e);
+        w[q] = h * 0.5 * M_PI * std::cosh(x) * (2.0 * e / ((1.0 + e) * (1.0 + e)));
+        if (!(logv[q] < 0.0) || !std::isfinite(logv[q])) w[q] = 0.0;
+    }
+}
+
 void make_nodes(int Q, double Smax, std::vector<double> &logv, std::vector<double> &w) {
+    if (g_config.quadrature == 1) {
+        make_nodes_tanh_sinh(Q, logv, w);
+        return;
+    }
     const double y_lo = -7.7;
     double y_hi = std::sqrt(2.0) * std::sqrt(std::log(Smax) + 25.0);
     if (y_hi < 6.5) y_hi = 6.5;

@@ -663,6 +663,7 @@ __global__ void k_node_reduce(int n, const double *__restrict__ partA, const dou
 // (the largest stack is the first player in sorted order; ties go to it)
 double node_shift_term(int Q, double Smax, const std::vector<int> &qidx, const std::vector<double> &w,
                        const std::vector<double> &A, const std::vector<double> &Bw) {
+    if (g_config.quadrature == 1) return 0.0;   // tanh-sinh nodes do not depend on the stacks
     const double y_lo = -7.7;
     const double r = std::sqrt(2.0) * std::sqrt(std::log(Smax) + 25.0);
     if (!(r > 6.5) || Q < 2) return 0.0;

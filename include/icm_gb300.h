@@ -42,7 +42,10 @@ int icm_last_status(void);
  *                     solve); 0 = the default k-dependent limit, -1 = never
  *   engine            0 = choose per (n, k); 1 = the tree engine (and the
  *                     small path); 2 = the linear engine (one warp per node,
- *                     O(n k); k <= 256, larger k uses the tree)          */
+ *                     O(n k); k <= 256, larger k uses the tree)
+ *   quadrature        0 = the reference's erfc-trapezoid rule; 1 = tanh-sinh
+ *                     on v in (0, 1) (nodes independent of the stacks; less
+ *                     accurate for widely spread stacks)                  */
 typedef struct {
     int block_size;
     int fft_min_degree;
@@ -53,6 +56,7 @@ typedef struct {
     int enable_subtree;
     int small_max_n;
     int engine;
+    int quadrature;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created
