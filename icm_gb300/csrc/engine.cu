@@ -696,6 +696,46 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     p->launches += 2;
 }
 
+// the kernel sequence of one run over nact active nodes (all chunks, the
+// ordered node sums and the scatter)
+static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
+    if (p->small && nact > 0) {   // one launch per chunk; its last CTA sums and scatters
+        SmallArgs A = small_args(p, p->d_S, p->d_node, p->d_payout, p->d_contrib, (size_t)p->n,
+                                 p->subset ? p->d_active : nullptr);
+        A.counter = p->d_counter;
+        A.acc = p->d_acc;
+        A.out = p->d_out;
+        A.perm = p->d_perm;
+        const double fq = small_flops(p);
+        for (int q0 = 0; q0 < nact; q0 += p->qc) {
+            const int nq = std::min(p->qc, nact - q0);
+            A.first = q0 == 0;
+            A.last = q0 + nq >= nact;
+            launch_small(A, nq, q0, p->stream, &p->prof, fq);
+            ++p->launches;
+        }
+    } else if (p->linear) {   // one warp per node, then the ordered sum
+        const LinearArgs A = linear_args(p, p->d_S, p->d_node, p->d_payout, p->d_a, p->d_contrib, (size_t)p->n,
+                                         p->subset ? p->d_active : nullptr, p->d_ck, p->zskip ? p->d_z : nullptr);
+        const double fq = linear_flops(p);
+        for (int q0 = 0; q0 < nact; q0 += p->qc) {
+            const int nq = std::min(p->qc, nact - q0);
+            launch_linear(A, nq, q0, p->stream, &p->prof, fq);
+            launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, q0 == 0 ? 1 : 0, p->stream, &p->prof);
+            p->launches += 2;
+        }
+        launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
+        ++p->launches;
+    } else {
+        for (int q0 = 0; q0 < nact; q0 += p->qc) {
+            const int nq = std::min(p->qc, nact - q0);
+            run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);
+        }
+        launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
+        ++p->launches;
+    }
+}
+
 int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats, std::string &err) {
     if (!p || Q < 1 || !payout || !equity) { err = "invalid arguments"; return -1; }
     const double t0 = now_ns();
@@ -746,41 +786,35 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     if (!p->ev0) { cudaEventCreate(&p->ev0); cudaEventCreate(&p->ev1); }
     p->prof.used = 0;
     p->prof.recs.clear();
+    // enable_graphs: the sequence is captured once per node count (and node
+    // buffer) and replayed; kernels read payouts and nodes from the plan's
+    // buffers, which every run refills before the launch
+    const bool use_graph = p->opts.enable_graphs == 1 && !p->prof.on && nact > 0;
+    if (use_graph && (!p->graph || p->graph_nq != nact || p->graph_node != p->d_node)) {
+        if (p->graph) cudaGraphExecDestroy(p->graph);
+        p->graph = nullptr;
+        cudaGraph_t g = nullptr;
+        const long l0 = p->launches;
+        e = cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_plan(p, nact, tw, logTW);
+            e = cudaStreamEndCapture(p->stream, &g);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return -1; }
+        p->graph_nq = nact;
+        p->graph_node = p->d_node;
+        p->graph_launches = p->launches - l0;
+        p->launches = l0;
+    }
     cudaEventRecord(p->ev0, p->stream);
-    if (p->small && nact > 0) {   // one launch per chunk; its last CTA sums and scatters
-        SmallArgs A = small_args(p, p->d_S, p->d_node, p->d_payout, p->d_contrib, (size_t)p->n,
-                                 p->subset ? p->d_active : nullptr);
-        A.counter = p->d_counter;
-        A.acc = p->d_acc;
-        A.out = p->d_out;
-        A.perm = p->d_perm;
-        const double fq = small_flops(p);
-        for (int q0 = 0; q0 < nact; q0 += p->qc) {
-            const int nq = std::min(p->qc, nact - q0);
-            A.first = q0 == 0;
-            A.last = q0 + nq >= nact;
-            launch_small(A, nq, q0, p->stream, &p->prof, fq);
-            ++p->launches;
-        }
-    } else if (p->linear) {   // one warp per node, then the ordered sum
-        const LinearArgs A = linear_args(p, p->d_S, p->d_node, p->d_payout, p->d_a, p->d_contrib, (size_t)p->n,
-                                         p->subset ? p->d_active : nullptr, p->d_ck, p->zskip ? p->d_z : nullptr);
-        const double fq = linear_flops(p);
-        for (int q0 = 0; q0 < nact; q0 += p->qc) {
-            const int nq = std::min(p->qc, nact - q0);
-            launch_linear(A, nq, q0, p->stream, &p->prof, fq);
-            launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, q0 == 0 ? 1 : 0, p->stream, &p->prof);
-            p->launches += 2;
-        }
-        launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
-        ++p->launches;
+    if (use_graph) {
+        e = cudaGraphLaunch(p->graph, p->stream);
+        if (e != cudaSuccess) { err = std::string("graph launch: ") + cudaGetErrorString(e); return -1; }
+        p->launches += p->graph_launches;
     } else {
-        for (int q0 = 0; q0 < nact; q0 += p->qc) {
-            const int nq = std::min(p->qc, nact - q0);
-            run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);
-        }
-        launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
-        ++p->launches;
+        enqueue_plan(p, nact, tw, logTW);
     }
     cudaEventRecord(p->ev1, p->stream);
     e = cudaGetLastError();

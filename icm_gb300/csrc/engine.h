@@ -100,6 +100,8 @@ struct Plan {
     // graph replay (enable_graphs)
     cudaGraphExec_t graph = nullptr;
     int graph_nq = -1;
+    const double *graph_node = nullptr;   // the node buffer the graph reads
+    long graph_launches = 0;
     double peak_bytes = 0;
     // timing: events around the kernel sequence of each run, optional
     // per-kernel events (prof.on) aggregated by kernel name

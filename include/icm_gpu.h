@@ -23,15 +23,19 @@ typedef struct {
     int device_id;              /* informational, overwritten by plan_create
                                    with the device chosen by icm_gpu_init */
     int use_cufftdx;            /* ignored: the engine has its own FP64 FFT */
-    int enable_graphs;          /* 1 = capture the per-chunk launch sequence
-                                   in a CUDA graph and replay it */
+    int enable_graphs;          /* 1 = capture the run's launch sequence (all
+                                   node chunks) in a CUDA graph once per node
+                                   count and replay it on later runs */
     int enable_q_pipeline;      /* ignored (all Q nodes of a chunk run
                                    level-synchronously in one launch per level) */
-    int memory_strategy;        /* 0 auto; 1 full (no pooled allocator);
-                                   2 pool; 3 selective recompute (no spectrum
-                                   cache: propagate recomputes child spectra) */
-    int force_uncached_fused_levels; /* -1 auto; else levels without spectrum cache */
-    int force_uncached_cufft_levels; /* -1 auto; ignored */
+    int memory_strategy;        /* 1 = plain cudaMalloc for the plan's arena;
+                                   any other value = the stream-ordered pool.
+                                   The reference's selective recompute (3) has
+                                   no counterpart: memory is bounded by the
+                                   node chunk instead */
+    int force_uncached_fused_levels; /* ignored: coefficient-FFT levels always
+                                   cache the children's spectra */
+    int force_uncached_cufft_levels; /* ignored (no cuFFT levels) */
     int fast_mode;              /* ignored */
     int verbose;                /* print the plan to stderr */
 } IcmGpuOptions;

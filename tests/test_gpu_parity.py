@@ -288,3 +288,21 @@ def test_subtree_kernels_equal_level_by_level(gpu_icm, B, fft_min):
     assert np.array_equal(out[0][1], out[1][1])
     for a, b in zip(out[0][2], out[1][2]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("n,k", [(40, 40), (3000, 450), (20000, 20000)])
+def test_plan_graph_replay(gpu_icm, n, k):
+    """IcmGpuOptions.enable_graphs: the run is captured once per node count and
+    replayed; results equal the direct launches bit for bit (small path, tree
+    levels, new payouts and node counts)."""
+    from icm_gb300._lib import IcmGpuOptions
+    rng = np.random.default_rng(n)
+    S = 1e4 * np.exp(rng.standard_normal(n))
+    P1, P2 = 0.8 ** np.arange(k), np.linspace(1.0, 0.1, k)
+    direct = gpu_icm.GpuPlan(S, k)
+    graphed = gpu_icm.GpuPlan(S, k, IcmGpuOptions(enable_graphs=1))
+    for P, Q in [(P1, 256), (P2, 256), (P1, 128), (P2, 256)]:
+        a, b = direct.equity(P, Q=Q), graphed.equity(P, Q=Q)
+        assert np.array_equal(a, b), (n, k, Q)
+    direct.close()
+    graphed.close()
