@@ -61,8 +61,8 @@ def parse():
     ap.add_argument("--no-gpu-scale", action="store_true", help="skip the n = 2^20 leg")
     ap.add_argument("--case", default="",
                     help="run one small workload once, untimed, and exit (for profilers): "
-                         "vjp_batch:T (T tournaments of the VJP leg's batch), batch:T (T of the batched leg), "
-                         "small:n:k (20 single solves)")
+                         "vjp_batch:T (T tournaments of the VJP leg's batch), batch:T[:Q] (T of the batched leg), "
+                         "small:n:k (20 single solves), dropin:n:Q (one drop-in solve), linear:n:k (linear engine)")
     return ap.parse_args()
 
 
@@ -523,18 +523,34 @@ def run_case(icm, W, case):
         vb.set_options(graphs=False)
         vb.vjp([P for _, P in ts], cots)
         vb.close()
-    elif kind == "batch":
+    elif kind == "batch":   # batch:T[:Q] -- Q nodes in one chunk (default 256)
         ts = W.batched(count=int(rest[0]))
+        Q = int(rest[1]) if len(rest) > 1 else 256
+        icm.configure(q_chunk=Q)
         b = icm.GpuBatch([S for S, _ in ts], [len(P) for _, P in ts])
         b.set_options(graphs=False)
-        b.equity([P for _, P in ts])
+        b.equity([P for _, P in ts], Q=Q)
         b.close()
+        icm.configure()
     elif kind == "small":
         n, k = int(rest[0]), int(rest[1])
         rng = np.random.default_rng(n)
         S, P = 1e4 * np.exp(rng.standard_normal(n)), 0.8 ** np.arange(k)
         for _ in range(20):
             icm.gpu_equity(S, P)
+    elif kind == "dropin":   # the drop-in distribution at n players and Q nodes (one chunk), one solve
+        n, Q = int(rest[0]), int(rest[1])
+        S, P, _ = W.dropin(n=n)
+        icm.configure(q_chunk=Q)
+        icm.gpu_equity(S, P, Q=Q)
+        icm.configure()
+    elif kind == "linear":   # the linear engine, one solve
+        n, k = int(rest[0]), int(rest[1])
+        rng = np.random.default_rng(n)
+        S, P = 1e4 * np.exp(rng.standard_normal(n)), 0.8 ** np.arange(k)
+        icm.configure(engine="linear")
+        icm.gpu_equity(S, P)
+        icm.configure()
     else:
         raise SystemExit(f"unknown case {case!r}")
     print(json.dumps({"case": case, "status": "ok"}))

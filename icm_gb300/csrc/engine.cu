@@ -397,6 +397,8 @@ size_t plan_tree_layout(Plan *p, int qc, char *base) {
     return off;
 }
 
+static bool root_gspec_forkable(const Plan *p);
+
 Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err, bool coeff_only,
                   double q_bytes_scale, size_t budget_bytes) {
     Plan *p = new Plan();
@@ -452,6 +454,16 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     }
     p->arena_bytes = off;
     p->peak_bytes = (double)off;
+    if (!p->small && !p->linear && root_gspec_forkable(p)) {   // stream and events for the root's spectrum
+        e = cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            err = std::string("side stream: ") + cudaGetErrorString(e);
+            plan_destroy(p);
+            return nullptr;
+        }
+    }
     char *A = p->arena;
     p->d_S = (double *)(A + o_S);
     p->d_perm = (int *)(A + o_perm);
@@ -503,9 +515,22 @@ void plan_destroy(Plan *p) {
     }
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->ev_join) cudaEventDestroy(p->ev_join);
+    if (p->side) {
+        cudaStreamSynchronize(p->side);
+        cudaStreamDestroy(p->side);
+    }
     for (cudaEvent_t ev : p->prof.pool) cudaEventDestroy(ev);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
+}
+
+// the root's payout spectrum can run beside the build: a one-kernel spectral
+// root writes only its own G buffer
+static bool root_gspec_forkable(const Plan *p) {
+    const int L = p->L;
+    return L >= 2 && p->Lf < L - 1 && p->lv[L - 1].kind == 2 && p->lv[L - 1].deg / 2 <= kSpecMaxD;
 }
 
 // subset: active players (sorted order) and per-level hot bitmaps
@@ -628,7 +653,9 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
         if (lv[l].kind == 2) {
             // the parent's g spectrum: the payout's at the root, converted from
             // coefficients below a coefficient level, else left by the level above
-            if (root || lv[l + 1].kind != 2) {
+            if (root && p->root_forked) {
+                cudaStreamWaitEvent(st, p->ev_join, 0);   // computed beside the build
+            } else if (root || lv[l + 1].kind != 2) {
                 const uint8_t *hot_p = p->subset ? p->d_hot + p->hot_off[l] : nullptr;
                 if (lv[l].deg / 2 > kSpecMaxD) {
                     int logd = 0;
@@ -727,6 +754,18 @@ static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
         launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
         ++p->launches;
     } else {
+        p->root_forked = false;
+        if (nact > 0 && p->side) {   // the payout's spectrum beside the build
+            const int l = p->L - 1;
+            cudaEventRecord(p->ev_fork, p->stream);
+            cudaStreamWaitEvent(p->side, p->ev_fork, 0);
+            launch_gspec_init(p->d_payout, 0, 0, p->k, p->lv[l].nreal, p->lv[l], p->lv[l].G, 0, 1,
+                              p->subset ? p->d_hot + p->hot_off[l] : nullptr, tw, logTW, p->side, &p->prof,
+                              nullptr, 0);
+            cudaEventRecord(p->ev_join, p->side);
+            ++p->launches;
+            p->root_forked = true;
+        }
         for (int q0 = 0; q0 < nact; q0 += p->qc) {
             const int nq = std::min(p->qc, nact - q0);
             run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);

@@ -73,6 +73,12 @@ struct Plan {
     IcmGpuOptions opts{};
     // device
     cudaStream_t stream = nullptr;
+    // the root's payout spectrum runs on a side stream, overlapping the build
+    // (one-kernel spectral roots only): fork after the uploads, join before
+    // the root's propagate
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool root_forked = false;
     char *arena = nullptr;
     size_t arena_bytes = 0;
     bool pooled = false;            // arena from the stream-ordered pool
