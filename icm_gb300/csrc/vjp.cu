@@ -576,6 +576,137 @@ __device__ __forceinline__ void adj_down_packed(const AdjDownFusedArgs *__restri
     adj_down_core(V, idx, nh, wmax, A0.logN, A0.tw, A0.logTW, sm);
 }
 
+// ------------------------------------------ multi-pass FFT adjoint levels
+// Levels whose transform exceeds one CTA (N > 8192): the one-kernel steps
+// above split into a packing kernel, global batched FFTs (fft_batched:
+// four-step, natural order) and pointwise kernels.  Every pair is computed,
+// as the forward's multi-pass levels compute every pair (their cached
+// spectra are complete).  Grids: (items of the level, nodes of the chunk).
+__global__ void k_adj_up_pack(const double *__restrict__ gbc, size_t gbc_q, int gst_c, int glen_c, int npairs, int N,
+                              double2 *__restrict__ z) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int j = (int)(idx / N), t = (int)(idx % N);
+    if (j >= npairs) return;
+    const double *gL = gbc + q * gbc_q + (size_t)(2 * j) * gst_c;
+    z[((size_t)q * npairs + j) * N + t] = (t < glen_c) ? make_double2(gL[t], gL[gst_c + t]) : make_double2(0.0, 0.0);
+}
+
+// children's gbar spectra (cached for the downward pass), Y = S_R G_L + S_L G_R,
+// and the half-size inverse input U[f] = E[f] + i O[f] of the real product
+__global__ void k_adj_up_mid(const double2 *__restrict__ Z, const double2 *__restrict__ spec,
+                             double2 *__restrict__ gspec, int npairs, int N, double2 *__restrict__ U,
+                             const double2 *__restrict__ tw, int logTW, int logN) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int h = N >> 1;
+    const int j = (int)(idx / h), f = (int)(idx % h);
+    if (j >= npairs) return;
+    const size_t item = (size_t)q * npairs + j;
+    const double2 *z = Z + item * N;
+    const int fc = h - f;
+    const double2 zf = z[f], zn = z[(N - f) & (N - 1)];
+    const double2 zc = z[fc], zcn = z[(N - fc) & (N - 1)];
+    const double2 GLf = cscale(cadd(zf, cconj(zn)), 0.5);
+    const double2 GRf = cscale(cmul_mi(csub(zf, cconj(zn))), 0.5);
+    const double2 GLc = cscale(cadd(zc, cconj(zcn)), 0.5);
+    const double2 GRc = cscale(cmul_mi(csub(zc, cconj(zcn))), 0.5);
+    const size_t so = (2 * item) * (size_t)(h + 1);
+    const double2 *sL = spec + so, *sR = sL + (h + 1);
+    double2 *gL = gspec + so, *gR = gL + (h + 1);
+    gL[f] = GLf;
+    gR[f] = GRf;
+    if (f == 0) { gL[h] = GLc; gR[h] = GRc; }
+    const double2 Yf = cadd(cmul(sR[f], GLf), cmul(sL[f], GRf));
+    const double2 Yc = cadd(cmul(sR[fc], GLc), cmul(sL[fc], GRc));
+    double2 E = cadd(Yf, cconj(Yc)), D = csub(Yf, cconj(Yc));
+    if (f == 0) { E.y = 0.0; D.y = 0.0; }
+    const double2 O = cmulc(D, __ldg(&tw[(long)f << (logTW - logN)]));
+    U[item * h + f] = cadd(E, cmul_pi(O));
+}
+
+__global__ void k_adj_up_post(const double2 *__restrict__ U, int npairs, int N, double *__restrict__ gbp,
+                              size_t gbp_q, int gst_p, int gpl) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int j = (int)(idx / gst_p), t = (int)(idx % gst_p);
+    if (j >= npairs) return;
+    double v = 0.0;
+    if (t < gpl) {
+        const double2 uv = U[((size_t)q * npairs + j) * (N >> 1) + (t >> 1)];
+        v = ((t & 1) ? uv.y : uv.x) * (1.0 / N);
+    }
+    gbp[q * gbp_q + (size_t)j * gst_p + t] = v;
+}
+
+__global__ void k_adj_down_pack(const double *__restrict__ gp, size_t gp_q, int gst_p, int gpl,
+                                const double *__restrict__ Pbp, size_t Pbp_q, int pst_p, int lp, int npairs, int N,
+                                double2 *__restrict__ z) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int j = (int)(idx / N), t = (int)(idx % N);
+    if (j >= npairs) return;
+    const double x = (t < gpl) ? gp[q * gp_q + (size_t)j * gst_p + t] : 0.0;
+    const double y = (Pbp && t < lp) ? Pbp[q * Pbp_q + (size_t)j * pst_p + t] : 0.0;
+    z[((size_t)q * npairs + j) * N + t] = make_double2(x, y);
+}
+
+// in place: Z = Y_L + i Y_R with Y_L = G conj(Gbar_R) + R conj(S_R) (and L/R swapped)
+__global__ void k_adj_down_mid(double2 *__restrict__ Z, const double2 *__restrict__ spec,
+                               const double2 *__restrict__ gspec, int npairs, int N) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int h = N >> 1;
+    const int j = (int)(idx / h), f = (int)(idx % h);
+    if (j >= npairs) return;
+    const size_t item = (size_t)q * npairs + j;
+    double2 *z = Z + item * N;
+    const size_t so = (2 * item) * (size_t)(h + 1);
+    const double2 *sL = spec + so, *sR = sL + (h + 1);
+    const double2 *gL = gspec + so, *gR = gL + (h + 1);
+    if (f == 0) {   // bins 0 and h: real spectra, each its own mirror
+        const double2 z0 = z[0], zh = z[h];
+        const double2 G0 = make_double2(z0.x, 0.0), R0 = make_double2(z0.y, 0.0);
+        const double2 Gh = make_double2(zh.x, 0.0), Rh = make_double2(zh.y, 0.0);
+        const double2 YL0 = cadd(cmulc(G0, gR[0]), cmulc(R0, sR[0]));
+        const double2 YR0 = cadd(cmulc(G0, gL[0]), cmulc(R0, sL[0]));
+        const double2 YLh = cadd(cmulc(Gh, gR[h]), cmulc(Rh, sR[h]));
+        const double2 YRh = cadd(cmulc(Gh, gL[h]), cmulc(Rh, sL[h]));
+        z[0] = cadd(YL0, cmul_pi(YR0));
+        z[h] = cadd(YLh, cmul_pi(YRh));
+    } else {
+        const double2 zf = z[f], zn = z[N - f];
+        const double2 G = cscale(cadd(zf, cconj(zn)), 0.5);
+        const double2 R = cscale(cmul_mi(csub(zf, cconj(zn))), 0.5);
+        const double2 YL = cadd(cmulc(G, gR[f]), cmulc(R, sR[f]));
+        const double2 YR = cadd(cmulc(G, gL[f]), cmulc(R, sL[f]));
+        z[f] = cadd(YL, cmul_pi(YR));
+        z[N - f] = cadd(cconj(YL), cmul_pi(cconj(YR)));
+    }
+}
+
+__global__ void k_adj_down_post(const double2 *__restrict__ Z, int npairs, int N, const double *__restrict__ Pbp,
+                                size_t Pbp_q, int pst_p, int lp, const double *__restrict__ Pc, size_t Pc_q, int pst_c,
+                                int lc, double *__restrict__ Pbc) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int c = (int)(idx / pst_c), i = (int)(idx % pst_c);
+    if (c >= 2 * npairs) return;
+    const int j = c >> 1, side = c & 1;
+    double v = 0.0;
+    if (i < lc) {
+        const double2 zv = Z[((size_t)q * npairs + j) * N + i];
+        v = (side ? zv.y : zv.x) * (1.0 / N);
+        if (Pbp && 2 * (lc - 1) == N && i == lc - 1) {   // the one wrapped term
+            const double *pb = Pbp + q * Pbp_q + (size_t)j * pst_p;
+            const double *Ps = Pc + q * Pc_q + (size_t)(c ^ 1) * pst_c;
+            const double top = (N < lp) ? pb[N] : 0.0;
+            v = fma(Ps[lc - 1], top - pb[0], v);
+        }
+    }
+    Pbc[q * Pc_q + (size_t)c * pst_c + i] = v;
+}
+
 // ---- kernels: single plans launch (nbx, nq) grids; work lists map blocks
 // to (descriptor, block) through tab
 template <int B>
@@ -731,6 +862,7 @@ void launch_node_reduce_members(int F, const longlong2 *mem, int nq, size_t sq, 
 
 // ------------------------------------------------------------ plans
 static bool level_fused(const Level &v) { return v.fft && v.npairs > 0 && v.fftn <= kVjpMaxN && fused_ok(v.fftn); }
+static bool level_big(const Level &v) { return v.fft && v.npairs > 0 && !level_fused(v); }
 
 // per-level adjoint buffers of one tournament for chunks of qc nodes: gbar
 // (shaped as g), Pbar (shaped as P) and the children's gbar spectra of
@@ -743,7 +875,7 @@ size_t vjp_level_layout(const Plan *p, int qc, char *base, VjpBufs *b) {
         const Level &lv = p->lv[l];
         o_gb[l] = lv.g_q ? take(8 * (size_t)qc * lv.g_q) : 0;
         o_Pb[l] = lv.P_q ? take(8 * (size_t)qc * lv.P_q) : 0;
-        o_gsp[l] = (l >= 1 && level_fused(lv)) ? take(16 * (size_t)qc * lv.spec_q) : 0;
+        o_gsp[l] = (l >= 1 && lv.fft && lv.npairs > 0) ? take(16 * (size_t)qc * lv.spec_q) : 0;
     }
     const size_t o_bw = (p->k < p->B) ? take(8 * (size_t)qc * p->nblocks * p->B) : 0;
     if (!base) return off;
@@ -888,6 +1020,8 @@ void adj_up_args(const Plan *p, const VjpBufs &b, int l, const double2 *tw, int 
         F = AdjUpFusedArgs{b.gb[l - 1], b.gb_q[l - 1], b.gb_st[l - 1], c.glen, pl.npairs, logN, pl.spec, b.gspec[l],
                            out, out_q, gst_p, gpl, tw, logTW, zp, pl.deg, (pl.npairs + cb - 1) / cb};
         j0 = pl.npairs;
+    } else if (level_big(pl)) {
+        j0 = pl.npairs;   // the pairs go through the multi-pass steps (adjoint_chunk)
     }
     const long work = (long)(pl.nreal - j0) * gst_p;
     if (work > 0)
@@ -914,6 +1048,8 @@ void adj_down_args(const Plan *p, const VjpBufs &b, int l, const double2 *tw, in
         F = AdjDownFusedArgs{gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen,
                              pl.npairs, logN, pl.spec, b.gspec[l], b.Pb[l - 1], tw, logTW, zp, pl.deg,
                              (pl.npairs + cb - 1) / cb};
+        c0 = 2 * pl.npairs;
+    } else if (level_big(pl)) {
         c0 = 2 * pl.npairs;
     }
     const long work = (long)(c.nreal - c0) * c.pst;
@@ -997,6 +1133,47 @@ void launch_accum_strided(int n, int nq, const double *src, size_t sq, double *a
     k_accum_strided<<<nblkv(n, 256), 256, 0, st>>>(n, nq, src, sq, acc, first ? 1 : 0);
 }
 
+// multi-pass upward / downward steps of level l (its pairs; lone parents
+// stay with the schoolbook kernels), through the plan's FFT work buffers
+static void adj_up_big(Plan *p, const VjpBufs &b, int l, int nq, const double2 *tw, int logTW, long &launches) {
+    const Level &c = p->lv[l - 1], &pl = p->lv[l];
+    const bool root = (l == p->L - 1);
+    double *out = root ? b.root : b.gb[l];
+    const size_t out_q = root ? b.root_q : b.gb_q[l];
+    const int gst_p = root ? b.kst : b.gb_st[l];
+    const int gpl = root ? p->k : pl.glen;
+    const int N = pl.fftn, logN = plan_ilog2(N), np = pl.npairs;
+    cudaStream_t st = p->stream;
+    k_adj_up_pack<<<dim3(nblkv((long)np * N, 256), nq), 256, 0, st>>>(b.gb[l - 1], b.gb_q[l - 1], b.gb_st[l - 1],
+                                                                      c.glen, np, N, p->d_fa);
+    fft_batched(p->d_fa, p->d_fc, (long)nq * np, logN, -1, tw, logTW, st, &launches, &p->prof);
+    k_adj_up_mid<<<dim3(nblkv((long)np * (N / 2), 256), nq), 256, 0, st>>>(p->d_fa, pl.spec, b.gspec[l], np, N,
+                                                                          p->d_fb, tw, logTW, logN);
+    fft_batched(p->d_fb, p->d_fc, (long)nq * np, logN - 1, +1, tw, logTW, st, &launches, &p->prof);
+    k_adj_up_post<<<dim3(nblkv((long)np * gst_p, 256), nq), 256, 0, st>>>(p->d_fb, np, N, out, out_q, gst_p, gpl);
+    launches += 3;
+}
+
+static void adj_down_big(Plan *p, const VjpBufs &b, int l, int nq, const double2 *tw, int logTW, long &launches) {
+    const Level &c = p->lv[l - 1], &pl = p->lv[l];
+    const bool root = (l == p->L - 1);
+    const double *gp = root ? p->d_payout : pl.g;
+    const size_t gp_q = root ? 0 : pl.g_q;
+    const int gst_p = root ? 0 : pl.gst;
+    const int gpl = root ? p->k : pl.glen;
+    const double *Pbp = root ? nullptr : b.Pb[l];
+    const int N = pl.fftn, logN = plan_ilog2(N), np = pl.npairs;
+    cudaStream_t st = p->stream;
+    k_adj_down_pack<<<dim3(nblkv((long)np * N, 256), nq), 256, 0, st>>>(gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst,
+                                                                        pl.plen, np, N, p->d_fa);
+    fft_batched(p->d_fa, p->d_fc, (long)nq * np, logN, -1, tw, logTW, st, &launches, &p->prof);
+    k_adj_down_mid<<<dim3(nblkv((long)np * (N / 2), 256), nq), 256, 0, st>>>(p->d_fa, pl.spec, b.gspec[l], np, N);
+    fft_batched(p->d_fa, p->d_fc, (long)nq * np, logN, +1, tw, logTW, st, &launches, &p->prof);
+    k_adj_down_post<<<dim3(nblkv((long)2 * np * c.pst, 256), nq), 256, 0, st>>>(
+        p->d_fa, np, N, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen, b.Pb[l - 1]);
+    launches += 3;
+}
+
 // adjoint passes of one chunk (the forward tree of the chunk is in place)
 static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int logTW, bool first, bool node_terms) {
     Plan *p = v->p;
@@ -1013,6 +1190,8 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         if (F.nbx > 0) {
             k_adj_up_fused<<<dim3(F.nbx, nq), kVjpThreads, adj_up_smem(F.logN), st>>>(F, q0);
             ++launches;
+        } else if (level_big(p->lv[l])) {
+            adj_up_big(p, b, l, nq, tw, logTW, launches);
         }
         if (Sa.nbx > 0) {
             k_adj_up_school<<<dim3(Sa.nbx, nq), 256, 0, st>>>(Sa, q0);
@@ -1026,6 +1205,8 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         if (F.nbx > 0) {
             k_adj_down_fused<<<dim3(F.nbx, nq), kVjpThreads, adj_down_smem(F.logN), st>>>(F, q0);
             ++launches;
+        } else if (level_big(p->lv[l])) {
+            adj_down_big(p, b, l, nq, tw, logTW, launches);
         }
         if (Sa.nbx > 0) {
             k_adj_down_school<<<dim3(Sa.nbx, nq), 256, 0, st>>>(Sa, q0);

@@ -21,7 +21,7 @@ import numpy as np
 import pytest
 
 from tests.conftest import max_rel
-from tests.vjp_reference import fd_directional, quadratic_loss_grad, v1_loss_grad
+from tests.vjp_reference import fd_directional, quadratic_loss_grad, v1_loss_grad, v1_loss_grad_blocked
 from icm_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -265,3 +265,19 @@ def test_vjp_batch_reuse_graphs(gpu_icm):
     with pytest.raises(gpu_icm.ICMError):
         vb.equity(Ps)
     vb.close()
+
+
+def test_vjp_multipass_levels(gpu_icm):
+    """n = k = 20000: the top two levels need transforms of 16384 and 32768
+    points (beyond one CTA), so their adjoint steps run through global
+    four-step FFTs.  Against the analytic V1 gradient and Euler's identity."""
+    rng = np.random.default_rng(20000)
+    n = 20000
+    S = 1 + 999 * rng.random(n)
+    P = (n - np.arange(n)).astype(float)
+    cot = rng.standard_normal(n)
+    gS, gP = gpu_icm.equity_vjp(S, P, cot)
+    ref = v1_loss_grad_blocked(S, cot)
+    assert np.abs(gS - ref).max() <= TOL_ANALYTIC * np.abs(ref).max()
+    E = gpu_icm.equity(S, P)
+    assert abs(gP @ P - cot @ E) <= 1e-12 * np.abs(cot * E).sum()

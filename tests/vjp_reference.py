@@ -19,6 +19,22 @@ def v1_loss_grad(S, cot):
     return cot * (M @ S) - (cot * S) @ M
 
 
+def v1_loss_grad_blocked(S, cot, block=1024):
+    """v1_loss_grad in row blocks (memory O(block n) for large n)."""
+    S = np.asarray(S, dtype=np.float64)
+    cot = np.asarray(cot, dtype=np.float64)
+    out = np.zeros_like(S)
+    for i0 in range(0, len(S), block):
+        Si = S[i0:i0 + block]
+        T = Si[:, None] + S[None, :]
+        M = 1.0 / (T * T)
+        idx = np.arange(i0, i0 + len(Si))
+        M[np.arange(len(Si)), idx] = 0.0
+        out[i0:i0 + block] += cot[i0:i0 + block] * (M @ S)
+        out -= (cot[i0:i0 + block] * Si) @ M
+    return out
+
+
 def v2_loss_grad(S, cot):
     """d/dS of sum_i cot_i V2_i (O(n^3); small n only)."""
     S = np.asarray(S, dtype=np.float64)
