@@ -74,6 +74,9 @@ SIGNATURES = {
     "icm_last_status": (ctypes.c_int, []),
     "icm_gb300_set_config": (ctypes.c_int, [ctypes.POINTER(IcmGb300Config)]),
     "icm_gb300_player_order": (ctypes.c_int, [ctypes.c_int, _dp, _ip]),
+    "icm_gb300_test_fail_allocation": (None, [ctypes.c_int]),
+    "icm_gb300_check_geometry": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_char_p, ctypes.c_int]),
     "icm_gpu_equity_batched": (ctypes.c_int, [ctypes.c_int, _ip, _ip, _dp, _dp, ctypes.c_int, _dp,
                                               ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gpu_measure_fp64_gflops": (ctypes.c_int, [_dp]),

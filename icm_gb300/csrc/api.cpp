@@ -290,6 +290,28 @@ int icm_gb300_player_order(int n, const double *S, int *perm) {
     return 0;
 }
 
+void icm_gb300_test_fail_allocation(int nth) { set_alloc_failure(nth); }
+
+int icm_gb300_check_geometry(int n, int k, int block_size, int fft_min_degree, int flags, char *why, int why_len) {
+    if (n < 1 || k < 1 || k > n) { set_error("icm_gb300_check_geometry: need 1 <= k <= n"); return -1; }
+    const IcmGb300Config saved = g_config;
+    g_config.block_size = block_size;
+    g_config.fft_min_degree = fft_min_degree;
+    Plan p;
+    p.coeff_only = (flags & 1) != 0;
+    std::string err;
+    const std::vector<double> S(n, 1.0);   // stack values do not shape the tree
+    int rc = plan_geometry(&p, n, S.data(), k, err);
+    g_config = saved;
+    if (rc != 0) { set_error("icm_gb300_check_geometry: " + err); return -1; }
+    rc = plan_check_geometry(&p, err) == 0 ? 0 : 1;
+    if (why && why_len > 0) {
+        std::strncpy(why, rc ? err.c_str() : "", why_len - 1);
+        why[why_len - 1] = 0;
+    }
+    return rc;
+}
+
 int icm_gb300_set_config(const IcmGb300Config *cfg) {
     if (cfg) g_config = *cfg;
     else memset(&g_config, 0, sizeof(g_config));

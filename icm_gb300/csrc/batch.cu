@@ -381,7 +381,7 @@ static int upload_steps(Forest *f, std::string &err) {
         if (f->d_desc) cudaFree(f->d_desc);
         f->d_desc = nullptr;
         f->desc_cap = 0;
-        cudaError_t e = cudaMalloc(&f->d_desc, bytes);
+        cudaError_t e = dev_alloc((void **)&f->d_desc, bytes, f->stream, false);
         if (e != cudaSuccess) { err = std::string("work lists: ") + cudaGetErrorString(e); return -1; }
         f->desc_cap = bytes;
     }
@@ -618,7 +618,7 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
         o_mem = take(sizeof(longlong2) * (size_t)F);
         for (int i = 0; i < F; ++i) o_adj[i] = take(vjp_level_layout(f->tr[i], qc, nullptr, nullptr));
     }
-    e = cudaMallocAsync((void **)&f->arena, off, f->stream);
+    e = dev_alloc((void **)&f->arena, off, f->stream, true);
     if (e != cudaSuccess) {
         err = "device allocation of " + std::to_string(off) + " bytes failed: " + cudaGetErrorString(e);
         forest_destroy(f);
@@ -735,7 +735,7 @@ static int prepare_nodes(Forest *f, int Q, std::string &err) {
     if (f->d_node) cudaFree(f->d_node);
     f->d_node = nullptr;
     const size_t nb = sizeof(double) * h.size();
-    cudaError_t e = cudaMalloc(&f->d_node, nb + sizeof(int) * hz.size());
+    cudaError_t e = dev_alloc((void **)&f->d_node, nb + sizeof(int) * hz.size(), f->stream, false);
     int *dz = e == cudaSuccess ? (int *)((char *)f->d_node + nb) : nullptr;
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(f->d_node, h.data(), nb, cudaMemcpyHostToDevice, f->stream);
@@ -768,7 +768,7 @@ static int forest_prepare(Forest *f, int Q, bool node_terms, std::string &err) {
             if (f->d_part) cudaFree(f->d_part);
             f->d_part = nullptr;
             f->part_cap = 0;
-            cudaError_t e = cudaMalloc((void **)&f->d_part, sizeof(double) * need);
+            cudaError_t e = dev_alloc((void **)&f->d_part, sizeof(double) * need, f->stream, false);
             if (e != cudaSuccess) { err = std::string("node-term buffers: ") + cudaGetErrorString(e); f->Q = 0; return -1; }
             f->part_cap = need;
         }

@@ -16,6 +16,18 @@ namespace icmg {
 IcmGb300Config g_config = {};
 int g_device = -1;
 
+// Device allocations of plans, batches and VJPs go through dev_alloc, so a
+// test can make the n-th one fail as an exhausted allocator would
+// (icm_gb300_test_fail_allocation); 0 = no injected failure.
+static std::atomic<int> g_fail_alloc{0};
+void set_alloc_failure(int nth) { g_fail_alloc.store(nth > 0 ? nth : 0); }
+cudaError_t dev_alloc(void **ptr, size_t bytes, cudaStream_t st, bool pooled) {
+    int c = g_fail_alloc.load();
+    while (c > 0 && !g_fail_alloc.compare_exchange_weak(c, c - 1)) {}
+    if (c == 1) return cudaErrorMemoryAllocation;
+    return pooled ? cudaMallocAsync(ptr, bytes, st) : cudaMalloc(ptr, bytes);
+}
+
 static double now_ns() {
     return (double)std::chrono::duration_cast<std::chrono::nanoseconds>(
                std::chrono::steady_clock::now().time_since_epoch())
@@ -354,6 +366,57 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     return 0;
 }
 
+// Invariants of a plan's geometry that the kernels rely on (host only; the
+// counterpart of the reference's planner checks, tools/test_gpu_wrap_feasibility.cu
+// and gpu_internal.h:321-342).  0 when all hold, else -1 and the first
+// violation in `why`.
+int plan_check_geometry(const Plan *p, std::string &why) {
+    auto bad = [&](int l, const std::string &m) {
+        why = "level " + std::to_string(l) + ": " + m;
+        return -1;
+    };
+    const int k = p->k, B = p->B, L = p->L;
+    if (p->nblocks != (p->n + B - 1) / B) return bad(0, "block count");
+    if (p->lv[L - 1].nreal != 1) return bad(L - 1, "the root level has more than one node");
+    for (int l = 0; l < L; ++l) {
+        const Level &v = p->lv[l];
+        if (v.deg != ((long)B << l)) return bad(l, "degree");
+        if (l == 0 ? v.nreal != p->nblocks : v.nreal != (p->lv[l - 1].nreal + 1) / 2) return bad(l, "node count");
+        if (v.plen != (int)std::min<long>(v.deg + 1, k) || v.glen != (int)std::min<long>(v.deg, k))
+            return bad(l, "truncation lengths");
+        if (v.pst < v.plen || v.gst < v.glen || (v.pst & 1) || (v.gst & 1)) return bad(l, "row strides");
+        if (l == 0) continue;
+        const Level &c = p->lv[l - 1];
+        if (v.npairs != c.nreal / 2) return bad(l, "pair count");
+        const int gpl = (l == L - 1) ? k : v.glen;   // the parent's g (the payout at the root)
+        if (c.glen > gpl) return bad(l, "a child's g is longer than its parent's");
+        if (v.kind == 1) {
+            const long N = v.fftn;
+            if (N < 4 || (N & (N - 1))) return bad(l, "FFT size is not a power of two");
+            // product: degree 2(lc - 1), one wrapped term at N = 2(lc - 1) is corrected
+            if (N < 2L * c.plen - 2) return bad(l, "FFT size below the product");
+            // middle product (and its transpose in the VJP): no wrap at all
+            if (N < (long)c.glen + c.plen - 1 || gpl > N) return bad(l, "FFT size below the correlation");
+        } else if (v.kind == 2) {
+            if (c.plen != c.deg + 1) return bad(l, "spectral level over truncated children");
+            if (c.deg > kSpecMaxD && !(l - 1 >= 1 && c.kind == 2))
+                return bad(l, "multi-pass spectral level without spectral children");
+            if (p->coeff_only || !p->spectral) return bad(l, "spectral level in a coefficient-only plan");
+        } else if (v.kind != 0) {
+            return bad(l, "unknown level kind");
+        } else if (c.deg >= p->fft_min_deg) {
+            return bad(l, "schoolbook level above the FFT crossover");
+        }
+    }
+    if (p->Lf > 0) {
+        if (p->Lf > L - 2) return bad(p->Lf, "subtree reaches the root");
+        for (int l = 1; l <= p->Lf; ++l)
+            if (p->lv[l].kind != 0) return bad(l, "subtree over a non-schoolbook level");
+    }
+    if (p->small && p->linear) return bad(0, "two engines chosen");
+    return 0;
+}
+
 // tree buffers for chunks of qc nodes: leaf block products, per-level
 // polynomials, spectra and end coefficients, FFT work buffers
 size_t plan_tree_layout(Plan *p, int qc, char *base) {
@@ -444,7 +507,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) {
         p->pooled = p->opts.memory_strategy != 1;
-        e = p->pooled ? cudaMallocAsync((void **)&p->arena, off, p->stream) : cudaMalloc(&p->arena, off);
+        e = dev_alloc((void **)&p->arena, off, p->stream, p->pooled);
     }
     if (e != cudaSuccess) {
         err = "device allocation of " + std::to_string(off) + " bytes failed: " + cudaGetErrorString(e);
@@ -797,7 +860,7 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         p->d_node = nullptr;
         p->d_z = nullptr;
         const size_t nb = sizeof(double) * 3 * (size_t)std::max(nact, 1);
-        e = cudaMallocAsync((void **)&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1), p->stream);
+        e = dev_alloc((void **)&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1), p->stream, true);
         if (e != cudaSuccess) { err = std::string("node buffer: ") + cudaGetErrorString(e); return -1; }
         p->d_z = (int *)((char *)p->d_node + nb);
         p->qmax = nact;

@@ -126,6 +126,12 @@ struct Plan {
 // lifecycle (engine.cu)
 // geometry only: validation, sort, levels, per-node element counts
 int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err);
+// device allocation of plans, batches and VJPs (stream-ordered pool or plain
+// cudaMalloc), with the test hook that makes the n-th one fail
+cudaError_t dev_alloc(void **ptr, size_t bytes, cudaStream_t st, bool pooled);
+void set_alloc_failure(int nth);
+// invariants the kernels rely on (host only): 0, or -1 with the violation
+int plan_check_geometry(const Plan *p, std::string &why);
 // player order: stacks descending, ties by index
 void sort_players_desc(const double *S, int n, std::vector<int> &perm);
 // tree buffers for chunks of qc nodes from `base` (nullptr: size only)

@@ -904,7 +904,7 @@ VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t
     const size_t o_cot = take(8 * (size_t)n), o_gs = take(8 * (size_t)n), o_gp = take(8 * (size_t)k);
     const size_t o_root = take(8 * (size_t)qc * v->kst);
     const size_t o_lv = take(vjp_level_layout(p, qc, nullptr, nullptr));
-    cudaError_t e = cudaMallocAsync((void **)&v->arena, off, p->stream);
+    cudaError_t e = dev_alloc((void **)&v->arena, off, p->stream, true);
     if (e != cudaSuccess) {
         err = "VJP buffers (" + std::to_string(off) + " bytes): " + cudaGetErrorString(e);
         plan_destroy(p);
@@ -1250,7 +1250,7 @@ int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot,
         if (v->d_partA) cudaFreeAsync(v->d_partA, p->stream);
         v->d_partA = nullptr;
         const size_t cap = std::max(nact, 1);
-        e = cudaMallocAsync((void **)&v->d_partA, sizeof(double) * (2 * (size_t)p->qc * n + 2 * cap), p->stream);
+        e = dev_alloc((void **)&v->d_partA, sizeof(double) * (2 * (size_t)p->qc * n + 2 * cap), p->stream, true);
         if (e != cudaSuccess) { err = std::string("node-term buffers: ") + cudaGetErrorString(e); return -1; }
         v->d_partB = v->d_partA + (size_t)p->qc * n;
         v->d_nodeA = v->d_partB + (size_t)p->qc * n;
@@ -1263,7 +1263,7 @@ int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot,
         p->d_node = nullptr;
         p->d_z = nullptr;
         const size_t nb = sizeof(double) * 3 * (size_t)std::max(nact, 1);
-        e = cudaMallocAsync((void **)&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1), p->stream);
+        e = dev_alloc((void **)&p->d_node, nb + sizeof(int) * (size_t)std::max(nact, 1), p->stream, true);
         if (e != cudaSuccess) { err = std::string("node buffer: ") + cudaGetErrorString(e); return -1; }
         p->d_z = (int *)((char *)p->d_node + nb);
         p->qmax = nact;

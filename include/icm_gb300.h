@@ -69,6 +69,21 @@ int icm_gb300_set_config(const IcmGb300Config *cfg);
  * invalid arguments (n < 1, a stack not finite and positive). */
 int icm_gb300_player_order(int n, const double *S, int *perm);
 
+/* The geometry of a plan for (n, k) under the given block size and FFT
+ * crossover (0 = the defaults), checked against the invariants the kernels
+ * rely on (host only: FFT sizes cover every product and correlation without
+ * wrap, spectral levels sit over untruncated children, truncation lengths
+ * and strides).  flags: 1 = the VJP's coefficient-only geometry.  Returns 0
+ * when they hold, 1 with the first violation in why, -1 for bad arguments. */
+int icm_gb300_check_geometry(int n, int k, int block_size, int fft_min_degree, int flags,
+                             char *why, int why_len);
+
+/* Test hook for error paths: the nth device allocation made by plans,
+ * batches and VJPs from now on fails as if the allocator were exhausted
+ * (the call that needed it returns -1 / NULL with the error text); 0 clears
+ * a pending failure.  No device fault is involved. */
+void icm_gb300_test_fail_allocation(int nth);
+
 /* Batched tournaments: T independent tournaments of uneven size.
  *   n[t], k[t]        players and paid places of tournament t
  *   S, payout         concatenated stacks (sum n) and payouts (sum k)

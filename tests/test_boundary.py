@@ -152,3 +152,28 @@ def test_player_order_host(built_lib, n):
     assert np.array_equal(icm.player_order(S), ref)
     with pytest.raises(icm.ICMError):
         icm.player_order(np.array([1.0, -2.0]))
+
+
+def test_plan_geometry_invariants(built_lib):
+    """Host-only sweep of the planner: for every size class, truncation, block
+    size and FFT crossover (and the VJP's coefficient-only geometry), the FFT
+    sizes cover every product and correlation, spectral levels sit over
+    untruncated children, lengths and strides are consistent."""
+    from icm_gb300._lib import lib
+    L = lib()
+    why = ctypes.create_string_buffer(256)
+    ns = sorted({1, 2, 3, 5, 7, 8, 9, 31, 33, 100, 255, 257, 1000, 4095, 4097, 9999, 16385, 65536, 65537,
+                 100003, 262144, 1 << 20, (1 << 21) + 3})
+    checked = 0
+    for n in ns:
+        ks = sorted({k for k in (1, 2, 7, 100, n // 7, n // 2, n - 1, n, 1000, 8193, 16385) if 1 <= k <= n})
+        big = n >= (1 << 18)   # fewer combinations where each geometry costs a sort of n players
+        for k in ks:
+            for B in ((8, 32) if big else (4, 8, 16, 32)):
+                for fm in ((16, 512) if big else (8, 16, 64, 512)):
+                    for flags in (0, 1):
+                        rc = L.icm_gb300_check_geometry(n, k, B, fm, flags, why, 256)
+                        assert rc == 0, (n, k, B, fm, flags, why.value.decode())
+                        checked += 1
+    assert checked > 1500
+    assert L.icm_gb300_check_geometry(5, 6, 8, 64, 0, why, 256) == -1

@@ -118,3 +118,32 @@ def test_batched_small_members_bitwise(gpu_icm):
     b.close()
     for x, y, z in zip(r1, r2, res):
         assert np.array_equal(x, z) and np.array_equal(y, z)
+
+
+@pytest.mark.parametrize("dist", ["uniform", "adversarial", "adv_1e9"])
+def test_exhaustive_small_fields(gpu_icm, oracle, dist):
+    """Every (n, k) with n <= 64, linear payouts, on the small path and on the
+    level path (small_max_n = -1), each as one batch, against the oracle.
+    Stacks as the reference's verify grid (bench/bench.c:65-88): uniform in
+    [1, 100], one 1e4 stack among ones, one 1e9 stack among ones.  Tolerance
+    1e-9 (1e-8 for the 1e9:1 field, the reference's own GPU gate)."""
+    rng = np.random.default_rng(42)
+    cases = []
+    for n in range(1, 65):
+        if dist == "uniform":
+            S = rng.integers(1, 101, n).astype(float)
+        else:
+            S = np.ones(n)
+            S[0] = 1e4 if dist == "adversarial" else 1e9
+        for k in range(1, n + 1):
+            cases.append((S, (k - np.arange(k)).astype(float)))
+    small = gpu_icm.equity_batched(cases)
+    gpu_icm.configure(small_max_n=-1)
+    level = gpu_icm.equity_batched(cases)
+    gpu_icm.configure()
+    tol = 1e-8 if dist == "adv_1e9" else 1e-9
+    for (S, P), a, b in zip(cases, small, level):
+        ref = oracle.equity(S, P, Q=256)
+        floor = 1e-12 * np.abs(ref).max()
+        assert max_rel(a, ref, floor=floor) < tol, (len(S), len(P))
+        assert max_rel(b, ref, floor=floor) < tol, (len(S), len(P))
