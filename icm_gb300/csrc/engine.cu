@@ -139,9 +139,10 @@ static int round2(int v) { return (v + 1) & ~1; }
 
 int select_block_size(int n, int k) {
     int B = g_config.block_size;
-    if (B <= 0) {   // the tuner table's choice for this size class, else 8
+    if (B <= 0) {   // the tuner table's choice for this size class, the built-in one, else 8
         int tF = 0;
         tune_lookup(n, k, &B, &tF);
+        if (B <= 0) tune_builtin(n, k, &B, &tF);
         if (B <= 0) B = 8;
     }
     if (B <= 4) B = 4;
@@ -155,6 +156,7 @@ static int select_fft_min(int n, int k) {
     if (g_config.fft_min_degree > 0) return g_config.fft_min_degree;
     int tB = 0, tF = 0;
     tune_lookup(n, k, &tB, &tF);
+    if (tF <= 0) tune_builtin(n, k, &tB, &tF);
     return tF > 0 ? tF : 64;
 }
 

@@ -173,6 +173,8 @@ int measure_hbm_gbps(double *out, std::string &err);
 
 // tuner table (tune.cpp)
 void tune_lookup(int n, int k, int *B, int *fft_min);
+// built-in choices for GB300 where the caller's table has none (0: none)
+void tune_builtin(int n, int k, int *B, int *fft_min);
 void tune_record(int n, int k, int B, int fft_min, double ms);
 int tune_load(const char *path, std::string &err);
 int tune_save(const char *path, std::string &err);

@@ -47,6 +47,33 @@ int tune_kbucket(int n, int k) {
     return r <= 1.0 / 64 ? 0 : r <= 1.0 / 8 ? 1 : r <= 0.5 ? 2 : 3;
 }
 
+// Built-in choices for GB300, consulted after the caller's table: the
+// fastest (B, fft_min_degree) of the search space measured on one GB300
+// (device time per solve, Q = 256, plans resident), kept only where the
+// choice also held up inside batches and VJPs.  Classes without an entry use
+// B = 8, fft_min_degree = 64.
+//   class (ceil log2 n, k/n bucket)   measured shape            default -> chosen (ms)
+//   (16, 3)                           n = k = 65536             18.96 -> 18.86
+//   (20, 0), (20, 3)                  n = 2^20, k = 1000 / n    161.8 -> 160.6, 380.0 -> 376.5
+// Crossover 128 was faster for single solves of n = 3000-20000 at k = 0.15 n
+// (up to 6%), but made the 4096-tournament batch slower (2.133 -> 2.200 s:
+// more schoolbook levels, which pack worse in work lists) and the n = 16384,
+// k = 2000 VJP slower, so those classes keep the defaults.
+namespace {
+const TuneEntry kBuiltin[] = {{16, 3, 4, 64, 0.0}, {20, 0, 4, 64, 0.0}, {20, 3, 4, 64, 0.0}};
+}
+
+void tune_builtin(int n, int k, int *B, int *fft_min) {
+    *B = 0;
+    *fft_min = 0;
+    const int ln = log2ceil(n), kb = tune_kbucket(n, k);
+    for (const TuneEntry &e : kBuiltin)
+        if (e.log2n == ln && e.kbucket == kb) {
+            *B = e.B;
+            *fft_min = e.fft_min;
+        }
+}
+
 // the table's choice for (n, k); 0 where the table has no entry
 void tune_lookup(int n, int k, int *B, int *fft_min) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
