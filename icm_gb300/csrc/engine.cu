@@ -580,6 +580,7 @@ void plan_destroy(Plan *p) {
     }
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
+    for (cudaEvent_t ev : p->stage_ev) cudaEventDestroy(ev);
     if (p->ev_fork) cudaEventDestroy(p->ev_fork);
     if (p->ev_join) cudaEventDestroy(p->ev_join);
     if (p->side) {
@@ -642,6 +643,17 @@ static double hot_frac(const Plan *p, int q0, int nq, long span, int nreal) {
     return hot / ((double)nq * nreal);
 }
 
+// a stage boundary of the current chunk (opts.verbose only)
+static void stage_mark(Plan *p, cudaStream_t st) {
+    if (!p->opts.verbose) return;
+    if (p->stage_used == p->stage_ev.size()) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        p->stage_ev.push_back(e);
+    }
+    cudaEventRecord(p->stage_ev[p->stage_used++], st);
+}
+
 void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide) {
     cudaStream_t st = p->stream;
     const int L = p->L;
@@ -665,6 +677,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
                     lv[0].plen, st, pr);
     }
     ++p->launches;
+    if (divide) stage_mark(p, st);   // end of the block build
     if (L >= 2 && lv[1].kind == 2) {
         frac(lv[0].deg, lv[0].nreal);
         launch_spec_init(lv[0], nq, tw, logTW, st, pr, zp, q0);
@@ -706,6 +719,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     pr->scale = 1.0;
     if (L >= 2 && lv[L - 1].fft)
         launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches, pr);
+    if (divide) stage_mark(p, st);   // end of the tree build
     for (int l = L - 1; l >= 1 + Lf; --l) {
         const bool root = (l == L - 1);
         const double *gp = root ? p->d_payout : lv[l].g;
@@ -755,6 +769,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
             ++p->launches;
         }
     }
+    if (divide) stage_mark(p, st);   // end of the propagate
     pr->scale = 1.0;
     if (Lf >= 1) {   // the bottom levels' propagate and (with divide) the division in one kernel
         double fl = 0.0, hotp = 1.0;
@@ -833,7 +848,9 @@ static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
         }
         for (int q0 = 0; q0 < nact; q0 += p->qc) {
             const int nq = std::min(p->qc, nact - q0);
+            stage_mark(p, p->stream);   // chunk start
             run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);
+            stage_mark(p, p->stream);   // end of the leaf extraction (division and node sum)
         }
         launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
         ++p->launches;
@@ -893,7 +910,8 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     // enable_graphs: the sequence is captured once per node count (and node
     // buffer) and replayed; kernels read payouts and nodes from the plan's
     // buffers, which every run refills before the launch
-    const bool use_graph = p->opts.enable_graphs == 1 && !p->prof.on && nact > 0;
+    p->stage_used = 0;
+    const bool use_graph = p->opts.enable_graphs == 1 && !p->prof.on && !p->opts.verbose && nact > 0;
     if (use_graph && (!p->graph || p->graph_nq != nact || p->graph_node != p->d_node)) {
         if (p->graph) cudaGraphExecDestroy(p->graph);
         p->graph = nullptr;
@@ -945,12 +963,24 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         }
     }
     const double t1 = now_ns();
+    for (double &m : p->stage_ms) m = 0.0;
+    for (size_t c = 0; c + 5 <= p->stage_used; c += 5)   // per chunk: 5 stage boundaries
+        for (int st = 0; st < 4; ++st) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, p->stage_ev[c + st], p->stage_ev[c + st + 1]) == cudaSuccess)
+                p->stage_ms[st] += ms;
+        }
     if (stats) {
         memset(stats, 0, sizeof(*stats));
         stats->total_ns = t1 - t0;
         stats->peak_vram_bytes = (size_t)p->peak_bytes;
         stats->engine = 1;
         stats->B = p->B;
+        // stage times on the instrumented (verbose) path, as the reference reports them
+        stats->block_build_ns = p->stage_ms[0] * 1e6;
+        stats->tree_build_ns = p->stage_ms[1] * 1e6;
+        stats->tree_propagate_cached_ns = p->stage_ms[2] * 1e6;
+        stats->leaf_extract_ns = p->stage_ms[3] * 1e6;
     }
     return 0;
 }

@@ -113,6 +113,11 @@ struct Plan {
     // per-kernel events (prof.on) aggregated by kernel name
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_device_ms = 0.0;
+    // stage timing (opts.verbose, as the reference's instrumented path):
+    // events at the stage boundaries of every chunk, 5 per chunk
+    std::vector<cudaEvent_t> stage_ev;
+    size_t stage_used = 0;
+    double stage_ms[4] = {};        // block build, tree build, propagate, leaf extract
     Prof prof;
     struct KStat {
         std::string name;

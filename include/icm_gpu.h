@@ -37,7 +37,10 @@ typedef struct {
                                    cache the children's spectra */
     int force_uncached_cufft_levels; /* ignored (no cuFFT levels) */
     int fast_mode;              /* ignored */
-    int verbose;                /* print the plan to stderr */
+    int verbose;                /* print the plan to stderr and report the
+                                   per-stage device times in IcmGpuRunStats
+                                   (block build, tree build, propagate, leaf
+                                   extraction; events at stage boundaries) */
 } IcmGpuOptions;
 
 /* [reference src/gpu/icm_gpu.h:36-50] */

@@ -306,3 +306,25 @@ def test_plan_graph_replay(gpu_icm, n, k):
         assert np.array_equal(a, b), (n, k, Q)
     direct.close()
     graphed.close()
+
+
+def test_verbose_stage_times(gpu_icm):
+    """IcmGpuOptions.verbose: per-stage device times in IcmGpuRunStats (block
+    build, tree build, propagate, leaf extraction), as the reference's
+    instrumented path reports them; the results do not change."""
+    from icm_gb300._lib import IcmGpuOptions
+    rng = np.random.default_rng(31)
+    S = 1e4 * np.exp(rng.standard_normal(20000))
+    P = 0.8 ** np.arange(3000)
+    gpu_icm.configure(q_chunk=100)   # three chunks: stage times add up over chunks
+    plain = gpu_icm.GpuPlan(S, len(P))
+    verbose = gpu_icm.GpuPlan(S, len(P), IcmGpuOptions(verbose=1))
+    a = plain.equity(P)
+    b, st = verbose.equity(P, return_stats=True)
+    gpu_icm.configure()
+    assert np.array_equal(a, b)
+    stages = [st["block_build_ns"], st["tree_build_ns"], st["tree_propagate_cached_ns"], st["leaf_extract_ns"]]
+    assert all(x > 0 for x in stages), stages
+    assert sum(stages) <= st["total_ns"]
+    plain.close()
+    verbose.close()
