@@ -445,8 +445,6 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
         case WOp::Divide:
         case WOp::SchoolBuild:
         case WOp::SchoolProp: launch_worklist_basic(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, f->stream); break;
-        case WOp::FusedBuild:
-        case WOp::FusedProp: launch_worklist_fused(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
         case WOp::SubBuild:
         case WOp::SubProp: launch_worklist_sub(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
         case WOp::Small: launch_worklist_small(s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;

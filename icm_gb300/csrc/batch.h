@@ -14,7 +14,7 @@ namespace icmg {
 // one launch: every descriptor of one step kind and transform size
 struct WStep {
     WOp op = WOp::Leaf;
-    int key = 0;                      // log2 of the transform size (0: plain kernels)
+    int key = 0;                      // launch variant: block size, transform size or lane width
     int one = 0;                      // 1: one node (the root's payout spectrum)
     int packed = 0;                   // 1: tab holds item slots (descriptor, item), cb per CTA
     int cb = 1;

@@ -49,10 +49,6 @@ struct Level {
     double *ends = nullptr;
 };
 
-struct TourDesc {          // batched mode: one tournament inside a batch plan
-    int n, k, off;         // players, paid places, offset into concatenated arrays
-};
-
 struct Plan {
     int n = 0, k = 0, B = 0, nblocks = 0, L = 0;
     int fft_min_deg = 64;

@@ -315,8 +315,6 @@ static size_t fused_smem_v_max() {
     for (int N = 8; N <= kFusedMaxN; N *= 2) mx = std::max(mx, fused_smem_v(N));
     return mx;
 }
-__global__ void kw_fused_build(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ tab, int q0);
-__global__ void kw_fused_prop(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ tab, int q0);
 
 bool fused_ok(int N) { return N >= 8 && N <= kFusedMaxN; }
 
@@ -345,8 +343,6 @@ void fused_set_smem_limits() {
     cudaFuncSetAttribute(kw_fused_prop_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fused_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fused_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(kw_fused_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(kw_fused_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
 static int ilog2i(int v) {
@@ -401,31 +397,5 @@ void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const 
     pr->end(st);
 }
 
-// ---------------------------------------------------------------- work lists
-__global__ void __launch_bounds__(kFusedThreads)
-kw_fused_build(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
-    const int2 t = tab[blockIdx.x];
-    FusedBuildArgs A = D[t.x];
-    A.z.q0 = q0;
-    fused_build_body(A, t.y, blockIdx.y);
-}
-__global__ void __launch_bounds__(kFusedThreads)
-kw_fused_prop(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
-    const int2 t = tab[blockIdx.x];
-    FusedPropArgs A = D[t.x];
-    A.z.q0 = q0;
-    fused_prop_body(A, t.y, blockIdx.y);
-}
-
-void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
-                           cudaStream_t st) {
-    if (nctas <= 0 || nq <= 0) return;
-    const dim3 g(nctas, nq);
-    switch (op) {
-        case WOp::FusedBuild: kw_fused_build<<<g, kFusedThreads, smem, st>>>((const FusedBuildArgs *)desc, tab, q0); break;
-        case WOp::FusedProp: kw_fused_prop<<<g, kFusedThreads, smem, st>>>((const FusedPropArgs *)desc, tab, q0); break;
-        default: break;
-    }
-}
 
 }  // namespace icmg

@@ -236,8 +236,6 @@ void launch_worklist_basic(WOp op, int B, const void *desc, const int2 *tab, int
                            cudaStream_t st);
 void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
                           cudaStream_t st);
-void launch_worklist_fused(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
-                           cudaStream_t st);
 // packed work lists: slots[s] = (descriptor, item); a CTA takes cb consecutive
 // slots, which may belong to different tournaments (SpecBuild, SpecProp)
 void launch_packed_spec(WOp op, const void *desc, const int2 *slots, int nslots, int cb, int nq, int q0, size_t smem,

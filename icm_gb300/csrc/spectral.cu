@@ -686,13 +686,6 @@ kw_spec_init(const SpecInitArgs *__restrict__ D, const int2 *__restrict__ tab, i
     spec_init_body(A, t.y, blockIdx.y);
 }
 __global__ void __launch_bounds__(kSpecThreads)
-kw_spec_build(const SpecBuildArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
-    const int2 t = tab[blockIdx.x];
-    SpecBuildArgs A = D[t.x];
-    A.z.q0 = q0;
-    spec_build_body(A, t.y, blockIdx.y);
-}
-__global__ void __launch_bounds__(kSpecThreads)
 kw_gspec(const GspecArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
     GspecArgs A = D[t.x];
@@ -707,20 +700,11 @@ __global__ void __launch_bounds__(kSpecThreads)
 kw_spec_prop_packed(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
     spec_prop_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
 }
-__global__ void __launch_bounds__(kSpecThreads)
-kw_spec_prop(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
-    const int2 t = tab[blockIdx.x];
-    SpecPropArgs A = D[t.x];
-    A.z.q0 = q0;
-    spec_prop_body(A, t.y, blockIdx.y);
-}
 
 void spec_wl_set_smem_limits() {
     const int mx = (int)spec_smem(kSpecMaxM), mv = (int)spec_smem_v_max();
     cudaFuncSetAttribute(kw_spec_init, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(kw_spec_build, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
     cudaFuncSetAttribute(kw_gspec, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(kw_spec_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
     cudaFuncSetAttribute(kw_spec_build_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
     cudaFuncSetAttribute(kw_spec_prop_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, mv);
 }
@@ -742,9 +726,7 @@ void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, 
     const dim3 g(nctas, nq);
     switch (op) {
         case WOp::SpecInit: kw_spec_init<<<g, kSpecThreads, smem, st>>>((const SpecInitArgs *)desc, tab, q0); break;
-        case WOp::SpecBuild: kw_spec_build<<<g, kSpecThreads, smem, st>>>((const SpecBuildArgs *)desc, tab, q0); break;
         case WOp::Gspec: kw_gspec<<<g, kSpecThreads, smem, st>>>((const GspecArgs *)desc, tab, q0); break;
-        case WOp::SpecProp: kw_spec_prop<<<g, kSpecThreads, smem, st>>>((const SpecPropArgs *)desc, tab, q0); break;
         default: break;
     }
 }
