@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <string>
 #include <vector>
 
@@ -71,39 +72,73 @@ namespace icmg {
 void api_set_error(const std::string &e) { set_error(e); }
 }
 
+// An entry point's work runs inside guarded(): a C++ exception (a host
+// allocation that fails, a thread that cannot start) becomes the entry
+// point's failure value with the message as the last error, instead of
+// unwinding into C callers.
+template <class R, class F>
+static R guarded(const char *name, R fail, F &&f) {
+    try {
+        return f();
+    } catch (const std::exception &e) {
+        set_error(std::string(name) + ": " + e.what());
+    } catch (...) {
+        set_error(std::string(name) + ": unknown error");
+    }
+    return fail;
+}
+
 extern "C" {
 
 // ------------------------------------------------------------ icm.h
 void icm_init(const char *wisdom_path) {
-    // The tuner table (the analogue of the reference's FFTW wisdom, read from
-    // the given path; a missing file keeps the defaults, as the reference's
-    // missing wisdom file does)
-    if (wisdom_path) {
-        std::string err;
-        tune_load(wisdom_path, err);
+    try {
+        // The tuner table (the analogue of the reference's FFTW wisdom, read from
+        // the given path; a missing file keeps the defaults, as the reference's
+        // missing wisdom file does)
+        if (wisdom_path) {
+            std::string err;
+            tune_load(wisdom_path, err);
+        }
+        if (g_device < 0) icm_gpu_init(0);
+    } catch (const std::exception &e) {
+        set_error(std::string("icm_init: ") + e.what());
+    } catch (...) {
+        set_error("icm_init: unknown error");
     }
-    if (g_device < 0) icm_gpu_init(0);
 }
 
 void icm_equity(int n, const double *S, int Q, const double *payout, int k, double *equity) {
-    t_last_status = 0;
-    if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !equity) {
-        fail_void(n, equity, "icm_equity: invalid arguments (need 1 <= k <= n, Q >= 1)");
-        return;
+    try {
+        t_last_status = 0;
+        if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !equity) {
+            fail_void(n, equity, "icm_equity: invalid arguments (need 1 <= k <= n, Q >= 1)");
+            return;
+        }
+        if (run_full(n, S, Q, payout, k, equity, nullptr, 0, nullptr, nullptr) != 0)
+            fail_void(n, equity, "icm_equity failed: " + t_last_error);
+    } catch (const std::exception &e) {
+        fail_void(n, equity, std::string("icm_equity: ") + e.what());
+    } catch (...) {
+        fail_void(n, equity, "icm_equity: unknown error");
     }
-    if (run_full(n, S, Q, payout, k, equity, nullptr, 0, nullptr, nullptr) != 0)
-        fail_void(n, equity, "icm_equity failed: " + t_last_error);
 }
 
 void icm_equity_subset(int n, const double *S, int Q, const double *payout, int k, double *equity,
                        const int *targets, int n_targets) {
-    t_last_status = 0;
-    if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !equity || !targets || n_targets < 1) {
-        fail_void(n, equity, "icm_equity_subset: invalid arguments");
-        return;
+    try {
+        t_last_status = 0;
+        if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !equity || !targets || n_targets < 1) {
+            fail_void(n, equity, "icm_equity_subset: invalid arguments");
+            return;
+        }
+        if (run_full(n, S, Q, payout, k, equity, targets, n_targets, nullptr, nullptr) != 0)
+            fail_void(n, equity, "icm_equity_subset failed: " + t_last_error);
+    } catch (const std::exception &e) {
+        fail_void(n, equity, std::string("icm_equity_subset: ") + e.what());
+    } catch (...) {
+        fail_void(n, equity, "icm_equity_subset: unknown error");
     }
-    if (run_full(n, S, Q, payout, k, equity, targets, n_targets, nullptr, nullptr) != 0)
-        fail_void(n, equity, "icm_equity_subset failed: " + t_last_error);
 }
 
 void *icm_tree_ctx_create(int, int) { return nullptr; }
@@ -150,26 +185,28 @@ void icm_v2_exact(int n, const double *S, double *V2) {
 
 // ------------------------------------------------------------ icm_gpu.h
 int icm_gpu_init(int device_id) {
-    int count = 0;
-    cudaError_t e = cudaGetDeviceCount(&count);
-    if (e != cudaSuccess) { set_error(std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e)); return 0; }
-    if (count <= 0) { set_error("No CUDA devices found"); return 0; }
-    if (device_id < 0) device_id = 0;
-    if (device_id >= count) {
-        set_error("Invalid CUDA device id " + std::to_string(device_id) + " (count=" + std::to_string(count) + ")");
-        return 0;
-    }
-    e = cudaSetDevice(device_id);
-    if (e != cudaSuccess) { set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e)); return 0; }
-    fft_set_smem_limits();
-    // keep freed plan arenas in this process's default pool for the next plan
-    cudaMemPool_t pool = nullptr;
-    if (cudaDeviceGetDefaultMemPool(&pool, device_id) == cudaSuccess) {
-        uint64_t keep = UINT64_MAX;
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    }
-    g_device = device_id;
-    return 1;
+    return guarded<int>("icm_gpu_init", 0, [&]() -> int {
+        int count = 0;
+        cudaError_t e = cudaGetDeviceCount(&count);
+        if (e != cudaSuccess) { set_error(std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e)); return 0; }
+        if (count <= 0) { set_error("No CUDA devices found"); return 0; }
+        if (device_id < 0) device_id = 0;
+        if (device_id >= count) {
+            set_error("Invalid CUDA device id " + std::to_string(device_id) + " (count=" + std::to_string(count) + ")");
+            return 0;
+        }
+        e = cudaSetDevice(device_id);
+        if (e != cudaSuccess) { set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e)); return 0; }
+        fft_set_smem_limits();
+        // keep freed plan arenas in this process's default pool for the next plan
+        cudaMemPool_t pool = nullptr;
+        if (cudaDeviceGetDefaultMemPool(&pool, device_id) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        g_device = device_id;
+        return 1;
+    });
 }
 
 void icm_gpu_shutdown(void) {
@@ -190,15 +227,17 @@ int icm_gpu_release_pooled_memory(void) {
 }
 
 IcmGpuPlan *icm_gpu_plan_create(int n, const double *S, int k, const IcmGpuOptions *opts) {
-    if (g_device < 0) {
-        set_error("icm_gpu_init must be called before icm_gpu_plan_create");
-        return nullptr;
-    }
-    if (!ensure_device()) return nullptr;
-    std::string err;
-    Plan *p = plan_create(n, S, k, opts, err);
-    if (!p) set_error(err);
-    return reinterpret_cast<IcmGpuPlan *>(p);
+    return guarded<IcmGpuPlan *>("icm_gpu_plan_create", nullptr, [&]() -> IcmGpuPlan * {
+        if (g_device < 0) {
+            set_error("icm_gpu_init must be called before icm_gpu_plan_create");
+            return nullptr;
+        }
+        if (!ensure_device()) return nullptr;
+        std::string err;
+        Plan *p = plan_create(n, S, k, opts, err);
+        if (!p) set_error(err);
+        return reinterpret_cast<IcmGpuPlan *>(p);
+    });
 }
 
 void icm_gpu_plan_destroy(IcmGpuPlan *plan) { plan_destroy(reinterpret_cast<Plan *>(plan)); }
@@ -224,48 +263,56 @@ int icm_gpu_plan_summary(const IcmGpuPlan *plan, IcmGpuPlanSummary *summary) {
 
 int icm_gpu_equity_with_plan(IcmGpuPlan *plan, int Q, const double *payout, double *equity,
                              IcmGpuRunStats *stats) {
-    Plan *p = reinterpret_cast<Plan *>(plan);
-    if (!p || !payout || !equity || Q <= 0) {
-        set_error("icm_gpu_equity_with_plan invalid arguments");
-        return -1;
-    }
-    if (!ensure_device()) return -1;
-    std::string err;
-    const int rc = plan_run(p, Q, payout, equity, stats, err);
-    t_launches = p->launches;
-    if (rc != 0) { set_error(err); return -1; }
-    return 0;
+    return guarded<int>("icm_gpu_equity_with_plan", -1, [&]() -> int {
+        Plan *p = reinterpret_cast<Plan *>(plan);
+        if (!p || !payout || !equity || Q <= 0) {
+            set_error("icm_gpu_equity_with_plan invalid arguments");
+            return -1;
+        }
+        if (!ensure_device()) return -1;
+        std::string err;
+        const int rc = plan_run(p, Q, payout, equity, stats, err);
+        t_launches = p->launches;
+        if (rc != 0) { set_error(err); return -1; }
+        return 0;
+    });
 }
 
 int icm_gpu_equity(int n, const double *S, int Q, const double *payout, int k, double *equity,
                    const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
-    if (n <= 0 || k <= 0 || k > n || Q <= 0 || !S || !payout || !equity) {
-        set_error("icm_gpu_equity invalid arguments");
-        return -1;
-    }
-    const double t0 = now_ns();
-    const int rc = run_full(n, S, Q, payout, k, equity, nullptr, 0, opts, stats);
-    if (rc == 0 && stats) stats->total_ns = now_ns() - t0;   // includes plan creation
-    return rc;
+    return guarded<int>("icm_gpu_equity", -1, [&]() -> int {
+        if (n <= 0 || k <= 0 || k > n || Q <= 0 || !S || !payout || !equity) {
+            set_error("icm_gpu_equity invalid arguments");
+            return -1;
+        }
+        const double t0 = now_ns();
+        const int rc = run_full(n, S, Q, payout, k, equity, nullptr, 0, opts, stats);
+        if (rc == 0 && stats) stats->total_ns = now_ns() - t0;   // includes plan creation
+        return rc;
+    });
 }
 
 int icm_gpu_equity_subset(int n, const double *S, int Q, const double *payout, int k, double *equity,
                           const int *targets, int n_targets, const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
-    if (n <= 0 || k <= 0 || k > n || Q <= 0 || n_targets <= 0 || !targets || !S || !payout || !equity) {
-        set_error("icm_gpu_equity_subset invalid arguments");
-        return -1;
-    }
-    const double t0 = now_ns();
-    const int rc = run_full(n, S, Q, payout, k, equity, targets, n_targets, opts, stats);
-    if (rc == 0 && stats) stats->total_ns = now_ns() - t0;
-    return rc;
+    return guarded<int>("icm_gpu_equity_subset", -1, [&]() -> int {
+        if (n <= 0 || k <= 0 || k > n || Q <= 0 || n_targets <= 0 || !targets || !S || !payout || !equity) {
+            set_error("icm_gpu_equity_subset invalid arguments");
+            return -1;
+        }
+        const double t0 = now_ns();
+        const int rc = run_full(n, S, Q, payout, k, equity, targets, n_targets, opts, stats);
+        if (rc == 0 && stats) stats->total_ns = now_ns() - t0;
+        return rc;
+    });
 }
 
 int icm_gpu_measure_hbm_bandwidth_gbps(double *gbps_out) {
-    if (!gbps_out || !ensure_device()) return 0;
-    std::string err;
-    if (measure_hbm_gbps(gbps_out, err) != 0) { set_error(err); return 0; }
-    return 1;
+    return guarded<int>("icm_gpu_measure_hbm_bandwidth_gbps", 0, [&]() -> int {
+        if (!gbps_out || !ensure_device()) return 0;
+        std::string err;
+        if (measure_hbm_gbps(gbps_out, err) != 0) { set_error(err); return 0; }
+        return 1;
+    });
 }
 
 int icm_gpu_measure_fused_pair_ns(int fft_n, int batch, int quick, double *build_ns_out, double *corr_ns_out);
@@ -278,38 +325,42 @@ int icm_gpu_measure_fused_r2c_pair_ns(int fft_n, int batch, int quick, double *b
 int icm_last_status(void) { return t_last_status; }
 
 int icm_gb300_player_order(int n, const double *S, int *perm) {
-    if (n < 1 || !S || !perm) { set_error("icm_gb300_player_order: invalid arguments"); return -1; }
-    for (int i = 0; i < n; ++i)
-        if (!(S[i] > 0.0) || !std::isfinite(S[i])) {
-            set_error("icm_gb300_player_order: stacks must be finite and positive");
-            return -1;
-        }
-    std::vector<int> p;
-    sort_players_desc(S, n, p);
-    std::copy(p.begin(), p.end(), perm);
-    return 0;
+    return guarded<int>("icm_gb300_player_order", -1, [&]() -> int {
+        if (n < 1 || !S || !perm) { set_error("icm_gb300_player_order: invalid arguments"); return -1; }
+        for (int i = 0; i < n; ++i)
+            if (!(S[i] > 0.0) || !std::isfinite(S[i])) {
+                set_error("icm_gb300_player_order: stacks must be finite and positive");
+                return -1;
+            }
+        std::vector<int> p;
+        sort_players_desc(S, n, p);
+        std::copy(p.begin(), p.end(), perm);
+        return 0;
+    });
 }
 
 void icm_gb300_test_fail_allocation(int nth) { set_alloc_failure(nth); }
 
 int icm_gb300_check_geometry(int n, int k, int block_size, int fft_min_degree, int flags, char *why, int why_len) {
-    if (n < 1 || k < 1 || k > n) { set_error("icm_gb300_check_geometry: need 1 <= k <= n"); return -1; }
-    const IcmGb300Config saved = g_config;
-    g_config.block_size = block_size;
-    g_config.fft_min_degree = fft_min_degree;
-    Plan p;
-    p.coeff_only = (flags & 1) != 0;
-    std::string err;
-    const std::vector<double> S(n, 1.0);   // stack values do not shape the tree
-    int rc = plan_geometry(&p, n, S.data(), k, err);
-    g_config = saved;
-    if (rc != 0) { set_error("icm_gb300_check_geometry: " + err); return -1; }
-    rc = plan_check_geometry(&p, err) == 0 ? 0 : 1;
-    if (why && why_len > 0) {
-        std::strncpy(why, rc ? err.c_str() : "", why_len - 1);
-        why[why_len - 1] = 0;
-    }
-    return rc;
+    return guarded<int>("icm_gb300_check_geometry", -1, [&]() -> int {
+        if (n < 1 || k < 1 || k > n) { set_error("icm_gb300_check_geometry: need 1 <= k <= n"); return -1; }
+        const IcmGb300Config saved = g_config;
+        g_config.block_size = block_size;
+        g_config.fft_min_degree = fft_min_degree;
+        Plan p;
+        p.coeff_only = (flags & 1) != 0;
+        std::string err;
+        const std::vector<double> S(n, 1.0);   // stack values do not shape the tree
+        int rc = plan_geometry(&p, n, S.data(), k, err);
+        g_config = saved;
+        if (rc != 0) { set_error("icm_gb300_check_geometry: " + err); return -1; }
+        rc = plan_check_geometry(&p, err) == 0 ? 0 : 1;
+        if (why && why_len > 0) {
+            std::strncpy(why, rc ? err.c_str() : "", why_len - 1);
+            why[why_len - 1] = 0;
+        }
+        return rc;
+    });
 }
 
 int icm_gb300_set_config(const IcmGb300Config *cfg) {
@@ -320,41 +371,47 @@ int icm_gb300_set_config(const IcmGb300Config *cfg) {
 
 int icm_gpu_equity_batched(int T, const int *n, const int *k, const double *S, const double *payout, int Q,
                            double *equity, IcmGpuRunStats *stats) {
-    if (T < 1 || !n || !k || !S || !payout || !equity || Q < 1) {
-        set_error("icm_gpu_equity_batched invalid arguments");
-        return -1;
-    }
-    if (!ensure_device()) return -1;
-    const double t0 = now_ns();
-    std::string err;
-    Forest *f = forest_create(T, n, k, S, err);
-    if (!f) { set_error("icm_gpu_equity_batched: " + err); return -1; }
-    f->graphs = false;   // one run: capturing would not pay
-    const int rc = forest_run(f, Q, payout, equity, stats, err);
-    t_launches = f->launches;
-    forest_destroy(f);
-    if (rc != 0) { set_error("icm_gpu_equity_batched: " + err); return -1; }
-    if (stats) stats->total_ns = now_ns() - t0;
-    return 0;
+    return guarded<int>("icm_gpu_equity_batched", -1, [&]() -> int {
+        if (T < 1 || !n || !k || !S || !payout || !equity || Q < 1) {
+            set_error("icm_gpu_equity_batched invalid arguments");
+            return -1;
+        }
+        if (!ensure_device()) return -1;
+        const double t0 = now_ns();
+        std::string err;
+        Forest *f = forest_create(T, n, k, S, err);
+        if (!f) { set_error("icm_gpu_equity_batched: " + err); return -1; }
+        f->graphs = false;   // one run: capturing would not pay
+        const int rc = forest_run(f, Q, payout, equity, stats, err);
+        t_launches = f->launches;
+        forest_destroy(f);
+        if (rc != 0) { set_error("icm_gpu_equity_batched: " + err); return -1; }
+        if (stats) stats->total_ns = now_ns() - t0;
+        return 0;
+    });
 }
 
 IcmGb300Batch *icm_gb300_batch_create(int T, const int *n, const int *k, const double *S) {
-    if (!ensure_device()) return nullptr;
-    std::string err;
-    Forest *f = forest_create(T, n, k, S, err);
-    if (!f) { set_error("icm_gb300_batch_create: " + err); return nullptr; }
-    return reinterpret_cast<IcmGb300Batch *>(f);
+    return guarded<IcmGb300Batch *>("icm_gb300_batch_create", nullptr, [&]() -> IcmGb300Batch * {
+        if (!ensure_device()) return nullptr;
+        std::string err;
+        Forest *f = forest_create(T, n, k, S, err);
+        if (!f) { set_error("icm_gb300_batch_create: " + err); return nullptr; }
+        return reinterpret_cast<IcmGb300Batch *>(f);
+    });
 }
 
 int icm_gb300_batch_run(IcmGb300Batch *b, int Q, const double *payout, double *equity, IcmGpuRunStats *stats) {
-    if (!b) { set_error("icm_gb300_batch_run: null batch"); return -1; }
-    if (!ensure_device()) return -1;
-    Forest *f = reinterpret_cast<Forest *>(b);
-    std::string err;
-    const int rc = forest_run(f, Q, payout, equity, stats, err);
-    t_launches = f->launches;
-    if (rc != 0) { set_error("icm_gb300_batch_run: " + err); return -1; }
-    return 0;
+    return guarded<int>("icm_gb300_batch_run", -1, [&]() -> int {
+        if (!b) { set_error("icm_gb300_batch_run: null batch"); return -1; }
+        if (!ensure_device()) return -1;
+        Forest *f = reinterpret_cast<Forest *>(b);
+        std::string err;
+        const int rc = forest_run(f, Q, payout, equity, stats, err);
+        t_launches = f->launches;
+        if (rc != 0) { set_error("icm_gb300_batch_run: " + err); return -1; }
+        return 0;
+    });
 }
 
 void icm_gb300_batch_destroy(IcmGb300Batch *b) { forest_destroy(reinterpret_cast<Forest *>(b)); }
@@ -402,23 +459,27 @@ int icm_gb300_batch_kernel_stats(const IcmGb300Batch *b, int i, char *name, int 
 
 // ------------------------------------------------------------ VJP
 IcmGb300Vjp *icm_gb300_vjp_create(int n, const double *S, int k) {
-    if (!ensure_device()) return nullptr;
-    std::string err;
-    VjpPlan *v = vjp_plan_create(n, S, k, err);
-    if (!v) { set_error("icm_gb300_vjp_create: " + err); return nullptr; }
-    return reinterpret_cast<IcmGb300Vjp *>(v);
+    return guarded<IcmGb300Vjp *>("icm_gb300_vjp_create", nullptr, [&]() -> IcmGb300Vjp * {
+        if (!ensure_device()) return nullptr;
+        std::string err;
+        VjpPlan *v = vjp_plan_create(n, S, k, err);
+        if (!v) { set_error("icm_gb300_vjp_create: " + err); return nullptr; }
+        return reinterpret_cast<IcmGb300Vjp *>(v);
+    });
 }
 
 int icm_gb300_vjp_run(IcmGb300Vjp *plan, int Q, const double *payout, const double *cot, double *grad_S,
                       double *grad_payout, int flags, IcmGpuRunStats *stats) {
-    if (!plan) { set_error("icm_gb300_vjp_run: null plan"); return -1; }
-    if (!ensure_device()) return -1;
-    VjpPlan *v = reinterpret_cast<VjpPlan *>(plan);
-    std::string err;
-    const int rc = vjp_plan_run(v, Q, payout, cot, grad_S, grad_payout, flags, stats, err);
-    t_launches = v->p->launches;
-    if (rc != 0) { set_error("icm_gb300_vjp_run: " + err); return -1; }
-    return 0;
+    return guarded<int>("icm_gb300_vjp_run", -1, [&]() -> int {
+        if (!plan) { set_error("icm_gb300_vjp_run: null plan"); return -1; }
+        if (!ensure_device()) return -1;
+        VjpPlan *v = reinterpret_cast<VjpPlan *>(plan);
+        std::string err;
+        const int rc = vjp_plan_run(v, Q, payout, cot, grad_S, grad_payout, flags, stats, err);
+        t_launches = v->p->launches;
+        if (rc != 0) { set_error("icm_gb300_vjp_run: " + err); return -1; }
+        return 0;
+    });
 }
 
 void icm_gb300_vjp_destroy(IcmGb300Vjp *plan) { vjp_plan_destroy(reinterpret_cast<VjpPlan *>(plan)); }
@@ -429,79 +490,91 @@ double icm_gb300_vjp_device_ms(const IcmGb300Vjp *plan) {
 
 int icm_gb300_equity_vjp(int n, const double *S, int Q, const double *payout, int k, const double *cot,
                          double *grad_S, double *grad_payout, int flags) {
-    if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !cot || !grad_S || !grad_payout) {
-        set_error("icm_gb300_equity_vjp: invalid arguments (need 1 <= k <= n, Q >= 1)");
-        return -1;
-    }
-    IcmGb300Vjp *v = icm_gb300_vjp_create(n, S, k);
-    if (!v) return -1;
-    const int rc = icm_gb300_vjp_run(v, Q, payout, cot, grad_S, grad_payout, flags, nullptr);
-    icm_gb300_vjp_destroy(v);
-    return rc;
+    return guarded<int>("icm_gb300_equity_vjp", -1, [&]() -> int {
+        if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !cot || !grad_S || !grad_payout) {
+            set_error("icm_gb300_equity_vjp: invalid arguments (need 1 <= k <= n, Q >= 1)");
+            return -1;
+        }
+        IcmGb300Vjp *v = icm_gb300_vjp_create(n, S, k);
+        if (!v) return -1;
+        const int rc = icm_gb300_vjp_run(v, Q, payout, cot, grad_S, grad_payout, flags, nullptr);
+        icm_gb300_vjp_destroy(v);
+        return rc;
+    });
 }
 
 int icm_gb300_equity_vjp_batched(int T, const int *n, const int *k, const double *S, const double *payout, int Q,
                                  const double *cot, double *grad_S, double *grad_payout, int flags) {
-    if (T < 1 || !n || !k || !S || !payout || !cot || !grad_S || !grad_payout || Q < 1) {
-        set_error("icm_gb300_equity_vjp_batched: invalid arguments");
-        return -1;
-    }
-    std::vector<long> so(T + 1, 0), po(T + 1, 0);
-    for (int t = 0; t < T; ++t) {
-        if (n[t] < 1 || k[t] < 1 || k[t] > n[t]) {
-            set_error("icm_gb300_equity_vjp_batched: tournament " + std::to_string(t) + " needs 1 <= k <= n");
+    return guarded<int>("icm_gb300_equity_vjp_batched", -1, [&]() -> int {
+        if (T < 1 || !n || !k || !S || !payout || !cot || !grad_S || !grad_payout || Q < 1) {
+            set_error("icm_gb300_equity_vjp_batched: invalid arguments");
             return -1;
         }
-        so[t + 1] = so[t] + n[t];
-        po[t + 1] = po[t] + k[t];
-    }
-    if (!ensure_device()) return -1;
-    std::string err;
-    Forest *f = forest_create(T, n, k, S, err, /*vjp=*/true);
-    if (!f) { set_error("icm_gb300_equity_vjp_batched: " + err); return -1; }
-    f->graphs = false;   // one run: capturing would not pay
-    const int rc = forest_vjp_run(f, Q, payout, cot, flags, grad_S, grad_payout, nullptr, err);
-    t_launches = f->launches;
-    forest_destroy(f);
-    if (rc != 0) { set_error("icm_gb300_equity_vjp_batched: " + err); return -1; }
-    return 0;
+        std::vector<long> so(T + 1, 0), po(T + 1, 0);
+        for (int t = 0; t < T; ++t) {
+            if (n[t] < 1 || k[t] < 1 || k[t] > n[t]) {
+                set_error("icm_gb300_equity_vjp_batched: tournament " + std::to_string(t) + " needs 1 <= k <= n");
+                return -1;
+            }
+            so[t + 1] = so[t] + n[t];
+            po[t + 1] = po[t] + k[t];
+        }
+        if (!ensure_device()) return -1;
+        std::string err;
+        Forest *f = forest_create(T, n, k, S, err, /*vjp=*/true);
+        if (!f) { set_error("icm_gb300_equity_vjp_batched: " + err); return -1; }
+        f->graphs = false;   // one run: capturing would not pay
+        const int rc = forest_vjp_run(f, Q, payout, cot, flags, grad_S, grad_payout, nullptr, err);
+        t_launches = f->launches;
+        forest_destroy(f);
+        if (rc != 0) { set_error("icm_gb300_equity_vjp_batched: " + err); return -1; }
+        return 0;
+    });
 }
 
 IcmGb300Batch *icm_gb300_vjp_batch_create(int T, const int *n, const int *k, const double *S) {
-    if (!ensure_device()) return nullptr;
-    std::string err;
-    Forest *f = forest_create(T, n, k, S, err, /*vjp=*/true);
-    if (!f) { set_error("icm_gb300_vjp_batch_create: " + err); return nullptr; }
-    return reinterpret_cast<IcmGb300Batch *>(f);
+    return guarded<IcmGb300Batch *>("icm_gb300_vjp_batch_create", nullptr, [&]() -> IcmGb300Batch * {
+        if (!ensure_device()) return nullptr;
+        std::string err;
+        Forest *f = forest_create(T, n, k, S, err, /*vjp=*/true);
+        if (!f) { set_error("icm_gb300_vjp_batch_create: " + err); return nullptr; }
+        return reinterpret_cast<IcmGb300Batch *>(f);
+    });
 }
 
 int icm_gb300_vjp_batch_run(IcmGb300Batch *b, int Q, const double *payout, const double *cot, double *grad_S,
                             double *grad_payout, int flags, IcmGpuRunStats *stats) {
-    if (!b) { set_error("icm_gb300_vjp_batch_run: null batch"); return -1; }
-    if (!ensure_device()) return -1;
-    Forest *f = reinterpret_cast<Forest *>(b);
-    std::string err;
-    const int rc = forest_vjp_run(f, Q, payout, cot, flags, grad_S, grad_payout, stats, err);
-    t_launches = f->launches;
-    if (rc != 0) { set_error("icm_gb300_vjp_batch_run: " + err); return -1; }
-    return 0;
+    return guarded<int>("icm_gb300_vjp_batch_run", -1, [&]() -> int {
+        if (!b) { set_error("icm_gb300_vjp_batch_run: null batch"); return -1; }
+        if (!ensure_device()) return -1;
+        Forest *f = reinterpret_cast<Forest *>(b);
+        std::string err;
+        const int rc = forest_vjp_run(f, Q, payout, cot, flags, grad_S, grad_payout, stats, err);
+        t_launches = f->launches;
+        if (rc != 0) { set_error("icm_gb300_vjp_batch_run: " + err); return -1; }
+        return 0;
+    });
 }
 
 // ------------------------------------------------------------ tuner, Q ladder
 int icm_gb300_tuner_load(const char *path) {
-    if (!path) { set_error("icm_gb300_tuner_load: null path"); return -1; }
-    std::string err;
-    const int r = tune_load(path, err);
-    if (r < 0) set_error("icm_gb300_tuner_load: " + err);
-    return r;
+    return guarded<int>("icm_gb300_tuner_load", -1, [&]() -> int {
+        if (!path) { set_error("icm_gb300_tuner_load: null path"); return -1; }
+        std::string err;
+        const int r = tune_load(path, err);
+        if (r < 0) set_error("icm_gb300_tuner_load: " + err);
+        return r;
+    });
 }
 
 int icm_gb300_tuner_save(const char *path) {
-    if (!path) { set_error("icm_gb300_tuner_save: null path"); return -1; }
-    std::string err;
-    const int r = tune_save(path, err);
-    if (r < 0) set_error("icm_gb300_tuner_save: " + err);
-    return r;
+    return guarded<int>("icm_gb300_tuner_save", -1, [&]() -> int {
+        if (!path) { set_error("icm_gb300_tuner_save: null path"); return -1; }
+        std::string err;
+        const int r = tune_save(path, err);
+        if (r < 0) set_error("icm_gb300_tuner_save: " + err);
+        return r;
+    });
 }
 
 void icm_gb300_tuner_clear(void) { tune_clear(); }
@@ -514,64 +587,70 @@ int icm_gb300_tuner_lookup(int n, int k, int *block_size, int *fft_min_degree) {
 
 int icm_gb300_autotune(int n, const double *S, int Q, const double *payout, int k, int runs, int *block_size,
                        int *fft_min_degree, double *best_ms) {
-    if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !block_size || !fft_min_degree || !best_ms) {
-        set_error("icm_gb300_autotune: invalid arguments");
-        return -1;
-    }
-    if (!ensure_device()) return -1;
-    std::string err;
-    if (tune_search(n, S, Q, payout, k, runs, block_size, fft_min_degree, best_ms, err) != 0) {
-        set_error("icm_gb300_autotune: " + err);
-        return -1;
-    }
-    return 0;
+    return guarded<int>("icm_gb300_autotune", -1, [&]() -> int {
+        if (n < 1 || k < 1 || k > n || Q < 1 || !S || !payout || !block_size || !fft_min_degree || !best_ms) {
+            set_error("icm_gb300_autotune: invalid arguments");
+            return -1;
+        }
+        if (!ensure_device()) return -1;
+        std::string err;
+        if (tune_search(n, S, Q, payout, k, runs, block_size, fft_min_degree, best_ms, err) != 0) {
+            set_error("icm_gb300_autotune: " + err);
+            return -1;
+        }
+        return 0;
+    });
 }
 
 int icm_gb300_equity_adaptive(int n, const double *S, const double *payout, int k, int Q0, double tol, int Qmax,
                               double *equity, int *Q_used, double *est_err) {
-    if (n < 1 || k < 1 || k > n || Q0 < 2 || Qmax < Q0 || !(tol > 0.0) || !S || !payout || !equity) {
-        set_error("icm_gb300_equity_adaptive: invalid arguments (need 1 <= k <= n, 2 <= Q0 <= Qmax, tol > 0)");
-        return -1;
-    }
-    if (!ensure_device()) return -1;
-    std::string err;
-    Plan *p = plan_create(n, S, k, nullptr, err);
-    if (!p) { set_error("icm_gb300_equity_adaptive: " + err); return -1; }
-    std::vector<double> prev(n), cur(n);
-    int Q = Q0;
-    double e = INFINITY;
-    int rc = plan_run(p, Q, payout, prev.data(), nullptr, err);
-    long launches = p->launches;
-    // double Q until two successive rules agree to tol (relative, per player,
-    // against a floor of 1e-12 of the largest equity)
-    while (rc == 0 && 2L * Q <= Qmax) {
-        rc = plan_run(p, 2 * Q, payout, cur.data(), nullptr, err);
-        launches += p->launches;
-        if (rc != 0) break;
-        Q *= 2;
-        double mx = 0.0;
-        for (int i = 0; i < n; ++i) mx = std::max(mx, std::fabs(cur[i]));
-        const double floor = 1e-12 * mx;
-        e = 0.0;
-        for (int i = 0; i < n; ++i)
-            e = std::max(e, std::fabs(cur[i] - prev[i]) / std::max(std::fabs(cur[i]), floor));
-        prev.swap(cur);
-        if (e <= tol) break;
-    }
-    plan_destroy(p);
-    t_launches = launches;
-    if (rc != 0) { set_error("icm_gb300_equity_adaptive: " + err); return -1; }
-    memcpy(equity, prev.data(), sizeof(double) * n);
-    if (Q_used) *Q_used = Q;
-    if (est_err) *est_err = e;
-    return 0;
+    return guarded<int>("icm_gb300_equity_adaptive", -1, [&]() -> int {
+        if (n < 1 || k < 1 || k > n || Q0 < 2 || Qmax < Q0 || !(tol > 0.0) || !S || !payout || !equity) {
+            set_error("icm_gb300_equity_adaptive: invalid arguments (need 1 <= k <= n, 2 <= Q0 <= Qmax, tol > 0)");
+            return -1;
+        }
+        if (!ensure_device()) return -1;
+        std::string err;
+        Plan *p = plan_create(n, S, k, nullptr, err);
+        if (!p) { set_error("icm_gb300_equity_adaptive: " + err); return -1; }
+        std::vector<double> prev(n), cur(n);
+        int Q = Q0;
+        double e = INFINITY;
+        int rc = plan_run(p, Q, payout, prev.data(), nullptr, err);
+        long launches = p->launches;
+        // double Q until two successive rules agree to tol (relative, per player,
+        // against a floor of 1e-12 of the largest equity)
+        while (rc == 0 && 2L * Q <= Qmax) {
+            rc = plan_run(p, 2 * Q, payout, cur.data(), nullptr, err);
+            launches += p->launches;
+            if (rc != 0) break;
+            Q *= 2;
+            double mx = 0.0;
+            for (int i = 0; i < n; ++i) mx = std::max(mx, std::fabs(cur[i]));
+            const double floor = 1e-12 * mx;
+            e = 0.0;
+            for (int i = 0; i < n; ++i)
+                e = std::max(e, std::fabs(cur[i] - prev[i]) / std::max(std::fabs(cur[i]), floor));
+            prev.swap(cur);
+            if (e <= tol) break;
+        }
+        plan_destroy(p);
+        t_launches = launches;
+        if (rc != 0) { set_error("icm_gb300_equity_adaptive: " + err); return -1; }
+        memcpy(equity, prev.data(), sizeof(double) * n);
+        if (Q_used) *Q_used = Q;
+        if (est_err) *est_err = e;
+        return 0;
+    });
 }
 
 int icm_gpu_measure_fp64_gflops(double *gflops_out) {
-    if (!gflops_out || !ensure_device()) return 0;
-    std::string err;
-    if (measure_fp64_gflops(gflops_out, err) != 0) { set_error(err); return 0; }
-    return 1;
+    return guarded<int>("icm_gpu_measure_fp64_gflops", 0, [&]() -> int {
+        if (!gflops_out || !ensure_device()) return 0;
+        std::string err;
+        if (measure_fp64_gflops(gflops_out, err) != 0) { set_error(err); return 0; }
+        return 1;
+    });
 }
 
 long icm_gpu_last_launch_count(void) { return t_launches; }
