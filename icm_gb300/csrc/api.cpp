@@ -56,6 +56,12 @@ int run_full(int n, const double *S, int Q, const double *payout, int k, double 
              int n_targets, const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
     if (!ensure_device()) return -1;
     std::string err;
+    if (!opts || (!opts->verbose && opts->memory_strategy != 1)) {   // small fields: no plan at all
+        long nl = 0;
+        const int r = small_solve(n, S, Q, payout, k, equity, targets, n_targets, stats, &nl, err);
+        if (r < 0) { set_error(err); return -1; }
+        if (r == 1) { t_launches = nl; return 0; }
+    }
     Plan *p = plan_create(n, S, k, opts, err);
     if (!p) { set_error(err); return -1; }
     int rc = 0;
@@ -213,6 +219,7 @@ void icm_gpu_shutdown(void) {
     if (g_device >= 0) {
         cudaSetDevice(g_device);
         cudaDeviceSynchronize();
+        small_context_release();   // this thread's one-shot buffers
     }
 }
 
@@ -220,6 +227,7 @@ const char *icm_gpu_last_error(void) { return t_last_error.c_str(); }
 
 int icm_gpu_release_pooled_memory(void) {
     if (g_device < 0) return -1;
+    small_context_release();   // this thread's one-shot buffers
     cudaMemPool_t pool = nullptr;
     if (cudaDeviceGetDefaultMemPool(&pool, g_device) != cudaSuccess) return -1;
     if (cudaMemPoolTrimTo(pool, 0) != cudaSuccess) return -1;

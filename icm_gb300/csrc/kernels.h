@@ -321,6 +321,11 @@ void launch_small(const SmallArgs &A, int nq, int q0, cudaStream_t st, Prof *pr,
 void launch_worklist_small(int B, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
                            cudaStream_t st);
 void small_set_smem_limits();
+// one-shot solve of a small tournament without a plan: 1 when solved, 0 when
+// the tournament is not on the small path, -1 on error (err set)
+int small_solve(int n, const double *S, int Q, const double *payout, int k, double *equity, const int *targets,
+                int n_targets, IcmGpuRunStats *stats, long *launches, std::string &err);
+void small_context_release();
 
 // ---- linear engine (linear.cu): one warp per (tournament, node), k <= 256
 constexpr int kLinearMaxK = 256;

@@ -18,6 +18,9 @@
 // schoolbook kernels' (same terms, same order) and the division is the
 // level path's divide_dot.
 #include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
 
 #include "engine.h"
 #include "kernels.h"
@@ -260,6 +263,126 @@ void launch_worklist_small(int B, const void *desc, const int2 *tab, int nctas, 
         case 16: kw_small<16><<<g, kSmallThreads, smem, st>>>(D, tab, q0, nq); break;
         default: kw_small<32><<<g, kSmallThreads, smem, st>>>(D, tab, q0, nq); break;
     }
+}
+
+// ---- one-shot small solves without a plan (icm_equity, icm_gpu_equity):
+// a per-thread context keeps a stream, a grow-only device buffer and a
+// grow-only pinned staging buffer across calls, so a solve is one packed
+// upload (stacks, nodes, payout, permutation, subset mask and the CTA
+// counter), one launch per 256 nodes and one download; no plan, arena or
+// stream is created.  The kernels and their arguments are the plan path's,
+// so the equities are identical to it.
+namespace {
+struct SmallCtx {
+    int dev = -1;
+    cudaStream_t st = nullptr;
+    char *d = nullptr;
+    size_t dcap = 0;
+    char *h = nullptr;
+    size_t hcap = 0;
+    void release() {
+        if (st) cudaStreamSynchronize(st);
+        if (d) cudaFree(d);
+        if (h) cudaFreeHost(h);
+        if (st) cudaStreamDestroy(st);
+        *this = SmallCtx{};
+    }
+};
+thread_local SmallCtx t_small;
+size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
+}  // namespace
+
+void small_context_release() { t_small.release(); }
+
+int small_solve(int n, const double *S, int Q, const double *payout, int k, double *equity, const int *targets,
+                int n_targets, IcmGpuRunStats *stats, long *launches, std::string &err) {
+    Plan p;
+    if (plan_geometry(&p, n, S, k, err) != 0) return -1;
+    if (!p.small) return 0;
+    std::vector<double> logv, w;
+    make_nodes(Q, p.Smax, logv, w);
+    int nact = 0;
+    for (int q = 0; q < Q; ++q) nact += w[q] != 0.0;
+    int qc = std::min(std::max(nact, 1), 256);   // node chunks as a plan would take them
+    if (g_config.q_chunk > 0) qc = std::min(qc, g_config.q_chunk);
+    // layout: the uploaded prefix, then the device-only arrays
+    size_t off = 0;
+    auto take = [&](size_t b) { size_t o = off; off += up256(b); return o; };
+    const size_t o_S = take(8 * (size_t)n), o_node = take(24 * (size_t)std::max(nact, 1)), o_pay = take(8 * (size_t)k);
+    const size_t o_perm = take(4 * (size_t)n), o_act = take(targets ? (size_t)n : 0), o_cnt = take(4);
+    const size_t up = off;
+    const size_t o_con = take(8 * (size_t)qc * n), o_acc = take(8 * (size_t)n), o_out = take(8 * (size_t)n);
+    SmallCtx &c = t_small;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (c.dev != dev) {
+        c.release();
+        if (cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) != cudaSuccess) { err = "stream"; return -1; }
+        c.dev = dev;
+    }
+    if (c.dcap < off) {
+        if (c.d) { cudaStreamSynchronize(c.st); cudaFree(c.d); c.d = nullptr; c.dcap = 0; }
+        const cudaError_t e = dev_alloc((void **)&c.d, off, c.st, false);
+        if (e != cudaSuccess) { err = std::string("device allocation: ") + cudaGetErrorString(e); return -1; }
+        c.dcap = off;
+    }
+    if (c.hcap < up) {
+        if (c.h) { cudaStreamSynchronize(c.st); cudaFreeHost(c.h); c.h = nullptr; c.hcap = 0; }
+        if (cudaMallocHost((void **)&c.h, up) != cudaSuccess) { err = "pinned staging buffer"; return -1; }
+        c.hcap = up;
+    }
+    char *H = c.h;
+    std::memcpy(H + o_S, p.S_sorted.data(), 8 * (size_t)n);
+    double *nd = (double *)(H + o_node);
+    for (int q = 0, j = 0; q < Q; ++q) {
+        if (w[q] == 0.0) continue;   // the reference skips zero-weight nodes
+        nd[3 * j] = logv[q];
+        nd[3 * j + 1] = w[q];
+        nd[3 * j + 2] = std::exp(-logv[q]);
+        ++j;
+    }
+    std::memcpy(H + o_pay, payout, 8 * (size_t)k);
+    std::memcpy(H + o_perm, p.perm.data(), 4 * (size_t)n);
+    if (targets) {
+        uint8_t *act = (uint8_t *)(H + o_act);
+        std::memset(act, 0, (size_t)n);
+        for (int t = 0; t < n_targets; ++t)
+            if (targets[t] >= 0 && targets[t] < n) act[p.inv_perm[targets[t]]] = 1;
+    }
+    *(unsigned *)(H + o_cnt) = 0u;
+    char *D = c.d;
+    cudaError_t e = cudaMemcpyAsync(D, H, up, cudaMemcpyHostToDevice, c.st);
+    if (nact == 0 && e == cudaSuccess) e = cudaMemsetAsync(D + o_out, 0, 8 * (size_t)n, c.st);
+    long nl = 0;
+    if (nact > 0 && e == cudaSuccess) {
+        SmallArgs A = small_args(&p, (const double *)(D + o_S), (const double *)(D + o_node),
+                                 (const double *)(D + o_pay), (double *)(D + o_con), (size_t)n,
+                                 targets ? (const uint8_t *)(D + o_act) : nullptr);
+        A.counter = (unsigned *)(D + o_cnt);
+        A.acc = (double *)(D + o_acc);
+        A.out = (double *)(D + o_out);
+        A.perm = (const int *)(D + o_perm);
+        Prof off_prof;
+        for (int q0 = 0; q0 < nact; q0 += qc) {
+            const int nq = std::min(qc, nact - q0);
+            A.first = q0 == 0;
+            A.last = q0 + nq >= nact;
+            launch_small(A, nq, q0, c.st, &off_prof, 0.0);
+            ++nl;
+        }
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(equity, D + o_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, c.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.st);
+    if (e != cudaSuccess) { err = std::string("small solve: ") + cudaGetErrorString(e); return -1; }
+    if (launches) *launches = nl;
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->peak_vram_bytes = off;
+        stats->engine = 1;
+        stats->B = p.B;
+    }
+    return 1;
 }
 
 template <int B>

@@ -2,8 +2,9 @@
 the n-th device allocation fail as an exhausted allocator would.  Every entry
 point must report the failure (-1 / NULL with the error text, ICMError in
 Python), leave nothing half-built, and give correct results on the next call.
-Allocation order: plans -- arena, node table; batches -- arena, node tables,
-work lists; VJP plans -- plan arena, VJP buffers, node table."""
+Allocation order: small one-shot solves -- the per-thread buffer; plans --
+arena, node table; batches -- arena, node tables, work lists; VJP plans --
+plan arena, VJP buffers, node table."""
 import numpy as np
 import pytest
 
@@ -22,11 +23,14 @@ def _tournaments(seed, sizes):
     return [(1e4 * np.exp(rng.standard_normal(n)), 0.8 ** np.arange(max(1, n // 6))) for n in sizes]
 
 
-@pytest.mark.parametrize("n", [40, 5000])    # small path, tree levels
-@pytest.mark.parametrize("nth", [1, 2])
+@pytest.mark.parametrize("n,nth", [(40, 1), (5000, 1), (5000, 2)])   # one-shot small path; plan arena, node table
 def test_single_solve_allocation_failure(gpu_icm, hook, n, nth):
+    """Small fields run without a plan on a per-thread context that keeps its
+    buffers; releasing them makes the next solve allocate again."""
+    from icm_gb300._lib import lib
     (S, P), = _tournaments(n, [n])
     ref = gpu_icm.gpu_equity(S, P)
+    lib().icm_gpu_release_pooled_memory()
     hook(nth)
     with pytest.raises(gpu_icm.ICMError, match="out of memory"):
         gpu_icm.gpu_equity(S, P)
