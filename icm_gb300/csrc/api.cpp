@@ -56,7 +56,10 @@ int run_full(int n, const double *S, int Q, const double *payout, int k, double 
              int n_targets, const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
     if (!ensure_device()) return -1;
     std::string err;
-    if (!opts || (!opts->verbose && opts->memory_strategy != 1)) {   // small fields: no plan at all
+    // small fields: no plan at all (only fields within the small path's largest
+    // limit are classified here, so larger ones are sorted once, by the plan)
+    const int small_cap = std::max(kSmallMaxN, g_config.small_max_n);
+    if (n <= small_cap && (!opts || (!opts->verbose && opts->memory_strategy != 1))) {
         long nl = 0;
         const int r = small_solve(n, S, Q, payout, k, equity, targets, n_targets, stats, &nl, err);
         if (r < 0) { set_error(err); return -1; }

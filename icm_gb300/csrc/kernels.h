@@ -288,6 +288,7 @@ void sub_set_smem_limits();
 
 // ---- small tournaments (small.cu): the whole per-node pipeline in one CTA
 constexpr size_t kSmallMaxSmem = 200 * 1024;
+constexpr int kSmallMaxN = 1536;   // the largest default limit of the small path (plan_small_ok)
 constexpr int kSmallMaxLevels = 24;
 struct SmallLevel {
     int nreal, pst, plen, gst, glen;

@@ -193,7 +193,7 @@ bool plan_small_ok(const Plan *p) {
     if (p->coeff_only || g_config.small_max_n < 0) return false;
     int lim;
     if (g_config.small_max_n > 0) lim = g_config.small_max_n;
-    else lim = p->k <= 16 ? 1536 : p->k <= 64 ? 768 : p->k <= 128 ? 640 : p->k <= 256 ? 384 : 288;
+    else lim = p->k <= 16 ? kSmallMaxN : p->k <= 64 ? 768 : p->k <= 128 ? 640 : p->k <= 256 ? 384 : 288;
     if (p->n > lim || p->L > kSmallMaxLevels) return false;
     return small_smem_bytes(p) <= kSmallMaxSmem;
 }
