@@ -52,6 +52,55 @@ void fail_void(int n, double *equity, const std::string &what) {
         for (int i = 0; i < n; ++i) equity[i] = std::nan("");
 }
 
+// The calling thread's last one-shot plan, kept when its arena is small:
+// reused by the next call of the same shape under the same options, engine
+// configuration and tuner table (the geometry depends on nothing else).
+struct PlanCache {
+    Plan *p = nullptr;
+    IcmGpuOptions opts{};
+    IcmGb300Config cfg{};
+    long tune_gen = -1;
+    int dev = -1;
+};
+thread_local PlanCache t_plan;
+constexpr size_t kPlanCacheMaxBytes = (size_t)512 << 20;
+
+bool same_opts(const IcmGpuOptions &a, const IcmGpuOptions &b) {
+    IcmGpuOptions x = a, y = b;
+    x.device_id = y.device_id = 0;
+    return std::memcmp(&x, &y, sizeof x) == 0;
+}
+
+void drop_cached_plan() {
+    if (t_plan.p) plan_destroy(t_plan.p);
+    t_plan = PlanCache{};
+}
+
+Plan *cached_plan(int n, int k, const IcmGpuOptions *opts) {
+    PlanCache &c = t_plan;
+    if (!c.p) return nullptr;
+    const IcmGpuOptions o = opts ? *opts : IcmGpuOptions{};
+    Plan *p = nullptr;
+    if (c.p->n == n && c.p->k == k && c.dev == g_device && c.tune_gen == g_tune_generation.load() &&
+        same_opts(c.opts, o) && std::memcmp(&c.cfg, &g_config, sizeof c.cfg) == 0)
+        p = c.p;
+    else
+        plan_destroy(c.p);
+    c = PlanCache{};
+    return p;   // taken out of the cache while in use
+}
+
+bool keep_plan(Plan *p, const IcmGpuOptions *opts) {
+    if (p->arena_bytes > kPlanCacheMaxBytes) return false;
+    drop_cached_plan();
+    t_plan.p = p;
+    t_plan.opts = opts ? *opts : IcmGpuOptions{};
+    t_plan.cfg = g_config;
+    t_plan.tune_gen = g_tune_generation.load();
+    t_plan.dev = g_device;
+    return true;
+}
+
 int run_full(int n, const double *S, int Q, const double *payout, int k, double *equity, const int *targets,
              int n_targets, const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
     if (!ensure_device()) return -1;
@@ -65,13 +114,19 @@ int run_full(int n, const double *S, int Q, const double *payout, int k, double 
         if (r < 0) { set_error(err); return -1; }
         if (r == 1) { t_launches = nl; return 0; }
     }
-    Plan *p = plan_create(n, S, k, opts, err);
-    if (!p) { set_error(err); return -1; }
+    // repeated calls of one shape reuse the thread's last plan (new stacks only)
+    Plan *p = targets ? nullptr : cached_plan(n, k, opts);
+    if (p) {
+        if (plan_restack(p, S, err) != 0) { set_error(err); return -1; }
+    } else {
+        p = plan_create(n, S, k, opts, err);
+        if (!p) { set_error(err); return -1; }
+    }
     int rc = 0;
     if (targets) rc = plan_set_targets(p, targets, n_targets, err);
     if (rc == 0) rc = plan_run(p, Q, payout, equity, stats, err);
     t_launches = p->launches;
-    plan_destroy(p);
+    if (rc != 0 || targets || !keep_plan(p, opts)) plan_destroy(p);
     if (rc != 0) { set_error(err); return -1; }
     return 0;
 }
@@ -222,7 +277,8 @@ void icm_gpu_shutdown(void) {
     if (g_device >= 0) {
         cudaSetDevice(g_device);
         cudaDeviceSynchronize();
-        small_context_release();   // this thread's one-shot buffers
+        small_context_release();   // this thread's one-shot buffers and plan
+        drop_cached_plan();
     }
 }
 
@@ -230,7 +286,8 @@ const char *icm_gpu_last_error(void) { return t_last_error.c_str(); }
 
 int icm_gpu_release_pooled_memory(void) {
     if (g_device < 0) return -1;
-    small_context_release();   // this thread's one-shot buffers
+    small_context_release();   // this thread's one-shot buffers and plan
+    drop_cached_plan();
     cudaMemPool_t pool = nullptr;
     if (cudaDeviceGetDefaultMemPool(&pool, g_device) != cudaSuccess) return -1;
     if (cudaMemPoolTrimTo(pool, 0) != cudaSuccess) return -1;

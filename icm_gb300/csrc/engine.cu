@@ -599,6 +599,26 @@ static bool root_gspec_forkable(const Plan *p) {
     return L >= 2 && p->Lf < L - 1 && p->lv[L - 1].kind == 2 && p->lv[L - 1].deg / 2 <= kSpecMaxD;
 }
 
+int plan_restack(Plan *p, const double *S, std::string &err) {
+    const int n = p->n;
+    for (int i = 0; i < n; ++i)
+        if (!(S[i] > 0.0) || !std::isfinite(S[i])) {
+            err = "stacks must be finite and positive (S[" + std::to_string(i) + "])";
+            return -1;
+        }
+    sort_players_desc(S, n, p->perm);
+    for (int i = 0; i < n; ++i) {
+        p->S_sorted[i] = S[p->perm[i]];
+        p->inv_perm[p->perm[i]] = i;
+    }
+    p->Smax = p->S_sorted[0];
+    cudaError_t e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p->d_perm, p->perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, p->stream);
+    if (e != cudaSuccess) { err = std::string("stack upload: ") + cudaGetErrorString(e); return -1; }
+    return 0;
+}
+
 // subset: active players (sorted order) and per-level hot bitmaps
 // (reference src/cpu/icm.c:2430-2473)
 int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &err) {

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -133,6 +134,9 @@ cudaError_t dev_alloc(void **ptr, size_t bytes, cudaStream_t st, bool pooled);
 void set_alloc_failure(int nth);
 // invariants the kernels rely on (host only): 0, or -1 with the violation
 int plan_check_geometry(const Plan *p, std::string &why);
+// new stacks for a plan of the same shape (n, k): sort, sorted copies on the
+// host and the device; the tree geometry and buffers are kept
+int plan_restack(Plan *p, const double *S, std::string &err);
 // player order: stacks descending, ties by index
 void sort_players_desc(const double *S, int n, std::vector<int> &perm);
 // tree buffers for chunks of qc nodes from `base` (nullptr: size only)
@@ -174,6 +178,7 @@ int measure_hbm_gbps(double *out, std::string &err);
 
 // tuner table (tune.cpp)
 void tune_lookup(int n, int k, int *B, int *fft_min);
+extern std::atomic<long> g_tune_generation;   // changes of the tuner table (tune.cpp)
 // built-in choices for GB300 where the caller's table has none (0: none)
 void tune_builtin(int n, int k, int *B, int *fft_min);
 void tune_record(int n, int k, int B, int fft_min, double ms);

@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -26,6 +27,10 @@
 #include "engine.h"
 
 namespace icmg {
+
+// bumped by every change to the table, so cached plans can tell that their
+// block size or crossover may be stale
+std::atomic<long> g_tune_generation{0};
 
 namespace {
 struct TuneEntry {
@@ -89,6 +94,7 @@ void tune_lookup(int n, int k, int *B, int *fft_min) {
 
 void tune_record(int n, int k, int B, int fft_min, double ms) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
+    ++g_tune_generation;
     const int ln = log2ceil(n), kb = tune_kbucket(n, k);
     for (TuneEntry &e : g_tune)
         if (e.log2n == ln && e.kbucket == kb) {
@@ -99,6 +105,7 @@ void tune_record(int n, int k, int B, int fft_min, double ms) {
 }
 
 int tune_load(const char *path, std::string &err) {
+    ++g_tune_generation;
     FILE *f = fopen(path, "r");
     if (!f) { err = std::string("cannot open ") + path; return -1; }
     char line[512];
@@ -146,6 +153,7 @@ int tune_save(const char *path, std::string &err) {
 
 void tune_clear() {
     std::lock_guard<std::mutex> lk(g_tune_mu);
+    ++g_tune_generation;
     g_tune.clear();
 }
 

@@ -328,3 +328,28 @@ def test_verbose_stage_times(gpu_icm):
     assert sum(stages) <= st["total_ns"]
     plain.close()
     verbose.close()
+
+
+def test_one_shot_plan_reuse(gpu_icm):
+    """Repeated one-shot calls of one shape reuse the thread's last plan with
+    new stacks; results equal fresh plans bit for bit, and a configuration
+    change is not served by a plan built under the old one."""
+    rng = np.random.default_rng(77)
+    n, k = 3000, 450
+    P = 0.9 ** np.arange(k)
+    stacks = [1e4 * np.exp(s * rng.standard_normal(n)) for s in (1.0, 2.0, 0.5, 1.0)]
+
+    def fresh(S):
+        p = gpu_icm.GpuPlan(S, k)
+        e = p.equity(P)
+        p.close()
+        return e
+    for S in stacks:
+        assert np.array_equal(gpu_icm.gpu_equity(S, P), fresh(S))
+    gpu_icm.configure(block_size=16, fft_min_degree=32)
+    try:
+        for S in stacks[:2]:
+            assert np.array_equal(gpu_icm.gpu_equity(S, P), fresh(S))
+    finally:
+        gpu_icm.configure()
+    assert np.array_equal(gpu_icm.gpu_equity(stacks[0], P), fresh(stacks[0]))
