@@ -284,11 +284,14 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
         const int cb = (M >= 4096) ? 1 : 4096 / M;
         const long blocks = (batch + cb - 1) / cb;
         const size_t smem = (size_t)cb * M * sizeof(double2);
+        // one CTA per SM when the transform takes more than half the shared
+        // memory: twice the warps to hide the butterflies' latency
+        const int tpb = smem > kOneCtaSmem ? 512 : threads;
         pr->begin("fft_smem", 5.0 * M * logM * (double)batch, st);
         if (sign < 0)
-            k_fft_smem<-1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
+            k_fft_smem<-1><<<(unsigned)blocks, tpb, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
         else
-            k_fft_smem<+1><<<(unsigned)blocks, threads, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
+            k_fft_smem<+1><<<(unsigned)blocks, tpb, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
         pr->end(st);
         ++*launches;
         return 0;

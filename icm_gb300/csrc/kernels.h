@@ -287,6 +287,7 @@ size_t sub_prop_smem(int B);
 void sub_set_smem_limits();
 
 // ---- small tournaments (small.cu): the whole per-node pipeline in one CTA
+constexpr size_t kOneCtaSmem = 113 * 1024;   // above this only one CTA fits on an SM
 constexpr size_t kSmallMaxSmem = 200 * 1024;
 constexpr int kSmallMaxN = 1536;   // the largest default limit of the small path (plan_small_ok)
 constexpr int kSmallMaxLevels = 24;

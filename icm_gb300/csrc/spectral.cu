@@ -34,6 +34,8 @@
 namespace icmg {
 
 constexpr int kSpecThreads = 256;
+constexpr int kSpecThreadsMax = 512;   // CTAs alone on an SM (one 8192-point item) take twice the warps
+static inline int spec_tpb(size_t smem) { return smem > kOneCtaSmem ? kSpecThreadsMax : kSpecThreads; }
 constexpr int kSpecMaxM = kSpecMaxD;   // largest transform one CTA holds in shared memory
 
 static inline int ilog2s(long v) {
@@ -568,10 +570,10 @@ __device__ void spec_prop_packed(const SpecPropArgs *__restrict__ Dsc, const int
     spec_prop_core(V, idx, nh, A0.logD, A0.tw, A0.logTW, sm, A0.Gout != nullptr);
 }
 
-__global__ void __launch_bounds__(kSpecThreads) k_spec_init(SpecInitArgs A) { spec_init_body(A, blockIdx.x, blockIdx.y); }
-__global__ void __launch_bounds__(kSpecThreads) k_spec_build(SpecBuildArgs A) { spec_build_body(A, blockIdx.x, blockIdx.y); }
-__global__ void __launch_bounds__(kSpecThreads) k_gspec_init(GspecArgs A) { gspec_body(A, blockIdx.x, blockIdx.y); }
-__global__ void __launch_bounds__(kSpecThreads) k_spec_prop(SpecPropArgs A) { spec_prop_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kSpecThreadsMax) k_spec_init(SpecInitArgs A) { spec_init_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kSpecThreadsMax) k_spec_build(SpecBuildArgs A) { spec_build_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kSpecThreadsMax) k_gspec_init(GspecArgs A) { gspec_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kSpecThreadsMax) k_spec_prop(SpecPropArgs A) { spec_prop_body(A, blockIdx.x, blockIdx.y); }
 
 size_t spec_smem_bytes(int M) { return spec_smem(M); }
 void spec_wl_set_smem_limits();
@@ -635,7 +637,7 @@ void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cuda
     A.z.zp = zp;
     A.z.q0 = zq0;
     pr->begin("spec_init", fq * nq, st);
-    k_spec_init<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
+    k_spec_init<<<dim3(A.nbx, nq), spec_tpb(sm), sm, st>>>(A);
     pr->end(st);
 }
 
@@ -647,7 +649,7 @@ void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq
     A.z.zp = zp;
     A.z.q0 = zq0;
     pr->begin("spec_build", fq * nq, st);
-    k_spec_build<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
+    k_spec_build<<<dim3(A.nbx, nq), spec_tpb(sm), sm, st>>>(A);
     pr->end(st);
 }
 
@@ -660,7 +662,7 @@ void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal
     A.z.zp = zp;
     A.z.q0 = zq0;
     pr->begin("gspec_init", fq * nq, st);
-    k_gspec_init<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
+    k_gspec_init<<<dim3(A.nbx, nq), spec_tpb(sm), sm, st>>>(A);
     pr->end(st);
 }
 
@@ -673,30 +675,30 @@ void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Leve
     A.z.zp = zp;
     A.z.q0 = zq0;
     pr->begin("spec_prop", fq * nq, st);
-    k_spec_prop<<<dim3(A.nbx, nq), kSpecThreads, sm, st>>>(A);
+    k_spec_prop<<<dim3(A.nbx, nq), spec_tpb(sm), sm, st>>>(A);
     pr->end(st);
 }
 
 // ---------------------------------------------------------------- work lists
-__global__ void __launch_bounds__(kSpecThreads)
+__global__ void __launch_bounds__(kSpecThreadsMax)
 kw_spec_init(const SpecInitArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
     SpecInitArgs A = D[t.x];
     A.z.q0 = q0;
     spec_init_body(A, t.y, blockIdx.y);
 }
-__global__ void __launch_bounds__(kSpecThreads)
+__global__ void __launch_bounds__(kSpecThreadsMax)
 kw_gspec(const GspecArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
     const int2 t = tab[blockIdx.x];
     GspecArgs A = D[t.x];
     A.z.q0 = q0;
     gspec_body(A, t.y, blockIdx.y);
 }
-__global__ void __launch_bounds__(kSpecThreads)
+__global__ void __launch_bounds__(kSpecThreadsMax)
 kw_spec_build_packed(const SpecBuildArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
     spec_build_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
 }
-__global__ void __launch_bounds__(kSpecThreads)
+__global__ void __launch_bounds__(kSpecThreadsMax)
 kw_spec_prop_packed(const SpecPropArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
     spec_prop_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
 }
@@ -715,9 +717,9 @@ void launch_packed_spec(WOp op, const void *desc, const int2 *slots, int nslots,
     if (nslots <= 0 || nq <= 0) return;
     const dim3 g((nslots + cb - 1) / cb, nq);
     if (op == WOp::SpecBuild)
-        kw_spec_build_packed<<<g, kSpecThreads, smem, st>>>((const SpecBuildArgs *)desc, slots, nslots, q0);
+        kw_spec_build_packed<<<g, spec_tpb(smem), smem, st>>>((const SpecBuildArgs *)desc, slots, nslots, q0);
     else
-        kw_spec_prop_packed<<<g, kSpecThreads, smem, st>>>((const SpecPropArgs *)desc, slots, nslots, q0);
+        kw_spec_prop_packed<<<g, spec_tpb(smem), smem, st>>>((const SpecPropArgs *)desc, slots, nslots, q0);
 }
 
 void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
@@ -725,8 +727,8 @@ void launch_worklist_spec(WOp op, const void *desc, const int2 *tab, int nctas, 
     if (nctas <= 0 || nq <= 0) return;
     const dim3 g(nctas, nq);
     switch (op) {
-        case WOp::SpecInit: kw_spec_init<<<g, kSpecThreads, smem, st>>>((const SpecInitArgs *)desc, tab, q0); break;
-        case WOp::Gspec: kw_gspec<<<g, kSpecThreads, smem, st>>>((const GspecArgs *)desc, tab, q0); break;
+        case WOp::SpecInit: kw_spec_init<<<g, spec_tpb(smem), smem, st>>>((const SpecInitArgs *)desc, tab, q0); break;
+        case WOp::Gspec: kw_gspec<<<g, spec_tpb(smem), smem, st>>>((const GspecArgs *)desc, tab, q0); break;
         default: break;
     }
 }
