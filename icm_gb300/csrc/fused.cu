@@ -26,6 +26,8 @@ namespace icmg {
 
 constexpr int kFusedMaxN = 8192;
 constexpr int kFusedThreads = 256;
+constexpr int kFusedThreadsMax = 512;   // CTAs alone on an SM (8192-point items) take twice the warps
+static inline int fused_tpb(size_t smem) { return smem > kOneCtaSmem ? kFusedThreadsMax : kFusedThreads; }
 
 __device__ __forceinline__ int fused_cb(int N) { return N >= 8192 ? 1 : 4096 / N; }
 
@@ -306,8 +308,8 @@ __device__ void fused_prop_packed(const FusedPropArgs *__restrict__ Dsc, const i
     fused_prop_core(V, idx, nh, cb, A0.logN, A0.tw, A0.logTW, sm);
 }
 
-__global__ void __launch_bounds__(kFusedThreads) k_fused_build(FusedBuildArgs A) { fused_build_body(A, blockIdx.x, blockIdx.y); }
-__global__ void __launch_bounds__(kFusedThreads) k_fused_prop(FusedPropArgs A) { fused_prop_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kFusedThreadsMax) k_fused_build(FusedBuildArgs A) { fused_build_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kFusedThreadsMax) k_fused_prop(FusedPropArgs A) { fused_prop_body(A, blockIdx.x, blockIdx.y); }
 
 size_t fused_smem_bytes(int N) { return fused_smem_v(N); }
 static size_t fused_smem_v_max() {
@@ -318,11 +320,11 @@ static size_t fused_smem_v_max() {
 
 bool fused_ok(int N) { return N >= 8 && N <= kFusedMaxN; }
 
-__global__ void __launch_bounds__(kFusedThreads)
+__global__ void __launch_bounds__(kFusedThreadsMax)
 kw_fused_build_packed(const FusedBuildArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
     fused_build_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
 }
-__global__ void __launch_bounds__(kFusedThreads)
+__global__ void __launch_bounds__(kFusedThreadsMax)
 kw_fused_prop_packed(const FusedPropArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
     fused_prop_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
 }
@@ -332,9 +334,9 @@ void launch_packed_fused(WOp op, const void *desc, const int2 *slots, int nslots
     if (nslots <= 0 || nq <= 0) return;
     const dim3 g((nslots + cb - 1) / cb, nq);
     if (op == WOp::FusedBuild)
-        kw_fused_build_packed<<<g, kFusedThreads, smem, st>>>((const FusedBuildArgs *)desc, slots, nslots, q0);
+        kw_fused_build_packed<<<g, fused_tpb(smem), smem, st>>>((const FusedBuildArgs *)desc, slots, nslots, q0);
     else
-        kw_fused_prop_packed<<<g, kFusedThreads, smem, st>>>((const FusedPropArgs *)desc, slots, nslots, q0);
+        kw_fused_prop_packed<<<g, fused_tpb(smem), smem, st>>>((const FusedPropArgs *)desc, slots, nslots, q0);
 }
 
 void fused_set_smem_limits() {
@@ -380,7 +382,7 @@ void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_onl
     A.z.zp = zp;
     A.z.q0 = zq0;
     pr->begin(spectra_only ? "fused_spectra" : "fused_build", fq * nq, st);
-    k_fused_build<<<dim3(A.nbx, nq), kFusedThreads, sm, st>>>(A);
+    k_fused_build<<<dim3(A.nbx, nq), fused_tpb(sm), sm, st>>>(A);
     pr->end(st);
 }
 
@@ -393,7 +395,7 @@ void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const 
     A.z.zp = zp;
     A.z.q0 = zq0;
     pr->begin("fused_prop", fq * nq, st);
-    k_fused_prop<<<dim3(A.nbx, nq), kFusedThreads, sm, st>>>(A);
+    k_fused_prop<<<dim3(A.nbx, nq), fused_tpb(sm), sm, st>>>(A);
     pr->end(st);
 }
 

@@ -46,6 +46,7 @@ namespace icmg {
 
 namespace {
 constexpr int kVjpThreads = 256;
+constexpr int kVjpThreadsMax = 512;   // CTAs alone on an SM (8192-point items) take twice the warps
 constexpr int kVjpMaxN = 8192;
 
 inline unsigned nblkv(long work, int threads) { return (unsigned)((work + threads - 1) / threads); }
@@ -59,6 +60,7 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 __device__ __forceinline__ int vjp_cb(int N) { return N >= 8192 ? 1 : 4096 / N; }
 static inline int vjp_cb_h(int N) { return N >= 8192 ? 1 : 4096 / N; }
+static inline int vjp_tpb(size_t smem) { return smem > kOneCtaSmem ? kVjpThreadsMax : kVjpThreads; }
 // Every pair of a CTA is described by a view staged in shared memory after
 // the transforms, so a CTA may hold pairs of different tournaments (packed
 // work lists) and pairs under wholly-zero parents are pruned per pair.
@@ -715,10 +717,10 @@ template <int B>
 __global__ void k_adj_leaf_down(AdjLeafDownArgs A, int q0) { adj_leaf_down_t<B>(A, blockIdx.x, blockIdx.y, q0); }
 __global__ void k_adj_up_school(AdjUpSchoolArgs A, int q0) { adj_up_school_body(A, blockIdx.x, blockIdx.y, q0); }
 __global__ void k_adj_down_school(AdjDownSchoolArgs A, int q0) { adj_down_school_body(A, blockIdx.x, blockIdx.y, q0); }
-__global__ void __launch_bounds__(kVjpThreads) k_adj_up_fused(AdjUpFusedArgs A, int q0) {
+__global__ void __launch_bounds__(kVjpThreadsMax) k_adj_up_fused(AdjUpFusedArgs A, int q0) {
     adj_up_fused_body(A, blockIdx.x, blockIdx.y, q0);
 }
-__global__ void __launch_bounds__(kVjpThreads) k_adj_down_fused(AdjDownFusedArgs A, int q0) {
+__global__ void __launch_bounds__(kVjpThreadsMax) k_adj_down_fused(AdjDownFusedArgs A, int q0) {
     adj_down_fused_body(A, blockIdx.x, blockIdx.y, q0);
 }
 template <int B>
@@ -740,11 +742,11 @@ __global__ void kw_adj_down_school(const AdjDownSchoolArgs *__restrict__ D, cons
     adj_down_school_body(D[t.x], t.y, blockIdx.y, q0);
 }
 
-__global__ void __launch_bounds__(kVjpThreads)
+__global__ void __launch_bounds__(kVjpThreadsMax)
 kw_adj_up_packed(const AdjUpFusedArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
     adj_up_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
 }
-__global__ void __launch_bounds__(kVjpThreads)
+__global__ void __launch_bounds__(kVjpThreadsMax)
 kw_adj_down_packed(const AdjDownFusedArgs *__restrict__ D, const int2 *__restrict__ slots, int nslots, int q0) {
     adj_down_packed(D, slots, nslots, blockIdx.x, blockIdx.y, q0);
 }
@@ -1122,9 +1124,9 @@ void launch_packed_adj(WOp op, const void *desc, const int2 *slots, int nslots, 
     if (nslots <= 0 || nq <= 0) return;
     const dim3 g((nslots + cb - 1) / cb, nq);
     if (op == WOp::AdjUpFused)
-        kw_adj_up_packed<<<g, kVjpThreads, smem, st>>>((const AdjUpFusedArgs *)desc, slots, nslots, q0);
+        kw_adj_up_packed<<<g, vjp_tpb(smem), smem, st>>>((const AdjUpFusedArgs *)desc, slots, nslots, q0);
     else
-        kw_adj_down_packed<<<g, kVjpThreads, smem, st>>>((const AdjDownFusedArgs *)desc, slots, nslots, q0);
+        kw_adj_down_packed<<<g, vjp_tpb(smem), smem, st>>>((const AdjDownFusedArgs *)desc, slots, nslots, q0);
 }
 
 int adj_items_per_cta(int logN) { return vjp_cb_h(1 << logN); }
@@ -1188,7 +1190,7 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         AdjUpSchoolArgs Sa;
         adj_up_args(p, b, l, tw, logTW, F, Sa);
         if (F.nbx > 0) {
-            k_adj_up_fused<<<dim3(F.nbx, nq), kVjpThreads, adj_up_smem(F.logN), st>>>(F, q0);
+            k_adj_up_fused<<<dim3(F.nbx, nq), vjp_tpb(adj_up_smem(F.logN)), adj_up_smem(F.logN), st>>>(F, q0);
             ++launches;
         } else if (level_big(p->lv[l])) {
             adj_up_big(p, b, l, nq, tw, logTW, launches);
@@ -1203,7 +1205,7 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         AdjDownSchoolArgs Sa;
         adj_down_args(p, b, l, tw, logTW, F, Sa);
         if (F.nbx > 0) {
-            k_adj_down_fused<<<dim3(F.nbx, nq), kVjpThreads, adj_down_smem(F.logN), st>>>(F, q0);
+            k_adj_down_fused<<<dim3(F.nbx, nq), vjp_tpb(adj_down_smem(F.logN)), adj_down_smem(F.logN), st>>>(F, q0);
             ++launches;
         } else if (level_big(p->lv[l])) {
             adj_down_big(p, b, l, nq, tw, logTW, launches);
