@@ -522,7 +522,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     if (!p->small && !p->linear && root_gspec_forkable(p)) {   // stream and events for the root's spectrum
         e = cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming);
+        if (e == cudaSuccess && !p->ev_join) e = cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             err = std::string("side stream: ") + cudaGetErrorString(e);
             plan_destroy(p);
@@ -542,6 +542,62 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     if (p->linear) p->d_ck = (double *)(A + o_ck);
     else plan_tree_layout(p, qc, A + o_tree);
     p->d_counter = (unsigned *)(A + o_cnt);
+    // after the arena's pointers: the views offset them
+    if (!p->small && !p->linear && !p->coeff_only && p->Lf == 0 && qc >= 2 && !p->opts.verbose) {
+        // node chunks in two halves on two streams: the second half's view of the arena
+        const int h = qc / 2;
+        ChunkView &v = p->half;
+        for (int l = 0; l < p->L; ++l) {
+            Level &x = v.lv[l];
+            x = p->lv[l];
+            if (x.P) x.P += (size_t)h * x.P_q;
+            if (x.g) x.g += (size_t)h * x.g_q;
+            if (x.spec) x.spec += (size_t)h * x.spec_q;
+            if (x.spec2) x.spec2 += (size_t)h * x.spec2_q;
+            if (x.ends) x.ends += (size_t)h * x.ends_q;
+            if (x.G && l != p->L - 1) x.G += (size_t)h * x.G_q;   // the root's spectrum is shared
+        }
+        v.a = p->d_a + (size_t)h * n;
+        v.contrib = p->d_contrib + (size_t)h * n;
+        v.blockP = p->d_blockP + (size_t)h * p->nblocks * (B + 1);
+        if (p->d_fa) {
+            v.fa = p->d_fa + (size_t)h * p->fa_elems;
+            v.fb = p->d_fb + (size_t)h * std::max(p->fa_elems, p->fb_elems);
+            v.fc = p->d_fc + (size_t)h * p->fa_elems;
+        }
+        // every view buffer, for the second half's qc - h nodes, inside the arena
+        const char *lo = p->arena, *hi = p->arena + off;
+        const size_t m = (size_t)(qc - h);
+        auto inside = [&](const void *q, size_t bytes) {
+            return !q || ((const char *)q >= lo && (const char *)q + bytes <= hi);
+        };
+        bool ok = inside(v.a, 8 * m * n) && inside(v.contrib, 8 * m * n) &&
+                  inside(v.blockP, 8 * m * p->nblocks * (B + 1)) && inside(v.fa, 16 * m * p->fa_elems) &&
+                  inside(v.fb, 16 * m * std::max(p->fa_elems, p->fb_elems)) && inside(v.fc, 16 * m * p->fa_elems);
+        for (int l = 0; l < p->L; ++l) {
+            const Level &x = v.lv[l];
+            ok = ok && inside(x.P, 8 * m * x.P_q) && inside(x.g, 8 * m * x.g_q) &&
+                 inside(x.spec, 16 * m * x.spec_q) && inside(x.spec2, 16 * m * x.spec2_q) &&
+                 inside(x.ends, 8 * m * x.ends_q) && inside(x.G, 16 * (l == p->L - 1 ? 1 : m) * x.G_q);
+        }
+        if (!ok) {
+            err = "internal: a half-chunk view leaves the plan's arena";
+            plan_destroy(p);
+            return nullptr;
+        }
+        e = cudaStreamCreateWithFlags(&v.st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_split, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_acc_a, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_acc_b, cudaEventDisableTiming);
+        if (e == cudaSuccess && !p->ev_join) e = cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            err = std::string("second stream: ") + cudaGetErrorString(e);
+            plan_destroy(p);
+            return nullptr;
+        }
+        p->half_off = h;
+        p->split = true;
+    }
     e = cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned), p->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
@@ -581,6 +637,12 @@ void plan_destroy(Plan *p) {
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     for (cudaEvent_t ev : p->stage_ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : {p->ev_split, p->ev_acc_a, p->ev_acc_b})
+        if (ev) cudaEventDestroy(ev);
+    if (p->half.st) {
+        cudaStreamSynchronize(p->half.st);
+        cudaStreamDestroy(p->half.st);
+    }
     if (p->ev_fork) cudaEventDestroy(p->ev_fork);
     if (p->ev_join) cudaEventDestroy(p->ev_join);
     if (p->side) {
@@ -674,10 +736,16 @@ static void stage_mark(Plan *p, cudaStream_t st) {
     cudaEventRecord(p->stage_ev[p->stage_used++], st);
 }
 
-void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide) {
-    cudaStream_t st = p->stream;
+void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide,
+               const ChunkView *view, cudaEvent_t acc_wait, cudaEvent_t acc_done) {
+    // the chunk's buffers: the plan's own, or a view on the second half of them
+    cudaStream_t st = view ? view->st : p->stream;
     const int L = p->L;
-    Level *lv = p->lv;
+    Level *lv = view ? const_cast<Level *>(view->lv) : p->lv;
+    double *d_a = view ? view->a : p->d_a, *d_contrib = view ? view->contrib : p->d_contrib;
+    double *d_blockP = view ? view->blockP : p->d_blockP;
+    double2 *d_fa = view ? view->fa : p->d_fa, *d_fb = view ? view->fb : p->d_fb;
+    double2 *d_fc = view ? view->fc : p->d_fc;
     Prof *pr = &p->prof;
     const int *zp = p->zskip ? p->d_z : nullptr;   // zero-prefix pruning (one-CTA levels)
     auto frac = [&](long span, int nreal) { pr->scale = zp ? hot_frac(p, q0, nq, span, nreal) : 1.0; };
@@ -685,15 +753,15 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     SubArgs SA{};
     SubFlops SF{};
     if (Lf >= 1) {   // leaf blocks and the bottom schoolbook levels in one kernel
-        SA = sub_args(p, Lf, p->d_S, p->d_node, p->d_a, (size_t)p->n, p->subset ? p->d_active : nullptr,
-                      p->d_contrib, !divide, divide, &SF);
+        SA = sub_args(p, Lf, p->d_S, p->d_node, d_a, (size_t)p->n, p->subset ? p->d_active : nullptr,
+                      d_contrib, !divide, divide, &SF);
         double fl = SF.leaf;
         for (int l = 1; l <= Lf; ++l)
             fl += SF.build[l] * (zp ? hot_frac(p, q0, nq, lv[l].deg, lv[l].nreal) : 1.0);
         pr->scale = 1.0;
         launch_sub_build(SA, nq, q0, st, pr, fl);
     } else {
-        launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, lv[0].P, lv[0].pst,
+        launch_leaf(p->B, p->n, p->nblocks, p->d_S, p->d_node, q0, nq, d_a, d_blockP, lv[0].P, lv[0].pst,
                     lv[0].plen, st, pr);
     }
     ++p->launches;
@@ -714,14 +782,14 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
         }
         if (lv[l].kind == 2) {
             if (lv[l - 1].deg > kSpecMaxD) {
-                launch_specbig_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, p->d_fa, p->d_fc, tw, logTW, st,
+                launch_specbig_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, d_fa, d_fc, tw, logTW, st,
                                      &p->launches, pr, zp, q0);
             } else {
                 launch_spec_build(lv[l - 1], lv[l], lv[l + 1].kind != 2, nq, tw, logTW, st, pr, zp, q0);
                 ++p->launches;
             }
         } else if (lv[l].fft) {
-            launch_fft_build(lv[l - 1], lv[l], nq, p->d_fa, p->d_fb, p->d_fc, false, tw, logTW, st, &p->launches, pr,
+            launch_fft_build(lv[l - 1], lv[l], nq, d_fa, d_fb, d_fc, false, tw, logTW, st, &p->launches, pr,
                              zp, q0);
             if (lv[l - 1].nreal & 1) {
                 launch_school_build(lv[l - 1], lv[l], nq, lv[l].npairs, st, pr, zp, q0);
@@ -738,7 +806,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     }
     pr->scale = 1.0;
     if (L >= 2 && lv[L - 1].fft)
-        launch_fft_build(lv[L - 2], lv[L - 1], nq, p->d_fa, p->d_fb, p->d_fc, true, tw, logTW, st, &p->launches, pr);
+        launch_fft_build(lv[L - 2], lv[L - 1], nq, d_fa, d_fb, d_fc, true, tw, logTW, st, &p->launches, pr);
     if (divide) stage_mark(p, st);   // end of the tree build
     for (int l = L - 1; l >= 1 + Lf; --l) {
         const bool root = (l == L - 1);
@@ -760,7 +828,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
                     int logd = 0;
                     while ((1L << logd) < lv[l].deg) ++logd;
                     launch_gspecbig_init(gp, gp_q, gst_p, gpl, lv[l].nreal, logd, lv[l].G, root ? 0 : lv[l].G_q,
-                                         root ? 1 : nq, hot_p, p->d_fa, p->d_fc, tw, logTW, st, &p->launches, pr,
+                                         root ? 1 : nq, hot_p, d_fa, d_fc, tw, logTW, st, &p->launches, pr,
                                          root ? nullptr : zp, q0);
                 } else {
                     // the root's spectrum is shared by the chunk's nodes: never pruned
@@ -770,7 +838,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
                 }
             }
             if (lv[l - 1].deg > kSpecMaxD) {
-                launch_specbig_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], nq, hot_c, p->d_fa, p->d_fc, tw, logTW,
+                launch_specbig_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], nq, hot_c, d_fa, d_fc, tw, logTW,
                                     st, &p->launches, pr, zp, q0);
             } else {
                 launch_spec_prop(lv[l].G, root ? 0 : lv[l].G_q, lv[l - 1], lv[l], l - 1 >= 1 && lv[l - 1].kind == 2,
@@ -778,7 +846,7 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
                 ++p->launches;
             }
         } else if (lv[l].fft) {
-            launch_fft_prop(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nq, hot_c, p->d_fa, p->d_fb, p->d_fc, tw, logTW,
+            launch_fft_prop(gp, gp_q, gst_p, gpl, lv[l - 1], lv[l], nq, hot_c, d_fa, d_fb, d_fc, tw, logTW,
                             st, &p->launches, pr, zp, q0);
             if (lv[l - 1].nreal & 1) {
                 launch_school_prop(gp, gp_q, gst_p, gpl, lv[l - 1], nq, hot_c, 2 * lv[l].npairs, st, pr, zp, q0);
@@ -803,7 +871,9 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
         launch_sub_prop(SA, nq, q0, st, pr, fl + SF.divide * hotp);
         ++p->launches;
         if (!divide) return;
-        launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, first ? 1 : 0, st, pr);
+        if (acc_wait) cudaStreamWaitEvent(st, acc_wait, 0);
+        launch_accumulate(p->n, nq, d_contrib, p->d_acc, first ? 1 : 0, st, pr);
+        if (acc_done) cudaEventRecord(acc_done, st);
         ++p->launches;
         return;
     }
@@ -816,10 +886,12 @@ void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first
     const double *g0 = (L == 1) ? p->d_payout : lv[0].g;
     const size_t g0_q = (L == 1) ? 0 : lv[0].g_q;
     const int gst0 = (L == 1) ? 0 : lv[0].gst;
-    launch_divide(p->B, p->n, p->k, p->nblocks, p->d_S, p->d_node, q0, nq, p->d_a, p->d_blockP, g0, g0_q, gst0,
-                  p->subset ? p->d_active : nullptr, p->d_contrib, st, pr);
+    launch_divide(p->B, p->n, p->k, p->nblocks, p->d_S, p->d_node, q0, nq, d_a, d_blockP, g0, g0_q, gst0,
+                  p->subset ? p->d_active : nullptr, d_contrib, st, pr);
     pr->scale = 1.0;
-    launch_accumulate(p->n, nq, p->d_contrib, p->d_acc, first ? 1 : 0, st, pr);
+    if (acc_wait) cudaStreamWaitEvent(st, acc_wait, 0);
+    launch_accumulate(p->n, nq, d_contrib, p->d_acc, first ? 1 : 0, st, pr);
+    if (acc_done) cudaEventRecord(acc_done, st);
     p->launches += 2;
 }
 
@@ -866,11 +938,40 @@ static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
             ++p->launches;
             p->root_forked = true;
         }
-        for (int q0 = 0; q0 < nact; q0 += p->qc) {
-            const int nq = std::min(p->qc, nact - q0);
-            stage_mark(p, p->stream);   // chunk start
-            run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);
-            stage_mark(p, p->stream);   // end of the leaf extraction (division and node sum)
+        if (p->split && nact >= 2 && !p->prof.on) {   // (per-kernel profiles: one stream)
+            const int L = p->L, l = L - 1;
+            if (!p->root_forked && L >= 2 && p->lv[l].kind == 2) {
+                // a multi-pass root spectrum: once, before the halves (they share it)
+                int logd = 0;
+                while ((1L << logd) < p->lv[l].deg) ++logd;
+                launch_gspecbig_init(p->d_payout, 0, 0, p->k, p->lv[l].nreal, logd, p->lv[l].G, 0, 1,
+                                     p->subset ? p->d_hot + p->hot_off[l] : nullptr, p->d_fa, p->d_fc, tw, logTW,
+                                     p->stream, &p->launches, &p->prof, nullptr, 0);
+                cudaEventRecord(p->ev_join, p->stream);
+                p->root_forked = true;
+            }
+            // every chunk in two halves, one per stream; the node sums stay in node
+            // order: each half's accumulate waits for the one before it
+            cudaEventRecord(p->ev_split, p->stream);
+            cudaStreamWaitEvent(p->half.st, p->ev_split, 0);
+            for (int q0 = 0; q0 < nact; q0 += p->qc) {
+                const int nq = std::min(p->qc, nact - q0);
+                const int na = std::min(p->half_off, (nq + 1) / 2), nb = nq - na;
+                run_chunk(p, q0, na, tw, logTW, q0 == 0, true, nullptr, q0 == 0 ? nullptr : p->ev_acc_b,
+                          p->ev_acc_a);
+                if (nb > 0)
+                    run_chunk(p, q0 + na, nb, tw, logTW, false, true, &p->half, p->ev_acc_a, p->ev_acc_b);
+                else
+                    cudaEventRecord(p->ev_acc_b, p->stream);
+            }
+            cudaStreamWaitEvent(p->stream, p->ev_acc_b, 0);
+        } else {
+            for (int q0 = 0; q0 < nact; q0 += p->qc) {
+                const int nq = std::min(p->qc, nact - q0);
+                stage_mark(p, p->stream);   // chunk start
+                run_chunk(p, q0, nq, tw, logTW, q0 == 0, true);
+                stage_mark(p, p->stream);   // end of the leaf extraction (division and node sum)
+            }
         }
         launch_scatter(p->n, p->d_acc, p->d_perm, p->subset ? p->d_active : nullptr, p->d_out, p->stream);
         ++p->launches;

@@ -50,6 +50,16 @@ struct Level {
     double *ends = nullptr;
 };
 
+// The per-node buffers of one half of a node chunk: the plan's own pointers
+// offset by the first half's node count (same arena), so the two halves of a
+// chunk run concurrently on two streams.
+struct ChunkView {
+    Level lv[kMaxLevels];
+    double *a = nullptr, *contrib = nullptr, *blockP = nullptr;
+    double2 *fa = nullptr, *fb = nullptr, *fc = nullptr;
+    cudaStream_t st = nullptr;
+};
+
 struct Plan {
     int n = 0, k = 0, B = 0, nblocks = 0, L = 0;
     int fft_min_deg = 64;
@@ -76,6 +86,12 @@ struct Plan {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool root_forked = false;
+    // node chunks split in two halves on two streams (tree path): the second
+    // half's buffers, its first slot, events ordering the node sums
+    bool split = false;
+    int half_off = 0;
+    ChunkView half;
+    cudaEvent_t ev_split = nullptr, ev_acc_a = nullptr, ev_acc_b = nullptr;
     char *arena = nullptr;
     size_t arena_bytes = 0;
     bool pooled = false;            // arena from the stream-ordered pool
@@ -148,7 +164,8 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
                   bool coeff_only = false, double q_bytes_scale = 1.0, size_t budget = 0);
 // launch sequence of one chunk of nq nodes (engine.cu); divide = false stops
 // after the propagate pass (the tree of the chunk stays in the plan's buffers)
-void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide);
+void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide,
+               const ChunkView *view = nullptr, cudaEvent_t acc_wait = nullptr, cudaEvent_t acc_done = nullptr);
 static inline int plan_ilog2(long v) {
     int l = 0;
     while ((1L << l) < v) ++l;
