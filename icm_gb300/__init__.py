@@ -464,7 +464,7 @@ def equity_adaptive(stacks, payouts, tol=1e-9, Q0=256, Qmax=4096):
 
 
 def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False,
-              zero_prefix=True, subtree=False, small_max_n=0, engine="auto", quadrature="erfc"):
+              zero_prefix=True, subtree=False, small_max_n=0, engine="auto", quadrature="erfc", chunk_streams=0):
     """Process-wide engine settings for plans created afterwards (0 = default).
 
     coefficient_fft_only=True keeps every FFT tree level on coefficients
@@ -476,7 +476,10 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
     small_max_n sets the largest n of the one-CTA-per-node small path
     (0 = default k-dependent limit, -1 = never); engine is "auto", "tree"
     or "linear" (the O(n k) linear engine, one warp per node, k <= 256);
-    quadrature is "erfc" (the reference's erfc-trapezoid rule) or "tanh_sinh"."""
+    quadrature is "erfc" (the reference's erfc-trapezoid rule) or "tanh_sinh";
+    chunk_streams spreads a tree plan's node chunks over that many streams
+    (0 = default: 4 from n = 12000, else 2; 1 = one stream; at most 4; same
+    results)."""
     engines = {"auto": 0, "tree": 1, "linear": 2}
     rules = {"erfc": 0, "tanh_sinh": 1}
     if engine not in engines:
@@ -485,7 +488,7 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
         raise ValueError(f"quadrature must be one of {sorted(rules)}, got {quadrature!r}")
     cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes,
                          0 if zero_prefix else 1, 1 if subtree else 0, int(small_max_n), engines[engine],
-                         rules[quadrature])
+                         rules[quadrature], int(chunk_streams))
     lib().icm_gb300_set_config(ctypes.byref(cfg))
 
 

@@ -464,6 +464,45 @@ size_t plan_tree_layout(Plan *p, int qc, char *base) {
 
 static bool root_gspec_forkable(const Plan *p);
 
+// The buffers of node slots [off, off + slots) of a plan's chunk: every
+// per-node pointer shifted by off nodes (the root's shared spectrum stays);
+// false if any of them would leave the arena's first arena_bytes.
+static bool make_chunk_view(const Plan *p, int off, int slots, size_t arena_bytes, ChunkView &v) {
+    const size_t h = (size_t)off, m = (size_t)slots, n = (size_t)p->n;
+    const size_t bp = (size_t)p->nblocks * (p->B + 1), fb = std::max(p->fa_elems, p->fb_elems);
+    for (int l = 0; l < p->L; ++l) {
+        Level &x = v.lv[l];
+        x = p->lv[l];
+        if (x.P) x.P += h * x.P_q;
+        if (x.g) x.g += h * x.g_q;
+        if (x.spec) x.spec += h * x.spec_q;
+        if (x.spec2) x.spec2 += h * x.spec2_q;
+        if (x.ends) x.ends += h * x.ends_q;
+        if (x.G && l != p->L - 1) x.G += h * x.G_q;
+    }
+    v.a = p->d_a + h * n;
+    v.contrib = p->d_contrib + h * n;
+    v.blockP = p->d_blockP + h * bp;
+    if (p->d_fa) {
+        v.fa = p->d_fa + h * p->fa_elems;
+        v.fb = p->d_fb + h * fb;
+        v.fc = p->d_fc + h * p->fa_elems;
+    }
+    const char *lo = p->arena, *hi = p->arena + arena_bytes;
+    auto inside = [&](const void *q, size_t bytes) {
+        return !q || ((const char *)q >= lo && (const char *)q + bytes <= hi);
+    };
+    bool ok = inside(v.a, 8 * m * n) && inside(v.contrib, 8 * m * n) && inside(v.blockP, 8 * m * bp) &&
+              inside(v.fa, 16 * m * p->fa_elems) && inside(v.fb, 16 * m * fb) && inside(v.fc, 16 * m * p->fa_elems);
+    for (int l = 0; l < p->L; ++l) {
+        const Level &x = v.lv[l];
+        ok = ok && inside(x.P, 8 * m * x.P_q) && inside(x.g, 8 * m * x.g_q) && inside(x.spec, 16 * m * x.spec_q) &&
+             inside(x.spec2, 16 * m * x.spec2_q) && inside(x.ends, 8 * m * x.ends_q) &&
+             inside(x.G, 16 * (l == p->L - 1 ? 1 : m) * x.G_q);
+    }
+    return ok;
+}
+
 Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err, bool coeff_only,
                   double q_bytes_scale, size_t budget_bytes) {
     Plan *p = new Plan();
@@ -543,60 +582,33 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     else plan_tree_layout(p, qc, A + o_tree);
     p->d_counter = (unsigned *)(A + o_cnt);
     // after the arena's pointers: the views offset them
-    if (!p->small && !p->linear && !p->coeff_only && p->Lf == 0 && qc >= 2 && !p->opts.verbose) {
-        // node chunks in two halves on two streams: the second half's view of the arena
-        const int h = qc / 2;
-        ChunkView &v = p->half;
-        for (int l = 0; l < p->L; ++l) {
-            Level &x = v.lv[l];
-            x = p->lv[l];
-            if (x.P) x.P += (size_t)h * x.P_q;
-            if (x.g) x.g += (size_t)h * x.g_q;
-            if (x.spec) x.spec += (size_t)h * x.spec_q;
-            if (x.spec2) x.spec2 += (size_t)h * x.spec2_q;
-            if (x.ends) x.ends += (size_t)h * x.ends_q;
-            if (x.G && l != p->L - 1) x.G += (size_t)h * x.G_q;   // the root's spectrum is shared
+    // default: four pieces from n = 12000 (measured on GB300: n = 16384 4.31 ->
+    // 4.16 ms, n = 65536 17.13 -> 16.89 ms against two), two below (n = 4096,
+    // k = 40: 0.58 ms with two, 0.66 with four)
+    const int want = g_config.chunk_streams > 0 ? g_config.chunk_streams : n >= 12000 ? 4 : 2;
+    const int np = std::min({want, kMaxChunkParts, qc});
+    if (!p->small && !p->linear && !p->coeff_only && p->Lf == 0 && np >= 2 && !p->opts.verbose) {
+        for (int i = 0; i < np; ++i) p->part_off[i] = i * (qc / np);
+        for (int i = 1; i < np; ++i) {
+            const int slots = (i + 1 < np ? p->part_off[i + 1] : qc) - p->part_off[i];
+            if (!make_chunk_view(p, p->part_off[i], slots, off, p->part[i])) {
+                err = "internal: a chunk view leaves the plan's arena";
+                plan_destroy(p);
+                return nullptr;
+            }
+            e = cudaStreamCreateWithFlags(&p->part[i].st, cudaStreamNonBlocking);
+            if (e != cudaSuccess) break;
         }
-        v.a = p->d_a + (size_t)h * n;
-        v.contrib = p->d_contrib + (size_t)h * n;
-        v.blockP = p->d_blockP + (size_t)h * p->nblocks * (B + 1);
-        if (p->d_fa) {
-            v.fa = p->d_fa + (size_t)h * p->fa_elems;
-            v.fb = p->d_fb + (size_t)h * std::max(p->fa_elems, p->fb_elems);
-            v.fc = p->d_fc + (size_t)h * p->fa_elems;
-        }
-        // every view buffer, for the second half's qc - h nodes, inside the arena
-        const char *lo = p->arena, *hi = p->arena + off;
-        const size_t m = (size_t)(qc - h);
-        auto inside = [&](const void *q, size_t bytes) {
-            return !q || ((const char *)q >= lo && (const char *)q + bytes <= hi);
-        };
-        bool ok = inside(v.a, 8 * m * n) && inside(v.contrib, 8 * m * n) &&
-                  inside(v.blockP, 8 * m * p->nblocks * (B + 1)) && inside(v.fa, 16 * m * p->fa_elems) &&
-                  inside(v.fb, 16 * m * std::max(p->fa_elems, p->fb_elems)) && inside(v.fc, 16 * m * p->fa_elems);
-        for (int l = 0; l < p->L; ++l) {
-            const Level &x = v.lv[l];
-            ok = ok && inside(x.P, 8 * m * x.P_q) && inside(x.g, 8 * m * x.g_q) &&
-                 inside(x.spec, 16 * m * x.spec_q) && inside(x.spec2, 16 * m * x.spec2_q) &&
-                 inside(x.ends, 8 * m * x.ends_q) && inside(x.G, 16 * (l == p->L - 1 ? 1 : m) * x.G_q);
-        }
-        if (!ok) {
-            err = "internal: a half-chunk view leaves the plan's arena";
-            plan_destroy(p);
-            return nullptr;
-        }
-        e = cudaStreamCreateWithFlags(&v.st, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_split, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_acc_a, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_acc_b, cudaEventDisableTiming);
+        for (int i = 0; i < np && e == cudaSuccess; ++i)
+            e = cudaEventCreateWithFlags(&p->ev_acc[i], cudaEventDisableTiming);
         if (e == cudaSuccess && !p->ev_join) e = cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming);
         if (e != cudaSuccess) {
-            err = std::string("second stream: ") + cudaGetErrorString(e);
+            err = std::string("chunk streams: ") + cudaGetErrorString(e);
             plan_destroy(p);
             return nullptr;
         }
-        p->half_off = h;
-        p->split = true;
+        p->nparts = np;
     }
     e = cudaMemsetAsync(p->d_counter, 0, sizeof(unsigned), p->stream);
     if (e == cudaSuccess)
@@ -637,11 +649,13 @@ void plan_destroy(Plan *p) {
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     for (cudaEvent_t ev : p->stage_ev) cudaEventDestroy(ev);
-    for (cudaEvent_t ev : {p->ev_split, p->ev_acc_a, p->ev_acc_b})
-        if (ev) cudaEventDestroy(ev);
-    if (p->half.st) {
-        cudaStreamSynchronize(p->half.st);
-        cudaStreamDestroy(p->half.st);
+    if (p->ev_split) cudaEventDestroy(p->ev_split);
+    for (int i = 0; i < kMaxChunkParts; ++i) {
+        if (p->ev_acc[i]) cudaEventDestroy(p->ev_acc[i]);
+        if (p->part[i].st) {
+            cudaStreamSynchronize(p->part[i].st);
+            cudaStreamDestroy(p->part[i].st);
+        }
     }
     if (p->ev_fork) cudaEventDestroy(p->ev_fork);
     if (p->ev_join) cudaEventDestroy(p->ev_join);
@@ -938,10 +952,10 @@ static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
             ++p->launches;
             p->root_forked = true;
         }
-        if (p->split && nact >= 2 && !p->prof.on) {   // (per-kernel profiles: one stream)
-            const int L = p->L, l = L - 1;
+        if (p->nparts >= 2 && nact >= 2 && !p->prof.on) {   // (per-kernel profiles: one stream)
+            const int L = p->L, l = L - 1, np = std::min(p->nparts, nact);
             if (!p->root_forked && L >= 2 && p->lv[l].kind == 2) {
-                // a multi-pass root spectrum: once, before the halves (they share it)
+                // a multi-pass root spectrum: once, before the pieces (they share it)
                 int logd = 0;
                 while ((1L << logd) < p->lv[l].deg) ++logd;
                 launch_gspecbig_init(p->d_payout, 0, 0, p->k, p->lv[l].nreal, logd, p->lv[l].G, 0, 1,
@@ -950,21 +964,24 @@ static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
                 cudaEventRecord(p->ev_join, p->stream);
                 p->root_forked = true;
             }
-            // every chunk in two halves, one per stream; the node sums stay in node
-            // order: each half's accumulate waits for the one before it
+            // every chunk in up to np pieces, one per stream (streams that get no
+            // piece are not forked); the node sums stay in node order: each
+            // piece's accumulate waits for the one before it
             cudaEventRecord(p->ev_split, p->stream);
-            cudaStreamWaitEvent(p->half.st, p->ev_split, 0);
+            for (int i = 1; i < np; ++i) cudaStreamWaitEvent(p->part[i].st, p->ev_split, 0);
+            cudaEvent_t prev = nullptr;
             for (int q0 = 0; q0 < nact; q0 += p->qc) {
-                const int nq = std::min(p->qc, nact - q0);
-                const int na = std::min(p->half_off, (nq + 1) / 2), nb = nq - na;
-                run_chunk(p, q0, na, tw, logTW, q0 == 0, true, nullptr, q0 == 0 ? nullptr : p->ev_acc_b,
-                          p->ev_acc_a);
-                if (nb > 0)
-                    run_chunk(p, q0 + na, nb, tw, logTW, false, true, &p->half, p->ev_acc_a, p->ev_acc_b);
-                else
-                    cudaEventRecord(p->ev_acc_b, p->stream);
+                int q = q0, r = std::min(p->qc, nact - q0);
+                for (int i = 0; i < np && r > 0; ++i) {
+                    const int cap = (i + 1 < p->nparts ? p->part_off[i + 1] : p->qc) - p->part_off[i];
+                    const int m = (i + 1 == np) ? r : std::min(cap, (r + np - i - 1) / (np - i));
+                    run_chunk(p, q, m, tw, logTW, q == 0, true, i ? &p->part[i] : nullptr, prev, p->ev_acc[i]);
+                    prev = p->ev_acc[i];
+                    q += m;
+                    r -= m;
+                }
             }
-            cudaStreamWaitEvent(p->stream, p->ev_acc_b, 0);
+            cudaStreamWaitEvent(p->stream, prev, 0);
         } else {
             for (int q0 = 0; q0 < nact; q0 += p->qc) {
                 const int nq = std::min(p->qc, nact - q0);

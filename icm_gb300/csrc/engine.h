@@ -50,9 +50,10 @@ struct Level {
     double *ends = nullptr;
 };
 
-// The per-node buffers of one half of a node chunk: the plan's own pointers
-// offset by the first half's node count (same arena), so the two halves of a
-// chunk run concurrently on two streams.
+// The per-node buffers of one piece of a node chunk: the plan's own pointers
+// offset by the piece's first node slot (same arena), so the pieces of a
+// chunk run concurrently, one stream each.
+constexpr int kMaxChunkParts = 4;
 struct ChunkView {
     Level lv[kMaxLevels];
     double *a = nullptr, *contrib = nullptr, *blockP = nullptr;
@@ -86,12 +87,13 @@ struct Plan {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool root_forked = false;
-    // node chunks split in two halves on two streams (tree path): the second
-    // half's buffers, its first slot, events ordering the node sums
-    bool split = false;
-    int half_off = 0;
-    ChunkView half;
-    cudaEvent_t ev_split = nullptr, ev_acc_a = nullptr, ev_acc_b = nullptr;
+    // node chunks split in nparts pieces, one stream each (tree path): each
+    // piece's first node slot and buffers (part[0] unused: the plan's own),
+    // events ordering the node sums
+    int nparts = 1;
+    int part_off[kMaxChunkParts] = {};
+    ChunkView part[kMaxChunkParts];
+    cudaEvent_t ev_split = nullptr, ev_acc[kMaxChunkParts] = {};
     char *arena = nullptr;
     size_t arena_bytes = 0;
     bool pooled = false;            // arena from the stream-ordered pool

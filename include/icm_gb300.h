@@ -45,7 +45,11 @@ int icm_last_status(void);
  *                     O(n k); k <= 256, larger k uses the tree)
  *   quadrature        0 = the reference's erfc-trapezoid rule; 1 = tanh-sinh
  *                     on v in (0, 1) (nodes independent of the stacks; less
- *                     accurate for widely spread stacks)                  */
+ *                     accurate for widely spread stacks)
+ *   chunk_streams     streams a tree plan's node chunks are spread over
+ *                     (pieces of consecutive nodes, same results); 0 = the
+ *                     default (4 from n = 12000, else 2), 1 = one stream,
+ *                     at most 4                                           */
 typedef struct {
     int block_size;
     int fft_min_degree;
@@ -57,6 +61,7 @@ typedef struct {
     int small_max_n;
     int engine;
     int quadrature;
+    int chunk_streams;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created

@@ -1,0 +1,76 @@
+"""Node chunks spread over several streams (IcmGb300Config.chunk_streams):
+each chunk's nodes run as pieces of consecutive nodes on up to four streams,
+each piece on its own node slots of the plan's arena, with the node sums
+chained in node order.  So the equities equal the one-stream run's bit for
+bit, whatever the piece count, the chunk size (several chunks, pieces of one
+node, fewer nodes than streams), the level kinds (schoolbook, coefficient
+FFT, spectral, multi-pass spectral), subsets, captured graphs and reuse."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def default_config(gpu_icm):
+    gpu_icm.configure()
+    yield
+    gpu_icm.configure()
+
+
+def _field(n, k, seed):
+    rng = np.random.default_rng(seed)
+    S = 10.0 ** (4 * rng.random(n))
+    P = 0.9 ** np.arange(k)
+    return S, P / P.sum()
+
+
+def _run(gpu_icm, S, P, streams, q_chunk=0, Q=256, targets=None):
+    gpu_icm.configure(chunk_streams=streams, q_chunk=q_chunk, small_max_n=-1)
+    if targets is not None:
+        return gpu_icm.gpu_equity_subset(S, P, targets, Q=Q)
+    return gpu_icm.gpu_equity(S, P, Q=Q)
+
+
+@pytest.mark.parametrize("n,k", [(300, 20), (5000, 120), (20000, 20000), (70000, 200)])
+@pytest.mark.parametrize("streams", [2, 3, 4])
+def test_streams_bitwise(gpu_icm, n, k, streams):
+    S, P = _field(n, k, n + k)
+    ref = _run(gpu_icm, S, P, 1)
+    assert np.array_equal(_run(gpu_icm, S, P, streams), ref)
+
+
+@pytest.mark.parametrize("q_chunk,Q", [(37, 256), (5, 64), (3, 16), (2, 3), (7, 2)])
+def test_streams_chunking(gpu_icm, q_chunk, Q):
+    """Chunks of q_chunk nodes: pieces of one node, more streams than the
+    chunk's or the run's nodes, a last chunk shorter than the others."""
+    S, P = _field(3000, 300, 11)
+    ref = _run(gpu_icm, S, P, 1, q_chunk, Q)
+    for streams in (2, 4):
+        assert np.array_equal(_run(gpu_icm, S, P, streams, q_chunk, Q), ref), (streams, q_chunk, Q)
+
+
+def test_streams_multipass_root(gpu_icm):
+    """k = n = 40000: a spectral root too large for the one-kernel transform;
+    its payout spectrum takes the multi-pass one (once, before the pieces)."""
+    S, P = _field(40000, 40000, 3)
+    ref = _run(gpu_icm, S, P, 1, 0, 64)
+    assert np.array_equal(_run(gpu_icm, S, P, 4, 0, 64), ref)
+    assert np.array_equal(_run(gpu_icm, S, P, 3, 10, 64), ref)
+
+
+def test_streams_subset_and_graphs(gpu_icm):
+    from icm_gb300._lib import IcmGpuOptions
+    S, P = _field(9000, 900, 5)
+    T = np.array([0, 17, 4500, 8999])
+    ref = _run(gpu_icm, S, P, 1, targets=T)
+    assert np.array_equal(_run(gpu_icm, S, P, 3, targets=T), ref)
+    gpu_icm.configure(chunk_streams=1, small_max_n=-1)
+    one = gpu_icm.GpuPlan(S, len(P))
+    gpu_icm.configure(chunk_streams=4, q_chunk=50, small_max_n=-1)
+    graphed = gpu_icm.GpuPlan(S, len(P), IcmGpuOptions(enable_graphs=1))
+    P2 = np.linspace(1.0, 0.1, len(P))
+    for Pr, Q in [(P, 256), (P2, 256), (P, 100), (P2, 256)]:
+        assert np.array_equal(graphed.equity(Pr, Q=Q), one.equity(Pr, Q=Q)), Q
+    one.close()
+    graphed.close()
