@@ -464,6 +464,33 @@ size_t plan_tree_layout(Plan *p, int qc, char *base) {
 
 static bool root_gspec_forkable(const Plan *p);
 
+int chunk_piece_nodes(const Plan *p, int i, int np, int r) {
+    const int cap = (i + 1 < p->nparts ? p->part_off[i + 1] : p->qc) - p->part_off[i];
+    return (i + 1 == np) ? r : std::min(cap, (r + np - i - 1) / (np - i));
+}
+
+static void swap_view(Plan *p, ChunkView &v) {
+    for (int l = 0; l < p->L; ++l) std::swap(p->lv[l], v.lv[l]);
+    std::swap(p->d_a, v.a);
+    std::swap(p->d_contrib, v.contrib);
+    std::swap(p->d_blockP, v.blockP);
+    std::swap(p->d_fa, v.fa);
+    std::swap(p->d_fb, v.fb);
+    std::swap(p->d_fc, v.fc);
+    std::swap(p->stream, v.st);
+}
+
+PieceScope::PieceScope(Plan *plan, const ChunkView *view) : p(plan), on(view != nullptr) {
+    if (on) {
+        saved = *view;
+        swap_view(p, saved);
+    }
+}
+
+PieceScope::~PieceScope() {
+    if (on) swap_view(p, saved);
+}
+
 // The buffers of node slots [off, off + slots) of a plan's chunk: every
 // per-node pointer shifted by off nodes (the root's shared spectrum stays);
 // false if any of them would leave the arena's first arena_bytes.
@@ -587,7 +614,7 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     // k = 40: 0.58 ms with two, 0.66 with four)
     const int want = g_config.chunk_streams > 0 ? g_config.chunk_streams : n >= 12000 ? 4 : 2;
     const int np = std::min({want, kMaxChunkParts, qc});
-    if (!p->small && !p->linear && !p->coeff_only && p->Lf == 0 && np >= 2 && !p->opts.verbose) {
+    if (!p->small && !p->linear && p->Lf == 0 && np >= 2 && !p->opts.verbose) {
         for (int i = 0; i < np; ++i) p->part_off[i] = i * (qc / np);
         for (int i = 1; i < np; ++i) {
             const int slots = (i + 1 < np ? p->part_off[i + 1] : qc) - p->part_off[i];
@@ -973,8 +1000,7 @@ static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
             for (int q0 = 0; q0 < nact; q0 += p->qc) {
                 int q = q0, r = std::min(p->qc, nact - q0);
                 for (int i = 0; i < np && r > 0; ++i) {
-                    const int cap = (i + 1 < p->nparts ? p->part_off[i + 1] : p->qc) - p->part_off[i];
-                    const int m = (i + 1 == np) ? r : std::min(cap, (r + np - i - 1) / (np - i));
+                    const int m = chunk_piece_nodes(p, i, np, r);
                     run_chunk(p, q, m, tw, logTW, q == 0, true, i ? &p->part[i] : nullptr, prev, p->ev_acc[i]);
                     prev = p->ev_acc[i];
                     q += m;

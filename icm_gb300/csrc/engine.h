@@ -61,6 +61,22 @@ struct ChunkView {
     cudaStream_t st = nullptr;
 };
 
+struct Plan;
+
+// Points a plan's per-node buffers and its stream at a chunk piece's view
+// while the scope lives (host-side enqueue only; a null view leaves the plan
+// as it is), so that code written for the plan's own buffers enqueues that
+// piece.
+struct PieceScope {
+    Plan *p;
+    bool on;
+    ChunkView saved;
+    PieceScope(Plan *plan, const ChunkView *view);
+    ~PieceScope();
+    PieceScope(const PieceScope &) = delete;
+    PieceScope &operator=(const PieceScope &) = delete;
+};
+
 struct Plan {
     int n = 0, k = 0, B = 0, nblocks = 0, L = 0;
     int fft_min_deg = 64;
@@ -168,6 +184,9 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
 // after the propagate pass (the tree of the chunk stays in the plan's buffers)
 void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide,
                const ChunkView *view = nullptr, cudaEvent_t acc_wait = nullptr, cudaEvent_t acc_done = nullptr);
+// nodes of piece i (of np) of a chunk with r nodes left for pieces i .. np-1:
+// an even share within the piece's node slots, the last piece the rest
+int chunk_piece_nodes(const Plan *p, int i, int np, int r);
 static inline int plan_ilog2(long v) {
     int l = 0;
     while ((1L << l) < v) ++l;

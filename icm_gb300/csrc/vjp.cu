@@ -932,6 +932,38 @@ VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t
     // the root's gbar summed over nodes: the level-0 buffer when the tree is one block
     b.root_acc = (L == 1) ? b.gb[0] : v->d_root;
     b.root_acc_q = (L == 1) ? p->lv[0].g_q : (size_t)v->kst;
+    v->pbufs[0] = b;
+    for (int i = 1; i < p->nparts; ++i) {   // the pieces' views, checked against the arena
+        const size_t h = (size_t)p->part_off[i];
+        const size_t m = (size_t)((i + 1 < p->nparts ? p->part_off[i + 1] : qc) - p->part_off[i]);
+        VjpBufs &c = v->pbufs[i];
+        c = b;
+        for (int l = 0; l < L; ++l) {
+            if (c.gb[l]) c.gb[l] += h * b.gb_q[l];
+            if (c.Pb[l]) c.Pb[l] += h * p->lv[l].P_q;
+            if (c.gspec[l]) c.gspec[l] += h * p->lv[l].spec_q;
+        }
+        if (c.blockW) c.blockW += h * p->nblocks * p->B;
+        c.root += h * b.root_q;
+        c.a += h * b.aq;
+        c.contrib += h * (size_t)n;
+        c.root_acc += h * b.root_acc_q;
+        const char *lo = v->arena, *hi = v->arena + off;
+        auto inside = [&](const void *q, size_t bytes) {
+            return !q || ((const char *)q >= lo && (const char *)q + bytes <= hi);
+        };
+        bool ok = inside(c.root, 8 * m * b.root_q) &&
+                  inside(c.blockW, 8 * m * p->nblocks * p->B) && c.a == p->part[i].a &&
+                  c.contrib == p->part[i].contrib && (L == 1 || c.root_acc == c.root);
+        for (int l = 0; l < L; ++l)
+            ok = ok && inside(c.gb[l], 8 * m * b.gb_q[l]) && inside(c.Pb[l], 8 * m * p->lv[l].P_q) &&
+                 inside(c.gspec[l], 16 * m * p->lv[l].spec_q);
+        if (!ok) {
+            err = "internal: a VJP chunk view leaves the VJP arena";
+            vjp_plan_destroy(v);
+            return nullptr;
+        }
+    }
     return v;
 }
 
@@ -1177,12 +1209,16 @@ static void adj_down_big(Plan *p, const VjpBufs &b, int l, int nq, const double2
 }
 
 // adjoint passes of one chunk (the forward tree of the chunk is in place)
-static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int logTW, bool first, bool node_terms) {
+// (piece i: the chunk piece's node slots, on its stream; the ordered sums wait
+// for acc_wait and record acc_done when given)
+static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int logTW, bool first, bool node_terms,
+                          int piece = 0, cudaEvent_t acc_wait = nullptr, cudaEvent_t acc_done = nullptr) {
     Plan *p = v->p;
+    PieceScope scope(p, piece ? &p->part[piece] : nullptr);
     cudaStream_t st = p->stream;
     const int L = p->L, n = p->n, k = p->k;
     long &launches = p->launches;
-    VjpBufs b = v->bufs;
+    const VjpBufs b = v->pbufs[piece];
     launch_leaf_up(adj_leaf_up_args(p, b), nq, q0, st);   // for L = 1 the single block is the root
     ++launches;
     for (int l = 1; l <= L - 1; ++l) {   // upward: the root's gbar is this chunk's dL/dpayout
@@ -1216,15 +1252,18 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         }
     }
     // per player: the node's share of dL/dS, then ordered sums over nodes
-    double *pA = node_terms ? v->d_partA : nullptr, *pB = node_terms ? v->d_partB : nullptr;
+    const size_t poff = (size_t)p->part_off[piece] * n;
+    double *pA = node_terms ? v->d_partA + poff : nullptr, *pB = node_terms ? v->d_partB + poff : nullptr;
     launch_leaf_down(adj_leaf_down_args(p, b, pA, pB), nq, q0, st);
-    launch_accum_strided(n, nq, p->d_contrib, (size_t)n, v->d_gradS, first, st);
+    if (acc_wait) cudaStreamWaitEvent(st, acc_wait, 0);
+    launch_accum_strided(n, nq, b.contrib, (size_t)n, v->d_gradS, first, st);
     launch_accum_strided(k, nq, b.root_acc, b.root_acc_q, v->d_gradP, first, st);
     launches += 3;
     if (node_terms) {
         k_node_reduce<<<nq, 256, 0, st>>>(n, pA, pB, v->d_nodeA + q0, v->d_nodeB + q0);
         ++launches;
     }
+    if (acc_done) cudaEventRecord(acc_done, st);   // after the piece's last launch
 }
 
 int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot, int flags, std::string &err) {
@@ -1293,10 +1332,32 @@ int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot,
     }
     if (!p->ev0) { cudaEventCreate(&p->ev0); cudaEventCreate(&p->ev1); }
     cudaEventRecord(p->ev0, p->stream);
-    for (int q0 = 0; q0 < nact; q0 += p->qc) {
-        const int nq = std::min(p->qc, nact - q0);
-        run_chunk(p, q0, nq, tw, logTW, q0 == 0, /*divide=*/false);
-        adjoint_chunk(v, q0, nq, tw, logTW, q0 == 0, node_terms);
+    const int np = (p->nparts >= 2 && nact >= 2 && !p->prof.on) ? std::min(p->nparts, nact) : 1;
+    if (np == 1) {
+        for (int q0 = 0; q0 < nact; q0 += p->qc) {
+            const int nq = std::min(p->qc, nact - q0);
+            run_chunk(p, q0, nq, tw, logTW, q0 == 0, /*divide=*/false);
+            adjoint_chunk(v, q0, nq, tw, logTW, q0 == 0, node_terms);
+        }
+    } else {
+        // every chunk in up to np pieces of consecutive nodes, one stream each
+        // (forward tree and adjoint passes); the sums over nodes stay in node
+        // order: each piece's sums wait for the piece before
+        cudaEventRecord(p->ev_split, p->stream);
+        for (int i = 1; i < np; ++i) cudaStreamWaitEvent(p->part[i].st, p->ev_split, 0);
+        cudaEvent_t prev = nullptr;
+        for (int q0 = 0; q0 < nact; q0 += p->qc) {
+            int q = q0, r = std::min(p->qc, nact - q0);
+            for (int i = 0; i < np && r > 0; ++i) {
+                const int m = chunk_piece_nodes(p, i, np, r);
+                run_chunk(p, q, m, tw, logTW, q == 0, /*divide=*/false, i ? &p->part[i] : nullptr);
+                adjoint_chunk(v, q, m, tw, logTW, q == 0, node_terms, i, prev, p->ev_acc[i]);
+                prev = p->ev_acc[i];
+                q += m;
+                r -= m;
+            }
+        }
+        cudaStreamWaitEvent(p->stream, prev, 0);
     }
     launch_scatter(n, v->d_gradS, p->d_perm, nullptr, p->d_out, p->stream);
     ++p->launches;

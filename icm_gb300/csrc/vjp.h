@@ -138,6 +138,9 @@ struct VjpPlan {
     double *d_gradP = nullptr;           // dL/dpayout
     double *d_root = nullptr;            // [qc][kst] gbar of the root
     VjpBufs bufs{};
+    // per chunk piece (the plan's node slots from part_off[i]): the same
+    // buffers offset by the piece's first slot; pbufs[0] = bufs
+    VjpBufs pbufs[kMaxChunkParts]{};
     std::vector<double> h_cot;
     // node terms (flag 1): per-player partials [qc][n] and per-node sums
     double *d_partA = nullptr, *d_partB = nullptr, *d_nodeA = nullptr, *d_nodeB = nullptr;

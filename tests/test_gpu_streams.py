@@ -74,3 +74,19 @@ def test_streams_subset_and_graphs(gpu_icm):
         assert np.array_equal(graphed.equity(Pr, Q=Q), one.equity(Pr, Q=Q)), Q
     one.close()
     graphed.close()
+
+
+@pytest.mark.parametrize("n,k,q_chunk", [(3000, 400, 0), (16384, 2000, 0), (9000, 9000, 11), (700, 5, 3)])
+def test_streams_vjp_bitwise(gpu_icm, n, k, q_chunk):
+    """VJP plans run the forward tree and the adjoint passes of every piece on
+    its stream; gradients (with and without the node terms) equal the
+    one-stream run's bit for bit."""
+    S, P = _field(n, k, 7 * n + k)
+    cot = np.random.default_rng(n).standard_normal(n)
+    gpu_icm.configure(chunk_streams=1, q_chunk=q_chunk, small_max_n=-1)
+    refs = [gpu_icm.equity_vjp(S, P, cot, node_terms=t) for t in (False, True)]
+    for streams in (2, 3, 4):
+        gpu_icm.configure(chunk_streams=streams, q_chunk=q_chunk, small_max_n=-1)
+        for t, (gS, gP) in zip((False, True), refs):
+            a, b = gpu_icm.equity_vjp(S, P, cot, node_terms=t)
+            assert np.array_equal(a, gS) and np.array_equal(b, gP), (streams, t)
