@@ -5,8 +5,12 @@
 #include <cstdio>
 #include <cstring>
 #include <atomic>
+#include <condition_variable>
+#include <functional>
 #include <mutex>
 #include <thread>
+
+#include <unistd.h>
 
 #include "engine.h"
 #include "kernels.h"
@@ -178,15 +182,92 @@ struct HostBarrier {
         }
     }
 };
+
+// Worker threads kept for the life of the process, parked on a condition
+// variable between jobs: run(T, fn) calls fn(t) for t in [0, T), t = 0 on the
+// calling thread, and returns when all have returned.  One job at a time; a
+// caller that finds the pool busy (another host thread sorting) or runs in a
+// forked child gets threads of its own instead.  fn must not throw.  The pool
+// is never destroyed (its workers outlive static destructors at exit).
+class HostPool {
+  public:
+    static HostPool &get() {
+        static HostPool *pool = new HostPool();
+        return *pool;
+    }
+    void run(int T, const std::function<void(int)> &fn) {
+        if (T <= 1) {
+            fn(0);
+            return;
+        }
+        std::unique_lock<std::mutex> busy(busy_, std::try_to_lock);
+        if (!busy.owns_lock() || getpid() != pid_) {
+            std::vector<std::thread> th;
+            for (int t = 1; t < T; ++t) th.emplace_back(fn, t);
+            fn(0);
+            for (auto &x : th) x.join();
+            return;
+        }
+        while (nthreads_ < T - 1) {
+            const int id = ++nthreads_;
+            std::thread([this, id] { loop(id); }).detach();
+        }
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            job_ = &fn;
+            active_ = T;
+            left_.store(T - 1, std::memory_order_relaxed);
+            ++gen_;
+        }
+        cv_.notify_all();
+        fn(0);
+        while (left_.load(std::memory_order_acquire) > 0) std::this_thread::yield();
+    }
+
+  private:
+    HostPool() : pid_(getpid()) {}
+    void loop(int id) {
+        long seen = 0;
+        for (;;) {
+            const std::function<void(int)> *f = nullptr;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (id >= active_) continue;   // not needed by this job
+                f = job_;
+            }
+            (*f)(id);
+            left_.fetch_sub(1, std::memory_order_acq_rel);
+        }
+    }
+    std::mutex busy_, m_;
+    std::condition_variable cv_;
+    const std::function<void(int)> *job_ = nullptr;
+    long gen_ = 0;
+    int active_ = 0, nthreads_ = 0;
+    std::atomic<int> left_{0};
+    const pid_t pid_;
+};
 }  // namespace
 
 // perm: player indices by stack, descending, ties by index.  Positive finite
-// doubles order like their bit patterns, so the complemented bits sorted
-// ascending by a stable LSD radix sort (11-bit digits) give that order in a
-// few linear passes.  T threads each count and scatter a contiguous chunk;
-// output offsets run digit-major then thread-minor, so every pass is stable.
-// Digits shared by every key are skipped.  Small fields use a comparison sort
-// with the same total order.
+// doubles order like their bit patterns, so sorting the complemented bits
+// ascending, stably, gives that order.  T threads (a persistent pool) each
+// take a contiguous chunk of the players:
+//   1. keys, and their range: the 12 bits below the highest bit in which any
+//      two keys differ form the bucket digit (the keys' common high bits and
+//      everything below the digit aside);
+//   2. per-thread histograms; offsets bucket-major, thread-minor, so the
+//      scatter into buckets keeps index order within a bucket;
+//   3. each thread sorts whole buckets (split among threads by count) by
+//      (key, index): insertion sort up to 32 players, std::sort above.
+// Stacks spread over many binades fill the 4096 buckets evenly (the bit
+// patterns grow like log S).  Where one bucket would hold more than
+// max(4096, n / 4T) players (many near-equal stacks beside a far outlier)
+// the threads run a stable LSD radix sort over all 64 bits instead (11-bit
+// digits, digits shared by every key skipped).  Small fields use a
+// comparison sort with the same total order.
 void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
     perm.resize(n);
     if (n <= 4096) {
@@ -198,39 +279,128 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
         for (int i = 0; i < n; ++i) perm[i] = kv[i].second;
         return;
     }
-    constexpr int kBits = 11, kBuckets = 1 << kBits, kPasses = (64 + kBits - 1) / kBits;
+    constexpr int kDig = 12, kNB = 1 << kDig;                      // bucket digit
+    constexpr int kBits = 11, kBuckets = 1 << kBits, kPasses = (64 + kBits - 1) / kBits;   // LSD
     const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    // measured on the 16-core Grace host: n = 65536 1.15 ms on one thread,
-    // 0.80 ms on 8; n = 2^20 19.1 ms on one, 2.8 ms on 16 (std::sort 72.6 ms)
     const int T = n < (1 << 15) ? 1 : std::min({hw, 16, n / 8192});
     std::vector<uint64_t> key(n), key2(n);
     std::vector<int> idx(n), idx2(n);
-    std::vector<uint32_t> hist((size_t)T * kBuckets);
+    std::vector<uint32_t> hist((size_t)T * kNB), offs((size_t)T * kNB), bstart(kNB + 1);
+    std::vector<uint64_t> lo(T), hi(T);
+    std::vector<int> brange(T + 1);
+    const int cap = std::max(4096, n / (4 * T));   // largest bucket the bucket sort takes
+    std::vector<std::pair<uint64_t, int>> scratch((size_t)T * cap);
+    uint64_t kmin = 0;
+    int shift = 0, nb = 1;
+    bool lsd = false;
     uint8_t skip[kPasses] = {};
     HostBarrier bar(T);
+    auto sync = [&] {
+        if (T > 1) bar.wait();
+    };
     auto work = [&](int t) {
         const int i0 = (int)((long)n * t / T), i1 = (int)((long)n * (t + 1) / T);
+        uint64_t mn = ~0ull, mx = 0;
         for (int i = i0; i < i1; ++i) {
             uint64_t b;
             std::memcpy(&b, S + i, sizeof b);
-            key[i] = ~b;
+            const uint64_t k = ~b;
+            key[i] = k;
             idx[i] = i;
+            mn = std::min(mn, k);
+            mx = std::max(mx, k);
         }
+        lo[t] = mn;
+        hi[t] = mx;
+        sync();
+        if (t == 0) {
+            kmin = *std::min_element(lo.begin(), lo.end());
+            const uint64_t span = *std::max_element(hi.begin(), hi.end()) - kmin;
+            int bits = 0;
+            while (bits < 64 && (span >> bits) != 0) ++bits;
+            shift = std::max(0, bits - kDig);
+            nb = (int)(span >> shift) + 1;
+        }
+        sync();
+        uint32_t *h = hist.data() + (size_t)t * kNB;
+        std::fill(h, h + nb, 0u);
+        for (int i = i0; i < i1; ++i) ++h[(key[i] - kmin) >> shift];
+        sync();
+        if (t == 0) {   // bucket starts, the largest bucket, bucket ranges of ~n/T players
+            uint32_t sum = 0, big = 0;
+            for (int b = 0; b < nb; ++b) {
+                bstart[b] = sum;
+                uint32_t c = 0;
+                for (int u = 0; u < T; ++u) c += hist[(size_t)u * kNB + b];
+                big = std::max(big, c);
+                sum += c;
+            }
+            bstart[nb] = sum;
+            lsd = big > (uint32_t)cap;
+            int b = 0;
+            for (int u = 0; u < T; ++u) {
+                const long want = (long)n * u / T;
+                while (b < nb && bstart[b] < want) ++b;
+                brange[u] = b;
+            }
+            brange[T] = nb;
+        }
+        sync();
+        if (!lsd) {
+            uint32_t *of = offs.data() + (size_t)t * kNB;
+            for (int b = 0; b < nb; ++b) {
+                uint32_t o = bstart[b];
+                for (int u = 0; u < t; ++u) o += hist[(size_t)u * kNB + b];
+                of[b] = o;
+            }
+            for (int i = i0; i < i1; ++i) {
+                const uint64_t k = key[i];
+                const uint32_t o = of[(k - kmin) >> shift]++;
+                key2[o] = k;
+                idx2[o] = i;
+            }
+            sync();
+            for (int b = brange[t]; b < brange[t + 1]; ++b) {
+                const int s0 = (int)bstart[b], e0 = (int)bstart[b + 1];
+                if (e0 - s0 <= 32) {   // insertion sort; index order already holds among equal keys
+                    for (int i = s0 + 1; i < e0; ++i) {
+                        const uint64_t k = key2[i];
+                        const int x = idx2[i];
+                        int j = i - 1;
+                        while (j >= s0 && key2[j] > k) {
+                            key2[j + 1] = key2[j];
+                            idx2[j + 1] = idx2[j];
+                            --j;
+                        }
+                        key2[j + 1] = k;
+                        idx2[j + 1] = x;
+                    }
+                } else {   // (key, index) pairs in this thread's scratch
+                    std::pair<uint64_t, int> *kv = scratch.data() + (size_t)t * cap;
+                    for (int i = s0; i < e0; ++i) kv[i - s0] = {key2[i], idx2[i]};
+                    std::sort(kv, kv + (e0 - s0));
+                    for (int i = s0; i < e0; ++i) idx2[i] = kv[i - s0].second;
+                }
+            }
+            sync();
+            std::copy(idx2.begin() + i0, idx2.begin() + i1, perm.begin() + i0);
+            return;
+        }
+        // LSD radix sort over all digits (keys and indices in key / idx)
         uint64_t *k = key.data(), *k2 = key2.data();
         int *x = idx.data(), *x2 = idx2.data();
-        uint32_t *h = hist.data() + (size_t)t * kBuckets;
         for (int d = 0; d < kPasses; ++d) {
             const int sh = d * kBits;
             std::fill(h, h + kBuckets, 0u);
             for (int i = i0; i < i1; ++i) ++h[(k[i] >> sh) & (kBuckets - 1)];
-            if (T > 1) bar.wait();
+            sync();
             if (t == 0) {   // offsets: digit-major, thread-minor
                 uint32_t sum = 0;
                 int used = 0;
                 for (int b = 0; b < kBuckets; ++b) {
                     uint32_t tot = 0;
                     for (int u = 0; u < T; ++u) {
-                        uint32_t &c = hist[(size_t)u * kBuckets + b];
+                        uint32_t &c = hist[(size_t)u * kNB + b];
                         const uint32_t cnt = c;
                         c = sum + tot;
                         tot += cnt;
@@ -240,7 +410,7 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
                 }
                 skip[d] = used <= 1;   // one digit value: the order stays
             }
-            if (T > 1) bar.wait();
+            sync();
             if (!skip[d]) {
                 for (int i = i0; i < i1; ++i) {
                     const uint32_t o = h[(k[i] >> sh) & (kBuckets - 1)]++;
@@ -250,14 +420,11 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
                 std::swap(k, k2);
                 std::swap(x, x2);
             }
-            if (T > 1) bar.wait();
+            sync();
         }
         if (t == 0) std::copy(x, x + n, perm.begin());
     };
-    std::vector<std::thread> th;
-    for (int t = 1; t < T; ++t) th.emplace_back(work, t);
-    work(0);
-    for (auto &x : th) x.join();
+    HostPool::get().run(T, work);
 }
 
 int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {

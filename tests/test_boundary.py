@@ -137,17 +137,36 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     importlib.reload(L)
 
 
-@pytest.mark.parametrize("n", [1, 2, 7, 4096, 4097, 70000, 300000])
-def test_player_order_host(built_lib, n):
+def _stacks(dist, n, rng):
+    if dist == "mixed":                                             # many ties beside extreme magnitudes
+        S = rng.integers(1, 50, n).astype(float)
+        if n > 3:
+            S[: n // 3] = 10.0 ** rng.uniform(-300, 300, n // 3)
+            S[1] = np.nextafter(S[0], 0.0)                          # neighbours in the last bit
+        return S
+    if dist == "loguniform":
+        return 10.0 ** rng.uniform(0, 9, n)
+    if dist == "lognormal":
+        return 1e4 * np.exp(1.5 * rng.standard_normal(n))
+    if dist == "ints100":
+        return rng.integers(1, 101, n).astype(float)
+    if dist == "equal":
+        return np.full(n, 2500.0)
+    S = np.full(n, 100.0)                                           # one far outlier, near-equal rest
+    S[::7] = np.nextafter(100.0, 200.0)
+    S[n // 2] = 1e9
+    return S
+
+
+@pytest.mark.parametrize("dist", ["mixed", "loguniform", "lognormal", "ints100", "equal", "outlier"])
+@pytest.mark.parametrize("n", [1, 2, 7, 4096, 4097, 20000, 70000, 300000])
+def test_player_order_host(built_lib, n, dist):
     """The engine's player order (host only): stacks descending, ties by index,
-    for the comparison sort (n <= 4096), the radix sort on one thread and on
-    several (n >= 32768)."""
+    for the comparison sort (n <= 4096), the bucket sort on one thread and on
+    several (n >= 32768), and its LSD fallback (one bucket would hold most
+    players: equal stacks, a far outlier, ties beside extreme magnitudes)."""
     import icm_gb300 as icm
-    rng = np.random.default_rng(n)
-    S = rng.integers(1, 50, n).astype(float)                    # many ties
-    if n > 3:
-        S[: n // 3] = 10.0 ** rng.uniform(-300, 300, n // 3)   # extreme magnitudes
-        S[1] = np.nextafter(S[0], 0.0)                          # neighbours in the last bit
+    S = _stacks(dist, n, np.random.default_rng(n))
     ref = np.lexsort((np.arange(n), -S))
     assert np.array_equal(icm.player_order(S), ref)
     with pytest.raises(icm.ICMError):
@@ -177,3 +196,36 @@ def test_plan_geometry_invariants(built_lib):
                         checked += 1
     assert checked > 1500
     assert L.icm_gb300_check_geometry(5, 6, 8, 64, 0, why, 256) == -1
+
+
+@pytest.mark.filterwarnings("ignore:This process .* is multi-threaded")
+def test_player_order_concurrent_and_forked(built_lib):
+    """The sort's worker pool serves one call at a time: concurrent callers
+    (ctypes releases the GIL) get threads of their own, and a forked child,
+    which has none of the parent's workers, sorts with fresh threads."""
+    import os
+    import threading
+    import icm_gb300 as icm
+    rng = np.random.default_rng(3)
+    cases = [10.0 ** rng.uniform(0, 9, n) for n in (70000, 150000, 40000, 90000)]
+    refs = [np.lexsort((np.arange(len(S)), -S)) for S in cases]
+    assert np.array_equal(icm.player_order(cases[0]), refs[0])   # the pool exists
+    bad = []
+
+    def worker(j):
+        for _ in range(5):
+            if not np.array_equal(icm.player_order(cases[j]), refs[j]):
+                bad.append(j)
+
+    th = [threading.Thread(target=worker, args=(j,)) for j in range(len(cases))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not bad
+    pid = os.fork()
+    if pid == 0:   # child: exit status 0 only for the right order
+        ok = np.array_equal(icm.player_order(cases[1]), refs[1])
+        os._exit(0 if ok else 1)
+    _, status = os.waitpid(pid, 0)
+    assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0
