@@ -170,13 +170,22 @@ class GpuPlan:
         if not self._p:
             raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
 
-    def equity(self, payouts, Q=256, return_stats=False):
+    def equity(self, payouts, Q=256, return_stats=False, nodes=None):
+        """Equities for ``payouts`` (length k).  ``nodes=(q_begin, q_end)``
+        sums only the rule's nodes q_begin <= q < q_end of Q (a part of the
+        quadrature; the parts of a partition of [0, Q) add up to the full
+        equities, to rounding)."""
         P = _to_double_array(payouts, "payouts")
         if len(P) != self.k:
             raise ValueError(f"payouts length {len(P)} != plan k={self.k}")
         out = np.zeros(self.n)
         st = IcmGpuRunStats()
-        if lib().icm_gpu_equity_with_plan(self._p, int(Q), _d(P), _d(out), ctypes.byref(st)) != 0:
+        if nodes is None:
+            rc = lib().icm_gpu_equity_with_plan(self._p, int(Q), _d(P), _d(out), ctypes.byref(st))
+        else:
+            qb, qe = (int(x) for x in nodes)
+            rc = lib().icm_gb300_plan_equity_nodes(self._p, int(Q), _d(P), qb, qe, _d(out), ctypes.byref(st))
+        if rc != 0:
             raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
         return (out, _stats_dict(st)) if return_stats else out
 

@@ -64,6 +64,8 @@ SIGNATURES = {
     "icm_gpu_plan_destroy": (None, [_vp]),
     "icm_gpu_plan_summary": (ctypes.c_int, [_vp, ctypes.POINTER(IcmGpuPlanSummary)]),
     "icm_gpu_equity_with_plan": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, ctypes.POINTER(IcmGpuRunStats)]),
+    "icm_gb300_plan_equity_nodes": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int, _dp,
+                                                   ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gpu_equity": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, _dp,
                                       ctypes.POINTER(IcmGpuOptions), ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gpu_equity_subset": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, _dp, _ip,

@@ -346,6 +346,23 @@ int icm_gpu_equity_with_plan(IcmGpuPlan *plan, int Q, const double *payout, doub
     });
 }
 
+int icm_gb300_plan_equity_nodes(IcmGpuPlan *plan, int Q, const double *payout, int q_begin, int q_end,
+                                double *equity, IcmGpuRunStats *stats) {
+    return guarded<int>("icm_gb300_plan_equity_nodes", -1, [&]() -> int {
+        Plan *p = reinterpret_cast<Plan *>(plan);
+        if (!p || !payout || !equity || Q <= 0 || q_begin < 0 || q_begin > q_end || q_end > Q) {
+            set_error("icm_gb300_plan_equity_nodes invalid arguments");
+            return -1;
+        }
+        if (!ensure_device()) return -1;
+        std::string err;
+        const int rc = plan_run(p, Q, payout, equity, stats, err, q_begin, q_end);
+        t_launches = p->launches;
+        if (rc != 0) { set_error(err); return -1; }
+        return 0;
+    });
+}
+
 int icm_gpu_equity(int n, const double *S, int Q, const double *payout, int k, double *equity,
                    const IcmGpuOptions *opts, IcmGpuRunStats *stats) {
     return guarded<int>("icm_gpu_equity", -1, [&]() -> int {

@@ -1188,15 +1188,18 @@ static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
     }
 }
 
-int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats, std::string &err) {
+int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats, std::string &err,
+             int q_begin, int q_end) {
     if (!p || Q < 1 || !payout || !equity) { err = "invalid arguments"; return -1; }
+    if (q_end < 0) q_end = Q;
+    if (q_begin < 0 || q_begin > q_end || q_end > Q) { err = "invalid node range"; return -1; }
     const double t0 = now_ns();
     p->launches = 0;
     std::vector<double> logv, w;
     make_nodes(Q, p->Smax, logv, w);
     std::vector<double> node;
     node.reserve(3 * (size_t)Q);
-    for (int q = 0; q < Q; ++q) {
+    for (int q = q_begin; q < q_end; ++q) {
         if (w[q] == 0.0) continue;   // the reference skips zero-weight nodes
         node.push_back(logv[q]);
         node.push_back(w[q]);

@@ -194,8 +194,9 @@ static inline int plan_ilog2(long v) {
 }
 void plan_destroy(Plan *p);
 int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &err);
+// q_begin, q_end: the rule's nodes [q_begin, q_end) only (q_end < 0: all Q)
 int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats,
-             std::string &err);
+             std::string &err, int q_begin = 0, int q_end = -1);
 int select_block_size(int n, int k);
 
 // quadrature nodes (host), restating the reference's erfc-trapezoid rule

@@ -189,6 +189,17 @@ int icm_gb300_tuner_lookup(int n, int k, int *block_size, int *fft_min_degree);
 int icm_gb300_autotune(int n, const double *S, int Q, const double *payout, int k, int runs,
                        int *block_size, int *fft_min_degree, double *best_ms);
 
+/* One plan, part of the quadrature: equity[i] = the sum over the rule's
+ * nodes q in [q_begin, q_end) of Q of player i's node contribution
+ * (icm_gpu_equity_with_plan sums all Q).  The partial sums of a partition
+ * of [0, Q) add up to the full equities (to rounding: the full run sums the
+ * nodes in one fixed order); [0, Q) equals icm_gpu_equity_with_plan bit for
+ * bit.  This is the node-range split a multi-GPU driver uses: each GPU takes
+ * a range, one all-reduce sums the partials (icm_gb300/distributed.py).
+ * Returns 0 / -1 (invalid range: 0 <= q_begin <= q_end <= Q). */
+int icm_gb300_plan_equity_nodes(IcmGpuPlan *plan, int Q, const double *payout, int q_begin, int q_end,
+                                double *equity, IcmGpuRunStats *stats);
+
 /* Quadrature ladder: solves with Q0, 2 Q0, 4 Q0, ... nodes of the
  * reference's rule (never more than Qmax) until two successive results
  * agree per player to tol (relative, against a floor of 1e-12 of the
