@@ -114,10 +114,15 @@ int run_full(int n, const double *S, int Q, const double *payout, int k, double 
         if (r < 0) { set_error(err); return -1; }
         if (r == 1) { t_launches = nl; return 0; }
     }
-    // repeated calls of one shape reuse the thread's last plan (new stacks only)
-    Plan *p = targets ? nullptr : cached_plan(n, k, opts);
+    // repeated calls of one shape reuse the thread's last plan (new stacks
+    // only; a subset query sets its targets for the one run)
+    Plan *p = cached_plan(n, k, opts);
     if (p) {
-        if (plan_restack(p, S, err) != 0) { set_error(err); return -1; }
+        if (plan_restack(p, S, err) != 0) {
+            plan_destroy(p);
+            set_error(err);
+            return -1;
+        }
     } else {
         p = plan_create(n, S, k, opts, err);
         if (!p) { set_error(err); return -1; }
@@ -125,8 +130,9 @@ int run_full(int n, const double *S, int Q, const double *payout, int k, double 
     int rc = 0;
     if (targets) rc = plan_set_targets(p, targets, n_targets, err);
     if (rc == 0) rc = plan_run(p, Q, payout, equity, stats, err);
+    p->subset = false;
     t_launches = p->launches;
-    if (rc != 0 || targets || !keep_plan(p, opts)) plan_destroy(p);
+    if (rc != 0 || !keep_plan(p, opts)) plan_destroy(p);
     if (rc != 0) { set_error(err); return -1; }
     return 0;
 }

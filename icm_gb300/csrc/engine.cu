@@ -1246,7 +1246,7 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     // buffers, which every run refills before the launch
     p->stage_used = 0;
     const bool use_graph = p->opts.enable_graphs == 1 && !p->prof.on && !p->opts.verbose && nact > 0;
-    if (use_graph && (!p->graph || p->graph_nq != nact || p->graph_node != p->d_node)) {
+    if (use_graph && (!p->graph || p->graph_nq != nact || p->graph_node != p->d_node || p->graph_subset != p->subset)) {
         if (p->graph) cudaGraphExecDestroy(p->graph);
         p->graph = nullptr;
         cudaGraph_t g = nullptr;
@@ -1261,6 +1261,7 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return -1; }
         p->graph_nq = nact;
         p->graph_node = p->d_node;
+        p->graph_subset = p->subset;
         p->graph_launches = p->launches - l0;
         p->launches = l0;
     }

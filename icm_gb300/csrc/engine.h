@@ -138,6 +138,7 @@ struct Plan {
     cudaGraphExec_t graph = nullptr;
     int graph_nq = -1;
     const double *graph_node = nullptr;   // the node buffer the graph reads
+    bool graph_subset = false;            // captured with the subset masks
     long graph_launches = 0;
     double peak_bytes = 0;
     // timing: events around the kernel sequence of each run, optional

@@ -353,3 +353,50 @@ def test_one_shot_plan_reuse(gpu_icm):
     finally:
         gpu_icm.configure()
     assert np.array_equal(gpu_icm.gpu_equity(stacks[0], P), fresh(stacks[0]))
+
+
+def test_one_shot_subset_reuses_plan(gpu_icm):
+    """Subset queries take the thread's cached plan too and set their targets
+    for that run only: subset and full one-shot calls of one shape, in any
+    order, with new stacks and with captured graphs, equal the same queries
+    on fresh plans (the subset's non-targets stay 0, a full call after a
+    subset call is not pruned)."""
+    from icm_gb300._lib import IcmGpuOptions, lib
+    import ctypes
+    rng = np.random.default_rng(78)
+    n, k = 6000, 600
+    P = 0.9 ** np.arange(k)
+    T = np.array([0, 5, 2999, 5999], dtype=np.int32)
+    stacks = [1e4 * np.exp(s * rng.standard_normal(n)) for s in (1.0, 2.0)]
+    dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+
+    def subset(S, opts):
+        out = np.zeros(n)
+        assert lib().icm_gpu_equity_subset(n, S.ctypes.data_as(dp), 256, P.ctypes.data_as(dp), k,
+                                           out.ctypes.data_as(dp), T.ctypes.data_as(ip), len(T),
+                                           ctypes.byref(opts) if opts else None, None) == 0
+        return out
+
+    def full(S, opts):
+        out = np.zeros(n)
+        assert lib().icm_gpu_equity(n, S.ctypes.data_as(dp), 256, P.ctypes.data_as(dp), k,
+                                    out.ctypes.data_as(dp), ctypes.byref(opts) if opts else None, None) == 0
+        return out
+
+    def evict():   # another shape replaces the cached plan
+        gpu_icm.gpu_equity(np.linspace(1.0, 2.0, 2500), np.ones(3))
+
+    sub_ref, full_ref = [], []
+    for S in stacks:
+        evict()
+        sub_ref.append(subset(S, None))   # on a fresh plan
+        plan = gpu_icm.GpuPlan(S, k)
+        full_ref.append(plan.equity(P))
+        plan.close()
+        assert np.count_nonzero(np.delete(sub_ref[-1], T)) == 0
+    for opts in (None, IcmGpuOptions(enable_graphs=1)):
+        evict()
+        for j in (0, 1, 0, 1):
+            assert np.array_equal(subset(stacks[j], opts), sub_ref[j])
+            assert np.array_equal(full(stacks[j], opts), full_ref[j])
+            assert np.array_equal(subset(stacks[j], opts), sub_ref[j])
