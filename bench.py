@@ -44,6 +44,81 @@ METRIC = "ms @n=k=65536 Q=256"
 UNIT = "ms/solve"
 WORKLOAD = "drop-in: one tournament n=k=65536, Q=256, stacks log-uniform [1,1e9], payout (k-j+1)^2 normalised"
 B200_PUBLISHED_MS = 20.26   # reference RESULTS.md:551, B200, n=k=65536, Q=256 (uniform [1,100] stacks)
+# the reference's block size for these configurations: its B200 lookup table
+# (devices/b200/gpu_fft_config.h:2373-, read by gpu_empirical_best_B,
+# src/gpu/gpu_cost_model.cu:833)
+REF_B = {(65536, 65536): 64, (1 << 20, 1 << 20): 32, (1 << 20, 1000): 144, (16384, 2000): 64}
+
+
+def canonical_work(n: int, k: int, B: int, Q: int = 256):
+    """The reference GPU engine's work per solve, (FP64 flops, HBM bytes), for
+    (n, k, B, Q): its tree geometry (src/gpu/gpu_cost_model.cu:517-572: nblocks
+    leaves of degree B, psz = min(B 2^(l+1), k_pad), g_needed, below_sat) and
+    per level the effective lengths of src/gpu/gpu_plan.cu:97-114 (p_eff,
+    g_eff, conv_build).  Per parent: schoolbook (conv_build <= 128) build
+    2 p_eff^2, propagate 4 out p_eff; FFT with N = nextpow2(max(conv_build,
+    g_eff)), T = 2.5 N log2 N: build 3T + 3N, propagate 5T + 6N; no build at
+    the root.  Leaves n (2B + 4B) + 20 n.  Bytes: per parent 8 (psz + 2 cps)
+    for the build, 8 (psz + 4 cps) for the propagate, plus 48 n.  Times Q.
+    k_pad = k (the reference's own padding for a power-of-two k; other k it
+    pads to a nearby smooth length, a difference of a few percent here)."""
+    def npow2(x):
+        p = 1
+        while p < x:
+            p <<= 1
+        return p
+    nb = -(-n // B)
+    L = npow2(nb).bit_length()
+    nreal = [nb]
+    for _ in range(1, L):
+        nreal.append((nreal[-1] + 1) // 2)
+    psz = [min(B << (l + 1), k) for l in range(L)]
+    gneed = [min(B, psz[0])]
+    for l in range(1, L):
+        gneed.append(min(gneed[-1] + psz[l - 1] - 1, psz[l]))
+    flop = byte = 0.0
+    for l in range(1, L):
+        cps, pg, P, root = psz[l - 1], psz[l], nreal[l], l == L - 1
+        doubled = (psz[l - 1] == 2 * psz[l - 2]) if l >= 2 else (psz[0] == 2 * B)
+        below = doubled and cps >= 2
+        p_eff = cps // 2 + 1 if below else cps
+        out = gneed[l - 1]
+        g_eff = min(out + p_eff - 1, min(cps + cps // 2, pg) if below else pg)
+        conv = 2 * (cps // 2) + 1 if below else 2 * cps - 1
+        if conv <= 128:
+            build, prop = 2.0 * p_eff * p_eff, 4.0 * out * p_eff
+        else:
+            N = npow2(max(conv, g_eff))
+            T = 2.5 * N * np.log2(N)
+            build, prop = 3 * T + 3 * N, 5 * T + 6 * N
+        flop += P * ((0.0 if root else build) + prop)
+        byte += P * 8.0 * ((0 if root else pg + 2 * cps) + pg + 4 * cps)
+    flop += n * 6.0 * B + 20.0 * n
+    byte += 48.0 * n
+    return flop * Q, byte * Q
+
+
+def hbm_peak_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json"
+    except (OSError, ValueError, KeyError):
+        return 6806.5, "fallback (copy bandwidth measured earlier on this pool)"
+
+
+def canonical_rates(n, k, ms, fp64_tflops):
+    """The reference's canonical work for (n, k) over this run's time: as a
+    fraction of the measured FP64 peak (above 1: this engine does that much
+    less FP64 work than the reference's algorithm) and of the HBM peak."""
+    B = REF_B.get((n, k))
+    if B is None:
+        return None
+    W, D = canonical_work(n, k, B)
+    hbm, src = hbm_peak_gbs()
+    t = ms * 1e-3
+    return {"B_ref": B, "W_ref_flop": float(W), "D_ref_bytes": float(D),
+            "achieved_fp64": float(W / (t * fp64_tflops * 1e12)), "achieved_hbm": float(D / (t * hbm * 1e9)),
+            "fp64_peak_tflops": fp64_tflops, "hbm_peak_gbs": hbm, "hbm_peak_source": src}
 
 
 def parse():
@@ -277,9 +352,10 @@ def main():
             sub_ms.append((t2 - t1) * 1e3)
             full_ms.append((t3 - t2) * 1e3)
 
-    batched = None if args.no_batched else batched_leg(icm, W, max(2, args.steps // 3), args.batch_count)
-    vjp = None if args.no_vjp else vjp_leg(icm, W, 3)
-    gscale = None if args.no_gpu_scale else gpu_scale_leg(icm, W, 2)
+    batched = (None if args.no_batched else
+               batched_leg(icm, W, max(2, args.steps // 3), args.batch_count, fp64_peak_gflops / 1e3))
+    vjp = None if args.no_vjp else vjp_leg(icm, W, 3, fp64_peak_gflops / 1e3)
+    gscale = None if args.no_gpu_scale else gpu_scale_leg(icm, W, 2, fp64_peak_gflops / 1e3)
 
     # end to end through icm_equity (host buffers, plan set-up inside)
     e2e = []
@@ -346,6 +422,7 @@ def main():
         "gpu_scale": gscale,
         "roofline": roofline,
         "algorithmic_tflops_per_s": total_flops / (ms_per_solve * 1e-3) / 1e12,
+        "canonical": canonical_rates(n, k, ms_per_solve, fp64_peak_gflops / 1e3),
         "fp64_peak_tflops_measured": fp64_peak_gflops / 1e3,
         "kernels": [{**r, "ms_per_solve": r["ms"] / args.steps} for r in kst],
         "cpu_baseline": cpu, "clocks": clocks, "wall_s": wall,
@@ -353,7 +430,7 @@ def main():
     print(json.dumps(line), flush=True)
 
 
-def batched_leg(icm, W, steps, count):
+def batched_leg(icm, W, steps, count, fp64_tflops=None):
     """Batched form: `count` tournaments, n log-uniform in [9, 20000],
     k = ceil(0.15 n), lognormal(sigma=1) stacks x 1e4, geometric payouts 0.8,
     Q = 256.  Device time of the work-list engine (graph replay, stacks and
@@ -416,10 +493,22 @@ def batched_leg(icm, W, steps, count):
         "kernels": [{"kernel": r["name"], "ms": r["ms"], "launches": r["launches"], "flops": r["flops"],
                      "share": r["ms"] / tot if tot else None} for r in kst],
         "config": "n log-uniform [9,20000], k=ceil(0.15n), stacks 1e4*lognormal(0,1), payout 0.8^j normalised",
+        "canonical": batch_canonical(Ss, ks, dev_ms, fp64_tflops),
     }
 
 
-def gpu_scale_leg(icm, W, steps):
+def batch_canonical(Ss, ks, ms, fp64_tflops):
+    """The reference's canonical work of the whole batch (each member with
+    the block size min(64, max(8, n/4))) over the batch's device time, as a
+    fraction of the measured FP64 peak."""
+    if not fp64_tflops:
+        return None
+    W = sum(canonical_work(len(S), k, min(64, max(8, len(S) // 4)))[0] for S, k in zip(Ss, ks))
+    return {"W_ref_flop": float(W), "achieved_fp64": float(W / (ms * 1e-3 * fp64_tflops * 1e12)),
+            "fp64_peak_tflops": fp64_tflops, "B_ref": "min(64, max(8, n/4)) per member"}
+
+
+def gpu_scale_leg(icm, W, steps, fp64_tflops=None):
     """GPU-only scale: n = 2^20 players, stacks 1e4 exp(1.5 N(0,1)), Q = 256;
     (a) k = n linear payout, (b) k = 1000 geometric 0.97.  Device ms per solve
     with the plan resident, end-to-end ms through icm_equity, and the
@@ -441,6 +530,8 @@ def gpu_scale_leg(icm, W, steps):
         e2e = time.perf_counter() - t0
         rec = {"k": len(P), "device_ms": float(np.median(dev)), "e2e_ms": e2e * 1e3,
                "q_chunk": summ["q_batch"], "device_bytes": summ["planned_peak_vram_bytes"]}
+        if fp64_tflops:
+            rec["canonical"] = canonical_rates(len(S), len(P), rec["device_ms"], fp64_tflops)
         if shape == "linear":   # V1_i = 1 + sum_{j != i} S_i / (S_i + S_j); payout (n - m) / sum
             idx = np.random.default_rng(3).choice(len(S), 64, replace=False)
             n = len(S)
@@ -450,7 +541,7 @@ def gpu_scale_leg(icm, W, steps):
     return out
 
 
-def vjp_leg(icm, W, steps):
+def vjp_leg(icm, W, steps, fp64_tflops=None):
     """Differentiated form: n = 16384, k = 2000, Q = 256, gamma(2, 5000)
     stacks, N(0, 1) cotangent, linear and quadratic payouts.  Device time of
     the VJP (forward tree recomputed inside) against the forward solve on the
@@ -477,6 +568,8 @@ def vjp_leg(icm, W, steps):
         t0 = time.perf_counter()
         icm.equity_vjp(S, P, cot)
         e2e = time.perf_counter() - t0
+        if fp64_tflops:
+            out.setdefault("canonical_fwd", canonical_rates(len(S), k, float(np.median(fwd)), fp64_tflops))
         out[shape] = {"fwd_ms": float(np.median(fwd)), "vjp_ms": float(np.median(vjp)),
                       "ratio": float(np.median(vjp) / np.median(fwd)), "vjp_e2e_ms": e2e * 1e3}
     ts, cots = vjp_batch_tournaments(256)
