@@ -946,7 +946,7 @@ static void stage_mark(Plan *p, cudaStream_t st) {
 
 void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide,
                const ChunkView *view, cudaEvent_t acc_wait, cudaEvent_t acc_done) {
-    // the chunk's buffers: the plan's own, or a view on the second half of them
+    // the chunk's buffers: the plan's own, or a piece's view of them (node slots from its offset)
     cudaStream_t st = view ? view->st : p->stream;
     const int L = p->L;
     Level *lv = view ? const_cast<Level *>(view->lv) : p->lv;

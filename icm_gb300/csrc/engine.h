@@ -182,7 +182,9 @@ size_t plan_tree_layout(Plan *p, int qc, char *base);
 Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err,
                   bool coeff_only = false, double q_bytes_scale = 1.0, size_t budget = 0);
 // launch sequence of one chunk of nq nodes (engine.cu); divide = false stops
-// after the propagate pass (the tree of the chunk stays in the plan's buffers)
+// after the propagate pass (the tree of the chunk stays in the plan's buffers).
+// view: run on a chunk piece's buffers and stream instead of the plan's own;
+// the node sum waits for acc_wait and records acc_done when they are given.
 void run_chunk(Plan *p, int q0, int nq, const double2 *tw, int logTW, bool first, bool divide,
                const ChunkView *view = nullptr, cudaEvent_t acc_wait = nullptr, cudaEvent_t acc_done = nullptr);
 // nodes of piece i (of np) of a chunk with r nodes left for pieces i .. np-1:
