@@ -90,3 +90,18 @@ def test_streams_vjp_bitwise(gpu_icm, n, k, q_chunk):
         for t, (gS, gP) in zip((False, True), refs):
             a, b = gpu_icm.equity_vjp(S, P, cot, node_terms=t)
             assert np.array_equal(a, gS) and np.array_equal(b, gP), (streams, t)
+
+
+def test_streams_random_shapes(gpu_icm):
+    """Random fields, payout lengths, chunk sizes and Q: four streams equal
+    one bit for bit."""
+    rng = np.random.default_rng(2024)
+    for _ in range(24):
+        n = int(np.exp(rng.uniform(np.log(1600), np.log(30000))))
+        k = int(rng.integers(1, n + 1)) if rng.random() < 0.5 else n
+        Q = int(rng.choice([16, 64, 256]))
+        qc = int(rng.choice([0, 0, 5, 17, 60]))
+        S = 10.0 ** rng.uniform(0, float(rng.choice([2, 5, 9])), n)
+        P = rng.random(k)
+        ref = _run(gpu_icm, S, P, 1, qc, Q)
+        assert np.array_equal(_run(gpu_icm, S, P, 4, qc, Q), ref), (n, k, Q, qc)
