@@ -163,7 +163,7 @@ def _stacks(dist, n, rng):
 def test_player_order_host(built_lib, n, dist):
     """The engine's player order (host only): stacks descending, ties by index,
     for the comparison sort (n <= 4096), the bucket sort on one thread and on
-    several (n >= 32768), and its LSD fallback (one bucket would hold most
+    several (n >= 16384), and its LSD fallback (one bucket would hold most
     players: equal stacks, a far outlier, ties beside extreme magnitudes)."""
     import icm_gb300 as icm
     S = _stacks(dist, n, np.random.default_rng(n))
