@@ -54,6 +54,7 @@ static void parallel_for(int count, F fn) {
     std::vector<std::thread> th;
     for (int w = 0; w < nt; ++w)
         th.emplace_back([&, w] {
+            SortThreadCap cap(1);   // the members' sorts: one thread each
             for (int i = w; i < count; i += nt) fn(i);
         });
     for (auto &t : th) t.join();

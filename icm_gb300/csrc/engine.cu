@@ -268,6 +268,10 @@ class HostPool {
 // the threads run a stable LSD radix sort over all 64 bits instead (11-bit
 // digits, digits shared by every key skipped).  Small fields use a
 // comparison sort with the same total order.
+static thread_local int t_sort_cap = 0;   // 0: no cap
+SortThreadCap::SortThreadCap(int cap) : prev(t_sort_cap) { t_sort_cap = cap; }
+SortThreadCap::~SortThreadCap() { t_sort_cap = prev; }
+
 void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
     perm.resize(n);
     if (n <= 4096) {
@@ -282,7 +286,8 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
     constexpr int kDig = 12, kNB = 1 << kDig;                      // bucket digit
     constexpr int kBits = 11, kBuckets = 1 << kBits, kPasses = (64 + kBits - 1) / kBits;   // LSD
     const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    const int T = n < 16384 ? 1 : std::min({hw, 16, n / 4096});   // measured crossover on the Grace host
+    int T = n < 16384 ? 1 : std::min({hw, 16, n / 4096});   // measured crossover on the Grace host
+    if (t_sort_cap > 0) T = std::min(T, t_sort_cap);
     std::vector<uint64_t> key(n), key2(n);
     std::vector<int> idx(n), idx2(n);
     std::vector<uint32_t> hist((size_t)T * kNB), offs((size_t)T * kNB), bstart(kNB + 1);

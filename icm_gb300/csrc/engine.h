@@ -163,6 +163,15 @@ struct Plan {
 // lifecycle (engine.cu)
 // geometry only: validation, sort, levels, per-node element counts
 int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err);
+// caps the player sort's threads on the calling thread while it lives (host
+// code that already runs on many threads sorts on one thread each)
+struct SortThreadCap {
+    int prev;
+    explicit SortThreadCap(int cap);
+    ~SortThreadCap();
+    SortThreadCap(const SortThreadCap &) = delete;
+    SortThreadCap &operator=(const SortThreadCap &) = delete;
+};
 // device allocation of plans, batches and VJPs (stream-ordered pool or plain
 // cudaMalloc), with the test hook that makes the n-th one fail
 cudaError_t dev_alloc(void **ptr, size_t bytes, cudaStream_t st, bool pooled);
