@@ -642,16 +642,19 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
         p->qc = qc;
         p->d_S = f->d_S + f->off[i];
         p->d_payout = f->d_payout + f->poff[i];
-        const long fo = f->off[i];
-        for (int j = 0; j < p->n; ++j) {
-            hS[fo + j] = p->S_sorted[j];
-            hperm[fo + j] = (int)(fo + p->perm[j]);
-        }
         for (int l = 1; l < p->L; ++l) {
             if (p->lv[l].fft) logNeed = std::max(logNeed, ilog2l(p->lv[l].fftn));
             if (p->lv[l].kind == 2) logNeed = std::max(logNeed, ilog2l(2 * p->lv[l].deg));
         }
     }
+    parallel_for(F, [&](int i) {   // sorted stacks and the permutation, members side by side
+        const Plan *p = f->tr[i];
+        const long fo = f->off[i];
+        for (int j = 0; j < p->n; ++j) {
+            hS[fo + j] = p->S_sorted[j];
+            hperm[fo + j] = (int)(fo + p->perm[j]);
+        }
+    });
     std::vector<longlong2> hmem;
     if (vjp) {
         f->d_cot = (double *)(A + o_cot);
