@@ -36,14 +36,22 @@ def test_node_ranges_add_up(gpu_icm, n, k):
         plan.close()
 
 
-def test_distributed_one_rank(gpu_icm):
+@pytest.mark.parametrize("backend", ["gloo", "nccl"])
+def test_distributed_one_rank(gpu_icm, backend):
+    """One rank: its range is [0, Q) and the all-reduce (on the host for gloo,
+    on the device for NCCL) leaves the equities unchanged."""
+    import torch
     import torch.distributed as dist
     from icm_gb300 import distributed as D
+    if backend == "nccl" and not dist.is_nccl_available():
+        pytest.skip("no NCCL in this torch build")
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
         port = s.getsockname()[1]
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
-    dist.init_process_group("gloo", rank=0, world_size=1)
+    if backend == "nccl":
+        torch.cuda.set_device(0)
+    dist.init_process_group(backend, rank=0, world_size=1)
     try:
         rng = np.random.default_rng(2)
         S = 1e4 * np.exp(rng.standard_normal(3000))
