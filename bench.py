@@ -285,7 +285,9 @@ def main():
             pg.barrier()
 
     from icm_gb300 import build as b
-    b.build()
+    if rank == 0:   # one rank compiles (a no-op when the library is up to date); the others wait
+        b.build()
+    barrier()
     import ctypes
     import icm_gb300 as icm
     from icm_gb300 import workloads as W
