@@ -142,6 +142,7 @@ struct SpecBuildArgs {
     int logTW;
     int nbx;
     ZeroPrefix z;
+    int cb;   // parents per CTA (single-plan launches; the packed work lists have their own)
 };
 struct GspecArgs {
     const double *g;
@@ -171,6 +172,7 @@ struct SpecPropArgs {
     int logTW;
     int nbx;
     ZeroPrefix z;
+    int cb;   // parents per CTA (single-plan launches; the packed work lists have their own)
 };
 struct FusedBuildArgs {
     const double *Pc;

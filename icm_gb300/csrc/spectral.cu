@@ -286,7 +286,7 @@ __device__ __forceinline__ int partition_items(const View *V, int *idx, int cnt)
 __device__ void spec_build_body(const SpecBuildArgs &A, int bx, int q) {
     extern __shared__ double2 sm[];
     const int D = 1 << A.logD;
-    const int cb = D >= 4096 ? 1 : 4096 / D;
+    const int cb = A.cb;
     const int j0 = bx * cb;
     const int cnt = min(cb, A.nreal_p - j0);
     if (cnt <= 0) return;
@@ -536,7 +536,7 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int logD
 __device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
     extern __shared__ double2 sm[];
     const int D = 1 << A.logD;
-    const int cbp = D >= 4096 ? 1 : 4096 / D;   // parents per CTA; 2 children each
+    const int cbp = A.cb;   // parents per CTA; 2 children each
     const int j0 = bx * cbp;
     const int cnt = min(cbp, A.npar - j0);
     if (cnt <= 0) return;
@@ -588,6 +588,21 @@ void spec_set_smem_limits() {
     spec_wl_set_smem_limits();
 }
 
+// Items per CTA of a single-plan build or propagate launch: the default
+// (4096 points per CTA) unless the launch would then have fewer than two CTAs
+// per SM, in which case fewer items per CTA (halving) spread it over more SMs.
+// Each item's arithmetic is the same either way.
+static int short_grid_cb(int cb, int nitems, int nq) {
+    static int sms = 0;
+    if (sms <= 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    }
+    while (cb > 1 && (long)((nitems + cb - 1) / cb) * nq < 2L * sms) cb >>= 1;
+    return cb;
+}
+
 SpecInitArgs spec_init_args(const Level &v, const double2 *tw, int logTW, double *fq, size_t *smem) {
     const int logd = ilog2s(v.deg), d = 1 << logd;
     const int cb = spec_cb(d);
@@ -605,7 +620,7 @@ SpecBuildArgs spec_build_args(const Level &c, const Level &p, bool write_coeffs,
     if (smem) *smem = spec_smem_v(D);
     return SpecBuildArgs{c.spec2, c.spec2_q, c.ends, c.ends_q, c.nreal, p.nreal, logD, p.spec2, p.spec2_q,
                          p.spec2 ? p.ends : nullptr, p.ends_q, write_coeffs ? p.P : nullptr, p.P_q, p.pst, p.plen, tw,
-                         logTW, (p.nreal + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}};
+                         logTW, (p.nreal + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}, cb};
 }
 
 GspecArgs gspec_args(const double *g, size_t g_q, int gst, int glen, int nreal, const Level &v, double2 *G, size_t G_q,
@@ -626,7 +641,7 @@ SpecPropArgs spec_prop_args(const double2 *Gp, size_t Gp_q, const Level &c, cons
     if (smem) *smem = spec_smem_v(D);
     return SpecPropArgs{Gp, Gp_q, c.spec2, c.spec2_q, c.nreal, p.nreal, logD, children_spectral ? c.G : nullptr,
                         c.G_q, c.g, c.g_q, c.gst, c.glen, hot_c, tw, logTW, (p.nreal + cbp - 1) / cbp,
-                        ZeroPrefix{nullptr, 0, p.deg}};
+                        ZeroPrefix{nullptr, 0, p.deg}, cbp};
 }
 
 void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cudaStream_t st, Prof *pr, const int *zp,
@@ -648,6 +663,9 @@ void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq
     SpecBuildArgs A = spec_build_args(c, p, write_coeffs, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
+    A.cb = short_grid_cb(A.cb, p.nreal, nq);
+    A.nbx = (p.nreal + A.cb - 1) / A.cb;
+    sm = (size_t)A.cb * ((size_t)(1 << A.logD) * sizeof(double2) + kItemBytes);
     pr->begin("spec_build", fq * nq, st);
     k_spec_build<<<dim3(A.nbx, nq), spec_tpb(sm), sm, st>>>(A);
     pr->end(st);
@@ -674,6 +692,9 @@ void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Leve
     SpecPropArgs A = spec_prop_args(Gp, Gp_q, c, p, children_spectral, hot_c, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
+    A.cb = short_grid_cb(A.cb, p.nreal, nq);
+    A.nbx = (p.nreal + A.cb - 1) / A.cb;
+    sm = (size_t)A.cb * ((size_t)(1 << A.logD) * sizeof(double2) + kItemBytes);
     pr->begin("spec_prop", fq * nq, st);
     k_spec_prop<<<dim3(A.nbx, nq), spec_tpb(sm), sm, st>>>(A);
     pr->end(st);
