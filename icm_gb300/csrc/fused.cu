@@ -37,10 +37,8 @@ __device__ __forceinline__ int fused_cb(int N) { return N >= 8192 ? 1 : 4096 / N
 // tournaments (packed work lists); wholly-zero items are pruned per item.
 constexpr size_t kFusedViewBytes = 80;
 constexpr size_t kFusedItemBytes = kFusedViewBytes + sizeof(int);
-static inline size_t fused_smem_v(int N) {
-    const int cb = N >= 8192 ? 1 : 4096 / N;
-    return (size_t)cb * ((N + N / 2) * sizeof(double2) + kFusedItemBytes);
-}
+static inline size_t fused_smem_cb(int N, int cb) { return (size_t)cb * ((N + N / 2) * sizeof(double2) + kFusedItemBytes); }
+static inline size_t fused_smem_v(int N) { return fused_smem_cb(N, N >= 8192 ? 1 : 4096 / N); }
 
 struct FbView {
     const double *L;   // left child coefficients (the right child's follow at + pst_c)
@@ -240,7 +238,7 @@ __device__ void fused_prop_core(const FpView *V, const int *idx, int nh, int cb,
 __device__ void fused_build_body(const FusedBuildArgs &A, int bx, int q) {
     extern __shared__ double2 sm[];
     const int N = 1 << A.logN, h = N >> 1;
-    const int cb = fused_cb(N);
+    const int cb = A.cb;
     const int j0 = bx * cb;
     const int cnt = min(cb, A.npairs - j0);
     if (cnt <= 0) return;
@@ -255,7 +253,7 @@ __device__ void fused_build_body(const FusedBuildArgs &A, int bx, int q) {
 __device__ void fused_prop_body(const FusedPropArgs &A, int bx, int q) {
     extern __shared__ double2 sm[];
     const int N = 1 << A.logN, h = N >> 1;
-    const int cb = fused_cb(N);
+    const int cb = A.cb;
     const int j0 = bx * cb;
     const int cnt = min(cb, A.npairs - j0);
     if (cnt <= 0) return;
@@ -361,7 +359,7 @@ FusedBuildArgs fused_build_args(const Level &c, const Level &p, bool spectra_onl
     if (fq) *fq = (5.0 * N * logN + (spectra_only ? 8.0 : 40.0 + 2.5 * logN) * (N / 2)) * p.npairs;
     if (smem) *smem = fused_smem_v(N);
     return FusedBuildArgs{c.P, c.P_q, c.pst, c.plen, p.npairs, logN, p.P, p.P_q, p.pst, p.plen, p.spec, tw, logTW,
-                          spectra_only ? 1 : 0, (p.npairs + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}};
+                          spectra_only ? 1 : 0, (p.npairs + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}, cb};
 }
 
 FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl, const Level &c, const Level &p,
@@ -371,7 +369,7 @@ FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl,
     if (fq) *fq = (5.0 * N * logN + 2.5 * N * (logN - 1) + 40.0 * (N / 2)) * p.npairs;
     if (smem) *smem = fused_smem_v(N);
     return FusedPropArgs{gp, gp_q, gst_p, gpl, p.npairs, logN, p.spec, c.g, c.g_q, c.gst, c.glen, hot_c, tw, logTW,
-                         (p.npairs + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}};
+                         (p.npairs + cb - 1) / cb, ZeroPrefix{nullptr, 0, p.deg}, cb};
 }
 
 void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_only, const double2 *tw, int logTW,
@@ -381,6 +379,9 @@ void launch_fused_build(const Level &c, const Level &p, int nq, bool spectra_onl
     FusedBuildArgs A = fused_build_args(c, p, spectra_only, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
+    A.cb = short_grid_cb(A.cb, p.npairs, nq);
+    A.nbx = (p.npairs + A.cb - 1) / A.cb;
+    sm = fused_smem_cb(1 << A.logN, A.cb);
     pr->begin(spectra_only ? "fused_spectra" : "fused_build", fq * nq, st);
     k_fused_build<<<dim3(A.nbx, nq), fused_tpb(sm), sm, st>>>(A);
     pr->end(st);
@@ -394,6 +395,9 @@ void launch_fused_prop(const double *gp, size_t gp_q, int gst_p, int gpl, const 
     FusedPropArgs A = fused_prop_args(gp, gp_q, gst_p, gpl, c, p, hot_c, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
+    A.cb = short_grid_cb(A.cb, p.npairs, nq);
+    A.nbx = (p.npairs + A.cb - 1) / A.cb;
+    sm = fused_smem_cb(1 << A.logN, A.cb);
     pr->begin("fused_prop", fq * nq, st);
     k_fused_prop<<<dim3(A.nbx, nq), fused_tpb(sm), sm, st>>>(A);
     pr->end(st);

@@ -646,6 +646,21 @@ void launch_accumulate(int n, int nq, const double *contrib, double *acc, int fi
     pr->end(st);
 }
 
+// Items per CTA of a single-plan FFT-level launch: the default (4096 points
+// per CTA) unless the launch would then have fewer than two CTAs
+// per SM, in which case fewer items per CTA (halving) spread it over more SMs.
+// Each item's arithmetic is the same either way.
+int short_grid_cb(int cb, int nitems, int nq) {
+    static int sms = 0;
+    if (sms <= 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    }
+    while (cb > 1 && (long)((nitems + cb - 1) / cb) * nq < 2L * sms) cb >>= 1;
+    return cb;
+}
+
 void launch_scatter(int n, const double *acc, const int *perm, const uint8_t *active, double *out,
                     cudaStream_t st) {
     k_scatter<<<nblk(n, 256), 256, 0, st>>>(n, acc, perm, active, out);

@@ -174,6 +174,10 @@ struct SpecPropArgs {
     ZeroPrefix z;
     int cb;   // parents per CTA (single-plan launches; the packed work lists have their own)
 };
+// items per CTA of a single-plan launch of nitems items over nq nodes: cb,
+// halved while the grid would hold fewer than two CTAs per SM (kernels.cu)
+int short_grid_cb(int cb, int nitems, int nq);
+
 struct FusedBuildArgs {
     const double *Pc;
     size_t Pc_q;
@@ -186,6 +190,7 @@ struct FusedBuildArgs {
     int logTW, spectra_only;
     int nbx;
     ZeroPrefix z;
+    int cb;   // pairs per CTA (single-plan launches; the packed work lists have their own)
 };
 struct FusedPropArgs {
     const double *gp;
@@ -200,6 +205,7 @@ struct FusedPropArgs {
     int logTW;
     int nbx;
     ZeroPrefix z;
+    int cb;   // pairs per CTA (single-plan launches; the packed work lists have their own)
 };
 
 // ---- argument builders shared by the single-plan launchers and the work

@@ -588,21 +588,6 @@ void spec_set_smem_limits() {
     spec_wl_set_smem_limits();
 }
 
-// Items per CTA of a single-plan build or propagate launch: the default
-// (4096 points per CTA) unless the launch would then have fewer than two CTAs
-// per SM, in which case fewer items per CTA (halving) spread it over more SMs.
-// Each item's arithmetic is the same either way.
-static int short_grid_cb(int cb, int nitems, int nq) {
-    static int sms = 0;
-    if (sms <= 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
-    }
-    while (cb > 1 && (long)((nitems + cb - 1) / cb) * nq < 2L * sms) cb >>= 1;
-    return cb;
-}
-
 SpecInitArgs spec_init_args(const Level &v, const double2 *tw, int logTW, double *fq, size_t *smem) {
     const int logd = ilog2s(v.deg), d = 1 << logd;
     const int cb = spec_cb(d);

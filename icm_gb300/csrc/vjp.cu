@@ -70,6 +70,9 @@ static inline size_t vjp_up_smem(int N) {
     return (size_t)vjp_cb_h(N) * ((N + N / 2) * sizeof(double2) + kAdjItemBytes);
 }
 static inline size_t vjp_down_smem(int N) { return (size_t)vjp_cb_h(N) * (N * sizeof(double2) + kAdjItemBytes); }
+// the same for cb pairs per CTA
+static inline size_t vjp_up_smem_cb(int N, int cb) { return (size_t)cb * ((N + N / 2) * sizeof(double2) + kAdjItemBytes); }
+static inline size_t vjp_down_smem_cb(int N, int cb) { return (size_t)cb * (N * sizeof(double2) + kAdjItemBytes); }
 
 // ------------------------------------------------------------ leaf adjoints
 // gbar of every leaf block: sum_i c_i Q_i by the running pair
@@ -506,7 +509,7 @@ __device__ void adj_down_core(const AdView *V, const int *idx, int nh, int wmax,
 __device__ __forceinline__ void adj_up_fused_body(const AdjUpFusedArgs &A, int bx, int q, int q0) {
     extern __shared__ double2 sm[];
     const int N = 1 << A.logN, h = N >> 1;
-    const int cb = vjp_cb(N);
+    const int cb = A.cb;
     const int j0 = bx * cb;
     const int cnt = min(cb, A.npairs - j0);
     if (cnt <= 0) return;
@@ -522,7 +525,7 @@ __device__ __forceinline__ void adj_up_fused_body(const AdjUpFusedArgs &A, int b
 __device__ __forceinline__ void adj_down_fused_body(const AdjDownFusedArgs &A, int bx, int q, int q0) {
     extern __shared__ double2 sm[];
     const int N = 1 << A.logN;
-    const int cb = vjp_cb(N);
+    const int cb = A.cb;
     const int j0 = bx * cb;
     const int cnt = min(cb, A.npairs - j0);
     if (cnt <= 0) return;
@@ -1052,7 +1055,7 @@ void adj_up_args(const Plan *p, const VjpBufs &b, int l, const double2 *tw, int 
     if (level_fused(pl)) {
         const int N = pl.fftn, logN = plan_ilog2(N), cb = vjp_cb_h(N);
         F = AdjUpFusedArgs{b.gb[l - 1], b.gb_q[l - 1], b.gb_st[l - 1], c.glen, pl.npairs, logN, pl.spec, b.gspec[l],
-                           out, out_q, gst_p, gpl, tw, logTW, zp, pl.deg, (pl.npairs + cb - 1) / cb};
+                           out, out_q, gst_p, gpl, tw, logTW, zp, pl.deg, (pl.npairs + cb - 1) / cb, cb};
         j0 = pl.npairs;
     } else if (level_big(pl)) {
         j0 = pl.npairs;   // the pairs go through the multi-pass steps (adjoint_chunk)
@@ -1081,7 +1084,7 @@ void adj_down_args(const Plan *p, const VjpBufs &b, int l, const double2 *tw, in
         const int N = pl.fftn, logN = plan_ilog2(N), cb = vjp_cb_h(N);
         F = AdjDownFusedArgs{gp, gp_q, gst_p, gpl, Pbp, pl.P_q, pl.pst, pl.plen, c.P, c.P_q, c.pst, c.plen,
                              pl.npairs, logN, pl.spec, b.gspec[l], b.Pb[l - 1], tw, logTW, zp, pl.deg,
-                             (pl.npairs + cb - 1) / cb};
+                             (pl.npairs + cb - 1) / cb, cb};
         c0 = 2 * pl.npairs;
     } else if (level_big(pl)) {
         c0 = 2 * pl.npairs;
@@ -1226,7 +1229,10 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         AdjUpSchoolArgs Sa;
         adj_up_args(p, b, l, tw, logTW, F, Sa);
         if (F.nbx > 0) {
-            k_adj_up_fused<<<dim3(F.nbx, nq), vjp_tpb(adj_up_smem(F.logN)), adj_up_smem(F.logN), st>>>(F, q0);
+            F.cb = short_grid_cb(F.cb, F.npairs, nq);
+            F.nbx = (F.npairs + F.cb - 1) / F.cb;
+            const size_t smu = vjp_up_smem_cb(1 << F.logN, F.cb);
+            k_adj_up_fused<<<dim3(F.nbx, nq), vjp_tpb(smu), smu, st>>>(F, q0);
             ++launches;
         } else if (level_big(p->lv[l])) {
             adj_up_big(p, b, l, nq, tw, logTW, launches);
@@ -1241,7 +1247,10 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         AdjDownSchoolArgs Sa;
         adj_down_args(p, b, l, tw, logTW, F, Sa);
         if (F.nbx > 0) {
-            k_adj_down_fused<<<dim3(F.nbx, nq), vjp_tpb(adj_down_smem(F.logN)), adj_down_smem(F.logN), st>>>(F, q0);
+            F.cb = short_grid_cb(F.cb, F.npairs, nq);
+            F.nbx = (F.npairs + F.cb - 1) / F.cb;
+            const size_t smd = vjp_down_smem_cb(1 << F.logN, F.cb);
+            k_adj_down_fused<<<dim3(F.nbx, nq), vjp_tpb(smd), smd, st>>>(F, q0);
             ++launches;
         } else if (level_big(p->lv[l])) {
             adj_down_big(p, b, l, nq, tw, logTW, launches);

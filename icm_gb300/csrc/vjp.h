@@ -89,6 +89,7 @@ struct AdjUpFusedArgs {
     const int *zp;
     long span;
     int nbx;
+    int cb;   // pairs per CTA (single plans; the packed work lists have their own)
 };
 struct AdjDownFusedArgs {
     const double *gp;
@@ -107,6 +108,7 @@ struct AdjDownFusedArgs {
     const int *zp;
     long span;
     int nbx;
+    int cb;   // pairs per CTA (single plans; the packed work lists have their own)
 };
 
 // one tournament's adjoint buffers and the views of shared arrays it uses
