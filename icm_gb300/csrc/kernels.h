@@ -124,6 +124,7 @@ struct SpecInitArgs {
     int logTW;
     int nbx;
     ZeroPrefix z;
+    int cb;   // items per CTA (single-plan launches may lower it; work lists keep the default)
 };
 struct SpecBuildArgs {
     const double2 *cspec;
@@ -155,6 +156,7 @@ struct GspecArgs {
     int logTW;
     int nbx;
     ZeroPrefix z;
+    int cb;   // items per CTA (single-plan launches may lower it; work lists keep the default)
 };
 struct SpecPropArgs {
     const double2 *Gp;

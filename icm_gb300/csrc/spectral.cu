@@ -76,7 +76,7 @@ __device__ void spec_init_body(const SpecInitArgs &A, int bx, int q) {
 
     extern __shared__ double2 sm[];
     const int d = 1 << logd;
-    const int cb = d >= 4096 ? 1 : 4096 / d;
+    const int cb = A.cb;
         const int j0 = bx * cb;
     const int cnt = min(cb, nreal - j0);
     if (cnt <= 0) return;
@@ -339,7 +339,7 @@ __device__ void gspec_body(const GspecArgs &A, int bx, int q) {
     extern __shared__ double2 sm[];
     const int h = 1 << (logd - 1);
     const int lh = logd - 1;
-    const int cb = h >= 4096 ? 1 : 4096 / h;
+    const int cb = A.cb;
         const int j0 = bx * cb;
     const int cnt = min(cb, nreal - j0);
     if (cnt <= 0 || zp_cold(A.z, q, j0 + cnt - 1)) return;   // nothing below reads a wholly-zero node's g
@@ -594,7 +594,7 @@ SpecInitArgs spec_init_args(const Level &v, const double2 *tw, int logTW, double
     if (fq) *fq = (5.0 * d * logd + 20.0 * d) * v.nreal;
     if (smem) *smem = spec_smem(d);
     return SpecInitArgs{v.P, v.P_q, v.pst, v.plen, v.nreal, logd, v.spec2, v.spec2_q, v.ends, v.ends_q, tw, logTW,
-                        (v.nreal + cb - 1) / cb, ZeroPrefix{nullptr, 0, v.deg}};
+                        (v.nreal + cb - 1) / cb, ZeroPrefix{nullptr, 0, v.deg}, cb};
 }
 
 SpecBuildArgs spec_build_args(const Level &c, const Level &p, bool write_coeffs, const double2 *tw, int logTW,
@@ -615,7 +615,7 @@ GspecArgs gspec_args(const double *g, size_t g_q, int gst, int glen, int nreal, 
     if (fq) *fq = (5.0 * h * (logd - 1) + 20.0 * h) * nreal;
     if (smem) *smem = spec_smem(h);
     return GspecArgs{g, g_q, gst, glen, nreal, logd, G, G_q, hot, tw, logTW, (nreal + cb - 1) / cb,
-                     ZeroPrefix{nullptr, 0, v.deg}};
+                     ZeroPrefix{nullptr, 0, v.deg}, cb};
 }
 
 SpecPropArgs spec_prop_args(const double2 *Gp, size_t Gp_q, const Level &c, const Level &p, bool children_spectral,
@@ -636,6 +636,9 @@ void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cuda
     SpecInitArgs A = spec_init_args(v, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
+    A.cb = short_grid_cb(A.cb, A.nreal, nq);
+    A.nbx = (A.nreal + A.cb - 1) / A.cb;
+    sm = (size_t)A.cb * (1 << A.logd) * sizeof(double2);
     pr->begin("spec_init", fq * nq, st);
     k_spec_init<<<dim3(A.nbx, nq), spec_tpb(sm), sm, st>>>(A);
     pr->end(st);
@@ -664,6 +667,9 @@ void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal
     GspecArgs A = gspec_args(g, g_q, gst, glen, nreal, v, G, G_q, hot, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
+    A.cb = short_grid_cb(A.cb, A.nreal, nq);
+    A.nbx = (A.nreal + A.cb - 1) / A.cb;
+    sm = (size_t)A.cb * (1 << (A.logd - 1)) * sizeof(double2);
     pr->begin("gspec_init", fq * nq, st);
     k_gspec_init<<<dim3(A.nbx, nq), spec_tpb(sm), sm, st>>>(A);
     pr->end(st);
