@@ -281,7 +281,7 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
     const int M = 1 << logM;
     const int threads = 256;
     if (M <= kSmemFftMax) {
-        const int cb = (M >= 4096) ? 1 : 4096 / M;
+        const int cb = short_grid_cb((M >= 4096) ? 1 : 4096 / M, (int)std::min(batch, 1L << 30), 1);
         const long blocks = (batch + cb - 1) / cb;
         const size_t smem = (size_t)cb * M * sizeof(double2);
         // one CTA per SM when the transform takes more than half the shared
@@ -307,8 +307,9 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
     }
     const int logM1 = (logM + 1) / 2, logM2 = logM - logM1;
     const int M1 = 1 << logM1, M2 = 1 << logM2;
-    const int cbA = max(1, min(M2, 4096 / M1));
-    const int cbB = max(1, min(M1, 4096 / M2));
+    // columns (rows) per CTA: 4096 points' worth, fewer on short grids
+    const int cbA = short_grid_cb(max(1, min(M2, 4096 / M1)), M2, (int)batch);
+    const int cbB = short_grid_cb(max(1, min(M1, 4096 / M2)), M1, (int)batch);
     dim3 gA(M2 / cbA, (unsigned)batch), gB(M1 / cbB, (unsigned)batch);
     const size_t smA = (size_t)cbA * M1 * sizeof(double2), smB = (size_t)cbB * M2 * sizeof(double2);
     pr->begin("fft4_cols", (5.0 * logM1 + 6.0) * M * (double)batch, st);
