@@ -652,12 +652,12 @@ void launch_accumulate(int n, int nq, const double *contrib, double *acc, int fi
 // per SM, in which case fewer items per CTA (halving) spread it over more SMs.
 // Each item's arithmetic is the same either way.
 int short_grid_cb(int cb, int nitems, int nq) {
-    static int sms = 0;
-    if (sms <= 0) {
-        int dev = 0;
+    static const int sms = [] {   // thread-safe one-time query of the SM count
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
-    }
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        return v;
+    }();
     while (cb > 1 && (long)((nitems + cb - 1) / cb) * nq < 2L * sms) cb >>= 1;
     return cb;
 }
