@@ -487,7 +487,7 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
     or "linear" (the O(n k) linear engine, one warp per node, k <= 256);
     quadrature is "erfc" (the reference's erfc-trapezoid rule) or "tanh_sinh";
     chunk_streams spreads a tree plan's node chunks over that many streams
-    (0 = default: 4 from n = 12000, else 2; 1 = one stream; at most 4; same
+    (0 = default: 4 from n = 6000, else 2; 1 = one stream; at most 4; same
     results)."""
     engines = {"auto": 0, "tree": 1, "linear": 2}
     rules = {"erfc": 0, "tanh_sinh": 1}

@@ -781,10 +781,11 @@ Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std:
     else plan_tree_layout(p, qc, A + o_tree);
     p->d_counter = (unsigned *)(A + o_cnt);
     // after the arena's pointers: the views offset them
-    // default: four pieces from n = 12000 (measured on GB300: n = 16384 4.31 ->
-    // 4.16 ms, n = 65536 17.13 -> 16.89 ms against two), two below (n = 4096,
-    // k = 40: 0.58 ms with two, 0.66 with four)
-    const int want = g_config.chunk_streams > 0 ? g_config.chunk_streams : n >= 12000 ? 4 : 2;
+    // default: four pieces from n = 6000, two below (measured on GB300 with
+    // one / two / four pieces: n = 16384 4.92 / 4.01 / 3.75 ms; n = 8000,
+    // k = 1200 2.51 / 2.02 / 1.92 ms; n = 4096, k = 40 0.62 / 0.55 / 0.57 ms;
+    // n = 2000 0.59 / 0.52 / 0.59 ms)
+    const int want = g_config.chunk_streams > 0 ? g_config.chunk_streams : n >= 6000 ? 4 : 2;
     const int np = std::min({want, kMaxChunkParts, qc});
     if (!p->small && !p->linear && p->Lf == 0 && np >= 2 && !p->opts.verbose) {
         for (int i = 0; i < np; ++i) p->part_off[i] = i * (qc / np);

@@ -48,7 +48,7 @@ int icm_last_status(void);
  *                     accurate for widely spread stacks)
  *   chunk_streams     streams a tree plan's node chunks are spread over
  *                     (pieces of consecutive nodes, same results); 0 = the
- *                     default (4 from n = 12000, else 2), 1 = one stream,
+ *                     default (4 from n = 6000, else 2), 1 = one stream,
  *                     at most 4                                           */
 typedef struct {
     int block_size;
