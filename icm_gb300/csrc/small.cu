@@ -187,13 +187,15 @@ size_t small_smem_bytes(const Plan *p) {
 // k-dependent size, as in the reference (gpu_exec.cu:26-60).  The limits are
 // the measured crossovers on GB300 (device time of one solve, Q = 256, both
 // paths): k <= 16 up to n = 1536, k <= 64 up to 768, k <= 128 up to 640,
-// k <= 256 up to 384, else up to 288.  g_config.small_max_n overrides them
-// (-1 disables the path).
+// k <= 256 up to 512, else up to 352 (n = 500, k = 200: 0.225 against
+// 0.249 ms; n = 320, k = 320: 0.193 against 0.213 ms; above the limits the
+// level path wins, e.g. n = 900, k = 120: 0.368 against 0.319 ms).
+// g_config.small_max_n overrides them (-1 disables the path).
 bool plan_small_ok(const Plan *p) {
     if (p->coeff_only || g_config.small_max_n < 0) return false;
     int lim;
     if (g_config.small_max_n > 0) lim = g_config.small_max_n;
-    else lim = p->k <= 16 ? kSmallMaxN : p->k <= 64 ? 768 : p->k <= 128 ? 640 : p->k <= 256 ? 384 : 288;
+    else lim = p->k <= 16 ? kSmallMaxN : p->k <= 64 ? 768 : p->k <= 128 ? 640 : p->k <= 256 ? 512 : 352;
     if (p->n > lim || p->L > kSmallMaxLevels) return false;
     return small_smem_bytes(p) <= kSmallMaxSmem;
 }

@@ -32,7 +32,8 @@ def _paths(gpu_icm, S, P, Q=256, **kw):
 
 
 @pytest.mark.parametrize("n,k", [(1, 1), (2, 1), (2, 2), (3, 3), (9, 3), (10, 10), (45, 9), (64, 64), (100, 15),
-                                 (128, 128), (200, 40), (256, 64), (500, 30), (512, 64)])
+                                 (128, 128), (200, 40), (256, 64), (500, 30), (512, 64), (500, 200), (512, 256),
+                                 (352, 300), (336, 336)])
 def test_small_path_matches_level_path(gpu_icm, oracle, n, k):
     rng = np.random.default_rng(n * 1000 + k)
     S = 1e4 * np.exp(1.5 * rng.standard_normal(n))
