@@ -229,3 +229,28 @@ def test_player_order_concurrent_and_forked(built_lib):
         os._exit(0 if ok else 1)
     _, status = os.waitpid(pid, 0)
     assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0
+
+
+def test_player_order_many_threads(built_lib):
+    """Sixteen host threads sorting fields of every size class at once (the
+    worker pool serves one of them, the others spawn their own threads, small
+    fields sort on the caller): every order is right."""
+    import threading
+    import icm_gb300 as icm
+    rng = np.random.default_rng(11)
+    cases = [10.0 ** rng.uniform(0, 9, n) for n in (100, 5000, 17000, 40000, 70000, 130000)]
+    refs = [np.lexsort((np.arange(len(S)), -S)) for S in cases]
+    bad = []
+
+    def worker(w):
+        for r in range(6):
+            j = (w + r) % len(cases)
+            if not np.array_equal(icm.player_order(cases[j]), refs[j]):
+                bad.append((w, j))
+
+    th = [threading.Thread(target=worker, args=(w,)) for w in range(16)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not bad
