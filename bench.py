@@ -134,6 +134,8 @@ def parse():
     ap.add_argument("--batch-count", type=int, default=4096, help="tournaments in the batched leg")
     ap.add_argument("--no-vjp", action="store_true", help="skip the VJP leg")
     ap.add_argument("--no-gpu-scale", action="store_true", help="skip the n = 2^20 leg")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="reference arm: skip the reference's own GPU library")
     ap.add_argument("--case", default="",
                     help="run one small workload once, untimed, and exit (for profilers): "
                          "vjp_batch:T (T tournaments of the VJP leg's batch), batch:T[:Q] (T of the batched leg), "
@@ -210,59 +212,174 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(ss)}
 
 
-def cpu_port_time(S, P, threads, q_sample):
-    """Seconds per full Q=256 solve of the C port, from a q_sample-node run."""
-    from oracle.oracle import Oracle, build
+def _median(xs):
+    return float(np.median(np.asarray(xs, dtype=np.float64)))
+
+
+def detail(name, obj):
+    """One detail record on its own stdout line, ahead of the JSON result
+    line (which stays compact); '#'-prefixed so that only the result line
+    parses as JSON."""
+    print(f"# {name}: " + json.dumps(obj), flush=True)
+
+
+def cpu_reference(S, P, steps=1, warmup=1, budget_s=30.0, single_thread=True):
+    """The reference's own CPU icm_equity (oracle/_ref, built from its
+    unmodified src/cpu/icm.c) on this host: the OpenMP build on all cores,
+    `steps` timed solves after `warmup`, median as the reference's bench.c
+    (bench/bench.c:57-59) reports; plus the serial build on one core.  A solve
+    is all 256 nodes while one takes at most budget_s, else a sample of
+    q nodes (the per-node tree work does not depend on the node), scaled by
+    256 / q.  Falls back to the C port (kind "port") where the reference
+    library was not built."""
+    from oracle.oracle import Oracle, ReferenceLib, build
     build()
-    orc = Oracle()
-    orc.equity(S[:4096], P[:512], Q=4, B=8, fft_min_deg=64, threads=threads)   # warm caches
+    cores = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(cores)
+    if ReferenceLib.available(openmp=True):
+        kind = "reference"
+        ref = ReferenceLib(openmp=True)
+
+        def solve(q):
+            t0 = time.perf_counter()
+            ref.equity(S, P, Q=q)
+            return time.perf_counter() - t0
+    else:
+        kind = "port"
+        orc = Oracle()
+
+        def solve(q):
+            t0 = time.perf_counter()
+            orc.equity(S, P, Q=q, B=8, fft_min_deg=64, threads=cores)
+            return time.perf_counter() - t0
+    q = 256
+    t = solve(q)                                  # first warm-up decides the sample
+    first_s = t
+    if t > budget_s:
+        q = max(8, 1 << int(np.floor(np.log2(256 * budget_s / t))))
+    for _ in range(max(0, warmup - 1)):
+        solve(q)
+    times = [solve(q) * 256.0 / q for _ in range(max(1, steps))]
+    out = {"value": 1e3 * _median(times), "unit": UNIT, "cores": cores, "kind": kind,
+           "sample": (f"median of {len(times)} full solves (256 nodes, n={len(S)}, k={len(P)}) "
+                      f"on {cores} threads (OpenMP build)" if q == 256 else
+                      f"median of {len(times)} runs of {q} of 256 quadrature nodes (full n={len(S)}, "
+                      f"k={len(P)} tree each) on {cores} threads (OpenMP build), scaled by 256/{q}"),
+           "steps": len(times), "first_solve_s": round(first_s, 3)}
+    if single_thread and kind == "reference" and ReferenceLib.available(openmp=False):
+        # serial build: two node samples, extrapolated linearly to 256 nodes
+        # (the difference gives the per-node cost, free of the per-call set-up)
+        ser = ReferenceLib(openmp=False)
+        ser.equity(S[:2048], P[:min(len(P), 2048)], Q=4)
+        q1 = 8 if len(S) >= 32768 else 32
+        ts1 = []
+        for q in (q1, 2 * q1):
+            t0 = time.perf_counter()
+            ser.equity(S, P, Q=q)
+            ts1.append(time.perf_counter() - t0)
+        per_node = max(ts1[1] - ts1[0], 0.0) / q1
+        est = ts1[0] + per_node * (256 - q1)
+        out["single_thread"] = {"value": 1e3 * est, "unit": UNIT, "cores": 1,
+                                "sample": f"serial build, {q1}- and {2 * q1}-node runs ({ts1[0]:.2f} s, "
+                                          f"{ts1[1]:.2f} s) extrapolated to 256 nodes"}
+    return out
+
+
+def reference_gpu_leg(W, cpu_equity=None, batch_sample=16):
+    """The reference's own GPU library (oracle/_ref/libicm_ref_gpu.so: its
+    src/gpu/*.cu, cuFFT tier, B200 calibration data) on this GPU: ms per
+    solve through icm_gpu_equity_with_plan (median of the library's own
+    total_ns, host wall time including its synchronisation, as its
+    tools/heatmap_gpu.cu reports the published figures; plan created once, the
+    reference benchmarks' options) for
+    the drop-in workload and for the inputs of its published B200 timings,
+    one-shot icm_gpu_equity, and the plain loop of one-shot calls over a
+    1-in-`batch_sample` sample of the batched workload, scaled to the whole
+    batch."""
+    from oracle.oracle import ReferenceGpu, build
+    try:
+        build(gpu=True)
+    except Exception as e:   # noqa: BLE001 -- report, do not fail the arm
+        return {"unavailable": f"reference GPU library did not build: {e}"}
+    if not ReferenceGpu.available():
+        return {"unavailable": "reference GPU sources not present on this host"}
+    ref = ReferenceGpu(0)
+    out = {"library": "reference src/gpu/*.cu (cuFFT tier; cuFFTDx/MathDx absent), devices/b200 data, sm_103a"}
+
+    def with_plan(S, P, reps):
+        t0 = time.perf_counter()
+        plan = ref.plan(S, len(P))
+        create = time.perf_counter() - t0
+        E, _ = ref.equity_with_plan(plan, len(S), P)
+        ts, wall = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            E, ns = ref.equity_with_plan(plan, len(S), P)
+            wall.append(time.perf_counter() - t0)
+            ts.append(ns * 1e-9)
+        ref.destroy(plan)
+        return E, {"ms": 1e3 * _median(ts), "wall_ms": 1e3 * _median(wall), "runs": reps,
+                   "plan_create_ms": 1e3 * create}
+
+    S, P, _ = W.dropin()
+    E, rec = with_plan(S, P, 3)
+    if cpu_equity is not None:
+        rec["max_rel_diff_vs_reference_cpu"] = float(np.max(np.abs(E - cpu_equity) /
+                                                           np.maximum(np.abs(cpu_equity), 1e-300)))
     t0 = time.perf_counter()
-    orc.equity(S, P, Q=q_sample, B=8, fft_min_deg=64, threads=threads)
+    ref.equity(S, P)
+    rec["one_shot_ms"] = 1e3 * (time.perf_counter() - t0)
+    out["dropin_65536"] = rec
+    S, P = W.b200_heatmap(65536)
+    out["b200_inputs_65536"] = with_plan(S, P, 3)[1]
+    out["b200_inputs_65536"]["published_b200_ms"] = B200_PUBLISHED_MS
+    if out["dropin_65536"]["ms"] < 2000.0:
+        S, P = W.b200_heatmap(1 << 20)
+        out["b200_inputs_1048576"] = with_plan(S, P, 1)[1]
+        out["b200_inputs_1048576"]["published_b200_ms"] = 507.90
+    ts = W.batched()
+    sample = ts[::batch_sample]
+    for S, P in sample[:4]:
+        ref.equity(S, P)
+    t0 = time.perf_counter()
+    for S, P in sample:
+        ref.equity(S, P)
     dt = time.perf_counter() - t0
-    return dt * 256.0 / q_sample
+    out["batch_loop"] = {"tournaments_timed": len(sample), "of": len(ts), "sample_s": dt,
+                         "ms_per_batch_est": 1e3 * dt * len(ts) / len(sample),
+                         "path": f"one icm_gpu_equity call per tournament, every {batch_sample}th tournament "
+                                 f"of the batched workload, time scaled by {len(ts)}/{len(sample)}"}
+    return out
 
 
 def run_reference(args):
-    """The reference's own CPU implementation, all host threads."""
+    """The reference's own CPU implementation (all host cores; its serial
+    build on one core beside it) on the drop-in workload, and its own GPU
+    library on this GPU beside that."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
     from icm_gb300 import workloads as W
     S, P, _ = W.dropin(n=args.n)
-    threads = os.cpu_count() or 1
-    # a full 256-node solve per step when it fits the time box (it does at
-    # n = 65536: seconds on the host cores); a node sample above that
-    q_sample = 256 if args.n <= 65536 else 2 * threads
-    kind, fn = "port", None
-    try:
-        from oracle.oracle import ReferenceLib
-        if ReferenceLib.available(openmp=True):
-            os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-            ref = ReferenceLib(openmp=True)
-            kind = "reference"
-
-            def fn():
-                t0 = time.perf_counter()
-                ref.equity(S, P, Q=q_sample)
-                return (time.perf_counter() - t0) * 256.0 / q_sample
-    except OSError:
-        fn = None
-    if fn is None:
-        def fn():
-            return cpu_port_time(S, P, threads, q_sample)
-    for _ in range(max(args.warmup, 0)):
-        fn()
-    times = [fn() for _ in range(args.steps)]
-    ms = 1e3 * float(np.mean(times))
-    sample = (f"one full solve per step (all 256 nodes, n=k={args.n})" if q_sample == 256 else
-              f"{q_sample} of the 256 quadrature nodes per step (full n=k={args.n} tree each), "
-              f"time scaled by 256/{q_sample}")
+    cpu = cpu_reference(S, P, steps=args.steps, warmup=max(args.warmup, 1))
+    ms = cpu["value"]
+    gpu = None
+    if not args.no_reference_gpu and args.n == 65536:
+        cpu_E = None
+        try:
+            from oracle.oracle import ReferenceLib
+            if cpu["kind"] == "reference":
+                cpu_E = ReferenceLib(openmp=True).equity(S, P)
+        except OSError:
+            cpu_E = None
+        gpu = reference_gpu_leg(W, cpu_E)
     line = {"metric": METRIC, "value": ms, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "steps": cpu["steps"], "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded splitmix64)",
             "config": {"workload": WORKLOAD, "n": args.n, "k": args.n, "Q": 256},
-            "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
-            "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "cpu_baseline": cpu,
+            "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_gpu": gpu}
     print(json.dumps(line), flush=True)
 
 
@@ -354,6 +471,9 @@ def main():
             sub_ms.append((t2 - t1) * 1e3)
             full_ms.append((t3 - t2) * 1e3)
 
+    subset = {"targets": int(len(T)), "ms": _r(_median(sub_ms)), "full_ms": _r(_median(full_ms)),
+              "path": "icm_gpu_equity_subset vs icm_gpu_equity, one-shot"}
+    b200 = b200_inputs_leg(icm, W, 5)
     batched = (None if args.no_batched else
                batched_leg(icm, W, max(2, args.steps // 3), args.batch_count, fp64_peak_gflops / 1e3))
     vjp = None if args.no_vjp else vjp_leg(icm, W, 3, fp64_peak_gflops / 1e3)
@@ -396,40 +516,104 @@ def main():
     total_flops = sum(r["flops"] for r in kst) / args.steps
     cpu = None
     if not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        q_sample = 256 if n <= 65536 else 2 * threads
-        secs = cpu_port_time(S, P, threads, q_sample)
-        cpu = {"value": secs * 1e3, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": (f"one full solve (256 nodes, n=k={n}) on {threads} threads" if q_sample == 256 else
-                          f"{q_sample} of 256 quadrature nodes (full n=k={n} tree each) on {threads} threads, "
-                          f"scaled by 256/{q_sample}")}
+        cpu = cpu_reference(S, P, steps=1, warmup=1)
+        cpu.pop("steps", None)
+    kernels = [{**r, "ms_per_solve": r["ms"] / args.steps} for r in kst]
+    detail("kernels (drop-in solve, profiled pass)", kernels)
+    canon = canonical_rates(n, k, ms_per_solve, fp64_peak_gflops / 1e3)
     metric = METRIC if n == 65536 else f"ms @n=k={n} Q=256"
+    b200_ms = b200["n65536"]["device_ms"] if b200 else None
     line = {
         "metric": metric, "value": ms_per_solve, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": total_dev / args.steps, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": ms_per_solve / B200_PUBLISHED_MS, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": (b200_ms / B200_PUBLISHED_MS) if b200_ms else None, "dtype": "f64",
         "data": "synthetic (seeded splitmix64; the reference publishes no dataset)",
-        "config": {"workload": WORKLOAD, "n": n, "k": k, "Q": 256, "B": summ["B"], "levels": summ["n_levels"],
-                   "q_chunk": summ["q_batch"], "device_bytes": summ["planned_peak_vram_bytes"],
+        "config": {"workload": WORKLOAD, "n": n, "k": k, "Q": 256, "B": summ["B"],
                    "l2": "inputs larger than L2: the plan's working set exceeds 129 MB",
                    "parallelism": f"replicas x{world}",
-                   "vs_baseline_note": "B200 reference, uniform [1,100] stacks (RESULTS.md:551); run time does not depend on stack values"},
+                   "vs_baseline_note": "this engine on the inputs of the published B200 figure (stacks 1+99U, "
+                                       "payout n-m, n=k=65536; RESULTS.md:551, tools/heatmap_gpu.cu:15-25) "
+                                       "over that figure, 20.26 ms"},
         "e2e": {"value": e2e_mean * 1e3, "unit": UNIT, "h2d_bytes_per_step": 8 * (n + k), "d2h_bytes_per_step": 8 * n,
                 "path": "icm_equity (C ABI, host buffers)"},
         "gpu_launches": launches,
-        "subset": {"targets": int(len(T)), "ms": float(np.median(sub_ms)), "full_ms": float(np.median(full_ms)),
-                   "path": "icm_gpu_equity_subset vs icm_gpu_equity, plan set-up included"},
-        "batched": batched,
-        "vjp": vjp,
-        "gpu_scale": gscale,
         "roofline": roofline,
+        "cpu_baseline": cpu, "clocks": clocks,
         "algorithmic_tflops_per_s": total_flops / (ms_per_solve * 1e-3) / 1e12,
-        "canonical": canonical_rates(n, k, ms_per_solve, fp64_peak_gflops / 1e3),
         "fp64_peak_tflops_measured": fp64_peak_gflops / 1e3,
-        "kernels": [{**r, "ms_per_solve": r["ms"] / args.steps} for r in kst],
-        "cpu_baseline": cpu, "clocks": clocks, "wall_s": wall,
+        "canonical": {"W_ref_flop": canon["W_ref_flop"], "achieved_fp64": canon["achieved_fp64"]} if canon else None,
+        "b200_inputs": b200,
+        "subset": subset,
+        "batched": compact_batched(batched),
+        "vjp": compact_vjp(vjp),
+        "gpu_scale": compact_scale(gscale),
     }
     print(json.dumps(line), flush=True)
+
+
+def _r(x, d=4):
+    return None if x is None else float(f"{x:.{d}g}")
+
+
+def compact_batched(b):
+    """The batched leg's headline figures (the full record is a detail line)."""
+    if not b:
+        return None
+    detail("batched", b)
+    return {"tourn_per_s": _r(b["value"]), "ms_per_batch": _r(b["ms_per_batch"]),
+            "e2e_tourn_per_s": _r(b["e2e"]["value"]), "loop_ms": _r(b["plain_loop"]["ms_per_batch"]),
+            "speedup_vs_loop": {"device": _r(b["speedup_vs_loop"]["device"]), "e2e": _r(b["speedup_vs_loop"]["e2e"])},
+            "max_rel_err_vs_loop": _r(b["max_rel_err_vs_loop"], 3),
+            "achieved_fp64_canonical": _r((b.get("canonical") or {}).get("achieved_fp64"))}
+
+
+def compact_vjp(v):
+    if not v:
+        return None
+    detail("vjp", v)
+    out = {}
+    for shape in ("linear", "quadratic"):
+        if shape in v:
+            out[shape] = {"ratio": _r(v[shape]["ratio"]), "vjp_ms": _r(v[shape]["vjp_ms"]),
+                          "fwd_ms": _r(v[shape]["fwd_ms"])}
+    if "batched_256" in v:
+        out["batched_256_device_ratio"] = _r(v["batched_256"]["device_ratio"])
+    return out
+
+
+def compact_scale(g):
+    if not g:
+        return None
+    detail("gpu_scale", g)
+    out = {}
+    for shape in ("linear", "geometric"):
+        if shape in g:
+            r = g[shape]
+            out[shape] = {"k": r["k"], "device_ms": _r(r["device_ms"]), "e2e_ms": _r(r["e2e_ms"])}
+            if "max_rel_err_vs_closed_form_64_players" in r:
+                out[shape]["rel_err_closed_form"] = _r(r["max_rel_err_vs_closed_form_64_players"], 3)
+    return out
+
+
+def b200_inputs_leg(icm, W, steps):
+    """This engine on the inputs of the reference's published B200 timings
+    (stacks 1 + 99 U, payout n - m; tools/heatmap_gpu.cu:15-25): device ms per
+    solve with the plan resident, at n = k = 65536 (published 20.26 ms,
+    RESULTS.md:551) and n = k = 2^20 (507.90 ms, RESULTS.md:553)."""
+    from icm_gb300._lib import lib
+    out = {}
+    for n, reps, pub in ((65536, steps, B200_PUBLISHED_MS), (1 << 20, 2, 507.90)):
+        S, P = W.b200_heatmap(n)
+        plan = icm.GpuPlan(S, n)
+        plan.equity(P)
+        dev = []
+        for _ in range(max(2, reps)):
+            plan.equity(P)
+            dev.append(lib().icm_gb300_plan_device_ms(plan._p))
+        plan.close()
+        out[f"n{n}"] = {"device_ms": _r(_median(dev)), "published_b200_ms": pub,
+                        "ratio_to_b200": _r(_median(dev) / pub)}
+    return out
 
 
 def batched_leg(icm, W, steps, count, fp64_tflops=None):

@@ -15,6 +15,8 @@ exponentials.  Shapes follow the five workloads the reference's scope lists:
                     k=min(n,ceil(0.15 n)), stacks 1e4*lognormal(0,1),
                     geometric payouts (0.8)
 * ``vjp``           n=16384, k=2000, stacks Gamma(2,5000), linear/quadratic payouts
+* ``b200_heatmap``  the inputs of the reference's published B200 timings:
+                    stacks 1 + 99 U(0,1), unnormalised payout n - m
 
 All payouts are normalised to sum 1 unless stated otherwise.
 """
@@ -126,3 +128,15 @@ def vjp(n: int = 16384, k: int = 2000, payout: str = "linear", seed: int = SEED 
     P = linear_payout(k) if payout == "linear" else quadratic_payout(k)
     cot = rng.normal(n)
     return S, P, cot
+
+
+def b200_heatmap(n: int = 65536, k: int | None = None, seed: int = SEED + 6):
+    """The inputs of the reference's published B200 timings
+    (tools/heatmap_gpu.cu:15-25): stacks 1 + 99 U(0,1), payout n - m
+    (unnormalised), m < k.  The reference draws U from the C library's rand()
+    seeded with 42 + n; here it is splitmix64 (same distribution; the tree's
+    work depends on the stacks only through their spread)."""
+    k = n if k is None else k
+    rng = SplitMix64(seed)
+    S = 1.0 + 99.0 * rng.uniform(n)
+    return S, (n - np.arange(k)).astype(np.float64)

@@ -10,17 +10,18 @@ import pytest
 from tests.conftest import GOLDEN, max_rel
 from tests.golden.webgen import all_cases
 from icm_gb300 import workloads as W
+from oracle.oracle import staged
 
 WEB = json.load(open(os.path.join(GOLDEN, "web_reference.json")))
 REFW = json.load(open(os.path.join(GOLDEN, "ref_workloads.json")))
-REF_JSON = "/root/reference/web/verify/reference.json"
+REF_JSON = staged("web/verify/reference.json") or ""
 
 
 def _web_inputs():
     return {name: (n, k, Q, S, P) for name, n, k, Q, S, P in all_cases()}
 
 
-@pytest.mark.skipif(not os.path.isfile(REF_JSON), reason="reference tree not mounted")
+@pytest.mark.skipif(not os.path.isfile(REF_JSON), reason="reference sources not staged")
 def test_webgen_rebuilds_reference_inputs_bit_for_bit():
     ref = json.load(open(REF_JSON))
     for (name, n, k, Q, S, P), c in zip(all_cases(), ref):
