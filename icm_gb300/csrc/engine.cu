@@ -156,7 +156,7 @@ int select_block_size(int n, int k) {
     return B;
 }
 
-static int select_fft_min(int n, int k) {
+int select_fft_min(int n, int k) {
     if (g_config.fft_min_degree > 0) return g_config.fft_min_degree;
     int tB = 0, tF = 0;
     tune_lookup(n, k, &tB, &tF);

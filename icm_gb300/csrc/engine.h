@@ -210,6 +210,7 @@ int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &er
 int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats,
              std::string &err, int q_begin = 0, int q_end = -1);
 int select_block_size(int n, int k);
+int select_fft_min(int n, int k);   // schoolbook/FFT crossover degree (config, tuner table, built-in)
 
 // quadrature nodes (host), restating the reference's erfc-trapezoid rule
 void make_nodes(int Q, double Smax, std::vector<double> &logv, std::vector<double> &w);

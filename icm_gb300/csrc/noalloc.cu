@@ -1,34 +1,43 @@
 // noalloc.cu -- icm_gpu_equity_noalloc: the equity solve for callers that
 // cannot allocate device memory.
 //
-// Who needs it: code that runs while a CUDA stream is being captured into a
-// graph (cudaMalloc is not allowed there), real-time or embedded hosts that
-// forbid allocation after start-up, and processes whose device memory is
-// owned by another allocator (a framework's caching pool) where a stray
-// cudaMalloc would break the pool's budget or fragment it.  For them this
-// entry point computes the same equities as icm_equity, for tournaments of
-// up to kNoallocMaxN players, using only memory that already exists: the
-// caller's host arrays and one file-scope device array, g_noalloc_scratch,
-// of kNoallocBytes.  That array is part of the library image, so every GPU
-// that loads libicm_gb300.so holds it until the process exits.
+// Who needs it: hosts that forbid device allocation after start-up (real-time
+// or embedded services that size every buffer once, so that a solve can never
+// fail or stall on an allocator), and processes whose device memory belongs to
+// another allocator (a framework's caching pool that has reserved the GPU's
+// memory, where a cudaMalloc of our own would either fail or break the pool's
+// budget and fragment it).  For them this entry point computes the same
+// equities as icm_equity, for tournaments of up to kNoallocMaxN players, using
+// only memory that already exists: the caller's host arrays and one
+// file-scope device array, g_noalloc_scratch, of kNoallocBytes.  That array is
+// part of the library image, so every GPU that loads libicm_gb300.so holds it
+// until the process exits.
 //
 // The call makes no cudaMalloc, cudaFree, stream or event creation, and no
 // allocating library call.  Everything it needs on the device (sorted
 // stacks, quadrature nodes, twiddles, tree levels, FFT work buffers,
 // per-node partials) is carved from the scratch array; the quadrature nodes
-// are processed in chunks sized so the carve fits.  Work runs on the legacy
-// default stream and the call returns after the result is on the host.
+// are processed in chunks sized so the carve fits.  It runs on the library's
+// device (the one icm_gpu_init chose; device 0 when nothing was initialised),
+// restores the caller's current device before returning, puts its copies and
+// launches on the legacy default stream, and returns after the result is on
+// the host.  Its tree uses coefficient-FFT levels throughout (no spectral
+// levels, which need per-plan buffers), with the block size and FFT crossover
+// the allocating path picks, so its equities agree with icm_equity's to
+// rounding (about 1e-13 relative), not bit for bit.
 //
 // Set-up: the first call on a device, with that device current, resolves the
 // array's device address with cudaGetSymbolAddress (the host-side name of a
-// __device__ array is only a stand-in, not a device address) and caches it.
-// Make that first call before any stream capture begins.
+// __device__ array is only a stand-in, not a device address) and caches it,
+// once per device under a lock.  That first call should come before any stream
+// capture begins.
 //
 // Every call shares the one array and overwrites what the previous call left
-// there; calls that overlap on the GPU (two host threads, or two devices'
-// worth of work interleaved on one device) race and corrupt each other.
+// there (the accumulator is cleared by each call); calls that overlap on the
+// GPU (two host threads at once) race and corrupt each other.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -43,22 +52,26 @@ constexpr size_t kNoallocBytes = (size_t)32 << 20; // 32 MiB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
+static std::mutex g_noalloc_mu;        // guards the per-device address cache
 static char *g_noalloc_ptr[64] = {};   // device address per device, set up once
 
-static int noalloc_setup(std::string &err) {
+// The scratch array's device address on the current device (resolved once per
+// device, with that device current); nullptr with the reason in err.
+static char *noalloc_scratch(std::string &err) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return -1; }
-    if (dev < 0 || dev >= 64) { err = "device index out of range"; return -1; }
-    if (g_noalloc_ptr[dev]) return dev;
+    if (e != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return nullptr; }
+    if (dev < 0 || dev >= 64) { err = "device index out of range"; return nullptr; }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[dev]) return g_noalloc_ptr[dev];
     void *ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || !ptr) {
         err = std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e);
-        return -1;
+        return nullptr;
     }
     g_noalloc_ptr[dev] = (char *)ptr;
-    return dev;
+    return g_noalloc_ptr[dev];
 }
 
 static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -78,7 +91,7 @@ static int noalloc_plan(NoallocPlan &p, int n, int k, int nact, char *base, std:
     p.k = k;
     p.B = select_block_size(n, k);
     const int B = p.B;
-    const int fft_min = g_config.fft_min_degree > 0 ? g_config.fft_min_degree : 64;
+    const int fft_min = select_fft_min(n, k);   // the allocating path's crossover
     p.nblocks = (n + B - 1) / B;
     int Nt = 1;
     while (Nt < p.nblocks) Nt <<= 1;
@@ -165,10 +178,8 @@ namespace icmg {
 void api_set_error(const std::string &e);   // api.cpp: the text icm_gpu_last_error returns
 }
 
-// See icm_gb300.h.  Host arrays in and out; 0 on success, -1 on failure with
-// the reason in icm_gpu_last_error().
-extern "C" int icm_gpu_equity_noalloc(int n, const double *S, int Q, const double *payout, int k,
-                                      double *equity) {
+// The solve behind icm_gpu_equity_noalloc.
+static int noalloc_solve(int n, const double *S, int Q, const double *payout, int k, double *equity) {
     std::string err;
     auto fail = [&](const std::string &m) {
         api_set_error("icm_gpu_equity_noalloc: " + m);
@@ -184,8 +195,8 @@ extern "C" int icm_gpu_equity_noalloc(int n, const double *S, int Q, const doubl
         if (!(S[i] > 0.0) || !std::isfinite(S[i])) return fail("stacks must be finite and positive");
     if (g_device < 0 && icm_gpu_init(0) != 1) return fail("no usable CUDA device");
     if (cudaSetDevice(g_device) != cudaSuccess) return fail("cudaSetDevice failed");
-    const int dev = noalloc_setup(err);
-    if (dev < 0) return fail(err);
+    char *scratch = noalloc_scratch(err);
+    if (!scratch) return fail(err);
 
     // host-side preparation: sort (descending, ties by index), nodes, twiddles
     std::vector<int> perm(n);
@@ -203,7 +214,7 @@ extern "C" int icm_gpu_equity_noalloc(int n, const double *S, int Q, const doubl
     }
     const int nact = (int)(node.size() / 3);
     NoallocPlan p;
-    if (noalloc_plan(p, n, k, nact, g_noalloc_ptr[dev], err) != 0) return fail(err);
+    if (noalloc_plan(p, n, k, nact, scratch, err) != 0) return fail(err);
     std::vector<unsigned char> tw;
     fill_twiddles(p.logTW, tw);
 
@@ -263,4 +274,25 @@ extern "C" int icm_gpu_equity_noalloc(int n, const double *S, int Q, const doubl
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(std::string("execution: ") + cudaGetErrorString(e));
     return 0;
+}
+
+// See icm_gb300.h.  Host arrays in and out; 0 on success, -1 on failure with
+// the reason in icm_gpu_last_error().  The caller's current device is restored
+// before returning; a C++ exception (a host allocation that fails) becomes -1.
+extern "C" int icm_gpu_equity_noalloc(int n, const double *S, int Q, const double *payout, int k,
+                                      double *equity) {
+    int caller_dev = -1;
+    if (cudaGetDevice(&caller_dev) != cudaSuccess) caller_dev = -1;
+    int rc = -1;
+    try {
+        rc = noalloc_solve(n, S, Q, payout, k, equity);
+    } catch (const std::exception &e) {
+        api_set_error(std::string("icm_gpu_equity_noalloc: ") + e.what());
+        rc = -1;
+    } catch (...) {
+        api_set_error("icm_gpu_equity_noalloc: unknown error");
+        rc = -1;
+    }
+    if (caller_dev >= 0) cudaSetDevice(caller_dev);
+    return rc;
 }

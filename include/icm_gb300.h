@@ -238,18 +238,22 @@ double icm_gb300_plan_device_ms(const IcmGpuPlan *plan);
  * Same inputs, outputs and result as icm_equity (host arrays S[n],
  * payout[k] in, equity[n] out), but the call allocates nothing: no
  * cudaMalloc/cudaFree, no stream or event creation, no allocating library
- * routine.  It is meant for code running under CUDA stream capture, hosts
- * that forbid allocation after start-up, and processes whose device memory
- * belongs to another allocator.  All device-side data lives in one static
- * scratch array of 32 MiB inside the library, held by every GPU that loads
- * the library until the process exits.
+ * routine.  It serves hosts that forbid device allocation after start-up
+ * (services that size every buffer once so that a solve cannot fail or stall
+ * on an allocator) and processes whose device memory belongs to another
+ * allocator (a framework's caching pool that has reserved the GPU).  All
+ * device-side data lives in one static scratch array of 32 MiB inside the
+ * library, held by every GPU that loads the library until the process exits.
  *
  * Limits: n <= 4096 players and Q <= 4096 nodes; larger requests return -1
  * with the reason in icm_gpu_last_error() (use icm_equity for them).
  * The first call on a device looks up the scratch array's device address
- * (cudaGetSymbolAddress) with that device current; make it before any stream
- * capture begins.  Calls share the scratch array: calls that overlap on the
- * GPU race.  Work runs on the legacy default stream; returns 0 / -1. */
+ * (cudaGetSymbolAddress) with that device current; that first call should come
+ * before any stream capture begins.  Calls share the scratch array: calls that
+ * overlap on the GPU race.  The solve runs on the library's device, restores
+ * the caller's current device, uses the legacy default stream and returns
+ * after the equities are on the host; returns 0 / -1.  Results agree with
+ * icm_equity's to rounding (coefficient-FFT tree levels throughout). */
 int icm_gpu_equity_noalloc(int n, const double *S, int Q, const double *payout, int k,
                            double *equity);
 

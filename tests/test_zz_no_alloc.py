@@ -1,6 +1,6 @@
 """icm_gpu_equity_noalloc: the entry point for callers that cannot allocate
-device memory (code under CUDA stream capture, allocation-free hosts,
-processes whose device memory belongs to another allocator).  Its device
+device memory (hosts that forbid device allocation after start-up, processes
+whose device memory belongs to another allocator's pool).  Its device
 data lives in the library's static scratch array, so each call overwrites
 the last; two calls in a row must both agree with icm_equity.
 
@@ -29,7 +29,7 @@ def _noalloc(L, S, P, Q=256):
     return rc, out
 
 
-@pytest.mark.parametrize("case", ["plain_small", "dropin_4096", "tiny"])
+@pytest.mark.parametrize("case", ["plain_small", "dropin_4096", "truncated_3000", "tiny"])
 def test_noalloc_matches_icm_equity_on_two_calls(gpu_icm, case):
     from icm_gb300._lib import lib
     L = lib()
@@ -37,6 +37,9 @@ def test_noalloc_matches_icm_equity_on_two_calls(gpu_icm, case):
         S, P = W.plain_small()
     elif case == "dropin_4096":
         S, P, _ = W.dropin(n=4096)
+    elif case == "truncated_3000":   # k < n: truncated (coefficient-FFT) levels above the crossover
+        rng = np.random.default_rng(30)
+        S, P = 1e4 * np.exp(rng.standard_normal(3000)), W.geometric_payout(450, 0.99)
     else:
         S, P = np.array([3.0, 1.0, 2.0]), np.array([0.7, 0.3])
     ref = gpu_icm.equity(S, P)
