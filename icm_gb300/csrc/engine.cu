@@ -156,6 +156,15 @@ int select_block_size(int n, int k) {
     return B;
 }
 
+// complex points per CTA of level l's one-CTA FFT launches: the
+// configuration's value, else the tuner table's for the level, else 4096
+int select_cta_points(int n, int k, int l) {
+    int v = g_config.cta_points;
+    if (v <= 0) v = tune_cta_points(n, k, l);
+    if (v != 1024 && v != 2048 && v != 8192) v = 4096;
+    return v;
+}
+
 int select_fft_min(int n, int k) {
     if (g_config.fft_min_degree > 0) return g_config.fft_min_degree;
     int tB = 0, tF = 0;
@@ -486,6 +495,7 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
             bool spec = p->spectral && can_fft && c.deg + 1 <= k;
             if (c.deg > kSpecMaxD) spec = spec && l - 1 >= 1 && p->lv[l - 1].kind == 2;
             v.kind = spec ? 2 : (can_fft ? 1 : 0);
+            v.cta_pts = select_cta_points(n, k, l);
             v.fft = (v.kind == 1) ? 1 : 0;
             if (v.fft) {
                 long need = std::max<long>(2L * c.plen - 2, (long)c.glen + c.plen - 1);

@@ -42,6 +42,10 @@ struct Level {
     // Level kind (as a parent level): 0 schoolbook, 1 FFT on coefficients,
     // 2 spectral (nodes carried as spectra; spectral.cu).
     int kind = 0;
+    // complex points per CTA of this level's one-CTA FFT launches (spectral
+    // build/propagate/init and g-spectrum steps of single plans): items per
+    // CTA = max(1, cta_pts / transform size); 0 = the default, 4096
+    int cta_pts = 0;
     // spectral representation of this level's nodes: spec2 = DFT_{2 deg} (deg+1
     // bins) and end coefficients, present when the parent level is spectral;
     // G = DFT_{deg}(g) (deg/2+1 bins), present when this level is spectral
@@ -230,6 +234,8 @@ int measure_hbm_gbps(double *out, std::string &err);
 
 // tuner table (tune.cpp)
 void tune_lookup(int n, int k, int *B, int *fft_min);
+int tune_cta_points(int n, int k, int level);   // the table's points per CTA at a level (0: none)
+int select_cta_points(int n, int k, int level);
 extern std::atomic<long> g_tune_generation;   // changes of the tuner table (tune.cpp)
 // built-in choices for GB300 where the caller's table has none (0: none)
 void tune_builtin(int n, int k, int *B, int *fft_min);

@@ -44,6 +44,13 @@ static inline int ilog2s(long v) {
     return l;
 }
 static inline int spec_cb(int M) { return M >= 4096 ? 1 : 4096 / M; }
+// items per CTA of a single plan's launch for a level with `pts` complex points
+// per CTA (0: 4096); never more points than spec_cb's largest CTA (8192)
+static inline int pts_cb(int pts, int M) {
+    if (pts <= 0) pts = 4096;
+    pts = std::min(pts, kSpecMaxM);
+    return M >= pts ? 1 : pts / M;
+}
 static inline size_t spec_smem(int M) { return (size_t)spec_cb(M) * M * sizeof(double2); }
 // build and propagate: the items' data plus one view and one index per item
 constexpr size_t kViewBytes = 96;
@@ -636,7 +643,7 @@ void launch_spec_init(const Level &v, int nq, const double2 *tw, int logTW, cuda
     SpecInitArgs A = spec_init_args(v, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
-    A.cb = short_grid_cb(A.cb, A.nreal, nq);
+    A.cb = short_grid_cb(pts_cb(v.cta_pts, 1 << A.logd), A.nreal, nq);
     A.nbx = (A.nreal + A.cb - 1) / A.cb;
     sm = (size_t)A.cb * (1 << A.logd) * sizeof(double2);
     pr->begin("spec_init", fq * nq, st);
@@ -651,7 +658,7 @@ void launch_spec_build(const Level &c, const Level &p, bool write_coeffs, int nq
     SpecBuildArgs A = spec_build_args(c, p, write_coeffs, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
-    A.cb = short_grid_cb(A.cb, p.nreal, nq);
+    A.cb = short_grid_cb(pts_cb(p.cta_pts, 1 << A.logD), p.nreal, nq);
     A.nbx = (p.nreal + A.cb - 1) / A.cb;
     sm = (size_t)A.cb * ((size_t)(1 << A.logD) * sizeof(double2) + kItemBytes);
     pr->begin("spec_build", fq * nq, st);
@@ -667,7 +674,7 @@ void launch_gspec_init(const double *g, size_t g_q, int gst, int glen, int nreal
     GspecArgs A = gspec_args(g, g_q, gst, glen, nreal, v, G, G_q, hot, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
-    A.cb = short_grid_cb(A.cb, A.nreal, nq);
+    A.cb = short_grid_cb(pts_cb(v.cta_pts, 1 << (A.logd - 1)), A.nreal, nq);
     A.nbx = (A.nreal + A.cb - 1) / A.cb;
     sm = (size_t)A.cb * (1 << (A.logd - 1)) * sizeof(double2);
     pr->begin("gspec_init", fq * nq, st);
@@ -683,7 +690,7 @@ void launch_spec_prop(const double2 *Gp, size_t Gp_q, const Level &c, const Leve
     SpecPropArgs A = spec_prop_args(Gp, Gp_q, c, p, children_spectral, hot_c, tw, logTW, &fq, &sm);
     A.z.zp = zp;
     A.z.q0 = zq0;
-    A.cb = short_grid_cb(A.cb, p.nreal, nq);
+    A.cb = short_grid_cb(pts_cb(p.cta_pts, 1 << A.logD), p.nreal, nq);
     A.nbx = (p.nreal + A.cb - 1) / A.cb;
     sm = (size_t)A.cb * ((size_t)(1 << A.logD) * sizeof(double2) + kItemBytes);
     pr->begin("spec_prop", fq * nq, st);

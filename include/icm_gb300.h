@@ -49,7 +49,11 @@ int icm_last_status(void);
  *   chunk_streams     streams a tree plan's node chunks are spread over
  *                     (pieces of consecutive nodes, same results); 0 = the
  *                     default (4 from n = 6000, else 2), 1 = one stream,
- *                     at most 4                                           */
+ *                     at most 4
+ *   cta_points        complex points per CTA of the one-CTA FFT steps of a
+ *                     single plan's spectral levels (1024, 2048, 4096 or
+ *                     8192; 0 = the tuner table's per-level choice, else
+ *                     4096); same results, only the CTA shape changes      */
 typedef struct {
     int block_size;
     int fft_min_degree;
@@ -62,6 +66,7 @@ typedef struct {
     int engine;
     int quadrature;
     int chunk_streams;
+    int cta_points;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created
