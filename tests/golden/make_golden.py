@@ -15,8 +15,16 @@ Writes:
                        full-size drop-in workload's 64 subset targets:
                        payout (k-j+1)^2 with k = n gives E = 2 V2 + 3 V1 - 2
                        (unnormalised), from oracle V1/V2.
+  vjp_fd_reference.json  directional derivatives of L = <cot, equity> taken
+                       by central finite differences of the reference's own
+                       icm_equity (oracle/_ref): along stacks S -> S (1 + h u)
+                       at h = 1e-6 and a Richardson pair h = 1e-4 / 5e-5, with
+                       u = 0 on stacks within 1% of the largest so that the
+                       quadrature nodes (which depend on max S) stay fixed;
+                       and along a payout
+                       direction v, where L is linear: <cot, icm_equity(S, v)>.
 
-Usage:  python tests/golden/make_golden.py [--skip-large]
+Usage:  python tests/golden/make_golden.py [--skip-large] [--only NAME]
 """
 from __future__ import annotations
 
@@ -123,13 +131,74 @@ def closed_form_fixture(orc: Oracle):
             "gen": "dropin()", "n": n, "targets": [int(t) for t in T], "equity": fl(exact)}
 
 
+# the VJP cases: (name, generator call, directions); stacks, payouts and the
+# cotangent come from icm_gb300.workloads, directions from splitmix64 normals
+VJP_CASES = [
+    ("vjp_16384_linear", "vjp(payout='linear')", 3),
+    ("vjp_16384_quadratic", "vjp(payout='quadratic')", 3),
+    ("dropin_2048_kn", "dropin(n=2048)", 3),
+]
+
+
+def vjp_inputs(gen: str, seed: int):
+    """(S, P, cot) of a VJP fixture case; the drop-in shape (k = n) gets a
+    splitmix64 N(0, 1) cotangent from `seed`."""
+    out = eval("W." + gen)   # noqa: S307 -- generator calls of this module's own table
+    if gen.startswith("vjp("):
+        return out
+    S, P, _ = out
+    return S, P, W.SplitMix64(seed).normal(len(S))
+
+
+def stack_direction(S, seed: int):
+    """A splitmix64 N(0, 1) direction that keeps max S (and with it the
+    quadrature nodes) fixed: stacks within 1% of the largest are not moved,
+    so no step changes which player sets the nodes."""
+    u = W.SplitMix64(seed).normal(len(S))
+    u[S > 0.99 * np.max(S)] = 0.0
+    return u
+
+
+def vjp_fd_fixture(ref: ReferenceLib):
+    cases = []
+    for name, gen, ndir in VJP_CASES:
+        t0 = time.time()
+        S, P, cot = vjp_inputs(gen, 9001)
+
+        def loss(x, pay=P):
+            return float(np.dot(cot, ref.equity(x, pay)))
+
+        dirs = []
+        for d in range(ndir):
+            seed = 7000 + d
+            u = stack_direction(S, seed)
+            fd = {}
+            for h in (1e-6, 1e-4, 5e-5):
+                fd[h] = (loss(S * (1.0 + h * u)) - loss(S * (1.0 - h * u))) / (2.0 * h)
+            rich = (4.0 * fd[5e-5] - fd[1e-4]) / 3.0
+            dirs.append({"seed": seed, "fd_1e-6": fd[1e-6], "fd_richardson": rich})
+        v = W.SplitMix64(8000).normal(len(P))
+        rec = {"name": name, "gen": gen, "cot_seed": 9001, "n": len(S), "k": len(P), "Q": 256,
+               "L": loss(S), "stack_directions": dirs,
+               "payout_direction": {"seed": 8000, "derivative": loss(S, v)}}
+        print(f"  {name}: n={len(S)} k={len(P)} {time.time() - t0:.1f}s", flush=True)
+        cases.append(rec)
+    return {"source": "central differences of the reference's src/cpu/icm.c icm_equity (oracle/_ref, OpenMP), "
+                      "Q = 256", "cases": cases}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-large", action="store_true")
+    ap.add_argument("--only", choices=["vjp_fd"], default=None, help="regenerate only this fixture")
     args = ap.parse_args()
     build()
     ref = ReferenceLib(openmp=True)
     orc = Oracle()
+    if args.only == "vjp_fd":
+        print("vjp_fd_reference.json")
+        json.dump(vjp_fd_fixture(ref), open(os.path.join(HERE, "vjp_fd_reference.json"), "w"), indent=1)
+        return
     print("web_reference.json")
     json.dump(web_fixture(), open(os.path.join(HERE, "web_reference.json"), "w"))
     print("ref_workloads.json")
@@ -137,6 +206,8 @@ def main():
     if not args.skip_large:
         print("closed_form.json")
         json.dump(closed_form_fixture(orc), open(os.path.join(HERE, "closed_form.json"), "w"))
+    print("vjp_fd_reference.json")
+    json.dump(vjp_fd_fixture(ref), open(os.path.join(HERE, "vjp_fd_reference.json"), "w"), indent=1)
 
 
 if __name__ == "__main__":

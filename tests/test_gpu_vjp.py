@@ -281,3 +281,36 @@ def test_vjp_multipass_levels(gpu_icm):
     assert np.abs(gS - ref).max() <= TOL_ANALYTIC * np.abs(ref).max()
     E = gpu_icm.equity(S, P)
     assert abs(gP @ P - cot @ E) <= 1e-12 * np.abs(cot * E).sum()
+
+
+# ---------------------------------------------------------------------------
+# against central differences of the reference itself (tests/golden/
+# vjp_fd_reference.json: the reference's own icm_equity, built from its
+# unmodified src/cpu/icm.c, differenced along stacks with max S fixed and
+# along a payout direction, where L is linear)
+def _fd_cases():
+    import json
+    import os
+    from tests.conftest import GOLDEN
+    return json.load(open(os.path.join(GOLDEN, "vjp_fd_reference.json")))["cases"]
+
+
+@pytest.mark.parametrize("case", _fd_cases(), ids=lambda c: c["name"])
+def test_vjp_against_reference_finite_differences(gpu_icm, case):
+    from tests.golden.make_golden import stack_direction, vjp_inputs
+    S, P, cot = vjp_inputs(case["gen"], case["cot_seed"])
+    assert len(S) == case["n"] and len(P) == case["k"]
+    gS, gP = gpu_icm.equity_vjp(S, P, cot, Q=case["Q"])
+    E = gpu_icm.equity(S, P, Q=case["Q"])
+    L = float(cot @ E)
+    floor = 1e-9 * float(np.abs(cot * E).sum())
+    assert abs(L - case["L"]) <= floor
+    for d in case["stack_directions"]:
+        u = stack_direction(S, d["seed"])
+        terms = gS * S * u
+        an, scale = float(terms.sum()), float(np.abs(terms).sum())
+        assert abs(d["fd_1e-6"] - an) <= TOL_FD * scale + floor, (d, an, scale)
+        assert abs(d["fd_richardson"] - an) <= TOL_FD_RICHARDSON * scale + floor, (d, an, scale)
+    v = W.SplitMix64(case["payout_direction"]["seed"]).normal(len(P))
+    pv = gP * v
+    assert abs(float(pv.sum()) - case["payout_direction"]["derivative"]) <= 1e-10 * float(np.abs(pv).sum())
