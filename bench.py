@@ -456,6 +456,15 @@ def main():
         L.icm_gb300_plan_kernel_stats(plan._p, i, nm, 64, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(fl))
         kst.append({"kernel": nm.value.decode(), "ms": ms.value, "launches": nl.value, "flops": fl.value})
     kst.sort(key=lambda r: -r["ms"])
+    # the drop-in workload's 64-target subset on the same resident plan
+    L.icm_gb300_plan_set_profiling(plan._p, 0)
+    plan.set_targets(T)
+    plan.equity(P)
+    sub_dev = []
+    for _ in range(max(3, args.steps // 2)):
+        plan.equity(P)
+        sub_dev.append(L.icm_gb300_plan_device_ms(plan._p))
+    plan.set_targets(None)
     plan.close()
 
     # the drop-in workload's subset query (64 targets) against the full query,
@@ -471,8 +480,11 @@ def main():
             sub_ms.append((t2 - t1) * 1e3)
             full_ms.append((t3 - t2) * 1e3)
 
-    subset = {"targets": int(len(T)), "ms": _r(_median(sub_ms)), "full_ms": _r(_median(full_ms)),
-              "path": "icm_gpu_equity_subset vs icm_gpu_equity, one-shot"}
+    subset = {"targets": int(len(T)), "device_ms": _r(_median(sub_dev)),
+              "device_ratio_to_full": _r(_median(sub_dev) / (float(np.sum(dev_ms)) / args.steps)),
+              "one_shot_ms": _r(_median(sub_ms)), "one_shot_full_ms": _r(_median(full_ms)),
+              "path": "resident plan with targets (icm_gb300_plan_set_targets) vs the full solve; "
+                      "one-shot icm_gpu_equity_subset vs icm_gpu_equity"}
     b200 = b200_inputs_leg(icm, W, 5)
     batched = (None if args.no_batched else
                batched_leg(icm, W, max(2, args.steps // 3), args.batch_count, fp64_peak_gflops / 1e3))

@@ -189,6 +189,18 @@ class GpuPlan:
             raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
         return (out, _stats_dict(st)) if return_stats else out
 
+    def set_targets(self, targets=None):
+        """Later equity() calls compute only these players' equities (others
+        0), pruning the propagate as equity_subset does; None or an empty
+        list returns the plan to full-field runs."""
+        if targets is None or len(targets) == 0:
+            rc = lib().icm_gb300_plan_set_targets(self._p, None, 0)
+        else:
+            t = _to_int_array(targets, "targets")
+            rc = lib().icm_gb300_plan_set_targets(self._p, t.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(t))
+        if rc != 0:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+
     def summary(self):
         s = IcmGpuPlanSummary()
         lib().icm_gpu_plan_summary(self._p, ctypes.byref(s))
@@ -416,8 +428,10 @@ class VjpPlan:
 
 def autotune(stacks, payouts, Q=256, runs=2):
     """Time every (block size, FFT crossover) candidate on these stacks and
-    payouts, record the fastest in the tuner table for their size class and
-    return (block_size, fft_min_degree, best_ms)."""
+    payouts, record the fastest in the tuner table for their size class, then
+    time each spectral level's alternatives (points per CTA, coefficients)
+    and record those faster by more than 1% (tuner_lookup_level); return
+    (block_size, fft_min_degree, best_ms)."""
     S = _to_double_array(stacks, "stacks")
     P = _to_double_array(payouts, "payouts")
     _check(len(S), len(P), Q)
@@ -454,6 +468,15 @@ def tuner_lookup(n, k):
     b, f = ctypes.c_int(), ctypes.c_int()
     if lib().icm_gb300_tuner_lookup(int(n), int(k), ctypes.byref(b), ctypes.byref(f)) == 1:
         return b.value, f.value
+    return None
+
+
+def tuner_lookup_level(n, k, level):
+    """(spectral, cta_points) the table holds for tree level `level` of
+    (n, k)'s class, or None."""
+    sp, pts = ctypes.c_int(), ctypes.c_int()
+    if lib().icm_gb300_tuner_lookup_level(int(n), int(k), int(level), ctypes.byref(sp), ctypes.byref(pts)) == 1:
+        return sp.value, pts.value
     return None
 
 

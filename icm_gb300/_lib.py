@@ -64,6 +64,8 @@ SIGNATURES = {
     "icm_gpu_plan_destroy": (None, [_vp]),
     "icm_gpu_plan_summary": (ctypes.c_int, [_vp, ctypes.POINTER(IcmGpuPlanSummary)]),
     "icm_gpu_equity_with_plan": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, ctypes.POINTER(IcmGpuRunStats)]),
+    "icm_gb300_plan_set_targets": (ctypes.c_int, [_vp, _ip, ctypes.c_int]),
+    "icm_gb300_node_work": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _ip]),
     "icm_gb300_plan_equity_nodes": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int, _dp,
                                                    ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gpu_equity": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, _dp,
@@ -102,6 +104,7 @@ SIGNATURES = {
     "icm_gb300_tuner_save": (ctypes.c_int, [ctypes.c_char_p]),
     "icm_gb300_tuner_clear": (None, []),
     "icm_gb300_tuner_lookup": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _ip, _ip]),
+    "icm_gb300_tuner_lookup_level": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _ip]),
     "icm_gb300_autotune": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int, _ip, _ip,
                                           _dp]),
     "icm_gb300_equity_adaptive": (ctypes.c_int, [ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,

@@ -335,6 +335,33 @@ int icm_gpu_plan_summary(const IcmGpuPlan *plan, IcmGpuPlanSummary *summary) {
     return 1;
 }
 
+int icm_gb300_plan_set_targets(IcmGpuPlan *plan, const int *targets, int n_targets) {
+    return guarded<int>("icm_gb300_plan_set_targets", -1, [&]() -> int {
+        Plan *p = reinterpret_cast<Plan *>(plan);
+        if (!p || n_targets < 0 || (n_targets > 0 && !targets)) {
+            set_error("icm_gb300_plan_set_targets: invalid arguments");
+            return -1;
+        }
+        if (n_targets == 0) {
+            p->subset = false;
+            return 0;
+        }
+        for (int t = 0; t < n_targets; ++t)
+            if (targets[t] < 0 || targets[t] >= p->n) {
+                set_error("icm_gb300_plan_set_targets: target " + std::to_string(targets[t]) + " outside [0, " +
+                          std::to_string(p->n) + ")");
+                return -1;
+            }
+        std::string err;
+        if (!ensure_device()) return -1;
+        if (plan_set_targets(p, targets, n_targets, err) != 0) {
+            set_error("icm_gb300_plan_set_targets: " + err);
+            return -1;
+        }
+        return 0;
+    });
+}
+
 int icm_gpu_equity_with_plan(IcmGpuPlan *plan, int Q, const double *payout, double *equity,
                              IcmGpuRunStats *stats) {
     return guarded<int>("icm_gpu_equity_with_plan", -1, [&]() -> int {
@@ -430,6 +457,23 @@ int icm_gb300_player_order(int n, const double *S, int *perm) {
     });
 }
 
+int icm_gb300_node_work(int n, const double *S, int Q, int *work) {
+    return guarded<int>("icm_gb300_node_work", -1, [&]() -> int {
+        if (n < 1 || !S || Q < 1 || !work) { set_error("icm_gb300_node_work: invalid arguments"); return -1; }
+        std::vector<double> Ss(S, S + n);
+        for (double v : Ss)
+            if (!(v > 0.0) || !std::isfinite(v)) {
+                set_error("icm_gb300_node_work: stacks must be finite and positive");
+                return -1;
+            }
+        std::sort(Ss.begin(), Ss.end(), [](double a, double b) { return a > b; });
+        std::vector<double> logv, w;
+        make_nodes(Q, Ss[0], logv, w);
+        for (int q = 0; q < Q; ++q) work[q] = (w[q] == 0.0) ? 0 : n - zero_prefix(Ss.data(), n, logv[q]);
+        return 0;
+    });
+}
+
 void icm_gb300_test_fail_allocation(int nth) { set_alloc_failure(nth); }
 
 int icm_gb300_check_geometry(int n, int k, int block_size, int fft_min_degree, int flags, char *why, int why_len) {
@@ -446,8 +490,12 @@ int icm_gb300_check_geometry(int n, int k, int block_size, int fft_min_degree, i
         g_config = saved;
         if (rc != 0) { set_error("icm_gb300_check_geometry: " + err); return -1; }
         rc = plan_check_geometry(&p, err) == 0 ? 0 : 1;
+        if (!rc) {   // the level kinds, bottom up: 0 schoolbook, 1 FFT on coefficients, 2 spectral
+            err = "kinds";
+            for (int l = 1; l < p.L; ++l) err += " " + std::to_string(p.lv[l].kind);
+        }
         if (why && why_len > 0) {
-            std::strncpy(why, rc ? err.c_str() : "", why_len - 1);
+            std::strncpy(why, err.c_str(), why_len - 1);
             why[why_len - 1] = 0;
         }
         return rc;
@@ -674,6 +722,13 @@ int icm_gb300_tuner_lookup(int n, int k, int *block_size, int *fft_min_degree) {
     if (!block_size || !fft_min_degree || n < 1 || k < 1) return -1;
     tune_lookup(n, k, block_size, fft_min_degree);
     return (*block_size > 0) ? 1 : 0;
+}
+
+int icm_gb300_tuner_lookup_level(int n, int k, int level, int *spectral, int *cta_points) {
+    if (!spectral || !cta_points || n < 1 || k < 1 || level < 0) return -1;
+    *spectral = 1;
+    *cta_points = 0;
+    return tune_level_lookup(n, k, level, spectral, cta_points);
 }
 
 int icm_gb300_autotune(int n, const double *S, int Q, const double *payout, int k, int runs, int *block_size,

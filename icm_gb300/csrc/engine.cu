@@ -494,6 +494,7 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
             // and a truncated parent never has a spectral level above it)
             bool spec = p->spectral && can_fft && c.deg + 1 <= k;
             if (c.deg > kSpecMaxD) spec = spec && l - 1 >= 1 && p->lv[l - 1].kind == 2;
+            if (spec && !tune_spectral_ok(n, k, l)) spec = false;   // the tuner table keeps it on coefficients
             v.kind = spec ? 2 : (can_fft ? 1 : 0);
             v.cta_pts = select_cta_points(n, k, l);
             v.fft = (v.kind == 1) ? 1 : 0;

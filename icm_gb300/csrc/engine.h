@@ -235,6 +235,10 @@ int measure_hbm_gbps(double *out, std::string &err);
 // tuner table (tune.cpp)
 void tune_lookup(int n, int k, int *B, int *fft_min);
 int tune_cta_points(int n, int k, int level);   // the table's points per CTA at a level (0: none)
+int tune_spectral_ok(int n, int k, int level);  // 0 where the table keeps a level on coefficients
+int tune_level_lookup(int n, int k, int level, int *spectral, int *pts);
+void tune_record_level(int n, int k, int level, int spectral, int pts, double ms);
+void tune_erase_level(int n, int k, int level);
 int select_cta_points(int n, int k, int level);
 extern std::atomic<long> g_tune_generation;   // changes of the tuner table (tune.cpp)
 // built-in choices for GB300 where the caller's table has none (0: none)

@@ -84,7 +84,9 @@ int icm_gb300_player_order(int n, const double *S, int *perm);
  * rely on (host only: FFT sizes cover every product and correlation without
  * wrap, spectral levels sit over untruncated children, truncation lengths
  * and strides).  flags: 1 = the VJP's coefficient-only geometry.  Returns 0
- * when they hold, 1 with the first violation in why, -1 for bad arguments. */
+ * when they hold (why: "kinds" and each parent level's kind from level 1 up,
+ * 0 schoolbook, 1 FFT on coefficients, 2 spectral), 1 with the first
+ * violation in why, -1 for bad arguments. */
 int icm_gb300_check_geometry(int n, int k, int block_size, int fft_min_degree, int flags,
                              char *why, int why_len);
 
@@ -175,24 +177,43 @@ IcmGb300Batch *icm_gb300_vjp_batch_create(int T, const int *n, const int *k, con
 int icm_gb300_vjp_batch_run(IcmGb300Batch *batch, int Q, const double *payout, const double *cot,
                             double *grad_S, double *grad_payout, int flags, IcmGpuRunStats *stats);
 
-/* Tuner table (the analogue of the reference's FFTW wisdom; icm_init(path)
- * loads it too).  Entries map a size class -- ceil(log2 n) and a k/n bucket
- * (<= 1/64, <= 1/8, <= 1/2, > 1/2) -- to a leaf block size and the child
- * degree where tree levels switch from schoolbook to FFT products; plans of
- * that class use them unless icm_gb300_set_config fixes the values.
+/* Tuner table (the analogue of the reference's FFTW wisdom, reference
+ * src/cpu/icm.c:184-192; icm_init(path) loads it too).  Entries map a size
+ * class -- ceil(log2 n) and a k/n bucket (<= 1/64, <= 1/8, <= 1/2, > 1/2) --
+ * to a leaf block size and the child degree where tree levels switch from
+ * schoolbook to FFT products, and per tree level (the counterpart of the
+ * reference planner's per-level tier choice, src/gpu/gpu_plan.cu:51-329)
+ * whether an untruncated FFT level is carried in the frequency domain
+ * (spectral = 1) or on coefficients (0) and the complex points per CTA of its
+ * one-CTA FFT launches (0 = 4096); plans of that class use them unless
+ * icm_gb300_set_config fixes the values.
  *   tuner_load/save   text file; return the number of entries or -1
  *   tuner_lookup      1 and the class's entry, 0 when the class has none
+ *   tuner_lookup_level 1 and the class's entry for a tree level, 0 when it
+ *                     has none (spectral 1, cta_points 0 then)
  *   autotune          times every candidate (block sizes 4, 8, 16; FFT
  *                     crossover 16, 32, 64, 128) on the given stacks and
  *                     payouts (best device time of `runs` solves after one
- *                     warm-up each), records the fastest in the table and
- *                     returns it; 0 / -1                                    */
+ *                     warm-up each) and records the fastest; then, on that
+ *                     tree, times each spectral level's alternatives (1024,
+ *                     2048, 8192 points per CTA; coefficients) bottom-up and
+ *                     records those faster by more than 1%; returns the
+ *                     block size, crossover and best time; 0 / -1           */
 int icm_gb300_tuner_load(const char *path);
 int icm_gb300_tuner_save(const char *path);
 void icm_gb300_tuner_clear(void);
 int icm_gb300_tuner_lookup(int n, int k, int *block_size, int *fft_min_degree);
+int icm_gb300_tuner_lookup_level(int n, int k, int level, int *spectral, int *cta_points);
 int icm_gb300_autotune(int n, const double *S, int Q, const double *payout, int k, int runs,
                        int *block_size, int *fft_min_degree, double *best_ms);
+
+/* Subset state of a resident plan: later icm_gpu_equity_with_plan calls
+ * compute only the target players' equities (non-targets are 0), pruning the
+ * propagate below nodes with no target, as icm_gpu_equity_subset does for one
+ * call (reference src/cpu/icm.c:2430-2473, 1733-1815); n_targets = 0 (or
+ * targets = NULL) returns the plan to full-field runs.  Targets are original
+ * player indices in [0, n).  Returns 0 / -1. */
+int icm_gb300_plan_set_targets(IcmGpuPlan *plan, const int *targets, int n_targets);
 
 /* One plan, part of the quadrature: equity[i] = the sum over the rule's
  * nodes q in [q_begin, q_end) of Q of player i's node contribution
@@ -204,6 +225,13 @@ int icm_gb300_autotune(int n, const double *S, int Q, const double *payout, int 
  * Returns 0 / -1 (invalid range: 0 <= q_begin <= q_end <= Q). */
 int icm_gb300_plan_equity_nodes(IcmGpuPlan *plan, int Q, const double *payout, int q_begin, int q_end,
                                 double *equity, IcmGpuRunStats *stats);
+
+/* Work of each node of the rule for these stacks (host only, no GPU):
+ * work[q] = the players outside node q's zero prefix (those whose leaf factor
+ * is not exactly 0, the part of the tree the engine computes), 0 for nodes
+ * of weight 0, which are skipped.  A multi-GPU driver cuts node ranges of
+ * equal total work from it.  Returns 0 / -1. */
+int icm_gb300_node_work(int n, const double *S, int Q, int *work);
 
 /* Quadrature ladder: solves with Q0, 2 Q0, 4 Q0, ... nodes of the
  * reference's rule (never more than Qmax) until two successive results

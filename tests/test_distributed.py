@@ -27,6 +27,35 @@ def test_node_ranges():
         node_ranges(0, 2)
 
 
+def test_weighted_node_ranges():
+    rng = np.random.default_rng(11)
+    for Q in (1, 5, 256):
+        w = rng.integers(0, 1000, Q).astype(float)
+        for W in (1, 2, 3, 8):
+            r = node_ranges(Q, W, w)
+            assert len(r) == W and r[0][0] == 0 and r[-1][1] == Q
+            assert all(a[1] == b[0] and a[0] <= a[1] for a, b in zip(r, r[1:]))
+            sums = [w[b:e].sum() for b, e in r]
+            assert max(sums) - w.sum() / W <= w.max() + 1e-9    # within one node's weight of an equal share
+    assert node_ranges(4, 2, [0, 0, 0, 0]) == [(0, 0), (0, 4)]
+    with pytest.raises(ValueError):
+        node_ranges(4, 2, [1.0, 2.0])
+
+
+def test_node_work_counts_players_outside_the_zero_prefix(oracle):
+    """icm_gb300_node_work: n - (players with S logv < -700) per node of the
+    rule, 0 for weight-0 nodes; the oracle's nodes give the same counts."""
+    from icm_gb300 import workloads as W
+    from icm_gb300.distributed import node_work
+    S, _, _ = W.dropin(n=5000)
+    Q = 256
+    work = node_work(S, Q)
+    logv, w = oracle.nodes(Q, float(S.max()))
+    ref = np.array([0 if w[q] == 0.0 else int(np.sum(S * logv[q] >= -700.0)) for q in range(Q)])
+    assert np.array_equal(work, ref)
+    assert work.min() < work.max() == len(S)      # the spread stacks give uneven nodes
+
+
 def partial_restated(oracle_path, stacks, payouts, Q, qb, qe):
     """sum over nodes q in [qb, qe) with w_q != 0 of w_q S_i a_i / v_q
     <payout, prod_{j != i} (a_j + (1 - a_j) x) mod x^k> (a = 0 when S logv < -700)."""

@@ -248,15 +248,67 @@ def test_autotune_and_table(gpu_icm, oracle, tmp_path):
     assert b in (4, 8, 16) and f in (16, 32, 64, 128) and ms > 0
     assert gpu_icm.tuner_lookup(len(S), len(P)) == (b, f)
     path = tmp_path / "tuner.txt"
-    assert gpu_icm.tuner_save(path) == 1
+    saved = gpu_icm.tuner_save(path)   # the class entry and any per-level entries
+    assert saved >= 1
     gpu_icm.tuner_clear()
-    assert gpu_icm.tuner_load(path) == 1
+    assert gpu_icm.tuner_load(path) == saved
     plan = gpu_icm.GpuPlan(S, len(P))
     assert plan.summary()["B"] == b
     E = plan.equity(P, Q=64)
     plan.close()
     assert max_rel(E, oracle.equity(S, P, Q=64, B=8, fft_min_deg=64), floor=1e-300) < 1e-9
     gpu_icm.tuner_clear()
+
+
+def test_per_level_tuning_stable_and_close(gpu_icm, tmp_path):
+    """Per-level tuner entries (a level kept on coefficients, other points per
+    CTA) change the plan's kernels, not its result beyond rounding: a tuned
+    plan repeats itself bit for bit and stays within 1e-12 of the default
+    plan (normwise, and per player above 1e-12 of the largest equity)."""
+    gpu_icm.tuner_clear()
+    S, P, _ = W.dropin(n=16384)
+    plan = gpu_icm.GpuPlan(S, len(P))
+    E0 = plan.equity(P)
+    plan.close()
+    path = tmp_path / "levels.txt"
+    path.write_text("tune_level 14 3 5 0 0 1.0\ntune_level 14 3 7 1 1024 1.0\ntune_level 14 3 9 1 8192 1.0\n")
+    assert gpu_icm.tuner_load(path) == 3
+    assert gpu_icm.tuner_lookup_level(len(S), len(P), 5) == (0, 0)
+    plan = gpu_icm.GpuPlan(S, len(P))
+    E1, E2 = plan.equity(P), plan.equity(P)
+    plan.close()
+    assert np.array_equal(E1, E2)
+    scale = float(np.abs(E0).max())
+    assert float(np.abs(E1 - E0).max()) <= 1e-12 * scale
+    assert max_rel(E1, E0, floor=1e-12 * scale) < 1e-12
+    # the search itself: every level entry it records names a spectral level
+    gpu_icm.tuner_clear()
+    b, f, ms = gpu_icm.autotune(S, P, Q=32, runs=1)
+    plan = gpu_icm.GpuPlan(S, len(P))
+    E3, E4 = plan.equity(P), plan.equity(P)
+    plan.close()
+    assert np.array_equal(E3, E4)
+    assert max_rel(E3, E0, floor=1e-11 * scale) < 1e-11
+    for lev in range(1, 15):
+        e = gpu_icm.tuner_lookup_level(len(S), len(P), lev)
+        assert e is None or (e[0] in (0, 1) and e[1] in (0, 1024, 2048, 8192))
+    gpu_icm.tuner_clear()
+
+
+def test_plan_targets_match_one_shot_subset(gpu_icm):
+    """A resident plan's subset state gives the one-shot subset query's
+    equities bit for bit, and clearing it the full field's."""
+    S, P, T = W.dropin(n=20000, n_targets=40)
+    full = gpu_icm.gpu_equity(S, P)
+    sub = gpu_icm.gpu_equity_subset(S, P, T)
+    plan = gpu_icm.GpuPlan(S, len(P))
+    plan.set_targets(T)
+    assert np.array_equal(plan.equity(P), sub)
+    plan.set_targets(None)
+    assert np.array_equal(plan.equity(P), full)
+    with pytest.raises(gpu_icm.ICMError):
+        plan.set_targets([0, len(S)])
+    plan.close()
 
 
 def test_quadrature_ladder(gpu_icm, oracle):

@@ -50,3 +50,50 @@ def test_later_entry_replaces_earlier(L, tmp_path):
     p.write_text("tune 10 2 4 16 1\ntune 10 2 16 128 2\n")
     assert L.icm_gb300_tuner_load(str(p).encode()) == 2
     assert _lookup(L, 1000, 300) == (16, 128)
+
+
+def _lookup_level(L, n, k, level):
+    import ctypes
+    sp, pts = ctypes.c_int(), ctypes.c_int()
+    r = L.icm_gb300_tuner_lookup_level(n, k, level, ctypes.byref(sp), ctypes.byref(pts))
+    return (sp.value, pts.value) if r == 1 else None
+
+
+def test_level_entries_roundtrip(L, tmp_path):
+    p = tmp_path / "t.txt"
+    p.write_text("tune 16 3 4 64 16.8\n"
+                 "tune_level 16 3 7 1 2048 16.7\n"
+                 "tune_level 16 3 9 0 0 16.6\n"
+                 "tune_level 16 3 9 2 0 1.0\n"          # spectral must be 0 or 1
+                 "tune_level 16 3 10 1 3000 1.0\n"      # points per CTA: 1024, 2048, 4096 or 8192 (0 = default)
+                 "tune_level 16 3 99 1 1024 1.0\n")     # level out of range
+    assert L.icm_gb300_tuner_load(str(p).encode()) == 3
+    assert _lookup_level(L, 65536, 65536, 7) == (1, 2048)
+    assert _lookup_level(L, 65536, 65536, 9) == (0, 0)
+    assert _lookup_level(L, 65536, 65536, 8) is None
+    assert _lookup_level(L, 65536, 1000, 7) is None      # another k/n bucket
+    out = tmp_path / "o.txt"
+    assert L.icm_gb300_tuner_save(str(out).encode()) == 3
+    L.icm_gb300_tuner_clear()
+    assert _lookup_level(L, 65536, 65536, 7) is None
+    assert L.icm_gb300_tuner_load(str(out).encode()) == 3
+    assert _lookup_level(L, 65536, 65536, 7) == (1, 2048) and _lookup_level(L, 65536, 65536, 9) == (0, 0)
+
+
+def test_level_entry_keeps_a_level_on_coefficients(L, tmp_path):
+    """A spectral level that the table keeps on coefficients is planned as a
+    coefficient-FFT level; the geometry invariants still hold for it and for
+    the levels above it (host-side check, no GPU)."""
+    import ctypes
+    n = k = 16384
+    buf = ctypes.create_string_buffer(256)
+    assert L.icm_gb300_check_geometry(n, k, 8, 64, 0, buf, 256) == 0, buf.value
+    kinds = [int(x) for x in buf.value.split()[1:]]          # parent levels 1 .. L-1
+    assert kinds[:3] == [0, 0, 0] and kinds[3:] == [2] * (len(kinds) - 3)
+    p = tmp_path / "t.txt"
+    p.write_text("tune_level 14 3 5 0 0 1.0\ntune_level 14 3 6 1 1024 1.0\n")
+    assert L.icm_gb300_tuner_load(str(p).encode()) == 2
+    assert L.icm_gb300_check_geometry(n, k, 8, 64, 0, buf, 256) == 0, buf.value
+    tuned = [int(x) for x in buf.value.split()[1:]]
+    assert tuned[4] == 1                                      # level 5 on coefficients
+    assert tuned[:4] == kinds[:4] and tuned[5:] == kinds[5:]
