@@ -324,10 +324,35 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
     return 0;
 }
 
+void launch_fft4_cols(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
+                      int logTW, cudaStream_t st, long *launches, Prof *pr, FftSkip skip) {
+    if (batch <= 0) return;
+    if (batch > 65535) {   // grid.y limit
+        for (long b0 = 0; b0 < batch; b0 += 65535) {
+            FftSkip sk = skip;
+            sk.item0 += b0;
+            launch_fft4_cols(data + (b0 << logM), scratch + (b0 << logM), std::min(65535L, batch - b0), logM, sign, tw,
+                             logTW, st, launches, pr, sk);
+        }
+        return;
+    }
+    const int logM1 = (logM + 1) / 2, logM2 = logM - logM1;
+    const int M1 = 1 << logM1, M2 = 1 << logM2;
+    const int cbA = short_grid_cb(max(1, min(M2, 4096 / M1)), M2, (int)batch);
+    dim3 gA(M2 / cbA, (unsigned)batch);
+    const size_t smA = (size_t)cbA * M1 * sizeof(double2);
+    pr->begin("fft4_cols", (5.0 * logM1 + 6.0) * (double)(1L << logM) * (double)batch, st);
+    if (sign < 0) k_fft4_cols<-1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    else k_fft4_cols<+1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    pr->end(st);
+    ++*launches;
+}
+
 void vjp_set_smem_limits();   // vjp.cu
 
 void fft_set_smem_limits() {
     fused_set_smem_limits();
+    specbig_set_smem_limits();
     spec_set_smem_limits();
     vjp_set_smem_limits();
     sub_set_smem_limits();

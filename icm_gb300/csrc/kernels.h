@@ -408,6 +408,10 @@ struct FftSkip {
 };
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
                 cudaStream_t st, long *launches, Prof *pr, FftSkip skip = FftSkip());
+// the column pass alone of fft_batched's four-step split (data -> scratch)
+void launch_fft4_cols(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
+                      int logTW, cudaStream_t st, long *launches, Prof *pr, FftSkip skip = FftSkip());
+void specbig_set_smem_limits();
 
 void launch_leaf(int B, int n, int nblocks, const double *S, const double *node, int q0, int nq, double *a,
                  double *blockP, double *P0, int pst0, int plen0, cudaStream_t st, Prof *pr);
