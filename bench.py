@@ -134,6 +134,7 @@ def parse():
     ap.add_argument("--batch-count", type=int, default=4096, help="tournaments in the batched leg")
     ap.add_argument("--no-vjp", action="store_true", help="skip the VJP leg")
     ap.add_argument("--no-gpu-scale", action="store_true", help="skip the n = 2^20 leg")
+    ap.add_argument("--no-b200", action="store_true", help="skip the leg on the B200 figures' inputs")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="reference arm: skip the reference's own GPU library")
     ap.add_argument("--case", default="",
@@ -485,7 +486,7 @@ def main():
               "one_shot_ms": _r(_median(sub_ms)), "one_shot_full_ms": _r(_median(full_ms)),
               "path": "resident plan with targets (icm_gb300_plan_set_targets) vs the full solve; "
                       "one-shot icm_gpu_equity_subset vs icm_gpu_equity"}
-    b200 = b200_inputs_leg(icm, W, 5)
+    b200 = None if args.no_b200 else b200_inputs_leg(icm, W, 5)
     batched = (None if args.no_batched else
                batched_leg(icm, W, max(2, args.steps // 3), args.batch_count, fp64_peak_gflops / 1e3))
     vjp = None if args.no_vjp else vjp_leg(icm, W, 3, fp64_peak_gflops / 1e3)
