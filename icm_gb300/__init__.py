@@ -189,6 +189,17 @@ class GpuPlan:
             raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
         return (out, _stats_dict(st)) if return_stats else out
 
+    def equity_device(self, payout_ptr, equity_ptr, stream=0, Q=256):
+        """Stream-ordered run on device memory (icm_gb300_plan_equity_dev):
+        ``payout_ptr`` (k doubles) and ``equity_ptr`` (n doubles) are device
+        addresses (e.g. a CUDA tensor's ``data_ptr()``), ``stream`` the
+        caller's cudaStream_t as an integer (0 = the legacy default stream).
+        Returns once the work is queued; the stream's later work sees the
+        equities."""
+        if lib().icm_gb300_plan_equity_dev(self._p, int(Q), ctypes.c_void_p(int(payout_ptr)),
+                                           ctypes.c_void_p(int(equity_ptr)), ctypes.c_void_p(int(stream))) != 0:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
+
     def set_targets(self, targets=None):
         """Later equity() calls compute only these players' equities (others
         0), pruning the propagate as equity_subset does; None or an empty
@@ -410,6 +421,15 @@ class VjpPlan:
                                    ctypes.byref(st)) != 0:
             raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
         return ((gS, gP), _stats_dict(st)) if return_stats else (gS, gP)
+
+    def run_device(self, payout_ptr, cot_ptr, grad_s_ptr, grad_p_ptr, stream=0, Q=256, node_terms=False):
+        """Stream-ordered VJP on device memory (icm_gb300_vjp_run_dev); the
+        pointers are device addresses (k, n, n and k doubles), ``stream`` the
+        caller's cudaStream_t as an integer."""
+        vp = ctypes.c_void_p
+        if lib().icm_gb300_vjp_run_dev(self._h, int(Q), vp(int(payout_ptr)), vp(int(cot_ptr)), vp(int(grad_s_ptr)),
+                                       vp(int(grad_p_ptr)), int(bool(node_terms)), vp(int(stream))) != 0:
+            raise ICMError(lib().icm_gpu_last_error().decode(errors="replace"))
 
     def device_ms(self):
         return lib().icm_gb300_vjp_device_ms(self._h)

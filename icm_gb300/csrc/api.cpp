@@ -335,6 +335,42 @@ int icm_gpu_plan_summary(const IcmGpuPlan *plan, IcmGpuPlanSummary *summary) {
     return 1;
 }
 
+// a pointer the library's kernels and device copies may use: device memory of
+// the library's device, or managed memory
+static bool device_pointer(const void *ptr, const char *what, const char *fn) {
+    cudaPointerAttributes a{};
+    if (!ptr || cudaPointerGetAttributes(&a, ptr) != cudaSuccess ||
+        !(a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == g_device))) {
+        cudaGetLastError();   // clear a failed query
+        set_error(std::string(fn) + ": " + what + " is not device memory of the library's device");
+        return false;
+    }
+    return true;
+}
+
+int icm_gb300_current_device(int *device) {
+    if (!device) return -1;
+    *device = g_device;
+    return 0;
+}
+
+int icm_gb300_plan_equity_dev(IcmGpuPlan *plan, int Q, const double *d_payout, double *d_equity, void *stream) {
+    return guarded<int>("icm_gb300_plan_equity_dev", -1, [&]() -> int {
+        Plan *p = reinterpret_cast<Plan *>(plan);
+        const char *fn = "icm_gb300_plan_equity_dev";
+        if (!p || Q < 1) { set_error(std::string(fn) + ": invalid arguments"); return -1; }
+        if (!ensure_device()) return -1;
+        if (!device_pointer(d_payout, "payout", fn) || !device_pointer(d_equity, "equity", fn)) return -1;
+        std::string err;
+        DevIO io;
+        io.st = static_cast<cudaStream_t>(stream);
+        const int rc = plan_run(p, Q, d_payout, d_equity, nullptr, err, 0, -1, &io);
+        t_launches = p->launches;
+        if (rc != 0) { set_error(std::string(fn) + ": " + err); return -1; }
+        return 0;
+    });
+}
+
 int icm_gb300_plan_set_targets(IcmGpuPlan *plan, const int *targets, int n_targets) {
     return guarded<int>("icm_gb300_plan_set_targets", -1, [&]() -> int {
         Plan *p = reinterpret_cast<Plan *>(plan);
@@ -617,6 +653,27 @@ int icm_gb300_vjp_run(IcmGb300Vjp *plan, int Q, const double *payout, const doub
         const int rc = vjp_plan_run(v, Q, payout, cot, grad_S, grad_payout, flags, stats, err);
         t_launches = v->p->launches;
         if (rc != 0) { set_error("icm_gb300_vjp_run: " + err); return -1; }
+        return 0;
+    });
+}
+
+int icm_gb300_vjp_run_dev(IcmGb300Vjp *plan, int Q, const double *d_payout, const double *d_cot,
+                          double *d_grad_S, double *d_grad_payout, int flags, void *stream) {
+    return guarded<int>("icm_gb300_vjp_run_dev", -1, [&]() -> int {
+        const char *fn = "icm_gb300_vjp_run_dev";
+        if (!plan || Q < 1) { set_error(std::string(fn) + ": invalid arguments"); return -1; }
+        if (!ensure_device()) return -1;
+        if (!device_pointer(d_payout, "payout", fn) || !device_pointer(d_cot, "cotangent", fn) ||
+            !device_pointer(d_grad_S, "grad_S", fn) || !device_pointer(d_grad_payout, "grad_payout", fn))
+            return -1;
+        VjpPlan *v = reinterpret_cast<VjpPlan *>(plan);
+        std::string err;
+        DevIO io;
+        io.st = static_cast<cudaStream_t>(stream);
+        int rc = vjp_plan_enqueue(v, Q, d_payout, d_cot, flags, err, &io);
+        if (rc == 0) rc = vjp_plan_finish(v, d_grad_S, d_grad_payout, nullptr, err, &io);
+        t_launches = v->p->launches;
+        if (rc != 0) { set_error(std::string(fn) + ": " + err); return -1; }
         return 0;
     });
 }

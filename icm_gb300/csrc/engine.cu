@@ -859,6 +859,8 @@ void plan_destroy(Plan *p) {
     }
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->ev_in) cudaEventDestroy(p->ev_in);
+    if (p->ev_out) cudaEventDestroy(p->ev_out);
     for (cudaEvent_t ev : p->stage_ev) cudaEventDestroy(ev);
     if (p->ev_split) cudaEventDestroy(p->ev_split);
     for (int i = 0; i < kMaxChunkParts; ++i) {
@@ -1205,8 +1207,15 @@ static void enqueue_plan(Plan *p, int nact, const double2 *tw, int logTW) {
     }
 }
 
+cudaError_t plan_dev_events(Plan *p) {
+    cudaError_t e = cudaSuccess;
+    if (!p->ev_in) e = cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess && !p->ev_out) e = cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming);
+    return e;
+}
+
 int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats, std::string &err,
-             int q_begin, int q_end) {
+             int q_begin, int q_end, const DevIO *dev) {
     if (!p || Q < 1 || !payout || !equity) { err = "invalid arguments"; return -1; }
     if (q_end < 0) q_end = Q;
     if (q_begin < 0 || q_begin > q_end || q_end > Q) { err = "invalid node range"; return -1; }
@@ -1241,8 +1250,15 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         e = cudaMemcpyAsync(p->d_node, node.data(), sizeof(double) * node.size(), cudaMemcpyHostToDevice, p->stream);
     if (nact && e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_z, p->h_z.data(), sizeof(int) * nact, cudaMemcpyHostToDevice, p->stream);
-    if (e == cudaSuccess)
+    if (dev) {   // the caller's payout is ready once its stream reaches this point
+        if (e == cudaSuccess) e = plan_dev_events(p);
+        if (e == cudaSuccess) e = cudaEventRecord(p->ev_in, dev->st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(p->stream, p->ev_in, 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * p->k, cudaMemcpyDeviceToDevice, p->stream);
+    } else if (e == cudaSuccess) {
         e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * p->k, cudaMemcpyHostToDevice, p->stream);
+    }
     if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return -1; }
     int logNeed = 12, logTW = 0;
     for (int l = 1; l < p->L; ++l) {
@@ -1292,9 +1308,28 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     }
     cudaEventRecord(p->ev1, p->stream);
     e = cudaGetLastError();
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(equity, p->d_out, sizeof(double) * p->n, cudaMemcpyDeviceToHost, p->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (dev) {   // equities into the caller's buffer; its stream waits for them
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(equity, p->d_out, sizeof(double) * p->n, cudaMemcpyDeviceToDevice, p->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(p->ev_out, p->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(dev->st, p->ev_out, 0);
+        if (e != cudaSuccess) { err = std::string("execution: ") + cudaGetErrorString(e); return -1; }
+        if (!p->prof.on) {   // no wait: the device time of this run is not read
+            if (stats) {
+                memset(stats, 0, sizeof(*stats));
+                stats->total_ns = now_ns() - t0;
+                stats->peak_vram_bytes = (size_t)p->peak_bytes;
+                stats->engine = 1;
+                stats->B = p->B;
+            }
+            return 0;
+        }
+        e = cudaStreamSynchronize(p->stream);
+    } else {
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(equity, p->d_out, sizeof(double) * p->n, cudaMemcpyDeviceToHost, p->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    }
     if (e != cudaSuccess) { err = std::string("execution: ") + cudaGetErrorString(e); return -1; }
     {
         float ms = 0.f;

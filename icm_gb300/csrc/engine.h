@@ -148,6 +148,9 @@ struct Plan {
     // timing: events around the kernel sequence of each run, optional
     // per-kernel events (prof.on) aggregated by kernel name
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // stream-ordered runs on device buffers: the caller's stream -> the plan's
+    // stream (inputs ready) and back (outputs written)
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     double last_device_ms = 0.0;
     // stage timing (opts.verbose, as the reference's instrumented path):
     // events at the stage boundaries of every chunk, 5 per chunk
@@ -211,8 +214,18 @@ static inline int plan_ilog2(long v) {
 void plan_destroy(Plan *p);
 int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &err);
 // q_begin, q_end: the rule's nodes [q_begin, q_end) only (q_end < 0: all Q)
+// Device memory in and out of a run, ordered on the caller's stream `st`: the
+// run starts after the work already queued on st, st's later work sees the
+// outputs, and the call returns without waiting for the GPU.
+struct DevIO {
+    cudaStream_t st = nullptr;
+};
+// q_begin, q_end: the rule's nodes [q_begin, q_end) only (q_end < 0: all Q);
+// dev: payout and equity are device pointers, stream-ordered on dev->st
 int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStats *stats,
-             std::string &err, int q_begin = 0, int q_end = -1);
+             std::string &err, int q_begin = 0, int q_end = -1, const DevIO *dev = nullptr);
+// event pair of stream-ordered runs, created on first use
+cudaError_t plan_dev_events(Plan *p);
 int select_block_size(int n, int k);
 int select_fft_min(int n, int k);   // schoolbook/FFT crossover degree (config, tuner table, built-in)
 

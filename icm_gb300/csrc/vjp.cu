@@ -1275,7 +1275,17 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
     if (acc_done) cudaEventRecord(acc_done, st);   // after the piece's last launch
 }
 
-int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot, int flags, std::string &err) {
+// cotangent into sorted order on the device: out[i] = cot[perm[i]]
+__global__ void k_gather_perm(int n, const double *__restrict__ cot, const int *__restrict__ perm,
+                              double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = cot[perm[i]];
+}
+// one entry of a device vector plus a host-computed value
+__global__ void k_add_one(double *x, int i, double v) { x[i] += v; }
+
+int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot, int flags, std::string &err,
+                     const DevIO *dev) {
     if (!v || Q < 1 || !payout || !cot) { err = "invalid arguments"; return -1; }
     Plan *p = v->p;
     const double t0 = now_ns();
@@ -1321,14 +1331,27 @@ int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot,
     p->h_z.resize(nact);
     for (int j = 0; j < nact; ++j) p->h_z[j] = zero_prefix(p->S_sorted.data(), n, node[3 * j]);
     if (nact) e = cudaMemcpyAsync(p->d_z, p->h_z.data(), sizeof(int) * nact, cudaMemcpyHostToDevice, p->stream);
-    v->h_cot.resize(n);
-    for (int i = 0; i < n; ++i) v->h_cot[i] = cot[p->perm[i]];   // sorted order
     if (nact && e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_node, node.data(), sizeof(double) * node.size(), cudaMemcpyHostToDevice, p->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * k, cudaMemcpyHostToDevice, p->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(v->d_cot, v->h_cot.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
+    if (dev) {   // the caller's payout and cotangent are ready once its stream reaches this point
+        if (e == cudaSuccess) e = plan_dev_events(p);
+        if (e == cudaSuccess) e = cudaEventRecord(p->ev_in, dev->st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(p->stream, p->ev_in, 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * k, cudaMemcpyDeviceToDevice, p->stream);
+        if (e == cudaSuccess) {
+            k_gather_perm<<<(n + 255) / 256, 256, 0, p->stream>>>(n, cot, p->d_perm, v->d_cot);
+            ++p->launches;
+            e = cudaGetLastError();
+        }
+    } else {
+        v->h_cot.resize(n);
+        for (int i = 0; i < n; ++i) v->h_cot[i] = cot[p->perm[i]];   // sorted order
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(p->d_payout, payout, sizeof(double) * k, cudaMemcpyHostToDevice, p->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(v->d_cot, v->h_cot.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
+    }
     if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return -1; }
     int logNeed = 12, logTW = 0;
     for (int l = 1; l < p->L; ++l)
@@ -1383,13 +1406,42 @@ int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot,
     return 0;
 }
 
-int vjp_plan_finish(VjpPlan *v, double *grad_S, double *grad_payout, IcmGpuRunStats *stats, std::string &err) {
+int vjp_plan_finish(VjpPlan *v, double *grad_S, double *grad_payout, IcmGpuRunStats *stats, std::string &err,
+                    const DevIO *dev) {
     if (!v || !v->pending || !grad_S || !grad_payout) { err = "invalid arguments (no VJP enqueued)"; return -1; }
     v->pending = false;
     Plan *p = v->p;
     const int n = p->n, k = p->k, nact = v->pnact, Q = v->pQ;
     const bool node_terms = v->pnode;
     cudaError_t e = cudaSuccess;
+    if (dev) {   // gradients into the caller's buffers; its stream waits for them
+        e = cudaMemcpyAsync(grad_S, p->d_out, sizeof(double) * n, cudaMemcpyDeviceToDevice, p->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(grad_payout, v->d_gradP, sizeof(double) * k, cudaMemcpyDeviceToDevice, p->stream);
+        if (node_terms && nact) {   // the largest stack's node term, chained on the host
+            std::vector<double> hA(nact), hB(nact);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(hA.data(), v->d_nodeA, sizeof(double) * nact, cudaMemcpyDeviceToHost, p->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(hB.data(), v->d_nodeB, sizeof(double) * nact, cudaMemcpyDeviceToHost, p->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+            if (e == cudaSuccess) {
+                k_add_one<<<1, 1, 0, p->stream>>>(grad_S, p->perm[0], node_shift_term(Q, p->Smax, v->pqidx, v->pw, hA, hB));
+                e = cudaGetLastError();
+            }
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(p->ev_out, p->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(dev->st, p->ev_out, 0);
+        if (e != cudaSuccess) { err = std::string("execution: ") + cudaGetErrorString(e); return -1; }
+        if (stats) {
+            memset(stats, 0, sizeof(*stats));
+            stats->total_ns = now_ns() - v->pt0;
+            stats->peak_vram_bytes = p->arena_bytes + v->arena_bytes;
+            stats->engine = 1;
+            stats->B = p->B;
+        }
+        return 0;
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(grad_S, p->d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, p->stream);
     if (e == cudaSuccess)

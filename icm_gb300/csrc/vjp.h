@@ -160,8 +160,13 @@ VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t
 void vjp_plan_destroy(VjpPlan *v);
 // enqueue a run on the plan's stream without waiting; finish waits, copies
 // the gradients out and adds the node terms
-int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot, int flags, std::string &err);
-int vjp_plan_finish(VjpPlan *v, double *grad_S, double *grad_payout, IcmGpuRunStats *stats, std::string &err);
+// dev: payout, cot, grad_S, grad_payout are device pointers, stream-ordered on
+// dev->st (the finish waits for the GPU only with node terms, whose host-side
+// chain rule needs the per-node sums)
+int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot, int flags, std::string &err,
+                     const DevIO *dev = nullptr);
+int vjp_plan_finish(VjpPlan *v, double *grad_S, double *grad_payout, IcmGpuRunStats *stats, std::string &err,
+                    const DevIO *dev = nullptr);
 // flags: 1 = add the dependence of the quadrature nodes on max S
 int vjp_plan_run(VjpPlan *v, int Q, const double *payout, const double *cot, double *grad_S, double *grad_payout,
                  int flags, IcmGpuRunStats *stats, std::string &err);

@@ -226,6 +226,25 @@ int icm_gb300_plan_set_targets(IcmGpuPlan *plan, const int *targets, int n_targe
 int icm_gb300_plan_equity_nodes(IcmGpuPlan *plan, int Q, const double *payout, int q_begin, int q_end,
                                 double *equity, IcmGpuRunStats *stats);
 
+/* Stream-ordered runs on device memory, for callers whose data already lives
+ * on the GPU (a torch tensor, a CUDA buffer): the payouts, cotangents,
+ * equities and gradients are device pointers (device memory of the library's
+ * device or managed memory, else -1), and `stream` is the caller's CUDA
+ * stream (cudaStream_t; NULL = the legacy default stream).  The run starts
+ * after the work already queued on that stream, later work on the stream sees
+ * the results, and the call returns without waiting for the GPU (the VJP with
+ * ICM_VJP_NODE_TERMS waits once, for its host-side chain rule).  Arrays are
+ * as in icm_gpu_equity_with_plan / icm_gb300_vjp_run (original player order,
+ * payout[k], equity[n], cot[n], grad_S[n], grad_payout[k]).  The plan's
+ * stacks stay on the host side (the player sort runs there).  The device time
+ * of such a run is not recorded.  Returns 0 / -1. */
+int icm_gb300_plan_equity_dev(IcmGpuPlan *plan, int Q, const double *d_payout, double *d_equity, void *stream);
+/* The device the library runs on (the one icm_gpu_init chose; -1 before any
+ * initialisation).  Returns 0 / -1 (null argument). */
+int icm_gb300_current_device(int *device);
+int icm_gb300_vjp_run_dev(IcmGb300Vjp *plan, int Q, const double *d_payout, const double *d_cot,
+                          double *d_grad_S, double *d_grad_payout, int flags, void *stream);
+
 /* Work of each node of the rule for these stacks (host only, no GPU):
  * work[q] = the players outside node q's zero prefix (those whose leaf factor
  * is not exactly 0, the part of the tree the engine computes), 0 for nodes
