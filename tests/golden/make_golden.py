@@ -15,6 +15,10 @@ Writes:
                        full-size drop-in workload's 64 subset targets:
                        payout (k-j+1)^2 with k = n gives E = 2 V2 + 3 V1 - 2
                        (unnormalised), from oracle V1/V2.
+  ref_gpu_scale_geometric.json  the reference's own icm_equity_subset on the
+                       GPU-only scale workload with geometric payouts (n = 2^20,
+                       k = 1000, Q = 256) at 16 seeded targets (minutes on the
+                       CPU: the full field would take hours).
   vjp_fd_reference.json  directional derivatives of L = <cot, equity> taken
                        by central finite differences of the reference's own
                        icm_equity (oracle/_ref): along stacks S -> S (1 + h u)
@@ -187,14 +191,30 @@ def vjp_fd_fixture(ref: ReferenceLib):
                       "Q = 256", "cases": cases}
 
 
+def scale_geometric_fixture(ref: ReferenceLib):
+    S, P = W.gpu_scale(shape="geometric")
+    T = np.sort(np.random.default_rng(20).choice(len(S), 16, replace=False)).astype(np.int32)
+    t0 = time.time()
+    E = ref.equity(S, P, Q=256, targets=T)
+    print(f"  gpu_scale geometric n={len(S)} k={len(P)}: {time.time() - t0:.1f}s", flush=True)
+    return {"source": "reference src/cpu/icm.c icm_equity_subset via oracle/_ref (FFTW shim, devices/generic, OpenMP)",
+            "gen": "gpu_scale(shape='geometric')", "n": len(S), "k": len(P), "Q": 256,
+            "targets": [int(t) for t in T], "subset_equity": fl(E[T])}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-large", action="store_true")
-    ap.add_argument("--only", choices=["vjp_fd"], default=None, help="regenerate only this fixture")
+    ap.add_argument("--only", choices=["vjp_fd", "scale_geometric"], default=None,
+                    help="regenerate only this fixture")
     args = ap.parse_args()
     build()
     ref = ReferenceLib(openmp=True)
     orc = Oracle()
+    if args.only == "scale_geometric":
+        print("ref_gpu_scale_geometric.json")
+        json.dump(scale_geometric_fixture(ref), open(os.path.join(HERE, "ref_gpu_scale_geometric.json"), "w"))
+        return
     if args.only == "vjp_fd":
         print("vjp_fd_reference.json")
         json.dump(vjp_fd_fixture(ref), open(os.path.join(HERE, "vjp_fd_reference.json"), "w"), indent=1)
@@ -208,6 +228,9 @@ def main():
         json.dump(closed_form_fixture(orc), open(os.path.join(HERE, "closed_form.json"), "w"))
     print("vjp_fd_reference.json")
     json.dump(vjp_fd_fixture(ref), open(os.path.join(HERE, "vjp_fd_reference.json"), "w"), indent=1)
+    if not args.skip_large:
+        print("ref_gpu_scale_geometric.json")
+        json.dump(scale_geometric_fixture(ref), open(os.path.join(HERE, "ref_gpu_scale_geometric.json"), "w"))
 
 
 if __name__ == "__main__":

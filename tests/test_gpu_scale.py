@@ -1,7 +1,8 @@
 """GPU-only scale: n = 2^20 players, stacks 1e4 exp(1.5 N(0,1)).
 (a) k = n linear payout: closed form E = V1 / sum(n - m) on sampled players
 (1e-9); (b) k = 1000 geometric payout 0.97: the oracle on sampled targets at
-a reduced node count (the same Q on both sides, 1e-8)."""
+a reduced node count (the same Q on both sides, 1e-8), and the reference's
+own subset query at Q = 256 (a committed fixture, 1e-8)."""
 import numpy as np
 import pytest
 
@@ -28,3 +29,21 @@ def test_geometric_k1000_against_oracle(gpu_icm, oracle):
     assert max_rel(E[T], R[T]) < 1e-8
     Es = gpu_icm.equity_subset(S, P, T, Q=24)
     assert max_rel(Es[T], E[T]) < 1e-12
+
+
+def test_geometric_k1000_against_reference_at_q256(gpu_icm):
+    """(b) at the full Q = 256 against the reference's own icm_equity_subset
+    (tests/golden/ref_gpu_scale_geometric.json, 16 targets), full field and
+    subset, within the reference's GPU gate of 1e-8."""
+    import json
+    import os
+    from tests.conftest import GOLDEN
+    fx = json.load(open(os.path.join(GOLDEN, "ref_gpu_scale_geometric.json")))
+    S, P = W.gpu_scale(shape="geometric")
+    assert len(S) == fx["n"] and len(P) == fx["k"]
+    T = fx["targets"]
+    E = gpu_icm.equity(S, P, Q=fx["Q"])
+    assert max_rel(E[T], fx["subset_equity"]) < 1e-8
+    Es = gpu_icm.equity_subset(S, P, T, Q=fx["Q"])
+    assert max_rel(Es[T], fx["subset_equity"]) < 1e-8
+    assert np.count_nonzero(np.delete(Es, T)) == 0
