@@ -517,7 +517,7 @@ def equity_adaptive(stacks, payouts, tol=1e-9, Q0=256, Qmax=4096):
 
 def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False,
               zero_prefix=True, subtree=False, small_max_n=0, engine="auto", quadrature="erfc", chunk_streams=0,
-              cta_points=0):
+              cta_points=0, tma=True):
     """Process-wide engine settings for plans created afterwards (0 = default).
 
     coefficient_fft_only=True keeps every FFT tree level on coefficients
@@ -534,7 +534,9 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
     (0 = default: 4 from n = 6000, else 2; 1 = one stream; at most 4; same
     results); cta_points sets the complex points per CTA of the spectral
     levels' one-CTA FFT steps (1024, 2048, 4096 or 8192; 0 = the tuner
-    table's per-level choice, else 4096; same results)."""
+    table's per-level choice, else 4096; same results); tma=False makes the
+    four-step column pass of the largest levels gather its tile with ordinary
+    loads instead of a TMA tensor copy (same results)."""
     engines = {"auto": 0, "tree": 1, "linear": 2}
     rules = {"erfc": 0, "tanh_sinh": 1}
     if engine not in engines:
@@ -543,7 +545,7 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
         raise ValueError(f"quadrature must be one of {sorted(rules)}, got {quadrature!r}")
     cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes,
                          0 if zero_prefix else 1, 1 if subtree else 0, int(small_max_n), engines[engine],
-                         rules[quadrature], int(chunk_streams), int(cta_points))
+                         rules[quadrature], int(chunk_streams), int(cta_points), 0 if tma else 1)
     lib().icm_gb300_set_config(ctypes.byref(cfg))
 
 

@@ -40,7 +40,8 @@ class IcmGb300Config(ctypes.Structure):
                 ("coefficient_fft_only", ctypes.c_int), ("max_device_bytes", ctypes.c_size_t),
                 ("disable_zero_prefix", ctypes.c_int), ("enable_subtree", ctypes.c_int),
                 ("small_max_n", ctypes.c_int), ("engine", ctypes.c_int), ("quadrature", ctypes.c_int),
-                ("chunk_streams", ctypes.c_int), ("cta_points", ctypes.c_int)]
+                ("chunk_streams", ctypes.c_int), ("cta_points", ctypes.c_int),
+                ("disable_tma", ctypes.c_int)]
 
 
 _dp = ctypes.POINTER(ctypes.c_double)

@@ -1220,6 +1220,7 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
     if (q_end < 0) q_end = Q;
     if (q_begin < 0 || q_begin > q_end || q_end > Q) { err = "invalid node range"; return -1; }
     const double t0 = now_ns();
+    const long tma0 = g_tma_launches.load();
     p->launches = 0;
     std::vector<double> logv, w;
     make_nodes(Q, p->Smax, logv, w);
@@ -1331,6 +1332,13 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     }
     if (e != cudaSuccess) { err = std::string("execution: ") + cudaGetErrorString(e); return -1; }
+    if (g_tma_launches.load() != tma0) {   // a TMA column pass ran: did every tile copy complete?
+        const int f = tma_take_failures();
+        if (f != 0) {
+            err = "TMA tile copies of " + std::to_string(f) + " CTAs did not complete within the wait limit";
+            return -1;
+        }
+    }
     {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, p->ev0, p->ev1);

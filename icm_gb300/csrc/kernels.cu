@@ -324,6 +324,8 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
     return 0;
 }
 
+std::atomic<long> g_tma_launches{0};
+
 void launch_fft4_cols(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
                       int logTW, cudaStream_t st, long *launches, Prof *pr, FftSkip skip) {
     if (batch <= 0) return;
@@ -342,8 +344,16 @@ void launch_fft4_cols(const double2 *data, double2 *scratch, long batch, int log
     dim3 gA(M2 / cbA, (unsigned)batch);
     const size_t smA = (size_t)cbA * M1 * sizeof(double2);
     pr->begin("fft4_cols", (5.0 * logM1 + 6.0) * (double)(1L << logM) * (double)batch, st);
-    if (sign < 0) k_fft4_cols<-1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
-    else k_fft4_cols<+1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    // the tile staged by TMA (measured 0.4-1% faster than the gathers below,
+    // bitwise the same); the plain gathers where a tensor map cannot be made
+    // or the configuration asks for them
+    const bool tma = g_config.disable_tma != 1 && launch_fft4_cols_tma(data, scratch, batch, logM, sign, tw, logTW,
+                                                                       cbA, st, skip);
+    if (tma) ++g_tma_launches;
+    else {
+        if (sign < 0) k_fft4_cols<-1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+        else k_fft4_cols<+1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    }
     pr->end(st);
     ++*launches;
 }
@@ -352,6 +362,7 @@ void vjp_set_smem_limits();   // vjp.cu
 
 void fft_set_smem_limits() {
     fused_set_smem_limits();
+    tma_set_smem_limits();
     specbig_set_smem_limits();
     spec_set_smem_limits();
     vjp_set_smem_limits();

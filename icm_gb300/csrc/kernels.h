@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <vector>
 
 namespace icmg {
@@ -412,6 +413,12 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
 void launch_fft4_cols(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
                       int logTW, cudaStream_t st, long *launches, Prof *pr, FftSkip skip = FftSkip());
 void specbig_set_smem_limits();
+// the column pass with its tile staged by TMA (tma_cols.cu); false: not launched
+bool launch_fft4_cols_tma(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
+                          int logTW, int cbA, cudaStream_t st, FftSkip skip);
+void tma_set_smem_limits();
+int tma_take_failures();
+extern std::atomic<long> g_tma_launches;   // column passes launched through TMA (all plans)
 
 void launch_leaf(int B, int n, int nblocks, const double *S, const double *node, int q0, int nq, double *a,
                  double *blockP, double *P0, int pst0, int plen0, cudaStream_t st, Prof *pr);

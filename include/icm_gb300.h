@@ -53,7 +53,11 @@ int icm_last_status(void);
  *   cta_points        complex points per CTA of the one-CTA FFT steps of a
  *                     single plan's spectral levels (1024, 2048, 4096 or
  *                     8192; 0 = the tuner table's per-level choice, else
- *                     4096); same results, only the CTA shape changes      */
+ *                     4096); same results, only the CTA shape changes
+ *   disable_tma       1 = the four-step column pass of the largest levels
+ *                     gathers its tile with ordinary loads instead of a
+ *                     tensor-map (TMA) copy (same results; read when a run
+ *                     is enqueued)                                           */
 typedef struct {
     int block_size;
     int fft_min_degree;
@@ -67,6 +71,7 @@ typedef struct {
     int quadrature;
     int chunk_streams;
     int cta_points;
+    int disable_tma;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created

@@ -105,3 +105,21 @@ def test_streams_random_shapes(gpu_icm):
         P = rng.random(k)
         ref = _run(gpu_icm, S, P, 1, qc, Q)
         assert np.array_equal(_run(gpu_icm, S, P, 4, qc, Q), ref), (n, k, Q, qc)
+
+
+def test_tma_column_pass_bitwise(gpu_icm):
+    """The largest levels' four-step column pass with its tile staged by a TMA
+    tensor copy equals the pass with ordinary gathers bit for bit (drop-in
+    field with two multi-pass levels, full and subset queries)."""
+    from icm_gb300 import workloads as W
+    S, P, T = W.dropin(n=40000, n_targets=30)
+    res = {}
+    for tma in (True, False):
+        gpu_icm.configure(tma=tma)
+        plan = gpu_icm.GpuPlan(S, len(P))
+        full = plan.equity(P)
+        plan.set_targets(T)
+        res[tma] = (full, plan.equity(P))
+        plan.close()
+    gpu_icm.configure()
+    assert np.array_equal(res[True][0], res[False][0]) and np.array_equal(res[True][1], res[False][1])
