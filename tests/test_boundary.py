@@ -254,3 +254,25 @@ def test_player_order_many_threads(built_lib):
     for t in th:
         t.join()
     assert not bad
+
+
+def test_config_struct_layout_matches_header(tmp_path):
+    """IcmGb300Config as the C compiler lays it out (include/icm_gb300.h)
+    equals the ctypes mirror field by field."""
+    import shutil
+    import subprocess
+    from icm_gb300._lib import IcmGb300Config
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    names = [f for f, _ in IcmGb300Config._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"icm_gb300.h\"\nint main(void) {\n"
+                   "  printf(\"%zu\\n\", sizeof(IcmGb300Config));\n" +
+                   "".join(f"  printf(\"%zu\\n\", offsetof(IcmGb300Config, {f}));\n" for f in names) +
+                   "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert vals[0] == ctypes.sizeof(IcmGb300Config)
+    assert vals[1:] == [getattr(IcmGb300Config, f).offset for f in names]
