@@ -67,6 +67,7 @@ SIGNATURES = {
     "icm_gpu_equity_with_plan": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gb300_plan_set_targets": (ctypes.c_int, [_vp, _ip, ctypes.c_int]),
     "icm_gb300_node_work": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _ip]),
+    "icm_gb300_tma_launch_count": (ctypes.c_long, []),
     "icm_gb300_current_device": (ctypes.c_int, [_ip]),
     "icm_gb300_plan_equity_dev": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     "icm_gb300_vjp_run_dev": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]),

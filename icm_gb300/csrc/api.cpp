@@ -348,6 +348,8 @@ static bool device_pointer(const void *ptr, const char *what, const char *fn) {
     return true;
 }
 
+long icm_gb300_tma_launch_count(void) { return g_tma_launches.load(); }
+
 int icm_gb300_current_device(int *device) {
     if (!device) return -1;
     *device = g_device;

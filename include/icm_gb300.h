@@ -247,6 +247,10 @@ int icm_gb300_plan_equity_dev(IcmGpuPlan *plan, int Q, const double *d_payout, d
 /* The device the library runs on (the one icm_gpu_init chose; -1 before any
  * initialisation).  Returns 0 / -1 (null argument). */
 int icm_gb300_current_device(int *device);
+
+/* Four-step column passes launched through TMA tensor copies since the
+ * library was loaded (all plans; a diagnostic for disable_tma). */
+long icm_gb300_tma_launch_count(void);
 int icm_gb300_vjp_run_dev(IcmGb300Vjp *plan, int Q, const double *d_payout, const double *d_cot,
                           double *d_grad_S, double *d_grad_payout, int flags, void *stream);
 

@@ -112,14 +112,18 @@ def test_tma_column_pass_bitwise(gpu_icm):
     tensor copy equals the pass with ordinary gathers bit for bit (drop-in
     field with two multi-pass levels, full and subset queries)."""
     from icm_gb300 import workloads as W
+    from icm_gb300._lib import lib
     S, P, T = W.dropin(n=40000, n_targets=30)
-    res = {}
+    res, used = {}, {}
     for tma in (True, False):
         gpu_icm.configure(tma=tma)
+        before = lib().icm_gb300_tma_launch_count()
         plan = gpu_icm.GpuPlan(S, len(P))
         full = plan.equity(P)
         plan.set_targets(T)
         res[tma] = (full, plan.equity(P))
         plan.close()
+        used[tma] = lib().icm_gb300_tma_launch_count() - before
     gpu_icm.configure()
+    assert used[True] > 0 and used[False] == 0   # the TMA pass ran, and only when asked for
     assert np.array_equal(res[True][0], res[False][0]) and np.array_equal(res[True][1], res[False][1])
