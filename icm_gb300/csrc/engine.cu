@@ -1297,6 +1297,7 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         p->graph_node = p->d_node;
         p->graph_subset = p->subset;
         p->graph_launches = p->launches - l0;
+        p->graph_tma = g_tma_launches.load() != tma0;
         p->launches = l0;
     }
     cudaEventRecord(p->ev0, p->stream);
@@ -1332,7 +1333,7 @@ int plan_run(Plan *p, int Q, const double *payout, double *equity, IcmGpuRunStat
         if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     }
     if (e != cudaSuccess) { err = std::string("execution: ") + cudaGetErrorString(e); return -1; }
-    if (g_tma_launches.load() != tma0) {   // a TMA column pass ran: did every tile copy complete?
+    if (g_tma_launches.load() != tma0 || (use_graph && p->graph_tma)) {   // a TMA column pass ran: did every tile copy complete?
         const int f = tma_take_failures();
         if (f != 0) {
             err = "TMA tile copies of " + std::to_string(f) + " CTAs did not complete within the wait limit";

@@ -144,6 +144,7 @@ struct Plan {
     const double *graph_node = nullptr;   // the node buffer the graph reads
     bool graph_subset = false;            // captured with the subset masks
     long graph_launches = 0;
+    bool graph_tma = false;               // the captured sequence holds TMA column passes
     double peak_bytes = 0;
     // timing: events around the kernel sequence of each run, optional
     // per-kernel events (prof.on) aggregated by kernel name
