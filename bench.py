@@ -585,7 +585,7 @@ def compact_vjp(v):
         return None
     detail("vjp", v)
     out = {}
-    for shape in ("linear", "quadratic"):
+    for shape in ("linear", "quadratic", "untruncated_262144"):
         if shape in v:
             out[shape] = {"ratio": _r(v[shape]["ratio"]), "vjp_ms": _r(v[shape]["vjp_ms"]),
                           "fwd_ms": _r(v[shape]["fwd_ms"])}
@@ -745,10 +745,12 @@ def vjp_leg(icm, W, steps, fp64_tflops=None):
     stacks, N(0, 1) cotangent, linear and quadratic payouts.  Device time of
     the VJP (forward tree recomputed inside) against the forward solve on the
     same stacks, both with plans resident; e2e through icm_gb300_equity_vjp;
-    and the batched VJP over 256 tournaments with n in [100, 4000]."""
+    the same at n = k = 2^18 (linear payout: every level untruncated, so the
+    tree's top levels are spectral in both directions); and the batched VJP
+    over 256 tournaments with n in [100, 4000]."""
     out = {"metric": "VJP/fwd time", "config": "n=16384, k=2000, Q=256, stacks gamma(2,5000), cotangent N(0,1)"}
-    for shape in ("linear", "quadratic"):
-        S, P, cot = W.vjp(payout=shape)
+    for shape in ("linear", "quadratic", "untruncated_262144"):
+        S, P, cot = W.vjp(payout=shape) if shape != "untruncated_262144" else W.vjp(n=1 << 18, k=1 << 18)
         k = len(P)
         fplan = icm.GpuPlan(S, k)
         vplan = icm.VjpPlan(S, k)

@@ -517,7 +517,7 @@ def equity_adaptive(stacks, payouts, tol=1e-9, Q0=256, Qmax=4096):
 
 def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coefficient_fft_only=False,
               zero_prefix=True, subtree=False, small_max_n=0, engine="auto", quadrature="erfc", chunk_streams=0,
-              cta_points=0, tma=True):
+              cta_points=0, tma=True, vjp_spectral_min_degree=0):
     """Process-wide engine settings for plans created afterwards (0 = default).
 
     coefficient_fft_only=True keeps every FFT tree level on coefficients
@@ -536,7 +536,11 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
     levels' one-CTA FFT steps (1024, 2048, 4096 or 8192; 0 = the tuner
     table's per-level choice, else 4096; same results); tma=False makes the
     four-step column pass of the largest levels gather its tile with ordinary
-    loads instead of a TMA tensor copy (same results)."""
+    loads instead of a TMA tensor copy (same results);
+    vjp_spectral_min_degree: levels of a single VJP plan whose children have
+    at least this degree run spectrally in the forward and adjoint passes
+    (0 = every level a forward plan would make spectral, -1 = all on
+    coefficients; results agree to rounding)."""
     engines = {"auto": 0, "tree": 1, "linear": 2}
     rules = {"erfc": 0, "tanh_sinh": 1}
     if engine not in engines:
@@ -545,7 +549,8 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
         raise ValueError(f"quadrature must be one of {sorted(rules)}, got {quadrature!r}")
     cfg = IcmGb300Config(block_size, fft_min_degree, q_chunk, 1 if coefficient_fft_only else 0, max_device_bytes,
                          0 if zero_prefix else 1, 1 if subtree else 0, int(small_max_n), engines[engine],
-                         rules[quadrature], int(chunk_streams), int(cta_points), 0 if tma else 1)
+                         rules[quadrature], int(chunk_streams), int(cta_points), 0 if tma else 1,
+                         int(vjp_spectral_min_degree))
     lib().icm_gb300_set_config(ctypes.byref(cfg))
 
 

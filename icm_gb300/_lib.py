@@ -41,7 +41,7 @@ class IcmGb300Config(ctypes.Structure):
                 ("disable_zero_prefix", ctypes.c_int), ("enable_subtree", ctypes.c_int),
                 ("small_max_n", ctypes.c_int), ("engine", ctypes.c_int), ("quadrature", ctypes.c_int),
                 ("chunk_streams", ctypes.c_int), ("cta_points", ctypes.c_int),
-                ("disable_tma", ctypes.c_int)]
+                ("disable_tma", ctypes.c_int), ("vjp_spectral_min_degree", ctypes.c_int)]
 
 
 _dp = ctypes.POINTER(ctypes.c_double)

@@ -521,7 +521,8 @@ int icm_gb300_check_geometry(int n, int k, int block_size, int fft_min_degree, i
         g_config.block_size = block_size;
         g_config.fft_min_degree = fft_min_degree;
         Plan p;
-        p.coeff_only = (flags & 1) != 0;
+        p.coeff_only = (flags & 1) != 0 || ((flags & 2) != 0 && g_config.vjp_spectral_min_degree < 0);
+        p.vjp = (flags & 2) != 0;
         std::string err;
         const std::vector<double> S(n, 1.0);   // stack values do not shape the tree
         int rc = plan_geometry(&p, n, S.data(), k, err);

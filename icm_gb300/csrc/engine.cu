@@ -474,6 +474,9 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     const int Nt = pow2_ge(p->nblocks);
     p->L = ilog2(Nt) + 1;
     if (p->L > kMaxLevels) { err = "tournament too large"; return -1; }
+    // a VJP plan's spectral band may reach the root only when the root's
+    // children are untruncated
+    const bool vjp_root_spec = p->L >= 2 && ((long)B << (p->L - 2)) + 1 <= k;
     for (int l = 0; l < p->L; ++l) {
         Level &v = p->lv[l];
         v.nreal = (l == 0) ? p->nblocks : (p->lv[l - 1].nreal + 1) / 2;
@@ -494,7 +497,17 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
             // and a truncated parent never has a spectral level above it)
             bool spec = p->spectral && can_fft && c.deg + 1 <= k;
             if (c.deg > kSpecMaxD) spec = spec && l - 1 >= 1 && p->lv[l - 1].kind == 2;
-            if (spec && !tune_spectral_ok(n, k, l)) spec = false;   // the tuner table keeps it on coefficients
+            if (p->vjp) {
+                // single VJP plans: spectral from the configured child degree up
+                // (the forward tuner table does not apply); a spectral band that
+                // ends below the root (children truncated at k above it) stays
+                // within one-CTA transforms, where its top level converts the
+                // coefficient Pbar handed down to it
+                if (g_config.vjp_spectral_min_degree > 0) spec = spec && c.deg >= g_config.vjp_spectral_min_degree;
+                if (!vjp_root_spec) spec = spec && c.deg <= kSpecMaxD;
+            } else if (spec && !tune_spectral_ok(n, k, l)) {
+                spec = false;   // the tuner table keeps it on coefficients
+            }
             v.kind = spec ? 2 : (can_fft ? 1 : 0);
             v.cta_pts = select_cta_points(n, k, l);
             v.fft = (v.kind == 1) ? 1 : 0;
@@ -546,7 +559,7 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     // engine: the small path, the linear engine or the tree
     const int eng = g_config.engine;
     p->small = eng != 2 && plan_small_ok(p);
-    p->linear = !p->coeff_only && !p->small && k <= kLinearMaxK &&
+    p->linear = !p->coeff_only && !p->vjp && !p->small && k <= kLinearMaxK &&
                 (eng == 2 || (eng == 0 && plan_linear_auto(n, k)));
     return 0;
 }
@@ -587,6 +600,11 @@ int plan_check_geometry(const Plan *p, std::string &why) {
             if (c.deg > kSpecMaxD && !(l - 1 >= 1 && c.kind == 2))
                 return bad(l, "multi-pass spectral level without spectral children");
             if (p->coeff_only || !p->spectral) return bad(l, "spectral level in a coefficient-only plan");
+            // a VJP band ending below the root converts its top's Pbar and
+            // writes its top's gbar coefficients in one CTA
+            if (p->vjp && l < L - 1 && p->lv[l + 1].kind != 2 && c.deg > kSpecMaxD)
+                return bad(l, "VJP spectral band ends on a multi-pass level below the root");
+            if (p->vjp && c.deg < 4) return bad(l, "VJP spectral level below degree 4");
         } else if (v.kind != 0) {
             return bad(l, "unknown level kind");
         } else if (c.deg >= p->fft_min_deg) {
@@ -714,11 +732,12 @@ static bool make_chunk_view(const Plan *p, int off, int slots, size_t arena_byte
 }
 
 Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err, bool coeff_only,
-                  double q_bytes_scale, size_t budget_bytes) {
+                  double q_bytes_scale, size_t budget_bytes, bool vjp) {
     Plan *p = new Plan();
     if (opts) p->opts = *opts;
     p->opts.device_id = g_device;
     p->coeff_only = coeff_only;
+    p->vjp = vjp;
     if (plan_geometry(p, n, S, k, err) != 0) { delete p; return nullptr; }
     const int B = p->B;
     const int Nt = 1 << (p->L - 1);

@@ -86,6 +86,7 @@ struct Plan {
     int fft_min_deg = 64;
     bool spectral = true;           // use spectral levels where they apply
     bool coeff_only = false;        // never use spectral levels
+    bool vjp = false;               // forward tree of a single VJP plan (its adjoint reads every level)
     bool zskip = true;              // prune wholly-zero tree nodes per quadrature node
     int Lf = 0;                     // bottom schoolbook levels fused into the subtree kernels
     bool small = false;             // whole pipeline in one CTA per node (small.cu)
@@ -193,11 +194,12 @@ int plan_restack(Plan *p, const double *S, std::string &err);
 void sort_players_desc(const double *S, int n, std::vector<int> &perm);
 // tree buffers for chunks of qc nodes from `base` (nullptr: size only)
 size_t plan_tree_layout(Plan *p, int qc, char *base);
-// coeff_only: every FFT level on coefficients (the adjoint passes need the
-// coefficients of every level); q_bytes_scale sizes the node chunk for
-// callers that add per-node buffers of their own
+// coeff_only: every FFT level on coefficients; q_bytes_scale sizes the node
+// chunk for callers that add per-node buffers of their own; vjp: the forward
+// tree of a single VJP plan (tree engine only, spectral levels under the VJP's
+// rules, plan_geometry)
 Plan *plan_create(int n, const double *S, int k, const IcmGpuOptions *opts, std::string &err,
-                  bool coeff_only = false, double q_bytes_scale = 1.0, size_t budget = 0);
+                  bool coeff_only = false, double q_bytes_scale = 1.0, size_t budget = 0, bool vjp = false);
 // launch sequence of one chunk of nq nodes (engine.cu); divide = false stops
 // after the propagate pass (the tree of the chunk stays in the plan's buffers).
 // view: run on a chunk piece's buffers and stream instead of the plan's own;

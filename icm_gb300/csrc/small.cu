@@ -192,7 +192,7 @@ size_t small_smem_bytes(const Plan *p) {
 // level path wins, e.g. n = 900, k = 120: 0.368 against 0.319 ms).
 // g_config.small_max_n overrides them (-1 disables the path).
 bool plan_small_ok(const Plan *p) {
-    if (p->coeff_only || g_config.small_max_n < 0) return false;
+    if (p->coeff_only || p->vjp || g_config.small_max_n < 0) return false;
     int lim;
     if (g_config.small_max_n > 0) lim = g_config.small_max_n;
     else lim = p->k <= 16 ? kSmallMaxN : p->k <= 64 ? 768 : p->k <= 128 ? 640 : p->k <= 256 ? 512 : 352;

@@ -26,12 +26,13 @@
 //
 // The upward pass is the transpose of the propagate pass and the downward
 // pass the transpose of the build pass.  Leaf quantities come from exact
-// leave-one-out recurrences over the block (no division).  Tree levels run
-// on coefficients (the plan is made without spectral levels); the forward
-// tree of a chunk of nodes is recomputed by the VJP call itself and stays in
-// the plan's buffers for the adjoint passes.  Levels whose FFT fits one CTA
-// use one-kernel transforms that reuse the children's spectra cached by the
-// forward build; other levels use schoolbook kernels.
+// leave-one-out recurrences over the block (no division).  The forward tree
+// of a chunk of nodes is recomputed by the VJP call itself and stays in the
+// plan's buffers for the adjoint passes.  Coefficient levels whose FFT fits
+// one CTA use one-kernel transforms that reuse the children's spectra cached
+// by the forward build, larger ones multi-pass transforms, the others
+// schoolbook kernels; spectral levels (untruncated children, as in forward
+// plans) keep their adjoint in the frequency domain too (vjp_spec.cu).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -827,6 +828,7 @@ void vjp_set_smem_limits() {
     cudaFuncSetAttribute(kw_adj_up_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vjp_up_smem(kVjpMaxN));
     cudaFuncSetAttribute(kw_adj_down_packed, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)vjp_down_smem(kVjpMaxN));
+    vjp_spec_set_smem_limits();
 }
 
 // per (member, node): k_node_reduce over one member's players of a forest
@@ -875,12 +877,22 @@ static bool level_big(const Level &v) { return v.fft && v.npairs > 0 && !level_f
 size_t vjp_level_layout(const Plan *p, int qc, char *base, VjpBufs *b) {
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
-    size_t o_gb[kMaxLevels], o_Pb[kMaxLevels], o_gsp[kMaxLevels];
+    size_t o_gb[kMaxLevels], o_Pb[kMaxLevels], o_gsp[kMaxLevels], o_A[kMaxLevels], o_PF[kMaxLevels],
+        o_Pe[kMaxLevels];
+    size_t A_q[kMaxLevels], PF_q[kMaxLevels], Pe_q[kMaxLevels];
     for (int l = 0; l < p->L; ++l) {
         const Level &lv = p->lv[l];
         o_gb[l] = lv.g_q ? take(8 * (size_t)qc * lv.g_q) : 0;
         o_Pb[l] = lv.P_q ? take(8 * (size_t)qc * lv.P_q) : 0;
         o_gsp[l] = (l >= 1 && lv.fft && lv.npairs > 0) ? take(16 * (size_t)qc * lv.spec_q) : 0;
+        // spectral levels: gbar spectra of nodes under a spectral parent level,
+        // folded Pbar spectra and ends of spectral levels below the root
+        A_q[l] = (l + 1 < p->L && p->lv[l + 1].kind == 2) ? (size_t)lv.nreal * (lv.deg + 1) : 0;
+        PF_q[l] = (lv.kind == 2 && l + 1 < p->L) ? (size_t)lv.nreal * (lv.deg / 2 + 1) : 0;
+        Pe_q[l] = PF_q[l] ? (size_t)lv.nreal * 2 : 0;
+        o_A[l] = A_q[l] ? take(16 * (size_t)qc * A_q[l]) : 0;
+        o_PF[l] = PF_q[l] ? take(16 * (size_t)qc * PF_q[l]) : 0;
+        o_Pe[l] = Pe_q[l] ? take(8 * (size_t)qc * Pe_q[l]) : 0;
     }
     const size_t o_bw = (p->k < p->B) ? take(8 * (size_t)qc * p->nblocks * p->B) : 0;
     if (!base) return off;
@@ -892,13 +904,21 @@ size_t vjp_level_layout(const Plan *p, int qc, char *base, VjpBufs *b) {
         b->gb_st[l] = lv.gst;
         b->Pb[l] = lv.P_q ? (double *)(base + o_Pb[l]) : nullptr;
         b->gspec[l] = o_gsp[l] ? (double2 *)(base + o_gsp[l]) : nullptr;
+        b->Gb2[l] = A_q[l] ? (double2 *)(base + o_A[l]) : nullptr;
+        b->Gb2_q[l] = A_q[l];
+        b->PF[l] = PF_q[l] ? (double2 *)(base + o_PF[l]) : nullptr;
+        b->PF_q[l] = PF_q[l];
+        b->Pe[l] = Pe_q[l] ? (double *)(base + o_Pe[l]) : nullptr;
+        b->Pe_q[l] = Pe_q[l];
     }
     return off;
 }
 
 VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t budget) {
-    // the adjoint buffers roughly double the tree's per-node memory
-    Plan *p = plan_create(n, S, k, nullptr, err, /*coeff_only=*/true, /*q_bytes_scale=*/2.2, budget);
+    // the adjoint buffers roughly double the tree's per-node memory; spectral
+    // levels as configured (vjp_spectral_min_degree < 0: all on coefficients)
+    Plan *p = plan_create(n, S, k, nullptr, err, /*coeff_only=*/g_config.vjp_spectral_min_degree < 0,
+                          /*q_bytes_scale=*/2.2, budget, /*vjp=*/true);
     if (!p) return nullptr;
     VjpPlan *v = new VjpPlan();
     v->p = p;
@@ -945,6 +965,9 @@ VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t
             if (c.gb[l]) c.gb[l] += h * b.gb_q[l];
             if (c.Pb[l]) c.Pb[l] += h * p->lv[l].P_q;
             if (c.gspec[l]) c.gspec[l] += h * p->lv[l].spec_q;
+            if (c.Gb2[l]) c.Gb2[l] += h * b.Gb2_q[l];
+            if (c.PF[l]) c.PF[l] += h * b.PF_q[l];
+            if (c.Pe[l]) c.Pe[l] += h * b.Pe_q[l];
         }
         if (c.blockW) c.blockW += h * p->nblocks * p->B;
         c.root += h * b.root_q;
@@ -960,7 +983,8 @@ VjpPlan *vjp_plan_create(int n, const double *S, int k, std::string &err, size_t
                   c.contrib == p->part[i].contrib && (L == 1 || c.root_acc == c.root);
         for (int l = 0; l < L; ++l)
             ok = ok && inside(c.gb[l], 8 * m * b.gb_q[l]) && inside(c.Pb[l], 8 * m * p->lv[l].P_q) &&
-                 inside(c.gspec[l], 16 * m * p->lv[l].spec_q);
+                 inside(c.gspec[l], 16 * m * p->lv[l].spec_q) && inside(c.Gb2[l], 16 * m * b.Gb2_q[l]) &&
+                 inside(c.PF[l], 16 * m * b.PF_q[l]) && inside(c.Pe[l], 8 * m * b.Pe_q[l]);
         if (!ok) {
             err = "internal: a VJP chunk view leaves the VJP arena";
             vjp_plan_destroy(v);
@@ -1225,6 +1249,10 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
     launch_leaf_up(adj_leaf_up_args(p, b), nq, q0, st);   // for L = 1 the single block is the root
     ++launches;
     for (int l = 1; l <= L - 1; ++l) {   // upward: the root's gbar is this chunk's dL/dpayout
+        if (p->lv[l].kind == 2) {
+            adj_spec_up(p, b, l, nq, q0, tw, logTW, launches);
+            continue;
+        }
         AdjUpFusedArgs F;
         AdjUpSchoolArgs Sa;
         adj_up_args(p, b, l, tw, logTW, F, Sa);
@@ -1243,6 +1271,10 @@ static void adjoint_chunk(VjpPlan *v, int q0, int nq, const double2 *tw, int log
         }
     }
     for (int l = L - 1; l >= 1; --l) {   // downward: Pbar of every level below the root
+        if (p->lv[l].kind == 2) {
+            adj_spec_down(p, b, l, nq, q0, tw, logTW, launches);
+            continue;
+        }
         AdjDownFusedArgs F;
         AdjDownSchoolArgs Sa;
         adj_down_args(p, b, l, tw, logTW, F, Sa);
@@ -1354,8 +1386,10 @@ int vjp_plan_enqueue(VjpPlan *v, int Q, const double *payout, const double *cot,
     }
     if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return -1; }
     int logNeed = 12, logTW = 0;
-    for (int l = 1; l < p->L; ++l)
+    for (int l = 1; l < p->L; ++l) {
         if (p->lv[l].fft) logNeed = std::max(logNeed, plan_ilog2(p->lv[l].fftn));
+        if (p->lv[l].kind == 2) logNeed = std::max(logNeed, plan_ilog2(2 * p->lv[l].deg));
+    }
     const double2 *tw = twiddles(logNeed, p->stream, err, &logTW);
     if (!tw) return -1;
     if (nact == 0) {

@@ -128,6 +128,17 @@ struct VjpBufs {
     const double *root_acc;      // what the payout gradient sums over nodes
     size_t root_acc_q;
     double *blockW;              // [qc][nblocks][B] full gbar of the leaf blocks when k < B
+    // spectral levels (vjp_spec.cu): gbar spectra DFT_{2 deg}(gbar) (deg + 1
+    // bins per node) of the nodes whose parent level is spectral; folded Pbar
+    // spectra DFT_{deg}(Pbar with Pbar[deg] added to Pbar[0]) (deg/2 + 1 bins)
+    // and Pbar's end coefficients (Pbar[0], Pbar[deg]) of spectral levels
+    // below the root
+    double2 *Gb2[kMaxLevels];
+    size_t Gb2_q[kMaxLevels];
+    double2 *PF[kMaxLevels];
+    size_t PF_q[kMaxLevels];
+    double *Pe[kMaxLevels];
+    size_t Pe_q[kMaxLevels];
 };
 
 struct VjpPlan {
@@ -191,6 +202,13 @@ void launch_packed_adj(WOp op, const void *desc, const int2 *slots, int nslots, 
                        cudaStream_t st);
 int adj_items_per_cta(int logN);
 void launch_accum_strided(int n, int nq, const double *src, size_t sq, double *acc, bool first, cudaStream_t st);
+// adjoint steps of a spectral level l (vjp_spec.cu): upward (the children's
+// gbar to the parents', converting coefficient gbar first where the level
+// below is not spectral) and downward (the parents' Pbar to the children's,
+// converting coefficient Pbar first where the level above is not spectral)
+void adj_spec_up(Plan *p, const VjpBufs &b, int l, int nq, int q0, const double2 *tw, int logTW, long &launches);
+void adj_spec_down(Plan *p, const VjpBufs &b, int l, int nq, int q0, const double2 *tw, int logTW, long &launches);
+void vjp_spec_set_smem_limits();
 void launch_node_reduce_members(int F, const longlong2 *mem, int nq, size_t sq, const double *pA, const double *pB,
                                 double *outA, double *outB, int Qs, int q0, cudaStream_t st);
 

@@ -57,7 +57,14 @@ int icm_last_status(void);
  *   disable_tma       1 = the four-step column pass of the largest levels
  *                     gathers its tile with ordinary loads instead of a
  *                     tensor-map (TMA) copy (same results; read when a run
- *                     is enqueued)                                           */
+ *                     is enqueued)
+ *   vjp_spectral_min_degree  levels of a single VJP plan (icm_gb300_vjp_*,
+ *                     icm_gb300_equity_vjp) whose children have at least this
+ *                     degree run spectrally, forward and adjoint (children
+ *                     untruncated at k, as for forward plans); 0 = the
+ *                     default (every level a forward plan would make
+ *                     spectral), -1 = every level on coefficients.  Batched
+ *                     VJPs keep their member trees on coefficients.            */
 typedef struct {
     int block_size;
     int fft_min_degree;
@@ -72,6 +79,7 @@ typedef struct {
     int chunk_streams;
     int cta_points;
     int disable_tma;
+    int vjp_spectral_min_degree;
 } IcmGb300Config;
 
 /* Set the process-wide engine configuration used by plans created
@@ -88,7 +96,8 @@ int icm_gb300_player_order(int n, const double *S, int *perm);
  * crossover (0 = the defaults), checked against the invariants the kernels
  * rely on (host only: FFT sizes cover every product and correlation without
  * wrap, spectral levels sit over untruncated children, truncation lengths
- * and strides).  flags: 1 = the VJP's coefficient-only geometry.  Returns 0
+ * and strides).  flags: 1 = every FFT level on coefficients, 2 = a single
+ * VJP plan's geometry (under vjp_spectral_min_degree).  Returns 0
  * when they hold (why: "kinds" and each parent level's kind from level 1 up,
  * 0 schoolbook, 1 FFT on coefficients, 2 spectral), 1 with the first
  * violation in why, -1 for bad arguments. */

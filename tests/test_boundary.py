@@ -190,11 +190,11 @@ def test_plan_geometry_invariants(built_lib):
         for k in ks:
             for B in ((8, 32) if big else (4, 8, 16, 32)):
                 for fm in ((16, 512) if big else (8, 16, 64, 512)):
-                    for flags in (0, 1):
+                    for flags in (0, 1, 2):
                         rc = L.icm_gb300_check_geometry(n, k, B, fm, flags, why, 256)
                         assert rc == 0, (n, k, B, fm, flags, why.value.decode())
                         checked += 1
-    assert checked > 1500
+    assert checked > 2250
     assert L.icm_gb300_check_geometry(5, 6, 8, 64, 0, why, 256) == -1
 
 
