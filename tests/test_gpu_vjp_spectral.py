@@ -76,6 +76,22 @@ def test_band_bottom_above_coefficient_levels(gpu_icm, min_degree):
     _close(got, ref, min_degree)
 
 
+@pytest.mark.parametrize("B", [4, 16, 32])
+def test_spectral_vjp_block_sizes(gpu_icm, B):
+    S, P, cot = _case(3000, 3000, 1.0, 31 + B)
+    got, ref = _pair(gpu_icm, S, P, cot, Q=48, block_size=B, fft_min_degree=16)
+    _close(got, ref, B)
+
+
+@pytest.mark.parametrize("k", [128, 129, 130, 256, 257, 513, 1025])
+def test_spectral_band_top_at_truncation_edges(gpu_icm, k):
+    """k at and around deg + 1 for the children degrees 128, 256, 512, 1024:
+    the band's top level moves by one level across each edge."""
+    S, P, cot = _case(4000, k, 1.0, 37 + k)
+    got, ref = _pair(gpu_icm, S, P, cot, Q=48, block_size=8, fft_min_degree=16)
+    _close(got, ref, k)
+
+
 def test_spectral_vjp_node_terms(gpu_icm):
     S, P, cot = _case(2500, 2500, 1.0, 11)
     got, ref = _pair(gpu_icm, S, P, cot, Q=64, node_terms=True, fft_min_degree=16)
