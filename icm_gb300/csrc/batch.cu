@@ -196,7 +196,7 @@ static void build_steps(Forest *f) {
                         FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], false, tw, logTW, &fq, &sm);
                         A.z.zp = zpre(p);
                         b.pack_items = lv[l].npairs;
-                        b.pack_cb = A.logN >= 13 ? 1 : 4096 >> A.logN;
+                        b.pack_cb = A.cb;   // items per CTA of the fused kernels
                         b.add(WOp::FusedBuild, 2 * A.logN, "wl_fused_build", A, sm, fq, 0, t, lv[l].deg, lv[l].nreal);
                         b.pack_items = 0;
                     }
@@ -214,7 +214,7 @@ static void build_steps(Forest *f) {
                 // the root: child spectra for its propagate only
                 FusedBuildArgs A = fused_build_args(lv[l - 1], lv[l], true, tw, logTW, &fq, &sm);
                 b.pack_items = lv[l].npairs;
-                b.pack_cb = A.logN >= 13 ? 1 : 4096 >> A.logN;
+                b.pack_cb = A.cb;   // items per CTA of the fused kernels
                 b.add(WOp::FusedBuild, 2 * A.logN + 1, "wl_fused_spectra", A, sm, fq);
                 b.pack_items = 0;
             }
@@ -283,7 +283,7 @@ static void build_steps(Forest *f) {
                                                       &sm);
                     A.z.zp = zpre(p);
                     b.pack_items = lv[l].npairs;
-                    b.pack_cb = A.logN >= 13 ? 1 : 4096 >> A.logN;
+                    b.pack_cb = A.cb;   // items per CTA of the fused kernels
                     b.add(WOp::FusedProp, A.logN, "wl_fused_prop", A, sm, fq, 0, t, root ? 0 : lv[l].deg, lv[l].nreal);
                     b.pack_items = 0;
                 }
