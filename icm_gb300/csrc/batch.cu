@@ -187,7 +187,7 @@ static void build_steps(Forest *f) {
                     SpecBuildArgs A = spec_build_args(lv[l - 1], lv[l], lv[l + 1].kind != 2, tw, logTW, &fq, &sm);
                     A.z.zp = zpre(p);
                     b.pack_items = lv[l].nreal;   // items of different members share CTAs
-                    b.pack_cb = A.logD >= 12 ? 1 : 4096 >> A.logD;
+                    b.pack_cb = A.cb;   // items per CTA of the spectral work lists
                     b.add(WOp::SpecBuild, 2 * A.logD + (A.pspec ? 1 : 0), "wl_spec_build", A, sm, fq, 0, t, lv[l].deg,
                           lv[l].nreal);
                     b.pack_items = 0;
@@ -273,7 +273,7 @@ static void build_steps(Forest *f) {
                                                 l - 1 >= 1 && lv[l - 1].kind == 2, nullptr, tw, logTW, &fq, &sm);
                 A.z.zp = zpre(p);
                 b.pack_items = lv[l].nreal;
-                b.pack_cb = A.logD >= 12 ? 1 : 4096 >> A.logD;
+                b.pack_cb = A.cb;   // items per CTA of the spectral work lists
                 b.add(WOp::SpecProp, 2 * A.logD + (A.Gout ? 1 : 0), "wl_spec_prop", A, sm, fq, 0, t,
                       root ? 0 : lv[l].deg, lv[l].nreal);
                 b.pack_items = 0;

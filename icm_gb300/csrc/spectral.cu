@@ -43,7 +43,9 @@ static inline int ilog2s(long v) {
     while ((1L << l) < v) ++l;
     return l;
 }
-static inline int spec_cb(int M) { return M >= 4096 ? 1 : 4096 / M; }
+// complex points per CTA of the work-list launches (batches): items = kSpecPts / M
+constexpr int kSpecPts = 2048;
+__host__ __device__ __forceinline__ int spec_cb(int M) { return M >= kSpecPts ? 1 : kSpecPts / M; }
 // items per CTA of a single plan's launch for a level with `pts` complex points
 // per CTA (0: 4096); never more points than spec_cb's largest CTA (8192)
 static inline int pts_cb(int pts, int M) {
@@ -312,7 +314,7 @@ __device__ void spec_build_packed(const SpecBuildArgs *__restrict__ Dsc, const i
     extern __shared__ double2 sm[];
     const SpecBuildArgs &A0 = Dsc[slots[0].x];
     const int D = 1 << A0.logD;
-    const int cb = D >= 4096 ? 1 : 4096 / D;
+    const int cb = spec_cb(D);
     const int s0 = bx * cb;
     const int cnt = min(cb, nslots - s0);
     if (cnt <= 0) return;
@@ -562,7 +564,7 @@ __device__ void spec_prop_packed(const SpecPropArgs *__restrict__ Dsc, const int
     extern __shared__ double2 sm[];
     const SpecPropArgs &A0 = Dsc[slots[0].x];
     const int D = 1 << A0.logD;
-    const int cbp = D >= 4096 ? 1 : 4096 / D;
+    const int cbp = spec_cb(D);
     const int s0 = bx * cbp;
     const int cnt = min(cbp, nslots - s0);
     if (cnt <= 0) return;
