@@ -59,8 +59,10 @@ double now_ns() {
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 }  // namespace
 
-__device__ __forceinline__ int vjp_cb(int N) { return N >= 8192 ? 1 : 4096 / N; }
-static inline int vjp_cb_h(int N) { return N >= 8192 ? 1 : 4096 / N; }
+// complex points per CTA of the one-kernel adjoint FFT steps (items = kVjpPts / N)
+constexpr int kVjpPts = 2048;
+__host__ __device__ __forceinline__ int vjp_cb(int N) { return N >= kVjpPts ? 1 : kVjpPts / N; }
+static inline int vjp_cb_h(int N) { return vjp_cb(N); }
 static inline int vjp_tpb(size_t smem) { return smem > kOneCtaSmem ? kVjpThreadsMax : kVjpThreads; }
 // Every pair of a CTA is described by a view staged in shared memory after
 // the transforms, so a CTA may hold pairs of different tournaments (packed
