@@ -537,8 +537,9 @@ def configure(block_size=0, fft_min_degree=0, q_chunk=0, max_device_bytes=0, coe
     table's per-level choice, else 4096; same results); tma=False makes the
     four-step column pass of the largest levels gather its tile with ordinary
     loads instead of a TMA tensor copy (same results);
-    vjp_spectral_min_degree: levels of a single VJP plan whose children have
-    at least this degree run spectrally in the forward and adjoint passes
+    vjp_spectral_min_degree: levels of a VJP (single or batched) whose
+    children have at least this degree run spectrally in the forward and
+    adjoint passes
     (0 = every level a forward plan would make spectral, -1 = all on
     coefficients; results agree to rounding)."""
     engines = {"auto": 0, "tree": 1, "linear": 2}

@@ -306,10 +306,25 @@ static void build_steps(Forest *f) {
         for (int t = 0; t < T; ++t)
             u.add(WOp::AdjLeafUp, f->tr[t]->B, "wl_adj_leaf_up", adj_leaf_up_args(f->tr[t], f->vb[t]), 0, 0.0);
         for (int l = 1; l < Lmax; ++l) {
+            // spectral levels over coefficient children: the children's gbar as spectra first
+            PhaseBuilder &cv = phase();
+            for (int t = 0; t < T; ++t) {
+                Plan *p = f->tr[t];
+                if (l > p->L - 1 || p->lv[l].kind != 2 || p->lv[l - 1].kind == 2) continue;
+                size_t sm = 0;
+                const VspRealArgs R = vsp_gbar_real_args(p, f->vb[t], l, 0, tw, logTW, &sm);
+                cv.add(WOp::AdjSpecReal, R.logM, "wl_adj_spec_real", R, sm, 0.0);
+            }
             PhaseBuilder &b = phase();
             for (int t = 0; t < T; ++t) {
                 Plan *p = f->tr[t];
                 if (l > p->L - 1) continue;
+                if (p->lv[l].kind == 2) {   // spectral level: the adjoint in the frequency domain
+                    size_t sm = 0;
+                    const VspUpArgs A = vsp_up_args(p, f->vb[t], l, 0, tw, logTW, &sm);
+                    b.add(WOp::AdjSpecUp, A.logD, "wl_adj_spec_up", A, sm, 0.0);
+                    continue;
+                }
                 AdjUpFusedArgs F;
                 AdjUpSchoolArgs Sa;
                 adj_up_args(p, f->vb[t], l, tw, logTW, F, Sa);
@@ -321,10 +336,25 @@ static void build_steps(Forest *f) {
             }
         }
         for (int l = Lmax - 1; l >= 1; --l) {
+            // spectral levels under a coefficient level: the parents' Pbar as folded spectra first
+            PhaseBuilder &cv = phase();
+            for (int t = 0; t < T; ++t) {
+                Plan *p = f->tr[t];
+                if (l >= p->L - 1 || p->lv[l].kind != 2 || p->lv[l + 1].kind == 2) continue;
+                size_t sm = 0;
+                const VspRealArgs R = vsp_pbar_real_args(p, f->vb[t], l, 0, tw, logTW, &sm);
+                cv.add(WOp::AdjSpecReal, R.logM, "wl_adj_spec_real", R, sm, 0.0);
+            }
             PhaseBuilder &b = phase();
             for (int t = 0; t < T; ++t) {
                 Plan *p = f->tr[t];
                 if (l > p->L - 1) continue;
+                if (p->lv[l].kind == 2) {
+                    size_t sm = 0;
+                    const VspDownArgs A = vsp_down_args(p, f->vb[t], l, 0, tw, logTW, &sm);
+                    b.add(WOp::AdjSpecDown, 2 * A.logD + (A.PFout ? 1 : 0), "wl_adj_spec_down", A, sm, 0.0);
+                    continue;
+                }
                 AdjDownFusedArgs F;
                 AdjDownSchoolArgs Sa;
                 adj_down_args(p, f->vb[t], l, tw, logTW, F, Sa);
@@ -458,6 +488,9 @@ static void launch_step(Forest *f, const WStep &s, int nq, int q0) {
         case WOp::AdjLeafDown:
             launch_worklist_adj(s.op, s.key, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream);
             break;
+        case WOp::AdjSpecReal:
+        case WOp::AdjSpecUp:
+        case WOp::AdjSpecDown: launch_worklist_vsp(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
         default: launch_worklist_spec(s.op, s.d_desc, s.d_tab, nctas, qn, q0, s.smem, f->stream); break;
     }
     f->prof.end(f->stream);
@@ -517,7 +550,9 @@ Forest *forest_create(int T, const int *n, const int *k, const double *S, std::s
     std::vector<std::string> errs(T);
     parallel_for(T, [&](int t) {
         Plan *p = new Plan();
-        p->coeff_only = vjp;   // the adjoint passes work on coefficients
+        // adjoint forests: member trees under a single VJP plan's rules
+        p->vjp = vjp;
+        p->coeff_only = vjp && g_config.vjp_spectral_min_degree < 0;
         if (plan_geometry(p, n[t], S + ioff[t], k[t], errs[t]) != 0) {
             delete p;
             p = nullptr;

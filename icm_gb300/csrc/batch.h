@@ -66,8 +66,9 @@ struct Forest {
     double last_device_ms = 0.0;
     Prof prof;
     std::vector<Plan::KStat> kstats;
-    // adjoint forests: coefficient-level member trees, forward without the
-    // divide, then the adjoint passes as work lists; d_acc sums dL/dS
+    // adjoint forests: member trees under the single VJP plan's level rules,
+    // forward without the divide, then the adjoint passes as work lists;
+    // d_acc sums dL/dS
     bool vjp = false;
     bool node_terms = false;          // the mode the steps were built for
     std::vector<VjpBufs> vb;          // per member adjoint buffers

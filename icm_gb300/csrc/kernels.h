@@ -240,7 +240,8 @@ FusedPropArgs fused_prop_args(const double *gp, size_t gp_q, int gst_p, int gpl,
 // block within the descriptor), blockIdx.y = node within the chunk.
 enum class WOp : int {
     Leaf, SchoolBuild, SchoolProp, Divide, SpecInit, SpecBuild, Gspec, SpecProp, FusedBuild, FusedProp, SubBuild, SubProp,
-    AdjLeafUp, AdjUpSchool, AdjUpFused, AdjDownSchool, AdjDownFused, AdjLeafDown, Small, Linear
+    AdjLeafUp, AdjUpSchool, AdjUpFused, AdjDownSchool, AdjDownFused, AdjLeafDown, Small, Linear,
+    AdjSpecReal, AdjSpecUp, AdjSpecDown
 };
 // B: leaf block size of the launch (Leaf and Divide lists are keyed by it)
 void launch_worklist_basic(WOp op, int B, const void *desc, const int2 *tab, int nctas, int nq, int q0,

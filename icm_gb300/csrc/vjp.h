@@ -202,6 +202,88 @@ void launch_packed_adj(WOp op, const void *desc, const int2 *slots, int nslots, 
                        cudaStream_t st);
 int adj_items_per_cta(int logN);
 void launch_accum_strided(int n, int nq, const double *src, size_t sq, double *acc, bool first, cudaStream_t st);
+// ---- argument blocks of the spectral adjoint steps (vjp_spec.cu), one
+// tournament level each (single plans launch (nbx, nq) grids, batches work
+// lists of (descriptor, block))
+// real sequences of length 2M (node coefficients) -> DFT_{2M} bins 0..M
+struct VspRealArgs {
+    const double *x;   // row j at x + q x_q + j xst; xlen entries used
+    size_t x_q;
+    int xst, xlen, nreal, logM;
+    int fold;          // add x[2M] onto x[0] (the folded spectrum of a degree-2M row)
+    double2 *out;      // M + 1 bins per node
+    size_t o_q;
+    double *ends;      // (x[0], x[2M]) per node, or null
+    size_t e_q;
+    const double2 *tw;
+    int logTW;
+    ZeroPrefix z;      // span: the nodes' degree (wholly-zero nodes: zeros)
+    int cb, nbx;       // nodes per CTA, CTAs per chunk node
+};
+
+struct VspUpArgs {
+    const double2 *A;   // children's gbar spectra, D + 1 bins per node
+    size_t A_q;
+    const double2 *S;   // children's spec2 (forward build)
+    size_t S_q;
+    int nreal_c, nreal_p, logD;
+    double2 *Aout;      // parents' gbar spectra (2D + 1 bins), or null: coefficients
+    size_t Ao_q;
+    double *gout;       // parents' gbar coefficients (glen entries, zero to gst)
+    size_t go_q;
+    int gst, glen;
+    double2 *buf;       // multi-pass levels: nreal_p x D complex per chunk node
+    const double2 *tw;
+    int logTW;
+    ZeroPrefix z;       // span: the parents' degree
+    int cb, nbx;        // parents per CTA, CTAs per chunk node
+};
+
+struct VspDownArgs {
+    const double2 *G;   // parents' g spectra, D + 1 bins (G_q = 0: one shared row, the root's)
+    size_t G_q;
+    const double2 *PF;  // parents' folded Pbar spectra, D + 1 bins, or null (the root: Pbar = 0)
+    size_t PF_q;
+    const double *Pe;   // parents' Pbar ends (Pbar[0], Pbar[2D])
+    size_t Pe_q;
+    const double2 *A;   // children's gbar spectra, D + 1 bins
+    size_t A_q;
+    const double2 *S;   // children's spec2
+    size_t S_q;
+    const double *E;    // children's ends (P[0], P[D])
+    size_t E_q;
+    int nreal_c, logD;
+    double2 *PFout;     // children's folded Pbar spectra (D/2 + 1 bins) and ends, or null
+    size_t PFo_q;
+    double *Peout;
+    size_t Peo_q;
+    double *Pout;       // children's Pbar coefficients (D + 1 entries, zero to pst)
+    size_t Po_q;
+    int pst;
+    double2 *buf;       // multi-pass levels: nreal_c x D/2 complex per chunk node
+    const double2 *tw;
+    int logTW;
+    ZeroPrefix z;       // span: the children's degree (wholly-zero children are skipped)
+    int cb, nbx;        // children per CTA, CTAs per chunk node
+};
+
+
+// argument blocks of level l's steps for plan p and its adjoint buffers b:
+// the conversion of the children's coefficient gbar to spectra (the band's
+// bottom), the upward step, the conversion of the parents' coefficient Pbar
+// (the band's top), the downward step; *smem: dynamic shared memory of a CTA
+VspRealArgs vsp_gbar_real_args(const Plan *p, const VjpBufs &b, int l, int q0, const double2 *tw, int logTW,
+                               size_t *smem);
+VspUpArgs vsp_up_args(const Plan *p, const VjpBufs &b, int l, int q0, const double2 *tw, int logTW, size_t *smem);
+VspRealArgs vsp_pbar_real_args(const Plan *p, const VjpBufs &b, int l, int q0, const double2 *tw, int logTW,
+                               size_t *smem);
+VspDownArgs vsp_down_args(const Plan *p, const VjpBufs &b, int l, int q0, const double2 *tw, int logTW, size_t *smem);
+// true: the level's steps run in one CTA (work lists hold no multi-pass levels)
+bool vsp_one_cta(const Plan *p, int l);
+// work lists of the spectral adjoint steps (AdjSpecReal, AdjSpecUp, AdjSpecDown)
+void launch_worklist_vsp(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                         cudaStream_t st);
+
 // adjoint steps of a spectral level l (vjp_spec.cu): upward (the children's
 // gbar to the parents', converting coefficient gbar first where the level
 // below is not spectral) and downward (the parents' Pbar to the children's,

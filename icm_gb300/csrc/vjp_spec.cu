@@ -77,69 +77,6 @@ __device__ __forceinline__ int vsp_partition(int *idx, int cnt, const ZeroPrefix
     return nh_s;
 }
 
-// ------------------------------------------------------------ arguments
-// real sequences of length 2M (node coefficients) -> DFT_{2M} bins 0..M
-struct VspRealArgs {
-    const double *x;   // row j at x + q x_q + j xst; xlen entries used
-    size_t x_q;
-    int xst, xlen, nreal, logM;
-    int fold;          // add x[2M] onto x[0] (the folded spectrum of a degree-2M row)
-    double2 *out;      // M + 1 bins per node
-    size_t o_q;
-    double *ends;      // (x[0], x[2M]) per node, or null
-    size_t e_q;
-    const double2 *tw;
-    int logTW;
-    ZeroPrefix z;      // span: the nodes' degree (wholly-zero nodes: zeros)
-    int cb;
-};
-
-struct VspUpArgs {
-    const double2 *A;   // children's gbar spectra, D + 1 bins per node
-    size_t A_q;
-    const double2 *S;   // children's spec2 (forward build)
-    size_t S_q;
-    int nreal_c, nreal_p, logD;
-    double2 *Aout;      // parents' gbar spectra (2D + 1 bins), or null: coefficients
-    size_t Ao_q;
-    double *gout;       // parents' gbar coefficients (glen entries, zero to gst)
-    size_t go_q;
-    int gst, glen;
-    double2 *buf;       // multi-pass levels: nreal_p x D complex per chunk node
-    const double2 *tw;
-    int logTW;
-    ZeroPrefix z;       // span: the parents' degree
-    int cb;
-};
-
-struct VspDownArgs {
-    const double2 *G;   // parents' g spectra, D + 1 bins (G_q = 0: one shared row, the root's)
-    size_t G_q;
-    const double2 *PF;  // parents' folded Pbar spectra, D + 1 bins, or null (the root: Pbar = 0)
-    size_t PF_q;
-    const double *Pe;   // parents' Pbar ends (Pbar[0], Pbar[2D])
-    size_t Pe_q;
-    const double2 *A;   // children's gbar spectra, D + 1 bins
-    size_t A_q;
-    const double2 *S;   // children's spec2
-    size_t S_q;
-    const double *E;    // children's ends (P[0], P[D])
-    size_t E_q;
-    int nreal_c, logD;
-    double2 *PFout;     // children's folded Pbar spectra (D/2 + 1 bins) and ends, or null
-    size_t PFo_q;
-    double *Peout;
-    size_t Peo_q;
-    double *Pout;       // children's Pbar coefficients (D + 1 entries, zero to pst)
-    size_t Po_q;
-    int pst;
-    double2 *buf;       // multi-pass levels: nreal_c x D/2 complex per chunk node
-    const double2 *tw;
-    int logTW;
-    ZeroPrefix z;       // span: the children's degree (wholly-zero children are skipped)
-    int cb;             // children per CTA
-};
-
 // one child of the downward step: the operands of Z = G conj(A_sib) + PF conj(S_sib)
 struct DnView {
     const double2 *G, *PF, *As, *Ss;   // null As: no sibling gbar; null Ss: sibling 1; null PF: Pbar_X = 0
@@ -214,11 +151,10 @@ __device__ __forceinline__ void odd_bins(double2 a, double2 bc, int f, const dou
 }
 
 // ------------------------------------------------------------ one-CTA kernels
-__global__ void __launch_bounds__(kVspThreadsMax) k_vsp_real(VspRealArgs A) {
+__device__ void vsp_real_body(const VspRealArgs &A, int bx, int q) {
     extern __shared__ double2 sm[];
-    const int q = blockIdx.y;
     const int M = 1 << A.logM;
-    const int j0 = blockIdx.x * A.cb;
+    const int j0 = bx * A.cb;
     const int cnt = min(A.cb, A.nreal - j0);
     if (cnt <= 0) return;
     int *idx = reinterpret_cast<int *>(sm + (size_t)A.cb * M);
@@ -262,11 +198,10 @@ __global__ void __launch_bounds__(kVspThreadsMax) k_vsp_real(VspRealArgs A) {
     }
 }
 
-__global__ void __launch_bounds__(kVspThreadsMax) k_vsp_up(VspUpArgs A) {
+__device__ void vsp_up_body(const VspUpArgs &A, int bx, int q) {
     extern __shared__ double2 sm[];
-    const int q = blockIdx.y;
     const int D = 1 << A.logD, hD = D >> 1;
-    const int j0 = blockIdx.x * A.cb;
+    const int j0 = bx * A.cb;
     const int cnt = min(A.cb, A.nreal_p - j0);
     if (cnt <= 0) return;
     int *idx = reinterpret_cast<int *>(sm + (size_t)A.cb * D);
@@ -328,13 +263,12 @@ __global__ void __launch_bounds__(kVspThreadsMax) k_vsp_up(VspUpArgs A) {
     }
 }
 
-__global__ void __launch_bounds__(kVspThreadsMax) k_vsp_down(VspDownArgs A) {
+__device__ void vsp_down_body(const VspDownArgs &A, int bx, int q) {
     extern __shared__ double2 sm[];
-    const int q = blockIdx.y;
     const int D = 1 << A.logD, h = D >> 1, lh = A.logD - 1;
     const bool spec = A.PFout != nullptr;
     const int per = spec ? h : D;   // complex points per child
-    const int c0 = blockIdx.x * A.cb;
+    const int c0 = bx * A.cb;
     const int cnt = min(A.cb, A.nreal_c - c0);
     if (cnt <= 0) return;
     DnView *V = reinterpret_cast<DnView *>(sm + (size_t)A.cb * per);
@@ -455,6 +389,33 @@ __global__ void __launch_bounds__(kVspThreadsMax) k_vsp_down(VspDownArgs A) {
         const double2 val = (f < h) ? sm[(size_t)it * h + f] : v.pfh;
         A.PFout[q * A.PFo_q + (size_t)v.c * (h + 1) + f] = make_double2(val.x + v.delta, val.y);
     }
+}
+
+// single plans: grid (nbx, nq); work lists: CTA i runs block tab[i].y of
+// descriptor tab[i].x (members of a batch, one level each)
+__global__ void __launch_bounds__(kVspThreadsMax) k_vsp_real(VspRealArgs A) { vsp_real_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kVspThreadsMax) k_vsp_up(VspUpArgs A) { vsp_up_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kVspThreadsMax) k_vsp_down(VspDownArgs A) { vsp_down_body(A, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(kVspThreadsMax)
+kw_vsp_real(const VspRealArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    VspRealArgs A = D[t.x];
+    A.z.q0 = q0;
+    vsp_real_body(A, t.y, blockIdx.y);
+}
+__global__ void __launch_bounds__(kVspThreadsMax)
+kw_vsp_up(const VspUpArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    VspUpArgs A = D[t.x];
+    A.z.q0 = q0;
+    vsp_up_body(A, t.y, blockIdx.y);
+}
+__global__ void __launch_bounds__(kVspThreadsMax)
+kw_vsp_down(const VspDownArgs *__restrict__ D, const int2 *__restrict__ tab, int q0) {
+    const int2 t = tab[blockIdx.x];
+    VspDownArgs A = D[t.x];
+    A.z.q0 = q0;
+    vsp_down_body(A, t.y, blockIdx.y);
 }
 
 // ------------------------------------------------------------ multi-pass kernels
@@ -617,15 +578,163 @@ void vjp_spec_set_smem_limits() {
     cudaFuncSetAttribute(k_vsp_real, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_vsp_up, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_vsp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_vsp_real, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_vsp_up, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kw_vsp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+static size_t real_smem(int M, int cb) { return (size_t)cb * M * sizeof(double2) + (size_t)cb * sizeof(int); }
+static size_t up_smem(int D, int cb) { return (size_t)cb * D * sizeof(double2) + (size_t)cb * sizeof(int); }
+static size_t down_smem(int per, int cb) {
+    return (size_t)cb * per * sizeof(double2) + (size_t)cb * (sizeof(DnView) + sizeof(int));
+}
+
+bool vsp_one_cta(const Plan *p, int l) {
+    const long D = p->lv[l - 1].deg;
+    return D <= kSpecMaxD;
+}
+
+VspRealArgs vsp_gbar_real_args(const Plan *p, const VjpBufs &b, int l, int q0, const double2 *tw, int logTW,
+                               size_t *smem) {
+    const Level &c = p->lv[l - 1];
+    VspRealArgs R{};
+    R.x = b.gb[l - 1];
+    R.x_q = b.gb_q[l - 1];
+    R.xst = b.gb_st[l - 1];
+    R.xlen = c.glen;
+    R.nreal = c.nreal;
+    R.logM = ilog2v(c.deg);
+    R.out = b.Gb2[l - 1];
+    R.o_q = b.Gb2_q[l - 1];
+    R.tw = tw;
+    R.logTW = logTW;
+    R.z = ZeroPrefix{p->zskip ? p->d_z : nullptr, q0, c.deg};
+    R.cb = vsp_cb(1 << R.logM);
+    R.nbx = (int)nbv(R.nreal, R.cb);
+    if (smem) *smem = real_smem(1 << R.logM, R.cb);
+    return R;
+}
+
+VspRealArgs vsp_pbar_real_args(const Plan *p, const VjpBufs &b, int l, int q0, const double2 *tw, int logTW,
+                               size_t *smem) {
+    const Level &c = p->lv[l - 1], &pl = p->lv[l];
+    VspRealArgs R{};
+    R.x = b.Pb[l];
+    R.x_q = pl.P_q;
+    R.xst = pl.pst;
+    R.xlen = pl.plen;
+    R.nreal = pl.nreal;
+    R.logM = ilog2v(c.deg);
+    R.fold = 1;
+    R.out = b.PF[l];
+    R.o_q = b.PF_q[l];
+    R.ends = b.Pe[l];
+    R.e_q = b.Pe_q[l];
+    R.tw = tw;
+    R.logTW = logTW;
+    R.z = ZeroPrefix{p->zskip ? p->d_z : nullptr, q0, pl.deg};
+    R.cb = vsp_cb(1 << R.logM);
+    R.nbx = (int)nbv(R.nreal, R.cb);
+    if (smem) *smem = real_smem(1 << R.logM, R.cb);
+    return R;
+}
+
+VspUpArgs vsp_up_args(const Plan *p, const VjpBufs &b, int l, int q0, const double2 *tw, int logTW, size_t *smem) {
+    const Level &c = p->lv[l - 1], &pl = p->lv[l];
+    const bool root = (l == p->L - 1);
+    const bool spec_out = !root && p->lv[l + 1].kind == 2;
+    VspUpArgs A{};
+    A.A = b.Gb2[l - 1];
+    A.A_q = b.Gb2_q[l - 1];
+    A.S = c.spec2;
+    A.S_q = c.spec2_q;
+    A.nreal_c = c.nreal;
+    A.nreal_p = pl.nreal;
+    A.logD = ilog2v(c.deg);
+    if (spec_out) {
+        A.Aout = b.Gb2[l];
+        A.Ao_q = b.Gb2_q[l];
+    } else {
+        A.gout = root ? b.root : b.gb[l];
+        A.go_q = root ? b.root_q : b.gb_q[l];
+        A.gst = root ? b.kst : b.gb_st[l];
+        A.glen = root ? p->k : pl.glen;
+    }
+    A.tw = tw;
+    A.logTW = logTW;
+    A.z = ZeroPrefix{p->zskip ? p->d_z : nullptr, q0, pl.deg};
+    A.cb = vsp_cb(1 << A.logD);
+    A.nbx = (int)nbv(A.nreal_p, A.cb);
+    if (smem) *smem = up_smem(1 << A.logD, A.cb);
+    return A;
+}
+
+VspDownArgs vsp_down_args(const Plan *p, const VjpBufs &b, int l, int q0, const double2 *tw, int logTW,
+                          size_t *smem) {
+    const Level &c = p->lv[l - 1], &pl = p->lv[l];
+    const bool root = (l == p->L - 1);
+    VspDownArgs A{};
+    A.G = pl.G;
+    A.G_q = root ? 0 : pl.G_q;
+    if (!root) {
+        A.PF = b.PF[l];
+        A.PF_q = b.PF_q[l];
+        A.Pe = b.Pe[l];
+        A.Pe_q = b.Pe_q[l];
+    }
+    A.A = b.Gb2[l - 1];
+    A.A_q = b.Gb2_q[l - 1];
+    A.S = c.spec2;
+    A.S_q = c.spec2_q;
+    A.E = c.ends;
+    A.E_q = c.ends_q;
+    A.nreal_c = c.nreal;
+    A.logD = ilog2v(c.deg);
+    const bool spec_out = c.kind == 2;
+    if (spec_out) {
+        A.PFout = b.PF[l - 1];
+        A.PFo_q = b.PF_q[l - 1];
+        A.Peout = b.Pe[l - 1];
+        A.Peo_q = b.Pe_q[l - 1];
+    } else {
+        A.Pout = b.Pb[l - 1];
+        A.Po_q = c.P_q;
+        A.pst = c.pst;
+    }
+    A.tw = tw;
+    A.logTW = logTW;
+    A.z = ZeroPrefix{p->zskip ? p->d_z : nullptr, q0, c.deg};
+    const int per = spec_out ? (1 << A.logD) / 2 : (1 << A.logD);
+    A.cb = vsp_cb(per);
+    A.nbx = (int)nbv(A.nreal_c, A.cb);
+    if (smem) *smem = down_smem(per, A.cb);
+    return A;
+}
+
+void launch_worklist_vsp(WOp op, const void *desc, const int2 *tab, int nctas, int nq, int q0, size_t smem,
+                         cudaStream_t st) {
+    if (nctas <= 0 || nq <= 0) return;
+    const dim3 g(nctas, nq);
+    switch (op) {
+        case WOp::AdjSpecReal:
+            kw_vsp_real<<<g, vsp_tpb(smem), smem, st>>>((const VspRealArgs *)desc, tab, q0);
+            break;
+        case WOp::AdjSpecUp: kw_vsp_up<<<g, vsp_tpb(smem), smem, st>>>((const VspUpArgs *)desc, tab, q0); break;
+        case WOp::AdjSpecDown:
+            kw_vsp_down<<<g, vsp_tpb(smem), smem, st>>>((const VspDownArgs *)desc, tab, q0);
+            break;
+        default: break;
+    }
 }
 
 static void launch_real(const VspRealArgs &R0, int nq, cudaStream_t st, Prof *pr, long &launches) {
     VspRealArgs R = R0;
     const int M = 1 << R.logM;
     R.cb = short_grid_cb(vsp_cb(M), R.nreal, nq);
-    const size_t sm = (size_t)R.cb * M * sizeof(double2) + (size_t)R.cb * sizeof(int);
+    R.nbx = (int)nbv(R.nreal, R.cb);
+    const size_t sm = real_smem(M, R.cb);
     pr->begin("adj_spec_real", (5.0 * M * R.logM + 20.0 * M) * R.nreal * nq, st);
-    k_vsp_real<<<dim3(nbv(R.nreal, R.cb), nq), vsp_tpb(sm), sm, st>>>(R);
+    k_vsp_real<<<dim3(R.nbx, nq), vsp_tpb(sm), sm, st>>>(R);
     pr->end(st);
     ++launches;
 }
@@ -638,47 +747,16 @@ void adj_spec_up(Plan *p, const VjpBufs &b, int l, int nq, int q0, const double2
     const int *zp = p->zskip ? p->d_z : nullptr;
     cudaStream_t st = p->stream;
     Prof *pr = &p->prof;
-    if (c.kind != 2) {   // the children's gbar as spectra (the band's bottom; D <= kSpecMaxD)
-        VspRealArgs R{};
-        R.x = b.gb[l - 1];
-        R.x_q = b.gb_q[l - 1];
-        R.xst = b.gb_st[l - 1];
-        R.xlen = c.glen;
-        R.nreal = c.nreal;
-        R.logM = logD;
-        R.out = b.Gb2[l - 1];
-        R.o_q = b.Gb2_q[l - 1];
-        R.tw = tw;
-        R.logTW = logTW;
-        R.z = ZeroPrefix{zp, q0, c.deg};
-        launch_real(R, nq, st, pr, launches);
-    }
-    VspUpArgs A{};
-    A.A = b.Gb2[l - 1];
-    A.A_q = b.Gb2_q[l - 1];
-    A.S = c.spec2;
-    A.S_q = c.spec2_q;
-    A.nreal_c = c.nreal;
-    A.nreal_p = pl.nreal;
-    A.logD = logD;
-    if (spec_out) {
-        A.Aout = b.Gb2[l];
-        A.Ao_q = b.Gb2_q[l];
-    } else {
-        A.gout = root ? b.root : b.gb[l];
-        A.go_q = root ? b.root_q : b.gb_q[l];
-        A.gst = root ? b.kst : b.gb_st[l];
-        A.glen = root ? p->k : pl.glen;
-    }
-    A.tw = tw;
-    A.logTW = logTW;
-    A.z = ZeroPrefix{zp, q0, pl.deg};
+    if (c.kind != 2)   // the children's gbar as spectra (the band's bottom; D <= kSpecMaxD)
+        launch_real(vsp_gbar_real_args(p, b, l, q0, tw, logTW, nullptr), nq, st, pr, launches);
+    VspUpArgs A = vsp_up_args(p, b, l, q0, tw, logTW, nullptr);
     const double fl = (spec_out ? 10.0 * D * logD + 40.0 * D : 5.0 * D * logD + 20.0 * D) * pl.nreal * nq;
-    if (D <= kSpecMaxD) {
-        A.cb = short_grid_cb(vsp_cb(D), pl.nreal, nq);
-        const size_t sm = (size_t)A.cb * D * sizeof(double2) + (size_t)A.cb * sizeof(int);
+    if (vsp_one_cta(p, l)) {
+        A.cb = short_grid_cb(A.cb, pl.nreal, nq);
+        A.nbx = (int)nbv(pl.nreal, A.cb);
+        const size_t sm = up_smem(D, A.cb);
         pr->begin("adj_spec_up", fl, st);
-        k_vsp_up<<<dim3(nbv(pl.nreal, A.cb), nq), vsp_tpb(sm), sm, st>>>(A);
+        k_vsp_up<<<dim3(A.nbx, nq), vsp_tpb(sm), sm, st>>>(A);
         pr->end(st);
         ++launches;
         return;
@@ -708,68 +786,24 @@ void adj_spec_up(Plan *p, const VjpBufs &b, int l, int nq, int q0, const double2
 }
 
 void adj_spec_down(Plan *p, const VjpBufs &b, int l, int nq, int q0, const double2 *tw, int logTW, long &launches) {
-    const Level &c = p->lv[l - 1], &pl = p->lv[l];
+    const Level &c = p->lv[l - 1];
     const bool root = (l == p->L - 1);
     const int logD = ilog2v(c.deg), D = 1 << logD, h = D / 2;
     const int *zp = p->zskip ? p->d_z : nullptr;
     cudaStream_t st = p->stream;
     Prof *pr = &p->prof;
-    if (!root && p->lv[l + 1].kind != 2) {   // the parents' Pbar as folded spectra (the band's top; D <= kSpecMaxD)
-        VspRealArgs R{};
-        R.x = b.Pb[l];
-        R.x_q = pl.P_q;
-        R.xst = pl.pst;
-        R.xlen = pl.plen;
-        R.nreal = pl.nreal;
-        R.logM = logD;
-        R.fold = 1;
-        R.out = b.PF[l];
-        R.o_q = b.PF_q[l];
-        R.ends = b.Pe[l];
-        R.e_q = b.Pe_q[l];
-        R.tw = tw;
-        R.logTW = logTW;
-        R.z = ZeroPrefix{zp, q0, pl.deg};
-        launch_real(R, nq, st, pr, launches);
-    }
-    VspDownArgs A{};
-    A.G = pl.G;
-    A.G_q = root ? 0 : pl.G_q;
-    if (!root) {
-        A.PF = b.PF[l];
-        A.PF_q = b.PF_q[l];
-        A.Pe = b.Pe[l];
-        A.Pe_q = b.Pe_q[l];
-    }
-    A.A = b.Gb2[l - 1];
-    A.A_q = b.Gb2_q[l - 1];
-    A.S = c.spec2;
-    A.S_q = c.spec2_q;
-    A.E = c.ends;
-    A.E_q = c.ends_q;
-    A.nreal_c = c.nreal;
-    A.logD = logD;
+    if (!root && p->lv[l + 1].kind != 2)   // the parents' Pbar as folded spectra (the band's top; D <= kSpecMaxD)
+        launch_real(vsp_pbar_real_args(p, b, l, q0, tw, logTW, nullptr), nq, st, pr, launches);
+    VspDownArgs A = vsp_down_args(p, b, l, q0, tw, logTW, nullptr);
     const bool spec_out = c.kind == 2;
-    if (spec_out) {
-        A.PFout = b.PF[l - 1];
-        A.PFo_q = b.PF_q[l - 1];
-        A.Peout = b.Pe[l - 1];
-        A.Peo_q = b.Pe_q[l - 1];
-    } else {
-        A.Pout = b.Pb[l - 1];
-        A.Po_q = c.P_q;
-        A.pst = c.pst;
-    }
-    A.tw = tw;
-    A.logTW = logTW;
-    A.z = ZeroPrefix{zp, q0, c.deg};
     const double fl = (spec_out ? 10.0 * h * (logD - 1) + 60.0 * h : 5.0 * D * logD + 30.0 * D) * c.nreal * nq;
     const int per = spec_out ? h : D;
     if (per <= kSpecMaxD) {
-        A.cb = short_grid_cb(vsp_cb(per), c.nreal, nq);
-        const size_t sm = (size_t)A.cb * per * sizeof(double2) + (size_t)A.cb * (sizeof(DnView) + sizeof(int));
+        A.cb = short_grid_cb(A.cb, c.nreal, nq);
+        A.nbx = (int)nbv(c.nreal, A.cb);
+        const size_t sm = down_smem(per, A.cb);
         pr->begin("adj_spec_down", fl, st);
-        k_vsp_down<<<dim3(nbv(c.nreal, A.cb), nq), vsp_tpb(sm), sm, st>>>(A);
+        k_vsp_down<<<dim3(A.nbx, nq), vsp_tpb(sm), sm, st>>>(A);
         pr->end(st);
         ++launches;
         return;

@@ -58,13 +58,13 @@ int icm_last_status(void);
  *                     gathers its tile with ordinary loads instead of a
  *                     tensor-map (TMA) copy (same results; read when a run
  *                     is enqueued)
- *   vjp_spectral_min_degree  levels of a single VJP plan (icm_gb300_vjp_*,
- *                     icm_gb300_equity_vjp) whose children have at least this
- *                     degree run spectrally, forward and adjoint (children
+ *   vjp_spectral_min_degree  levels of a VJP (icm_gb300_vjp_*,
+ *                     icm_gb300_equity_vjp[_batched]) whose children have at
+ *                     least this degree run spectrally, forward and adjoint (children
  *                     untruncated at k, as for forward plans); 0 = the
  *                     default (every level a forward plan would make
- *                     spectral), -1 = every level on coefficients.  Batched
- *                     VJPs keep their member trees on coefficients.            */
+ *                     spectral), -1 = every level on coefficients; batch
+ *                     members equal their single VJPs bit for bit either way */
 typedef struct {
     int block_size;
     int fft_min_degree;

@@ -99,8 +99,6 @@ def test_tanh_sinh_batched_bitwise(gpu_icm):
     for (S, P), E in zip(ts, res):
         assert np.array_equal(E, gpu_icm.gpu_equity(S, P))
     cots = [rng.standard_normal(len(S)) for S, _ in ts]
-    # batched VJPs keep their member trees on coefficients: so do the single ones here
-    gpu_icm.configure(quadrature="tanh_sinh", vjp_spectral_min_degree=-1)
     for (S, P), c, (gS, gP) in zip(ts, cots, gpu_icm.equity_vjp_batched(ts, cots)):
         a, b = gpu_icm.equity_vjp(S, P, c)
         assert np.array_equal(a, gS) and np.array_equal(b, gP)

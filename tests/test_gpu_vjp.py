@@ -148,10 +148,6 @@ def test_vjp_workload_size(gpu_icm, oracle):
 
 
 def test_vjp_plan_reuse_and_batched(gpu_icm):
-    # batched VJPs keep their member trees on coefficients: compare with
-    # single VJPs on coefficients (spectral single VJPs agree to rounding,
-    # tests/test_gpu_vjp_spectral.py)
-    gpu_icm.configure(vjp_spectral_min_degree=-1)
     rng = np.random.default_rng(8)
     ts, cots = [], []
     for n in (100, 700, 4000, 1):
@@ -227,9 +223,7 @@ def _mixed_batch(rng, count=40, big=False):
 @pytest.mark.parametrize("node_terms", [False, True])
 def test_batched_vjp_forest_bitwise(gpu_icm, node_terms):
     """Every tournament's gradients from the adjoint forest equal its single
-    VJP on coefficient levels bit for bit (the member trees of a batch are
-    on coefficients; so are the members solved by their own plans here)."""
-    gpu_icm.configure(vjp_spectral_min_degree=-1)
+    VJP bit for bit (spectral levels in both, as configured)."""
     rng = np.random.default_rng(21 + node_terms)
     ts, cots = _mixed_batch(rng, big=node_terms)
     res = gpu_icm.equity_vjp_batched(ts, cots, Q=128, node_terms=node_terms)
@@ -238,9 +232,20 @@ def test_batched_vjp_forest_bitwise(gpu_icm, node_terms):
         assert np.array_equal(a, gS) and np.array_equal(b, gP), (len(S), len(P))
 
 
+def test_batched_vjp_forest_bitwise_coefficients(gpu_icm):
+    """The same with every VJP level on coefficients (vjp_spectral_min_degree = -1)."""
+    gpu_icm.configure(vjp_spectral_min_degree=-1)
+    rng = np.random.default_rng(24)
+    ts, cots = _mixed_batch(rng, count=16)
+    res = gpu_icm.equity_vjp_batched(ts, cots, Q=96)
+    for (S, P), c, (gS, gP) in zip(ts, cots, res):
+        a, b = gpu_icm.equity_vjp(S, P, c, Q=96)
+        assert np.array_equal(a, gS) and np.array_equal(b, gP), (len(S), len(P))
+
+
 @pytest.mark.parametrize("B,fft_min", [(4, 16), (16, 32)])
 def test_batched_vjp_forest_block_sizes(gpu_icm, B, fft_min):
-    gpu_icm.configure(block_size=B, fft_min_degree=fft_min, vjp_spectral_min_degree=-1)
+    gpu_icm.configure(block_size=B, fft_min_degree=fft_min)
     rng = np.random.default_rng(B)
     ts, cots = _mixed_batch(rng, count=20)
     res = gpu_icm.equity_vjp_batched(ts, cots, Q=64)

@@ -145,8 +145,8 @@ def test_spectral_vjp_plan_reuse(gpu_icm):
 
 
 def test_batched_vjp_against_spectral_single(gpu_icm):
-    """Batched VJPs (member trees on coefficients) against the default single
-    VJPs (spectral levels) of the same tournaments, to rounding."""
+    """Batched VJPs (adjoint forests, spectral levels as in single plans)
+    equal the default single VJPs of the same tournaments bit for bit."""
     rng = np.random.default_rng(29)
     ts, cots = [], []
     for n in (150, 1200, 3000, 4000):
@@ -155,4 +155,15 @@ def test_batched_vjp_against_spectral_single(gpu_icm):
         cots.append(cot)
     res = gpu_icm.equity_vjp_batched(ts, cots, Q=64)
     for (S, P), c, got in zip(ts, cots, res):
-        _close(gpu_icm.equity_vjp(S, P, c, Q=64), got, len(S))
+        one = gpu_icm.equity_vjp(S, P, c, Q=64)
+        assert np.array_equal(one[0], got[0]) and np.array_equal(one[1], got[1]), len(S)
+    gpu_icm.configure(fft_min_degree=16)   # spectral levels from degree 16 up, in both
+    res = gpu_icm.equity_vjp_batched(ts, cots, Q=64, node_terms=True)
+    for (S, P), c, got in zip(ts, cots, res):
+        one = gpu_icm.equity_vjp(S, P, c, Q=64, node_terms=True)
+        assert np.array_equal(one[0], got[0]) and np.array_equal(one[1], got[1]), len(S)
+    # batches against the coefficient-level VJP, to rounding
+    gpu_icm.configure(fft_min_degree=16, vjp_spectral_min_degree=-1)
+    ref = gpu_icm.equity_vjp_batched(ts, cots, Q=64, node_terms=True)
+    for got, r in zip(res, ref):
+        _close(got, r, "batch")
