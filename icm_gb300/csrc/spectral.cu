@@ -407,6 +407,8 @@ struct SpView {
     int cold;              // wholly-zero parent: the item is skipped
 };
 static_assert(sizeof(SpView) <= kViewBytes, "view size");
+// per item: its view, its index in the partition and two child slots
+static_assert(sizeof(SpView) + 3 * sizeof(int) <= kItemBytes, "propagate item bytes");
 __device__ __forceinline__ bool item_skip(const SpView &v) {
     return v.cold || !((v.live[0] && !v.zero[0]) || (v.live[1] && !v.zero[1]));
 }
@@ -429,24 +431,57 @@ __device__ __forceinline__ void sp_fill(const SpecPropArgs &A, int q, int q0, in
     v.cold = zp_cold(z, q, j) ? 1 : 0;
 }
 
-// the propagate of the nh parents idx[0, nh) (2 nh children) whose views are
-// in V (the others skipped: nothing below a wholly-zero parent or a pair of
-// subset-cold children is read); want_G: children get g spectra (else
-// coefficients), uniform over a launch
-__device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int logD, const double2 *__restrict__ tw,
-                               int logTW, double2 *sm, bool want_G) {
+// the propagate of the nh parents idx[0, nh) whose views are in V (the
+// others skipped: nothing below a wholly-zero parent or a pair of
+// subset-cold children is read).  Only the children that exist and are not
+// subset-cold are transformed (cidx: 2 cb slots of shared memory, those
+// children first as view * 2 + side, then the subset-cold ones from the
+// end, whose outputs are zero; the reference CPU's single-sided correlate,
+// src/cpu/icm.c:1733-1815).  want_G: children get g spectra (else
+// coefficients), uniform over a launch.
+__device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int *cidx, int cb, int logD,
+                               const double2 *__restrict__ tw, int logTW, double2 *sm, bool want_G) {
     const int D = 1 << logD;
     const int h = D >> 1, lh = logD - 1;
-    const int nk = 2 * nh;   // children handled, h slots each
     if (nh == 0) return;
+    __shared__ int nk_s, nz_s;
+    if (threadIdx.x == 0) {
+        int c = 0, z = 0;
+        for (int it = 0; it < nh; ++it) {
+            const SpView &v = V[idx[it]];
+            for (int side = 0; side < 2; ++side) {
+                if (!v.live[side]) continue;
+                if (v.zero[side]) cidx[2 * cb - 1 - z++] = 2 * idx[it] + side;
+                else cidx[c++] = 2 * idx[it] + side;
+            }
+        }
+        nk_s = c;
+        nz_s = z;
+    }
+    __syncthreads();
+    const int nk = nk_s, nz = nz_s;   // children transformed, h slots each; subset-cold children
+    {   // subset-cold children: zero outputs, one warp each
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int zc = warp; zc < nz; zc += nw) {
+            const int c2 = cidx[2 * cb - 1 - zc];
+            const SpView &v = V[c2 >> 1];
+            const int side = c2 & 1;
+            if (want_G)
+                for (int f = lane; f <= h; f += 32) v.Gout[side][f] = make_double2(0.0, 0.0);
+            else
+                for (int t = lane; t < v.gst; t += 32) v.gout[side][t] = 0.0;
+        }
+    }
+    if (nk == 0) return;
     const double2 one = make_double2(1.0, 0.0);
     // 1. odd bins of Y -> inverse half-bin input, by mirror pairs
     const int hp = (h + 1) >> 1;   // pairs per child (h = 1: one self pair)
     for (int e = threadIdx.x; e < nk * hp; e += blockDim.x) {
         const int kk = e / hp, f = e - kk * hp;
         const int fp = h - 1 - f;
-        const SpView &v = V[idx[kk >> 1]];
-        const double2 *S = v.S[(kk & 1) ^ 1];   // the sibling's spectrum
+        const int c2 = cidx[kk];
+        const SpView &v = V[c2 >> 1];
+        const double2 *S = v.S[(c2 & 1) ^ 1];   // the sibling's spectrum
         const double2 *G = v.G;
         const double2 Y1 = cmulc(G[2 * f + 1], S ? S[2 * f + 1] : one);
         const double2 Y2 = cconj(cmulc(G[2 * fp + 1], S ? S[2 * fp + 1] : one));
@@ -471,15 +506,10 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int logD
         for (int e = threadIdx.x; e < nk * hq; e += blockDim.x) {
             const int kk = e / hq, f = e - kk * hq;
             const int fp = h - f;
-            const SpView &v = V[idx[kk >> 1]];
-            const int side = kk & 1;
-            if (!v.live[side]) continue;   // lone child: no right sibling node
+            const int c2 = cidx[kk];
+            const SpView &v = V[c2 >> 1];
+            const int side = c2 & 1;
             double2 *out = v.Gout[side];
-            if (v.zero[side]) {
-                out[f] = make_double2(0.0, 0.0);
-                out[fp] = make_double2(0.0, 0.0);
-                continue;
-            }
             const double2 *G = v.G;
             const double2 *S = v.S[side ^ 1];
             const double2 *z = sm + (size_t)kk * h;
@@ -503,10 +533,9 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int logD
     const double ka = 1.0 / (4.0 * h);
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
         const int kk = e >> lh, s = e & (h - 1);
-        const SpView &v = V[idx[kk >> 1]];
-        const int side = kk & 1;
-        if (!v.live[side]) continue;
-        double *out = v.gout[side];
+        const int c2 = cidx[kk];
+        const SpView &v = V[c2 >> 1];
+        double *out = v.gout[c2 & 1];
         const double2 w = untwist(kk, s, sm[e]);
         if (2 * s < v.glen) out[2 * s] = ka * w.x;
         if (2 * s + 1 < v.glen) out[2 * s + 1] = ka * w.y;
@@ -515,8 +544,9 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int logD
     // U[f] = E + i O of the even-bin spectrum Ye (bins 0..h of a real size-D spectrum)
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
         const int kk = e >> lh, f = e & (h - 1);
-        const SpView &v = V[idx[kk >> 1]];
-        const double2 *S = v.S[(kk & 1) ^ 1];
+        const int c2 = cidx[kk];
+        const SpView &v = V[c2 >> 1];
+        const double2 *S = v.S[(c2 & 1) ^ 1];
         const double2 *G = v.G;
         const double2 Cf = cmulc(G[2 * f], S ? S[2 * f] : one);
         const double2 Cc = cmulc(G[2 * (h - f)], S ? S[2 * (h - f)] : one);
@@ -530,15 +560,13 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int logD
     const double inv_D = 1.0 / D;
     for (int e = threadIdx.x; e < nk * h; e += blockDim.x) {
         const int kk = e >> lh, s = e & (h - 1);
-        const SpView &v = V[idx[kk >> 1]];
-        const int side = kk & 1;
-        if (!v.live[side]) continue;
-        double *out = v.gout[side];
-        const bool zr = v.zero[side];
+        const int c2 = cidx[kk];
+        const SpView &v = V[c2 >> 1];
+        double *out = v.gout[c2 & 1];
         const int gst = v.gst, glen = v.glen;
         const double2 w = sm[e];
-        if (2 * s < gst) out[2 * s] = (zr || 2 * s >= glen) ? 0.0 : out[2 * s] + 0.5 * w.x * inv_D;
-        if (2 * s + 1 < gst) out[2 * s + 1] = (zr || 2 * s + 1 >= glen) ? 0.0 : out[2 * s + 1] + 0.5 * w.y * inv_D;
+        if (2 * s < gst) out[2 * s] = (2 * s >= glen) ? 0.0 : out[2 * s] + 0.5 * w.x * inv_D;
+        if (2 * s + 1 < gst) out[2 * s + 1] = (2 * s + 1 >= glen) ? 0.0 : out[2 * s + 1] + 0.5 * w.y * inv_D;
     }
 }
 
@@ -554,7 +582,7 @@ __device__ void spec_prop_body(const SpecPropArgs &A, int bx, int q) {
     for (int it = threadIdx.x; it < cnt; it += blockDim.x) sp_fill(A, q, A.z.q0, j0 + it, D, V[it]);
     __syncthreads();
     const int nh = partition_items(V, idx, cnt);
-    spec_prop_core(V, idx, nh, A.logD, A.tw, A.logTW, sm, A.Gout != nullptr);
+    spec_prop_core(V, idx, nh, idx + cbp, cbp, A.logD, A.tw, A.logTW, sm, A.Gout != nullptr);
 }
 
 // packed: slots[s] = (descriptor, parent); all descriptors of a launch share
@@ -576,7 +604,7 @@ __device__ void spec_prop_packed(const SpecPropArgs *__restrict__ Dsc, const int
     }
     __syncthreads();
     const int nh = partition_items(V, idx, cnt);
-    spec_prop_core(V, idx, nh, A0.logD, A0.tw, A0.logTW, sm, A0.Gout != nullptr);
+    spec_prop_core(V, idx, nh, idx + cbp, cbp, A0.logD, A0.tw, A0.logTW, sm, A0.Gout != nullptr);
 }
 
 __global__ void __launch_bounds__(kSpecThreadsMax) k_spec_init(SpecInitArgs A) { spec_init_body(A, blockIdx.x, blockIdx.y); }
