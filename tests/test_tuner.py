@@ -97,3 +97,37 @@ def test_level_entry_keeps_a_level_on_coefficients(L, tmp_path):
     tuned = [int(x) for x in buf.value.split()[1:]]
     assert tuned[4] == 1                                      # level 5 on coefficients
     assert tuned[:4] == kinds[:4] and tuned[5:] == kinds[5:]
+
+
+def _kinds(L, n, k, B=8, fm=64, flags=0):
+    import ctypes
+    buf = ctypes.create_string_buffer(512)
+    assert L.icm_gb300_check_geometry(n, k, B, fm, flags, buf, 512) == 0, buf.value
+    return [int(x) for x in buf.value.split()[1:]]
+
+
+def test_vjp_geometry_spectral_band(L):
+    """A VJP plan's tree (flags 2): the spectral band over untruncated children
+    reaches the root when the root's children are untruncated; otherwise it
+    ends at children of degree 8192 at most (its top converts coefficient
+    Pbar in one CTA), with coefficient-FFT levels above (host-side, no GPU)."""
+    from icm_gb300 import configure
+    configure()
+    try:
+        full = _kinds(L, 1 << 18, 1 << 18, flags=2)
+        assert full[-1] == 2 and full.count(2) >= 10      # band up to the root, multi-pass levels included
+        trunc = _kinds(L, 40000, 20000, flags=2)          # children of degree 16384 would be untruncated
+        degs = [8 << l for l in range(len(trunc))]        # children's degree of parent level l + 1
+        top = max(i for i, kd in enumerate(trunc) if kd == 2)
+        assert degs[top] == 8192 and all(kd == 1 for kd in trunc[top + 1:])
+        fwd = _kinds(L, 40000, 20000, flags=0)            # a forward plan goes one level further
+        assert max(i for i, kd in enumerate(fwd) if kd == 2) > top
+        assert 2 not in _kinds(L, 1 << 18, 1 << 18, flags=1)
+        configure(vjp_spectral_min_degree=-1)             # the VJP on coefficients
+        assert 2 not in _kinds(L, 1 << 18, 1 << 18, flags=2)
+        configure(vjp_spectral_min_degree=1024)           # the band from children of degree 1024
+        band = _kinds(L, 1 << 18, 1 << 18, flags=2)
+        first = min(i for i, kd in enumerate(band) if kd == 2)
+        assert (8 << first) == 1024
+    finally:
+        configure()
