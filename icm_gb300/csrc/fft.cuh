@@ -51,6 +51,13 @@ __device__ __forceinline__ double2 twmul(double2 a, double2 w) {
 //   R4C[h + j] rotation codes of those three twiddles (bits 0-1, 2-3, 4-5)
 //   R2[h + j]  {tau, r} of e^{-2 pi i j/2h} for the final radix-2 pass
 //   R2C[h + j] its rotation code
+// Two more sets of the same four tables follow for the half-shifted forward
+// transforms X(k + sigma/2) = sum_s x_s e^{-2 pi i s (k + sigma/2)/M},
+// sigma = +1 or -1 (a DFT of x_s e^{-pi i sigma s/M} without the twist):
+// in decimation in time a half shift of the whole transform is a half shift
+// of both halves, X(k + 1/2) = E(k + 1/2) + W_M^{k+1/2} O(k + 1/2), so every
+// pass keeps its butterflies and takes the twiddles w^{j + sigma/2} (the
+// first radix-4 pass then has general twiddles too).
 constexpr int kTwMaxH4 = 2048;   // radix-4 passes of transforms up to 8192 points
 constexpr int kTwMaxH2 = 4096;   // radix-2 pass of an 8192-point transform
 
@@ -65,8 +72,15 @@ struct TwTables {
     const int *r2c;
 };
 
-__device__ __forceinline__ TwTables tw_tables(const double2 *tw, int logTW) {
-    const char *base = (const char *)(tw + (1L << logTW));
+// bytes of one set of tangent tables
+constexpr size_t kTwSetBytes = sizeof(GTw) * 2 * kTwMaxH4 + sizeof(int) * 2 * kTwMaxH4 +
+                               sizeof(double2) * 2 * kTwMaxH2 + sizeof(int) * 2 * kTwMaxH2;
+static_assert(kTwSetBytes % 256 == 0, "table sets stay aligned");
+// the set of a transform with half shift sigma: 0 plain, 1 for +1/2, 2 for -1/2
+__host__ __device__ constexpr int tw_set(int sigma) { return sigma == 0 ? 0 : (sigma > 0 ? 1 : 2); }
+
+__device__ __forceinline__ TwTables tw_tables(const double2 *tw, int logTW, int set = 0) {
+    const char *base = (const char *)(tw + (1L << logTW)) + (size_t)set * kTwSetBytes;
     TwTables t;
     t.r4 = (const GTw *)base;
     base += sizeof(GTw) * 2 * kTwMaxH4;
@@ -78,9 +92,8 @@ __device__ __forceinline__ TwTables tw_tables(const double2 *tw, int logTW) {
     return t;
 }
 
-// bytes of the tangent tables that follow the plain table
-constexpr size_t kTwExtraBytes = sizeof(double2) * 3 * 2 * kTwMaxH4 + sizeof(int) * 2 * kTwMaxH4 +
-                                 sizeof(double2) * 2 * kTwMaxH2 + sizeof(int) * 2 * kTwMaxH2;
+// bytes of the tangent tables that follow the plain table: three sets
+constexpr size_t kTwExtraBytes = 3 * kTwSetBytes;
 
 __device__ __forceinline__ double dneg_if(double v, int neg) {
     return __longlong_as_double(__double_as_longlong(v) ^ ((long long)neg << 63));
@@ -106,10 +119,12 @@ __device__ __forceinline__ double2 tanmul(double2 z, int code, double tau) {
 // `cnt` transforms of size 2^logM stored back to back in x (shared memory),
 // each already in bit-reversed order.  All threads of the block take part;
 // the caller synchronises before (after filling x) and this function ends
-// with a barrier.
-template <int SIGN>
+// with a barrier.  SHIFT = +1 / -1: the forward transform half-shifted by
+// +1/2 / -1/2 bin (SIGN = -1 only).
+template <int SIGN, int SHIFT = 0>
 __device__ void smem_fft_dit(double2 *x, int logM, int cnt, const double2 *__restrict__ tw, int logTW) {
-    const TwTables T = tw_tables(tw, logTW);
+    static_assert(SHIFT == 0 || SIGN < 0, "half-shifted transforms are forward only");
+    const TwTables T = tw_tables(tw, logTW, tw_set(SHIFT));
     const int M = 1 << logM;
     int s = 0;
     for (; s + 1 < logM; s += 2) {
@@ -122,7 +137,7 @@ __device__ void smem_fft_dit(double2 *x, int logM, int cnt, const double2 *__res
             const int i = item * M + ((r >> s) << (s + 2)) + j;
             const double2 a = x[i], bq = x[i + h], c = x[i + 2 * h], d = x[i + 3 * h];
             double2 x0, x1, x2, x3;
-            if (h == 1) {   // first pass: all twiddles are 1
+            if (SHIFT == 0 && h == 1) {   // first pass: all twiddles are 1
                 const double2 s0 = cadd(a, bq), d0 = csub(a, bq);
                 const double2 s1 = cadd(c, d), d1 = csub(c, d);
                 x0 = cadd(s0, s1);

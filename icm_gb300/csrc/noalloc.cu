@@ -53,6 +53,16 @@ constexpr size_t kNoallocBytes = (size_t)32 << 20; // 32 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 static std::mutex g_noalloc_mu;        // guards the per-device address cache
+
+// host copy of the twiddle tables per table size, built once (the upload
+// reads it on every call; entries are never replaced)
+static const std::vector<unsigned char> &host_twiddles(int logTW) {
+    static std::mutex mu;
+    static std::vector<unsigned char> tabs[32];
+    std::lock_guard<std::mutex> lock(mu);
+    if (tabs[logTW].empty()) fill_twiddles(logTW, tabs[logTW]);
+    return tabs[logTW];
+}
 static char *g_noalloc_ptr[64] = {};   // device address per device, set up once
 
 // The scratch array's device address on the current device (resolved once per
@@ -215,8 +225,7 @@ static int noalloc_solve(int n, const double *S, int Q, const double *payout, in
     const int nact = (int)(node.size() / 3);
     NoallocPlan p;
     if (noalloc_plan(p, n, k, nact, scratch, err) != 0) return fail(err);
-    std::vector<unsigned char> tw;
-    fill_twiddles(p.logTW, tw);
+    const std::vector<unsigned char> &tw = host_twiddles(p.logTW);
 
     cudaStream_t st = 0;   // legacy default stream: no stream creation
     cudaError_t e = cudaMemcpyAsync(p.d_S, Ss.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);

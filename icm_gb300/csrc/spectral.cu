@@ -21,9 +21,11 @@
 //         or, where the level below works on coefficients, a = (IDFT_D(even
 //         bins) + (a - b))/2.  Two size-D/2 transforms per child.
 //
-// All transforms are decimation-in-time (bit-reversed in, natural out); the
-// pointwise twist between two transforms is applied while permuting the data
-// into bit-reversed order in place (smem_bitrev_map).  A missing sibling
+// All transforms are decimation-in-time (bit-reversed in, natural out).  The
+// twist in front of a second (forward) transform is that transform's half
+// shift, folded into its twiddles (fft.cuh); other pointwise maps between two
+// transforms are applied while permuting the data into bit-reversed order in
+// place (smem_bitrev_map).  A missing sibling
 // (ragged tree edge) is the polynomial 1: spectrum 1, ends (1, 0).
 #include <algorithm>
 
@@ -218,8 +220,8 @@ __device__ void spec_build_core(const SbView *V, const int *idx, int cnt, int nh
     __syncthreads();
     smem_fft_dit<+1>(sm, logD, nh, tw, logTW);
     // 2. u_s = 2D (x_{2s} + i x_{2s+1}); coefficients where a coefficient level
-    //    sits above (truncated at plen, zero padding to pst), the endpoint fix,
-    //    and the (unscaled) twist
+    //    sits above (truncated at plen, zero padding to pst) and the endpoint
+    //    fix; the twist e^{-2 pi i s/2D} is the forward transform's half shift
     const double one_over_2D = 1.0 / (2.0 * D);
     auto coeffs = [&](int it, int s, double2 u) -> double2 {
         const SbView &v = V[idx[it]];
@@ -242,14 +244,14 @@ __device__ void spec_build_core(const SbView *V, const int *idx, int cnt, int nh
                 for (int t = 2 * D + 1; t < pst; ++t) v.po[t] = 0.0;
             }
         }
-        return (s == 0) ? u : cmul(u, twl(tw, (long)s << (logTW - logD - 1)));   // e^{-2 pi i s/2D}
+        return u;
     };
     if (!want_spec) {   // the level above works on coefficients: no spectrum needed
         for (int e = threadIdx.x; e < nh * D; e += blockDim.x) coeffs(e >> logD, e & (D - 1), sm[e]);
         return;
     }
     smem_bitrev_map(sm, logD, nh, coeffs);
-    smem_fft_dit<-1>(sm, logD, nh, tw, logTW);
+    smem_fft_dit<-1, +1>(sm, logD, nh, tw, logTW);   // c_f = sum_s u_s e^{-2 pi i s (f + 1/2)/D}
     // 3. odd bins by mirror pairs (f, D-1-f), f < D/2
     const double kb = 1.0 / (4.0 * D);
     for (int e = threadIdx.x; e < nh * hD; e += blockDim.x) {
@@ -493,13 +495,14 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int *cid
     }
     __syncthreads();
     smem_fft_dit<+1>(sm, lh, nk, tw, logTW);
-    // 2. untwist (unscaled): w_s = c'_s e^{+2 pi i s/D}
+    // 2. untwist (unscaled): w_s = c'_s e^{+2 pi i s/D}; in front of the
+    //    forward transform it is that transform's half shift by -1/2 bin
     auto untwist = [&](int, int s, double2 v) -> double2 {
         return (s == 0) ? v : cmulc(v, twl(tw, (long)s << (logTW - logD)));
     };
     if (want_G) {
-        smem_bitrev_map(sm, lh, nk, untwist);
-        smem_fft_dit<-1>(sm, lh, nk, tw, logTW);
+        smem_bitrev_map(sm, lh, nk, [](int, int, double2 v) { return v; });
+        smem_fft_dit<-1, -1>(sm, lh, nk, tw, logTW);   // z_f = sum_s w_s e^{-2 pi i s f/h}
         // 3a. child spectra by mirror pairs (f, h-f), f <= h/2
         const double kx = 1.0 / (8.0 * h);
         const int hq = (h >> 1) + 1;

@@ -1,8 +1,8 @@
 // twiddle.cpp -- host construction of the device twiddle tables:
 // tw[t] = exp(-2 pi i t / 2^logTW) followed by the tangent-form tables of
-// the FFT butterflies (fft.cuh).  Every value is computed in long double
-// from an angle folded into [0, pi/4] with exact integer reflections, then
-// rounded once to double.
+// the FFT butterflies (fft.cuh): plain and half-shifted by +-1/2 bin.  Every
+// value is computed in long double from an angle folded into [0, pi/4] with
+// exact integer reflections, then rounded once to double.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -62,34 +62,41 @@ void fill_twiddles(int logTW, std::vector<unsigned char> &out) {
         unit_root_ld(t, N, &re, &im);
         tw[t] = make_double2((double)re, (double)im);
     }
-    unsigned char *base = out.data() + sizeof(double2) * (size_t)N;
-    GTw *r4 = (GTw *)base;
-    base += sizeof(GTw) * 2 * kTwMaxH4;
-    int *r4c = (int *)base;
-    base += sizeof(int) * 2 * kTwMaxH4;
-    double2 *r2 = (double2 *)base;
-    base += sizeof(double2) * 2 * kTwMaxH2;
-    int *r2c = (int *)base;
-    for (long h = 1; h <= kTwMaxH4; h *= 4) {
-        for (long j = 0; j < h; ++j) {
-            int c1, c2, c3;
-            long double a1, t1, a2, t2, a3, t3;
-            tangent_form(j, 4 * h, &c1, &a1, &t1);
-            tangent_form(2 * j, 4 * h, &c2, &a2, &t2);
-            tangent_form(3 * j, 4 * h, &c3, &a3, &t3);
-            r4[h + j].a = make_double2((double)t1, (double)a1);
-            r4[h + j].b = make_double2((double)t2, (double)a2);
-            r4[h + j].c = make_double2((double)t3, (double)(a3 / a1));
-            r4c[h + j] = c1 | (c2 << 2) | (c3 << 4);
+    // set 0: twiddles w^j; sets 1 and 2: w^{j + 1/2} and w^{j - 1/2}, the angle
+    // (2j + sigma) over twice the group size
+    for (int set = 0; set < 3; ++set) {
+        const long sigma = set == 0 ? 0 : (set == 1 ? 1 : -1);
+        const long m = set == 0 ? 1 : 2;   // angle numerator 2j + sigma over 2N when shifted
+        unsigned char *base = out.data() + sizeof(double2) * (size_t)N + (size_t)set * kTwSetBytes;
+        GTw *r4 = (GTw *)base;
+        base += sizeof(GTw) * 2 * kTwMaxH4;
+        int *r4c = (int *)base;
+        base += sizeof(int) * 2 * kTwMaxH4;
+        double2 *r2 = (double2 *)base;
+        base += sizeof(double2) * 2 * kTwMaxH2;
+        int *r2c = (int *)base;
+        for (long h = 1; h <= kTwMaxH4; h *= 4) {
+            for (long j = 0; j < h; ++j) {
+                const long t = m * j + sigma;
+                int c1, c2, c3;
+                long double a1, t1, a2, t2, a3, t3;
+                tangent_form(t, m * 4 * h, &c1, &a1, &t1);
+                tangent_form(2 * t, m * 4 * h, &c2, &a2, &t2);
+                tangent_form(3 * t, m * 4 * h, &c3, &a3, &t3);
+                r4[h + j].a = make_double2((double)t1, (double)a1);
+                r4[h + j].b = make_double2((double)t2, (double)a2);
+                r4[h + j].c = make_double2((double)t3, (double)(a3 / a1));
+                r4c[h + j] = c1 | (c2 << 2) | (c3 << 4);
+            }
         }
-    }
-    for (long h = 1; h <= kTwMaxH2; h *= 4) {
-        for (long j = 0; j < h; ++j) {
-            int c;
-            long double a, t;
-            tangent_form(j, 2 * h, &c, &a, &t);
-            r2[h + j] = make_double2((double)t, (double)a);
-            r2c[h + j] = c;
+        for (long h = 1; h <= kTwMaxH2; h *= 4) {
+            for (long j = 0; j < h; ++j) {
+                int c;
+                long double a, t;
+                tangent_form(m * j + sigma, m * 2 * h, &c, &a, &t);
+                r2[h + j] = make_double2((double)t, (double)a);
+                r2c[h + j] = c;
+            }
         }
     }
 }
