@@ -95,6 +95,16 @@ __device__ __forceinline__ TwTables tw_tables(const double2 *tw, int logTW, int 
 // bytes of the tangent tables that follow the plain table: three sets
 constexpr size_t kTwExtraBytes = 3 * kTwSetBytes;
 
+// After the sets: the tangent form of every plain entry, tw[t] = e^{-2 pi i t/N}
+// = R r (1 + i tau) with {tau, r} stored and R = (1, -i, -1, i)[tan_code(t)],
+// the quarter turn nearest the angle (taken from t, so not stored).
+__host__ __device__ __forceinline__ int tan_code(long t, int logTW) {
+    return (int)(((8 * t + (1L << logTW) - 1) >> (logTW + 1)) & 3);
+}
+__device__ __forceinline__ const double2 *tw_tangent(const double2 *tw, int logTW) {
+    return (const double2 *)((const char *)(tw + (1L << logTW)) + kTwExtraBytes);
+}
+
 __device__ __forceinline__ double dneg_if(double v, int neg) {
     return __longlong_as_double(__double_as_longlong(v) ^ ((long long)neg << 63));
 }
@@ -114,6 +124,49 @@ __device__ __forceinline__ double2 tanmul(double2 z, int code, double tau) {
     const double2 v = rot<SIGN>(z, code);
     if (SIGN < 0) return make_double2(fma(-tau, v.y, v.x), fma(tau, v.x, v.y));
     return make_double2(fma(tau, v.y, v.x), fma(-tau, v.x, v.y));
+}
+
+// z w_t / r (SIGN < 0) or z conj(w_t) / r (SIGN > 0) for the plain entry
+// w_t = tw[t] in tangent form (tt = tw_tangent(tw, logTW)); r goes to *r
+template <int SIGN>
+__device__ __forceinline__ double2 tanmul_t(double2 z, const double2 *__restrict__ tt, long t, int logTW, double *r) {
+    const double2 g = __ldg(&tt[t]);
+    *r = g.y;
+    return tanmul<SIGN>(z, tan_code(t, logTW), g.x);
+}
+
+// Pointwise steps of a real transform of size 2M done as a complex one of
+// size M, on a mirror pair of bins.
+// Inverse input: Uf = E + i O, Uc = conj(E) + i conj(O), O = Dd conj(w_t),
+// the factor r of w_t folded into the sums.
+__device__ __forceinline__ void mirror_inv_input(double2 E, double2 Dd, const double2 *__restrict__ tt, long t,
+                                                 int logTW, double2 &Uf, double2 &Uc) {
+    double r;
+    const double2 o = tanmul_t<+1>(Dd, tt, t, logTW, &r);   // O = r o
+    Uf = make_double2(fma(-r, o.y, E.x), fma(r, o.x, E.y));
+    Uc = make_double2(fma(r, o.y, E.x), fma(r, o.x, -E.y));
+}
+// Output pair from the forward transform's bins a and b (b already
+// conjugated): Hf = kb (Ep + T), Hc = kb conj(Ep - T), Ep = a + b,
+// T = -i (a - b) w_t; kb a power of two (exact scaling).
+__device__ __forceinline__ void mirror_out_pair(double2 a, double2 b, double kb, const double2 *__restrict__ tt, long t,
+                                                int logTW, double2 &Hf, double2 &Hc) {
+    const double2 Ek = cscale(cadd(a, b), kb);
+    double r;
+    const double2 u = tanmul_t<-1>(cmul_mi(csub(a, b)), tt, t, logTW, &r);   // T = r u
+    const double rk = r * kb;
+    Hf = make_double2(fma(rk, u.x, Ek.x), fma(rk, u.y, Ek.y));
+    Hc = make_double2(fma(-rk, u.x, Ek.x), fma(rk, u.y, -Ek.y));
+}
+
+// Unpack bin f of a real transform from the complex one z of half the size:
+// 0.5 (a + w_t b), a = z_f + conj z_{M-f}, b = -i (z_f - conj z_{M-f}); the
+// factors r of w_t and 0.5 folded into one FMA per component.
+__device__ __forceinline__ double2 half_sum_tw(double2 a, double2 b, const double2 *__restrict__ tt, long t, int logTW) {
+    double r;
+    const double2 u = tanmul_t<-1>(b, tt, t, logTW, &r);
+    const double hr = 0.5 * r;
+    return make_double2(fma(hr, u.x, 0.5 * a.x), fma(hr, u.y, 0.5 * a.y));
 }
 
 // `cnt` transforms of size 2^logM stored back to back in x (shared memory),

@@ -152,8 +152,9 @@ __device__ void fused_build_core(const FbView *V, const int *idx, int cnt, int n
         const double2 Cf = cmul(SLf, SRf), Cc = cmul(SLc, SRc);
         double2 E = cadd(Cf, cconj(Cc)), D = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; D.y = 0.0; }
-        const double2 O = cmulc(D, __ldg(&tw[(long)f << (logTW - logN)]));
-        U[(size_t)it * h + bitrev(f, logN - 1)] = cadd(E, cmul_pi(O));
+        double2 Uf, Uc;   // O = D e^{+2 pi i f/N}; Uc unused
+        mirror_inv_input(E, D, tw_tangent(tw, logTW), (long)f << (logTW - logN), logTW, Uf, Uc);
+        U[(size_t)it * h + bitrev(f, logN - 1)] = Uf;
     }
     if (spectra_only) return;
     __syncthreads();
@@ -206,16 +207,15 @@ __device__ void fused_prop_core(const FpView *V, const int *idx, int nh, int cb,
         const double2 *sR = sL + (h + 1);
         double2 *z = Z + (size_t)it * N;
         const double2 wf = w[f], wc = w[(h - f) & (h - 1)];
-        const double2 Ev = cscale(cadd(wf, cconj(wc)), 0.5);
-        const double2 Od = cscale(cmul_mi(csub(wf, cconj(wc))), 0.5);
-        const double2 G = cadd(Ev, cmul(Od, __ldg(&tw[(long)f << (logTW - logN)])));
+        const double2 Ev = cadd(wf, cconj(wc)), Od = cmul_mi(csub(wf, cconj(wc)));   // both doubled
+        const double2 G = half_sum_tw(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logN), logTW);
         const double2 YL = cmulc(G, sR[f]), YR = cmulc(G, sL[f]);
         z[bitrev(f, logN)] = cadd(YL, cmul_pi(YR));
         if (f != 0) {
             z[bitrev(N - f, logN)] = cadd(cconj(YL), cmul_pi(cconj(YR)));
         } else {
             // bin h: W[h mod h] = W[0] on both sides; e^{-i pi} = -1
-            const double2 Gh = csub(Ev, Od);
+            const double2 Gh = cscale(csub(Ev, Od), 0.5);
             const double2 YLh = cmulc(Gh, sR[h]), YRh = cmulc(Gh, sL[h]);
             z[bitrev(h, logN)] = cadd(YLh, cmul_pi(YRh));
         }

@@ -117,12 +117,11 @@ __device__ void spec_init_body(const SpecInitArgs &A, int bx, int q) {
         const int it = e >> logd, f = e & (d - 1);
         const double2 *z = sm + (size_t)it * d;
         const double2 zf = z[f], zc = z[(d - f) & (d - 1)];
-        const double2 Ev = cscale(cadd(zf, cconj(zc)), 0.5);
-        const double2 Od = cscale(cmul_mi(csub(zf, cconj(zc))), 0.5);
+        const double2 Ev = cadd(zf, cconj(zc)), Od = cmul_mi(csub(zf, cconj(zc)));   // both doubled
         double2 *out = spec2 + q * s2_q + (size_t)(j0 + it) * (d + 1);
-        out[f] = cadd(Ev, cmul(Od, twl(tw, (long)f << (logTW - logd - 1))));
+        out[f] = half_sum_tw(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logd - 1), logTW);
         if (f == 0) {
-            out[d] = csub(Ev, Od);
+            out[d] = cscale(csub(Ev, Od), 0.5);
             const double *x = P + q * P_q + (size_t)(j0 + it) * pst;
             double *en = ends + q * e_q + (size_t)(j0 + it) * 2;
             en[0] = x[0];
@@ -199,6 +198,7 @@ __device__ void spec_build_core(const SbView *V, const int *idx, int cnt, int nh
     }
     if (nh == 0) return;
     const double2 one = make_double2(1.0, 0.0);
+    const double2 *tt = tw_tangent(tw, logTW);
     // 1. product spectrum (even bins of spec2(X)) and the inverse input, by mirror pairs
     const int np1 = hD + 1;
     for (int e = threadIdx.x; e < nh * np1; e += blockDim.x) {
@@ -212,10 +212,11 @@ __device__ void spec_build_core(const SbView *V, const int *idx, int cnt, int nh
         }
         double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
-        const double2 O = (f == 0) ? Dd : cmulc(Dd, twl(tw, (long)f << (logTW - logD - 1)));   // e^{+2 pi i f/2D}
+        double2 Uf, Uc;   // O = Dd e^{+2 pi i f/2D}
+        mirror_inv_input(E, Dd, tt, (long)f << (logTW - logD - 1), logTW, Uf, Uc);
         double2 *u = sm + (size_t)it * D;
-        u[bitrev(f, logD)] = cadd(E, cmul_pi(O));
-        if (f != 0 && f != hD) u[bitrev(D - f, logD)] = cadd(cconj(E), cmul_pi(cconj(O)));
+        u[bitrev(f, logD)] = Uf;
+        if (f != 0 && f != hD) u[bitrev(D - f, logD)] = Uc;
     }
     __syncthreads();
     smem_fft_dit<+1>(sm, logD, nh, tw, logTW);
@@ -257,12 +258,11 @@ __device__ void spec_build_core(const SbView *V, const int *idx, int cnt, int nh
     for (int e = threadIdx.x; e < nh * hD; e += blockDim.x) {
         const int it = e / hD, f = e - it * hD;
         const double2 *c = sm + (size_t)it * D;
-        const double2 a = c[f], b = cconj(c[D - 1 - f]);
-        const double2 Ep = cadd(a, b);
-        const double2 T = cmul(cmul_mi(csub(a, b)), twl(tw, (long)(2 * f + 1) << (logTW - logD - 2)));
+        double2 Hf, Hc;   // T = -i (a - b) e^{-2 pi i (2f+1)/4D}
+        mirror_out_pair(c[f], cconj(c[D - 1 - f]), kb, tt, (long)(2 * f + 1) << (logTW - logD - 2), logTW, Hf, Hc);
         double2 *ps = V[idx[it]].ps;
-        ps[2 * f + 1] = cscale(cadd(Ep, T), kb);
-        ps[2 * (D - 1 - f) + 1] = cscale(cconj(csub(Ep, T)), kb);
+        ps[2 * f + 1] = Hf;
+        ps[2 * (D - 1 - f) + 1] = Hc;
     }
 }
 
@@ -374,10 +374,9 @@ __device__ void gspec_body(const GspecArgs &A, int bx, int q) {
         }
         const double2 *z = sm + (size_t)it * h;
         const double2 zf = z[f], zc = z[(h - f) & (h - 1)];
-        const double2 Ev = cscale(cadd(zf, cconj(zc)), 0.5);
-        const double2 Od = cscale(cmul_mi(csub(zf, cconj(zc))), 0.5);
-        out[f] = cadd(Ev, cmul(Od, twl(tw, (long)f << (logTW - logd))));
-        if (f == 0) out[h] = csub(Ev, Od);
+        const double2 Ev = cadd(zf, cconj(zc)), Od = cmul_mi(csub(zf, cconj(zc)));   // both doubled
+        out[f] = half_sum_tw(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logd), logTW);
+        if (f == 0) out[h] = cscale(csub(Ev, Od), 0.5);
     }
 }
 
@@ -476,6 +475,7 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int *cid
     }
     if (nk == 0) return;
     const double2 one = make_double2(1.0, 0.0);
+    const double2 *tt = tw_tangent(tw, logTW);
     // 1. odd bins of Y -> inverse half-bin input, by mirror pairs
     const int hp = (h + 1) >> 1;   // pairs per child (h = 1: one self pair)
     for (int e = threadIdx.x; e < nk * hp; e += blockDim.x) {
@@ -487,11 +487,11 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int *cid
         const double2 *G = v.G;
         const double2 Y1 = cmulc(G[2 * f + 1], S ? S[2 * f + 1] : one);
         const double2 Y2 = cconj(cmulc(G[2 * fp + 1], S ? S[2 * fp + 1] : one));
-        const double2 A = cadd(Y1, Y2);
-        const double2 B = cmulc(csub(Y1, Y2), twl(tw, (long)(2 * f + 1) << (logTW - logD - 1)));
+        double2 Xf, Xc;   // A + i B, conj(A) + i conj(B), B = (Y1 - Y2) conj(w_f)
+        mirror_inv_input(cadd(Y1, Y2), csub(Y1, Y2), tt, (long)(2 * f + 1) << (logTW - logD - 1), logTW, Xf, Xc);
         double2 *x = sm + (size_t)kk * h;
-        x[bitrev(f, lh)] = cadd(A, cmul_pi(B));
-        if (fp != f) x[bitrev(fp, lh)] = cadd(cconj(A), cmul_pi(cconj(B)));
+        x[bitrev(f, lh)] = Xf;
+        if (fp != f) x[bitrev(fp, lh)] = Xc;
     }
     __syncthreads();
     smem_fft_dit<+1>(sm, lh, nk, tw, logTW);

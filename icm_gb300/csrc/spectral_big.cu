@@ -53,10 +53,9 @@ __global__ void k_sb_gpost(int nreal, int logd, const double2 *__restrict__ buf,
     }
     const double2 *z = buf + ((size_t)q * nreal + j) * h;
     const double2 zf = z[f], zc = z[(h - f) & (h - 1)];
-    const double2 Ev = cscale(cadd(zf, cconj(zc)), 0.5);
-    const double2 Od = cscale(cmul_mi(csub(zf, cconj(zc))), 0.5);
-    out[f] = cadd(Ev, cmul(Od, twb(tw, (long)f << (logTW - logd))));
-    if (f == 0) out[h] = csub(Ev, Od);
+    const double2 Ev = cadd(zf, cconj(zc)), Od = cmul_mi(csub(zf, cconj(zc)));   // both doubled
+    out[f] = half_sum_tw(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logd), logTW);
+    if (f == 0) out[h] = cscale(csub(Ev, Od), 0.5);
 }
 
 // ============================================================================
@@ -196,9 +195,8 @@ __global__ void __launch_bounds__(256) k_sbf_build_cols(SbfArgs A) {
         }
         double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
         if (g == 0) { E.y = 0.0; Dd.y = 0.0; }
-        const double2 O = (g == 0) ? Dd : cmulc(Dd, twb(A.tw, (long)g << (A.logTW - logD - 1)));
-        const double2 ug = cadd(E, cmul_pi(O));                 // U[g]
-        const double2 um = cadd(cconj(E), cmul_pi(cconj(O)));   // U[D - g]
+        double2 ug, um;   // U[g], U[D - g]
+        mirror_inv_input(E, Dd, tw_tangent(A.tw, A.logTW), (long)g << (A.logTW - logD - 1), A.logTW, ug, um);
         const int pa = c0 * M1 + (int)bitrev(r0, logM1);
         if (fa == g) {
             sx[pa] = ug;
@@ -324,10 +322,11 @@ __global__ void __launch_bounds__(256) k_sbf_build_rows2(SbfArgs A) {
         double2 a, b;
         if (fa < hD) { f = fa; a = za; b = cconj(zb); }
         else { f = D - 1 - fa; a = zb; b = cconj(za); }
-        const double2 Ep = cadd(a, b);
-        const double2 T = cmul(cmul_mi(csub(a, b)), twb(A.tw, (long)(2 * f + 1) << (A.logTW - logD - 2)));
-        ps[2 * f + 1] = cscale(cadd(Ep, T), kb);
-        ps[2 * (D - 1 - f) + 1] = cscale(cconj(csub(Ep, T)), kb);
+        double2 Hf, Hc;
+        mirror_out_pair(a, b, kb, tw_tangent(A.tw, A.logTW), (long)(2 * f + 1) << (A.logTW - logD - 2), A.logTW, Hf,
+                        Hc);
+        ps[2 * f + 1] = Hf;
+        ps[2 * (D - 1 - f) + 1] = Hc;
     }
 }
 
@@ -342,10 +341,8 @@ __device__ __forceinline__ void sbf_prop_input(const SbfArgs &A, int q, int c, i
     const double2 *S = A.cspec + q * A.cs_q + (size_t)sib * (D + 1);
     const double2 Y1 = cmulc(G[2 * f + 1], has_sib ? S[2 * f + 1] : one);
     const double2 Y2 = cconj(cmulc(G[2 * fp + 1], has_sib ? S[2 * fp + 1] : one));
-    const double2 Av = cadd(Y1, Y2);
-    const double2 Bv = cmulc(csub(Y1, Y2), twb(A.tw, (long)(2 * f + 1) << (A.logTW - A.logD - 1)));
-    xf = cadd(Av, cmul_pi(Bv));
-    xfp = cadd(cconj(Av), cmul_pi(cconj(Bv)));
+    mirror_inv_input(cadd(Y1, Y2), csub(Y1, Y2), tw_tangent(A.tw, A.logTW), (long)(2 * f + 1) << (A.logTW - A.logD - 1),
+                     A.logTW, xf, xfp);
 }
 
 // ---- propagate: child c's g spectrum bins f and h-f (f <= h/2) from the
@@ -391,10 +388,9 @@ __global__ void __launch_bounds__(512) k_sbf_prop_one(SbfArgs A) {
     }
     __syncthreads();
     smem_fft_dit<+1>(sx, lh, 1, A.tw, A.logTW);
-    smem_bitrev_map(sx, lh, 1, [&](int, int s, double2 v) -> double2 {
-        return (s == 0) ? v : cmulc(v, twb(A.tw, (long)s << (A.logTW - logD)));
-    });
-    smem_fft_dit<-1>(sx, lh, 1, A.tw, A.logTW);
+    // the untwist e^{+2 pi i s/D} is the forward transform's half shift by -1/2 bin
+    smem_bitrev_map(sx, lh, 1, [](int, int, double2 v) { return v; });
+    smem_fft_dit<-1, -1>(sx, lh, 1, A.tw, A.logTW);
     for (int f = threadIdx.x; f <= (h >> 1); f += blockDim.x)
         sbf_prop_output(A, q, c, f, sx[f & (h - 1)], sx[(h - f) & (h - 1)], out);
 }

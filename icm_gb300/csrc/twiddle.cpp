@@ -51,16 +51,22 @@ static void tangent_form(long t, long N, int *code, long double *r, long double 
     *tau = vy[best] / vx[best];
 }
 
-size_t twiddle_bytes(int logTW) { return sizeof(double2) * ((size_t)1 << logTW) + kTwExtraBytes; }
+size_t twiddle_bytes(int logTW) { return 2 * sizeof(double2) * ((size_t)1 << logTW) + kTwExtraBytes; }
 
 void fill_twiddles(int logTW, std::vector<unsigned char> &out) {
     const long N = 1L << logTW;
     out.assign(twiddle_bytes(logTW), 0);
     double2 *tw = (double2 *)out.data();
+    // and the plain entries in tangent form, the rotation from tan_code
+    double2 *tt = (double2 *)(out.data() + sizeof(double2) * (size_t)N + kTwExtraBytes);
     for (long t = 0; t < N; ++t) {
-        long double re, im;
-        unit_root_ld(t, N, &re, &im);
-        tw[t] = make_double2((double)re, (double)im);
+        long double wr, wi;
+        unit_root_ld(t, N, &wr, &wi);
+        tw[t] = make_double2((double)wr, (double)wi);
+        const long double vx[4] = {wr, -wi, -wr, wi};   // w / R
+        const long double vy[4] = {wi, wr, -wi, -wr};
+        const int c = tan_code(t, logTW);
+        tt[t] = make_double2((double)(vy[c] / vx[c]), (double)vx[c]);
     }
     // set 0: twiddles w^j; sets 1 and 2: w^{j + 1/2} and w^{j - 1/2}, the angle
     // (2j + sigma) over twice the group size

@@ -420,8 +420,9 @@ __device__ void adj_up_core(const AuView *V, const int *idx, int cnt, int nh, in
         const double2 Yc = cadd(cmul(sR[fc], GLc), cmul(sL[fc], GRc));
         double2 E = cadd(Yf, cconj(Yc)), D = csub(Yf, cconj(Yc));
         if (f == 0) { E.y = 0.0; D.y = 0.0; }
-        const double2 O = cmulc(D, __ldg(&tw[(long)f << (logTW - logN)]));
-        U[(size_t)it * h + bitrev(f, logN - 1)] = cadd(E, cmul_pi(O));
+        double2 Uf, Uc;   // O = D e^{+2 pi i f/N}; Uc unused
+        mirror_inv_input(E, D, tw_tangent(tw, logTW), (long)f << (logTW - logN), logTW, Uf, Uc);
+        U[(size_t)it * h + bitrev(f, logN - 1)] = Uf;
     }
     __syncthreads();
     smem_fft_dit<+1>(U, logN - 1, nh, tw, logTW);
@@ -629,8 +630,9 @@ __global__ void k_adj_up_mid(const double2 *__restrict__ Z, const double2 *__res
     const double2 Yc = cadd(cmul(sR[fc], GLc), cmul(sL[fc], GRc));
     double2 E = cadd(Yf, cconj(Yc)), D = csub(Yf, cconj(Yc));
     if (f == 0) { E.y = 0.0; D.y = 0.0; }
-    const double2 O = cmulc(D, __ldg(&tw[(long)f << (logTW - logN)]));
-    U[item * h + f] = cadd(E, cmul_pi(O));
+    double2 Uf, Uc;   // O = D e^{+2 pi i f/N}; Uc unused
+    mirror_inv_input(E, D, tw_tangent(tw, logTW), (long)f << (logTW - logN), logTW, Uf, Uc);
+    U[item * h + f] = Uf;
 }
 
 __global__ void k_adj_up_post(const double2 *__restrict__ U, int npairs, int N, double *__restrict__ gbp,

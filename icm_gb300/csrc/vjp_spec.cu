@@ -134,20 +134,14 @@ __device__ __forceinline__ void inv_input(double2 Cf, double2 Cc, int f, const d
                                           int logD, double2 &Uf, double2 &Uc) {
     double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
     if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
-    const double2 O = (f == 0) ? Dd : cmulc(Dd, twv(tw, (long)f << (logTW - logD - 1)));
-    Uf = cadd(E, cmul_pi(O));
-    Uc = cadd(cconj(E), cmul_pi(cconj(O)));
+    mirror_inv_input(E, Dd, tw_tangent(tw, logTW), (long)f << (logTW - logD - 1), logTW, Uf, Uc);
 }
 
 // odd bins of DFT_{4D} from the forward transform c of the twisted packing, mirror pair (f, D-1-f)
 __device__ __forceinline__ void odd_bins(double2 a, double2 bc, int f, const double2 *__restrict__ tw, int logTW,
                                          int logD, double2 &Hf, double2 &Hc) {
-    const double2 b = cconj(bc);
-    const double2 Ep = cadd(a, b);
-    const double2 T = cmul(cmul_mi(csub(a, b)), twv(tw, (long)(2 * f + 1) << (logTW - logD - 2)));
     const double kb = 1.0 / (4.0 * (1 << logD));
-    Hf = cscale(cadd(Ep, T), kb);
-    Hc = cscale(cconj(csub(Ep, T)), kb);
+    mirror_out_pair(a, cconj(bc), kb, tw_tangent(tw, logTW), (long)(2 * f + 1) << (logTW - logD - 2), logTW, Hf, Hc);
 }
 
 // ------------------------------------------------------------ one-CTA kernels
@@ -182,12 +176,11 @@ __device__ void vsp_real_body(const VspRealArgs &A, int bx, int q) {
         const int j = j0 + idx[it];
         const double2 *zz = sm + (size_t)it * M;
         const double2 zf = zz[f], zc = zz[(M - f) & (M - 1)];
-        const double2 Ev = cscale(cadd(zf, cconj(zc)), 0.5);
-        const double2 Od = cscale(cmul_mi(csub(zf, cconj(zc))), 0.5);
+        const double2 Ev = cadd(zf, cconj(zc)), Od = cmul_mi(csub(zf, cconj(zc)));   // both doubled
         double2 *out = A.out + q * A.o_q + (size_t)j * (M + 1);
-        out[f] = cadd(Ev, cmul(Od, twv(A.tw, (long)f << (A.logTW - A.logM - 1))));
+        out[f] = half_sum_tw(Ev, Od, tw_tangent(A.tw, A.logTW), (long)f << (A.logTW - A.logM - 1), A.logTW);
         if (f == 0) {
-            out[M] = csub(Ev, Od);
+            out[M] = cscale(csub(Ev, Od), 0.5);
             if (A.ends) {
                 const double *x = A.x + q * A.x_q + (size_t)j * A.xst;
                 double *en = A.ends + q * A.e_q + (size_t)j * 2;
@@ -245,13 +238,12 @@ __device__ void vsp_up_body(const VspUpArgs &A, int bx, int q) {
         }
         return;
     }
-    // 3. odd bins: twisted packing (y_{2s} + i y_{2s+1}) e^{-2 pi i s/2D}, forward transform
+    // 3. odd bins: twisted packing (y_{2s} + i y_{2s+1}) e^{-2 pi i s/2D}, forward
+    //    transform; the twist is the transform's half shift by +1/2 bin
     const double2 *tw = A.tw;
     const int logTW = A.logTW, logD = A.logD;
-    smem_bitrev_map(sm, logD, nh, [tw, logTW, logD](int, int s, double2 v) -> double2 {
-        return (s == 0) ? v : cmul(v, twv(tw, (long)s << (logTW - logD - 1)));
-    });
-    smem_fft_dit<-1>(sm, logD, nh, tw, logTW);
+    smem_bitrev_map(sm, logD, nh, [](int, int, double2 v) { return v; });
+    smem_fft_dit<-1, +1>(sm, logD, nh, tw, logTW);
     for (int e = threadIdx.x; e < nh * hD; e += blockDim.x) {
         const int it = e / hD, f = e - it * hD;
         const double2 *c = sm + (size_t)it * D;
@@ -326,16 +318,14 @@ __device__ void vsp_down_body(const VspDownArgs &A, int bx, int q) {
     }
     __syncthreads();
     smem_fft_dit<+1>(sm, lh, nh, tw, logTW);
-    // 2. untwist w_s = c'_s e^{+2 pi i s/D} into bit-reversed order; (a - b)[0] = w_0.x / D
+    // 2. untwist w_s = c'_s e^{+2 pi i s/D} (the forward transform's half shift
+    //    by -1/2 bin), into bit-reversed order; (a - b)[0] = w_0.x / D
     const double invD = 1.0 / D;
-    smem_bitrev_map(sm, lh, nh, [V, tw, logTW, logD, invD](int it, int s, double2 v) -> double2 {
-        if (s == 0) {
-            V[it].amb0 = v.x * invD;
-            return v;
-        }
-        return cmulc(v, twv(tw, (long)s << (logTW - logD)));
+    smem_bitrev_map(sm, lh, nh, [V, invD](int it, int s, double2 v) -> double2 {
+        if (s == 0) V[it].amb0 = v.x * invD;
+        return v;
     });
-    smem_fft_dit<-1>(sm, lh, nh, tw, logTW);
+    smem_fft_dit<-1, -1>(sm, lh, nh, tw, logTW);
     // 3. DFT_D(a) = Z_even/2 + DFT_D(a - b)/2 by mirror pairs (f, h - f), in
     //    place (bin h beside the view)
     const double kx = 1.0 / (8.0 * h);
