@@ -132,9 +132,12 @@ __device__ void fused_build_core(const FbView *V, const int *idx, int cnt, int n
     }
     __syncthreads();
     smem_fft_dit<-1>(Z, logN, nh, tw, logTW);
-    // 2. spectra of both children; half-size inverse input of their product
-    for (int e = threadIdx.x; e < nh * h; e += blockDim.x) {
-        const int it = e / h, f = e - it * h;
+    // 2. spectra of both children and the half-size inverse input of their
+    //    product, by mirror pairs of bins (f, h - f), f <= h/2
+    const double2 *tt = tw_tangent(tw, logTW);
+    const int hp = (h >> 1) + 1;
+    for (int e = threadIdx.x; e < nh * hp; e += blockDim.x) {
+        const int it = e / hp, f = e - it * hp;
         const double2 *z = Z + (size_t)it * N;
         const int fc = h - f;
         const double2 zf = z[f], zn = z[(N - f) & (N - 1)];
@@ -147,14 +150,15 @@ __device__ void fused_build_core(const FbView *V, const int *idx, int cnt, int n
         double2 *sR = sL + (h + 1);
         sL[f] = SLf;
         sR[f] = SRf;
-        if (f == 0) { sL[h] = SLc; sR[h] = SRc; }
+        if (fc != f) { sL[fc] = SLc; sR[fc] = SRc; }   // f = 0: bin h
         if (spectra_only) continue;
         const double2 Cf = cmul(SLf, SRf), Cc = cmul(SLc, SRc);
         double2 E = cadd(Cf, cconj(Cc)), D = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; D.y = 0.0; }
-        double2 Uf, Uc;   // O = D e^{+2 pi i f/N}; Uc unused
-        mirror_inv_input(E, D, tw_tangent(tw, logTW), (long)f << (logTW - logN), logTW, Uf, Uc);
+        double2 Uf, Uc;   // O = D e^{+2 pi i f/N}; Uc is U[h - f]
+        mirror_inv_input(E, D, tt, (long)f << (logTW - logN), logTW, Uf, Uc);
         U[(size_t)it * h + bitrev(f, logN - 1)] = Uf;
+        if (f != 0 && fc != f) U[(size_t)it * h + bitrev(fc, logN - 1)] = Uc;
     }
     if (spectra_only) return;
     __syncthreads();
@@ -199,26 +203,33 @@ __device__ void fused_prop_core(const FpView *V, const int *idx, int nh, int cb,
     }
     __syncthreads();
     smem_fft_dit<-1>(W, logN - 1, nh, tw, logTW);
-    // 2. G, then Z = G conj(S_R) + i G conj(S_L) over all N bins (bit-reversed)
-    for (int e = threadIdx.x; e < nh * h; e += blockDim.x) {
-        const int it = e / h, f = e - it * h;
+    // 2. G by mirror pairs of bins (f, h - f), f <= h/2 (G[h - f] =
+    //    conj(Ev - w Od) / 2), then Z = G conj(S_R) + i G conj(S_L) over all N
+    //    bins (bit-reversed)
+    const double2 *tt = tw_tangent(tw, logTW);
+    const int hp = (h >> 1) + 1;
+    for (int e = threadIdx.x; e < nh * hp; e += blockDim.x) {
+        const int it = e / hp, f = e - it * hp;
+        const int fc = h - f;
         const double2 *w = W + (size_t)it * h;
         const double2 *sL = V[idx[it]].sL;
         const double2 *sR = sL + (h + 1);
         double2 *z = Z + (size_t)it * N;
-        const double2 wf = w[f], wc = w[(h - f) & (h - 1)];
+        const double2 wf = w[f], wc = w[fc & (h - 1)];
         const double2 Ev = cadd(wf, cconj(wc)), Od = cmul_mi(csub(wf, cconj(wc)));   // both doubled
-        const double2 G = half_sum_tw(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logN), logTW);
-        const double2 YL = cmulc(G, sR[f]), YR = cmulc(G, sL[f]);
-        z[bitrev(f, logN)] = cadd(YL, cmul_pi(YR));
-        if (f != 0) {
-            z[bitrev(N - f, logN)] = cadd(cconj(YL), cmul_pi(cconj(YR)));
-        } else {
-            // bin h: W[h mod h] = W[0] on both sides; e^{-i pi} = -1
-            const double2 Gh = cscale(csub(Ev, Od), 0.5);
-            const double2 YLh = cmulc(Gh, sR[h]), YRh = cmulc(Gh, sL[h]);
-            z[bitrev(h, logN)] = cadd(YLh, cmul_pi(YRh));
-        }
+        double r;
+        const double2 u = tanmul_t<-1>(Od, tt, (long)f << (logTW - logN), logTW, &r);
+        const double hr = 0.5 * r;
+        const double2 E5 = cscale(Ev, 0.5);
+        const double2 Gf = make_double2(fma(hr, u.x, E5.x), fma(hr, u.y, E5.y));
+        const double2 Gc = make_double2(fma(-hr, u.x, E5.x), fma(hr, u.y, -E5.y));
+        auto bin = [&](int b, double2 G) {   // bins b and N - b
+            const double2 YL = cmulc(G, sR[b]), YR = cmulc(G, sL[b]);
+            z[bitrev(b, logN)] = cadd(YL, cmul_pi(YR));
+            if (b != 0 && b != h) z[bitrev(N - b, logN)] = cadd(cconj(YL), cmul_pi(cconj(YR)));
+        };
+        bin(f, Gf);
+        if (fc != f) bin(fc, Gc);   // f = 0: bin h (W[h mod h] = W[0]; e^{-i pi} = -1)
     }
     __syncthreads();
     smem_fft_dit<+1>(Z, logN, nh, tw, logTW);

@@ -400,8 +400,11 @@ __device__ void adj_up_core(const AuView *V, const int *idx, int cnt, int nh, in
     }
     __syncthreads();
     smem_fft_dit<-1>(Z, logN, nh, tw, logTW);
-    for (int e = threadIdx.x; e < nh * h; e += blockDim.x) {
-        const int it = e / h, f = e - it * h;
+    // by mirror pairs of bins (f, h - f), f <= h/2
+    const double2 *tt = tw_tangent(tw, logTW);
+    const int hp = (h >> 1) + 1;
+    for (int e = threadIdx.x; e < nh * hp; e += blockDim.x) {
+        const int it = e / hp, f = e - it * hp;
         const AuView &v = V[idx[it]];
         const double2 *z = Z + (size_t)it * N;
         const int fc = h - f;
@@ -415,14 +418,15 @@ __device__ void adj_up_core(const AuView *V, const int *idx, int cnt, int nh, in
         double2 *gL = v.gsL, *gR = gL + (h + 1);
         gL[f] = GLf;
         gR[f] = GRf;
-        if (f == 0) { gL[h] = GLc; gR[h] = GRc; }
+        if (fc != f) { gL[fc] = GLc; gR[fc] = GRc; }   // f = 0: bin h
         const double2 Yf = cadd(cmul(sR[f], GLf), cmul(sL[f], GRf));
         const double2 Yc = cadd(cmul(sR[fc], GLc), cmul(sL[fc], GRc));
         double2 E = cadd(Yf, cconj(Yc)), D = csub(Yf, cconj(Yc));
         if (f == 0) { E.y = 0.0; D.y = 0.0; }
-        double2 Uf, Uc;   // O = D e^{+2 pi i f/N}; Uc unused
-        mirror_inv_input(E, D, tw_tangent(tw, logTW), (long)f << (logTW - logN), logTW, Uf, Uc);
+        double2 Uf, Uc;   // O = D e^{+2 pi i f/N}; Uc is U[h - f]
+        mirror_inv_input(E, D, tt, (long)f << (logTW - logN), logTW, Uf, Uc);
         U[(size_t)it * h + bitrev(f, logN - 1)] = Uf;
+        if (f != 0 && fc != f) U[(size_t)it * h + bitrev(fc, logN - 1)] = Uc;
     }
     __syncthreads();
     smem_fft_dit<+1>(U, logN - 1, nh, tw, logTW);
