@@ -90,6 +90,7 @@ SIGNATURES = {
     "icm_gpu_equity_batched": (ctypes.c_int, [ctypes.c_int, _ip, _ip, _dp, _dp, ctypes.c_int, _dp,
                                               ctypes.POINTER(IcmGpuRunStats)]),
     "icm_gpu_measure_fp64_gflops": (ctypes.c_int, [_dp]),
+    "icm_gb300_leaf_factors": (ctypes.c_int, [ctypes.c_int, _dp, _dp]),
     "icm_gpu_last_launch_count": (ctypes.c_long, []),
     "icm_gb300_plan_set_profiling": (ctypes.c_int, [_vp, ctypes.c_int]),
     "icm_gb300_plan_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _dp,

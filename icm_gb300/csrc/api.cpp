@@ -859,6 +859,17 @@ int icm_gpu_measure_fp64_gflops(double *gflops_out) {
     });
 }
 
+int icm_gb300_leaf_factors(int n, const double *arg, double *out) {
+    return guarded<int>("icm_gb300_leaf_factors", -1, [&]() -> int {
+        if (n < 0 || (n > 0 && (!arg || !out))) { set_error("icm_gb300_leaf_factors: invalid arguments"); return -1; }
+        if (n == 0) return 0;
+        if (!ensure_device()) return -1;
+        std::string err;
+        if (leaf_factors(n, arg, out, err) != 0) { set_error(err); return -1; }
+        return 0;
+    });
+}
+
 long icm_gpu_last_launch_count(void) { return t_launches; }
 
 int icm_gb300_plan_set_profiling(IcmGpuPlan *plan, int enable) {

@@ -246,6 +246,7 @@ void fill_twiddles(int logTW, std::vector<unsigned char> &out);
 
 // probes (probes.cu)
 int measure_fp64_gflops(double *out, std::string &err);
+int leaf_factors(int n, const double *arg, double *out, std::string &err);
 int measure_hbm_gbps(double *out, std::string &err);
 
 // tuner table (tune.cpp)

@@ -44,6 +44,26 @@ __device__ __forceinline__ void leaf_body_t(const LeafArgs &A, int bx, int q) {
     for (int m = B + 1; m < pst0; ++m) leaf[m] = 0.0;
 }
 
+// leaf factors of given arguments, as the leaves compute them (checks)
+__global__ void k_leaf_factors(int n, const double *__restrict__ arg, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = leaf_factor(arg[i]);
+}
+
+int leaf_factors(int n, const double *arg, double *out, std::string &err) {
+    double *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(double) * 2 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(d, arg, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_leaf_factors<<<(n + 255) / 256, 256>>>(n, d, d + n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) { err = std::string("leaf factors: ") + cudaGetErrorString(e); return -1; }
+    return 0;
+}
+
 // one kernel per block size: registers sized for that B
 template <int B>
 __global__ void k_leaf_t(LeafArgs A) { leaf_body_t<B>(A, blockIdx.x, blockIdx.y); }

@@ -5,7 +5,45 @@
 
 #include <cuda_runtime.h>
 
+#include "exp2_table.cuh"
+
 namespace icmg {
+
+// exp(x) for -700 <= x <= 0 (the leaf factor's domain) by Tang's
+// table-driven method (P. T. P. Tang, "Table-driven implementation of the
+// exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2),
+// 1989) with a 128-entry table: x = (128 m + j) ln2/128 + r, |r| <= ln2/256,
+// and exp(x) = 2^m 2^(j/128) (1 + p(r)), p the degree-5 Taylor polynomial of
+// e^r - 1 (its truncation is below 6e-19 relative at |r| <= ln2/256).
+// 2^(j/128) is a double-double (exp2_table.cuh), ln2/128 a two-part constant
+// (the reduction's error is below 1e-18 relative), and the scaling by 2^m
+// (m >= -1010, so every result is a normal number) adds m to the exponent
+// field.  Error about 0.5 ulp; 11 FP64 instructions.
+__device__ __forceinline__ double exp_nonpos(double x) {
+    constexpr double kShift = 0x1.8p52;                // 1.5 2^52: rint into the low bits
+    constexpr double kInvLn2x128 = 0x1.71547652b82fep+7;
+    constexpr double kLn2hi = 0x1.62e42fefa39efp-8;    // ln2/128 = kLn2hi + kLn2lo
+    constexpr double kLn2lo = 0x1.abc9e3b39803fp-63;
+    const double t = fma(x, kInvLn2x128, kShift);
+    const int k = __double2loint(t);                    // rint(x 128/ln2)
+    const double kd = t - kShift;
+    double r = fma(kd, -kLn2hi, x);
+    r = fma(kd, -kLn2lo, r);
+    double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+    q = fma(q, r, 1.0 / 6.0);
+    q = fma(q, r, 0.5);
+    const double p = fma(q, r * r, r);
+    const int j = k & 127, m = k >> 7;                  // floor division: k < 0
+    const double thi = __ldg(&kExp2Tab[j][0]), tlo = __ldg(&kExp2Tab[j][1]);
+    const double y = thi + fma(thi, p, tlo);
+    return __hiloint2double(__double2hiint(y) + (m << 20), __double2loint(y));
+}
+
+// the leaf factor a = exp(S logv), 0 below -700 (reference src/cpu/icm.c:2575-2581)
+__device__ __forceinline__ double leaf_factor(double arg) {
+    if (arg < -700.0) return 0.0;
+    return arg <= 0.0 ? exp_nonpos(arg) : exp(arg);   // arg > 0 only for nodes v > 1 (none)
+}
 
 // Leaf factors and block product (reference src/cpu/icm.c:2199-2224,
 // src/gpu/gpu_kernels.cu:909-936,1030-1091): a_j = exp(S_j logv), 0 when the
@@ -24,8 +62,7 @@ __device__ __forceinline__ void block_product(const double *__restrict__ S, int 
 #pragma unroll
     for (int j = 0; j < B; ++j) {
         if (j >= bs) break;
-        const double arg = S[j] * logv;
-        const double a = (arg < -700.0) ? 0.0 : exp(arg);
+        const double a = leaf_factor(S[j] * logv);
         arow[j] = a;
         const double bb = 1.0 - a;
         P[j + 1] = bb * P[j];

@@ -29,6 +29,7 @@
 
 #include "engine.h"
 #include "kernels.h"
+#include "leafdiv.cuh"
 
 namespace icmg {
 
@@ -90,8 +91,7 @@ __device__ __forceinline__ void linear_t(const LinearArgs &A, int q, int q0) {
         const int i = j0 + lane;
         double al = 0.0;
         if (i < n) {
-            const double arg = A.S[i] * logv;
-            al = (arg < -700.0) ? 0.0 : exp(arg);
+            al = leaf_factor(A.S[i] * logv);
             arow[i] = al;
         }
         const int cnt = min(32, n - j0);

@@ -518,14 +518,14 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int *cid
             const double2 *z = sm + (size_t)kk * h;
             const double2 zf = z[f & (h - 1)], zc = cconj(z[fp & (h - 1)]);
             const double2 E = cadd(zf, zc);
-            const double2 T = (f == 0) ? cmul_mi(csub(zf, zc))
-                                       : cmul(cmul_mi(csub(zf, zc)), twl(tw, (long)f << (logTW - logD)));
+            double r;   // T = r u = -i (zf - zc) e^{-2 pi i f/D}
+            const double2 u = tanmul_t<-1>(cmul_mi(csub(zf, zc)), tt, (long)f << (logTW - logD), logTW, &r);
             const double2 Yf = cmulc(G[2 * f], S ? S[2 * f] : one);
-            const double2 Xf = cadd(E, T);
+            const double2 Xf = make_double2(fma(r, u.x, E.x), fma(r, u.y, E.y));
             out[f] = make_double2(fma(kx, Xf.x, 0.5 * Yf.x), fma(kx, Xf.y, 0.5 * Yf.y));
             if (fp != f) {
                 const double2 Yc = cmulc(G[2 * fp], S ? S[2 * fp] : one);
-                const double2 Xc = cconj(csub(E, T));
+                const double2 Xc = make_double2(fma(-r, u.x, E.x), fma(r, u.y, -E.y));   // conj(E - T)
                 out[fp] = make_double2(fma(kx, Xc.x, 0.5 * Yc.x), fma(kx, Xc.y, 0.5 * Yc.y));
             }
         }
@@ -555,8 +555,9 @@ __device__ void spec_prop_core(const SpView *V, const int *idx, int nh, int *cid
         const double2 Cc = cmulc(G[2 * (h - f)], S ? S[2 * (h - f)] : one);
         double2 E = cadd(Cf, cconj(Cc)), Dd = csub(Cf, cconj(Cc));
         if (f == 0) { E.y = 0.0; Dd.y = 0.0; }
-        const double2 O = cmulc(Dd, twl(tw, (long)f << (logTW - logD)));   // e^{+2 pi i f/D}
-        sm[(size_t)kk * h + bitrev(f, lh)] = cadd(E, cmul_pi(O));
+        double2 Uf, Uc;   // O = Dd e^{+2 pi i f/D}; Uc unused
+        mirror_inv_input(E, Dd, tt, (long)f << (logTW - logD), logTW, Uf, Uc);
+        sm[(size_t)kk * h + bitrev(f, lh)] = Uf;
     }
     __syncthreads();
     smem_fft_dit<+1>(sm, lh, nk, tw, logTW);

@@ -357,14 +357,16 @@ __device__ __forceinline__ void sbf_prop_output(const SbfArgs &A, int q, int c, 
     const double2 *S = A.cspec + q * A.cs_q + (size_t)sib * (D + 1);
     const double2 zf = zf0, zc = cconj(zc0);
     const double2 E = cadd(zf, zc);
-    const double2 T = (f == 0) ? cmul_mi(csub(zf, zc)) : cmul(cmul_mi(csub(zf, zc)), twb(A.tw, (long)f << (A.logTW - A.logD)));
+    double r;   // T = r u = -i (zf - zc) e^{-2 pi i f/D}
+    const double2 u =
+        tanmul_t<-1>(cmul_mi(csub(zf, zc)), tw_tangent(A.tw, A.logTW), (long)f << (A.logTW - A.logD), A.logTW, &r);
     const double kx = 1.0 / (8.0 * h);
     const double2 Yf = cmulc(G[2 * f], has_sib ? S[2 * f] : one);
-    const double2 Xf = cadd(E, T);
+    const double2 Xf = make_double2(fma(r, u.x, E.x), fma(r, u.y, E.y));
     out[f] = make_double2(fma(kx, Xf.x, 0.5 * Yf.x), fma(kx, Xf.y, 0.5 * Yf.y));
     if (fp != f) {
         const double2 Yc = cmulc(G[2 * fp], has_sib ? S[2 * fp] : one);
-        const double2 Xc = cconj(csub(E, T));
+        const double2 Xc = make_double2(fma(-r, u.x, E.x), fma(r, u.y, -E.y));   // conj(E - T)
         out[fp] = make_double2(fma(kx, Xc.x, 0.5 * Yc.x), fma(kx, Xc.y, 0.5 * Yc.y));
     }
 }

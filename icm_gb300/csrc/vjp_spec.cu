@@ -310,11 +310,12 @@ __device__ void vsp_down_body(const VspDownArgs &A, int bx, int q) {
         const DnView &v = V[it];
         const double2 Y1 = dn_z(v, 2 * f + 1);
         const double2 Y2 = cconj(dn_z(v, 2 * fp + 1));
-        const double2 Aa = cadd(Y1, Y2);
-        const double2 Bb = cmulc(csub(Y1, Y2), twv(tw, (long)(2 * f + 1) << (logTW - logD - 1)));
+        double2 Xf, Xc;   // A + i B, conj(A) + i conj(B), B = (Y1 - Y2) conj(w_f)
+        mirror_inv_input(cadd(Y1, Y2), csub(Y1, Y2), tw_tangent(tw, logTW), (long)(2 * f + 1) << (logTW - logD - 1),
+                         logTW, Xf, Xc);
         double2 *x = sm + (size_t)it * h;
-        x[bitrev(f, lh)] = cadd(Aa, cmul_pi(Bb));
-        if (fp != f) x[bitrev(fp, lh)] = cadd(cconj(Aa), cmul_pi(cconj(Bb)));
+        x[bitrev(f, lh)] = Xf;
+        if (fp != f) x[bitrev(fp, lh)] = Xc;
     }
     __syncthreads();
     smem_fft_dit<+1>(sm, lh, nh, tw, logTW);
@@ -337,14 +338,15 @@ __device__ void vsp_down_body(const VspDownArgs &A, int bx, int q) {
         double2 *zz = sm + (size_t)it * h;
         const double2 zf = zz[f & (h - 1)], zc = cconj(zz[fp & (h - 1)]);
         const double2 E = cadd(zf, zc);
-        const double2 T = (f == 0) ? cmul_mi(csub(zf, zc))
-                                   : cmul(cmul_mi(csub(zf, zc)), twv(tw, (long)f << (logTW - logD)));
+        double r;   // T = r u = -i (zf - zc) e^{-2 pi i f/D}
+        const double2 u =
+            tanmul_t<-1>(cmul_mi(csub(zf, zc)), tw_tangent(tw, logTW), (long)f << (logTW - logD), logTW, &r);
         const double2 Yf = dn_z(v, 2 * f);
-        const double2 Xf = cadd(E, T);
+        const double2 Xf = make_double2(fma(r, u.x, E.x), fma(r, u.y, E.y));
         const double2 of = make_double2(fma(kx, Xf.x, 0.5 * Yf.x), fma(kx, Xf.y, 0.5 * Yf.y));
         if (fp != f) {
             const double2 Yc = dn_z(v, 2 * fp);
-            const double2 Xc = cconj(csub(E, T));
+            const double2 Xc = make_double2(fma(-r, u.x, E.x), fma(r, u.y, -E.y));   // conj(E - T)
             const double2 oc = make_double2(fma(kx, Xc.x, 0.5 * Yc.x), fma(kx, Xc.y, 0.5 * Yc.y));
             if (fp == h) v.pfh = oc;
             else zz[fp] = oc;
@@ -484,11 +486,12 @@ __global__ void k_vsb_dn_in(VspDownArgs A) {
     const int fp = h - 1 - f;
     const double2 Y1 = dn_z(v, 2 * f + 1);
     const double2 Y2 = cconj(dn_z(v, 2 * fp + 1));
-    const double2 Aa = cadd(Y1, Y2);
-    const double2 Bb = cmulc(csub(Y1, Y2), twv(A.tw, (long)(2 * f + 1) << (A.logTW - A.logD - 1)));
+    double2 Xf, Xc;   // A + i B, conj(A) + i conj(B), B = (Y1 - Y2) conj(w_f)
+    mirror_inv_input(cadd(Y1, Y2), csub(Y1, Y2), tw_tangent(A.tw, A.logTW), (long)(2 * f + 1) << (A.logTW - A.logD - 1),
+                     A.logTW, Xf, Xc);
     double2 *x = A.buf + ((size_t)q * A.nreal_c + c) * h;
-    x[f] = cadd(Aa, cmul_pi(Bb));
-    if (fp != f) x[fp] = cadd(cconj(Aa), cmul_pi(cconj(Bb)));
+    x[f] = Xf;
+    if (fp != f) x[fp] = Xc;
 }
 
 // untwist after the inverse; (a - b)[0] parked in the child's first end slot
@@ -517,14 +520,15 @@ __global__ void k_vsb_dn_pf(VspDownArgs A) {
     const double kx = 1.0 / (8.0 * h);
     const double2 zf = zz[f & (h - 1)], zc = cconj(zz[fp & (h - 1)]);
     const double2 E = cadd(zf, zc);
-    const double2 T = (f == 0) ? cmul_mi(csub(zf, zc))
-                               : cmul(cmul_mi(csub(zf, zc)), twv(A.tw, (long)f << (A.logTW - A.logD)));
+    double r;   // T = r u = -i (zf - zc) e^{-2 pi i f/D}
+    const double2 u =
+        tanmul_t<-1>(cmul_mi(csub(zf, zc)), tw_tangent(A.tw, A.logTW), (long)f << (A.logTW - A.logD), A.logTW, &r);
     const double2 Yf = dn_z(v, 2 * f);
-    const double2 Xf = cadd(E, T);
+    const double2 Xf = make_double2(fma(r, u.x, E.x), fma(r, u.y, E.y));
     out[f] = make_double2(fma(kx, Xf.x, 0.5 * Yf.x), fma(kx, Xf.y, 0.5 * Yf.y));
     if (fp != f) {
         const double2 Yc = dn_z(v, 2 * fp);
-        const double2 Xc = cconj(csub(E, T));
+        const double2 Xc = make_double2(fma(-r, u.x, E.x), fma(r, u.y, -E.y));   // conj(E - T)
         out[fp] = make_double2(fma(kx, Xc.x, 0.5 * Yc.x), fma(kx, Xc.y, 0.5 * Yc.y));
     }
 }

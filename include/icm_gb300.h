@@ -285,6 +285,11 @@ int icm_gb300_equity_adaptive(int n, const double *S, const double *payout, int 
  * all SMs, in GFLOP/s (2 flops per DFMA).  Returns 1 / 0. */
 int icm_gpu_measure_fp64_gflops(double *gflops_out);
 
+/* The leaf factors a = exp(arg) (0 below -700) of n arguments, computed on
+ * the GPU exactly as the tree's leaves compute them (a check of the device
+ * exponential against the host's).  Returns 0 / -1. */
+int icm_gb300_leaf_factors(int n, const double *arg, double *out);
+
 /* Number of kernels the last equity call launched (for benchmarks). */
 long icm_gpu_last_launch_count(void);
 
