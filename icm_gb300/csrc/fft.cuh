@@ -169,6 +169,14 @@ __device__ __forceinline__ double2 half_sum_tw(double2 a, double2 b, const doubl
     return make_double2(fma(hr, u.x, 0.5 * a.x), fma(hr, u.y, 0.5 * a.y));
 }
 
+// the twiddle between the four-step passes, W_M^{n2 (k1 + SHIFT/2)}: index
+// into the plain table (SHIFT = 0: n2 k1 mod M, else n2 (2 k1 + SHIFT) mod 2M)
+template <int SHIFT>
+__device__ __forceinline__ long fft4_tw_index(int n2, int k1, int logM, int logTW) {
+    if (SHIFT == 0) return (long)((n2 * k1) & ((1 << logM) - 1)) << (logTW - logM);
+    return (long)((n2 * (2 * k1 + SHIFT)) & ((2 << logM) - 1)) << (logTW - logM - 1);
+}
+
 // `cnt` transforms of size 2^logM stored back to back in x (shared memory),
 // each already in bit-reversed order.  All threads of the block take part;
 // the caller synchronises before (after filling x) and this function ends

@@ -223,7 +223,7 @@ __device__ __forceinline__ bool fft_skip(const FftSkip &k, long item) {
     return (j + 1) * k.span <= (long)k.zp[k.q0 + q];
 }
 
-template <int SIGN>
+template <int SIGN, int SHIFT = 0>
 __global__ void k_fft_smem(double2 *__restrict__ data, long batch, int logM, int cb,
                            const double2 *__restrict__ tw, int logTW, FftSkip skip) {
     extern __shared__ double2 sx[];
@@ -240,12 +240,14 @@ __global__ void k_fft_smem(double2 *__restrict__ data, long batch, int logM, int
         sx[e] = data[(item0 + it) * M + bitrev(s, logM)];
     }
     __syncthreads();
-    smem_fft_dit<SIGN>(sx, logM, cnt, tw, logTW);
+    smem_fft_dit<SIGN, SHIFT>(sx, logM, cnt, tw, logTW);
     for (int e = threadIdx.x; e < cnt * M; e += blockDim.x) data[item0 * M + e] = sx[e];
 }
 
-// four-step, pass A: columns n2 of the M1 x M2 view x[M2 n1 + n2]
-template <int SIGN>
+// four-step, pass A: columns n2 of the M1 x M2 view x[M2 n1 + n2]; SHIFT =
+// +1 / -1 makes the whole transform half-shifted (forward only): half-shifted
+// column transforms and twiddles W_M^{n2 (k1 + SHIFT/2)}, plain rows
+template <int SIGN, int SHIFT = 0>
 __global__ void k_fft4_cols(const double2 *__restrict__ in, double2 *__restrict__ out, int logM1, int logM2,
                             int cb, const double2 *__restrict__ tw, int logTW, FftSkip skip) {
     extern __shared__ double2 sx[];
@@ -259,15 +261,15 @@ __global__ void k_fft4_cols(const double2 *__restrict__ in, double2 *__restrict_
         sx[c * M1 + s] = src[(long)bitrev(s, logM1) * M2 + n20 + c];
     }
     __syncthreads();
-    smem_fft_dit<SIGN>(sx, logM1, cb, tw, logTW);
+    smem_fft_dit<SIGN, SHIFT>(sx, logM1, cb, tw, logTW);
     const int logM = logM1 + logM2;
     double2 *dst = out + (item << logM);
     for (int e = threadIdx.x; e < cb * M1; e += blockDim.x) {
         const int c = e >> logM1, k1 = e & (M1 - 1);
         const int n2 = n20 + c;
-        const int t = (n2 * k1) & ((1 << logM) - 1);
+        const long t = fft4_tw_index<SHIFT>(n2, k1, logM, logTW);
         double2 v = sx[e];
-        if (t) v = twmul<SIGN>(v, __ldg(&tw[(long)t << (logTW - logM)]));
+        if (t) v = twmul<SIGN>(v, __ldg(&tw[t]));
         dst[(long)n2 * M1 + k1] = v;
     }
 }
@@ -296,7 +298,7 @@ __global__ void k_fft4_rows(const double2 *__restrict__ in, double2 *__restrict_
 }
 
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
-                cudaStream_t st, long *launches, Prof *pr, FftSkip skip) {
+                cudaStream_t st, long *launches, Prof *pr, FftSkip skip, int shift) {
     if (batch <= 0) return 0;
     const int M = 1 << logM;
     const int threads = 256;
@@ -308,7 +310,11 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
         // memory: twice the warps to hide the butterflies' latency
         const int tpb = smem > kOneCtaSmem ? 512 : threads;
         pr->begin("fft_smem", 5.0 * M * logM * (double)batch, st);
-        if (sign < 0)
+        if (shift > 0)
+            k_fft_smem<-1, +1><<<(unsigned)blocks, tpb, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
+        else if (shift < 0)
+            k_fft_smem<-1, -1><<<(unsigned)blocks, tpb, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
+        else if (sign < 0)
             k_fft_smem<-1><<<(unsigned)blocks, tpb, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
         else
             k_fft_smem<+1><<<(unsigned)blocks, tpb, smem, st>>>(data, batch, logM, cb, tw, logTW, skip);
@@ -321,7 +327,7 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
             FftSkip sk = skip;
             sk.item0 += b0;
             fft_batched(data + (b0 << logM), scratch + (b0 << logM), std::min(65535L, batch - b0), logM, sign, tw,
-                        logTW, st, launches, pr, sk);
+                        logTW, st, launches, pr, sk, shift);
         }
         return 0;
     }
@@ -333,7 +339,9 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
     dim3 gA(M2 / cbA, (unsigned)batch), gB(M1 / cbB, (unsigned)batch);
     const size_t smA = (size_t)cbA * M1 * sizeof(double2), smB = (size_t)cbB * M2 * sizeof(double2);
     pr->begin("fft4_cols", (5.0 * logM1 + 6.0) * M * (double)batch, st);
-    if (sign < 0) k_fft4_cols<-1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    if (shift > 0) k_fft4_cols<-1, +1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    else if (shift < 0) k_fft4_cols<-1, -1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    else if (sign < 0) k_fft4_cols<-1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
     else k_fft4_cols<+1><<<gA, threads, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
     pr->end(st);
     pr->begin("fft4_rows", 5.0 * logM2 * M * (double)batch, st);
@@ -347,14 +355,14 @@ int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign,
 std::atomic<long> g_tma_launches{0};
 
 void launch_fft4_cols(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
-                      int logTW, cudaStream_t st, long *launches, Prof *pr, FftSkip skip) {
+                      int logTW, cudaStream_t st, long *launches, Prof *pr, FftSkip skip, int shift) {
     if (batch <= 0) return;
     if (batch > 65535) {   // grid.y limit
         for (long b0 = 0; b0 < batch; b0 += 65535) {
             FftSkip sk = skip;
             sk.item0 += b0;
             launch_fft4_cols(data + (b0 << logM), scratch + (b0 << logM), std::min(65535L, batch - b0), logM, sign, tw,
-                             logTW, st, launches, pr, sk);
+                             logTW, st, launches, pr, sk, shift);
         }
         return;
     }
@@ -368,12 +376,12 @@ void launch_fft4_cols(const double2 *data, double2 *scratch, long batch, int log
     // bitwise the same); the plain gathers where a tensor map cannot be made
     // or the configuration asks for them
     const bool tma = g_config.disable_tma != 1 && launch_fft4_cols_tma(data, scratch, batch, logM, sign, tw, logTW,
-                                                                       cbA, st, skip);
+                                                                       cbA, st, skip, shift);
     if (tma) ++g_tma_launches;
-    else {
-        if (sign < 0) k_fft4_cols<-1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
-        else k_fft4_cols<+1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
-    }
+    else if (shift > 0) k_fft4_cols<-1, +1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    else if (shift < 0) k_fft4_cols<-1, -1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    else if (sign < 0) k_fft4_cols<-1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
+    else k_fft4_cols<+1><<<gA, 256, smA, st>>>(data, scratch, logM1, logM2, cbA, tw, logTW, skip);
     pr->end(st);
     ++*launches;
 }
@@ -391,8 +399,12 @@ void fft_set_smem_limits() {
     const int mx = kSmemFftMax * (int)sizeof(double2);
     cudaFuncSetAttribute(k_fft_smem<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft_smem<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft_smem<-1, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft_smem<-1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft4_cols<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft4_cols<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_cols<-1, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_cols<-1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft4_rows<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fft4_rows<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }

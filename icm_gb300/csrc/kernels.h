@@ -408,15 +408,17 @@ struct FftSkip {
     int per_q = 1;
     long item0 = 0;
 };
+// shift = +1 / -1 (forward only): the transforms half-shifted by +1/2 / -1/2 bin
 int fft_batched(double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw, int logTW,
-                cudaStream_t st, long *launches, Prof *pr, FftSkip skip = FftSkip());
-// the column pass alone of fft_batched's four-step split (data -> scratch)
+                cudaStream_t st, long *launches, Prof *pr, FftSkip skip = FftSkip(), int shift = 0);
+// the column pass alone of fft_batched's four-step split (data -> scratch);
+// shift = +1 / -1 (forward only): the transform half-shifted by +1/2 / -1/2 bin
 void launch_fft4_cols(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
-                      int logTW, cudaStream_t st, long *launches, Prof *pr, FftSkip skip = FftSkip());
+                      int logTW, cudaStream_t st, long *launches, Prof *pr, FftSkip skip = FftSkip(), int shift = 0);
 void specbig_set_smem_limits();
 // the column pass with its tile staged by TMA (tma_cols.cu); false: not launched
 bool launch_fft4_cols_tma(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
-                          int logTW, int cbA, cudaStream_t st, FftSkip skip);
+                          int logTW, int cbA, cudaStream_t st, FftSkip skip, int shift = 0);
 void tma_set_smem_limits();
 int tma_take_failures();
 extern std::atomic<long> g_tma_launches;   // column passes launched through TMA (all plans)

@@ -18,7 +18,6 @@ static inline int ilog2b(long v) {
     return l;
 }
 static inline unsigned nb(long work, int threads) { return (unsigned)((work + threads - 1) / threads); }
-__device__ __forceinline__ double2 twb(const double2 *__restrict__ tw, long idx) { return __ldg(&tw[idx]); }
 // tree node `node` of chunk node q lies wholly inside the zero prefix
 __device__ __forceinline__ bool zcold(const int *__restrict__ zp, int zq0, long span, int q, long node) {
     return zp && (node + 1) * span <= (long)zp[zq0 + q];
@@ -69,14 +68,15 @@ __global__ void k_sb_gpost(int nreal, int logd, const double2 *__restrict__ buf,
 //
 //   build (transform size D):  column pass loading the product spectrum's
 //     inverse input U from the children's spectra (mirror bins f, D - f),
-//     row pass storing the coefficients / ends and the twisted sequence, a
-//     plain column pass, and a row pass storing the parent's odd bins (mirror
-//     bins f, D - 1 - f);
+//     row pass storing the coefficients / ends and the sequence, a column pass
+//     half-shifted by +1/2 bin (the twist, folded into its twiddles), and a
+//     row pass storing the parent's odd bins (mirror bins f, D - 1 - f);
 //   propagate (size h = D/2, per child): column pass loading the inverse
 //     half-bin input from the parent's g spectrum and the sibling's spectrum
-//     (mirror bins f, h - 1 - f), row pass storing the untwisted sequence, a
-//     plain column pass, and a row pass storing the child's g spectrum (mirror
-//     bins f, h - f); children with h <= kSmemFftMax run all of it in one CTA.
+//     (mirror bins f, h - 1 - f), row pass storing the sequence, a column pass
+//     half-shifted by -1/2 bin (the untwist), and a row pass storing the
+//     child's g spectrum (mirror bins f, h - f); children with h <= kSmemFftMax
+//     run all of it in one CTA.
 //
 // A mirror pair's two bins lie in two columns (rows) that map onto each other,
 // so a CTA holds whole mirror-paired columns (rows): slot 0 = {0, M/2} (each
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(256) k_sbf_build_cols(SbfArgs A) {
     }
 }
 
-// ---- build, pass 2: rows of the inverse; coefficients, ends, endpoint fix, twist
+// ---- build, pass 2: rows of the inverse; coefficients, ends, endpoint fix
 __global__ void __launch_bounds__(256) k_sbf_build_rows1(SbfArgs A) {
     extern __shared__ double2 sx[];
     const int j = blockIdx.y, q = blockIdx.z;
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256) k_sbf_build_rows1(SbfArgs A) {
             u.x = (x0 - xtop) * (2.0 * D);
             if (A.pspec) up[0] = u;
         } else if (A.pspec) {
-            up[s] = cmul(u, twb(A.tw, (long)s << (A.logTW - logD - 1)));
+            up[s] = u;   // the twist e^{-2 pi i s/2D} is the next column pass's half shift
         }
     }
 }
@@ -429,7 +429,8 @@ __global__ void __launch_bounds__(256) k_sbf_prop_cols(SbfArgs A) {
     }
 }
 
-// ---- propagate, pass 2: rows; untwist (unscaled) into buf
+// ---- propagate, pass 2: rows into buf (the untwist e^{+2 pi i s/D} is the
+// next column pass's half shift by -1/2 bin)
 __global__ void __launch_bounds__(256) k_sbf_prop_rows1(SbfArgs A) {
     extern __shared__ double2 sx[];
     const int c = blockIdx.y, q = blockIdx.z;
@@ -448,9 +449,7 @@ __global__ void __launch_bounds__(256) k_sbf_prop_rows1(SbfArgs A) {
     double2 *x = A.buf + item * h;
     for (int e = threadIdx.x; e < cb * M2; e += blockDim.x) {
         const int cc = e % cb, k2 = e / cb;
-        const int s = k2 * M1 + k10 + cc;
-        const double2 v = sx[cc * M2 + k2];
-        x[s] = (s == 0) ? v : cmulc(v, twb(A.tw, (long)s << (A.logTW - logD)));
+        x[k2 * M1 + k10 + cc] = sx[cc * M2 + k2];
     }
 }
 
@@ -556,7 +555,7 @@ void launch_specbig_build(const Level &c, const Level &p, bool write_coeffs, int
     sk.q0 = zq0;
     sk.span = p.deg;
     sk.per_q = p.nreal;
-    launch_fft4_cols(buf, scratch, items, logD, -1, tw, logTW, st, launches, pr, sk);
+    launch_fft4_cols(buf, scratch, items, logD, -1, tw, logTW, st, launches, pr, sk, +1);   // half-shifted
     A.cb = cbB;
     pr->begin("specbig_build", 5.0 * A.logM2 * pts + pts * 8.0, st);
     k_sbf_build_rows2<<<dim3(M1 / cbB, p.nreal, nq), 256, (size_t)cbB * M2 * sizeof(double2), st>>>(A);
@@ -611,7 +610,7 @@ void launch_specbig_prop(const double2 *Gp, size_t Gp_q, const Level &c, int nq,
     sk.q0 = zq0;
     sk.span = c.deg;
     sk.per_q = c.nreal;
-    launch_fft4_cols(buf, scratch, items, logh, -1, tw, logTW, st, launches, pr, sk);
+    launch_fft4_cols(buf, scratch, items, logh, -1, tw, logTW, st, launches, pr, sk, -1);   // half-shifted
     A.cb = cbB;
     pr->begin("specbig_prop", 5.0 * A.logM2 * pts + pts * 14.0, st);
     k_sbf_prop_rows2<<<dim3(M1 / cbB, c.nreal, nq), 256, (size_t)cbB * M2 * sizeof(double2), st>>>(A);

@@ -46,10 +46,10 @@ __device__ __forceinline__ unsigned smem_u32(const void *p) {
 
 // The column transforms of `cnt` items stored with stride `cnt`: element i of
 // item c at x[i cnt + c]; bit-reversed input, natural output (smem_fft_dit's
-// passes, addressed through the stride).
-template <int SIGN>
+// passes, addressed through the stride, its half shifts included).
+template <int SIGN, int SHIFT>
 __device__ void smem_fft_dit_strided(double2 *x, int logM, int cnt, const double2 *__restrict__ tw, int logTW) {
-    const TwTables T = tw_tables(tw, logTW);
+    const TwTables T = tw_tables(tw, logTW, tw_set(SHIFT));
     const int M = 1 << logM;
     int s = 0;
     for (; s + 1 < logM; s += 2) {
@@ -64,7 +64,7 @@ __device__ void smem_fft_dit_strided(double2 *x, int logM, int cnt, const double
             const size_t hs = (size_t)h * cnt;
             const double2 a = xi[0], bq = xi[hs], c = xi[2 * hs], d = xi[3 * hs];
             double2 x0, x1, x2, x3;
-            if (h == 1) {
+            if (SHIFT == 0 && h == 1) {
                 const double2 s0 = cadd(a, bq), d0 = csub(a, bq);
                 const double2 s1 = cadd(c, d), d1 = csub(c, d);
                 x0 = cadd(s0, s1);
@@ -120,7 +120,7 @@ __device__ void smem_fft_dit_strided(double2 *x, int logM, int cnt, const double
     (void)M;
 }
 
-template <int SIGN>
+template <int SIGN, int SHIFT>
 __global__ void __launch_bounds__(256) k_fft4_cols_tma(const __grid_constant__ CUtensorMap tmap,
                                                        double2 *__restrict__ out, int logM1, int logM2, int cb,
                                                        const double2 *__restrict__ tw, int logTW, FftSkip skip,
@@ -172,15 +172,15 @@ __global__ void __launch_bounds__(256) k_fft4_cols_tma(const __grid_constant__ C
         tile[(size_t)rr * cb + c] = va;
     }
     __syncthreads();
-    smem_fft_dit_strided<SIGN>(tile, logM1, cb, tw, logTW);
+    smem_fft_dit_strided<SIGN, SHIFT>(tile, logM1, cb, tw, logTW);
     const int logM = logM1 + logM2;
     double2 *dst = out + (item << logM);
     for (int e = threadIdx.x; e < cb * M1; e += blockDim.x) {
         const int c = e >> logM1, k1 = e & (M1 - 1);
         const int n2 = n20 + c;
-        const int t = (n2 * k1) & ((1 << logM) - 1);
+        const long t = fft4_tw_index<SHIFT>(n2, k1, logM, logTW);
         double2 v = tile[(size_t)k1 * cb + c];
-        if (t) v = twmul<SIGN>(v, __ldg(&tw[(long)t << (logTW - logM)]));
+        if (t) v = twmul<SIGN>(v, __ldg(&tw[t]));
         dst[(long)n2 * M1 + k1] = v;
     }
 }
@@ -207,15 +207,17 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 void tma_set_smem_limits() {
     const int mx = 4096 * (int)sizeof(double2);
-    cudaFuncSetAttribute(k_fft4_cols_tma<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_fft4_cols_tma<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_cols_tma<-1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_cols_tma<+1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_cols_tma<-1, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fft4_cols_tma<-1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
 // The column pass of a four-step transform of `batch` items (batch <= 65535)
 // through a tensor map; false (nothing launched) where the map cannot be
 // made, so that the caller runs the plain pass.
 bool launch_fft4_cols_tma(const double2 *data, double2 *scratch, long batch, int logM, int sign, const double2 *tw,
-                          int logTW, int cbA, cudaStream_t st, FftSkip skip) {
+                          int logTW, int cbA, cudaStream_t st, FftSkip skip, int shift) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc || batch > 65535) return false;
     const int logM1 = (logM + 1) / 2, logM2 = logM - logM1;
@@ -232,8 +234,10 @@ bool launch_fft4_cols_tma(const double2 *data, double2 *scratch, long batch, int
         return false;
     const dim3 g(M2 / cbA, (unsigned)batch);
     const size_t sm = (size_t)cbA * M1 * sizeof(double2);
-    if (sign < 0) k_fft4_cols_tma<-1><<<g, 256, sm, st>>>(tmap, scratch, logM1, logM2, cbA, tw, logTW, skip, 0);
-    else k_fft4_cols_tma<+1><<<g, 256, sm, st>>>(tmap, scratch, logM1, logM2, cbA, tw, logTW, skip, 0);
+    if (shift > 0) k_fft4_cols_tma<-1, +1><<<g, 256, sm, st>>>(tmap, scratch, logM1, logM2, cbA, tw, logTW, skip, 0);
+    else if (shift < 0) k_fft4_cols_tma<-1, -1><<<g, 256, sm, st>>>(tmap, scratch, logM1, logM2, cbA, tw, logTW, skip, 0);
+    else if (sign < 0) k_fft4_cols_tma<-1, 0><<<g, 256, sm, st>>>(tmap, scratch, logM1, logM2, cbA, tw, logTW, skip, 0);
+    else k_fft4_cols_tma<+1, 0><<<g, 256, sm, st>>>(tmap, scratch, logM1, logM2, cbA, tw, logTW, skip, 0);
     return true;
 }
 

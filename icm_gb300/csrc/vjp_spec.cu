@@ -59,8 +59,6 @@ inline unsigned nbv(long work, int threads) { return (unsigned)((work + threads 
 inline int vsp_cb(int pts) { return std::min(kVspMaxItems, pts >= kVspPts ? 1 : kVspPts / pts); }
 }  // namespace
 
-__device__ __forceinline__ double2 twv(const double2 *__restrict__ tw, long idx) { return __ldg(&tw[idx]); }
-
 // idx[0, nh) = items to compute, idx[nh, cnt) = wholly-zero ones, in order
 __device__ __forceinline__ int vsp_partition(int *idx, int cnt, const ZeroPrefix &z, int q, int node0) {
     __shared__ int nh_s;
@@ -435,7 +433,8 @@ __global__ void k_vsb_up_in(VspUpArgs A) {
     if (f != 0 && f != hD) u[D - f] = Uc;
 }
 
-// after the inverse: coefficients (zero for wholly-zero parents), or the twist
+// after the inverse, where the level above works on coefficients: the
+// parents' gbar coefficients (zero for wholly-zero parents)
 __global__ void k_vsb_up_mid(VspUpArgs A, int W) {
     const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
@@ -443,18 +442,13 @@ __global__ void k_vsb_up_mid(VspUpArgs A, int W) {
     const int j = (int)(e / W), s = (int)(e % W);
     if (j >= A.nreal_p) return;
     const bool cold = zp_cold(A.z, q, j);
-    double2 *u = A.buf + ((size_t)q * A.nreal_p + j) * D;
-    if (!A.Aout) {
-        double *go = A.gout + q * A.go_q + (size_t)j * A.gst;
-        const double2 v = (!cold && s < D) ? u[s] : make_double2(0.0, 0.0);
-        const double inv2D = 1.0 / (2.0 * D);
-        const int t0 = 2 * s, t1 = 2 * s + 1;
-        if (t0 < A.gst) go[t0] = t0 < A.glen ? v.x * inv2D : 0.0;
-        if (t1 < A.gst) go[t1] = t1 < A.glen ? v.y * inv2D : 0.0;
-        return;
-    }
-    if (cold || s == 0) return;
-    u[s] = cmul(u[s], twv(A.tw, (long)s << (A.logTW - A.logD - 1)));
+    const double2 *u = A.buf + ((size_t)q * A.nreal_p + j) * D;
+    double *go = A.gout + q * A.go_q + (size_t)j * A.gst;
+    const double2 v = (!cold && s < D) ? u[s] : make_double2(0.0, 0.0);
+    const double inv2D = 1.0 / (2.0 * D);
+    const int t0 = 2 * s, t1 = 2 * s + 1;
+    if (t0 < A.gst) go[t0] = t0 < A.glen ? v.x * inv2D : 0.0;
+    if (t1 < A.gst) go[t1] = t1 < A.glen ? v.y * inv2D : 0.0;
 }
 
 __global__ void k_vsb_up_odd(VspUpArgs A) {
@@ -494,16 +488,15 @@ __global__ void k_vsb_dn_in(VspDownArgs A) {
     if (fp != f) x[fp] = Xc;
 }
 
-// untwist after the inverse; (a - b)[0] parked in the child's first end slot
-__global__ void k_vsb_dn_untwist(VspDownArgs A) {
-    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+// after the inverse: (a - b)[0] parked in the child's first end slot (the
+// untwist is the next forward transform's half shift by -1/2 bin)
+__global__ void k_vsb_dn_park(VspDownArgs A) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     const int D = 1 << A.logD, h = D >> 1;
-    const int c = (int)(e / h), s = (int)(e % h);
     if (c >= A.nreal_c || zp_cold(A.z, q, c)) return;
-    double2 *x = A.buf + ((size_t)q * A.nreal_c + c) * h;
-    if (s == 0) A.Peout[q * A.Peo_q + (size_t)c * 2] = x[0].x * (1.0 / D);
-    else x[s] = cmulc(x[s], twv(A.tw, (long)s << (A.logTW - A.logD)));
+    const double2 *x = A.buf + ((size_t)q * A.nreal_c + c) * h;
+    A.Peout[q * A.Peo_q + (size_t)c * 2] = x[0].x * (1.0 / D);
 }
 
 // DFT_D(a) by mirror pairs (f, h - f) into the child's spectrum row (no fold correction yet)
@@ -755,7 +748,7 @@ void adj_spec_up(Plan *p, const VjpBufs &b, int l, int nq, int q0, const double2
         ++launches;
         return;
     }
-    // multi-pass: inverse input, inverse, coefficients or twist, forward, odd bins
+    // multi-pass: inverse input, inverse, then coefficients or a half-shifted forward transform and the odd bins
     A.buf = p->d_fa;
     const FftSkip sk{zp, q0, pl.deg, pl.nreal, 0};
     const long items = (long)nq * pl.nreal;
@@ -764,18 +757,22 @@ void adj_spec_up(Plan *p, const VjpBufs &b, int l, int nq, int q0, const double2
     k_vsb_up_in<<<dim3(nbv((long)pl.nreal * (D / 2 + 1), 256), nq), 256, 0, st>>>(A);
     pr->end(st);
     fft_batched(A.buf, p->d_fc, items, logD, +1, tw, logTW, st, &launches, pr, sk);
-    const int W = spec_out ? D : std::max(D, (A.gst + 1) / 2);
-    pr->begin("adj_specbig_up_mid", pw, st);
-    k_vsb_up_mid<<<dim3(nbv((long)pl.nreal * W, 256), nq), 256, 0, st>>>(A, W);
-    pr->end(st);
-    launches += 2;
-    if (spec_out) {
-        fft_batched(A.buf, p->d_fc, items, logD, -1, tw, logTW, st, &launches, pr, sk);
-        pr->begin("adj_specbig_up_odd", pw, st);
-        k_vsb_up_odd<<<dim3(nbv((long)pl.nreal * (D / 2), 256), nq), 256, 0, st>>>(A);
+    ++launches;
+    if (!spec_out) {   // the level above works on coefficients
+        const int W = std::max(D, (A.gst + 1) / 2);
+        pr->begin("adj_specbig_up_mid", pw, st);
+        k_vsb_up_mid<<<dim3(nbv((long)pl.nreal * W, 256), nq), 256, 0, st>>>(A, W);
         pr->end(st);
         ++launches;
+        return;
     }
+    // odd bins: the forward transform of the twisted packing, the twist
+    // e^{-2 pi i s/2D} folded into the transform as its half shift
+    fft_batched(A.buf, p->d_fc, items, logD, -1, tw, logTW, st, &launches, pr, sk, +1);
+    pr->begin("adj_specbig_up_odd", pw, st);
+    k_vsb_up_odd<<<dim3(nbv((long)pl.nreal * (D / 2), 256), nq), 256, 0, st>>>(A);
+    pr->end(st);
+    ++launches;
     (void)fl;
 }
 
@@ -812,10 +809,10 @@ void adj_spec_down(Plan *p, const VjpBufs &b, int l, int nq, int q0, const doubl
     k_vsb_dn_in<<<dim3(nbv((long)c.nreal * ((h + 1) / 2), 256), nq), 256, 0, st>>>(A);
     pr->end(st);
     fft_batched(A.buf, p->d_fc, items, lh, +1, tw, logTW, st, &launches, pr, sk);
-    pr->begin("adj_specbig_down_untwist", pw, st);
-    k_vsb_dn_untwist<<<dim3(nbv((long)c.nreal * h, 256), nq), 256, 0, st>>>(A);
+    pr->begin("adj_specbig_down_park", 0.0, st);
+    k_vsb_dn_park<<<dim3(nbv(c.nreal, 256), nq), 256, 0, st>>>(A);
     pr->end(st);
-    fft_batched(A.buf, p->d_fc, items, lh, -1, tw, logTW, st, &launches, pr, sk);
+    fft_batched(A.buf, p->d_fc, items, lh, -1, tw, logTW, st, &launches, pr, sk, -1);   // half-shifted: the untwist
     pr->begin("adj_specbig_down_pf", pw, st);
     k_vsb_dn_pf<<<dim3(nbv((long)c.nreal * (h / 2 + 1), 256), nq), 256, 0, st>>>(A);
     pr->end(st);
