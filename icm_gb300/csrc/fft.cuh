@@ -177,6 +177,18 @@ __device__ __forceinline__ long fft4_tw_index(int n2, int k1, int logM, int logT
     return (long)((n2 * (2 * k1 + SHIFT)) & ((2 << logM) - 1)) << (logTW - logM - 1);
 }
 
+// Both bins of an unpack mirror pair (f, M - f): Xf = 0.5 (a + w_t b) and
+// Xc = 0.5 conj(a - w_t b), bin M - f of the same real transform.
+__device__ __forceinline__ void half_sum_tw_pair(double2 a, double2 b, const double2 *__restrict__ tt, long t,
+                                                 int logTW, double2 &Xf, double2 &Xc) {
+    double r;
+    const double2 u = tanmul_t<-1>(b, tt, t, logTW, &r);
+    const double hr = 0.5 * r;
+    const double2 a5 = cscale(a, 0.5);
+    Xf = make_double2(fma(hr, u.x, a5.x), fma(hr, u.y, a5.y));
+    Xc = make_double2(fma(-hr, u.x, a5.x), fma(hr, u.y, -a5.y));
+}
+
 // `cnt` transforms of size 2^logM stored back to back in x (shared memory),
 // each already in bit-reversed order.  All threads of the block take part;
 // the caller synchronises before (after filling x) and this function ends

@@ -112,14 +112,19 @@ __device__ void spec_init_body(const SpecInitArgs &A, int bx, int q) {
     }
     __syncthreads();
     smem_fft_dit<-1>(sm, logd, cnt, tw, logTW);
-    // X[f] = (Z[f] + conj Z[d-f])/2 + e^{-2 pi i f/2d} (Z[f] - conj Z[d-f])/(2i), f = 0..d
-    for (int e = threadIdx.x; e < cnt * d; e += blockDim.x) {
-        const int it = e >> logd, f = e & (d - 1);
+    // X[f] = (Z[f] + conj Z[d-f])/2 + e^{-2 pi i f/2d} (Z[f] - conj Z[d-f])/(2i),
+    // by mirror pairs (f, d - f), f <= d/2
+    const int dp = (d >> 1) + 1;
+    for (int e = threadIdx.x; e < cnt * dp; e += blockDim.x) {
+        const int it = e / dp, f = e - it * dp;
         const double2 *z = sm + (size_t)it * d;
         const double2 zf = z[f], zc = z[(d - f) & (d - 1)];
         const double2 Ev = cadd(zf, cconj(zc)), Od = cmul_mi(csub(zf, cconj(zc)));   // both doubled
         double2 *out = spec2 + q * s2_q + (size_t)(j0 + it) * (d + 1);
-        out[f] = half_sum_tw(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logd - 1), logTW);
+        double2 Xf, Xc;
+        half_sum_tw_pair(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logd - 1), logTW, Xf, Xc);
+        out[f] = Xf;
+        if (f != 0 && 2 * f != d) out[d - f] = Xc;
         if (f == 0) {
             out[d] = cscale(csub(Ev, Od), 0.5);
             const double *x = P + q * P_q + (size_t)(j0 + it) * pst;
@@ -363,19 +368,22 @@ __device__ void gspec_body(const GspecArgs &A, int bx, int q) {
     }
     __syncthreads();
     smem_fft_dit<-1>(sm, lh, cnt, tw, logTW);
-    for (int e = threadIdx.x; e < cnt * h; e += blockDim.x) {
-        const int it = e >> lh, f = e & (h - 1);
+    const int hp = (h >> 1) + 1;   // mirror pairs (f, h - f), f <= h/2
+    for (int e = threadIdx.x; e < cnt * hp; e += blockDim.x) {
+        const int it = e / hp, f = e - it * hp;
         const int j = j0 + it;
         double2 *out = G + q * G_q + (size_t)j * (h + 1);
         if (hot && !hot[j]) {
-            out[f] = make_double2(0.0, 0.0);
-            if (f == 0) out[h] = make_double2(0.0, 0.0);
+            out[f] = out[h - f] = make_double2(0.0, 0.0);
             continue;
         }
         const double2 *z = sm + (size_t)it * h;
         const double2 zf = z[f], zc = z[(h - f) & (h - 1)];
         const double2 Ev = cadd(zf, cconj(zc)), Od = cmul_mi(csub(zf, cconj(zc)));   // both doubled
-        out[f] = half_sum_tw(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logd), logTW);
+        double2 Xf, Xc;
+        half_sum_tw_pair(Ev, Od, tw_tangent(tw, logTW), (long)f << (logTW - logd), logTW, Xf, Xc);
+        out[f] = Xf;
+        if (f != 0 && 2 * f != h) out[h - f] = Xc;
         if (f == 0) out[h] = cscale(csub(Ev, Od), 0.5);
     }
 }

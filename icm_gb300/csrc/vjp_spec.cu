@@ -168,15 +168,20 @@ __device__ void vsp_real_body(const VspRealArgs &A, int bx, int q) {
     }
     __syncthreads();
     smem_fft_dit<-1>(sm, A.logM, nh, A.tw, A.logTW);
-    // X[f] = (Z[f] + conj Z[M-f])/2 + e^{-2 pi i f/2M} (Z[f] - conj Z[M-f])/(2i)
-    for (int e = threadIdx.x; e < nh * M; e += blockDim.x) {
-        const int it = e >> A.logM, f = e & (M - 1);
+    // X[f] = (Z[f] + conj Z[M-f])/2 + e^{-2 pi i f/2M} (Z[f] - conj Z[M-f])/(2i),
+    // by mirror pairs (f, M - f), f <= M/2
+    const int mp = (M >> 1) + 1;
+    for (int e = threadIdx.x; e < nh * mp; e += blockDim.x) {
+        const int it = e / mp, f = e - it * mp;
         const int j = j0 + idx[it];
         const double2 *zz = sm + (size_t)it * M;
         const double2 zf = zz[f], zc = zz[(M - f) & (M - 1)];
         const double2 Ev = cadd(zf, cconj(zc)), Od = cmul_mi(csub(zf, cconj(zc)));   // both doubled
         double2 *out = A.out + q * A.o_q + (size_t)j * (M + 1);
-        out[f] = half_sum_tw(Ev, Od, tw_tangent(A.tw, A.logTW), (long)f << (A.logTW - A.logM - 1), A.logTW);
+        double2 Xf, Xc;
+        half_sum_tw_pair(Ev, Od, tw_tangent(A.tw, A.logTW), (long)f << (A.logTW - A.logM - 1), A.logTW, Xf, Xc);
+        out[f] = Xf;
+        if (f != 0 && 2 * f != M) out[M - f] = Xc;
         if (f == 0) {
             out[M] = cscale(csub(Ev, Od), 0.5);
             if (A.ends) {
