@@ -63,7 +63,11 @@ struct PlanCache {
     int dev = -1;
 };
 thread_local PlanCache t_plan;
-constexpr size_t kPlanCacheMaxBytes = (size_t)512 << 20;
+// Freed arenas stay in the device's default pool (release threshold: all), so
+// keeping a plan holds no more device memory than freeing it would; the cap
+// only keeps an outsized one-off call from pinning its arena outside the
+// pool.  icm_gpu_release_pooled_memory drops the cached plan.
+constexpr size_t kPlanCacheMaxBytes = (size_t)64 << 30;
 
 bool same_opts(const IcmGpuOptions &a, const IcmGpuOptions &b) {
     IcmGpuOptions x = a, y = b;
