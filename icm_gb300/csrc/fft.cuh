@@ -4,8 +4,9 @@
 // passes over bit-reversed input (two radix-2 stages fused per pass, so the
 // output is in natural order), with one radix-2 pass when log2(M) is odd.
 // Twiddles for pointwise steps come from one device table
-// tw[t] = exp(-2 pi i t / 2^logTW); the butterflies use the tangent-form
-// tables stored right after it (below).
+// tw[t] = exp(-2 pi i t / 2^logTW) and its tangent-form copy; the butterflies
+// use the tangent-form tables stored between the two (plain and half-shifted
+// sets, below).
 #pragma once
 
 #include <cuda_runtime.h>
