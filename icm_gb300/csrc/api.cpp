@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -63,11 +64,13 @@ struct PlanCache {
     int dev = -1;
 };
 thread_local PlanCache t_plan;
-// Freed arenas stay in the device's default pool (release threshold: all), so
-// keeping a plan holds no more device memory than freeing it would; the cap
-// only keeps an outsized one-off call from pinning its arena outside the
-// pool.  icm_gpu_release_pooled_memory drops the cached plan.
-constexpr size_t kPlanCacheMaxBytes = (size_t)64 << 30;
+// Arenas of kept plans, summed over the process's threads, stay within this
+// budget: a kept plan's arena cannot go back to the device's default pool for
+// another thread's plan, and a thread that exits leaves its kept plan behind,
+// so the budget bounds both.  icm_gpu_release_pooled_memory drops the calling
+// thread's kept plan.
+constexpr size_t kPlanCacheTotalBytes = (size_t)16 << 30;
+std::atomic<size_t> g_plan_cache_bytes{0};
 
 bool same_opts(const IcmGpuOptions &a, const IcmGpuOptions &b) {
     IcmGpuOptions x = a, y = b;
@@ -76,13 +79,17 @@ bool same_opts(const IcmGpuOptions &a, const IcmGpuOptions &b) {
 }
 
 void drop_cached_plan() {
-    if (t_plan.p) plan_destroy(t_plan.p);
+    if (t_plan.p) {
+        g_plan_cache_bytes.fetch_sub(t_plan.p->arena_bytes);
+        plan_destroy(t_plan.p);
+    }
     t_plan = PlanCache{};
 }
 
 Plan *cached_plan(int n, int k, const IcmGpuOptions *opts) {
     PlanCache &c = t_plan;
     if (!c.p) return nullptr;
+    g_plan_cache_bytes.fetch_sub(c.p->arena_bytes);   // out of the cache while in use
     const IcmGpuOptions o = opts ? *opts : IcmGpuOptions{};
     Plan *p = nullptr;
     if (c.p->n == n && c.p->k == k && c.dev == g_device && c.tune_gen == g_tune_generation.load() &&
@@ -95,8 +102,12 @@ Plan *cached_plan(int n, int k, const IcmGpuOptions *opts) {
 }
 
 bool keep_plan(Plan *p, const IcmGpuOptions *opts) {
-    if (p->arena_bytes > kPlanCacheMaxBytes) return false;
     drop_cached_plan();
+    const size_t b = p->arena_bytes;
+    size_t cur = g_plan_cache_bytes.load();
+    do {
+        if (cur + b > kPlanCacheTotalBytes) return false;
+    } while (!g_plan_cache_bytes.compare_exchange_weak(cur, cur + b));
     t_plan.p = p;
     t_plan.opts = opts ? *opts : IcmGpuOptions{};
     t_plan.cfg = g_config;

@@ -66,3 +66,29 @@ def test_errors_stay_with_their_thread(gpu_icm):
     t1.start(); t2.start(); t1.join(); t2.join()
     assert b"invalid" in msgs["bad"]
     assert b"invalid" not in msgs["good"]
+
+
+def test_large_one_shot_plans_from_threads(gpu_icm):
+    """One-shot solves whose plans (several GB of arena each) are kept per
+    thread while the process-wide budget allows: three threads solving
+    drop-in fields twice each give the serial results bit for bit, whichever
+    of their plans were kept."""
+    from icm_gb300 import workloads as W
+    fields = [W.dropin(n=40000 + 1000 * i)[:2] for i in range(3)]
+    serial = [gpu_icm.equity(S, P) for S, P in fields]
+    results, errors = [None] * 3, []
+
+    def worker(i):
+        try:
+            for _ in range(2):
+                results[i] = gpu_icm.equity(*fields[i])
+        except Exception as e:   # reported below
+            errors.append(repr(e))
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for got, ref in zip(results, serial):
+        assert np.array_equal(got, ref)
