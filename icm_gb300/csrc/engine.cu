@@ -281,16 +281,29 @@ static thread_local int t_sort_cap = 0;   // 0: no cap
 SortThreadCap::SortThreadCap(int cap) : prev(t_sort_cap) { t_sort_cap = cap; }
 SortThreadCap::~SortThreadCap() { t_sort_cap = prev; }
 
-void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
+static inline bool bad_stack(double v) { return !(v > 0.0) || !std::isfinite(v); }
+static inline double key_stack(uint64_t k) {   // the stack whose sort key is k (keys are ~bits)
+    const uint64_t b = ~k;
+    double v;
+    std::memcpy(&v, &b, sizeof v);
+    return v;
+}
+
+int sort_players_desc(const double *S, int n, std::vector<int> &perm, double *S_sorted) {
     perm.resize(n);
     if (n <= 4096) {
+        int bad = -1;
+        for (int i = 0; i < n && bad < 0; ++i)
+            if (bad_stack(S[i])) bad = i;
         std::vector<std::pair<double, int>> kv(n);
         for (int i = 0; i < n; ++i) kv[i] = {S[i], i};
         std::sort(kv.begin(), kv.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
             return a.first > b.first || (a.first == b.first && a.second < b.second);
         });
         for (int i = 0; i < n; ++i) perm[i] = kv[i].second;
-        return;
+        if (S_sorted)
+            for (int i = 0; i < n; ++i) S_sorted[i] = kv[i].first;
+        return bad;
     }
     constexpr int kDig = 12, kNB = 1 << kDig;                      // bucket digit
     constexpr int kBits = 11, kBuckets = 1 << kBits, kPasses = (64 + kBits - 1) / kBits;   // LSD
@@ -301,7 +314,7 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
     std::vector<int> idx(n), idx2(n);
     std::vector<uint32_t> hist((size_t)T * kNB), offs((size_t)T * kNB), bstart(kNB + 1);
     std::vector<uint64_t> lo(T), hi(T);
-    std::vector<int> brange(T + 1);
+    std::vector<int> brange(T + 1), bad_t(T, -1);
     const int cap = std::max(4096, n / (4 * T));   // largest bucket the bucket sort takes
     std::vector<std::pair<uint64_t, int>> scratch((size_t)T * cap);
     uint64_t kmin = 0;
@@ -315,7 +328,9 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
     auto work = [&](int t) {
         const int i0 = (int)((long)n * t / T), i1 = (int)((long)n * (t + 1) / T);
         uint64_t mn = ~0ull, mx = 0;
+        int bad = -1;
         for (int i = i0; i < i1; ++i) {
+            if (bad < 0 && bad_stack(S[i])) bad = i;
             uint64_t b;
             std::memcpy(&b, S + i, sizeof b);
             const uint64_t k = ~b;
@@ -324,6 +339,7 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
             mn = std::min(mn, k);
             mx = std::max(mx, k);
         }
+        bad_t[t] = bad;
         lo[t] = mn;
         hi[t] = mx;
         sync();
@@ -393,11 +409,16 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
                     std::pair<uint64_t, int> *kv = scratch.data() + (size_t)t * cap;
                     for (int i = s0; i < e0; ++i) kv[i - s0] = {key2[i], idx2[i]};
                     std::sort(kv, kv + (e0 - s0));
-                    for (int i = s0; i < e0; ++i) idx2[i] = kv[i - s0].second;
+                    for (int i = s0; i < e0; ++i) {
+                        key2[i] = kv[i - s0].first;
+                        idx2[i] = kv[i - s0].second;
+                    }
                 }
             }
             sync();
             std::copy(idx2.begin() + i0, idx2.begin() + i1, perm.begin() + i0);
+            if (S_sorted)   // the sorted stacks from the sorted keys: no gather
+                for (int i = i0; i < i1; ++i) S_sorted[i] = key_stack(key2[i]);
             return;
         }
         // LSD radix sort over all digits (keys and indices in key / idx)
@@ -436,9 +457,23 @@ void sort_players_desc(const double *S, int n, std::vector<int> &perm) {
             }
             sync();
         }
-        if (t == 0) std::copy(x, x + n, perm.begin());
+        if (t == 0) {
+            std::copy(x, x + n, perm.begin());
+            if (S_sorted)
+                for (int i = 0; i < n; ++i) S_sorted[i] = key_stack(k[i]);
+        }
     };
     HostPool::get().run(T, work);
+    for (int v : bad_t)   // threads hold increasing index ranges
+        if (v >= 0) return v;
+    return -1;
+}
+
+// the inverse of p->perm, built when a subset query first needs it after a sort
+void plan_inv_perm(Plan *p) {
+    if ((int)p->inv_perm.size() == p->n) return;
+    p->inv_perm.resize(p->n);
+    for (int i = 0; i < p->n; ++i) p->inv_perm[p->perm[i]] = i;
 }
 
 int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
@@ -446,11 +481,6 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
         err = "invalid plan arguments n=" + std::to_string(n) + " k=" + std::to_string(k);
         return -1;
     }
-    for (int i = 0; i < n; ++i)
-        if (!(S[i] > 0.0) || !std::isfinite(S[i])) {
-            err = "stacks must be finite and positive (S[" + std::to_string(i) + "])";
-            return -1;
-        }
     p->n = n;
     p->k = k;
     p->B = select_block_size(n, k);
@@ -459,14 +489,15 @@ int plan_geometry(Plan *p, int n, const double *S, int k, std::string &err) {
     p->zskip = g_config.disable_zero_prefix != 1;
     const int B = p->B;
 
-    // descending stacks, ties by original index (reference gpu_plan.cu:405-409)
-    sort_players_desc(S, n, p->perm);
+    // descending stacks, ties by original index (reference gpu_plan.cu:405-409);
+    // the sort also checks the stacks and writes them in sorted order
     p->S_sorted.resize(n);
-    p->inv_perm.resize(n);
-    for (int i = 0; i < n; ++i) {
-        p->S_sorted[i] = S[p->perm[i]];
-        p->inv_perm[p->perm[i]] = i;
+    const int bad = sort_players_desc(S, n, p->perm, p->S_sorted.data());
+    if (bad >= 0) {
+        err = "stacks must be finite and positive (S[" + std::to_string(bad) + "])";
+        return -1;
     }
+    p->inv_perm.clear();
     p->Smax = p->S_sorted[0];
 
     // geometry: node at level l covers B << l players
@@ -909,16 +940,12 @@ static bool root_gspec_forkable(const Plan *p) {
 
 int plan_restack(Plan *p, const double *S, std::string &err) {
     const int n = p->n;
-    for (int i = 0; i < n; ++i)
-        if (!(S[i] > 0.0) || !std::isfinite(S[i])) {
-            err = "stacks must be finite and positive (S[" + std::to_string(i) + "])";
-            return -1;
-        }
-    sort_players_desc(S, n, p->perm);
-    for (int i = 0; i < n; ++i) {
-        p->S_sorted[i] = S[p->perm[i]];
-        p->inv_perm[p->perm[i]] = i;
+    const int bad = sort_players_desc(S, n, p->perm, p->S_sorted.data());
+    if (bad >= 0) {
+        err = "stacks must be finite and positive (S[" + std::to_string(bad) + "])";
+        return -1;
     }
+    p->inv_perm.clear();
     p->Smax = p->S_sorted[0];
     cudaError_t e = cudaMemcpyAsync(p->d_S, p->S_sorted.data(), sizeof(double) * n, cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess)
@@ -931,6 +958,7 @@ int plan_restack(Plan *p, const double *S, std::string &err) {
 // (reference src/cpu/icm.c:2430-2473)
 int plan_set_targets(Plan *p, const int *targets, int n_targets, std::string &err) {
     const int n = p->n, B = p->B;
+    plan_inv_perm(p);
     std::vector<uint8_t> act(n, 0);
     for (int t = 0; t < n_targets; ++t) {
         const int o = targets[t];

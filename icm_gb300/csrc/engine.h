@@ -190,8 +190,12 @@ int plan_check_geometry(const Plan *p, std::string &why);
 // new stacks for a plan of the same shape (n, k): sort, sorted copies on the
 // host and the device; the tree geometry and buffers are kept
 int plan_restack(Plan *p, const double *S, std::string &err);
-// player order: stacks descending, ties by index
-void sort_players_desc(const double *S, int n, std::vector<int> &perm);
+// player order: stacks descending, ties by index; S_sorted (optional) gets the
+// stacks in that order.  Returns the first index whose stack is not finite and
+// positive, else -1 (the order is then still a permutation).
+int sort_players_desc(const double *S, int n, std::vector<int> &perm, double *S_sorted = nullptr);
+// p->inv_perm for the current order (built on first use after a sort)
+void plan_inv_perm(Plan *p);
 // tree buffers for chunks of qc nodes from `base` (nullptr: size only)
 size_t plan_tree_layout(Plan *p, int qc, char *base);
 // coeff_only: every FFT level on coefficients; q_bytes_scale sizes the node

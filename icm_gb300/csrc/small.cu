@@ -346,6 +346,7 @@ int small_solve(int n, const double *S, int Q, const double *payout, int k, doub
     std::memcpy(H + o_pay, payout, 8 * (size_t)k);
     std::memcpy(H + o_perm, p.perm.data(), 4 * (size_t)n);
     if (targets) {
+        plan_inv_perm(&p);
         uint8_t *act = (uint8_t *)(H + o_act);
         std::memset(act, 0, (size_t)n);
         for (int t = 0; t < n_targets; ++t)
